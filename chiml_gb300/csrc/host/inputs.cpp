@@ -1,0 +1,467 @@
+// JSON input -> Inputs. Each block cites the lines of chiML's
+// INPUTS/parallelInputs.cpp whose conversions it keeps.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+#include "model.hpp"
+
+namespace chiml {
+
+const double kSpeedOfLight = 2.9979245e8;
+const double kEps0 = 1 / (4 * M_PI * 1.0e-7 * std::pow(kSpeedOfLight, 2.0));
+const double kElementaryCharge = 1.6021766208000000926392586608069679194921272585907390121132132243531032145256176590919494628906250000e-19;
+const double kHbar = 1.0545718001391127086220667148574871851002905804237980726847871017460777904741746884127674612624536721e-34;
+
+int Inputs::nSteps() const { return static_cast<int>(std::ceil(tMax / dt)); }
+
+namespace {
+
+int find_pt(double pt, double d) { return static_cast<int>(std::floor(pt / d + 0.5)); }
+
+Pol string2pol(const std::string& p) {
+    if (p == "Ex") return Pol::EX;
+    if (p == "Ey") return Pol::EY;
+    if (p == "Ez") return Pol::EZ;
+    if (p == "Hx") return Pol::HX;
+    if (p == "Hy") return Pol::HY;
+    if (p == "Hz") return Pol::HZ;
+    if (p == "L") return Pol::L;
+    if (p == "R") return Pol::R;
+    throw InputError("POLARIZATION undefined");
+}
+
+PulseShape string2prof(const std::string& p) {
+    if (p == "gaussian") return PulseShape::GAUSSIAN;
+    if (p == "BH") return PulseShape::BH;
+    if (p == "rectangle") return PulseShape::RECT;
+    if (p == "continuous") return PulseShape::CONTINUOUS;
+    if (p == "ricker") return PulseShape::RICKER;
+    if (p == "ramped_cont") return PulseShape::RAMP_CONT;
+    throw InputError("Pulse shape undefined");
+}
+
+DtcType string2out(const std::string& t) {
+    static const char* names[] = {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz", "Dx", "Dy", "Dz",
+                                  "Bx", "By", "Bz", "E_pow", "H_pow", "Px", "Py", "Pz"};
+    for (int i = 0; i < 17; ++i)
+        if (t == names[i]) return static_cast<DtcType>(i);
+    if (t == "Mx" || t == "My" || t == "Mz" || t.rfind("Chi", 0) == 0)
+        throw UnsupportedError("detector type " + t + " needs magnetic or chiral media, which are not supported");
+    throw InputError("DTCTYPE (DetectorList.type) from input file not defined");
+}
+
+DipOr string2dipor(const std::string& s) {
+    if (s == "isotropic") return DipOr::ISOTROPIC;
+    if (s == "normal" || s == "tangent" || s == "rel_norm") return DipOr::REL_TO_NORM;
+    if (s == "lat_tangent") return DipOr::LAT_TAN;
+    if (s == "long_tangent") return DipOr::LONG_TAN;
+    if (s == "unidirectional") return DipOr::UNIDIRECTIONAL;
+    throw InputError("The dipole orientation style is undefined");
+}
+
+// Pulse parameter lists, parallelInputs.cpp:133-172 (sources) and 351-390 (TFSF).
+PulseSpec read_pulse(const JNode& pul, double a, double I0) {
+    PulseSpec p;
+    p.shape = string2prof(pul.get<std::string>("profile"));
+    double emax = pul.get<double>("Field_Intensity", 1.0) * a * kEps0 * kSpeedOfLight / I0;
+    std::vector<cplx>& f = p.param;
+    switch (p.shape) {
+        case PulseShape::GAUSSIAN:
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            f.push_back(1.0 / pul.get<double>("fwidth"));
+            f.push_back(pul.get<double>("cutoff") * f[1]);
+            f.push_back(pul.get<double>("t_0", std::real(f[1] * f[2])));
+            f[2] += f[3];
+            break;
+        case PulseShape::BH:
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            f.push_back(pul.get<double>("tau", 1.0 / pul.get<double>("fwidth")));
+            // f[2] is read before it exists in the reference (parallelInputs.cpp:145); it is required here
+            f.push_back(pul.get<double>("t_0"));
+            f.push_back(pul.get<double>("BH1", 0.35875));
+            f.push_back(pul.get<double>("BH2", 0.48829));
+            f.push_back(pul.get<double>("BH3", 0.14128));
+            f.push_back(pul.get<double>("BH4", 0.01168));
+            break;
+        case PulseShape::RECT:
+            f.push_back(pul.get<double>("tau"));
+            f.push_back(pul.get<double>("t_0"));
+            f.push_back(pul.get<double>("n", 30.0) * 2.0);
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            break;
+        case PulseShape::CONTINUOUS:
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            break;
+        case PulseShape::RAMP_CONT:
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            f.push_back(pul.get<double>("ramp_val"));
+            break;
+        case PulseShape::RICKER:
+            f.push_back(cplx(0.0, -1.0 * pul.get<double>("fcen") * 2 * M_PI));
+            f.push_back(pul.get<double>("fwidth"));
+            f.push_back(pul.get<double>("cutoff"));
+            break;
+    }
+    // The amplitude is appended when the source is built (parallelFDTDField.cpp:476)
+    f.push_back(emax);
+    return p;
+}
+
+Object make_vacuum_block(const std::array<double, 3>& size) {
+    Object o;
+    o.shape = Shape::BLOCK;
+    o.geo = {size[0], size[1], size[2]};
+    o.geoML = o.geo;
+    return o;
+}
+
+// parallelProgramInputs::ptreeToObject, parallelInputs.cpp:1263-1623 (custom materials,
+// sphere / block / ellipsoid / cylinder).
+Object read_object(const JNode& node, const Inputs& ip) {
+    Object o;
+    o.loc = as_arr3(node, "loc");
+    std::string material = node.get<std::string>("material");
+    if (material != "custom") {
+        if (material == "vac" || material == "Vac" || material == "VAC") {
+            o.epsInf = 1.0;
+        } else {
+            throw UnsupportedError("named material '" + material + "' is not supported; give a custom material");
+        }
+    } else {
+        o.epsInf = node.get<double>("eps", 1.00);
+        if (node.get<double>("mu", 1.0) != 1.0)
+            throw UnsupportedError("magnetic materials (mu != 1) are not supported");
+        if (node.get<double>("tellegen", 0.0) != 0.0)
+            throw UnsupportedError("Tellegen media are not supported");
+        for (auto& kv : node.child("pols").kids) {
+            const JNode& pn = kv.second;
+            if (pn.get<bool>("tanIso", false)) throw UnsupportedError("tangential-isotropic poles are not supported");
+            if (pn.get<bool>("molecular_trans", false)) throw UnsupportedError("molecular-transition poles are not supported");
+            Oscillator osc;
+            osc.dipOrE = string2dipor(pn.get<std::string>("dipOrE", "isotropic"));
+            if (string2dipor(pn.get<std::string>("dipOrM", "isotropic")) != DipOr::ISOTROPIC)
+                throw UnsupportedError("magnetic dipole orientations are not supported");
+            if (osc.dipOrE != DipOr::ISOTROPIC && osc.dipOrE != DipOr::UNIDIRECTIONAL)
+                throw UnsupportedError("surface-relative dipole orientations are not supported");
+            osc.gam = pn.get<double>("gamma") * M_PI;
+            osc.omg = pn.get<double>("omega") * 2 * M_PI;
+            osc.sigP = pn.get<double>("sigma_p", 0.0);
+            if (pn.get<double>("sigma_m", 0.0) != 0.0) throw UnsupportedError("magnetic poles (sigma_m) are not supported");
+            if (pn.get<double>("tau", 0.0) != 0.0) throw UnsupportedError("chiral poles (tau) are not supported");
+            if (osc.dipOrE == DipOr::UNIDIRECTIONAL) {
+                if (osc.sigP > 0.0) {
+                    osc.uVecDipE = as_arr3(pn, "dirDipE");
+                    double nrm = std::sqrt(std::accumulate(osc.uVecDipE.begin(), osc.uVecDipE.end(), 0.0,
+                                                           [](double s, double v) { return s + v * v; }));
+                    for (auto& v : osc.uVecDipE) v = v / nrm;
+                } else {
+                    osc.uVecDipE = {0.0, 0.0, 0.0};
+                }
+            } else {
+                osc.uVecDipE = {1.0, 1.0, 1.0};
+            }
+            o.pols.push_back(osc);
+        }
+    }
+    // unit vectors (parallelInputs.cpp:1439-1466)
+    std::array<std::array<double, 3>, 3> uv{};
+    const JNode& uvecs = node.child("unit_vectors");
+    int cc = 0;
+    for (auto& kv : uvecs.kids) {
+        if (cc > 2) throw InputError("unit_vectors has more than three entries");
+        uv[cc] = as_arr3(kv.second, "uvec");
+        ++cc;
+    }
+    if (uvecs.size() == 0) {
+        double orTheta = M_PI / 2.0 - node.get<double>("orTheta", 90.0) * M_PI / 180.0;
+        double orPhi = -1.0 * node.get<double>("orPhi", 0.0) * M_PI / 180.0;
+        if (ip.size[2] == 0) {
+            uv[0] = {std::cos(orPhi), -1.0 * std::sin(orPhi), 0};
+            uv[1] = {std::sin(orPhi), std::cos(orPhi), 0};
+            uv[2] = {0.0, 0.0, 0};
+        } else {
+            uv[0] = {std::cos(orTheta) * std::cos(orPhi), -1.0 * std::cos(orTheta) * std::sin(orPhi), std::sin(orTheta)};
+            uv[1] = {std::sin(orPhi), std::cos(orPhi), 0};
+            uv[2] = {-1.0 * std::sin(orTheta) * std::cos(orPhi), std::sin(orTheta) * std::sin(orPhi), std::cos(orTheta)};
+        }
+    }
+    // coordTransform_ rows (Obj.cpp:61-69): unit vector component / vector norm
+    for (int ii = 0; ii < 3; ++ii) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += uv[ii][k] * uv[ii][k];
+        for (int jj = 0; jj < 3; ++jj) {
+            double dot = 0.0;
+            for (int k = 0; k < 3; ++k) dot += uv[ii][k] * (k == jj ? 1.0 : 0.0);
+            o.coord[ii * 3 + jj] = dot / std::sqrt(s);
+        }
+    }
+    if (node.child("Basis_Set").size() > 0)
+        throw UnsupportedError("quantum-emitter objects (Basis_Set) are not supported by this build");
+    o.ML = false;
+    std::string s = node.get<std::string>("shape");
+    if (s == "block") {
+        o.shape = Shape::BLOCK;
+        o.geo = as_vector(node, "size");
+        if (node.get<double>("rad_curve", 0.0) != 0.0) throw UnsupportedError("rounded blocks are not supported");
+        o.geo.push_back(0.0);
+    } else if (s == "ellipsoid") {
+        o.shape = Shape::ELLIPSOID;
+        o.geo = as_vector(node, "size");
+        o.cutNeg = as_arr3(node, "cut_neg", -1.0);
+        o.cutPos = as_arr3(node, "cut_pos", 1.0);
+        o.cutGlobal = as_arr3(node, "cut_global", 1.0);
+        for (int nn = 0; nn < 3; ++nn)
+            if (std::abs(o.cutNeg[nn]) > 1.0 || std::abs(o.cutPos[nn]) > 1.0 || std::abs(o.cutGlobal[nn]) > 1.0)
+                throw InputError("abs(ellipsoid cutoff) must be <= 1.0");
+    } else if (s == "sphere") {
+        o.shape = Shape::SPHERE;
+        o.geo = {node.get<double>("radius", 0.0)};
+    } else if (s == "cylinder") {
+        o.shape = Shape::CYLINDER;
+        o.geo = {node.get<double>("radius", 0.0), node.get<double>("length", 0.0)};
+    } else {
+        throw UnsupportedError("shape '" + s + "' is not supported");
+    }
+    o.geoML = o.geo;
+    return o;
+}
+
+std::vector<double> read_freq_list(const JNode& n, const char* what) {
+    double fCen = n.get<double>("fcen", -1.0);
+    double fWidth = n.get<double>("fwidth", -1.0);
+    double lamL = n.get<double>("lamL", -1.0);
+    double lamR = n.get<double>("lamR", -1.0);
+    int nFreq = n.get<int>("nfreq", -1);
+    if (nFreq < 1) throw InputError(std::string(what) + " regions need a number of frequencies");
+    std::vector<double> fl(nFreq, 0.0);
+    if (fCen != -1.0 && fWidth != -1.0) {
+        if (lamL != -1.0 && lamR != -1.0) throw InputError("Both a freq and wavelength range is defined");
+        double dOmg = fWidth / static_cast<double>(nFreq - 1);
+        for (int ii = 0; ii < nFreq; ++ii) fl[ii] = (fCen - fWidth / 2.0 + ii * dOmg) * 2.0 * M_PI;
+    } else if (lamL != -1.0 && lamR != -1.0) {
+        double dLam = (lamR - lamL) / static_cast<double>(nFreq - 1);
+        for (int ii = 0; ii < nFreq; ++ii) fl[ii] = 2.0 * M_PI / (lamL + ii * dLam);
+    } else {
+        throw InputError(std::string(what) + " needs fcen and fwidth or lamL and lamR");
+    }
+    return fl;
+}
+
+}  // namespace
+
+cplx PulseSpec::value(double tt) const {
+    // UTIL/PulseFxn.hpp:19-89
+    const std::vector<cplx>& p = param;
+    switch (shape) {
+        case PulseShape::GAUSSIAN:
+            return (tt <= std::real(p[2])) ? p[4] * std::exp(p[0] * tt - (std::pow((tt - p[3]) / p[1], 2.0) / 2.0)) : cplx(0.0);
+        case PulseShape::CONTINUOUS:
+            return p[1] * std::exp(p[0] * tt);
+        case PulseShape::RAMP_CONT:
+            return (std::abs(p[2] * p[1] * tt) <= std::abs(p[2])) ? std::abs(p[1] * tt) * p[2] * std::exp(p[0] * tt)
+                                                                    : p[2] * std::exp(p[0] * tt);
+        case PulseShape::BH:
+            return (std::real(p[2] - p[1] / 2.0) <= tt && tt <= std::real(p[2] + p[1] / 2.0))
+                       ? p[7] * std::exp(p[0] * (tt - p[2])) *
+                             (p[3] + p[4] * std::cos(2.0 * M_PI * (tt - p[2]) / p[1]) +
+                              p[5] * std::cos(4.0 * M_PI * (tt - p[2]) / p[1]) +
+                              p[6] * std::cos(6.0 * M_PI * (tt - p[2]) / p[1]))
+                       : cplx(0.0);
+        case PulseShape::RECT:
+            return (tt < std::real(p[1] + p[0]) && tt > std::real(p[1] - p[0]))
+                       ? p[4] / (std::pow(2.0 * (tt - p[1]) / p[0], p[2]) + 1.0) * (std::exp(p[3] * (tt - p[1])))
+                       : cplx(0.0);
+        case PulseShape::RICKER:
+            return (tt < std::real(p[2] * p[1] / p[0]))
+                       ? p[3] * (1.0 - 2.0 * std::pow(M_PI * (tt * p[0] - p[1]), 2.0)) *
+                             std::exp(-std::pow(M_PI * (tt * p[0] - p[1]), 2.0))
+                       : cplx(0.0);
+    }
+    return 0.0;
+}
+
+Inputs read_inputs(const JNode& IP, const std::string& filename) {
+    Inputs ip;
+    ip.filename = filename;
+    // parallelInputs.cpp:14-27
+    if (IP.get<bool>("CompCell.PBC", false)) throw UnsupportedError("periodic boundaries are not supported");
+    if (IP.get<bool>("CompCell.cplxFields", false)) throw UnsupportedError("complex fields are not supported");
+    ip.pol = string2pol(IP.get<std::string>("CompCell.pol"));
+    ip.res = IP.get<int>("CompCell.res", -1);
+    ip.courant = IP.get<double>("CompCell.courant", 0.5);
+    ip.a = IP.get<double>("CompCell.a", 1e-7);
+    ip.tMax = IP.get<double>("CompCell.tLim");
+    ip.I0 = IP.get<double>("CompCell.I0", ip.a * kEps0 * kSpeedOfLight);
+    ip.size = as_arr3(IP, "CompCell.size");
+    ip.d = as_arr3(IP, "CompCell.stepSize", 1.0 / ip.res);
+    ip.dt = IP.get<double>("CompCell.dt", ip.courant / std::sqrt(1.0 / (ip.d[0] * ip.d[0]) + 1.0 / (ip.d[1] * ip.d[1]) +
+                                                                   1.0 / (ip.d[2] * ip.d[2])));
+    ip.pmlSigOptRat = IP.get<double>("PML.sigOptRat", 1.0);
+    ip.pmlKappaMax = IP.get<double>("PML.kappaMax", 1.0);
+    ip.pmlAMax = IP.get<double>("PML.aMax", 0.00);
+    ip.pmlMa = IP.get<double>("PML.ma", 1.0);
+    ip.pmlM = IP.get<double>("PML.m", 3.0);
+    if (IP.child("TFSF").size() > 0) throw UnsupportedError("TFSF surfaces are not supported by this build");
+    // parallelInputs.cpp:96-107
+    if (ip.d[0] < 0 || ip.d[1] < 0 || ip.d[2] < 0) throw InputError("Please define a positive step size.");
+    double stab = 0.0;
+    for (double dd : ip.d) stab += 1.0 / (dd * dd);
+    if (ip.dt > 1.0 / std::sqrt(stab)) throw InputError("Time step is larger than the stable time step for the calculation.");
+    std::array<double, 3> pmlT = as_arr3(IP, "PML.thickness");
+    for (int ii = 0; ii < 3; ++ii) {
+        if (pmlT[ii] * 2 > ip.size[ii]) throw InputError("PML size is larger than the cell size");
+        ip.pmlThickness[ii] = find_pt(pmlT[ii], ip.d[ii]);
+    }
+    // Sources, parallelInputs.cpp:114-216
+    for (auto& kv : IP.child("SourceList").kids) {
+        const JNode& sn = kv.second;
+        SourceSpec s;
+        s.pol = string2pol(sn.get<std::string>("pol"));
+        if (s.pol == Pol::L || s.pol == Pol::R) throw UnsupportedError("circularly polarised soft sources are not supported");
+        for (auto& pk : sn.child("PulseList").kids) s.pulses.push_back(read_pulse(pk.second, ip.a, ip.I0));
+        std::array<double, 3> tempSz = as_arr3(sn, "size");
+        for (int cc = 0; cc < 3; ++cc) s.sz[cc] = find_pt(tempSz[cc], ip.d[cc]) + 1;
+        s.phi = sn.get<double>("phi", 90);
+        if (static_cast<int>(std::round(s.phi)) % 90 != 0)
+            throw UnsupportedError("oblique soft sources are not supported");
+        std::array<double, 3> loc = as_arr3(sn, "loc");
+        for (int i = 0; i < 3; ++i) {
+            if (loc[i] + tempSz[i] / 2.0 > ip.size[i] / 2.0 || loc[i] - tempSz[i] / 2.0 < -1.0 * ip.size[i] / 2.0)
+                throw InputError("The source is at least partially outside the FDTD Cell");
+            if (s.phi == 90 || s.phi == 180 || s.phi == 270 || s.phi == 0)
+                s.loc[i] = find_pt(loc[i] + ip.size[i] / 2.0 - tempSz[i] / 2.0, ip.d[i]);
+            else
+                s.loc[i] = find_pt(loc[i] + ip.size[i] / 2.0, ip.d[i]);
+        }
+        ip.sources.push_back(s);
+    }
+    // Objects, parallelInputs.cpp:410-666; objArr_[0] is the vacuum block of the whole cell
+    ip.objects.push_back(make_vacuum_block(ip.size));
+    for (auto& kv : IP.child("ObjectList").kids) ip.objects.push_back(read_object(kv.second, ip));
+    // Detectors, parallelInputs.cpp:667-755
+    int ii = 0;
+    for (auto& kv : IP.child("DetectorList").kids) {
+        const JNode& dn = kv.second;
+        DetectorSpec d;
+        d.outputMaps = dn.get<bool>("output_map", false);
+        d.type = string2out(dn.get<std::string>("type"));
+        d.name = dn.get<std::string>("fname") + "_field_" + std::to_string(ii) + ".dat";
+        ++ii;
+        std::string cls = dn.get<std::string>("dtc_class", "cout");
+        if (cls == "txt") d.cls = DtcClass::TXT;
+        else if (cls == "bin") d.cls = DtcClass::BIN;
+        else if (cls == "freq") d.cls = DtcClass::FREQ;
+        else if (cls == "cout" || cls == "bmp") throw UnsupportedError("detector class '" + cls + "' is not supported");
+        else throw InputError("DTCCLASS (DetectorList.class) for input file is not defined");
+        if (d.cls == DtcClass::FREQ) throw UnsupportedError("frequency-domain field detectors are not supported by this build");
+        d.SI = dn.get<bool>("SI", true);
+        d.timeInt = dn.get<double>("Time_Interval", ip.dt);
+        std::array<double, 3> tempSz = as_arr3(dn, "size");
+        for (int cc = 0; cc < 3; ++cc) d.sz[cc] = find_pt(tempSz[cc], ip.d[cc]) + 1;
+        std::array<double, 3> loc = as_arr3(dn, "loc");
+        for (int i = 0; i < 3; ++i) {
+            if (loc[i] - tempSz[i] / 2.0 < -1.0 * ip.size[i] / 2.0 || loc[i] + tempSz[i] / 2.0 > ip.size[i] / 2.0)
+                throw InputError("A detector is outside the FDTD cell.");
+            d.loc[i] = find_pt(loc[i] + ip.size[i] / 2.0 - tempSz[i] / 2.0, ip.d[i]);
+        }
+        ip.detectors.push_back(d);
+    }
+    // Flux regions, parallelInputs.cpp:756-838
+    for (auto& kv : IP.child("FluxList").kids) {
+        const JNode& fn = kv.second;
+        FluxSpec f;
+        f.name = fn.get<std::string>("name");
+        std::array<double, 3> tempSz = as_arr3(fn, "size");
+        for (int cc = 0; cc < 3; ++cc) f.sz[cc] = find_pt(tempSz[cc], ip.d[cc]) + 1;
+        std::array<double, 3> loc = as_arr3(fn, "loc");
+        for (int i = 0; i < 3; ++i) {
+            if (loc[i] - tempSz[i] / 2.0 < -1.0 * ip.size[i] || loc[i] + tempSz[i] / 2.0 > ip.size[i])
+                throw InputError("A flux region is outside the FDTD cell.");
+            f.loc[i] = find_pt(loc[i] + ip.size[i] / 2.0 - tempSz[i] / 2, ip.d[i]);
+        }
+        f.weight = fn.get<double>("weight", 1.0);
+        f.timeInt = static_cast<int>(std::floor(fn.get<double>("Time_Interval", ip.dt) / (ip.dt) + 0.50));
+        if (f.timeInt <= 0) f.timeInt = 1;
+        f.freqList = read_freq_list(fn, "flux");
+        f.SI = fn.get<bool>("SI", false);
+        f.crossSec = fn.get<bool>("cross_sec", false);
+        f.incdFile = fn.get<std::string>("incd_fileds", "");
+        f.save = fn.get<bool>("save", false);
+        f.load = fn.get<bool>("load", false);
+        if (f.load) throw UnsupportedError("loading saved flux fields is not supported by this build");
+        ip.fluxes.push_back(f);
+    }
+    return ip;
+}
+
+Inputs read_inputs_file(const std::string& path) { return read_inputs(parse_json_file(path), path); }
+
+// Obj::setUpConsts (Obj.cpp:299-370), electric poles only
+void Object::setUpConsts(double dt) {
+    alpha.clear();
+    xi.clear();
+    gamma.clear();
+    dipOr.clear();
+    dipE.clear();
+    orDip = false;
+    for (auto& p : pols) {
+        if (p.dipOrE != DipOr::ISOTROPIC) orDip = true;
+        if (std::abs(p.sigP) != 0.0) {
+            dipOr.push_back(p.dipOrE);
+            dipE.push_back(p.uVecDipE);
+            alpha.push_back(((2 - std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
+            xi.push_back(((p.gam * dt - 1) / (1 + p.gam * dt)));
+            gamma.push_back(((p.sigP * std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
+        }
+    }
+}
+
+// Shape tests, Obj.cpp:373-540
+bool Object::isObj(const std::array<double, 3>& v, double dx, const std::vector<double>& geo_) const {
+    auto toObj = [&](const std::array<double, 3>& p) {
+        std::array<double, 3> c = {p[0] - loc[0], p[1] - loc[1], p[2] - loc[2]};
+        std::array<double, 3> t;
+        for (int i = 0; i < 3; ++i) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k) s += coord[i * 3 + k] * c[k];
+            t[i] = s;
+        }
+        return t;
+    };
+    switch (shape) {
+        case Shape::SPHERE: {
+            double sum = 0.0;
+            for (int cc = 0; cc < 3; ++cc) sum += std::pow((v[cc] - loc[cc]), 2);
+            return !(std::sqrt(sum) > geo_[0] + dx / 1.0e6);
+        }
+        case Shape::BLOCK: {
+            std::array<double, 3> t = toObj(v);
+            for (int i = 0; i < 3; ++i)
+                if ((t[i] > geo_[i] / 2.0 + dx / 1.0e6) || (t[i] < -1.0 * geo_[i] / 2.0 - dx / 1.0e6)) return false;
+            return true;
+        }
+        case Shape::ELLIPSOID: {
+            std::array<double, 3> t = toObj(v);
+            double ptSum = 0.0;
+            for (int i = 0; i < (geo_[2] != 0.0 ? 3 : 2); ++i) ptSum += std::pow((t[i] - dx / 1.0e6) / (geo_[i] / 2.0), 2.0);
+            if (1.0 < ptSum) return false;
+            for (int i = 0; i < 3; ++i) {
+                if ((2.0 * t[i] / geo_[i] < cutNeg[i]) || (2.0 * t[i] / geo_[i] > cutPos[i])) return false;
+                if (cutGlobal[i] >= 0.0 && (t[i] + geo_[i] / 2.0) / geo_[i] >= cutGlobal[i]) return false;
+                else if (cutGlobal[i] <= 0.0 && (t[i] - geo_[i] / 2.0) / geo_[i] <= cutGlobal[i]) return false;
+            }
+            return true;
+        }
+        case Shape::CYLINDER: {
+            std::array<double, 3> t = toObj(v);
+            if ((t[1] < -1.0 * geo_[1] / 2.0 - dx * 1e-6) || (t[1] > geo_[1] / 2.0 + dx * 1e-6)) return false;
+            double s = std::sqrt(std::pow(t[0], 2) + std::pow(0.0, 2) + std::pow(t[2], 2));
+            if (s > geo_[0] + 1.0e-6 * dx) return false;
+            return true;
+        }
+    }
+    return false;
+}
+
+}  // namespace chiml

@@ -1,0 +1,125 @@
+// Input model of a chiML simulation: the parsed JSON input, in FDTD units.
+//
+// Field names follow chiML's parallelProgramInputs (INPUTS/parallelInputs.hpp)
+// so that each value can be traced to the line of parallelInputs.cpp that
+// produces it. Only the features of the time-step loop handled by this
+// library are representable; everything else is rejected at parse time with
+// UnsupportedError (there is no CPU fallback).
+#pragma once
+
+#include <array>
+#include <complex>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "json.hpp"
+
+namespace chiml {
+
+typedef std::complex<double> cplx;
+
+struct UnsupportedError : public std::runtime_error {
+    explicit UnsupportedError(const std::string& w) : std::runtime_error(w) {}
+};
+
+// Physical constants exactly as UTIL/ml_consts.hpp:13-17 defines them.
+extern const double kSpeedOfLight;
+extern const double kEps0;
+extern const double kElementaryCharge;
+extern const double kHbar;
+
+enum class Pol { EX, EY, EZ, HX, HY, HZ, L, R };
+enum class PulseShape { GAUSSIAN, CONTINUOUS, RICKER, RAMP_CONT, BH, RECT };
+enum class Shape { SPHERE, BLOCK, ELLIPSOID, CYLINDER };
+enum class DipOr { REL_TO_NORM, ISOTROPIC, UNIDIRECTIONAL, LONG_TAN, LAT_TAN };
+enum class DtcClass { TXT, BIN, FREQ };
+// Same ordering as DTCTYPE (UTIL/enum.hpp:17)
+enum class DtcType { EX, EY, EZ, HX, HY, HZ, DX, DY, DZ, BX, BY, BZ, EPOW, HPOW, PX, PY, PZ };
+
+// One Lorentz oscillator of a custom material (LorenzDipoleOscillator, OBJECTS/Obj.hpp:18-39).
+struct Oscillator {
+    DipOr dipOrE = DipOr::ISOTROPIC;
+    double omg = 0.0, gam = 0.0, sigP = 0.0;
+    std::array<double, 3> uVecDipE = {1.0, 1.0, 1.0};
+};
+
+// A geometric object with its material; coefficients from Obj::setUpConsts (Obj.cpp:299-370).
+struct Object {
+    Shape shape = Shape::BLOCK;
+    bool ML = false;               // has an emitter basis set
+    double epsInf = 1.0;
+    std::vector<double> geo;       // shape parameters (Obj::geoParam_)
+    std::vector<double> geoML;     // geoParamML_: geo with the emitter buffer added
+    std::array<double, 3> loc = {0.0, 0.0, 0.0};
+    std::array<double, 9> coord = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // rows: normalised unit vectors
+    std::array<double, 3> cutNeg = {-1, -1, -1}, cutPos = {1, 1, 1}, cutGlobal = {1, 1, 1};
+    std::vector<Oscillator> pols;
+    // derived per time step (setUpConsts)
+    bool orDip = false;
+    std::vector<double> alpha, xi, gamma;
+    std::vector<DipOr> dipOr;
+    std::vector<std::array<double, 3>> dipE;
+
+    bool isObj(const std::array<double, 3>& v, double dx, const std::vector<double>& g) const;
+    bool isVacuum() const { return !(gamma.size() > 0 || epsInf != 1.0 || ML); }
+    void setUpConsts(double dt);
+};
+
+struct PulseSpec {
+    PulseShape shape = PulseShape::GAUSSIAN;
+    std::vector<cplx> param;  // parameter list as built in parallelInputs.cpp:133-172 (+ amplitude appended)
+    cplx value(double t) const;
+};
+
+struct SourceSpec {
+    Pol pol = Pol::EZ;
+    std::vector<PulseSpec> pulses;
+    std::array<int, 3> loc = {0, 0, 0}, sz = {1, 1, 1};
+    double phi = 90.0;
+};
+
+struct DetectorSpec {
+    DtcClass cls = DtcClass::TXT;
+    DtcType type = DtcType::EZ;
+    std::string name;
+    std::array<int, 3> loc = {0, 0, 0}, sz = {1, 1, 1};
+    bool SI = true;
+    double timeInt = 0.0;
+    std::vector<double> freqList;
+    bool outputMaps = false;
+};
+
+struct FluxSpec {
+    std::string name;
+    std::array<int, 3> loc = {0, 0, 0}, sz = {1, 1, 1};
+    double weight = 1.0;
+    int timeInt = 1;
+    std::vector<double> freqList;
+    bool SI = false, crossSec = false, save = false, load = false;
+    std::string incdFile;
+};
+
+struct Inputs {
+    std::string filename;
+    Pol pol = Pol::EZ;
+    double a = 1e-7, I0 = 0.0, tMax = 0.0, courant = 0.5, dt = 0.0;
+    int res = -1;
+    std::array<double, 3> size = {0, 0, 0}, d = {0, 0, 0};
+    // PML
+    std::array<int, 3> pmlThickness = {0, 0, 0};
+    double pmlSigOptRat = 1.0, pmlKappaMax = 1.0, pmlAMax = 0.0, pmlMa = 1.0, pmlM = 3.0;
+    std::vector<SourceSpec> sources;
+    std::vector<Object> objects;  // objects[0] is the vacuum cell block
+    std::vector<DetectorSpec> detectors;
+    std::vector<FluxSpec> fluxes;
+
+    int nSteps() const;
+};
+
+// Builds Inputs from a parsed JSON tree (parallelProgramInputs ctor, parallelInputs.cpp:12-838).
+Inputs read_inputs(const JNode& root, const std::string& filename);
+Inputs read_inputs_file(const std::string& path);
+
+}  // namespace chiml

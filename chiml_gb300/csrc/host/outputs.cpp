@@ -1,0 +1,318 @@
+#include "outputs.hpp"
+
+#include <cmath>
+#include <complex>
+#include <fstream>
+#include <iomanip>
+#include <memory>
+#include <sys/stat.h>
+
+namespace chiml {
+
+std::string out_path(const std::string& outDir, const std::string& name) {
+    std::string full = (outDir.empty() || (!name.empty() && name[0] == '/')) ? name : outDir + "/" + name;
+    // create the parent directories, as the reader does for every output name
+    std::size_t slash = full.find_last_of('/');
+    if (slash != std::string::npos && slash > 0) {
+        std::string dir = full.substr(0, slash);
+        for (std::size_t i = 1; i <= dir.size(); ++i)
+            if (i == dir.size() || dir[i] == '/') ::mkdir(dir.substr(0, i).c_str(), 0755);
+    }
+    return full;
+}
+
+long long detector_event_values(const DetectorPlan& dp) {
+    long long n = 0;
+    for (auto& f : dp.fields) n += static_cast<long long>(f.cells.size());
+    return n;
+}
+
+int detector_events(const DetectorPlan& dp, int nSteps) { return nSteps / dp.timeInt + 1; }
+
+namespace {
+
+// Field value accumulation of fieldOutputFunction / pwrOutputFunction
+// (DTC/parallelDTCOutputFxn.hpp:22-40).
+inline double accum(double cur, double pt, double conv, bool power) {
+    return power ? cur + conv * std::pow(std::abs(pt), 2.0) : cur + conv * pt;
+}
+
+}  // namespace
+
+void write_detectors(const Plan& P, const RunRecord& R, const std::string& outDir, int stepsDone) {
+    for (std::size_t k = 0; k < P.detectors.size(); ++k) {
+        const DetectorPlan& dp = P.detectors[k];
+        const auto& ev = R.detectors[k];
+        const int nev = std::min(static_cast<int>(ev.size()), stepsDone / dp.timeInt + 1);
+        std::vector<long long> base(dp.fields.size(), 0);
+        for (std::size_t f = 1; f < dp.fields.size(); ++f) base[f] = base[f - 1] + static_cast<long long>(dp.fields[f - 1].cells.size());
+        const std::string path = out_path(outDir, dp.spec.name);
+        const double half = dp.convFactor / 2.0;
+        if (dp.spec.cls == DtcClass::TXT) {
+            std::ofstream os(path);
+            if (!os) throw InputError("cannot open detector output " + path);
+            os << "# time\tx\ty\tz\tfield" << std::endl;
+            const auto& o0 = dp.fields[0].outSz;
+            for (int e = 0; e < nev; ++e) {
+                const std::vector<double>& v = ev[e];
+                double t = P.tcur[static_cast<std::size_t>(e) * dp.timeInt];
+                os << std::setprecision(6) << t * dp.tConv << "\t" << dp.realLoc[0] << "\t" << dp.realLoc[1] << "\t"
+                   << dp.realLoc[2];
+                for (int jj = 0; jj < o0[1]; ++jj)
+                    for (int kk = 0; kk < o0[2]; ++kk)
+                        for (int ii = 0; ii < o0[0]; ++ii) {
+                            double point = 0.0;
+                            for (std::size_t f = 0; f < dp.fields.size(); ++f) {
+                                const auto& F = dp.fields[f];
+                                const auto& s = F.outSz;
+                                long long i0 = ii + s[0] * (kk + s[2] * static_cast<long long>(jj));
+                                long long i1 = (ii + std::abs(F.off[0])) + s[0] * ((kk + std::abs(F.off[2])) + s[2] * static_cast<long long>(jj + std::abs(F.off[1])));
+                                point = accum(point, v[base[f] + i0], half, dp.power);
+                                point = accum(point, v[base[f] + i1], half, dp.power);
+                            }
+                            os << "\t" << std::setw(24) << std::setprecision(18) << point;
+                        }
+                os << '\n';
+            }
+        } else {
+            std::ofstream os(path, std::ios::out | std::ios::binary);
+            if (!os) throw InputError("cannot open detector output " + path);
+            os.write(reinterpret_cast<const char*>(dp.spec.sz.data()), 3 * sizeof(int));
+            os.write(reinterpret_cast<const char*>(dp.spec.loc.data()), 3 * sizeof(int));
+            const auto& sz = dp.spec.sz;
+            std::vector<double> row(static_cast<std::size_t>(sz[0]), 0.0);
+            for (int e = 0; e < nev; ++e) {
+                const std::vector<double>& v = ev[e];
+                double tt = P.tcur[static_cast<std::size_t>(e) * dp.timeInt] * dp.tConv;
+                os.write(reinterpret_cast<const char*>(&tt), sizeof(tt));
+                for (int kk = 0; kk < sz[2]; ++kk)
+                    for (int jj = 0; jj < sz[1]; ++jj) {
+                        std::fill(row.begin(), row.end(), 0.0);
+                        for (std::size_t f = 0; f < dp.fields.size(); ++f) {
+                            const auto& F = dp.fields[f];
+                            const auto& s = F.outSz;
+                            std::array<int, 3> ao = {std::abs(F.off[0]), std::abs(F.off[1]), std::abs(F.off[2])};
+                            for (int x = 0; x < sz[0]; ++x) {
+                                long long i0 = x + s[0] * (kk + s[2] * static_cast<long long>(jj));
+                                row[x] = accum(row[x], v[base[f] + i0], half, dp.power);
+                            }
+                            for (int x = 0; x < sz[0]; ++x) {
+                                long long i1 = (x + ao[0]) + s[0] * ((kk + ao[2]) + s[2] * static_cast<long long>(jj + ao[1]));
+                                row[x] = accum(row[x], v[base[f] + i1], half, dp.power);
+                            }
+                        }
+                        os.write(reinterpret_cast<const char*>(row.data()), static_cast<std::streamsize>(row.size() * sizeof(double)));
+                    }
+            }
+        }
+    }
+}
+
+namespace {
+
+typedef std::complex<double> cx;
+
+// simps (parallelFlux.hpp:548-576)
+cx simps(const cx* v, int n, double d) {
+    if (n == 1) return v[0] * d;
+    cx r(0.0, 0.0);
+    if (n % 2 == 0) {
+        for (int ii = 0; ii < (n - 2) / 2; ii++) r += d / 6.0 * (v[ii * 2] + 4.0 * v[ii * 2 + 1] + v[(ii + 1) * 2]);
+        for (int ii = 1; ii < (n) / 2; ii++) r += d / 6.0 * (v[ii * 2 - 1] + 4.0 * v[ii * 2] + v[ii * 2 + 1]);
+        r += d / 4.0 * (v[0] + v[1] + v[n - 1] + v[n - 2]);
+    } else {
+        for (int ii = 0; ii < (n - 1) / 2; ii++) r += d / 3.0 * (v[ii * 2] + 4.0 * v[ii * 2 + 1] + v[(ii + 1) * 2]);
+    }
+    return r;
+}
+
+struct CGrid {  // Grid<cplx> with dims (x, y, z), index x + nx*(z + y*nz)
+    int nx = 0, ny = 0, nz = 0;
+    double dx = 0, dy = 0, dz = 0;
+    std::vector<cx> v;
+    CGrid(int x, int y, int z, double ddx, double ddy, double ddz)
+        : nx(x), ny(y), nz(z), dx(ddx), dy(ddy), dz(ddz), v(static_cast<std::size_t>(x) * y * z, cx(0.0, 0.0)) {}
+    cx& at(int x, int y, int z) {
+        if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz)
+            throw InputError("flux combination index out of range (the reference asserts here)");
+        return v[static_cast<std::size_t>(x) + static_cast<std::size_t>(nx) * (z + static_cast<std::size_t>(nz) * y)];
+    }
+};
+
+// simps2D (parallelFlux.hpp:578-597) on a (x, y) grid
+cx simps2D(CGrid& g) {
+    if (g.ny > 1 && g.nx > 1) {
+        std::vector<cx> res(static_cast<std::size_t>(g.ny), 0.0);
+        for (int jj = 0; jj < g.ny; ++jj) res[jj] = simps(&g.at(0, jj, 0), g.nx, g.dx);
+        return simps(res.data(), static_cast<int>(res.size()), g.dy);
+    } else if (g.nx > 1) {
+        return simps(&g.at(0, 0, 0), g.nx, g.dx);
+    } else if (g.ny > 1) {
+        return simps(&g.at(0, 0, 0), g.ny, g.dy);
+    }
+    throw UnsupportedError("a single-point flux face has no defined integral in the reference");
+}
+
+}  // namespace
+
+void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) {
+    const Dims& D = P.dims;
+    auto lnv = [&](int ax) { return ax == 0 ? D.lx : (ax == 1 ? D.ly : D.lz); };
+    for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
+        const FluxPlan& fp = P.fluxes[q];
+        const int nfreq = static_cast<int>(fp.spec.freqList.size());
+        const std::vector<double>& re = R.fluxRe[q];
+        const std::vector<double>& im = R.fluxIm[q];
+        const int nt = R.fluxSamples[q];
+        const auto& loc_ = fp.spec.loc;
+        std::vector<std::unique_ptr<CGrid>> Ef[2], Hf[2];  // [J/K][face]
+        for (const FluxFace& f : fp.faces) {
+            std::array<int, 2> addIndex = {std::max(0, 0 - loc_[f.transCor1]), std::max(0, 0 - loc_[f.cor])};
+            const std::vector<int>* lists[4] = {&f.Ej, &f.Ek, &f.Hj, &f.Hk};
+            std::unique_ptr<CGrid> grids[4];
+            for (int w = 0; w < 4; ++w) {
+                if (lists[w]->empty()) continue;
+                grids[w].reset(new CGrid(nfreq, f.faceSz[f.transCor1], f.faceSz[f.cor], fp.dLam, P.in.d[f.transCor1], P.in.d[f.cor]));
+                // act / trans fields and the J/K coordinate of constructSzProcOffsetLists (Real flux)
+                bool act = true, trans = false;
+                int corJK = 0;
+                int actComp = P.fluxes[q].stores[(*lists[w])[0]].comp;
+                (void)actComp;
+                const std::vector<int>* other = nullptr;
+                if (w == 0) { other = lists[1]; corJK = f.corJ; }
+                if (w == 1) { other = lists[0]; corJK = f.corK; }
+                if (w == 2) { other = lists[3]; corJK = f.corK; }
+                if (w == 3) { other = lists[2]; corJK = f.corJ; }
+                // the complementary field exists when its component is present
+                {
+                    int ej, ek, hj, hk;
+                    if (f.corI == 0) { ej = EY; hj = HY; ek = EZ; hk = HZ; }
+                    else if (f.corI == 1) { ej = EZ; hj = HZ; ek = EX; hk = HX; }
+                    else { ej = EX; hj = HX; ek = EY; hk = HY; }
+                    int comps[4] = {ej, ek, hj, hk};
+                    int oth[4] = {1, 0, 3, 2};
+                    act = P.comp[comps[w]].present;
+                    trans = P.comp[comps[oth[w]]].present;
+                }
+                (void)other;
+                const std::vector<int>& lst = *lists[w];
+                const double scaleDen = static_cast<double>(lst.size());
+                for (std::size_t dd = 0; dd < lst.size(); ++dd) {
+                    const FreqStore& st = fp.stores[lst[dd]];
+                    if (st.outN[0] == 0) continue;  // outside the grid: no out grid
+                    std::vector<std::array<int, 9>> so;
+                    const int oy = st.outN[1], oz = st.outN[2];
+                    if (act && trans) {
+                        so.assign(2, {0, oy, oz, 0, 0, 0, 0, 0, 0});
+                        if (f.cor == corJK) {
+                            if (addIndex[1] == 0) {
+                                so[1][6] = 1;
+                                so[1][4] = 1;
+                            } else {
+                                so[0][8] = 1;
+                            }
+                            if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][4] = 1;
+                        } else if (f.transCor1 == corJK) {
+                            if (addIndex[0] == 0) {
+                                so[1][5] = 1;
+                                so[1][3] = 1;
+                            } else {
+                                so[0][7] = 1;
+                            }
+                            if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][3] = 1;
+                        }
+                    } else {
+                        so.assign(1, {0, oy, oz, 0, 0, 0, 0, 0, 0});
+                    }
+                    const double scale = 1.0 / (scaleDen * static_cast<double>(so.size()));
+                    for (auto& o : so)
+                        for (int jj = 0; jj < o[2] - o[4]; ++jj)
+                            for (int ii = 0; ii < o[1] - o[3]; ++ii) {
+                                long long pt = st.accOffset + (jj + o[6]) + static_cast<long long>(ii + o[5]) * oz;
+                                for (int fq = 0; fq < nfreq; ++fq) {
+                                    cx v(re[static_cast<std::size_t>(pt) * nfreq + fq], im[static_cast<std::size_t>(pt) * nfreq + fq]);
+                                    grids[w]->at(fq, ii + addIndex[0] + o[7], jj + addIndex[1] + o[8]) += scale * v;
+                                }
+                            }
+                }
+            }
+            Ef[0].push_back(std::move(grids[0]));
+            Ef[1].push_back(std::move(grids[1]));
+            Hf[0].push_back(std::move(grids[2]));
+            Hf[1].push_back(std::move(grids[3]));
+        }
+        // getFlux (parallelFlux.hpp:406-545)
+        const std::string path = out_path(outDir, fp.spec.name + ".dat");
+        std::ofstream f(path);
+        if (!f) throw InputError("cannot open flux output " + path);
+        const std::size_t nFaces = fp.faces.size();
+        f << "#" << std::setw(16) << "freq\tabs(incd)\treal(incd)\timag(incd)";
+        if (nFaces > 1) {
+            f << std::setw(16) << "\tabs(right)\treal(right)\timag(right)\tabs(left)\treal(left)\timag(left)\tabs(top)\treal(top)\timag(top)\tabs(bot)\treal(bot)\timag(bot)";
+            if (fp.spec.sz[0] > 1 && fp.spec.sz[1] > 1 && fp.spec.sz[2] > 1)
+                f << std::setw(16) << "\tabs(front)\treal(front)\timag(front)\tabs(back)\treal(back)\timag(back)";
+        }
+        f << std::setw(16) << "freq\tabs(total)\treal(total)\timag(total)\n";
+        const double tInt = static_cast<double>(fp.spec.timeInt);
+        const std::size_t nIncd = 2 * (static_cast<std::size_t>(P.nSteps) + 1) + 2;
+        for (int ff = 0; ff < nfreq; ++ff) {
+            cx flux = 0.0;
+            // incident fields are zero without a TFSF surface; the transform is kept for its form
+            cx inc[6] = {0, 0, 0, 0, 0, 0};
+            (void)nIncd;
+            cx flux_incd = std::pow(fp.incdConv[0] * (inc[1] * std::conj(inc[5]) - inc[2] * std::conj(inc[4])) /
+                                        (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
+            flux_incd += std::pow(fp.incdConv[1] * (inc[2] * std::conj(inc[3]) - inc[0] * std::conj(inc[5])) /
+                                      (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
+            flux_incd += std::pow(fp.incdConv[2] * (inc[0] * std::conj(inc[4]) - inc[1] * std::conj(inc[3])) /
+                                      (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
+            flux_incd = std::sqrt(flux_incd);
+            (void)tInt;
+            f << std::setw(18) << std::setprecision(15) << fp.freqConv * fp.spec.freqList[ff] << "\t" << std::setw(16)
+              << std::setprecision(15) << std::abs(flux_incd) << "\t" << std::setw(16) << std::setprecision(15)
+              << std::abs(std::real(flux_incd)) << "\t" << std::setw(16) << std::setprecision(15) << std::imag(flux_incd)
+              << "\t";
+            for (std::size_t vv = 0; vv < nFaces; ++vv) {
+                CGrid* Ej = Ef[0][vv].get();
+                CGrid* Ek = Ef[1][vv].get();
+                CGrid* Hj = Hf[0][vv].get();
+                CGrid* Hk = Hf[1][vv].get();
+                CGrid* gE = Ej ? Ej : Ek;
+                CGrid* gH = Ej ? Hk : Hj;
+                if (!gE || !gH) throw InputError("flux face without field pairs");
+                // flux grids are (x = sz[cor], y = sz[transCor1]), spacing (d[cor], d[transCor1])
+                CGrid ijk(gE->nz, gE->ny, 1, gE->dz, gE->dy, 1.0);
+                CGrid ikj(ijk.nx, ijk.ny, 1, ijk.dx, ijk.dy, 1.0);
+                const double nt2 = std::pow(static_cast<double>(nt), 2.0);
+                const int sz = fp.faces[vv].sz;
+                if (Ej) {
+                    for (int s = 0; s < sz; ++s) {
+                        cx e = Ej->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                        cx h = Hk->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                        ijk.v[s] = e * std::conj(h) / nt2;
+                    }
+                }
+                if (Ek) {
+                    for (int s = 0; s < sz; ++s) {
+                        cx e = Ek->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                        cx h = Hj->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                        ikj.v[s] = e * std::conj(h) / nt2;
+                    }
+                    for (std::size_t s = 0; s < ijk.v.size(); ++s) ijk.v[s] += cx(-1.0) * ikj.v[s];
+                }
+                cx tempFlux = fp.fluxConv * fp.faces[vv].weight * simps2D(ijk);
+                flux += tempFlux;
+                f << std::setw(16) << std::setprecision(15) << std::abs(tempFlux) << "\t" << std::setw(16)
+                  << std::setprecision(15) << std::real(tempFlux) << "\t" << std::setw(16) << std::setprecision(15)
+                  << std::imag(tempFlux) << "\t";
+            }
+            if (nFaces > 1)
+                f << std::setw(16) << std::setprecision(15) << std::abs(flux) << "\t" << std::setw(16) << std::setprecision(15)
+                  << std::real(flux) << "\t" << std::setw(16) << std::setprecision(15) << std::imag(flux) << std::endl;
+            else
+                f << std::endl;
+        }
+    }
+}
+
+}  // namespace chiml

@@ -1,0 +1,34 @@
+// End-of-run products of a simulation: detector files and DFT-flux spectra,
+// written in chiML's formats.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "plan.hpp"
+
+namespace chiml {
+
+// Values gathered during the run, in the layout the writers expect.
+struct RunRecord {
+    // detectors[k][e] = concatenated field boxes (fields in plan order, each
+    // box in storage order) at output event e (step e * timeInt)
+    std::vector<std::vector<std::vector<double>>> detectors;
+    // flux accumulators per flux: re/im [point][freq], and the number of DFT samples
+    std::vector<std::vector<double>> fluxRe, fluxIm;
+    std::vector<int> fluxSamples;
+};
+
+// Number of values one output event of detector k stores.
+long long detector_event_values(const DetectorPlan& dp);
+// Number of output events of a detector over nSteps steps (including t = 0).
+int detector_events(const DetectorPlan& dp, int nSteps);
+
+// Writes every detector file (TXT: parallelDTC_TXT.cpp:13-55; BIN: parallelDTC_BIN.cpp:12-50).
+void write_detectors(const Plan& P, const RunRecord& R, const std::string& outDir, int stepsDone);
+// Combines the flux accumulators and writes "<name>.dat" (parallelFlux.hpp:325-560).
+void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir);
+
+std::string out_path(const std::string& outDir, const std::string& name);
+
+}  // namespace chiml

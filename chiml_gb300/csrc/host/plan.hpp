@@ -1,0 +1,159 @@
+// The compiled form of a simulation that the CUDA kernels (and the CPU oracle)
+// execute: grid dimensions, a per-cell class code for every Yee component, a
+// small table of per-class coefficients, 1-D CPML profiles, and the source,
+// detector and DFT-flux descriptors.
+//
+// Every cell of component c follows one update rule:
+//
+//   psi_t  <- b_t[a] * psi_t + cpsi_t[a] * (G_t[i] - G_t[i + off_t])          (if psi_t flag)
+//   U[i]   += (cint_t + nplain_t * db_t + (kflag_t ? kprof_t[a] : 0))
+//               * (G_t[i] - G_t[i + off_t])  + npsi_t * dbpsi_t * psi_t[i]     (for t = J, K)
+//
+// where U is E/H or D (per class), G_J / G_K are the two neighbouring field
+// components, a is the cell's coordinate along the term's derivative axis, and
+// the class table supplies cint/nplain/kflag/npsi. This reproduces the sum of
+// chiML's interior curl lists (FDTD_MANAGER/parallelFDTDField.hpp:628-856)
+// and CPML lists (PML/parallelPML.hpp:321-697) cell by cell; build_plan checks
+// the compressed form against a literal accumulation of those lists.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "model.hpp"
+
+namespace chiml {
+
+// Grid layout kept from chiML's Grid (GRID/Grid.hpp:201-205): x fastest, then z,
+// then y, with a one-cell halo on every side (2-D: lz == 1, no z halo).
+struct Dims {
+    int nx = 0, ny = 0, nz = 1;  // physical points (n_vec_)
+    int lx = 0, ly = 0, lz = 1;  // local extents including the halo
+    bool threeD = false;
+    long long cells() const { return static_cast<long long>(lx) * ly * lz; }
+    long long idx(int x, int y, int z) const { return x + static_cast<long long>(lx) * (z + static_cast<long long>(lz) * y); }
+};
+
+// Component ids: 0..2 = Ex,Ey,Ez ; 3..5 = Hx,Hy,Hz
+enum Comp { EX = 0, EY = 1, EZ = 2, HX = 3, HY = 4, HZ = 5 };
+
+struct TermPlan {
+    bool present = false;   // the component has this neighbour field
+    int field = -1;         // component id of G_t
+    int axis = 0;           // derivative axis (0 x, 1 y, 2 z)
+    long long off = 0;      // index offset of the neighbour (i + off)
+    double db = 0.0;        // DbFieldBase of the CPML term (dt / d, signed)
+    double dbpsi = 0.0;     // Db of the CPML term (+-dt)
+    bool hasPsi = false;    // psi storage exists for this term
+    std::vector<double> kprof;  // per coordinate along axis: CPML coefficient of deriv-normal slab cells
+    std::vector<double> b, cpsi; // per coordinate along axis: psi recursion coefficients
+};
+
+struct ClassInfo {
+    uint8_t toD = 0;       // 1: the curl and CPML terms update D instead of the field
+    uint8_t lor = 0;       // 1: Lorentz P update before and D -> E after (upLorD list)
+    uint8_t ordip = 0;     // 1: oriented-dipole D -> E (upOrDipD list)
+    int obj = 0;           // object whose poles apply (lor)
+    double eps = 1.0;      // eps_inf used by D -> E
+    double cint[2] = {0.0, 0.0};  // interior curl coefficients of terms J, K
+    uint8_t nplain[2] = {0, 0};
+    uint8_t kflag[2] = {0, 0};
+    uint8_t npsi[2] = {0, 0};
+    uint8_t psiUpd[2] = {0, 0};  // psi recursion applied at this cell
+    bool operator==(const ClassInfo& o) const;
+};
+
+struct CompPlan {
+    bool present = false;
+    bool isE = true;
+    bool hasD = false;
+    std::vector<uint8_t> code;     // per cell, index into classes
+    std::vector<ClassInfo> classes;
+    TermPlan term[2];              // J (uses grid_j), K (uses grid_k)
+    int nPoles = 0;                // number of Lorentz pole grids of this component
+};
+
+// Oriented-dipole Lorentz cells (upOrDipP list) on the cell-corner grid.
+struct OrDipPlan {
+    bool present = false;
+    int nPoles = 0;
+    std::vector<long long> cells;           // grid index of each updated cell
+    std::vector<int> obj;                   // object of each cell
+    std::vector<std::array<double, 3>> dip; // per pole per cell: dip_x, dip_y, dip_z (cells * nPoles)
+    long long offA[3] = {0, 0, 0};          // E_c neighbour offsets for the averaged dot product
+};
+
+struct SourcePlan {
+    int comp = EZ;
+    std::vector<long long> cells;
+    std::vector<double> value;  // dt * Re(sum of pulses) per step (index = step)
+};
+
+// A box of grid cells sampled by a time-domain detector.
+struct DetectorPlan {
+    DetectorSpec spec;
+    int timeInt = 1;
+    double tConv = 1.0, convFactor = 1.0;
+    std::array<double, 3> realLoc = {0, 0, 0};
+    bool power = false;
+    struct Field {
+        int comp;           // component id, or 6+c for D_c
+        std::array<int, 3> off;
+        std::array<int, 3> outSz;  // storage box size
+        std::vector<long long> cells;  // outGrid order (x + sx*(z + sz*y)), -1 where not stored
+    };
+    std::vector<Field> fields;
+    std::array<int, 3> sz = {1, 1, 1};
+};
+
+// One DFT accumulator box (parallelStorageFreqDTC) of a flux region.
+struct FreqStore {
+    int comp = 0;
+    std::array<int, 3> loc = {0, 0, 0}, sz = {1, 1, 1};
+    int propDir = 0;              // 0 X, 1 Y, 2 Z
+    std::array<int, 3> inSz = {0, 0, 0};  // fieldInFreq_.sz_
+    std::array<int, 3> outN = {0, 0, 0}; // outGrid dims {nfreq, sz1, sz0}
+    std::vector<long long> cells; // grid index of accumulated points, outGrid point order
+    long long accOffset = 0;      // offset (in points) into the flux's accumulator
+};
+
+struct FluxFace {
+    double weight = 1.0;
+    int sz = 0;
+    std::vector<int> Ej, Ek, Hj, Hk;   // indices into FluxPlan::stores
+    int cor = 0, transCor1 = 0, transCor2 = 0, corI = 0, corJ = 0, corK = 0;
+    std::array<int, 3> faceSz = {1, 1, 1};
+};
+
+struct FluxPlan {
+    FluxSpec spec;
+    std::vector<FreqStore> stores;
+    std::vector<FluxFace> faces;
+    long long npts = 0;            // total accumulated points
+    double dt = 0.0;
+    double fluxConv = 1.0, incdConv[3] = {1, 1, 1}, freqConv = 1.0, dLam = 0.0, dOmg = 0.0;
+    bool real3D = false;
+};
+
+struct Plan {
+    Inputs in;
+    Dims dims;
+    double dt = 0.0;
+    int nSteps = 0;
+    std::vector<double> tcur;  // time at the start of each step (tcur_ accumulation), size nSteps + 1
+    bool disp = false, dielectricMatInPML = false;
+    CompPlan comp[6];
+    OrDipPlan ordip;
+    std::vector<SourcePlan> sources;
+    std::vector<DetectorPlan> detectors;
+    std::vector<FluxPlan> fluxes;
+    // object pole coefficients, flattened: per object, per pole
+    std::vector<std::vector<double>> alpha, xi, gamma;
+};
+
+// Builds the plan; throws InputError / UnsupportedError.
+Plan build_plan(const Inputs& in);
+
+}  // namespace chiml

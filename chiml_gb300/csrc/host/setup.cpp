@@ -1,0 +1,1190 @@
+// Plan construction: a single-process restatement of the set-up work of chiML's
+// field manager (FDTD_MANAGER/parallelFDTDField.hpp:214-1048,
+// FDTD_MANAGER/parallelFDTDField.cpp:13-852) and CPML (PML/parallelPML.hpp:102-765).
+//
+// The reference builds lists of x-runs per update kind; here the same lists are
+// generated (for one process: procLoc = 0, rank = size - 1 = 0), accumulated per
+// cell, and compressed into the class-code form of plan.hpp. The compressed form
+// is then checked cell by cell against the literal accumulation.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <set>
+#include <tuple>
+
+#include "plan.hpp"
+
+namespace chiml {
+
+bool ClassInfo::operator==(const ClassInfo& o) const {
+    return toD == o.toD && lor == o.lor && ordip == o.ordip && obj == o.obj && eps == o.eps &&
+           cint[0] == o.cint[0] && cint[1] == o.cint[1] && nplain[0] == o.nplain[0] && nplain[1] == o.nplain[1] &&
+           kflag[0] == o.kflag[0] && kflag[1] == o.kflag[1] && npsi[0] == o.npsi[0] && npsi[1] == o.npsi[1] &&
+           psiUpd[0] == o.psiUpd[0] && psiUpd[1] == o.psiUpd[1];
+}
+
+namespace {
+
+template <typename T>
+struct Field3 {
+    Dims d;
+    std::vector<T> v;
+    Field3() {}
+    Field3(const Dims& dd, T init) : d(dd), v(static_cast<std::size_t>(dd.cells()), init) {}
+    T& at(int x, int y, int z) { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
+    T at(int x, int y, int z) const { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
+};
+
+// Polarisation sets used by the CPML list builders: component c in 0..5
+// (Ex,Ey,Ez,Hx,Hy,Hz) belongs to a set given as a bit mask.
+constexpr int bEX = 1, bEY = 2, bEZ = 4, bHX = 8, bHY = 16, bHZ = 32;
+inline bool inSet(int comp, int mask) { return (mask >> comp) & 1; }
+
+struct Builder {
+    const Inputs& in;
+    Plan& P;
+    Dims D;
+    std::array<int, 3> nvec;        // physical points per axis (n_vec_)
+    std::array<double, 3> d;
+    double dt;
+    std::vector<Object> objs;
+    bool matInPML = false;
+    // phys (object id) and eps maps per staggered grid: 0..2 E, 3..5 H, 6 POrDip, 7 MOrDip
+    Field3<int> phys[8];
+    Field3<double> epsRel[8];
+
+    Builder(const Inputs& i, Plan& p) : in(i), P(p) {}
+
+    // setupPhysFields, parallelFDTDField.hpp:867-947
+    void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff) {
+        Field3<int> ph(D, 0);
+        Field3<double> ep(D, 1.0);
+        const bool twoD = (D.lz == 1);
+        int zmin = twoD ? 0 : 1;
+        int zmax = twoD ? 1 : D.lz - 1;
+        for (std::size_t oo = 1; oo < objs.size(); ++oo) {
+            const Object& o = objs[oo];
+            if (!(o.ML || o.gamma.size() > 0 || o.epsInf != 1.0)) continue;
+            for (int ii = 1; ii < D.lx - 1; ++ii)
+                for (int jj = 1; jj < D.ly - 1; ++jj)
+                    for (int kk = zmin; kk < zmax; ++kk) {
+                        std::array<double, 3> pt;
+                        pt[0] = ((ii - 1) + offPt[0] + 0 - (nvec[0] - nvec[0] % 2) / 2.0) * d[0];
+                        pt[1] = ((jj - 1) + offPt[1] + 0 - (nvec[1] - nvec[1] % 2) / 2.0) * d[1];
+                        pt[2] = ((kk - 1) + offPt[2] + 0 - (nvec[2] - nvec[2] % 2) / 2.0) * d[2];
+                        if (o.isObj(pt, d[0], o.geoML)) ph.at(ii, jj, kk) = static_cast<int>(oo);
+                        if (o.isObj(pt, d[0], o.geo)) ep.at(ii, jj, kk) = E ? o.epsInf : 1.0;
+                    }
+        }
+        zmin = 0;
+        zmax = twoD ? 1 : D.lz;
+        if (!twoD) {
+            for (int ii = 0; ii < D.lx; ++ii)
+                for (int jj = 0; jj < D.ly; ++jj) {
+                    ph.at(ii, jj, 0) = -1;
+                    ph.at(ii, jj, zmax - 1) = -1;
+                    if (endOff[2] == 1) {
+                        ph.at(ii, jj, zmax - 2) = -1;
+                        ep.at(ii, jj, zmax - 2) = 0.0;
+                    }
+                }
+        }
+        for (int ii = 0; ii < D.lx; ++ii)
+            for (int kk = zmin; kk < zmax; ++kk) {
+                ph.at(ii, 0, kk) = -1;
+                ph.at(ii, D.ly - 1, kk) = -1;
+                if (endOff[1] == 1 && D.ly > 3) {
+                    ph.at(ii, D.ly - 2, kk) = -1;
+                    ep.at(ii, D.ly - 2, kk) = 0.0;
+                }
+            }
+        for (int kk = zmin; kk < zmax; ++kk)
+            for (int jj = 0; jj < D.ly; ++jj) {
+                ph.at(0, jj, kk) = -1;
+                ph.at(D.lx - 1, jj, kk) = -1;
+                if (endOff[0] == 1 && D.lx > 3) {
+                    ph.at(D.lx - 2, jj, kk) = -1;
+                    ep.at(D.lx - 2, jj, kk) = 0.0;
+                }
+            }
+        phys[g] = std::move(ph);
+        epsRel[g] = std::move(ep);
+    }
+
+    // Material-in-PML scan, parallelFDTDField.hpp:274-370 (including its loop-bound carry-over)
+    void scanPML() {
+        for (int pp = 0; pp < 3; ++pp) {
+            int ci = pp, cj = (pp + 1) % 3, ck = (pp + 2) % 3;
+            std::array<int, 3> mn, mx;
+            for (int q = 0; q < 3; ++q) {
+                mn[q] = static_cast<int>(-1 * static_cast<double>(nvec[q]) / 2);
+                mx[q] = static_cast<int>(static_cast<double>(nvec[q]) / 2);
+            }
+            mx[ci] = static_cast<int>(in.pmlThickness[ci] - nvec[ci] / 2.0);
+            for (std::size_t oo = 0; oo < objs.size(); ++oo) {
+                const Object& o = objs[oo];
+                if (o.epsInf == 1.0 && o.gamma.size() < 1 && !o.ML) continue;
+                bool dielc = !(o.epsInf == 1.0 && o.gamma.size() < 1);
+                for (int jj = mn[cj]; jj < mx[cj]; ++jj)
+                    for (int kk = mn[ck]; kk < mx[ck]; ++kk) {
+                        for (int pass = 0; pass < 2; ++pass) {
+                            if (pass == 1) {
+                                mn[ci] = nvec[ci] / 2 - in.pmlThickness[ci];
+                                mx[ci] = nvec[ci] / 2;
+                            }
+                            for (int ii = mn[ci]; ii < mx[ci]; ++ii) {
+                                std::array<double, 3> pt = {0, 0, 0};
+                                pt[ci] = static_cast<double>(ii) * d[ci];
+                                pt[cj] = static_cast<double>(jj) * d[cj];
+                                pt[ck] = static_cast<double>(kk) * d[ck];
+                                pt[0] += d[0] / 2.0;
+                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                pt[1] += d[1] / 2.0;
+                                pt[0] -= d[0] / 2.0;
+                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                pt[2] += d[2] / 2.0;
+                                pt[1] -= d[0] / 2.0;
+                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                pt[0] += d[2] / 2.0;
+                            }
+                        }
+                    }
+            }
+        }
+    }
+
+    // ---- CPML (parallelPML.hpp) ----
+    struct Pml {
+        int comp;  // 0..5
+        bool E;
+        int ax_i, ax_j, ax_k;
+        std::array<int, 3> T;          // thickness n_vec_
+        std::array<int, 3> lnMn = {0, 0, 0}, lnPl = {0, 0, 0};
+        std::vector<double> eta[3][2];  // [axis][pl]
+        bool gridJ, gridK, psiJ, psiK;  // grid_j / grid_k exist, psi_j / psi_k exist
+    };
+
+    double sigmaMax(int ax) const { return in.pmlSigOptRat * 0.8 * (in.pmlM + 1) / d[ax]; }
+    double kappaF(double ii, double iiMax) const {
+        return (0.0 <= ii && ii <= iiMax) ? 1.0 + (in.pmlKappaMax - 1.0) * std::pow((iiMax - ii) / iiMax, in.pmlM) : 1.0;
+    }
+    double aValF(double ii, double iiMax) const {
+        return (0.0 <= ii && ii <= iiMax) ? in.pmlAMax * std::pow(ii / iiMax, in.pmlMa) : 0.0;
+    }
+    double sigmaF(double ii, double iiMax, double eta, double sMax) const {
+        return (0.0 <= ii && ii <= iiMax) ? sMax / eta * std::pow((iiMax - ii) / iiMax, in.pmlM) : 0.0;
+    }
+    double bF(double sig, double a, double kap) const { return std::exp(-1.0 * (sig / kap + a) * dt); }
+    double cF(double sig, double a, double kap) const {
+        return (sig == 0 && a == 0) ? 0 : sig * (bF(sig, a, kap) - 1.0) / (kap * (sig + kap * a));
+    }
+    int lnv(int ax) const { return ax == 0 ? D.lx : (ax == 1 ? D.ly : D.lz); }
+    // parallelGrid n_vec_ (x, y include the halo; z is 1 in 2-D)
+    int gnv(int ax) const { return ax == 0 ? D.lx : (ax == 1 ? D.ly : D.lz); }
+
+    // genEtaEff (parallelPML.hpp:192-275) with the single-process plane getters
+    void genEta(Pml& p, int g, int dir, bool pl, std::vector<double>& eta) {
+        std::array<int, 3> pst = {D.lx - 2, D.ly - 2, D.lz - 2};
+        int c = p.comp;
+        if (inSet(c, bEX | bHY | bHZ)) pst[0] -= 1;
+        if (inSet(c, bEY | bHX | bHZ)) pst[1] -= 1;
+        if (inSet(c, bEZ | bHX | bHY)) pst[2] -= 1;
+        if (D.lz == 1) pst[2] = 1;
+        std::array<int, 2> psz;
+        if (dir == 0) psz = {pst[2], pst[1]};
+        else if (dir == 1) psz = {pst[0], pst[2]};
+        else psz = {pst[0], pst[1]};
+        int mn = pl ? gnv(dir) - 2 - p.T[dir] : 0;
+        int mx = pl ? gnv(dir) - 2 : p.T[dir];
+        const int zoff = (D.lz != 1) ? 1 : 0;
+        const Field3<int>& ph = phys[g];
+        for (int ii = mn; ii < mx; ++ii) {
+            std::vector<int> plane(static_cast<std::size_t>(std::max(0, psz[0] * psz[1])), 0);
+            if (dir == 0) {
+                int ySz = (D.ly - 2 > psz[1]) ? psz[1] : D.ly - 2;
+                for (int yy = 0; yy < ySz; ++yy)
+                    for (int zz = 0; zz < psz[0]; ++zz) plane[zz + yy * psz[0]] = ph.at(ii + 1, yy + 1, zz + zoff);
+            } else if (dir == 1) {
+                for (int zz = 0; zz < psz[1]; ++zz)
+                    for (int x = 0; x < psz[0]; ++x) plane[zz * psz[0] + x] = ph.at(1 + x, ii + 1, zz + zoff);
+            } else {
+                int ySz = (D.ly - 2 > psz[1]) ? psz[1] : D.ly - 2;
+                for (int yy = 0; yy < ySz; ++yy)
+                    for (int x = 0; x < psz[0]; ++x) plane[psz[0] * yy + x] = ph.at(1 + x, yy + 1, ii + zoff);
+            }
+            double eps_sum = 0.0, mu_sum = 0.0;
+            for (int val : plane)
+                if (val != -1) {
+                    eps_sum += objs[val].epsInf / static_cast<double>(plane.size());
+                    mu_sum += 1.0 / static_cast<double>(plane.size());
+                }
+            double etaSum = eps_sum * mu_sum;
+            double etaVal = (etaSum != 0.00) ? etaSum : 0;
+            if (static_cast<int>(eta.size()) < p.T[dir] && etaVal != 0.0) eta.push_back(etaVal);
+        }
+    }
+
+    struct PsiEntry {  // one run of the psi list
+        long long ind, indOff;
+        int n;
+        long long stride;
+        double b, c;
+        int normCoord;  // coordinate along the normal axis
+    };
+    struct GridEntry {  // one run of the grid list
+        long long ind, indOff;
+        int n;
+        long long stride;
+        double Db, DbField;
+        int startDeriv;  // coordinate of the run start along the derivative axis
+        int slab;        // slab normal axis
+        bool pl;
+    };
+
+    // getPsiUpList, parallelPML.hpp:321-451
+    void psiList(const Pml& p, int dir, bool pl, int startPt, int nDir, int dirMax, std::vector<PsiEntry>& out) {
+        const bool E = p.E;
+        const int c = p.comp;
+        int transSz2 = 1;
+        int cn = -1, t1 = -1, t2 = -1, tr1Off = 0, tr2Off = 0, ccStart = 0;
+        long long stride = 0;
+        double sMax = sigmaMax(dir);
+        const std::vector<double>* eta;
+        if (dir == 0) {
+            cn = 0;
+            t1 = (D.lz == 1) ? 1 : 2;
+            t2 = (D.lz == 1) ? 2 : 1;
+            stride = D.lx;
+            eta = &p.eta[0][pl ? 1 : 0];
+            if (inSet(c, bEY | bHX | bHZ)) (D.lz == 1) ? tr1Off = 1 : tr2Off = 1;
+            if (inSet(c, bHY | bHX | bEZ)) (D.lz == 1) ? tr2Off = 1 : tr1Off = 1;
+            if (inSet(c, bHZ | bHY | bEX)) pl ? ccStart = 1 : dirMax -= 1;
+        } else if (dir == 1) {
+            cn = 1; t1 = 0; t2 = 2;
+            stride = 1;
+            eta = &p.eta[1][pl ? 1 : 0];
+            if (inSet(c, bEX | bHY | bHZ)) tr1Off = 1;
+            if (inSet(c, bHX | bHY | bEZ)) tr2Off = 1;
+            if (pl && inSet(c, bHZ | bHX | bEY)) ccStart = 1;
+            if (!pl && startPt + dirMax == nDir && inSet(c, bHZ | bHX | bEY)) dirMax -= 1;
+        } else {
+            cn = 2; t1 = 0; t2 = 1;
+            stride = 1;
+            eta = &p.eta[2][pl ? 1 : 0];
+            if (inSet(c, bEX | bHY | bHZ)) tr1Off = 1;
+            if (inSet(c, bHX | bHZ | bEY)) tr2Off = 1;
+            if (inSet(c, bHX | bHY | bEZ)) pl ? ccStart = 1 : dirMax -= 1;
+        }
+        int transSz = lnv(t1) - 2 - tr1Off;
+        transSz2 = lnv(t2) - 2 - tr2Off;
+        if (D.lz == 1 && t2 == 2) transSz2 = 1;
+        double distOff = E ? 0.0 : 0.5;
+        std::array<int, 3> loc = {-1, -1, -1};
+        loc[t1] = 1;
+        for (int cc = ccStart; cc < dirMax; ++cc) {
+            loc[cn] = pl ? lnv(cn) - 2 - cc : cc + 1;
+            double dist = 0 + (loc[cn] - 1) + distOff;
+            if (pl) dist = gnv(cn) - 2 - 1 - dist;
+            if (dist < 0 || static_cast<std::size_t>(dist) >= eta->size())
+                throw UnsupportedError("CPML eta profile index out of range (the reference aborts here)");
+            double sig = sigmaF(dist, static_cast<double>(nDir - 1), eta->at(static_cast<std::size_t>(dist)), sMax);
+            double kap = kappaF(dist, static_cast<double>(nDir - 1));
+            double a = aValF(dist, static_cast<double>(nDir - 1));
+            PsiEntry e;
+            e.b = bF(sig, a, kap);
+            e.c = cF(sig, a, kap) / d[cn];
+            if (!E) e.c *= -1.0;
+            e.n = transSz;
+            e.stride = stride;
+            e.normCoord = loc[cn];
+            for (int jj = 0; jj < transSz2; ++jj) {
+                loc[t2] = 1 + jj;
+                if (D.lz == 1) loc[2] = 0;
+                std::array<int, 3> lo = loc;
+                lo[cn] += E ? -1 : 1;
+                e.ind = D.idx(loc[0], loc[1], loc[2]);
+                e.indOff = D.idx(lo[0], lo[1], lo[2]);
+                out.push_back(e);
+            }
+        }
+    }
+
+    // getGridUpList, parallelPML.hpp:500-656
+    void gridList(const Pml& p, int dir, int derivDir, bool pl, std::vector<GridEntry>& out) {
+        const bool E = p.E;
+        const int c = p.comp;
+        std::array<int, 3> mn = {0, 0, 0}, mx = {0, 0, 0};
+        int ci = 0, cj = 0, ck = 0, offii = 0;
+        long long stride = 1;
+        double Db = dt, DbBase = dt;
+        std::array<int, 3> offset = {0, 0, 0};
+        if (dir == 0) {
+            ci = 0; cj = 1; ck = 2;
+            stride = D.lx;
+            if (pl && inSet(c, bHZ | bEX | bHY)) offii = -1;
+            else if (!pl) offii = 1;
+        } else if (dir == 1) {
+            ci = 1; cj = 2; ck = 0;
+            stride = 1;
+            if (pl && inSet(c, bHZ | bHX | bEY)) offii = -1;
+            if (!pl) offii = 1;
+        } else {
+            ci = 2; cj = 0; ck = 1;
+            stride = 1;
+            if (pl && inSet(c, bEZ | bHX | bHY)) offii = -1;
+            else if (!pl) offii = 1;
+        }
+        int cd = derivDir;
+        if (derivDir == 0) {
+            if (inSet(c, bHZ | bEY)) Db *= -1.0;
+            if (inSet(c, bHY | bEY)) DbBase *= -1.0;
+        } else if (derivDir == 1) {
+            if (inSet(c, bHX | bEZ)) Db *= -1.0;
+            if (inSet(c, bHZ | bEZ)) DbBase *= -1.0;
+        } else {
+            if (inSet(c, bHY | bEX)) Db *= -1.0;
+            if (inSet(c, bHX | bEX)) DbBase *= -1.0;
+        }
+        DbBase /= d[cd];
+        offset[cd] = E ? -1 : 1;
+        mn[ci] += pl ? lnv(ci) - p.lnPl[ci] - 1 : 1;
+        mx[ci] += offii + (pl ? lnv(ci) - 1 : p.lnMn[ci]);
+        mn[cj] = 1;
+        mx[cj] = lnv(cj) - 1;
+        mn[ck] = 1;
+        mx[ck] = lnv(ck) - 1;
+        if (dir == p.ax_i) {
+            mn[cj] += p.lnMn[cj];
+            mx[cj] -= p.lnPl[cj] - ((E || (cj == 1 && false)) ? 0 : 1);
+            mn[ck] += p.lnMn[ck];
+            mx[ck] -= p.lnPl[ck] - ((E || (ck == 1 && false)) ? 0 : 1);
+        } else if (cd != ci) {
+            mn[cd] += p.lnMn[cd];
+            mx[cd] -= p.lnPl[cd] - ((E || (cd == 1 && false)) ? 0 : 1);
+        }
+        if (ci != 0 && inSet(c, bHZ | bEX | bHY)) mx[0] -= 1;
+        if (ci != 1 && inSet(c, bHZ | bHX | bEY)) mx[1] -= 1;
+        if (ci != 2 && D.lz != 1 && inSet(c, bHX | bHY | bEZ)) mx[2] -= 1;
+        if (D.lz == 1) {
+            mn[2] = 0;
+            mx[2] = 1;
+        }
+        // getAxLists (parallelPML.hpp:462-489)
+        std::vector<std::array<int, 5>> ax;
+        if (stride == 1) {
+            for (int kk = mn[2]; kk < mx[2]; ++kk)
+                for (int jj = mn[1]; jj < mx[1]; ++jj) ax.push_back({mn[0], jj, kk, mx[0] - mn[0], 0});
+        } else if (D.lz == 1) {
+            for (int kk = mn[2]; kk < mx[2]; ++kk)
+                for (int ii = mn[0]; ii < mx[0]; ++ii) ax.push_back({ii, mn[1], kk, mx[1] - mn[1], 0});
+        } else {
+            for (int jj = mn[1]; jj < mx[1]; ++jj)
+                for (int ii = mn[0]; ii < mx[0]; ++ii) ax.push_back({ii, jj, mn[2], mx[2] - mn[2], 0});
+        }
+        double distOff = E ? 0.0 : 0.5;
+        for (auto& a : ax) {
+            double dist = 0 + a[cd] - 1 + distOff;
+            if (pl) dist = gnv(cd) - 2 - 1 - dist;
+            double kap = kappaF(dist, static_cast<double>(p.T[cd] - 1));
+            GridEntry e;
+            e.DbField = DbBase / kap;
+            e.Db = Db;
+            e.ind = D.idx(a[0], a[1], a[2]);
+            e.indOff = D.idx(a[0] + offset[0], a[1] + offset[1], a[2] + offset[2]);
+            e.n = a[3];
+            e.stride = stride;
+            e.startDeriv = a[cd];
+            e.slab = dir;
+            e.pl = pl;
+            out.push_back(e);
+        }
+    }
+
+    // The CPML of one component: ctor + initalizeLists (parallelPML.hpp:102-182, 669-689)
+    void buildPml(int comp, bool gridJ, bool gridK, std::vector<PsiEntry> psi[2], std::vector<GridEntry> grid[2],
+                  double dbBase[2], double dbPsi[2], bool hasPsi[2]) {
+        Pml p;
+        p.comp = comp;
+        p.E = comp < 3;
+        p.ax_i = comp % 3;
+        p.ax_j = (p.ax_i + 1) % 3;
+        p.ax_k = (p.ax_i + 2) % 3;
+        p.T = in.pmlThickness;
+        p.gridJ = gridJ;
+        p.gridK = gridK;
+        p.psiJ = gridK && (D.lz != 1 || p.ax_j != 2);  // psi_j_ (uses grid_k)
+        p.psiK = gridJ && (D.lz != 1 || p.ax_k != 2);  // psi_k_ (uses grid_j)
+        if (!p.psiJ && !p.psiK)
+            throw InputError("Both PML auxiliary fields are undefined");
+        // findLnVecs (single process)
+        for (int q = 0; q < 3; ++q) {
+            if (q == 2 && D.lz == 1) continue;
+            int ln = lnv(q) - 2;
+            if (0 < p.T[q]) p.lnMn[q] = (ln < p.T[q]) ? ln : p.T[q];
+            if (ln > ln - p.T[q]) p.lnPl[q] = (0 > ln - p.T[q]) ? ln : ln - (ln - p.T[q]);
+        }
+        int g = comp;
+        genEta(p, g, 0, false, p.eta[0][0]);
+        genEta(p, g, 0, true, p.eta[0][1]);
+        genEta(p, g, 1, false, p.eta[1][0]);
+        genEta(p, g, 1, true, p.eta[1][1]);
+        if (D.lz != 1) {
+            genEta(p, g, 2, false, p.eta[2][0]);
+            genEta(p, g, 2, true, p.eta[2][1]);
+        }
+        // term K: derivative along j_, field grid_k, psi_j ; term J: derivative along k_, field grid_j, psi_k
+        auto init = [&](int lnPml, int dir, bool pl, int startPt, int nDir, int dirMax) {
+            if (lnPml == 0) return;
+            if (gridK) {
+                if (dir == p.ax_j && p.psiJ) psiList(p, dir, pl, startPt, nDir, dirMax, psi[1]);
+                gridList(p, dir, p.ax_j, pl, grid[1]);
+            }
+            if (gridJ) {
+                if (dir == p.ax_k && p.psiK) psiList(p, dir, pl, startPt, nDir, dirMax, psi[0]);
+                gridList(p, dir, p.ax_k, pl, grid[0]);
+            }
+        };
+        init(p.lnMn[0], 0, false, 0, p.T[0], p.lnMn[0]);
+        init(p.lnPl[0], 0, true, D.lx - 2, p.T[0], p.lnPl[0]);
+        init(p.lnMn[1], 1, false, 0, p.T[1], p.lnMn[1]);
+        init(p.lnPl[1], 1, true, D.ly - 2, p.T[1], p.lnPl[1]);
+        init(p.lnMn[2], 2, false, 0, p.T[2], p.lnMn[2]);
+        init(p.lnPl[2], 2, true, D.lz - 2, p.T[2], p.lnPl[2]);
+        hasPsi[0] = p.psiK;
+        hasPsi[1] = p.psiJ;
+        for (int t = 0; t < 2; ++t) {
+            dbBase[t] = 0.0;
+            dbPsi[t] = 0.0;
+            if (!grid[t].empty()) {
+                dbPsi[t] = grid[t][0].Db;
+            }
+        }
+        lnMnOut[comp] = p.lnMn;
+        lnPlOut[comp] = p.lnPl;
+    }
+    std::array<int, 3> lnMnOut[6], lnPlOut[6];
+
+    // ---- update lists (parallelFDTDField.hpp:628-856) ----
+    enum ListKind { L_NONE = 0, L_U = 1, L_D = 2 };
+
+    void buildComp(int comp) {
+        CompPlan& cp = P.comp[comp];
+        const bool E = comp < 3;
+        const int i = comp % 3;
+        const int jc = (i + 1) % 3, kc = (i + 2) % 3;
+        const int other = E ? 3 : 0;
+        const bool gridJ = P.comp[other + jc].present;
+        const bool gridK = P.comp[other + kc].present;
+        std::array<int, 3> fieldEnd = {0, 0, 0};
+        if (E) fieldEnd[i] = 1;
+        else {
+            fieldEnd = {1, 1, 1};
+            fieldEnd[i] = 0;
+        }
+        const Field3<int>& ph = phys[comp];
+        const Field3<double>& ep = epsRel[comp];
+        const double dj = d[jc], dk = d[kc];
+        const bool twoD = (D.lz == 1);
+
+        // CPML lists for this component
+        std::vector<PsiEntry> psi[2];
+        std::vector<GridEntry> grid[2];
+        double dbBase[2], dbPsi[2];
+        bool hasPsi[2] = {false, false};
+        buildPml(comp, gridJ, gridK, psi, grid, dbBase, dbPsi, hasPsi);
+        const std::array<int, 3> lnMn = lnMnOut[comp], lnPl = lnPlOut[comp];
+
+        // initializeList ranges
+        std::array<int, 3> mn = {1, 1, twoD ? 0 : 1};
+        std::array<int, 3> mx = {D.lx - 1 - fieldEnd[0], D.ly - 1, twoD ? 1 : D.lz - 1 - fieldEnd[2]};
+        mx[1] -= fieldEnd[1];
+
+        // per-cell list membership
+        std::vector<uint8_t> curlKind(static_cast<std::size_t>(D.cells()), L_NONE);
+        std::vector<uint8_t> lorFlag(static_cast<std::size_t>(D.cells()), 0);
+        std::vector<uint8_t> ordipFlag(static_cast<std::size_t>(D.cells()), 0);
+
+        auto classify = [&](std::array<int, 3> a, std::array<int, 3> b, bool includeU, bool finalFill) {
+            for (int jj = a[1]; jj < b[1]; ++jj)
+                for (int kk = a[2]; kk < b[2]; ++kk)
+                    for (int ii = a[0]; ii < b[0]; ++ii) {
+                        int o = ph.at(ii, jj, kk);
+                        if (o < 0) throw InputError("update list reaches a border cell");
+                        const Object& ob = objs[o];
+                        std::size_t id = static_cast<std::size_t>(D.idx(ii, jj, kk));
+                        bool orDipCell = ob.orDip && (E && ob.gamma.size() > 0);
+                        bool uCell = includeU && ((!E) || (E && ob.gamma.size() < 1 && !ob.ML));
+                        if (finalFill) {
+                            if (!orDipCell && uCell) curlKind[id] = L_U;
+                            else curlKind[id] = L_D;
+                        } else {
+                            if (orDipCell) ordipFlag[id] = 1;
+                            else if (!uCell) lorFlag[id] = 1;
+                        }
+                    }
+        };
+        // getBlasLists
+        bool pmlMat = (E && matInPML);
+        int xl = pmlMat ? lnMn[0] : 0, xr = pmlMat ? lnPl[0] : 0;
+        if (xr != 0) xr -= fieldEnd[0];
+        int yb = pmlMat ? lnMn[1] : 0, yt = pmlMat ? lnPl[1] : 0;
+        if (yt != 0) yt -= fieldEnd[1];
+        bool threeBoth = D.threeD;
+        int zb = (threeBoth && pmlMat) ? lnPl[2] : 0, zf = (threeBoth && pmlMat) ? lnMn[2] : 0;
+        if (zf != 0) zf -= fieldEnd[2];
+        bool incPML = !matInPML;
+        classify({mn[0], mn[1], mn[2]}, {mx[0], mn[1] + yb, mx[2]}, incPML, false);
+        classify({mn[0], mx[1] - yt, mn[2]}, {mx[0], mx[1], mx[2]}, incPML, false);
+        classify({mn[0], mn[1] + yb, mn[2]}, {mx[0], mx[1] - yt, mn[2] + zb}, incPML, false);
+        classify({mn[0], mn[1] + yb, mx[2] - zf}, {mx[0], mx[1] - yt, mx[2]}, incPML, false);
+        classify({mn[0], mn[1] + yb, mn[2] + zb}, {mn[0] + xl, mx[1] - yt, mx[2] - zf}, incPML, false);
+        classify({mx[0] - xr, mn[1] + yb, mn[2] + zb}, {mx[0], mx[1] - yt, mx[2] - zf}, incPML, false);
+        classify({mn[0] + xl, mn[1] + yb, mn[2] + zb}, {mx[0] - xr, mx[1] - yt, mx[2] - zf}, true, false);
+        std::array<int, 3> fmn = mn, fmx = mx;
+        fmn[0] += lnMn[0];
+        fmx[0] -= lnPl[0];
+        if (lnPl[0] != 0) fmx[0] += fieldEnd[0];
+        fmn[1] += lnMn[1];
+        fmx[1] -= lnPl[1];
+        if (lnPl[1] != 0) fmx[1] += fieldEnd[1];
+        fmn[2] += lnPl[2];  // lnz_back() returns the plus-side thickness
+        fmx[2] -= lnMn[2];  // lnz_front() returns the minus-side thickness
+        if (lnMn[2] != 0) fmx[2] += fieldEnd[2];
+        classify(fmn, fmx, true, true);
+
+        // term geometry: J uses grid_j (derivative along k), K uses grid_k (derivative along j)
+        TermPlan* tp = cp.term;
+        const int sgn = E ? -1 : 1;
+        for (int t = 0; t < 2; ++t) {
+            TermPlan& T = tp[t];
+            T.present = (t == 0) ? gridJ : gridK;
+            T.field = other + ((t == 0) ? jc : kc);
+            T.axis = (t == 0) ? kc : jc;
+            std::array<int, 3> o = {0, 0, 0};
+            o[T.axis] = sgn;
+            if (twoD && T.axis == 2) {
+                T.present = false;
+            }
+            T.off = o[0] + static_cast<long long>(D.lx) * (o[2] + static_cast<long long>(D.lz) * o[1]);
+            T.hasPsi = hasPsi[t];
+            T.dbpsi = dbPsi[t];
+            int L = lnv(T.axis);
+            T.kprof.assign(L, 0.0);
+            T.b.assign(L, 0.0);
+            T.cpsi.assign(L, 0.0);
+        }
+
+        // literal per-cell accumulation of every list (for the check) and compression
+        const std::size_t N = static_cast<std::size_t>(D.cells());
+        std::vector<double> coef[2] = {std::vector<double>(N, 0.0), std::vector<double>(N, 0.0)};
+        std::vector<uint8_t> npsi[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
+        std::vector<uint8_t> psiUpd[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
+        std::vector<uint8_t> nplain[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
+        std::vector<uint8_t> kflag[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
+        std::vector<double> kval[2] = {std::vector<double>(N, 0.0), std::vector<double>(N, 0.0)};
+        auto coordOf = [&](long long id, int ax) {
+            long long x = id % D.lx;
+            long long r = id / D.lx;
+            long long z = r % D.lz;
+            long long y = r / D.lz;
+            return static_cast<int>(ax == 0 ? x : (ax == 1 ? y : z));
+        };
+        for (int t = 0; t < 2; ++t) {
+            TermPlan& T = tp[t];
+            double base = 0.0;
+            for (auto& e : grid[t]) {
+                for (int q = 0; q < e.n; ++q) {
+                    long long id = e.ind + q * e.stride;
+                    if (e.indOff + q * e.stride - id != T.off) throw InputError("CPML offset does not match the curl offset");
+                    coef[t][id] += e.DbField;
+                    npsi[t][id] += 1;
+                    if (e.slab == T.axis) {
+                        if (kflag[t][id]) throw UnsupportedError("overlapping CPML slabs along one axis");
+                        kflag[t][id] = 1;
+                        kval[t][id] = e.DbField;
+                        int a = coordOf(id, T.axis);
+                        if (T.kprof[a] != 0.0 && T.kprof[a] != e.DbField)
+                            throw UnsupportedError("CPML coefficient is not a function of the normal coordinate");
+                        T.kprof[a] = e.DbField;
+                    } else {
+                        double db = e.DbField;
+                        if (base == 0.0) base = db;
+                        if (db != base) throw UnsupportedError("CPML transverse coefficient varies");
+                        nplain[t][id] += 1;
+                    }
+                }
+            }
+            T.db = base;
+            for (auto& e : psi[t]) {
+                for (int q = 0; q < e.n; ++q) {
+                    long long id = e.ind + q * e.stride;
+                    if (e.indOff + q * e.stride - id != T.off) throw InputError("psi offset does not match the curl offset");
+                    if (psiUpd[t][id]) throw UnsupportedError("a psi cell is updated twice");
+                    psiUpd[t][id] = 1;
+                    int a = e.normCoord;
+                    if ((T.b[a] != 0.0 || T.cpsi[a] != 0.0) && (T.b[a] != e.b || T.cpsi[a] != e.c))
+                        throw UnsupportedError("psi coefficients are not a function of the normal coordinate");
+                    T.b[a] = e.b;
+                    T.cpsi[a] = e.c;
+                }
+            }
+            if (!T.hasPsi) {
+                std::fill(npsi[t].begin(), npsi[t].end(), 0);
+            }
+        }
+
+        // build classes
+        cp.present = true;
+        cp.isE = E;
+        std::map<std::vector<double>, int> index;  // key -> class id
+        cp.code.assign(N, 0);
+        cp.classes.clear();
+        {
+            ClassInfo none;
+            cp.classes.push_back(none);
+            std::vector<double> key(16, 0.0);
+            index[key] = 0;
+        }
+        bool anyD = false;
+        for (int y = 0; y < D.ly; ++y)
+            for (int z = 0; z < D.lz; ++z)
+                for (int x = 0; x < D.lx; ++x) {
+                    std::size_t id = static_cast<std::size_t>(D.idx(x, y, z));
+                    ClassInfo c;
+                    int o = ph.at(x, y, z);
+                    c.obj = (o < 0) ? 0 : o;
+                    double cellEps = ep.at(x, y, z);
+                    uint8_t kind = curlKind[id];
+                    bool pmlCell = false;
+                    for (int t = 0; t < 2; ++t) pmlCell = pmlCell || npsi[t][id] > 0 || (coef[t][id] != 0.0);
+                    if (kind == L_U || kind == L_D) {
+                        double em = (kind == L_U) ? cellEps : 1.0;
+                        double pref1 = -1.0 * dt / (em * dj), pref2 = -1.0 * dt / (em * dk);
+                        if (tp[0].present) c.cint[0] = pref2;
+                        if (tp[1].present) c.cint[1] = -pref1;
+                        c.toD = (kind == L_D) ? 1 : 0;
+                    }
+                    if (pmlCell) {
+                        uint8_t pmlToD = (E && matInPML) ? 1 : 0;
+                        if (kind != L_NONE && c.toD != pmlToD)
+                            throw UnsupportedError("a cell's interior and CPML updates target different fields");
+                        c.toD = pmlToD;
+                    }
+                    c.lor = lorFlag[id];
+                    c.ordip = ordipFlag[id];
+                    if (c.lor || c.ordip) c.eps = cellEps;
+                    if (c.toD || c.lor || c.ordip) anyD = true;
+                    for (int t = 0; t < 2; ++t) {
+                        if (!tp[t].present) {
+                            if (coef[t][id] != 0.0 || npsi[t][id] || psiUpd[t][id])
+                                throw InputError("CPML term without a neighbour field");
+                            continue;
+                        }
+                        c.nplain[t] = nplain[t][id];
+                        c.kflag[t] = kflag[t][id];
+                        c.npsi[t] = npsi[t][id];
+                        c.psiUpd[t] = psiUpd[t][id];
+                    }
+                    std::vector<double> key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
+                                               c.cint[0], c.cint[1], double(c.nplain[0]), double(c.nplain[1]),
+                                               double(c.kflag[0]), double(c.kflag[1]), double(c.npsi[0]),
+                                               double(c.npsi[1]), double(c.psiUpd[0]), double(c.psiUpd[1]), 0.0};
+                    if (!(c.lor || c.ordip)) key[4] = 1.0, c.eps = 1.0;
+                    if (!c.lor) key[3] = 0.0, c.obj = 0;
+                    auto it = index.find(key);
+                    int cid;
+                    if (it == index.end()) {
+                        cid = static_cast<int>(cp.classes.size());
+                        if (cid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
+                        cp.classes.push_back(c);
+                        index[key] = cid;
+                    } else {
+                        cid = it->second;
+                    }
+                    cp.code[id] = static_cast<uint8_t>(cid);
+                    // check the compressed CPML coefficient against the literal sum
+                    for (int t = 0; t < 2; ++t) {
+                        if (!tp[t].present) continue;
+                        int a = (t == 0) ? 0 : 0;
+                        a = coordOf(static_cast<long long>(id), tp[t].axis);
+                        double comp = c.nplain[t] * tp[t].db + (c.kflag[t] ? tp[t].kprof[a] : 0.0);
+                        double lit = coef[t][id];
+                        if (std::abs(comp - lit) > 1e-14 * std::max(1.0, std::abs(lit)) * std::abs(dt))
+                            throw UnsupportedError("compressed CPML coefficient differs from the list sum");
+                    }
+                }
+        cp.hasD = anyD;
+        int np = 0;
+        for (auto& o : objs) np = std::max(np, static_cast<int>(o.gamma.size()));
+        cp.nPoles = (E && P.disp) ? np : 0;
+    }
+
+    void build() {
+        P.in = in;
+        objs = in.objects;
+        d = in.d;
+        dt = in.dt;
+        P.dt = dt;
+        for (int q = 0; q < 3; ++q) nvec[q] = static_cast<int>(std::floor(in.size[q] / d[q] + 0.5)) + 1;
+        for (auto& o : objs) o.setUpConsts(dt);
+        D.nx = nvec[0];
+        D.ny = nvec[1];
+        D.nz = nvec[2];
+        D.threeD = in.size[2] != 0;
+        D.lx = nvec[0] + 2;
+        D.ly = nvec[1] + 2;
+        D.lz = D.threeD ? nvec[2] + 2 : 1;
+        P.dims = D;
+        P.nSteps = in.nSteps();
+        P.tcur.resize(static_cast<std::size_t>(P.nSteps) + 1);
+        double t = 0.0;
+        for (int s = 0; s <= P.nSteps; ++s) {
+            P.tcur[s] = t;
+            t += dt;
+        }
+        setupPhys(6, true, {0.0, 0.0, 0.0}, {0, 0, 0});
+        setupPhys(0, true, {0.5, 0.0, 0.0}, {1, 0, 0});
+        setupPhys(1, true, {0.0, 0.5, 0.0}, {0, 1, 0});
+        setupPhys(2, true, {0.0, 0.0, 0.5}, {0, 0, 1});
+        setupPhys(3, false, {0.0, 0.5, 0.5}, {0, 1, 1});
+        setupPhys(4, false, {0.5, 0.0, 0.5}, {1, 0, 1});
+        setupPhys(5, false, {0.5, 0.5, 0.0}, {1, 1, 0});
+        scanPML();
+        bool disp = false;
+        for (auto& o : objs)
+            if (o.gamma.size() > 0 || o.ML || o.epsInf > 1.0) disp = true;
+        if (matInPML) disp = true;
+        P.disp = disp;
+        P.dielectricMatInPML = matInPML;
+        bool te = D.threeD || in.pol == Pol::HZ || in.pol == Pol::EX || in.pol == Pol::EY;
+        bool tm = D.threeD || in.pol == Pol::EZ || in.pol == Pol::HX || in.pol == Pol::HY;
+        if (te) P.comp[EX].present = P.comp[EY].present = P.comp[HZ].present = true;
+        if (tm) P.comp[HX].present = P.comp[HY].present = P.comp[EZ].present = true;
+        for (auto& o : objs)
+            if (o.orDip && o.gamma.size() > 0)
+                throw UnsupportedError("oriented-dipole (anisotropic) poles are not supported by this build");
+        // the reference's list order: TE (Hz, Ex, Ey) then TM (Ez, Hx, Hy)
+        const int order[6] = {HZ, EX, EY, EZ, HX, HY};
+        bool present[6];
+        for (int c = 0; c < 6; ++c) present[c] = P.comp[c].present;
+        for (int c : order)
+            if (present[c]) buildComp(c);
+        for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
+        P.alpha.clear();
+        P.xi.clear();
+        P.gamma.clear();
+        for (auto& o : objs) {
+            P.alpha.push_back(o.alpha);
+            P.xi.push_back(o.xi);
+            P.gamma.push_back(o.gamma);
+        }
+        P.in.objects = objs;
+        buildSources();
+        buildDetectors();
+        buildFluxes();
+    }
+
+    // ---- sources (parallelSourceNormal.hpp:60-150, parallelSourceNormal.cpp:15-37) ----
+    void buildSources() {
+        for (auto& s : in.sources) {
+            SourcePlan sp;
+            int comp = EX;
+            switch (s.pol) {
+                case Pol::EX: comp = EX; break;
+                case Pol::EY: comp = EY; break;
+                case Pol::EZ: comp = EZ; break;
+                case Pol::HX: comp = HX; break;
+                case Pol::HY: comp = HY; break;
+                case Pol::HZ: comp = HZ; break;
+                default: throw UnsupportedError("source polarisation");
+            }
+            if (!P.comp[comp].present) throw InputError("a source acts on a field that this polarisation does not have");
+            sp.comp = comp;
+            std::array<int, 3> lloc, lsz = {0, 0, 0};
+            bool inside = true;
+            for (int ii = 0; ii < 3; ++ii) {
+                int ln = lnv(ii);
+                if (s.loc[ii] >= 0 && s.loc[ii] < ln - 2) lloc[ii] = s.loc[ii] + 1;
+                else if (s.loc[ii] < 0 && s.loc[ii] + s.sz[ii] > 0) lloc[ii] = 1;
+                else lloc[ii] = -1;
+            }
+            if (D.lz == 1) lloc[2] = 0;
+            if (lloc[0] == -1 || lloc[1] == -1 || lloc[2] == -1) inside = false;
+            if (inside) {
+                for (int ii = 0; ii < 3; ++ii) {
+                    int ln = lnv(ii);
+                    lsz[ii] = (s.sz[ii] + s.loc[ii] > ln - 2) ? ln - lloc[ii] - 1 : s.loc[ii] + s.sz[ii] - (lloc[ii] - 1);
+                }
+                if (D.lz == 1) lsz[2] = 1;
+                for (int z = 0; z < lsz[2]; ++z)
+                    for (int y = 0; y < lsz[1]; ++y)
+                        for (int x = 0; x < lsz[0]; ++x) sp.cells.push_back(D.idx(lloc[0] + x, lloc[1] + y, lloc[2] + z));
+            }
+            sp.value.resize(static_cast<std::size_t>(P.nSteps));
+            for (int st = 0; st < P.nSteps; ++st) {
+                cplx v = 0.0;
+                for (auto& pul : s.pulses) v += pul.value(P.tcur[st]);
+                sp.value[st] = dt * std::real(v);
+            }
+            P.sources.push_back(std::move(sp));
+        }
+    }
+
+    // ---- time-domain detectors (parallelDTC.hpp:40-120, parallelStorageDTC.hpp) ----
+    void buildDetectors() {
+        for (auto& ds : in.detectors) {
+            DetectorPlan dp;
+            dp.spec = ds;
+            dp.sz = ds.sz;
+            dp.timeInt = static_cast<int>(std::floor(ds.timeInt / dt));
+            if (dp.timeInt == 0) throw InputError("The time step of a detector is less than the main grid or set to 0.");
+            std::vector<std::pair<int, std::array<int, 3>>> flds;
+            auto need = [&](int c) {
+                if (!P.comp[c].present) throw InputError("DTC TYPE IS NOT DEFINED for this polarisation");
+            };
+            switch (ds.type) {
+                case DtcType::EX: need(EX); flds.push_back({EX, {0, 0, 0}}); break;
+                case DtcType::EY: need(EY); flds.push_back({EY, {0, 0, 0}}); break;
+                case DtcType::EZ: need(EZ); flds.push_back({EZ, {0, 0, 0}}); break;
+                case DtcType::HX: need(HX); flds.push_back({HX, {0, 0, 0}}); break;
+                case DtcType::HY: need(HY); flds.push_back({HY, {0, 0, 0}}); break;
+                case DtcType::HZ: need(HZ); flds.push_back({HZ, {0, 0, 0}}); break;
+                case DtcType::DX: case DtcType::DY: case DtcType::DZ: {
+                    int c = static_cast<int>(ds.type) - static_cast<int>(DtcType::DX);
+                    if (!P.comp[c].present || !P.disp) throw InputError("D detector without a D field");
+                    flds.push_back({6 + c, {0, 0, 0}});
+                    break;
+                }
+                case DtcType::EPOW:
+                case DtcType::HPOW: {
+                    bool e = ds.type == DtcType::EPOW;
+                    bool h2 = P.comp[HZ].present, e2 = P.comp[EZ].present;
+                    if (h2 && e2) {
+                        if (e) flds = {{EX, {-1, 0, 0}}, {EY, {0, -1, 0}}, {EZ, {0, 0, -1}}};
+                        else flds = {{HX, {1, 0, 0}}, {HY, {0, 1, 0}}, {HZ, {0, 0, 1}}};
+                    } else if (h2) {
+                        if (e) flds = {{EX, {-1, 0, 0}}, {EY, {0, -1, 0}}};
+                        else flds = {{HZ, {0, 0, 0}}};
+                    } else {
+                        if (e) flds = {{EZ, {0, 0, 0}}};
+                        else flds = {{HX, {1, 0, 0}}, {HY, {0, 1, 0}}};
+                    }
+                    break;
+                }
+                default: throw UnsupportedError("detector type needs polarisation or magnetic fields");
+            }
+            // conversions
+            for (int ii = 0; ii < 3; ++ii) {
+                int gn = gnv(ii);
+                dp.realLoc[ii] = d[ii] * (ds.loc[ii] - (gn - 1 * 2 - gn % 2) / 2);
+            }
+            if (ds.SI) {
+                dp.tConv *= in.a / kSpeedOfLight;
+                for (auto& r : dp.realLoc) r *= in.a;
+                dp.convFactor = (in.I0 / in.a);
+                if (ds.type == DtcType::EX || ds.type == DtcType::EY || ds.type == DtcType::EZ)
+                    dp.convFactor /= kEps0 * kSpeedOfLight;
+                for (auto& r : dp.realLoc) r *= in.a;
+            }
+            dp.power = (ds.type == DtcType::EPOW || ds.type == DtcType::HPOW);
+            if (dp.power) dp.convFactor *= dp.convFactor;
+            for (auto& f : flds) {
+                DetectorPlan::Field F;
+                F.comp = f.first;
+                F.off = f.second;
+                std::array<int, 3> loc = ds.loc, sz = ds.sz;
+                for (int oo = 0; oo < 3; ++oo) {
+                    sz[oo] += (1 + std::abs(F.off[oo])) / 2;
+                    loc[oo] -= (1 - F.off[oo]) / 2;
+                }
+                F.outSz = sz;
+                F.cells.assign(static_cast<std::size_t>(sz[0]) * sz[1] * sz[2], -1);
+                std::array<int, 3> ll, ls;
+                bool inside = true;
+                for (int ii = 0; ii < 3; ++ii) {
+                    int ln = lnv(ii);
+                    if (loc[ii] >= 0 && loc[ii] < ln - 2) ll[ii] = loc[ii] + 1;
+                    else if (loc[ii] == -1) ll[ii] = 0;
+                    else if (loc[ii] < 0 && loc[ii] + sz[ii] > 0) ll[ii] = 1;
+                    else ll[ii] = -1;
+                }
+                if (D.lz == 1) ll[2] = 0;
+                for (int ii = 0; ii < 3; ++ii)
+                    if (ll[ii] == -1) inside = false;
+                if (inside) {
+                    for (int ii = 0; ii < 3; ++ii) {
+                        int ln = lnv(ii);
+                        ls[ii] = (sz[ii] + loc[ii] > ln - 2) ? ln - ll[ii] - 1 : loc[ii] + sz[ii] - (ll[ii] - 1);
+                    }
+                    if (D.lz == 1) ls[2] = 1;
+                    std::array<int, 3> lo = {ll[0] - 1 - loc[0], ll[1] - 1 - loc[1], (D.lz == 1) ? 0 : ll[2] - 1 - loc[2]};
+                    for (int y = 0; y < ls[1]; ++y)
+                        for (int z = 0; z < ls[2]; ++z)
+                            for (int x = 0; x < ls[0]; ++x) {
+                                int ox = lo[0] + x, oy = lo[1] + y, oz = lo[2] + z;
+                                if (ox < 0 || oy < 0 || oz < 0 || ox >= sz[0] || oy >= sz[1] || oz >= sz[2]) continue;
+                                F.cells[static_cast<std::size_t>(ox + sz[0] * (oz + sz[2] * oy))] =
+                                    D.idx(ll[0] + x, ll[1] + y, ll[2] + z);
+                            }
+                }
+                dp.fields.push_back(std::move(F));
+            }
+            if (ds.cls == DtcClass::TXT) {
+                // the text writer loops over the first field's enlarged box and reads box+offset
+                const auto& F0 = dp.fields[0];
+                for (auto& F : dp.fields)
+                    for (int q = 0; q < 3; ++q)
+                        if (F0.outSz[q] - 1 + std::abs(F.off[q]) >= F.outSz[q])
+                            throw UnsupportedError("text detector of a staggered power field reads past its box (the reference aborts)");
+            }
+            P.detectors.push_back(std::move(dp));
+        }
+    }
+
+    // ---- DFT flux (parallelFlux.hpp:80-140, parallelFlux.cpp:13-70,338-542,
+    //      parallelStorageFreqDTC.hpp:120-240) ----
+    FreqStore makeStore(int comp, int propDir, std::array<int, 3> loc, std::array<int, 3> sz, int nfreq) {
+        FreqStore st;
+        st.comp = comp;
+        st.loc = loc;
+        st.sz = sz;
+        st.propDir = propDir;
+        std::array<int, 3> ll;
+        for (int ii = 0; ii < 3; ++ii) {
+            int ln = lnv(ii);
+            if (loc[ii] >= 0 && loc[ii] < ln - 2) ll[ii] = loc[ii] + 1;
+            else if (loc[ii] == -1) ll[ii] = 0;
+            else if (loc[ii] < 0 && loc[ii] + sz[ii] > 0) ll[ii] = 1;
+            else ll[ii] = -1;
+        }
+        if (D.lz == 1) ll[2] = 0;
+        if (ll[0] == -1 || ll[1] == -1 || ll[2] == -1) {
+            st.outN = {0, 0, 0};
+            return st;
+        }
+        auto lsz = [&](int ind, int localLoc) {
+            int ln = lnv(ind);
+            return (sz[ind] + loc[ind] > ln - 2) ? ln - localLoc - 1 : loc[ind] + sz[ind] - (localLoc - 1);
+        };
+        std::array<int, 3> insz = {0, 0, 0}, add = {0, 0, 0};
+        long long stride = 1;
+        if (propDir == 0) {
+            stride = D.lx;
+            insz[2] = lsz(0, ll[0]);
+            if (D.lz == 1) {
+                insz[0] = lsz(1, ll[1]);
+                insz[1] = 1;
+                add = {0, 0, 1};
+            } else {
+                insz[0] = lsz(2, ll[2]);
+                insz[1] = lsz(1, ll[1]);
+                add = {0, 1, 0};
+            }
+        } else if (propDir == 1) {
+            stride = 1;
+            insz[0] = lsz(0, ll[0]);
+            insz[1] = (D.lz == 1) ? 1 : lsz(2, ll[2]);
+            insz[2] = lsz(1, ll[1]);
+            add = {0, 0, 1};
+        } else {
+            stride = 1;
+            insz[0] = lsz(0, ll[0]);
+            insz[1] = lsz(1, ll[1]);
+            insz[2] = lsz(2, ll[2]);
+            add = {0, 1, 0};
+        }
+        st.inSz = insz;
+        st.outN = {nfreq, insz[1], insz[0]};
+        for (int ii = 0; ii < insz[1]; ++ii) {
+            long long base = D.idx(ll[0] + ii * add[0], ll[1] + ii * add[1], ll[2] + ii * add[2]);
+            for (int p = 0; p < insz[0]; ++p) st.cells.push_back(base + p * stride);
+        }
+        return st;
+    }
+
+    void buildFluxes() {
+        for (auto& fs : in.fluxes) {
+            FluxPlan fp;
+            fp.spec = fs;
+            const std::vector<double>& fl = fs.freqList;
+            const int nfreq = static_cast<int>(fl.size());
+            fp.dt = dt * static_cast<double>(fs.timeInt);
+            fp.fluxConv = fs.weight;
+            bool eq = (fl.size() > 1 && fl[1] - fl[0] == fl[2] - fl[1]);
+            if (fl.size() < 3) throw UnsupportedError("flux regions need at least three frequencies (the reference reads freqList[2])");
+            fp.dOmg = eq ? fl[1] - fl[0] : 0.0;
+            fp.dLam = eq ? 0.0 : 1.0 / fl[1] - 1.0 / fl[0];
+            if (fs.SI) {
+                fp.freqConv = kSpeedOfLight / in.a;
+                double cv = in.I0 / in.a * in.I0 / (kEps0 * in.a * kSpeedOfLight);
+                fp.fluxConv = cv;
+                for (auto& v : fp.incdConv) v = cv;
+            }
+            fp.real3D = P.comp[EZ].present && P.comp[HZ].present;
+            fp.freqConv /= (M_PI * 2.0);
+            // faces
+            std::vector<std::pair<int, bool>> faces;
+            const auto& sz = fs.sz;
+            if (!fp.real3D) {
+                if (sz[0] > 1 && sz[1] > 1) faces = {{1, false}, {1, true}, {0, false}, {0, true}};
+                else if (sz[0] == 1 && (D.lx != 3)) faces = {{0, true}};
+                else faces = {{1, true}};
+            } else {
+                if (sz[0] > 1 && sz[1] > 1 && sz[2] > 1) faces = {{0, true}, {0, false}, {1, true}, {1, false}, {2, true}, {2, false}};
+                else if (sz[0] == 1) faces = {{0, true}};
+                else if (sz[1] == 1) faces = {{1, true}};
+                else if (sz[2] == 1) faces = {{2, true}};
+            }
+            for (auto& fc : faces) makeFace(fp, fc.first, fc.second, nfreq);
+            long long off = 0;
+            for (auto& st : fp.stores) {
+                st.accOffset = off;
+                off += static_cast<long long>(st.cells.size());
+            }
+            fp.npts = off;
+            P.fluxes.push_back(std::move(fp));
+        }
+    }
+
+    void makeFace(FluxPlan& fp, int dir, bool pl, int nfreq) {
+        FluxFace f;
+        const auto& loc_ = fp.spec.loc;
+        const auto& sz_ = fp.spec.sz;
+        int Ej, Ek, Hj, Hk;
+        std::array<int, 3> sz;
+        if (dir == 0) {
+            Ej = EY; Hj = HY; Ek = EZ; Hk = HZ;
+            bool z1 = (P.comp[Ej].present && D.lz == 1) || (P.comp[Ek].present && D.lz == 1);
+            if (z1) { f.cor = 1; f.transCor1 = 2; f.transCor2 = 0; }
+            else { f.cor = 2; f.transCor1 = 1; f.transCor2 = 0; }
+            f.corI = 0; f.corJ = 1; f.corK = 2;
+            sz = {1, sz_[1], sz_[2]};
+        } else if (dir == 1) {
+            Ej = EZ; Hj = HZ; Ek = EX; Hk = HX;
+            f.cor = 0; f.transCor1 = 2; f.transCor2 = 1;
+            f.corI = 1; f.corJ = 2; f.corK = 0;
+            sz = {sz_[0], 1, sz_[2]};
+        } else {
+            Ej = EX; Hj = HX; Ek = EY; Hk = HY;
+            f.cor = 0; f.transCor1 = 1; f.transCor2 = 2;
+            f.corI = 2; f.corJ = 0; f.corK = 1;
+            sz = {sz_[0], sz_[1], 1};
+        }
+        std::array<int, 3> loc = loc_;
+        if (pl) loc[f.transCor2] = loc_[f.transCor2] + sz_[f.transCor2] - 1;
+        std::array<int, 3> locOff = loc;
+        f.sz = sz[f.cor] * sz[f.transCor1];
+        f.faceSz = sz;
+        auto add = [&](std::vector<int>& v, int comp, std::array<int, 3> l, std::array<int, 3> s) {
+            v.push_back(static_cast<int>(fp.stores.size()));
+            fp.stores.push_back(makeStore(comp, dir, l, s, nfreq));
+        };
+        bool e2 = P.comp[EZ].present, h2 = P.comp[HZ].present;
+        if (e2 && h2) {
+            std::array<int, 3> szOff = sz;
+            locOff[f.corK] -= 1;
+            szOff[f.corK] += 1;
+            add(f.Ek, Ek, locOff, szOff);
+            add(f.Hj, Hj, locOff, szOff);
+            locOff[f.corI] -= 1;
+            add(f.Hj, Hj, locOff, szOff);
+            locOff[f.corK] += 1;
+            szOff[f.corK] -= 1;
+            locOff[f.corJ] -= 1;
+            szOff[f.corJ] += 1;
+            add(f.Hk, Hk, locOff, szOff);
+            locOff[f.corI] += 1;
+            add(f.Hk, Hk, locOff, szOff);
+            add(f.Ej, Ej, locOff, szOff);
+        } else if (e2) {
+            if (P.comp[Ek].present) {
+                locOff[f.corI] += -1;
+                add(f.Ek, Ek, loc, sz);
+                add(f.Hj, Hj, loc, sz);
+                add(f.Hj, Hj, locOff, sz);
+            } else {
+                locOff[f.corI] += -1;
+                add(f.Ej, Ej, loc, sz);
+                add(f.Hk, Hk, loc, sz);
+                add(f.Hk, Hk, locOff, sz);
+            }
+        } else {
+            if (P.comp[Ej].present) {
+                locOff[f.corI] += 1;
+                add(f.Ej, Ej, loc, sz);
+                add(f.Hk, Hk, loc, sz);
+                add(f.Ej, Ej, locOff, sz);
+            } else {
+                locOff[f.corI] += 1;
+                add(f.Ek, Ek, loc, sz);
+                add(f.Hj, Hj, loc, sz);
+                add(f.Ek, Ek, locOff, sz);
+            }
+        }
+        f.weight = pl ? 1.0 : -1.0;
+        bool any = false;
+        for (auto* v : {&f.Ej, &f.Ek, &f.Hj, &f.Hk})
+            for (int s : *v)
+                if (fp.stores[s].outN[0] != 0) any = true;
+        if (!any) throw InputError("One of the flux surfaces is outside the FDTD cell.");
+        fp.faces.push_back(f);
+    }
+};
+
+}  // namespace
+
+Plan build_plan(const Inputs& in) {
+    Plan P;
+    Builder b(in, P);
+    b.build();
+    // incident-flux normalisation areas (parallelFlux.hpp:110-135)
+    for (auto& fp : P.fluxes) {
+        if (!fp.spec.crossSec) {
+            auto simps = [](int n, double d) {
+                std::vector<cplx> v(static_cast<std::size_t>(n), cplx(1.0, 0.0));
+                if (n == 1) return v[0] * d;
+                cplx r(0.0, 0.0);
+                if (n % 2 == 0) {
+                    for (int ii = 0; ii < (n - 2) / 2; ii++) r += d / 6.0 * (v[ii * 2] + 4.0 * v[ii * 2 + 1] + v[(ii + 1) * 2]);
+                    for (int ii = 1; ii < n / 2; ii++) r += d / 6.0 * (v[ii * 2 - 1] + 4.0 * v[ii * 2] + v[ii * 2 + 1]);
+                    r += d / 4.0 * (v[0] + v[1] + v[n - 1] + v[n - 2]);
+                } else {
+                    for (int ii = 0; ii < (n - 1) / 2; ii++) r += d / 3.0 * (v[ii * 2] + 4.0 * v[ii * 2 + 1] + v[(ii + 1) * 2]);
+                }
+                return r;
+            };
+            auto simps2DNorm = [&](int nx, int ny, double dx, double dy) {
+                std::vector<cplx> res(static_cast<std::size_t>(ny), 0.0);
+                for (auto& r : res) r = simps(nx, dx);
+                // simps over a non-constant vector: re-implement on the values
+                int n = ny;
+                double d = dy;
+                cplx r(0.0, 0.0);
+                if (n == 1) return res[0] * d;
+                if (n % 2 == 0) {
+                    for (int ii = 0; ii < (n - 2) / 2; ii++) r += d / 6.0 * (res[ii * 2] + 4.0 * res[ii * 2 + 1] + res[(ii + 1) * 2]);
+                    for (int ii = 1; ii < n / 2; ii++) r += d / 6.0 * (res[ii * 2 - 1] + 4.0 * res[ii * 2] + res[ii * 2 + 1]);
+                    r += d / 4.0 * (res[0] + res[1] + res[n - 1] + res[n - 2]);
+                } else {
+                    for (int ii = 0; ii < (n - 1) / 2; ii++) r += d / 3.0 * (res[ii * 2] + 4.0 * res[ii * 2 + 1] + res[(ii + 1) * 2]);
+                }
+                return r;
+            };
+            const auto& sz = fp.spec.sz;
+            const auto& d = P.in.d;
+            if (fp.real3D) {
+                fp.incdConv[0] *= (sz[2] > 1 && sz[1] > 1) ? std::real(simps2DNorm(sz[1], sz[2], d[1], d[2])) : 0.0;
+                fp.incdConv[1] *= (sz[0] > 1 && sz[2] > 1) ? std::real(simps2DNorm(sz[0], sz[2], d[0], d[2])) : 0.0;
+                fp.incdConv[2] *= (sz[0] > 1 && sz[1] > 1) ? std::real(simps2DNorm(sz[0], sz[1], d[0], d[1])) : 0.0;
+            } else {
+                fp.incdConv[1] *= std::real(simps(sz[0], d[0]));
+                fp.incdConv[0] *= std::real(simps(sz[1], d[1]));
+                fp.incdConv[2] = 0.0;
+            }
+        }
+    }
+    return P;
+}
+
+}  // namespace chiml
