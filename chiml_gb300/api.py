@@ -1,0 +1,167 @@
+"""ctypes binding of include/chiml_gpu.h."""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libchiml_gb300.so")
+
+PREC_FP64 = 0
+PREC_SPLIT = 1
+COMPONENTS = {"Ex": 0, "Ey": 1, "Ez": 2, "Hx": 3, "Hy": 4, "Hz": 5, "Dx": 6, "Dy": 7, "Dz": 8}
+_STATUS = {
+    0: "CHIML_OK",
+    1: "CHIML_E_INPUT",
+    2: "CHIML_E_UNSUPPORTED",
+    3: "CHIML_E_CUDA",
+    4: "CHIML_E_OOM",
+    5: "CHIML_E_NUMERIC",
+    6: "CHIML_E_TIMEOUT",
+    7: "CHIML_E_STATE",
+}
+
+
+class ChimlError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s: %s" % (_STATUS.get(status, status), message))
+        self.status = status
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int),
+        ("device", ctypes.c_int),
+        ("steps_per_graph", ctypes.c_int),
+        ("out_dir", ctypes.c_char_p),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("cells", ctypes.c_int64),
+        ("cells_physical", ctypes.c_int64),
+        ("nx", ctypes.c_int32),
+        ("ny", ctypes.c_int32),
+        ("nz", ctypes.c_int32),
+        ("steps_total", ctypes.c_int32),
+        ("steps_done", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("bytes_per_cell_update", ctypes.c_double),
+        ("device_bytes", ctypes.c_double),
+        ("kernels_per_step", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+EXPORTED = [
+    "chiml_create",
+    "chiml_step",
+    "chiml_sync",
+    "chiml_finalize",
+    "chiml_destroy",
+    "chiml_last_error",
+    "chiml_query",
+    "chiml_get_field",
+    "chiml_stream",
+]
+
+
+def load_library(path=None):
+    """Loads the engine library; raises FileNotFoundError when it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError("chiml_gb300 engine library not built: %s (run __graft_entry__.build())" % p)
+    lib = ctypes.CDLL(p)
+    lib.chiml_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(_Options), ctypes.POINTER(ctypes.c_void_p)]
+    lib.chiml_create.restype = ctypes.c_int
+    lib.chiml_step.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    lib.chiml_step.restype = ctypes.c_int
+    lib.chiml_sync.argtypes = [ctypes.c_void_p]
+    lib.chiml_sync.restype = ctypes.c_int
+    lib.chiml_finalize.argtypes = [ctypes.c_void_p]
+    lib.chiml_finalize.restype = ctypes.c_int
+    lib.chiml_destroy.argtypes = [ctypes.c_void_p]
+    lib.chiml_destroy.restype = None
+    lib.chiml_last_error.argtypes = [ctypes.c_void_p]
+    lib.chiml_last_error.restype = ctypes.c_char_p
+    lib.chiml_query.argtypes = [ctypes.c_void_p, ctypes.POINTER(Stats)]
+    lib.chiml_query.restype = ctypes.c_int
+    lib.chiml_get_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.chiml_get_field.restype = ctypes.c_int
+    lib.chiml_stream.argtypes = [ctypes.c_void_p]
+    lib.chiml_stream.restype = ctypes.c_void_p
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class Simulation:
+    """One simulation on one GPU, driven like chiML's main loop."""
+
+    def __init__(self, json_path, precision="fp64", device=0, steps_per_graph=0, out_dir=None):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        prec = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision]
+        self._out_dir = out_dir
+        opt = _Options(prec, device, steps_per_graph, out_dir.encode() if out_dir else None)
+        st = self._lib.chiml_create(os.fsencode(json_path), ctypes.byref(opt), ctypes.byref(self._h))
+        if st != 0:
+            raise ChimlError(st, self._lib.chiml_last_error(None).decode())
+
+    def _check(self, st):
+        if st != 0:
+            raise ChimlError(st, self._lib.chiml_last_error(self._h).decode())
+
+    def step(self, n=None):
+        """Advances n steps (all remaining when n is None)."""
+        if n is None:
+            s = self.stats()
+            n = s.steps_total - s.steps_done
+        self._check(self._lib.chiml_step(self._h, int(n)))
+
+    def sync(self):
+        self._check(self._lib.chiml_sync(self._h))
+
+    def finalize(self):
+        self._check(self._lib.chiml_finalize(self._h))
+
+    def stats(self):
+        s = Stats()
+        self._check(self._lib.chiml_query(self._h, ctypes.byref(s)))
+        return s
+
+    def field(self, name):
+        """Returns a field as an FP64 array shaped (y, z, x) (chiML's local layout, halo included)."""
+        s = self.stats()
+        lx, ly = s.nx + 2, s.ny + 2
+        lz = s.cells // (lx * ly)
+        out = np.empty(s.cells, dtype=np.float64)
+        self._check(self._lib.chiml_get_field(self._h, COMPONENTS[name], out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out.reshape(ly, lz, lx)
+
+    @property
+    def stream(self):
+        return self._lib.chiml_stream(self._h)
+
+    def close(self):
+        if self._h:
+            self._lib.chiml_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

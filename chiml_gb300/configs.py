@@ -1,0 +1,138 @@
+"""Input generators for the benchmark configurations, in chiML's JSON schema.
+
+Each function returns a dict ready for ``write_json``; lengths are in units of
+``a`` (100 nm), time in a/c, following the input conventions of chiML's reader
+(INPUTS/parallelInputs.cpp). Random geometry is drawn from a seeded PCG64
+generator (seed 20261203 + config id) so every run sees the same objects.
+``scale`` shrinks a configuration for parity tests (fewer cells, same physics).
+"""
+import json
+import math
+
+import numpy as np
+
+A = 1e-7                 # length unit (m)
+C0 = 2.9979245e8         # speed of light, as the reference defines it
+T_UNIT = A / C0          # one time unit in seconds
+SEED0 = 20261203
+
+
+def ev2fdtd(ev):
+    """Photon energy in eV -> frequency in c/a (parallelInputs.cpp:1182-1185)."""
+    return ev / 4.135666e-15 * A / C0
+
+
+def _tlim(steps, dt):
+    # ceil(tLim / dt) == steps for any rounding of the quotient
+    return (steps - 0.5) * dt
+
+
+def _obj(shape, loc, **kw):
+    o = {"shape": shape, "loc": list(loc), "unit_vectors": [], "Basis_Set": []}
+    o.update(kw)
+    return o
+
+
+def _gauss(fcen, fwidth, cutoff, t0, amp=1.0):
+    return {"profile": "gaussian", "Field_Intensity": amp, "fcen": fcen, "fwidth": fwidth, "cutoff": cutoff, "t_0": t0}
+
+
+def drude_lorentz_pols(wp_ev, poles):
+    """Custom-material poles from (strength, width_eV, centre_eV) triples; centre 0 = Drude.
+
+    Mirrors getMetal (parallelInputs.cpp:1187-1221): sigma = f (wp / Omega)^2 with
+    Omega = 1e-20 eV for a Drude term; the JSON gamma / omega are the FDTD-unit
+    values that the reader multiplies by pi and 2 pi.
+    """
+    wp = ev2fdtd(wp_ev)
+    out = []
+    for f, width_ev, centre_ev in poles:
+        om = ev2fdtd(centre_ev if centre_ev != 0.0 else 1.0e-20)
+        out.append({"gamma": ev2fdtd(width_ev), "omega": om, "sigma_p": f * (wp / om) ** 2})
+    return out
+
+
+def config1(n=400, pml=20, steps=4000, radius_cells=50, src_gap_cells=60, ndtc=8, nfreq=100):
+    """2-D TMz (Ez, Hx, Hy), dielectric disk eps=2.25, Ez point source, 8 point detectors, flux line."""
+    dx = 0.05
+    dt = dx / 2.0
+    size = (n - 1) * dx
+    r = radius_cells * dx
+    width = 2e-15 / T_UNIT
+    t0 = 6e-15 / T_UNIT
+    src_x = -(r + src_gap_cells * dx)
+    dets = []
+    for k in range(ndtc):
+        ang = 2 * math.pi * k / ndtc
+        rr = r + 0.35 * (size / 2 - pml * dx - r)
+        p = [round(rr * math.cos(ang) / dx) * dx, round(rr * math.sin(ang) / dx) * dx, 0.0]
+        dets.append({"loc": p, "size": [0.0, 0.0, 0.0], "type": "Ez", "fname": "out/c1_pt%d" % k,
+                     "dtc_class": "txt", "SI": False, "Time_Interval": dt})
+    flux_x = round((size / 2 - pml * dx - 4 * dx) / dx) * dx
+    flux_h = round((size - 2 * pml * dx - 10 * dx) / dx) * dx
+    return {
+        "CompCell": {"size": [size, size, 0.0], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
+                     "a": A, "pol": "Ez", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
+        "PML": {"thickness": [pml * dx, pml * dx, 0.0], "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
+        "SourceList": [{"pol": "Ez", "loc": [round(src_x / dx) * dx, 0.0, 0.0], "size": [0.0, 0.0, 0.0],
+                        "PulseList": [_gauss(A / 500e-9, 1.0 / width, 5.0, t0)]}],
+        "TFSF": [],
+        "ObjectList": [_obj("sphere", [0.0, 0.0, 0.0], radius=r, material="custom", eps=2.25, pols=[])],
+        "DetectorList": dets,
+        "FluxList": [{"name": "out/c1_flux", "loc": [flux_x, 0.0, 0.0], "size": [0.0, flux_h, 0.0],
+                      "lamL": 4.0, "lamR": 7.0, "nfreq": nfreq, "SI": False}],
+    }
+
+
+def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal_radius_cells=30):
+    """3-D dispersive scene: seeded ellipsoids, a Drude + 2 Lorentz metal sphere, a plane Ex
+    source sheet and a DFT flux box."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dx = 0.05
+    dt = 0.5 * dx / math.sqrt(3.0)
+    size = (n - 1) * dx
+    half = size / 2
+    inner = half - (pml + 6) * dx
+    objs = []
+    for _ in range(nell):
+        semi = rng.uniform(10, 40, size=3) * dx * (n / 256.0)
+        eps_o = float(rng.uniform(1.5, 4.0))
+        rng.uniform(1.5, 4.0)              # eps_e: the uniaxial part needs oriented-dipole poles
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        lim = np.maximum(inner - semi.max(), 0.0)
+        c = rng.uniform(-lim, lim, size=3)
+        u0 = axis
+        tmp = np.array([1.0, 0.0, 0.0]) if abs(axis[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        u1 = np.cross(u0, tmp)
+        u1 /= np.linalg.norm(u1)
+        u2 = np.cross(u0, u1)
+        objs.append(_obj("ellipsoid", [float(v) for v in c], size=[float(2 * s) for s in semi], material="custom",
+                         eps=eps_o, pols=[],
+                         unit_vectors=[{"uvec": [float(v) for v in u]} for u in (u0, u1, u2)]))
+    rm = metal_radius_cells * dx * (n / 256.0)
+    objs.append(_obj("sphere", [0.0, 0.0, 0.0], radius=rm, material="custom", eps=6.0,
+                     pols=drude_lorentz_pols(9.0, [(1.0, 0.07, 0.0), (1.0, 0.4, 2.6), (0.5, 0.8, 3.5)])))
+    src_z = -(half - (pml + 3) * dx)
+    sheet = size - 2 * (pml + 1) * dx
+    fb = 2 * (half - (pml + 5) * dx)
+    width = 5e-15 / T_UNIT
+    return {
+        "CompCell": {"size": [size, size, size], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
+                     "a": A, "pol": "Ex", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
+        "PML": {"thickness": [pml * dx] * 3, "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
+        "SourceList": [{"pol": "Ex", "loc": [0.0, 0.0, round(src_z / dx) * dx], "size": [sheet, sheet, 0.0],
+                        "PulseList": [_gauss(A / 550e-9, 1.0 / width, 4.0, 3 * width)]}],
+        "TFSF": [],
+        "ObjectList": objs,
+        "DetectorList": [{"loc": [0.0, 0.0, round((half - (pml + 8) * dx) / dx) * dx], "size": [0.0, 0.0, 0.0],
+                          "type": "Ex", "fname": "out/c2_pt", "dtc_class": "txt", "SI": False, "Time_Interval": dt}],
+        "FluxList": [{"name": "out/c2_flux", "loc": [0.0, 0.0, 0.0], "size": [fb, fb, fb],
+                      "lamL": 4.0, "lamR": 7.0, "nfreq": nfreq, "SI": False}],
+    }
+
+
+def write_json(cfg, path):
+    with open(path, "w") as f:
+        json.dump(cfg, f, indent=1)
+    return path

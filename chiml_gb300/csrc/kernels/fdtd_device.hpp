@@ -1,0 +1,114 @@
+// Device-side descriptors of the time-step kernels, shared by the kernel
+// translation unit (fdtd_kernels.cu) and the host engine (engine.cpp).
+// Plain structs of device pointers and sizes; passed to kernels by value.
+#pragma once
+
+#include <cstdint>
+
+namespace chiml {
+namespace dev {
+
+constexpr int kMaxPoles = 8;
+
+// One cell class of a component (the compressed update lists, see plan.hpp).
+template <typename T>
+struct Class {
+    T cint[2];       // interior curl coefficients of terms J, K
+    T epsInv;        // 1 / eps_inf      (D -> E)
+    T negEpsInv;     // -1 / eps_inf     (D -> E)
+    int32_t obj;     // object whose Lorentz poles apply
+    uint8_t toD;     // curl and CPML terms update D
+    uint8_t lor;     // Lorentz P update before, D -> E after
+    uint8_t nplain[2];
+    uint8_t kflag[2];
+    uint8_t npsi[2];
+    uint8_t psiUpd[2];
+    uint8_t pad[2];
+};
+
+template <typename T>
+struct Comp {
+    T* U;                  // field component
+    T* D;                  // D component (E components of dispersive runs)
+    const uint8_t* code;   // per-cell class code
+    const Class<T>* cls;   // class table
+    int present;
+    int nPoles;
+    T* P[kMaxPoles];
+    T* Pprev[kMaxPoles];
+    // neighbour terms J (uses grid_j) and K (uses grid_k)
+    int tpresent[2];
+    int axis[2];
+    int hasPsi[2];
+    long long off[2];
+    const T* G[2];
+    T* psi[2];
+    const T* kprof[2];
+    const T* b[2];
+    const T* cpsi[2];
+    T db[2];
+    T dbpsi[2];
+};
+
+template <typename T>
+struct Pass {
+    Comp<T> c[3];
+    int lx, ly, lz;
+    const int* poleStart;   // per object: first pole in the coefficient arrays
+    const int* poleCount;   // per object: number of poles
+    const T* alpha;
+    const T* xi;
+    const T* gamma;
+};
+
+template <typename T>
+struct Fields {
+    T* f[9];  // Ex,Ey,Ez,Hx,Hy,Hz,Dx,Dy,Dz (null where absent)
+};
+
+struct SourceTable {
+    int n;                    // source cells
+    const int* comp;          // per cell: component
+    const long long* cell;    // per cell: grid index
+    const int* src;           // per cell: source id
+    const double* value;      // [src * nSteps + step]
+    int nSteps;
+};
+
+struct RecordTable {
+    int n;                      // gathered values per event, summed over detectors
+    const int* det;             // per entry: detector id
+    const int* comp;            // per entry: component (0..8)
+    const long long* cell;      // per entry: grid index or -1
+    const long long* outIndex;  // per entry: index inside the detector event
+    const int* timeInt;         // per detector
+    const long long* nvals;     // per detector: values per event
+    const long long* recBase;   // per detector: offset of event 0 in rec
+    const int* nEvents;         // per detector
+    double* rec;
+};
+
+struct DftTable {
+    long long npts;
+    int nfreq;
+    int timeInt;
+    const int* comp;           // per point
+    const long long* cell;     // per point
+    const double* phasor;      // [(step * nfreq + f) * 2 + {0: cos, 1: -sin}]
+    double* re;                // [pt * nfreq + f]
+    double* im;
+};
+
+// Launchers (fdtd_kernels.cu). All run on the given stream.
+template <typename T>
+void launch_pass(const Pass<T>& p, bool ePass, void* stream);
+template <typename T>
+void launch_sources(const SourceTable& s, const Fields<T>& f, const int* step, void* stream);
+template <typename T>
+void launch_record(const RecordTable& r, const Fields<T>& f, const int* step, void* stream);
+template <typename T>
+void launch_dft(const DftTable& d, const Fields<T>& f, const int* step, void* stream);
+void launch_increment(int* step, void* stream);
+
+}  // namespace dev
+}  // namespace chiml

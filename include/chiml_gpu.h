@@ -1,0 +1,95 @@
+/* chiml_gpu.h - C ABI of the GB300 time-step engine for chiML inputs.
+ *
+ * The boundary replaces the C++ class interface that chiML's driver uses:
+ *   parallelFDTDFieldReal(parallelProgramInputs&, mpiInterface)  FDTD_MANAGER/parallelFDTDField.hpp:1793
+ *   void step()                                                   FDTD_MANAGER/parallelFDTDField.hpp:1228
+ *   final outputs (flux, detectors)                               src/main.cpp:67-118
+ * A caller mirrors main.cpp: create from the JSON input, step ceil(tLim/dt)
+ * times (main.cpp:54), finalize (writes the same files), destroy.
+ *
+ * Errors are integer status codes; no C++ exception crosses this boundary.
+ * One handle owns one CUDA stream and all of its device memory; handles are
+ * independent and each must be used from one host thread at a time.
+ */
+#ifndef CHIML_GPU_H
+#define CHIML_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct chiml_sim chiml_sim;
+
+typedef enum chiml_status {
+    CHIML_OK = 0,
+    CHIML_E_INPUT = 1,       /* malformed or inconsistent input (the reference throws std::logic_error) */
+    CHIML_E_UNSUPPORTED = 2, /* a feature outside this engine (magnetic/chiral media, PBC, TFSF, ...) */
+    CHIML_E_CUDA = 3,        /* a CUDA runtime error */
+    CHIML_E_OOM = 4,         /* device memory exhausted */
+    CHIML_E_NUMERIC = 5,     /* a NaN or Inf reached a monitored field value */
+    CHIML_E_TIMEOUT = 6,     /* a bounded device wait gave up */
+    CHIML_E_STATE = 7        /* call out of order (e.g. step after finalize) */
+} chiml_status;
+
+typedef enum chiml_precision {
+    CHIML_PREC_FP64 = 0,  /* every field, coefficient and accumulator in FP64 (the parity form) */
+    CHIML_PREC_SPLIT = 1  /* fields, CPML and polarisations in FP32; DFT accumulators in FP64 */
+} chiml_precision;
+
+typedef struct chiml_options {
+    int precision;        /* chiml_precision */
+    int device;           /* CUDA device ordinal */
+    int steps_per_graph;  /* steps captured per CUDA graph; 0 = launch kernels without graphs */
+    const char* out_dir;  /* directory that relative output names resolve against; NULL = current directory */
+} chiml_options;
+
+typedef struct chiml_stats {
+    int64_t cells;             /* grid cells including the halo */
+    int64_t cells_physical;    /* nx * ny * nz */
+    int32_t nx, ny, nz;
+    int32_t steps_total;       /* ceil(tLim / dt) */
+    int32_t steps_done;
+    int32_t precision;
+    double bytes_per_cell_update;  /* algorithmic HBM bytes per physical cell per step */
+    double device_bytes;           /* device memory held by the handle */
+    int32_t kernels_per_step;      /* kernel launches per step */
+    int32_t reserved;
+} chiml_stats;
+
+/* Reads the JSON input (chiML schema), builds the update plan and uploads it. */
+chiml_status chiml_create(const char* json_path, const chiml_options* opt, chiml_sim** out);
+
+/* Advances nsteps time steps (clamped to the steps left). Asynchronous with
+ * respect to the host only inside the call: it returns after the work is queued
+ * and checked for launch errors. */
+chiml_status chiml_step(chiml_sim* sim, int64_t nsteps);
+
+/* Waits for queued work. */
+chiml_status chiml_sync(chiml_sim* sim);
+
+/* Copies detector records and DFT accumulators to the host and writes the
+ * detector and flux files in chiML's formats. */
+chiml_status chiml_finalize(chiml_sim* sim);
+
+void chiml_destroy(chiml_sim* sim);
+
+/* Last error message of the handle; with sim == NULL, of the calling thread's last chiml_create. */
+const char* chiml_last_error(const chiml_sim* sim);
+
+chiml_status chiml_query(const chiml_sim* sim, chiml_stats* out);
+
+/* Copies one field to host memory as FP64, in chiML's local grid layout
+ * (x fastest, then z, then y, with a one-cell halo). comp: 0..2 Ex..Ez,
+ * 3..5 Hx..Hz, 6..8 Dx..Dz. out holds stats.cells doubles. */
+chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out);
+
+/* Device stream of the handle (a cudaStream_t), for callers that time kernels. */
+void* chiml_stream(chiml_sim* sim);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHIML_GPU_H */

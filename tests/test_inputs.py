@@ -1,0 +1,61 @@
+"""Host-side input handling: the reader's conversions and the rejection of unsupported features."""
+import copy
+import json
+import os
+
+import pytest
+
+from chiml_gb300 import configs
+from conftest import GOLDEN
+
+
+def _create(built_engine, cfg, tmp_path):
+    from chiml_gb300 import ChimlError, Simulation
+    p = str(tmp_path / "in.json")
+    configs.write_json(cfg, p)
+    with pytest.raises(ChimlError) as ei:
+        Simulation(p)
+    return ei.value
+
+
+def _base():
+    return configs.config1(n=40, pml=6, steps=10, radius_cells=5, src_gap_cells=5, ndtc=1, nfreq=4)
+
+
+@pytest.mark.parametrize("mutate,status", [
+    (lambda c: c["CompCell"].__setitem__("PBC", True), 2),
+    (lambda c: c["CompCell"].__setitem__("cplxFields", True), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("mu", 2.0), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("material", "Au"), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("shape", "torus"), 2),
+    (lambda c: c["DetectorList"][0].__setitem__("dtc_class", "bmp"), 2),
+    (lambda c: c["DetectorList"][0].__setitem__("type", "Mx"), 2),
+    (lambda c: c["CompCell"].__setitem__("dt", 1.0), 1),
+    (lambda c: c["CompCell"].__setitem__("pol", "Q"), 1),
+    (lambda c: c["ObjectList"][0].pop("Basis_Set"), 1),
+    (lambda c: c.pop("FluxList"), 1),
+])
+def test_rejections_are_reported_with_status(built_engine, tmp_path, mutate, status):
+    cfg = copy.deepcopy(_base())
+    mutate(cfg)
+    err = _create(built_engine, cfg, tmp_path)
+    assert err.status == status, str(err)
+
+
+def test_comments_are_stripped(built_oracle, tmp_path):
+    import oracle
+    src = open(os.path.join(GOLDEN, "c1_small", "in.json")).read().splitlines()
+    src.insert(1, "   // a comment line")
+    src[3] = src[3] + "   // trailing comment"
+    p = tmp_path / "in.json"
+    p.write_text("\n".join(src))
+    sim = oracle.OracleSim(str(p))
+    assert sim.steps_total == 300
+
+
+def test_step_count_is_ceil_of_tlim_over_dt(built_oracle, tmp_path):
+    import oracle
+    cfg = _base()
+    cfg["CompCell"]["tLim"] = 10.2 * cfg["CompCell"]["dt"]
+    p = configs.write_json(cfg, str(tmp_path / "in.json"))
+    assert oracle.OracleSim(p).steps_total == 11
