@@ -51,6 +51,11 @@ class Stats(ctypes.Structure):
         ("device_bytes", ctypes.c_double),
         ("kernels_per_step", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
+        ("bytes_h_pass", ctypes.c_double),
+        ("bytes_e_pass", ctypes.c_double),
+        ("bytes_dft", ctypes.c_double),
+        ("h2d_bytes", ctypes.c_double),
+        ("d2h_bytes", ctypes.c_double),
     ]
 
 
@@ -66,6 +71,7 @@ EXPORTED = [
     "chiml_query",
     "chiml_get_field",
     "chiml_stream",
+    "chiml_profile_steps",
 ]
 
 
@@ -96,6 +102,9 @@ def load_library(path=None):
     lib.chiml_get_field.restype = ctypes.c_int
     lib.chiml_stream.argtypes = [ctypes.c_void_p]
     lib.chiml_stream.restype = ctypes.c_void_p
+    lib.chiml_profile_steps.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_int)]
+    lib.chiml_profile_steps.restype = ctypes.c_int
     if path is None:
         _lib = lib
     return lib
@@ -144,6 +153,17 @@ class Simulation:
         out = np.empty(s.cells, dtype=np.float64)
         self._check(self._lib.chiml_get_field(self._h, COMPONENTS[name], out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out.reshape(ly, lz, lx)
+
+    def profile_steps(self, n):
+        """Runs n steps with per-kernel CUDA-event timing; returns {slot name: total ms}."""
+        ms = (ctypes.c_double * 64)()
+        ns = ctypes.c_int()
+        self._check(self._lib.chiml_profile_steps(self._h, int(n), ms, 64, ctypes.byref(ns)))
+        names = ["h_pass", "sources", "e_pass", "step_counter", "records"]
+        out = {}
+        for k in range(ns.value):
+            out[names[k] if k < len(names) else "dft%d" % (k - len(names))] = ms[k]
+        return out
 
     @property
     def stream(self):

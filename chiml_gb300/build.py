@@ -59,14 +59,14 @@ def build_engine(force=False):
     o = os.path.join(BUILD, "fdtd_kernels.o")
     jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu, "-o", o])
     objs.append(o)
-    cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-I" + os.path.join(CUDA_HOME, "include")]
+    cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-I" + os.path.join(CUDA_HOME, "include")]
     for f in ["engine.cpp"] + ["host/" + h for h in HOST_SRCS]:
         o = os.path.join(BUILD, os.path.basename(f).replace(".cpp", ".o"))
         jobs.append(cxx + ["-c", os.path.join(CSRC, f), "-o", o])
         objs.append(o)
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_run, jobs))
-    _run([NVCC] + ARCH + ["-shared", "-o", LIB_ENGINE] + objs)
+    _run([NVCC] + ARCH + ["-shared", "-o", LIB_ENGINE] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"])
     return LIB_ENGINE
 
 

@@ -24,6 +24,10 @@ namespace {
 
 thread_local std::string g_createError;
 
+struct DeviceStateError : public std::runtime_error {
+    explicit DeviceStateError(const std::string& w) : std::runtime_error(w) {}
+};
+
 struct CudaError : public std::runtime_error {
     cudaError_t code;
     CudaError(cudaError_t c, const std::string& w) : std::runtime_error(w), code(c) {}
@@ -67,6 +71,8 @@ struct SimBase {
     virtual void getField(int comp, double* out) = 0;
     virtual void fillStats(chiml_stats* s) const = 0;
     virtual cudaStream_t stream() const = 0;
+    virtual int profile(int nsteps, double* ms, int maxSlots) = 0;
+    virtual void checkDeviceErrors() = 0;
 };
 
 template <typename T>
@@ -74,7 +80,9 @@ class Sim : public SimBase {
 public:
     Sim(Plan&& plan, const chiml_options& opt) : P(std::move(plan)), opt_(opt) {
         ck(cudaSetDevice(opt.device), "cudaSetDevice");
-        ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+        // A blocking stream: ordered after the uploads and memsets that run on
+        // the legacy default stream.
+        ck(cudaStreamCreate(&stream_), "cudaStreamCreate");
         outDir_ = opt.out_dir ? opt.out_dir : "";
         upload();
     }
@@ -106,8 +114,16 @@ public:
         ck(cudaGetLastError(), "kernel launch");
     }
 
-    void finalize() override {
+    // Raises when a kernel recorded a bounds error (it skipped the cell instead of faulting).
+    void checkDeviceErrors() override {
         ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        unsigned int e = 0;
+        ck(cudaMemcpy(&e, dErr_, sizeof(e), cudaMemcpyDeviceToHost), "D2H error word");
+        if (e) throw DeviceStateError("device bounds check failed (code " + std::to_string(e) + ")");
+    }
+
+    void finalize() override {
+        checkDeviceErrors();
         RunRecord R;
         R.detectors.resize(P.detectors.size());
         std::vector<double> rec(recTotal_);
@@ -166,6 +182,50 @@ public:
         s->bytes_per_cell_update = bytesPerCell_;
         s->device_bytes = mem_.bytes;
         s->kernels_per_step = kernelsPerStep_;
+        s->bytes_h_pass = passBytes_[0];
+        s->bytes_e_pass = passBytes_[1];
+        s->bytes_dft = dftBytes_;
+        s->h2d_bytes = mem_.h2d;
+        s->d2h_bytes = d2h_;
+    }
+
+    int profile(int nsteps, double* ms, int maxSlots) override {
+        if (finalized_) throw std::logic_error("step after finalize");
+        const int nslots = 5 + static_cast<int>(dft_.size());
+        std::vector<cudaEvent_t> ev(static_cast<std::size_t>(nslots) + 1);
+        for (auto& e : ev) ck(cudaEventCreate(&e), "cudaEventCreate");
+        std::vector<double> acc(static_cast<std::size_t>(nslots), 0.0);
+        long long left = P.nSteps - stepsDone_;
+        if (nsteps > left) nsteps = static_cast<int>(left);
+        for (int st = 0; st < nsteps; ++st) {
+            void* s = stream_;
+            ck(cudaEventRecord(ev[0], stream_), "cudaEventRecord");
+            dev::launch_pass<T>(hPass_, false, s);
+            ck(cudaEventRecord(ev[1], stream_), "cudaEventRecord");
+            dev::launch_sources<T>(src_, fields_, dStep_, s);
+            ck(cudaEventRecord(ev[2], stream_), "cudaEventRecord");
+            dev::launch_pass<T>(ePass_, true, s);
+            ck(cudaEventRecord(ev[3], stream_), "cudaEventRecord");
+            dev::launch_increment(dStep_, s);
+            ck(cudaEventRecord(ev[4], stream_), "cudaEventRecord");
+            dev::launch_record<T>(recT_, fields_, dStep_, s);
+            ck(cudaEventRecord(ev[5], stream_), "cudaEventRecord");
+            for (std::size_t q = 0; q < dft_.size(); ++q) {
+                dev::launch_dft<T>(dft_[q], fields_, dStep_, s);
+                ck(cudaEventRecord(ev[6 + q], stream_), "cudaEventRecord");
+            }
+            ck(cudaEventSynchronize(ev[static_cast<std::size_t>(nslots)]), "cudaEventSynchronize");
+            for (int k = 0; k < nslots; ++k) {
+                float m = 0.f;
+                ck(cudaEventElapsedTime(&m, ev[k], ev[k + 1]), "cudaEventElapsedTime");
+                acc[k] += m;
+            }
+            ++stepsDone_;
+        }
+        for (auto& e : ev) cudaEventDestroy(e);
+        int n = std::min(nslots, maxSlots);
+        for (int k = 0; k < n; ++k) ms[k] = acc[k];
+        return n;
     }
 
     double h2dBytes() const { return mem_.h2d; }
@@ -187,10 +247,13 @@ private:
     std::size_t recTotal_ = 0;
     double* dRec_ = nullptr;
     int* dStep_ = nullptr;
+    unsigned int* dErr_ = nullptr;
     int stepsDone_ = 0;
     bool finalized_ = false;
     double d2h_ = 0;
     double bytesPerCell_ = 0;
+    double passBytes_[2] = {0, 0};
+    double dftBytes_ = 0;
     int kernelsPerStep_ = 0;
 
     void enqueueStep() {
@@ -212,7 +275,46 @@ private:
         cudaGraphDestroy(g);
     }
 
+    // Host-side bounds validation of every index the kernels will dereference.
+    void validatePlan() const {
+        const Dims& D = P.dims;
+        const long long N = D.cells();
+        for (int c = 0; c < 6; ++c) {
+            const CompPlan& cp = P.comp[c];
+            if (!cp.present) continue;
+            if (static_cast<long long>(cp.code.size()) != N) throw InputError("class code array size");
+            for (uint8_t k : cp.code)
+                if (k >= cp.classes.size()) throw InputError("class code outside the class table");
+            for (int t = 0; t < 2; ++t) {
+                const TermPlan& tp = cp.term[t];
+                if (!tp.present) continue;
+                int L = tp.axis == 0 ? D.lx : (tp.axis == 1 ? D.ly : D.lz);
+                if (static_cast<int>(tp.kprof.size()) != L || static_cast<int>(tp.b.size()) != L) throw InputError("profile size");
+                if (!P.comp[tp.field].present) throw InputError("neighbour field absent");
+            }
+            // every coded cell's neighbour stays inside the grid
+            for (long long i = 0; i < N; ++i) {
+                if (cp.code[i] == 0) continue;
+                for (int t = 0; t < 2; ++t)
+                    if (cp.term[t].present && (i + cp.term[t].off < 0 || i + cp.term[t].off >= N))
+                        throw InputError("stencil neighbour outside the grid");
+            }
+        }
+        for (auto& s : P.sources)
+            for (long long c : s.cells)
+                if (c < 0 || c >= N) throw InputError("source cell outside the grid");
+        for (auto& d : P.detectors)
+            for (auto& f : d.fields)
+                for (long long c : f.cells)
+                    if (c >= N) throw InputError("detector cell outside the grid");
+        for (auto& fp : P.fluxes)
+            for (auto& st : fp.stores)
+                for (long long c : st.cells)
+                    if (c < 0 || c >= N) throw InputError("flux cell outside the grid");
+    }
+
     void upload() {
+        validatePlan();
         const Dims& D = P.dims;
         const std::size_t N = static_cast<std::size_t>(D.cells());
         // fields
@@ -253,6 +355,7 @@ private:
             pass.alpha = dAl;
             pass.xi = dXi;
             pass.gamma = dGa;
+            pass.nObj = static_cast<int>(pCount.size());
             for (int ci = 0; ci < 3; ++ci) {
                 const int c = (half ? 0 : 3) + ci;
                 const CompPlan& cp = P.comp[c];
@@ -285,6 +388,7 @@ private:
                     if (k.lor && !cp.hasD) throw InputError("dispersive cell without a D field");
                 }
                 dc.cls = mem_.upload(cls);
+                dc.ncls = static_cast<int>(cls.size());
                 dc.nPoles = cp.nPoles;
                 if (cp.nPoles > dev::kMaxPoles) throw UnsupportedError("more than 8 Lorentz poles on one component");
                 for (int q = 0; q < cp.nPoles; ++q) {
@@ -400,6 +504,11 @@ private:
             dft_.push_back(d);
         }
         dStep_ = mem_.alloc<int>(1);
+        dErr_ = mem_.alloc<unsigned int>(1);
+        hPass_.err = dErr_;
+        ePass_.err = dErr_;
+        // every copy and memset above has landed before the first kernel runs
+        ck(cudaDeviceSynchronize(), "upload");
         kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + static_cast<int>(dft_.size());
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
@@ -407,31 +516,46 @@ private:
         ck(cudaStreamSynchronize(stream_), "initial samples");
     }
 
-    // Algorithmic HBM bytes per physical cell per step: each field array read
-    // and written once, one class byte per component, CPML psi and dispersive
-    // D/P arrays weighted by the fraction of cells that use them.
-    double algorithmicBytesPerCell() const {
+    // Algorithmic HBM bytes of the passes: every array a pass touches is read
+    // (and, if it is updated, written) once per launch -- the field components
+    // of the pass, the neighbour components it reads, one class byte per
+    // component and cell, and CPML psi, D and Lorentz P/P_prev only at the
+    // cells whose class uses them. Per-step bytes per physical cell are the sum
+    // of both passes over the physical cell count.
+    double algorithmicBytesPerCell() {
         const Dims& D = P.dims;
-        double phys = static_cast<double>(D.nx) * D.ny * D.nz;
-        double total = 0;
-        for (int c = 0; c < 6; ++c) {
-            const CompPlan& cp = P.comp[c];
-            if (!cp.present) continue;
-            total += phys * (2.0 * sizeof(T) + 1.0);
-            long long psiCells[2] = {0, 0}, dCells = 0;
-            std::vector<long long> classCount(cp.classes.size(), 0);
-            for (uint8_t k : cp.code) classCount[k]++;
-            for (std::size_t q = 0; q < cp.classes.size(); ++q) {
-                const ClassInfo& k = cp.classes[q];
-                for (int t = 0; t < 2; ++t)
-                    if (k.psiUpd[t]) psiCells[t] += classCount[q];
-                if (k.lor) dCells += classCount[q] * (2 + 4 * static_cast<long long>(P.alpha[k.obj].size()));
-                else if (k.toD) dCells += classCount[q] * 2;
+        const double phys = static_cast<double>(D.nx) * D.ny * D.nz;
+        const double cells = static_cast<double>(D.cells());
+        const double t = static_cast<double>(sizeof(T));
+        for (int half = 0; half < 2; ++half) {
+            double b = 0.0;
+            int own = 0, nbr = 0;
+            for (int ci = 0; ci < 3; ++ci) {
+                const int c = (half ? 0 : 3) + ci;
+                if (P.comp[c].present) ++own;
+                if (P.comp[(half ? 3 : 0) + ci].present) ++nbr;
             }
-            total += (psiCells[0] + psiCells[1]) * 2.0 * sizeof(T);
-            total += dCells * static_cast<double>(sizeof(T));
+            b += cells * (own * (2.0 * t + 1.0) + nbr * t);
+            for (int ci = 0; ci < 3; ++ci) {
+                const int c = (half ? 0 : 3) + ci;
+                const CompPlan& cp = P.comp[c];
+                if (!cp.present) continue;
+                std::vector<long long> count(cp.classes.size(), 0);
+                for (uint8_t k : cp.code) count[k]++;
+                for (std::size_t q = 0; q < cp.classes.size(); ++q) {
+                    const ClassInfo& k = cp.classes[q];
+                    for (int tt = 0; tt < 2; ++tt)
+                        if (k.psiUpd[tt] || k.npsi[tt]) b += count[q] * 2.0 * t;
+                    if (k.lor) b += count[q] * t * (2.0 + 4.0 * P.alpha[k.obj].size());
+                    else if (k.toD) b += count[q] * 2.0 * t;
+                }
+            }
+            passBytes_[half] = b;  // [0] H pass, [1] E pass
         }
-        return total / phys;
+        dftBytes_ = 0.0;
+        for (auto& fp : P.fluxes)
+            dftBytes_ += static_cast<double>(fp.npts) * (t + fp.spec.freqList.size() * 4.0 * sizeof(double));
+        return (passBytes_[0] + passBytes_[1]) / phys;
     }
 };
 
@@ -447,6 +571,7 @@ chiml_status status_of(const std::exception& e) {
     if (auto* c = dynamic_cast<const CudaError*>(&e))
         return c->code == cudaErrorMemoryAllocation ? CHIML_E_OOM : CHIML_E_CUDA;
     if (dynamic_cast<const std::bad_alloc*>(&e)) return CHIML_E_OOM;
+    if (dynamic_cast<const DeviceStateError*>(&e)) return CHIML_E_NUMERIC;
     if (dynamic_cast<const std::logic_error*>(&e)) return CHIML_E_STATE;
     return CHIML_E_INPUT;
 }
@@ -497,12 +622,13 @@ chiml_status chiml_step(chiml_sim* sim, int64_t nsteps) {
 
 chiml_status chiml_sync(chiml_sim* sim) {
     if (!sim) return CHIML_E_STATE;
-    cudaError_t e = cudaStreamSynchronize(sim->h.sim->stream());
-    if (e != cudaSuccess) {
-        sim->h.err = cudaGetErrorString(e);
-        return CHIML_E_CUDA;
+    try {
+        sim->h.sim->checkDeviceErrors();
+        return CHIML_OK;
+    } catch (const std::exception& e) {
+        sim->h.err = e.what();
+        return status_of(e);
     }
-    return CHIML_OK;
 }
 
 chiml_status chiml_finalize(chiml_sim* sim) {
@@ -541,5 +667,16 @@ chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out) {
 }
 
 void* chiml_stream(chiml_sim* sim) { return sim ? static_cast<void*>(sim->h.sim->stream()) : nullptr; }
+
+chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots) {
+    if (!sim || !ms_out || !nslots) return CHIML_E_STATE;
+    try {
+        *nslots = sim->h.sim->profile(nsteps, ms_out, max_slots);
+        return CHIML_OK;
+    } catch (const std::exception& e) {
+        sim->h.err = e.what();
+        return status_of(e);
+    }
+}
 
 }  // extern "C"

@@ -56,6 +56,62 @@ struct Builder {
 
     Builder(const Inputs& i, Plan& p) : in(i), P(p) {}
 
+    // Index range [lo, hi) per axis that contains every cell whose sample point can
+    // lie inside the object (isObj is only ever true within the object's extent).
+    // Radius of a sphere about o.loc that contains every point isObj accepts
+    // (with geo or geoML), or 1e300 when no finite bound is known.
+    double boundingRadius(const Object& o) const {
+        double r = 0.0;
+        switch (o.shape) {
+            case Shape::SPHERE: r = std::max(o.geoML[0], o.geo[0]); break;
+            case Shape::ELLIPSOID: r = 0.5 * std::max(std::max(std::abs(o.geoML[0]), std::abs(o.geoML[1])), std::abs(o.geoML[2])); break;
+            case Shape::BLOCK: r = 0.5 * std::sqrt(o.geoML[0] * o.geoML[0] + o.geoML[1] * o.geoML[1] + o.geoML[2] * o.geoML[2]); break;
+            case Shape::CYLINDER: r = std::sqrt(o.geoML[0] * o.geoML[0] + 0.25 * o.geoML[1] * o.geoML[1]); break;
+        }
+        r += 2.0 * std::max(std::max(d[0], d[1]), d[2]) + 1e-9 * std::abs(r);
+        if (!(r < 1e300)) return 1e300;
+        if (o.shape == Shape::ELLIPSOID && o.geo[2] == 0.0 && D.threeD) return 1e300;
+        if (o.shape != Shape::SPHERE)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    double dot = 0.0;
+                    for (int k = 0; k < 3; ++k) dot += o.coord[a * 3 + k] * o.coord[b * 3 + k];
+                    if (!(std::abs(dot - (a == b ? 1.0 : 0.0)) < 1e-9)) return 1e300;
+                }
+        return r;
+    }
+
+    void objectIndexBox(const Object& o, std::array<double, 3> offPt, int lo[3], int hi[3]) const {
+        double r = 0.0;
+        switch (o.shape) {
+            case Shape::SPHERE: r = o.geoML[0]; break;
+            case Shape::ELLIPSOID: r = 0.5 * std::max(std::max(std::abs(o.geoML[0]), std::abs(o.geoML[1])), std::abs(o.geoML[2])); break;
+            case Shape::BLOCK: r = 0.5 * std::sqrt(o.geoML[0] * o.geoML[0] + o.geoML[1] * o.geoML[1] + o.geoML[2] * o.geoML[2]); break;
+            case Shape::CYLINDER: r = std::sqrt(o.geoML[0] * o.geoML[0] + 0.25 * o.geoML[1] * o.geoML[1]); break;
+        }
+        if (!(r < 1e300)) r = 1e300;  // NaN or huge: no narrowing
+        if (o.shape != Shape::SPHERE) {
+            // the object-space distance equals the real-space one only for orthonormal axes
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    double dot = 0.0;
+                    for (int k = 0; k < 3; ++k) dot += o.coord[a * 3 + k] * o.coord[b * 3 + k];
+                    if (!(std::abs(dot - (a == b ? 1.0 : 0.0)) < 1e-9)) r = 1e300;
+                }
+        }
+        for (int q = 0; q < 3; ++q) {
+            const double pad = 2.0 * d[q] + 1e-9 * std::abs(r);
+            const double c0 = (nvec[q] - nvec[q] % 2) / 2.0 - offPt[q] + 1.0;  // index of the origin
+            if (d[q] <= 0 || r >= 1e300) {
+                lo[q] = -1;
+                hi[q] = 1 << 30;
+                continue;
+            }
+            lo[q] = static_cast<int>(std::floor((o.loc[q] - r - pad) / d[q] + c0)) - 1;
+            hi[q] = static_cast<int>(std::ceil((o.loc[q] + r + pad) / d[q] + c0)) + 2;
+        }
+    }
+
     // setupPhysFields, parallelFDTDField.hpp:867-947
     void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff) {
         Field3<int> ph(D, 0);
@@ -66,9 +122,17 @@ struct Builder {
         for (std::size_t oo = 1; oo < objs.size(); ++oo) {
             const Object& o = objs[oo];
             if (!(o.ML || o.gamma.size() > 0 || o.epsInf != 1.0)) continue;
-            for (int ii = 1; ii < D.lx - 1; ++ii)
-                for (int jj = 1; jj < D.ly - 1; ++jj)
-                    for (int kk = zmin; kk < zmax; ++kk) {
+            // Cells outside a generous bounding box of the object cannot pass isObj;
+            // the box only narrows the loops, the test itself is unchanged.
+            int lo[3], hi[3];
+            objectIndexBox(o, offPt, lo, hi);
+            const int i0 = std::max(1, lo[0]), i1 = std::min(D.lx - 1, hi[0]);
+            const int j0 = std::max(1, lo[1]), j1 = std::min(D.ly - 1, hi[1]);
+            const int k0 = twoD ? zmin : std::max(zmin, lo[2]), k1 = twoD ? zmax : std::min(zmax, hi[2]);
+#pragma omp parallel for schedule(dynamic, 4)
+            for (int jj = j0; jj < j1; ++jj)
+                for (int ii = i0; ii < i1; ++ii)
+                    for (int kk = k0; kk < k1; ++kk) {
                         std::array<double, 3> pt;
                         pt[0] = ((ii - 1) + offPt[0] + 0 - (nvec[0] - nvec[0] % 2) / 2.0) * d[0];
                         pt[1] = ((jj - 1) + offPt[1] + 0 - (nvec[1] - nvec[1] % 2) / 2.0) * d[1];
@@ -126,6 +190,12 @@ struct Builder {
                 const Object& o = objs[oo];
                 if (o.epsInf == 1.0 && o.gamma.size() < 1 && !o.ML) continue;
                 bool dielc = !(o.epsInf == 1.0 && o.gamma.size() < 1);
+                double rad = boundingRadius(o);
+                auto maybeIn = [&](const std::array<double, 3>& pt) {
+                    double s2 = 0.0;
+                    for (int q = 0; q < 3; ++q) s2 += (pt[q] - o.loc[q]) * (pt[q] - o.loc[q]);
+                    return s2 <= rad * rad;
+                };
                 for (int jj = mn[cj]; jj < mx[cj]; ++jj)
                     for (int kk = mn[ck]; kk < mx[ck]; ++kk) {
                         for (int pass = 0; pass < 2; ++pass) {
@@ -139,13 +209,13 @@ struct Builder {
                                 pt[cj] = static_cast<double>(jj) * d[cj];
                                 pt[ck] = static_cast<double>(kk) * d[ck];
                                 pt[0] += d[0] / 2.0;
-                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
                                 pt[1] += d[1] / 2.0;
                                 pt[0] -= d[0] / 2.0;
-                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
                                 pt[2] += d[2] / 2.0;
                                 pt[1] -= d[0] / 2.0;
-                                if (!matInPML && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
                                 pt[0] += d[2] / 2.0;
                             }
                         }
@@ -637,16 +707,23 @@ struct Builder {
         // build classes
         cp.present = true;
         cp.isE = E;
-        std::map<std::vector<double>, int> index;  // key -> class id
+        std::map<std::array<double, 16>, int> index;  // key -> class id
         cp.code.assign(N, 0);
         cp.classes.clear();
         {
+            // class 0: cells no list updates (the halo and staggered borders); the
+            // kernels skip them without touching any neighbour
             ClassInfo none;
             cp.classes.push_back(none);
-            std::vector<double> key(16, 0.0);
+            std::array<double, 16> key;
+            key.fill(0.0);
+            key[4] = 1.0;  // eps as normalised below for non-dispersive classes
             index[key] = 0;
         }
         bool anyD = false;
+        std::array<double, 16> lastKey;
+        lastKey.fill(-1.0);
+        int lastId = -1;
         for (int y = 0; y < D.ly; ++y)
             for (int z = 0; z < D.lz; ++z)
                 for (int x = 0; x < D.lx; ++x) {
@@ -686,14 +763,20 @@ struct Builder {
                         c.npsi[t] = npsi[t][id];
                         c.psiUpd[t] = psiUpd[t][id];
                     }
-                    std::vector<double> key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
+                    std::array<double, 16> key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
                                                c.cint[0], c.cint[1], double(c.nplain[0]), double(c.nplain[1]),
                                                double(c.kflag[0]), double(c.kflag[1]), double(c.npsi[0]),
                                                double(c.npsi[1]), double(c.psiUpd[0]), double(c.psiUpd[1]), 0.0};
                     if (!(c.lor || c.ordip)) key[4] = 1.0, c.eps = 1.0;
                     if (!c.lor) key[3] = 0.0, c.obj = 0;
-                    auto it = index.find(key);
                     int cid;
+                    if (key == lastKey) {
+                        cid = lastId;
+                        cp.code[id] = static_cast<uint8_t>(cid);
+                        goto check;
+                    }
+                    {
+                    auto it = index.find(key);
                     if (it == index.end()) {
                         cid = static_cast<int>(cp.classes.size());
                         if (cid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
@@ -702,7 +785,11 @@ struct Builder {
                     } else {
                         cid = it->second;
                     }
+                    }
+                    lastKey = key;
+                    lastId = cid;
                     cp.code[id] = static_cast<uint8_t>(cid);
+                check:
                     // check the compressed CPML coefficient against the literal sum
                     for (int t = 0; t < 2; ++t) {
                         if (!tp[t].present) continue;
@@ -714,6 +801,13 @@ struct Builder {
                             throw UnsupportedError("compressed CPML coefficient differs from the list sum");
                     }
                 }
+        for (std::size_t q = 1; q < cp.classes.size(); ++q) {
+            const ClassInfo& k = cp.classes[q];
+            bool acts = k.toD || k.lor || k.ordip;
+            for (int t = 0; t < 2; ++t)
+                acts = acts || k.cint[t] != 0.0 || k.nplain[t] || k.kflag[t] || k.npsi[t] || k.psiUpd[t];
+            if (!acts) throw InputError("internal: a cell class with no update");
+        }
         cp.hasD = anyD;
         int np = 0;
         for (auto& o : objs) np = std::max(np, static_cast<int>(o.gamma.size()));

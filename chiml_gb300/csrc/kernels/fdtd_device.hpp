@@ -32,6 +32,7 @@ struct Comp {
     T* D;                  // D component (E components of dispersive runs)
     const uint8_t* code;   // per-cell class code
     const Class<T>* cls;   // class table
+    int ncls;              // entries in cls
     int present;
     int nPoles;
     T* P[kMaxPoles];
@@ -59,7 +60,12 @@ struct Pass {
     const T* alpha;
     const T* xi;
     const T* gamma;
+    int nObj;
+    unsigned int* err;      // device error word (kErr* bits); the kernel skips the cell instead of faulting
 };
+
+constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class table
+constexpr unsigned int kErrPoleCount = 2u;   // a class asks for more poles than its component stores
 
 template <typename T>
 struct Fields {

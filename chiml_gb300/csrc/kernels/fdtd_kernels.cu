@@ -28,8 +28,16 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
         if (!c.present) continue;
         const uint8_t code = c.code[i];
         if (code == 0) continue;
+        if (code >= c.ncls) {
+            atomicOr(p.err, kErrClassCode);
+            continue;
+        }
         const Class<T> k = c.cls[code];
         if (EPASS && k.lor) {
+            if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
+                atomicOr(p.err, kErrPoleCount);
+                continue;
+            }
             const T e = c.U[i];
             const int s = p.poleStart[k.obj];
             const int n = p.poleCount[k.obj];
@@ -48,8 +56,10 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
         for (int t = 0; t < 2; ++t) {
             if (!c.tpresent[t]) continue;
             const int a = coord[c.axis[t]];
-            const T diff = c.G[t][i] - c.G[t][i + c.off[t]];
             const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? c.kprof[t][a] : T(0));
+            const bool psiTerm = c.hasPsi[t] && (k.psiUpd[t] || k.npsi[t]);
+            if (coef == T(0) && !psiTerm) continue;
+            const T diff = c.G[t][i] - c.G[t][i + c.off[t]];
             if (coef != T(0)) {
                 add += coef * diff;
                 any = true;

@@ -56,6 +56,11 @@ typedef struct chiml_stats {
     double device_bytes;           /* device memory held by the handle */
     int32_t kernels_per_step;      /* kernel launches per step */
     int32_t reserved;
+    double bytes_h_pass;           /* algorithmic HBM bytes of one H-pass launch */
+    double bytes_e_pass;           /* algorithmic HBM bytes of one E-pass launch */
+    double bytes_dft;              /* algorithmic HBM bytes of the DFT launches of one sampled step */
+    double h2d_bytes;              /* bytes copied host to device so far */
+    double d2h_bytes;              /* bytes copied device to host so far */
 } chiml_stats;
 
 /* Reads the JSON input (chiML schema), builds the update plan and uploads it. */
@@ -87,6 +92,13 @@ chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out);
 
 /* Device stream of the handle (a cudaStream_t), for callers that time kernels. */
 void* chiml_stream(chiml_sim* sim);
+
+/* Advances nsteps steps without graphs, timing every kernel launch with CUDA
+ * events on the handle's stream. ms_out[k] receives the summed milliseconds of
+ * kernel slot k: 0 H pass, 1 sources, 2 E pass, 3 step counter, 4 detector
+ * records, 5 + q DFT of flux region q. *nslots receives the number of slots
+ * written (at most max_slots). */
+chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
 #ifdef __cplusplus
 }

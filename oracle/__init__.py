@@ -38,6 +38,7 @@ def load():
         lib.chiml_oracle_destroy.argtypes = [ctypes.c_void_p]
         lib.chiml_oracle_run.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
         lib.chiml_oracle_run.restype = ctypes.c_double
+        lib.chiml_oracle_threads.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -86,6 +87,10 @@ class OracleSim:
             self.close()
         except Exception:
             pass
+
+
+def threads():
+    return load().chiml_oracle_threads()
 
 
 def run(json_path, out_dir, steps=-1):

@@ -97,6 +97,7 @@ struct OracleSim {
             }
             for (const FreqStore& s : fp.stores) {
                 const double* src = F[s.comp].data();
+#pragma omp parallel for schedule(static)
                 for (std::size_t p = 0; p < s.cells.size(); ++p) {
                     double v = src[s.cells[p]];
                     std::size_t base = static_cast<std::size_t>(s.accOffset + static_cast<long long>(p)) * nf;
@@ -118,10 +119,12 @@ struct OracleSim {
         double* Dc = (c < 3 && cp.hasD) ? Dd[c].data() : nullptr;
         const TermPlan* T = cp.term;
         const double* G[2] = {T[0].present ? F[T[0].field].data() : nullptr, T[1].present ? F[T[1].field].data() : nullptr};
+#pragma omp parallel for schedule(static)
         for (int y = 0; y < D.ly; ++y)
             for (int z = 0; z < D.lz; ++z)
                 for (int x = 0; x < D.lx; ++x) {
                     long long i = D.idx(x, y, z);
+                    if (cp.code[i] == 0) continue;
                     const ClassInfo& k = cp.classes[cp.code[i]];
                     int coord[3] = {x, y, z};
                     double add = 0.0;
@@ -130,6 +133,8 @@ struct OracleSim {
                         if (!T[t].present) continue;
                         int a = coord[T[t].axis];
                         double coef = k.cint[t] + k.nplain[t] * T[t].db + (k.kflag[t] ? T[t].kprof[a] : 0.0);
+                        bool psiTerm = T[t].hasPsi && (k.psiUpd[t] || k.npsi[t]);
+                        if (coef == 0.0 && !psiTerm) continue;
                         double diff = G[t][i] - G[t][i + T[t].off];
                         if (k.psiUpd[t]) {
                             double& ps = psi[c][t][i];
@@ -155,6 +160,7 @@ struct OracleSim {
         if (cp.nPoles == 0) return;
         const Dims& D = P.dims;
         const double* E = F[c].data();
+#pragma omp parallel for schedule(static)
         for (long long i = 0; i < D.cells(); ++i) {
             const ClassInfo& k = cp.classes[cp.code[i]];
             if (!k.lor) continue;
@@ -178,6 +184,7 @@ struct OracleSim {
         const Dims& D = P.dims;
         double* E = F[c].data();
         const double* Dc = Dd[c].data();
+#pragma omp parallel for schedule(static)
         for (long long i = 0; i < D.cells(); ++i) {
             const ClassInfo& k = cp.classes[cp.code[i]];
             if (!k.lor) continue;
@@ -230,6 +237,15 @@ void* chiml_oracle_create(const char* json_path) {
 }
 
 int chiml_oracle_steps_total(void* h) { return static_cast<OracleSim*>(h)->P.nSteps; }
+
+// Host threads the step loops use.
+int chiml_oracle_threads() {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
 
 long long chiml_oracle_cells(void* h) { return static_cast<OracleSim*>(h)->P.dims.cells(); }
 
