@@ -162,7 +162,11 @@ class Simulation:
         names = ["h_pass", "sources", "e_pass", "step_counter", "records"]
         out = {}
         for k in range(ns.value):
-            out[names[k] if k < len(names) else "dft%d" % (k - len(names))] = ms[k]
+            if k < len(names):
+                out[names[k]] = ms[k]
+            else:
+                q, r = divmod(k - len(names), 2)
+                out["dft%d_%s" % (q, "sample" if r == 0 else "fold")] = ms[k]
         return out
 
     @property

@@ -138,6 +138,14 @@ public:
                 R.detectors[k].emplace_back(b, b + nv);
             }
         }
+        // fold the samples of the last, partial block into the accumulators
+        for (std::size_t q = 0; q < dft_.size(); ++q) {
+            const dev::DftTable<T>& d = dft_[q];
+            const int samples = stepsDone_ / d.timeInt + 1;
+            const int pending = samples % d.K;
+            if (pending > 0) dev::launch_dft_fold<T>(d, dStep_, pending, samples - pending, stream_);
+        }
+        ck(cudaStreamSynchronize(stream_), "DFT flush");
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
             const FluxPlan& fp = P.fluxes[q];
             std::size_t n = static_cast<std::size_t>(fp.npts) * fp.spec.freqList.size();
@@ -191,7 +199,7 @@ public:
 
     int profile(int nsteps, double* ms, int maxSlots) override {
         if (finalized_) throw std::logic_error("step after finalize");
-        const int nslots = 5 + static_cast<int>(dft_.size());
+        const int nslots = 5 + 2 * static_cast<int>(dft_.size());
         std::vector<cudaEvent_t> ev(static_cast<std::size_t>(nslots) + 1);
         for (auto& e : ev) ck(cudaEventCreate(&e), "cudaEventCreate");
         std::vector<double> acc(static_cast<std::size_t>(nslots), 0.0);
@@ -211,8 +219,10 @@ public:
             dev::launch_record<T>(recT_, fields_, dStep_, s);
             ck(cudaEventRecord(ev[5], stream_), "cudaEventRecord");
             for (std::size_t q = 0; q < dft_.size(); ++q) {
-                dev::launch_dft<T>(dft_[q], fields_, dStep_, s);
-                ck(cudaEventRecord(ev[6 + q], stream_), "cudaEventRecord");
+                dev::launch_dft_sample<T>(dft_[q], fields_, dStep_, s);
+                ck(cudaEventRecord(ev[6 + 2 * q], stream_), "cudaEventRecord");
+                dev::launch_dft_fold<T>(dft_[q], dStep_, -1, 0, s);
+                ck(cudaEventRecord(ev[7 + 2 * q], stream_), "cudaEventRecord");
             }
             ck(cudaEventSynchronize(ev[static_cast<std::size_t>(nslots)]), "cudaEventSynchronize");
             for (int k = 0; k < nslots; ++k) {
@@ -242,7 +252,7 @@ private:
     dev::Fields<T> fields_{};
     dev::SourceTable src_{};
     dev::RecordTable recT_{};
-    std::vector<dev::DftTable> dft_;
+    std::vector<dev::DftTable<T>> dft_;
     std::vector<long long> recBase_;
     std::size_t recTotal_ = 0;
     double* dRec_ = nullptr;
@@ -263,7 +273,10 @@ private:
         dev::launch_pass<T>(ePass_, true, s);
         dev::launch_increment(dStep_, s);
         dev::launch_record<T>(recT_, fields_, dStep_, s);
-        for (auto& d : dft_) dev::launch_dft<T>(d, fields_, dStep_, s);
+        for (auto& d : dft_) {
+            dev::launch_dft_sample<T>(d, fields_, dStep_, s);
+            dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
+        }
     }
 
     void buildGraph(int K) {
@@ -475,30 +488,38 @@ private:
             dRec_ = mem_.alloc<double>(recTotal_);
             recT_.rec = dRec_;
         }
-        // DFT flux accumulators and phasor tables
+        // DFT flux: point tables, phasors per sample, ring of K samples, FP64 accumulators
         for (auto& fp : P.fluxes) {
-            dev::DftTable d{};
-            std::vector<int> comp;
-            std::vector<long long> cell;
+            dev::DftTable<T> d{};
+            std::vector<int> comp, cell;
             for (auto& st : fp.stores)
                 for (long long c : st.cells) {
+                    if (c > 0x7fffffffLL) throw UnsupportedError("grid too large for 32-bit flux point indices");
                     comp.push_back(st.comp);
-                    cell.push_back(c);
+                    cell.push_back(static_cast<int>(c));
                 }
             const int nf = static_cast<int>(fp.spec.freqList.size());
-            std::vector<double> ph(static_cast<std::size_t>(P.nSteps + 1) * nf * 2);
-            for (int s = 0; s <= P.nSteps; ++s)
+            const int ti = fp.spec.timeInt;
+            const int nSamples = P.nSteps / ti + 1;
+            std::vector<T> ph(static_cast<std::size_t>(nSamples) * nf * 2);
+            for (int n = 0; n < nSamples; ++n)
                 for (int f = 0; f < nf; ++f) {
-                    std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[s] * fp.spec.freqList[f]));
-                    ph[(static_cast<std::size_t>(s) * nf + f) * 2 + 0] = e.real();
-                    ph[(static_cast<std::size_t>(s) * nf + f) * 2 + 1] = e.imag();
+                    std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * fp.spec.freqList[f]));
+                    ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 0] = static_cast<T>(e.real());
+                    ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 1] = static_cast<T>(e.imag());
                 }
+            // samples per fold: as many as fit the fold kernel's shared memory (<= 64)
+            int K = 64;
+            while (K > 1 && (static_cast<std::size_t>(K) * nf * 2 + static_cast<std::size_t>(K) * 32) * sizeof(T) > 190 * 1024) K /= 2;
             d.npts = static_cast<long long>(cell.size());
             d.nfreq = nf;
-            d.timeInt = fp.spec.timeInt;
+            d.timeInt = ti;
+            d.K = K;
+            d.nSamples = nSamples;
             d.comp = mem_.upload(comp);
             d.cell = mem_.upload(cell);
             d.phasor = mem_.upload(ph);
+            d.ring = mem_.alloc<T>(cell.size() * static_cast<std::size_t>(K));
             d.re = mem_.alloc<double>(cell.size() * nf);
             d.im = mem_.alloc<double>(cell.size() * nf);
             dft_.push_back(d);
@@ -509,10 +530,10 @@ private:
         ePass_.err = dErr_;
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
-        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + static_cast<int>(dft_.size());
+        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size());
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
-        for (auto& d : dft_) dev::launch_dft<T>(d, fields_, dStep_, stream_);
+        for (auto& d : dft_) dev::launch_dft_sample<T>(d, fields_, dStep_, stream_);
         ck(cudaStreamSynchronize(stream_), "initial samples");
     }
 
@@ -552,9 +573,15 @@ private:
             }
             passBytes_[half] = b;  // [0] H pass, [1] E pass
         }
+        // DFT per sampled step: gather (index 4 B + component 4 B + value read + ring write)
+        // plus the fold's accumulator read-modify-write and ring read amortised over K
         dftBytes_ = 0.0;
-        for (auto& fp : P.fluxes)
-            dftBytes_ += static_cast<double>(fp.npts) * (t + fp.spec.freqList.size() * 4.0 * sizeof(double));
+        for (auto& fp : P.fluxes) {
+            int nf = static_cast<int>(fp.spec.freqList.size());
+            int K = 64;
+            while (K > 1 && (static_cast<std::size_t>(K) * nf * 2 + static_cast<std::size_t>(K) * 32) * sizeof(T) > 190 * 1024) K /= 2;
+            dftBytes_ += static_cast<double>(fp.npts) * (8.0 + 2.0 * t + t + nf * 4.0 * sizeof(double) / K);
+        }
         return (passBytes_[0] + passBytes_[1]) / phys;
     }
 };

@@ -94,14 +94,24 @@ struct RecordTable {
     double* rec;
 };
 
+// Time-blocked DFT of one flux region. Every sampled step gathers the field
+// value of each accumulated point into a ring of K samples; every K samples one
+// launch folds the ring into the FP64 accumulators:
+//   re[pt][f] += sum_k cos(w_f t_k) F_k[pt],  im[pt][f] += sum_k -sin(w_f t_k) F_k[pt]
+// which is the per-step update of parallelStorageFreqDTCReal::fieldIn
+// (DTC/parallelStorageFreqDTC.cpp:21-30) regrouped over K steps.
+template <typename T>
 struct DftTable {
     long long npts;
     int nfreq;
     int timeInt;
-    const int* comp;           // per point
-    const long long* cell;     // per point
-    const double* phasor;      // [(step * nfreq + f) * 2 + {0: cos, 1: -sin}]
-    double* re;                // [pt * nfreq + f]
+    int K;                      // samples per block
+    int nSamples;               // samples a full run takes (phasor rows)
+    const int* comp;            // per point
+    const int* cell;            // per point (grid index)
+    const T* phasor;            // [(sample * nfreq + f) * 2 + {0: cos, 1: -sin}]
+    T* ring;                    // [K][npts]
+    double* re;                 // [pt * nfreq + f]
     double* im;
 };
 
@@ -113,7 +123,12 @@ void launch_sources(const SourceTable& s, const Fields<T>& f, const int* step, v
 template <typename T>
 void launch_record(const RecordTable& r, const Fields<T>& f, const int* step, void* stream);
 template <typename T>
-void launch_dft(const DftTable& d, const Fields<T>& f, const int* step, void* stream);
+void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step, void* stream);
+// Folds the ring into the accumulators when the current sample completes a block
+// (flushCount < 0), or unconditionally folds the first flushCount ring slots,
+// taken as samples [firstSample, firstSample + flushCount) (flushCount > 0).
+template <typename T>
+void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream);
 void launch_increment(int* step, void* stream);
 
 }  // namespace dev

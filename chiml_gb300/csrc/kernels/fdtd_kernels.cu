@@ -92,13 +92,138 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
     }
 }
 
+// Marching form of the same update. A block covers a 32 (x) by BZ (z) tile of
+// one component and walks a chunk of CY planes along y, the slowest axis of the
+// layout. The neighbour along y is carried in a register from the previous
+// plane, so each plane loads it once instead of twice; the class table sits in
+// shared memory. Per cell the arithmetic is the same as k_pass.
+constexpr int kMarchBZ = 8;
+constexpr int kMarchCY = 16;
+
+template <typename T, bool EPASS>
+__global__ void __launch_bounds__(256) k_pass_march(const Pass<T> p) {
+    __shared__ Class<T> tab[256];
+    const int ci = blockIdx.z % 3;
+    const Comp<T>& c = p.c[ci];
+    if (!c.present) return;
+    for (int q = threadIdx.x + threadIdx.y * 32; q < c.ncls; q += 32 * kMarchBZ) tab[q] = c.cls[q];
+    __syncthreads();
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int z = blockIdx.y * kMarchBZ + threadIdx.y;
+    const int y0 = (blockIdx.z / 3) * kMarchCY;
+    if (x >= p.lx || z >= p.lz || y0 >= p.ly) return;
+    const long long plane = static_cast<long long>(p.lx) * p.lz;
+    const int y1 = min(y0 + kMarchCY, p.ly);
+    // y-carried neighbour: for the term whose offset is along y, G(i + off) of this
+    // plane is G(i) of the neighbouring plane, which the march visits in turn
+    int ty = -1;
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+        if (c.tpresent[t] && c.axis[t] == 1) ty = t;
+    const bool yUp = (ty >= 0) && c.off[ty] > 0;  // H: +y neighbour ; E: -y neighbour
+    long long i = x + static_cast<long long>(p.lx) * (z + static_cast<long long>(p.lz) * y0);
+    // H terms (offset +y): diff = G(y) - G(y+1), the carry holds G(y).
+    // E terms (offset -y): diff = G(y) - G(y-1), the carry holds G(y-1).
+    T carry = T(0);
+    if (ty >= 0) {
+        if (yUp) carry = c.G[ty][i];
+        else if (y0 > 0) carry = c.G[ty][i - plane];
+    }
+    for (int y = y0; y < y1; ++y, i += plane) {
+        T gy = T(0), gyn = T(0);
+        if (ty >= 0) {
+            if (yUp) {
+                gy = carry;
+                gyn = (y + 1 < p.ly) ? c.G[ty][i + plane] : T(0);
+                carry = gyn;
+            } else {
+                gy = c.G[ty][i];
+                gyn = carry;
+                carry = gy;
+            }
+        }
+        const uint8_t code = c.code[i];
+        if (code == 0) continue;
+        if (code >= c.ncls) {
+            atomicOr(p.err, kErrClassCode);
+            continue;
+        }
+        const Class<T>& k = tab[code];
+        if (EPASS && k.lor) {
+            if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
+                atomicOr(p.err, kErrPoleCount);
+                continue;
+            }
+            const T e = c.U[i];
+            const int s = p.poleStart[k.obj];
+            const int n = p.poleCount[k.obj];
+            for (int q = 0; q < n; ++q) {
+                const T old = c.P[q][i];
+                T np = p.alpha[s + q] * old;
+                np += p.xi[s + q] * c.Pprev[q][i];
+                np += p.gamma[s + q] * e;
+                c.P[q][i] = np;
+                c.Pprev[q][i] = old;
+            }
+        }
+        const int coord[3] = {x, y, z};
+        T add = T(0);
+        bool any = false;
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (!c.tpresent[t]) continue;
+            const int a = coord[c.axis[t]];
+            const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? c.kprof[t][a] : T(0));
+            const bool psiTerm = c.hasPsi[t] && (k.psiUpd[t] || k.npsi[t]);
+            if (coef == T(0) && !psiTerm) continue;
+            const T diff = (t == ty) ? (gy - gyn) : (c.G[t][i] - c.G[t][i + c.off[t]]);
+            if (coef != T(0)) {
+                add += coef * diff;
+                any = true;
+            }
+            if (c.hasPsi[t]) {
+                if (k.psiUpd[t]) {
+                    T ps = c.psi[t][i];
+                    ps = c.b[t][a] * ps + c.cpsi[t][a] * diff;
+                    c.psi[t][i] = ps;
+                    if (k.npsi[t]) {
+                        add += T(k.npsi[t]) * c.dbpsi[t] * ps;
+                        any = true;
+                    }
+                } else if (k.npsi[t]) {
+                    add += T(k.npsi[t]) * c.dbpsi[t] * c.psi[t][i];
+                    any = true;
+                }
+            }
+        }
+        if (any) {
+            if (k.toD) c.D[i] += add;
+            else c.U[i] += add;
+        }
+        if (EPASS && k.lor) {
+            T e = c.D[i];
+            e *= k.epsInv;
+            for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
+            c.U[i] = e;
+        }
+    }
+}
+
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
-    dim3 block(32, p.lz > 1 ? 4 : 1, p.lz > 1 ? 2 : 8);
-    dim3 grid((p.lx + block.x - 1) / block.x, (p.lz + block.y - 1) / block.y, (p.ly + block.z - 1) / block.z);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (ePass) k_pass<T, true><<<grid, block, 0, s>>>(p);
-    else k_pass<T, false><<<grid, block, 0, s>>>(p);
+    if (p.lz > 1) {
+        dim3 block(32, kMarchBZ, 1);
+        dim3 grid((p.lx + 31) / 32, (p.lz + kMarchBZ - 1) / kMarchBZ, 3 * ((p.ly + kMarchCY - 1) / kMarchCY));
+        if (ePass) k_pass_march<T, true><<<grid, block, 0, s>>>(p);
+        else k_pass_march<T, false><<<grid, block, 0, s>>>(p);
+    } else {
+        // 2-D grids: one thread per cell, all components of the pass
+        dim3 block(32, 1, 8);
+        dim3 grid((p.lx + 31) / 32, 1, (p.ly + 7) / 8);
+        if (ePass) k_pass<T, true><<<grid, block, 0, s>>>(p);
+        else k_pass<T, false><<<grid, block, 0, s>>>(p);
+    }
 }
 
 template <typename T>
@@ -139,24 +264,103 @@ void launch_record(const RecordTable& r, const Fields<T>& f, const int* step, vo
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft(const DftTable d, const Fields<T> f, const int* __restrict__ step) {
-    const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__global__ void __launch_bounds__(256) k_dft_sample(const DftTable<T> d, const Fields<T> f, const int* __restrict__ step) {
+    const long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     const int st = *step;
-    if (st % d.timeInt != 0) return;
-    if (j >= d.npts * d.nfreq) return;
-    const long long pt = j / d.nfreq;
-    const int fq = static_cast<int>(j - pt * d.nfreq);
-    const double v = static_cast<double>(f.f[d.comp[pt]][d.cell[pt]]);
-    const double* ph = d.phasor + (static_cast<long long>(st) * d.nfreq + fq) * 2;
-    d.re[j] += ph[0] * v;
-    d.im[j] += ph[1] * v;
+    if (st % d.timeInt != 0 || p >= d.npts) return;
+    const int slot = (st / d.timeInt) % d.K;
+    d.ring[static_cast<long long>(slot) * d.npts + p] = f.f[d.comp[p]][d.cell[p]];
 }
 
 template <typename T>
-void launch_dft(const DftTable& d, const Fields<T>& f, const int* step, void* stream) {
-    const long long n = d.npts * d.nfreq;
-    if (n == 0) return;
-    k_dft<T><<<static_cast<unsigned>((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(d, f, step);
+void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step, void* stream) {
+    if (d.npts == 0) return;
+    k_dft_sample<T><<<static_cast<unsigned>((d.npts + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(d, f, step);
+}
+
+constexpr int kFoldPts = 32;   // points per tile of the fold kernel
+constexpr int kFoldWarps = 8;  // 256 threads: lane -> frequency, warp -> 4 points of the tile
+
+// Fold of K ring samples into the accumulators. Shared memory holds the K
+// phasor rows (nfreq cos/-sin pairs each) and the tile's K x kFoldPts samples.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
+                                                  int firstSample) {
+    extern __shared__ unsigned char smem_raw[];
+    T* ph = reinterpret_cast<T*>(smem_raw);          // [K][nfreq][2]
+    T* smp = ph + static_cast<long long>(d.K) * d.nfreq * 2;  // [K][kFoldPts]
+    int count, first;
+    if (flushCount > 0) {
+        count = flushCount;
+        first = firstSample;
+    } else {
+        const int st = *step;
+        if (st % d.timeInt != 0) return;
+        const int n = st / d.timeInt;
+        if (n % d.K != d.K - 1) return;
+        count = d.K;
+        first = n - (d.K - 1);
+    }
+    const int nf = d.nfreq;
+    for (int q = threadIdx.x; q < count * nf * 2; q += blockDim.x)
+        ph[q] = d.phasor[static_cast<long long>(first) * nf * 2 + q];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long tiles = (d.npts + kFoldPts - 1) / kFoldPts;
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const long long p0 = tile * kFoldPts;
+        __syncthreads();
+        for (int q = threadIdx.x; q < count * kFoldPts; q += blockDim.x) {
+            const int k = q / kFoldPts, pp = q % kFoldPts;
+            const long long p = p0 + pp;
+            const int slot = (first + k) % d.K;
+            smp[q] = (p < d.npts) ? d.ring[static_cast<long long>(slot) * d.npts + p] : T(0);
+        }
+        __syncthreads();
+        constexpr int PPW = kFoldPts / kFoldWarps;  // points per warp
+        for (int fb = 0; fb < nf; fb += 32) {
+            const int fq = fb + lane;
+            if (fq >= nf) break;
+            T are[PPW], aim[PPW];
+#pragma unroll
+            for (int j = 0; j < PPW; ++j) are[j] = aim[j] = T(0);
+            for (int k = 0; k < count; ++k) {
+                const T c = ph[(k * nf + fq) * 2 + 0];
+                const T sn = ph[(k * nf + fq) * 2 + 1];
+#pragma unroll
+                for (int j = 0; j < PPW; ++j) {
+                    const T v = smp[k * kFoldPts + warp * PPW + j];
+                    are[j] += c * v;
+                    aim[j] += sn * v;
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < PPW; ++j) {
+                const long long p = p0 + warp * PPW + j;
+                if (p >= d.npts) continue;
+                d.re[p * nf + fq] += static_cast<double>(are[j]);
+                d.im[p * nf + fq] += static_cast<double>(aim[j]);
+            }
+        }
+    }
+}
+
+template <typename T>
+static size_t fold_smem(const DftTable<T>& d) {
+    return (static_cast<size_t>(d.K) * d.nfreq * 2 + static_cast<size_t>(d.K) * kFoldPts) * sizeof(T);
+}
+
+template <typename T>
+void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream) {
+    if (d.npts == 0) return;
+    const size_t sm = fold_smem(d);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_dft_fold<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    const long long tiles = (d.npts + kFoldPts - 1) / kFoldPts;
+    const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
+    k_dft_fold<T><<<grid, 256, sm, static_cast<cudaStream_t>(stream)>>>(d, step, flushCount, firstSample);
 }
 
 __global__ void k_increment(int* step) { *step += 1; }
@@ -169,8 +373,10 @@ template void launch_sources<double>(const SourceTable&, const Fields<double>&, 
 template void launch_sources<float>(const SourceTable&, const Fields<float>&, const int*, void*);
 template void launch_record<double>(const RecordTable&, const Fields<double>&, const int*, void*);
 template void launch_record<float>(const RecordTable&, const Fields<float>&, const int*, void*);
-template void launch_dft<double>(const DftTable&, const Fields<double>&, const int*, void*);
-template void launch_dft<float>(const DftTable&, const Fields<float>&, const int*, void*);
+template void launch_dft_sample<double>(const DftTable<double>&, const Fields<double>&, const int*, void*);
+template void launch_dft_sample<float>(const DftTable<float>&, const Fields<float>&, const int*, void*);
+template void launch_dft_fold<double>(const DftTable<double>&, const int*, int, int, void*);
+template void launch_dft_fold<float>(const DftTable<float>&, const int*, int, int, void*);
 
 }  // namespace dev
 }  // namespace chiml

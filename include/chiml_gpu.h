@@ -96,8 +96,8 @@ void* chiml_stream(chiml_sim* sim);
 /* Advances nsteps steps without graphs, timing every kernel launch with CUDA
  * events on the handle's stream. ms_out[k] receives the summed milliseconds of
  * kernel slot k: 0 H pass, 1 sources, 2 E pass, 3 step counter, 4 detector
- * records, 5 + q DFT of flux region q. *nslots receives the number of slots
- * written (at most max_slots). */
+ * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of flux region q.
+ * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
 #ifdef __cplusplus
