@@ -72,7 +72,10 @@ EXPORTED = [
     "chiml_get_field",
     "chiml_stream",
     "chiml_profile_steps",
+    "chiml_get_box_noalloc",
 ]
+
+BOX_NOALLOC_MAX_CELLS = 1048576
 
 
 def load_library(path=None):
@@ -105,6 +108,9 @@ def load_library(path=None):
     lib.chiml_profile_steps.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_int)]
     lib.chiml_profile_steps.restype = ctypes.c_int
+    lib.chiml_get_box_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
+                                          ctypes.POINTER(ctypes.c_double)]
+    lib.chiml_get_box_noalloc.restype = ctypes.c_int
     if path is None:
         _lib = lib
     return lib
@@ -153,6 +159,20 @@ class Simulation:
         out = np.empty(s.cells, dtype=np.float64)
         self._check(self._lib.chiml_get_field(self._h, COMPONENTS[name], out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return out.reshape(ly, lz, lx)
+
+    def box_noalloc(self, name, origin, shape, out=None):
+        """Reads the box at origin (x0, y0, z0) of shape (nx, ny, nz) of one field as an FP64 array
+        shaped (ny, nz, nx), through the engine's fixed device array (no device allocation).
+        A caller-provided `out` (C-contiguous float64, nx*ny*nz values) is filled and returned."""
+        nx, ny, nz = (int(v) for v in shape)
+        if out is None:
+            out = np.empty(nx * ny * nz, dtype=np.float64)
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != nx * ny * nz:
+            raise ValueError("out must be a C-contiguous float64 array of nx*ny*nz values")
+        box = (ctypes.c_int32 * 6)(int(origin[0]), int(origin[1]), int(origin[2]), nx, ny, nz)
+        self._check(self._lib.chiml_get_box_noalloc(self._h, COMPONENTS[name], box,
+                                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out.reshape(ny, nz, nx)
 
     def profile_steps(self, n):
         """Runs n steps with per-kernel CUDA-event timing; returns {slot name: total ms}."""

@@ -55,10 +55,11 @@ def build_engine(force=False):
         return LIB_ENGINE
     objs = []
     jobs = []
-    cu = os.path.join(CSRC, "kernels", "fdtd_kernels.cu")
-    o = os.path.join(BUILD, "fdtd_kernels.o")
-    jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu, "-o", o])
-    objs.append(o)
+    for name in ("fdtd_kernels", "box_noalloc"):
+        cu = os.path.join(CSRC, "kernels", name + ".cu")
+        o = os.path.join(BUILD, name + ".o")
+        jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu, "-o", o])
+        objs.append(o)
     cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-I" + os.path.join(CUDA_HOME, "include")]
     for f in ["engine.cpp"] + ["host/" + h for h in HOST_SRCS]:
         o = os.path.join(BUILD, os.path.basename(f).replace(".cpp", ".o"))

@@ -16,6 +16,7 @@
 #include "../../include/chiml_gpu.h"
 #include "host/outputs.hpp"
 #include "host/plan.hpp"
+#include "kernels/box_noalloc.hpp"
 #include "kernels/fdtd_device.hpp"
 
 using namespace chiml;
@@ -73,6 +74,7 @@ struct SimBase {
     virtual cudaStream_t stream() const = 0;
     virtual int profile(int nsteps, double* ms, int maxSlots) = 0;
     virtual void checkDeviceErrors() = 0;
+    virtual chiml_status getBoxNoAlloc(int comp, const int box[6], double* out, std::string& why) = 0;
 };
 
 template <typename T>
@@ -175,6 +177,32 @@ public:
             ck(cudaMemcpy(tmp.data(), fields_.f[comp], N * sizeof(T), cudaMemcpyDeviceToHost), "D2H field");
             for (std::size_t i = 0; i < N; ++i) out[i] = static_cast<double>(tmp[i]);
         }
+    }
+
+    // Validates the box and reads it through the fixed device array; no allocation.
+    chiml_status getBoxNoAlloc(int comp, const int box[6], double* out, std::string& why) override {
+        const Dims& D = P.dims;
+        if (comp < 0 || comp > 8 || !fields_.f[comp]) {
+            why = "field not present";
+            return CHIML_E_INPUT;
+        }
+        const int ext[3] = {D.lx, D.ly, D.lz};
+        for (int a = 0; a < 3; ++a) {
+            if (box[3 + a] < 1 || box[a] < 0 || box[a] > ext[a] - box[3 + a]) {
+                why = "box outside the local grid (x0, y0, z0, nx, ny, nz against lx, ly, lz)";
+                return CHIML_E_INPUT;
+            }
+        }
+        const long long n = static_cast<long long>(box[3]) * box[4] * box[5];
+        if (n > dev::kBoxScratchCells) {
+            why = "box of " + std::to_string(n) + " cells exceeds the limit of " +
+                  std::to_string(dev::kBoxScratchCells) + " cells of chiml_get_box_noalloc";
+            return CHIML_E_INPUT;
+        }
+        cudaError_t e = dev::gather_box_noalloc<T>(opt_.device, fields_.f[comp], D.lx, D.lz, box, out, stream_);
+        if (e == cudaSuccess) return CHIML_OK;
+        why = std::string("chiml_get_box_noalloc: ") + cudaGetErrorString(e);
+        return CHIML_E_CUDA;
     }
 
     void fillStats(chiml_stats* s) const override {
@@ -691,6 +719,15 @@ chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out) {
         sim->h.err = e.what();
         return status_of(e);
     }
+}
+
+chiml_status chiml_get_box_noalloc(chiml_sim* sim, int comp, const int32_t box[6], double* out) {
+    if (!sim || !box || !out) return CHIML_E_STATE;
+    const int b[6] = {box[0], box[1], box[2], box[3], box[4], box[5]};
+    std::string why;
+    const chiml_status st = sim->h.sim->getBoxNoAlloc(comp, b, out, why);
+    if (st != CHIML_OK) sim->h.err = why;
+    return st;
 }
 
 void* chiml_stream(chiml_sim* sim) { return sim ? static_cast<void*>(sim->h.sim->stream()) : nullptr; }

@@ -100,6 +100,29 @@ void* chiml_stream(chiml_sim* sim);
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
+/* Largest box, in cells, that chiml_get_box_noalloc reads in one call. */
+#define CHIML_BOX_NOALLOC_MAX_CELLS 1048576
+
+/* Copies the box {x0, y0, z0, nx, ny, nz} of one field (local grid, halo
+ * included, as chiml_get_field) to host memory as FP64, x fastest, then z, then
+ * y; out holds nx*ny*nz doubles. No counterpart in the reference: chiML has no
+ * device memory to read back.
+ *
+ * It allocates nothing, on the device or through any library: it is for
+ * callers that cannot allocate device memory when they read a field, such as a
+ * run that fills HBM and has no room for a temporary, or a host application
+ * whose own memory pool must not see cudaMalloc/cudaFree (which also stall the
+ * device) from a library. The values pass through one fixed device array of
+ * CHIML_BOX_NOALLOC_MAX_CELLS doubles (8 MiB) per device; a larger box, or one
+ * outside the grid, returns CHIML_E_INPUT with the reason in chiml_last_error.
+ * The first call on a device looks up that array's address (the only set-up);
+ * make that first call before any stream capture on the device. Every call
+ * shares the array and leaves its values there; each call writes every value
+ * it returns before copying, so nothing needs clearing. The call waits for its
+ * copy. Calls that overlap on the GPU (handles of one device used from several
+ * host threads at once) race on the array. */
+chiml_status chiml_get_box_noalloc(chiml_sim* sim, int comp, const int32_t box[6], double* out);
+
 #ifdef __cplusplus
 }
 #endif
