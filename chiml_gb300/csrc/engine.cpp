@@ -316,6 +316,74 @@ private:
         cudaGraphDestroy(g);
     }
 
+    // Per term, the coordinate bounds outside which no cell uses the term's CPML
+    // profile or psi, and whether the 3-D interior kernel form applies.
+    void setSlabsAndForm(dev::Pass<T>& pass, bool ePass) const {
+        const Dims& D = P.dims;
+        bool interior = D.lz > 1;
+        for (int ci = 0; ci < 3; ++ci) {
+            const CompPlan& cp = P.comp[(ePass ? 0 : 3) + ci];
+            dev::Comp<T>& dc = pass.c[ci];
+            const int axes[2] = {(ci + 2) % 3, (ci + 1) % 3};
+            if (!cp.present) {
+                interior = false;
+                continue;
+            }
+            for (int t = 0; t < 2; ++t) {
+                const TermPlan& tp = cp.term[t];
+                const int L = tp.axis == 0 ? D.lx : (tp.axis == 1 ? D.ly : D.lz);
+                dc.slabLo[t] = 0;
+                dc.slabHi[t] = L;
+                if (!tp.present || tp.axis != axes[t]) {
+                    interior = false;
+                    continue;
+                }
+                const long long unit[3] = {1, static_cast<long long>(D.lx) * D.lz, D.lx};
+                if (tp.off != (ePass ? -1 : 1) * unit[tp.axis]) interior = false;
+                std::vector<uint8_t> uses(cp.classes.size(), 0);
+                bool anyUse = false;
+                for (std::size_t q = 0; q < cp.classes.size(); ++q) {
+                    const ClassInfo& k = cp.classes[q];
+                    uses[q] = (k.kflag[t] || k.psiUpd[t] || k.npsi[t]) ? 1 : 0;
+                    anyUse = anyUse || uses[q];
+                }
+                if (!anyUse) continue;  // empty slab: no a satisfies a < 0 or a >= L
+                int lo = 0, hi = L;
+                for (int y = 0; y < D.ly; ++y)
+                    for (int z = 0; z < D.lz; ++z) {
+                        const long long row = static_cast<long long>(D.lx) * (z + static_cast<long long>(D.lz) * y);
+                        for (int x = 0; x < D.lx; ++x) {
+                            if (!uses[cp.code[row + x]]) continue;
+                            const int a = tp.axis == 0 ? x : (tp.axis == 1 ? y : z);
+                            if (2 * a < L) lo = std::max(lo, a + 1);
+                            else hi = std::min(hi, a);
+                        }
+                    }
+                dc.slabLo[t] = lo;
+                dc.slabHi[t] = hi;
+            }
+        }
+        // the interior form never visits halo cells: all of them must be inactive
+        if (interior) {
+            for (int ci = 0; ci < 3 && interior; ++ci) {
+                const std::vector<uint8_t>& code = P.comp[(ePass ? 0 : 3) + ci].code;
+                for (int y = 0; y < D.ly && interior; ++y)
+                    for (int z = 0; z < D.lz && interior; ++z) {
+                        const long long row = static_cast<long long>(D.lx) * (z + static_cast<long long>(D.lz) * y);
+                        const bool edge = (y == 0 || y == D.ly - 1 || z == 0 || z == D.lz - 1);
+                        if (edge) {
+                            for (int x = 0; x < D.lx; ++x)
+                                if (code[row + x]) interior = false;
+                        } else if (code[row] || code[row + D.lx - 1]) {
+                            interior = false;
+                        }
+                    }
+            }
+        }
+        pass.interior3d = interior ? 1 : 0;
+        pass.index64 = D.cells() + 2LL * D.lx * D.lz >= (1LL << 31) ? 1 : 0;
+    }
+
     // Host-side bounds validation of every index the kernels will dereference.
     void validatePlan() const {
         const Dims& D = P.dims;
@@ -426,7 +494,7 @@ private:
                         o.psiUpd[t] = k.psiUpd[t];
                     }
                     if (k.ordip) throw UnsupportedError("oriented-dipole cells are not supported by the device engine");
-                    if (k.lor && !cp.hasD) throw InputError("dispersive cell without a D field");
+                    if ((k.lor || k.toD) && !cp.hasD) throw InputError("dispersive cell without a D field");
                 }
                 dc.cls = mem_.upload(cls);
                 dc.ncls = static_cast<int>(cls.size());
@@ -454,6 +522,7 @@ private:
                 }
                 bytes += 3.0 * sizeof(T) + 1.0;  // field read + write, neighbour read, code
             }
+            setSlabsAndForm(pass, half == 1);
         }
         (void)bytes;
         bytesPerCell_ = algorithmicBytesPerCell();

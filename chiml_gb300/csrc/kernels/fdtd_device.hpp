@@ -49,6 +49,10 @@ struct Comp {
     const T* cpsi[2];
     T db[2];
     T dbpsi[2];
+    // Coordinates along each term's axis outside which no cell uses that term's
+    // CPML profile or psi: the slab is a < slabLo or a >= slabHi.
+    int slabLo[2];
+    int slabHi[2];
 };
 
 template <typename T>
@@ -62,10 +66,15 @@ struct Pass {
     const T* gamma;
     int nObj;
     unsigned int* err;      // device error word (kErr* bits); the kernel skips the cell instead of faulting
+    // 3-D interior form usable: every halo cell has code 0, term j of component c
+    // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
+    int interior3d;
+    int index64;            // grid too large for 32-bit cell indices
 };
 
 constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class table
 constexpr unsigned int kErrPoleCount = 2u;   // a class asks for more poles than its component stores
+constexpr unsigned int kErrSlab = 4u;        // a class uses a CPML term outside its term's slab bounds
 
 template <typename T>
 struct Fields {

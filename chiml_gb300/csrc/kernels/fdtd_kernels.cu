@@ -92,135 +92,187 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
     }
 }
 
-// Marching form of the same update. A block covers a 32 (x) by BZ (z) tile of
-// one component and walks a chunk of CY planes along y, the slowest axis of the
-// layout. The neighbour along y is carried in a register from the previous
-// plane, so each plane loads it once instead of twice; the class table sits in
-// shared memory. Per cell the arithmetic is the same as k_pass.
-constexpr int kMarchBZ = 8;
-constexpr int kMarchCY = 16;
+// 3-D form of the same update for grids whose halo cells carry no update.
+// A block covers a 32 (x) by kP3BZ (z) tile of interior cells of one
+// component and walks kP3CY planes along y, the slowest axis of the layout.
+// The component (and with it the two derivative axes) is a template
+// parameter. Every load a cell needs in the common case (class code, the
+// field, both neighbour pairs, psi inside the slab) is issued before the class
+// is known, so a warp keeps several independent loads in flight; the class
+// only selects the arithmetic. The neighbour along y is carried in a register
+// from the previous plane. Per cell the arithmetic is the same as k_pass.
+constexpr int kP3BZ = 8;
+constexpr int kP3CY = 16;
 
-template <typename T, bool EPASS>
-__global__ void __launch_bounds__(256) k_pass_march(const Pass<T> p) {
-    __shared__ Class<T> tab[256];
-    const int ci = blockIdx.z % 3;
-    const Comp<T>& c = p.c[ci];
-    if (!c.present) return;
-    for (int q = threadIdx.x + threadIdx.y * 32; q < c.ncls; q += 32 * kMarchBZ) tab[q] = c.cls[q];
-    __syncthreads();
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    const int z = blockIdx.y * kMarchBZ + threadIdx.y;
-    const int y0 = (blockIdx.z / 3) * kMarchCY;
-    if (x >= p.lx || z >= p.lz || y0 >= p.ly) return;
-    const long long plane = static_cast<long long>(p.lx) * p.lz;
-    const int y1 = min(y0 + kMarchCY, p.ly);
-    // y-carried neighbour: for the term whose offset is along y, G(i + off) of this
-    // plane is G(i) of the neighbouring plane, which the march visits in turn
-    int ty = -1;
+template <typename T, bool EPASS, int CI, typename I>
+__device__ __forceinline__ void pass3d(const Pass<T>& p, const Class<T>* __restrict__ tab) {
+    constexpr int A0 = (CI + 2) % 3;  // derivative axis of term J
+    constexpr int A1 = (CI + 1) % 3;  // derivative axis of term K
+    constexpr int TY = (A0 == 1) ? 0 : ((A1 == 1) ? 1 : -1);  // term along y, or none
+    constexpr bool UP = !EPASS;       // H: neighbour at +1 ; E: neighbour at -1
+    const Comp<T>& c = p.c[CI];
+    const int x = 1 + blockIdx.x * 32 + threadIdx.x;
+    const int z = 1 + blockIdx.y * kP3BZ + threadIdx.y;
+    const int y0 = 1 + (blockIdx.z / 3) * kP3CY;
+    if (x > p.lx - 2 || z > p.lz - 2 || y0 > p.ly - 2) return;
+    const int y1 = min(y0 + kP3CY, p.ly - 1);
+    const I plane = static_cast<I>(p.lx) * p.lz;
+    I i = x + static_cast<I>(p.lx) * (z + static_cast<I>(p.lz) * y0);
+
+    const uint8_t* __restrict__ code = c.code;
+    T* __restrict__ U = c.U;
+    const T* __restrict__ G[2] = {c.G[0], c.G[1]};
+    const I off[2] = {static_cast<I>(c.off[0]), static_cast<I>(c.off[1])};
+    // profile values of the terms along x or z are fixed for the thread
+    bool in[2] = {false, false};
+    T kp[2] = {T(0), T(0)}, bq[2] = {T(0), T(0)}, cq[2] = {T(0), T(0)};
 #pragma unroll
-    for (int t = 0; t < 2; ++t)
-        if (c.tpresent[t] && c.axis[t] == 1) ty = t;
-    const bool yUp = (ty >= 0) && c.off[ty] > 0;  // H: +y neighbour ; E: -y neighbour
-    long long i = x + static_cast<long long>(p.lx) * (z + static_cast<long long>(p.lz) * y0);
-    // H terms (offset +y): diff = G(y) - G(y+1), the carry holds G(y).
-    // E terms (offset -y): diff = G(y) - G(y-1), the carry holds G(y-1).
-    T carry = T(0);
-    if (ty >= 0) {
-        if (yUp) carry = c.G[ty][i];
-        else if (y0 > 0) carry = c.G[ty][i - plane];
-    }
-    for (int y = y0; y < y1; ++y, i += plane) {
-        T gy = T(0), gyn = T(0);
-        if (ty >= 0) {
-            if (yUp) {
-                gy = carry;
-                gyn = (y + 1 < p.ly) ? c.G[ty][i + plane] : T(0);
-                carry = gyn;
-            } else {
-                gy = c.G[ty][i];
-                gyn = carry;
-                carry = gy;
+    for (int t = 0; t < 2; ++t) {
+        const int ax = t == 0 ? A0 : A1;
+        if (ax == 1) continue;
+        const int a = ax == 0 ? x : z;
+        in[t] = a < c.slabLo[t] || a >= c.slabHi[t];
+        if (in[t]) {
+            kp[t] = c.kprof[t][a];
+            if (c.hasPsi[t]) {
+                bq[t] = c.b[t][a];
+                cq[t] = c.cpsi[t][a];
             }
         }
-        const uint8_t code = c.code[i];
-        if (code == 0) continue;
-        if (code >= c.ncls) {
+    }
+    T carry = T(0);
+    if constexpr (TY >= 0) carry = UP ? G[TY][i] : G[TY][i - plane];
+
+    for (int y = y0; y < y1; ++y, i += plane) {
+        const uint8_t cd = code[i];
+        const T u = U[i];
+        T g[2], n[2];
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (t == TY) {
+                if (UP) {
+                    g[t] = carry;
+                    n[t] = G[t][i + plane];
+                    carry = n[t];
+                } else {
+                    g[t] = G[t][i];
+                    n[t] = carry;
+                    carry = g[t];
+                }
+            } else {
+                g[t] = G[t][i];
+                n[t] = G[t][i + off[t]];
+            }
+        }
+        if constexpr (TY >= 0) {
+            in[TY] = y < c.slabLo[TY] || y >= c.slabHi[TY];
+            kp[TY] = T(0);
+            if (in[TY]) {
+                kp[TY] = c.kprof[TY][y];
+                if (c.hasPsi[TY]) {
+                    bq[TY] = c.b[TY][y];
+                    cq[TY] = c.cpsi[TY][y];
+                }
+            }
+        }
+        T ps[2] = {T(0), T(0)};
+#pragma unroll
+        for (int t = 0; t < 2; ++t)
+            if (c.hasPsi[t] && in[t]) ps[t] = c.psi[t][i];
+
+        if (cd == 0) continue;
+        if (cd >= c.ncls) {
             atomicOr(p.err, kErrClassCode);
             continue;
         }
-        const Class<T>& k = tab[code];
+        const Class<T>& k = tab[cd];
         if (EPASS && k.lor) {
             if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
                 atomicOr(p.err, kErrPoleCount);
                 continue;
             }
-            const T e = c.U[i];
             const int s = p.poleStart[k.obj];
-            const int n = p.poleCount[k.obj];
-            for (int q = 0; q < n; ++q) {
+            const int np = p.poleCount[k.obj];
+            for (int q = 0; q < np; ++q) {
                 const T old = c.P[q][i];
-                T np = p.alpha[s + q] * old;
-                np += p.xi[s + q] * c.Pprev[q][i];
-                np += p.gamma[s + q] * e;
-                c.P[q][i] = np;
+                T v = p.alpha[s + q] * old;
+                v += p.xi[s + q] * c.Pprev[q][i];
+                v += p.gamma[s + q] * u;
+                c.P[q][i] = v;
                 c.Pprev[q][i] = old;
             }
         }
-        const int coord[3] = {x, y, z};
         T add = T(0);
         bool any = false;
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
-            if (!c.tpresent[t]) continue;
-            const int a = coord[c.axis[t]];
-            const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? c.kprof[t][a] : T(0));
-            const bool psiTerm = c.hasPsi[t] && (k.psiUpd[t] || k.npsi[t]);
-            if (coef == T(0) && !psiTerm) continue;
-            const T diff = (t == ty) ? (gy - gyn) : (c.G[t][i] - c.G[t][i + c.off[t]]);
+            if (!in[t] && (k.kflag[t] | k.psiUpd[t] | k.npsi[t])) {
+                atomicOr(p.err, kErrSlab);
+                continue;
+            }
+            const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? kp[t] : T(0));
+            const T diff = g[t] - n[t];
             if (coef != T(0)) {
                 add += coef * diff;
                 any = true;
             }
-            if (c.hasPsi[t]) {
+            if (c.hasPsi[t] && in[t]) {
                 if (k.psiUpd[t]) {
-                    T ps = c.psi[t][i];
-                    ps = c.b[t][a] * ps + c.cpsi[t][a] * diff;
-                    c.psi[t][i] = ps;
+                    const T q = bq[t] * ps[t] + cq[t] * diff;
+                    c.psi[t][i] = q;
                     if (k.npsi[t]) {
-                        add += T(k.npsi[t]) * c.dbpsi[t] * ps;
+                        add += T(k.npsi[t]) * c.dbpsi[t] * q;
                         any = true;
                     }
                 } else if (k.npsi[t]) {
-                    add += T(k.npsi[t]) * c.dbpsi[t] * c.psi[t][i];
+                    add += T(k.npsi[t]) * c.dbpsi[t] * ps[t];
                     any = true;
                 }
             }
         }
         if (any) {
             if (k.toD) c.D[i] += add;
-            else c.U[i] += add;
+            else U[i] = u + add;
         }
         if (EPASS && k.lor) {
             T e = c.D[i];
             e *= k.epsInv;
             for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
-            c.U[i] = e;
+            U[i] = e;
         }
     }
+}
+
+template <typename T, bool EPASS, typename I>
+__global__ void __launch_bounds__(256) k_pass3d(const Pass<T> p) {
+    __shared__ Class<T> tab[256];
+    const int ci = blockIdx.z % 3;
+    const Comp<T>& c = p.c[ci];
+    for (int q = threadIdx.x + threadIdx.y * 32; q < c.ncls; q += 32 * kP3BZ) tab[q] = c.cls[q];
+    __syncthreads();
+    if (ci == 0) pass3d<T, EPASS, 0, I>(p, tab);
+    else if (ci == 1) pass3d<T, EPASS, 1, I>(p, tab);
+    else pass3d<T, EPASS, 2, I>(p, tab);
 }
 
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (p.lz > 1) {
-        dim3 block(32, kMarchBZ, 1);
-        dim3 grid((p.lx + 31) / 32, (p.lz + kMarchBZ - 1) / kMarchBZ, 3 * ((p.ly + kMarchCY - 1) / kMarchCY));
-        if (ePass) k_pass_march<T, true><<<grid, block, 0, s>>>(p);
-        else k_pass_march<T, false><<<grid, block, 0, s>>>(p);
+    if (p.interior3d) {
+        dim3 block(32, kP3BZ, 1);
+        dim3 grid((p.lx - 2 + 31) / 32, (p.lz - 2 + kP3BZ - 1) / kP3BZ, 3 * ((p.ly - 2 + kP3CY - 1) / kP3CY));
+        if (p.index64) {
+            if (ePass) k_pass3d<T, true, long long><<<grid, block, 0, s>>>(p);
+            else k_pass3d<T, false, long long><<<grid, block, 0, s>>>(p);
+        } else {
+            if (ePass) k_pass3d<T, true, int><<<grid, block, 0, s>>>(p);
+            else k_pass3d<T, false, int><<<grid, block, 0, s>>>(p);
+        }
     } else {
-        // 2-D grids: one thread per cell, all components of the pass
+        // 2-D grids, and 3-D grids with updated halo cells: one thread per cell,
+        // all components of the pass
         dim3 block(32, 1, 8);
-        dim3 grid((p.lx + 31) / 32, 1, (p.ly + 7) / 8);
+        dim3 grid((p.lx + 31) / 32, p.lz, (p.ly + 7) / 8);
         if (ePass) k_pass<T, true><<<grid, block, 0, s>>>(p);
         else k_pass<T, false><<<grid, block, 0, s>>>(p);
     }
