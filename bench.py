@@ -311,7 +311,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT, help="cells per side")
     ap.add_argument("--graph", type=int, default=20, help="steps per CUDA graph")
-    ap.add_argument("--profile-steps", type=int, default=64)
+    ap.add_argument("--profile-steps", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -334,7 +335,8 @@ private:
                 const int L = tp.axis == 0 ? D.lx : (tp.axis == 1 ? D.ly : D.lz);
                 dc.slabLo[t] = 0;
                 dc.slabHi[t] = L;
-                if (!tp.present || tp.axis != axes[t]) {
+                const int field = (ePass ? 3 : 0) + (t == 0 ? (ci + 1) % 3 : (ci + 2) % 3);
+                if (!tp.present || tp.axis != axes[t] || tp.field != field) {
                     interior = false;
                     continue;
                 }
@@ -344,7 +346,8 @@ private:
                 bool anyUse = false;
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
-                    uses[q] = (k.kflag[t] || k.psiUpd[t] || k.npsi[t]) ? 1 : 0;
+                    // cells that only add psi without updating it add zero (their psi is never written)
+                    uses[q] = (k.kflag[t] || k.psiUpd[t]) ? 1 : 0;
                     anyUse = anyUse || uses[q];
                 }
                 if (!anyUse) continue;  // empty slab: no a satisfies a < 0 or a >= L
@@ -497,6 +500,28 @@ private:
                     if ((k.lor || k.toD) && !cp.hasD) throw InputError("dispersive cell without a D field");
                 }
                 dc.cls = mem_.upload(cls);
+                std::vector<dev::FastClass<T>> fcls(cp.classes.size());
+                for (std::size_t q = 0; q < cp.classes.size(); ++q) {
+                    const ClassInfo& k = cp.classes[q];
+                    dev::FastClass<T>& o = fcls[q];
+                    std::memset(&o, 0, sizeof(o));
+                    bool write = false;
+                    for (int t = 0; t < 2; ++t) {
+                        const TermPlan& tp = cp.term[t];
+                        const double base = k.cint[t] + static_cast<double>(k.nplain[t]) * (tp.present ? tp.db : 0.0);
+                        o.coef[t] = static_cast<T>(base);
+                        if (k.kflag[t]) o.flags |= (t == 0 ? dev::kFcKp0 : dev::kFcKp1);
+                        const bool psiUpd = k.psiUpd[t] && tp.present && tp.hasPsi;
+                        o.psiCoef[t] = psiUpd ? static_cast<T>(static_cast<double>(k.npsi[t]) * tp.dbpsi) : T(0);
+                        if (psiUpd) o.flags |= (t == 0 ? dev::kFcPsi0 : dev::kFcPsi1);
+                        if (k.kflag[t] || k.psiUpd[t]) o.flags |= (t == 0 ? dev::kFcSlab0 : dev::kFcSlab1);
+                        if (base != 0.0 || k.kflag[t] || (psiUpd && k.npsi[t])) write = true;
+                    }
+                    if (k.lor) o.flags |= dev::kFcLor;
+                    if (k.toD) o.flags |= dev::kFcToD;
+                    if (write) o.flags |= dev::kFcWrite;
+                }
+                dc.fcls = mem_.upload(fcls);
                 dc.ncls = static_cast<int>(cls.size());
                 dc.nPoles = cp.nPoles;
                 if (cp.nPoles > dev::kMaxPoles) throw UnsupportedError("more than 8 Lorentz poles on one component");
@@ -523,9 +548,29 @@ private:
                 bytes += 3.0 * sizeof(T) + 1.0;  // field read + write, neighbour read, code
             }
             setSlabsAndForm(pass, half == 1);
+            if (half == 1 && pass.interior3d) {
+                // dispersive cells leave the interior form for their own list kernel
+                std::vector<int> lc;
+                std::vector<long long> li;
+                for (int ci = 0; ci < 3; ++ci) {
+                    const CompPlan& cp = P.comp[ci];
+                    if (!cp.present) continue;
+                    for (long long i = 0; i < static_cast<long long>(cp.code.size()); ++i)
+                        if (cp.code[i] && cp.classes[cp.code[i]].lor) {
+                            lc.push_back(ci);
+                            li.push_back(i);
+                        }
+                }
+                pass.nLor = static_cast<long long>(li.size());
+                pass.lorComp = mem_.upload(lc);
+                pass.lorCell = mem_.upload(li);
+            }
+            {
+                const char* sh = std::getenv("CHIML_P3SHAPE");
+                pass.shape = sh ? std::atoi(sh) : 0;
+            }
         }
         (void)bytes;
-        bytesPerCell_ = algorithmicBytesPerCell();
         // sources
         {
             std::vector<int> comp, srcId;
@@ -605,9 +650,7 @@ private:
                     ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 0] = static_cast<T>(e.real());
                     ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 1] = static_cast<T>(e.imag());
                 }
-            // samples per fold: as many as fit the fold kernel's shared memory (<= 64)
-            int K = 64;
-            while (K > 1 && (static_cast<std::size_t>(K) * nf * 2 + static_cast<std::size_t>(K) * 32) * sizeof(T) > 190 * 1024) K /= 2;
+            const int K = dftBlockLength(static_cast<long long>(cell.size()), nSamples);
             d.npts = static_cast<long long>(cell.size());
             d.nfreq = nf;
             d.timeInt = ti;
@@ -621,24 +664,36 @@ private:
             d.im = mem_.alloc<double>(cell.size() * nf);
             dft_.push_back(d);
         }
+        bytesPerCell_ = algorithmicBytesPerCell();
         dStep_ = mem_.alloc<int>(1);
         dErr_ = mem_.alloc<unsigned int>(1);
         hPass_.err = dErr_;
         ePass_.err = dErr_;
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
-        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size());
+        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size()) +
+                          (ePass_.nLor > 0 ? 1 : 0);
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
         for (auto& d : dft_) dev::launch_dft_sample<T>(d, fields_, dStep_, stream_);
         ck(cudaStreamSynchronize(stream_), "initial samples");
     }
 
+    // Samples per fold of a flux region: long blocks cut the accumulator
+    // read-modify-write per step; the ring (K x points values) stays within 2 GB
+    // and K stays near the run's sample count.
+    static int dftBlockLength(long long npts, int nSamples) {
+        int K = 256;
+        while (K > 32 && static_cast<double>(K) * npts * sizeof(T) > 2.0e9) K /= 2;
+        while (K > 32 && K / 2 >= nSamples) K /= 2;
+        return K;
+    }
+
     // Algorithmic HBM bytes of the passes: every array a pass touches is read
     // (and, if it is updated, written) once per launch -- the field components
     // of the pass, the neighbour components it reads, one class byte per
-    // component and cell, and CPML psi, D and Lorentz P/P_prev only at the
-    // cells whose class uses them. Per-step bytes per physical cell are the sum
+    // component and cell, and CPML psi (at the cells that update it), D and
+    // Lorentz P/P_prev only at the cells whose class uses them. Per-step bytes per physical cell are the sum
     // of both passes over the physical cell count.
     double algorithmicBytesPerCell() {
         const Dims& D = P.dims;
@@ -663,7 +718,7 @@ private:
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
                     for (int tt = 0; tt < 2; ++tt)
-                        if (k.psiUpd[tt] || k.npsi[tt]) b += count[q] * 2.0 * t;
+                        if (k.psiUpd[tt]) b += count[q] * 2.0 * t;
                     if (k.lor) b += count[q] * t * (2.0 + 4.0 * P.alpha[k.obj].size());
                     else if (k.toD) b += count[q] * 2.0 * t;
                 }
@@ -673,11 +728,9 @@ private:
         // DFT per sampled step: gather (index 4 B + component 4 B + value read + ring write)
         // plus the fold's accumulator read-modify-write and ring read amortised over K
         dftBytes_ = 0.0;
-        for (auto& fp : P.fluxes) {
-            int nf = static_cast<int>(fp.spec.freqList.size());
-            int K = 64;
-            while (K > 1 && (static_cast<std::size_t>(K) * nf * 2 + static_cast<std::size_t>(K) * 32) * sizeof(T) > 190 * 1024) K /= 2;
-            dftBytes_ += static_cast<double>(fp.npts) * (8.0 + 2.0 * t + t + nf * 4.0 * sizeof(double) / K);
+        for (auto& d : dft_) {
+            const double pts = static_cast<double>(d.npts);
+            dftBytes_ += pts * (8.0 + 2.0 * t) + pts * (t + d.nfreq * 4.0 * sizeof(double)) / d.K;
         }
         return (passBytes_[0] + passBytes_[1]) / phys;
     }

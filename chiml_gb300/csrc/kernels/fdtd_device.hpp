@@ -26,12 +26,34 @@ struct Class {
     uint8_t pad[2];
 };
 
+// The same class in the shape the interior form's arithmetic uses: per term
+// the folded interior coefficient and the psi coefficient, plus flag bits. The
+// first 16 bytes (coefficients and flags) are all a cell outside the CPML
+// slabs needs.
+template <typename T>
+struct alignas(16) FastClass {
+    T coef[2];     // cint + nplain * db
+    uint32_t flags;
+    uint32_t pad0;
+    T psiCoef[2];  // npsi * dbpsi
+};
+constexpr uint32_t kFcPsi0 = 1u;     // term J updates psi
+constexpr uint32_t kFcPsi1 = 2u;     // term K updates psi
+constexpr uint32_t kFcLor = 4u;      // Lorentz ADE and D -> E (E pass)
+constexpr uint32_t kFcToD = 8u;      // the update goes to D
+constexpr uint32_t kFcWrite = 16u;   // the class changes the field
+constexpr uint32_t kFcSlab0 = 32u;   // term J needs the slab (profile or psi)
+constexpr uint32_t kFcSlab1 = 64u;   // term K needs the slab
+constexpr uint32_t kFcKp0 = 128u;    // term J adds its normal-slab profile kprof
+constexpr uint32_t kFcKp1 = 256u;    // term K adds its normal-slab profile kprof
+
 template <typename T>
 struct Comp {
     T* U;                  // field component
     T* D;                  // D component (E components of dispersive runs)
     const uint8_t* code;   // per-cell class code
     const Class<T>* cls;   // class table
+    const FastClass<T>* fcls;  // the same table for the interior form
     int ncls;              // entries in cls
     int present;
     int nPoles;
@@ -70,6 +92,11 @@ struct Pass {
     // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
     int interior3d;
     int index64;            // grid too large for 32-bit cell indices
+    int shape;              // tile shape of the interior form
+    // dispersive cells of the E pass, run by their own kernel in the interior form
+    long long nLor;
+    const int* lorComp;
+    const long long* lorCell;
 };
 
 constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class table

@@ -9,10 +9,78 @@
 // PML/parallelPML.cpp:12-40) into one read and one write of each array.
 #include <cuda_runtime.h>
 
+#include <cstdint>
+#include <type_traits>
+
 #include "fdtd_device.hpp"
 
 namespace chiml {
 namespace dev {
+
+// One component of one cell, any class (the arithmetic every pass form shares).
+template <typename T, bool EPASS>
+__device__ __forceinline__ void cellGeneric(const Pass<T>& p, int ci, long long i, const int coord[3]) {
+    const Comp<T>& c = p.c[ci];
+    const uint8_t code = c.code[i];
+    if (code == 0) return;
+    if (code >= c.ncls) {
+        atomicOr(p.err, kErrClassCode);
+        return;
+    }
+    const Class<T> k = c.cls[code];
+    if (EPASS && k.lor) {
+        if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
+            atomicOr(p.err, kErrPoleCount);
+            return;
+        }
+        const T e = c.U[i];
+        const int s = p.poleStart[k.obj];
+        const int n = p.poleCount[k.obj];
+        for (int q = 0; q < n; ++q) {
+            const T old = c.P[q][i];
+            T np = p.alpha[s + q] * old;
+            np += p.xi[s + q] * c.Pprev[q][i];
+            np += p.gamma[s + q] * e;
+            c.P[q][i] = np;
+            c.Pprev[q][i] = old;
+        }
+    }
+    T add = T(0);
+    bool any = false;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        if (!c.tpresent[t]) continue;
+        const int a = coord[c.axis[t]];
+        const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? c.kprof[t][a] : T(0));
+        const bool psiTerm = c.hasPsi[t] && k.psiUpd[t];
+        if (coef == T(0) && !psiTerm) continue;
+        const T diff = c.G[t][i] - c.G[t][i + c.off[t]];
+        if (coef != T(0)) {
+            add += coef * diff;
+            any = true;
+        }
+        // psi of a cell that never updates it stays zero: only updated cells add it
+        if (psiTerm) {
+            T ps = c.psi[t][i];
+            ps = c.b[t][a] * ps + c.cpsi[t][a] * diff;
+            c.psi[t][i] = ps;
+            if (k.npsi[t]) {
+                add += T(k.npsi[t]) * c.dbpsi[t] * ps;
+                any = true;
+            }
+        }
+    }
+    if (any) {
+        if (k.toD) c.D[i] += add;
+        else c.U[i] += add;
+    }
+    if (EPASS && k.lor) {
+        T e = c.D[i];
+        e *= k.epsInv;
+        for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
+        c.U[i] = e;
+    }
+}
 
 template <typename T, bool EPASS>
 __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
@@ -23,251 +91,235 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
     const long long i = x + static_cast<long long>(p.lx) * (z + static_cast<long long>(p.lz) * y);
     const int coord[3] = {x, y, z};
 #pragma unroll
-    for (int ci = 0; ci < 3; ++ci) {
-        const Comp<T>& c = p.c[ci];
-        if (!c.present) continue;
-        const uint8_t code = c.code[i];
-        if (code == 0) continue;
-        if (code >= c.ncls) {
-            atomicOr(p.err, kErrClassCode);
-            continue;
-        }
-        const Class<T> k = c.cls[code];
-        if (EPASS && k.lor) {
-            if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
-                atomicOr(p.err, kErrPoleCount);
-                continue;
-            }
-            const T e = c.U[i];
-            const int s = p.poleStart[k.obj];
-            const int n = p.poleCount[k.obj];
-            for (int q = 0; q < n; ++q) {
-                const T old = c.P[q][i];
-                T np = p.alpha[s + q] * old;
-                np += p.xi[s + q] * c.Pprev[q][i];
-                np += p.gamma[s + q] * e;
-                c.P[q][i] = np;
-                c.Pprev[q][i] = old;
-            }
-        }
-        T add = T(0);
-        bool any = false;
-#pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            if (!c.tpresent[t]) continue;
-            const int a = coord[c.axis[t]];
-            const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? c.kprof[t][a] : T(0));
-            const bool psiTerm = c.hasPsi[t] && (k.psiUpd[t] || k.npsi[t]);
-            if (coef == T(0) && !psiTerm) continue;
-            const T diff = c.G[t][i] - c.G[t][i + c.off[t]];
-            if (coef != T(0)) {
-                add += coef * diff;
-                any = true;
-            }
-            if (c.hasPsi[t]) {
-                if (k.psiUpd[t]) {
-                    T ps = c.psi[t][i];
-                    ps = c.b[t][a] * ps + c.cpsi[t][a] * diff;
-                    c.psi[t][i] = ps;
-                    if (k.npsi[t]) {
-                        add += T(k.npsi[t]) * c.dbpsi[t] * ps;
-                        any = true;
-                    }
-                } else if (k.npsi[t]) {
-                    add += T(k.npsi[t]) * c.dbpsi[t] * c.psi[t][i];
-                    any = true;
-                }
-            }
-        }
-        if (any) {
-            if (k.toD) c.D[i] += add;
-            else c.U[i] += add;
-        }
-        if (EPASS && k.lor) {
-            T e = c.D[i];
-            e *= k.epsInv;
-            for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
-            c.U[i] = e;
-        }
-    }
+    for (int ci = 0; ci < 3; ++ci)
+        if (p.c[ci].present) cellGeneric<T, EPASS>(p, ci, i, coord);
+}
+
+// The dispersive (Lorentz) cells of the E pass, from a list: the interior form
+// leaves them out so that its common path stays small.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pass_lorentz(const Pass<T> p) {
+    const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    if (j >= p.nLor) return;
+    const long long i = p.lorCell[j];
+    const int x = static_cast<int>(i % p.lx);
+    const long long r = i / p.lx;
+    const int z = static_cast<int>(r % p.lz);
+    const int y = static_cast<int>(r / p.lz);
+    const int coord[3] = {x, y, z};
+    cellGeneric<T, true>(p, p.lorComp[j], i, coord);
 }
 
 // 3-D form of the same update for grids whose halo cells carry no update.
 // A block covers a 32 (x) by kP3BZ (z) tile of interior cells of one
-// component and walks kP3CY planes along y, the slowest axis of the layout.
-// The component (and with it the two derivative axes) is a template
-// parameter. Every load a cell needs in the common case (class code, the
-// field, both neighbour pairs, psi inside the slab) is issued before the class
-// is known, so a warp keeps several independent loads in flight; the class
-// only selects the arithmetic. The neighbour along y is carried in a register
-// from the previous plane. Per cell the arithmetic is the same as k_pass.
+// component and walks CY planes along y, the slowest axis of the layout. The
+// component (and with it the two derivative axes) is a template parameter.
+// Every load a cell needs (class code, the field, both neighbour pairs, psi
+// inside the slab) is issued before the class is known; the neighbour along y
+// is carried in a register from the previous plane, and the plane PD ahead is
+// prefetched into L2. A block decides once whether its tile and planes touch
+// the CPML slab of either of its component's terms: blocks that do not run the
+// plain path, with no profile or psi logic. The class table (FastClass:
+// coefficients folded on the host, flag bits) is read through the read-only
+// cache; the cells of a warp mostly share a class. Dispersive cells of the E
+// pass are left to k_pass_lorentz. Per cell the arithmetic is that of
+// cellGeneric.
 constexpr int kP3BZ = 8;
-constexpr int kP3CY = 16;
 
-template <typename T, bool EPASS, int CI, typename I>
-__device__ __forceinline__ void pass3d(const Pass<T>& p, const Class<T>* __restrict__ tab) {
+__device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
+template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML>
+__device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1) {
     constexpr int A0 = (CI + 2) % 3;  // derivative axis of term J
     constexpr int A1 = (CI + 1) % 3;  // derivative axis of term K
     constexpr int TY = (A0 == 1) ? 0 : ((A1 == 1) ? 1 : -1);  // term along y, or none
-    constexpr bool UP = !EPASS;       // H: neighbour at +1 ; E: neighbour at -1
     const Comp<T>& c = p.c[CI];
-    const int x = 1 + blockIdx.x * 32 + threadIdx.x;
-    const int z = 1 + blockIdx.y * kP3BZ + threadIdx.y;
-    const int y0 = 1 + (blockIdx.z / 3) * kP3CY;
-    if (x > p.lx - 2 || z > p.lz - 2 || y0 > p.ly - 2) return;
-    const int y1 = min(y0 + kP3CY, p.ly - 1);
     const I plane = static_cast<I>(p.lx) * p.lz;
     I i = x + static_cast<I>(p.lx) * (z + static_cast<I>(p.lz) * y0);
-
-    const uint8_t* __restrict__ code = c.code;
-    T* __restrict__ U = c.U;
-    const T* __restrict__ G[2] = {c.G[0], c.G[1]};
-    const I off[2] = {static_cast<I>(c.off[0]), static_cast<I>(c.off[1])};
-    // profile values of the terms along x or z are fixed for the thread
-    bool in[2] = {false, false};
-    T kp[2] = {T(0), T(0)}, bq[2] = {T(0), T(0)}, cq[2] = {T(0), T(0)};
+    const T* __restrict__ G0 = c.G[0];
+    const T* __restrict__ G1 = c.G[1];
+    const I off0 = static_cast<I>(c.off[0]);
+    const I off1 = static_cast<I>(c.off[1]);
+    // CPML profile of the terms along x or z at this thread's coordinate
+    bool inC[2] = {false, false};
+    T kpC[2] = {T(0), T(0)}, bqC[2] = {T(0), T(0)}, cqC[2] = {T(0), T(0)};
+    if (PML) {
 #pragma unroll
-    for (int t = 0; t < 2; ++t) {
-        const int ax = t == 0 ? A0 : A1;
-        if (ax == 1) continue;
-        const int a = ax == 0 ? x : z;
-        in[t] = a < c.slabLo[t] || a >= c.slabHi[t];
-        if (in[t]) {
-            kp[t] = c.kprof[t][a];
-            if (c.hasPsi[t]) {
-                bq[t] = c.b[t][a];
-                cq[t] = c.cpsi[t][a];
+        for (int t = 0; t < 2; ++t) {
+            const int ax = t == 0 ? A0 : A1;
+            if (ax == 1) continue;
+            const int a = ax == 0 ? x : z;
+            inC[t] = a < c.slabLo[t] || a >= c.slabHi[t];
+            if (inC[t]) {
+                kpC[t] = c.kprof[t][a];
+                if (c.hasPsi[t]) {
+                    bqC[t] = c.b[t][a];
+                    cqC[t] = c.cpsi[t][a];
+                }
             }
         }
     }
+    // field of the y term carried between planes: H holds G(y), E holds G(y-1)
     T carry = T(0);
-    if constexpr (TY >= 0) carry = UP ? G[TY][i] : G[TY][i - plane];
+    if constexpr (TY >= 0) carry = EPASS ? c.G[TY][i - plane] : c.G[TY][i];
 
     for (int y = y0; y < y1; ++y, i += plane) {
-        const uint8_t cd = code[i];
-        const T u = U[i];
+        if (PD > 0 && y + PD < y1) {
+            const I ip = i + PD * plane;
+            prefetchL2(c.code + ip);
+            prefetchL2(c.U + ip);
+            prefetchL2(G0 + ip);
+            prefetchL2(G1 + ip);
+        }
+        const uint8_t cd = c.code[i];
+        const T u = c.U[i];
         T g[2], n[2];
-#pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            if (t == TY) {
-                if (UP) {
-                    g[t] = carry;
-                    n[t] = G[t][i + plane];
-                    carry = n[t];
-                } else {
-                    g[t] = G[t][i];
-                    n[t] = carry;
-                    carry = g[t];
-                }
+        if (TY == 0) {
+            if (EPASS) {
+                g[0] = G0[i];
+                n[0] = carry;
+                carry = g[0];
             } else {
-                g[t] = G[t][i];
-                n[t] = G[t][i + off[t]];
+                g[0] = carry;
+                n[0] = G0[i + plane];
+                carry = n[0];
             }
+        } else {
+            g[0] = G0[i];
+            n[0] = G0[i + off0];
         }
-        if constexpr (TY >= 0) {
-            in[TY] = y < c.slabLo[TY] || y >= c.slabHi[TY];
-            kp[TY] = T(0);
-            if (in[TY]) {
-                kp[TY] = c.kprof[TY][y];
-                if (c.hasPsi[TY]) {
-                    bq[TY] = c.b[TY][y];
-                    cq[TY] = c.cpsi[TY][y];
+        if (TY == 1) {
+            if (EPASS) {
+                g[1] = G1[i];
+                n[1] = carry;
+                carry = g[1];
+            } else {
+                g[1] = carry;
+                n[1] = G1[i + plane];
+                carry = n[1];
+            }
+        } else {
+            g[1] = G1[i];
+            n[1] = G1[i + off1];
+        }
+        bool in[2] = {inC[0], inC[1]};
+        T kp[2] = {kpC[0], kpC[1]}, bq[2] = {bqC[0], bqC[1]}, cq[2] = {cqC[0], cqC[1]};
+        T ps[2] = {T(0), T(0)};
+        if (PML) {
+            if constexpr (TY >= 0) {
+                in[TY] = y < c.slabLo[TY] || y >= c.slabHi[TY];
+                kp[TY] = bq[TY] = cq[TY] = T(0);
+                if (in[TY]) {
+                    kp[TY] = c.kprof[TY][y];
+                    if (c.hasPsi[TY]) {
+                        bq[TY] = c.b[TY][y];
+                        cq[TY] = c.cpsi[TY][y];
+                    }
                 }
             }
-        }
-        T ps[2] = {T(0), T(0)};
 #pragma unroll
-        for (int t = 0; t < 2; ++t)
-            if (c.hasPsi[t] && in[t]) ps[t] = c.psi[t][i];
-
+            for (int t = 0; t < 2; ++t)
+                if (c.hasPsi[t] && in[t]) ps[t] = c.psi[t][i];
+        }
         if (cd == 0) continue;
         if (cd >= c.ncls) {
             atomicOr(p.err, kErrClassCode);
             continue;
         }
-        const Class<T>& k = tab[cd];
-        if (EPASS && k.lor) {
-            if (k.obj < 0 || k.obj >= p.nObj || p.poleCount[k.obj] > c.nPoles) {
-                atomicOr(p.err, kErrPoleCount);
-                continue;
-            }
-            const int s = p.poleStart[k.obj];
-            const int np = p.poleCount[k.obj];
-            for (int q = 0; q < np; ++q) {
-                const T old = c.P[q][i];
-                T v = p.alpha[s + q] * old;
-                v += p.xi[s + q] * c.Pprev[q][i];
-                v += p.gamma[s + q] * u;
-                c.P[q][i] = v;
-                c.Pprev[q][i] = old;
-            }
+        const FastClass<T>* kc = c.fcls + cd;
+        const T coef0 = kc->coef[0], coef1 = kc->coef[1];
+        const uint32_t fl = kc->flags;
+        if (EPASS && (fl & kFcLor)) continue;  // dispersive cells run in k_pass_lorentz
+        if (((fl & kFcSlab0) && !in[0]) || ((fl & kFcSlab1) && !in[1])) {
+            atomicOr(p.err, kErrSlab);
+            continue;
         }
         T add = T(0);
-        bool any = false;
+        if (PML) {
+            const T coef[2] = {coef0, coef1};
 #pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            if (!in[t] && (k.kflag[t] | k.psiUpd[t] | k.npsi[t])) {
-                atomicOr(p.err, kErrSlab);
-                continue;
-            }
-            const T coef = k.cint[t] + T(k.nplain[t]) * c.db[t] + (k.kflag[t] ? kp[t] : T(0));
-            const T diff = g[t] - n[t];
-            if (coef != T(0)) {
-                add += coef * diff;
-                any = true;
-            }
-            if (c.hasPsi[t] && in[t]) {
-                if (k.psiUpd[t]) {
+            for (int t = 0; t < 2; ++t) {
+                const T ct = (fl & (t == 0 ? kFcKp0 : kFcKp1)) ? coef[t] + kp[t] : coef[t];
+                const T diff = g[t] - n[t];
+                add += ct * diff;
+                if (fl & (t == 0 ? kFcPsi0 : kFcPsi1)) {
                     const T q = bq[t] * ps[t] + cq[t] * diff;
                     c.psi[t][i] = q;
-                    if (k.npsi[t]) {
-                        add += T(k.npsi[t]) * c.dbpsi[t] * q;
-                        any = true;
-                    }
-                } else if (k.npsi[t]) {
-                    add += T(k.npsi[t]) * c.dbpsi[t] * ps[t];
-                    any = true;
+                    add += kc->psiCoef[t] * q;
                 }
             }
+        } else {
+            add += coef0 * (g[0] - n[0]);
+            add += coef1 * (g[1] - n[1]);
         }
-        if (any) {
-            if (k.toD) c.D[i] += add;
-            else U[i] = u + add;
-        }
-        if (EPASS && k.lor) {
-            T e = c.D[i];
-            e *= k.epsInv;
-            for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
-            U[i] = e;
+        if (fl & kFcWrite) {
+            if (fl & kFcToD) c.D[i] += add;
+            else c.U[i] = u + add;
         }
     }
 }
 
-template <typename T, bool EPASS, typename I>
-__global__ void __launch_bounds__(256) k_pass3d(const Pass<T> p) {
-    __shared__ Class<T> tab[256];
+// Whether the block's tile or planes reach into the CPML slab of a term of component c.
+template <typename T>
+__device__ __forceinline__ bool blockTouchesSlab(const Comp<T>& c, int ci, int xa, int xb, int ya, int yb, int za, int zb) {
+    const int axes[2] = {(ci + 2) % 3, (ci + 1) % 3};
+    bool touch = false;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int lo = axes[t] == 0 ? xa : (axes[t] == 1 ? ya : za);
+        const int hi = axes[t] == 0 ? xb : (axes[t] == 1 ? yb : zb);
+        if (lo < c.slabLo[t] || hi >= c.slabHi[t]) touch = true;
+    }
+    return touch;
+}
+
+template <typename T, bool EPASS, int CI, typename I, int CY, int PD>
+__device__ __forceinline__ void pass3d(const Pass<T>& p) {
+    const int x = 1 + blockIdx.x * 32 + threadIdx.x;
+    const int z = 1 + blockIdx.y * kP3BZ + threadIdx.y;
+    const int y0 = 1 + (blockIdx.z / 3) * CY;
+    const int y1 = min(y0 + CY, p.ly - 1);
+    const int xa = 1 + blockIdx.x * 32, za = 1 + blockIdx.y * kP3BZ;
+    const bool pml = blockTouchesSlab(p.c[CI], CI, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, za,
+                                      min(za + kP3BZ - 1, p.lz - 2));
+    if (x > p.lx - 2 || z > p.lz - 2 || y0 > p.ly - 2) return;
+    if (pml) pass3dRun<T, EPASS, CI, I, CY, PD, true>(p, x, z, y0, y1);
+    else pass3dRun<T, EPASS, CI, I, CY, PD, false>(p, x, z, y0, y1);
+}
+
+template <typename T, bool EPASS, typename I, int CY, int PD>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (sizeof(I) == 4 ? 8 : 6) : 4) k_pass3d(const Pass<T> p) {
     const int ci = blockIdx.z % 3;
-    const Comp<T>& c = p.c[ci];
-    for (int q = threadIdx.x + threadIdx.y * 32; q < c.ncls; q += 32 * kP3BZ) tab[q] = c.cls[q];
-    __syncthreads();
-    if (ci == 0) pass3d<T, EPASS, 0, I>(p, tab);
-    else if (ci == 1) pass3d<T, EPASS, 1, I>(p, tab);
-    else pass3d<T, EPASS, 2, I>(p, tab);
+    if (ci == 0) pass3d<T, EPASS, 0, I, CY, PD>(p);
+    else if (ci == 1) pass3d<T, EPASS, 1, I, CY, PD>(p);
+    else pass3d<T, EPASS, 2, I, CY, PD>(p);
+}
+
+template <typename T, typename I, int CY, int PD>
+static void launch_pass3d(const Pass<T>& p, bool ePass, cudaStream_t s) {
+    dim3 block(32, kP3BZ, 1);
+    dim3 grid((p.lx - 2 + 31) / 32, (p.lz - 2 + kP3BZ - 1) / kP3BZ, 3 * ((p.ly - 2 + CY - 1) / CY));
+    if (ePass) k_pass3d<T, true, I, CY, PD><<<grid, block, 0, s>>>(p);
+    else k_pass3d<T, false, I, CY, PD><<<grid, block, 0, s>>>(p);
 }
 
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (p.interior3d) {
-        dim3 block(32, kP3BZ, 1);
-        dim3 grid((p.lx - 2 + 31) / 32, (p.lz - 2 + kP3BZ - 1) / kP3BZ, 3 * ((p.ly - 2 + kP3CY - 1) / kP3CY));
         if (p.index64) {
-            if (ePass) k_pass3d<T, true, long long><<<grid, block, 0, s>>>(p);
-            else k_pass3d<T, false, long long><<<grid, block, 0, s>>>(p);
+            launch_pass3d<T, long long, 16, 2>(p, ePass, s);
         } else {
-            if (ePass) k_pass3d<T, true, int><<<grid, block, 0, s>>>(p);
-            else k_pass3d<T, false, int><<<grid, block, 0, s>>>(p);
+            switch (p.shape) {
+            case 1: launch_pass3d<T, int, 16, 0>(p, ePass, s); break;
+            case 2: launch_pass3d<T, int, 32, 2>(p, ePass, s); break;
+            case 3: launch_pass3d<T, int, 32, 0>(p, ePass, s); break;
+            case 4: launch_pass3d<T, int, 8, 2>(p, ePass, s); break;
+            default: launch_pass3d<T, int, 16, 2>(p, ePass, s); break;
+            }
         }
+        if (ePass && p.nLor > 0)
+            k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else {
         // 2-D grids, and 3-D grids with updated halo cells: one thread per cell,
         // all components of the pass
@@ -330,17 +382,38 @@ void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step
     k_dft_sample<T><<<static_cast<unsigned>((d.npts + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(d, f, step);
 }
 
-constexpr int kFoldPts = 32;   // points per tile of the fold kernel
-constexpr int kFoldWarps = 8;  // 256 threads: lane -> frequency, warp -> 4 points of the tile
+// Fold of the ring into the accumulators: a block takes a tile of kFoldTP
+// points by kFoldTF frequencies; each thread keeps a 4-point by 4-frequency
+// register tile of FP-T partial sums (re and im) over all samples of the fold,
+// staged kFoldKS samples at a time through shared memory (samples and cos/-sin
+// rows), and adds the partial sums to the FP64 accumulators once at the end.
+// Per staged sample a thread does 32 FMAs for three 4-wide shared loads.
+constexpr int kFoldTP = 128;  // points per tile (32 threads x 4)
+constexpr int kFoldTF = 32;   // frequencies per tile (8 threads x 4)
+constexpr int kFoldKS = 32;   // samples per shared-memory stage
 
-// Fold of K ring samples into the accumulators. Shared memory holds the K
-// phasor rows (nfreq cos/-sin pairs each) and the tile's K x kFoldPts samples.
+__device__ __forceinline__ void lds4(const float* p, float v[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double v[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
                                                   int firstSample) {
-    extern __shared__ unsigned char smem_raw[];
-    T* ph = reinterpret_cast<T*>(smem_raw);          // [K][nfreq][2]
-    T* smp = ph + static_cast<long long>(d.K) * d.nfreq * 2;  // [K][kFoldPts]
+    __shared__ __align__(16) T smp[kFoldKS][kFoldTP];
+    __shared__ __align__(16) T pcos[kFoldKS][kFoldTF];
+    __shared__ __align__(16) T psin[kFoldKS][kFoldTF];
     int count, first;
     if (flushCount > 0) {
         count = flushCount;
@@ -354,65 +427,79 @@ __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int
         first = n - (d.K - 1);
     }
     const int nf = d.nfreq;
-    for (int q = threadIdx.x; q < count * nf * 2; q += blockDim.x)
-        ph[q] = d.phasor[static_cast<long long>(first) * nf * 2 + q];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const long long tiles = (d.npts + kFoldPts - 1) / kFoldPts;
+    const int tf = threadIdx.x & 7;   // frequencies 4*tf .. 4*tf+3 of the tile
+    const int tp = threadIdx.x >> 3;  // points 4*tp .. 4*tp+3 of the tile
+    const int fTiles = (nf + kFoldTF - 1) / kFoldTF;
+    const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * fTiles;
     for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const long long p0 = tile * kFoldPts;
-        __syncthreads();
-        for (int q = threadIdx.x; q < count * kFoldPts; q += blockDim.x) {
-            const int k = q / kFoldPts, pp = q % kFoldPts;
-            const long long p = p0 + pp;
-            const int slot = (first + k) % d.K;
-            smp[q] = (p < d.npts) ? d.ring[static_cast<long long>(slot) * d.npts + p] : T(0);
-        }
-        __syncthreads();
-        constexpr int PPW = kFoldPts / kFoldWarps;  // points per warp
-        for (int fb = 0; fb < nf; fb += 32) {
-            const int fq = fb + lane;
-            if (fq >= nf) break;
-            T are[PPW], aim[PPW];
+        const long long p0 = (tile / fTiles) * kFoldTP;
+        const int f0 = static_cast<int>(tile % fTiles) * kFoldTF;
+        T are[4][4], aim[4][4];
 #pragma unroll
-            for (int j = 0; j < PPW; ++j) are[j] = aim[j] = T(0);
-            for (int k = 0; k < count; ++k) {
-                const T c = ph[(k * nf + fq) * 2 + 0];
-                const T sn = ph[(k * nf + fq) * 2 + 1];
+        for (int j = 0; j < 4; ++j)
 #pragma unroll
-                for (int j = 0; j < PPW; ++j) {
-                    const T v = smp[k * kFoldPts + warp * PPW + j];
-                    are[j] += c * v;
-                    aim[j] += sn * v;
+            for (int m = 0; m < 4; ++m) are[j][m] = aim[j][m] = T(0);
+        for (int k0 = 0; k0 < count; k0 += kFoldKS) {
+            const int kn = min(kFoldKS, count - k0);
+            __syncthreads();
+            for (int q = threadIdx.x; q < kFoldKS * kFoldTP; q += blockDim.x) {
+                const int k = q / kFoldTP, pp = q % kFoldTP;
+                const long long p = p0 + pp;
+                T v = T(0);
+                if (k < kn && p < d.npts) {
+                    const int slot = (first + k0 + k) % d.K;
+                    v = d.ring[static_cast<long long>(slot) * d.npts + p];
                 }
+                smp[k][pp] = v;
             }
+            for (int q = threadIdx.x; q < kFoldKS * kFoldTF; q += blockDim.x) {
+                const int k = q / kFoldTF, ff = q % kFoldTF;
+                const int f = f0 + ff;
+                T c = T(0), sn = T(0);
+                if (k < kn && f < nf) {
+                    const T* ph = d.phasor + (static_cast<long long>(first + k0 + k) * nf + f) * 2;
+                    c = ph[0];
+                    sn = ph[1];
+                }
+                pcos[k][ff] = c;
+                psin[k][ff] = sn;
+            }
+            __syncthreads();
+            for (int k = 0; k < kn; ++k) {
+                T v[4], c[4], sn[4];
+                lds4(&smp[k][4 * tp], v);
+                lds4(&pcos[k][4 * tf], c);
+                lds4(&psin[k][4 * tf], sn);
 #pragma unroll
-            for (int j = 0; j < PPW; ++j) {
-                const long long p = p0 + warp * PPW + j;
-                if (p >= d.npts) continue;
-                d.re[p * nf + fq] += static_cast<double>(are[j]);
-                d.im[p * nf + fq] += static_cast<double>(aim[j]);
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        are[j][m] += c[m] * v[j];
+                        aim[j][m] += sn[m] * v[j];
+                    }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const long long p = p0 + 4 * tp + j;
+            if (p >= d.npts) continue;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int f = f0 + 4 * tf + m;
+                if (f >= nf) continue;
+                d.re[p * nf + f] += static_cast<double>(are[j][m]);
+                d.im[p * nf + f] += static_cast<double>(aim[j][m]);
             }
         }
     }
-}
-
-template <typename T>
-static size_t fold_smem(const DftTable<T>& d) {
-    return (static_cast<size_t>(d.K) * d.nfreq * 2 + static_cast<size_t>(d.K) * kFoldPts) * sizeof(T);
 }
 
 template <typename T>
 void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream) {
     if (d.npts == 0) return;
-    const size_t sm = fold_smem(d);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_dft_fold<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
-    const long long tiles = (d.npts + kFoldPts - 1) / kFoldPts;
-    const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
-    k_dft_fold<T><<<grid, 256, sm, static_cast<cudaStream_t>(stream)>>>(d, step, flushCount, firstSample);
+    const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
+    const unsigned grid = static_cast<unsigned>(tiles < 152 * 8 ? tiles : 152 * 8);
+    k_dft_fold<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, step, flushCount, firstSample);
 }
 
 __global__ void k_increment(int* step) { *step += 1; }
