@@ -643,15 +643,18 @@ private:
             const int nf = static_cast<int>(fp.spec.freqList.size());
             const int ti = fp.spec.timeInt;
             const int nSamples = P.nSteps / ti + 1;
-            std::vector<T> ph(static_cast<std::size_t>(nSamples) * nf * 2);
+            const int nfPad = (nf + 31) / 32 * 32;
+            std::vector<T> ph(static_cast<std::size_t>(nSamples) * nfPad * 2, T(0));
             for (int n = 0; n < nSamples; ++n)
                 for (int f = 0; f < nf; ++f) {
                     std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * fp.spec.freqList[f]));
-                    ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 0] = static_cast<T>(e.real());
-                    ph[(static_cast<std::size_t>(n) * nf + f) * 2 + 1] = static_cast<T>(e.imag());
+                    ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 0] = static_cast<T>(e.real());
+                    ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 1] = static_cast<T>(e.imag());
                 }
             const int K = dftBlockLength(static_cast<long long>(cell.size()), nSamples);
             d.npts = static_cast<long long>(cell.size());
+            d.stride = (d.npts + 127) / 128 * 128;
+            d.nfreqPad = nfPad;
             d.nfreq = nf;
             d.timeInt = ti;
             d.K = K;
@@ -659,7 +662,7 @@ private:
             d.comp = mem_.upload(comp);
             d.cell = mem_.upload(cell);
             d.phasor = mem_.upload(ph);
-            d.ring = mem_.alloc<T>(cell.size() * static_cast<std::size_t>(K));
+            d.ring = mem_.alloc<T>(static_cast<std::size_t>(d.stride) * static_cast<std::size_t>(K));
             d.re = mem_.alloc<double>(cell.size() * nf);
             d.im = mem_.alloc<double>(cell.size() * nf);
             dft_.push_back(d);

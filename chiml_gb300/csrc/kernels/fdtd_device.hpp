@@ -143,10 +143,12 @@ struct DftTable {
     int timeInt;
     int K;                      // samples per block
     int nSamples;               // samples a full run takes (phasor rows)
+    int nfreqPad;               // frequencies per phasor row, a multiple of 32 (zero-filled past nfreq)
+    long long stride;           // ring row pitch: points rounded up to a multiple of 128
     const int* comp;            // per point
     const int* cell;            // per point (grid index)
-    const T* phasor;            // [(sample * nfreq + f) * 2 + {0: cos, 1: -sin}]
-    T* ring;                    // [K][npts]
+    const T* phasor;            // [(sample * nfreqPad + f) * 2 + {0: cos, 1: -sin}]
+    T* ring;                    // [K][stride]
     double* re;                 // [pt * nfreq + f]
     double* im;
 };

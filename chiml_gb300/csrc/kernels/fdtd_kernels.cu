@@ -372,8 +372,8 @@ __global__ void __launch_bounds__(256) k_dft_sample(const DftTable<T> d, const F
     const long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     const int st = *step;
     if (st % d.timeInt != 0 || p >= d.npts) return;
-    const int slot = (st / d.timeInt) % d.K;
-    d.ring[static_cast<long long>(slot) * d.npts + p] = f.f[d.comp[p]][d.cell[p]];
+    const int slot = (st / d.timeInt) & (d.K - 1);
+    d.ring[static_cast<long long>(slot) * d.stride + p] = f.f[d.comp[p]][d.cell[p]];
 }
 
 template <typename T>
@@ -384,13 +384,26 @@ void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step
 
 // Fold of the ring into the accumulators: a block takes a tile of kFoldTP
 // points by kFoldTF frequencies; each thread keeps a 4-point by 4-frequency
-// register tile of FP-T partial sums (re and im) over all samples of the fold,
-// staged kFoldKS samples at a time through shared memory (samples and cos/-sin
-// rows), and adds the partial sums to the FP64 accumulators once at the end.
-// Per staged sample a thread does 32 FMAs for three 4-wide shared loads.
+// register tile of FP-T partial sums (re and im) over all samples of the fold
+// and adds them to the FP64 accumulators once at the end. Samples and phasor
+// rows are staged kFoldKS samples at a time into two shared-memory buffers by
+// 16-byte cp.async copies, so the next stage loads while this one computes.
+// Per staged sample a thread does 32 FMAs for three 16-byte shared loads.
 constexpr int kFoldTP = 128;  // points per tile (32 threads x 4)
 constexpr int kFoldTF = 32;   // frequencies per tile (8 threads x 4)
-constexpr int kFoldKS = 32;   // samples per shared-memory stage
+
+template <typename T>
+struct FoldCfg {
+    static constexpr int KS = sizeof(T) == 4 ? 32 : 16;  // samples per stage: 2 stages fit 48 KB
+};
+
+__device__ __forceinline__ void cpAsync16(void* dst, const void* src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 __device__ __forceinline__ void lds4(const float* p, float v[4]) {
     const float4 q = *reinterpret_cast<const float4*>(p);
@@ -411,9 +424,10 @@ __device__ __forceinline__ void lds4(const double* p, double v[4]) {
 template <typename T>
 __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
                                                   int firstSample) {
-    __shared__ __align__(16) T smp[kFoldKS][kFoldTP];
-    __shared__ __align__(16) T pcos[kFoldKS][kFoldTF];
-    __shared__ __align__(16) T psin[kFoldKS][kFoldTF];
+    constexpr int KS = FoldCfg<T>::KS;
+    constexpr int EV = 16 / sizeof(T);  // values per 16-byte copy
+    __shared__ __align__(16) T smp[2][KS][kFoldTP];
+    __shared__ __align__(16) T ph[2][KS][kFoldTF * 2];  // cos, -sin pairs
     int count, first;
     if (flushCount > 0) {
         count = flushCount;
@@ -431,45 +445,51 @@ __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int
     const int tp = threadIdx.x >> 3;  // points 4*tp .. 4*tp+3 of the tile
     const int fTiles = (nf + kFoldTF - 1) / kFoldTF;
     const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * fTiles;
+    const int stages = (count + KS - 1) / KS;
     for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const long long p0 = (tile / fTiles) * kFoldTP;
         const int f0 = static_cast<int>(tile % fTiles) * kFoldTF;
+        // copies of stage s into buffer s & 1 (the ring pitch and the phasor rows are 16-byte multiples)
+        auto issue = [&](int sg) {
+            const int b = sg & 1;
+            const int k0 = sg * KS;
+            const int kn = min(KS, count - k0);
+            for (int q = threadIdx.x; q < KS * (kFoldTP / EV); q += blockDim.x) {
+                const int k = q / (kFoldTP / EV), c = q % (kFoldTP / EV);
+                if (k < kn) {
+                    const int slot = (first + k0 + k) & (d.K - 1);
+                    cpAsync16(&smp[b][k][c * EV], d.ring + static_cast<long long>(slot) * d.stride + p0 + c * EV);
+                }
+            }
+            for (int q = threadIdx.x; q < KS * (kFoldTF * 2 / EV); q += blockDim.x) {
+                const int k = q / (kFoldTF * 2 / EV), c = q % (kFoldTF * 2 / EV);
+                if (k < kn)
+                    cpAsync16(&ph[b][k][c * EV],
+                              d.phasor + (static_cast<long long>(first + k0 + k) * d.nfreqPad + f0) * 2 + c * EV);
+            }
+            cpAsyncCommit();
+        };
         T are[4][4], aim[4][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j)
 #pragma unroll
             for (int m = 0; m < 4; ++m) are[j][m] = aim[j][m] = T(0);
-        for (int k0 = 0; k0 < count; k0 += kFoldKS) {
-            const int kn = min(kFoldKS, count - k0);
+        __syncthreads();  // the previous tile's last stage is no longer read
+        issue(0);
+        for (int sg = 0; sg < stages; ++sg) {
+            if (sg + 1 < stages) issue(sg + 1);
+            else cpAsyncCommit();
+            cpAsyncWait1();
             __syncthreads();
-            for (int q = threadIdx.x; q < kFoldKS * kFoldTP; q += blockDim.x) {
-                const int k = q / kFoldTP, pp = q % kFoldTP;
-                const long long p = p0 + pp;
-                T v = T(0);
-                if (k < kn && p < d.npts) {
-                    const int slot = (first + k0 + k) % d.K;
-                    v = d.ring[static_cast<long long>(slot) * d.npts + p];
-                }
-                smp[k][pp] = v;
-            }
-            for (int q = threadIdx.x; q < kFoldKS * kFoldTF; q += blockDim.x) {
-                const int k = q / kFoldTF, ff = q % kFoldTF;
-                const int f = f0 + ff;
-                T c = T(0), sn = T(0);
-                if (k < kn && f < nf) {
-                    const T* ph = d.phasor + (static_cast<long long>(first + k0 + k) * nf + f) * 2;
-                    c = ph[0];
-                    sn = ph[1];
-                }
-                pcos[k][ff] = c;
-                psin[k][ff] = sn;
-            }
-            __syncthreads();
+            const int b = sg & 1;
+            const int kn = min(KS, count - sg * KS);
             for (int k = 0; k < kn; ++k) {
-                T v[4], c[4], sn[4];
-                lds4(&smp[k][4 * tp], v);
-                lds4(&pcos[k][4 * tf], c);
-                lds4(&psin[k][4 * tf], sn);
+                T v[4], cs0[4], cs1[4];
+                lds4(&smp[b][k][4 * tp], v);
+                lds4(&ph[b][k][8 * tf], cs0);      // cos f, -sin f, cos f+1, -sin f+1
+                lds4(&ph[b][k][8 * tf + 4], cs1);  // f+2, f+3
+                const T c[4] = {cs0[0], cs0[2], cs1[0], cs1[2]};
+                const T sn[4] = {cs0[1], cs0[3], cs1[1], cs1[3]};
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -478,7 +498,9 @@ __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int
                         aim[j][m] += sn[m] * v[j];
                     }
             }
+            __syncthreads();  // buffer b is free for stage sg + 2
         }
+        cpAsyncWait0();
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const long long p = p0 + 4 * tp + j;
@@ -498,7 +520,7 @@ template <typename T>
 void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream) {
     if (d.npts == 0) return;
     const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
-    const unsigned grid = static_cast<unsigned>(tiles < 152 * 8 ? tiles : 152 * 8);
+    const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
     k_dft_fold<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, step, flushCount, firstSample);
 }
 
