@@ -31,6 +31,11 @@ sys.path.insert(0, ROOT)
 
 N_DEFAULT = 256
 
+# DRAM bytes of one launch per physical cell, split form of this workload, measured with
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum, --cache-control none) at 256^3:
+# H pass 749.6 MB, E pass (main kernel 757.5 MB + dispersive-cell list 41.1 MB) 798.6 MB.
+MEASURED_TRAFFIC_PER_CELL = {"h_pass": 749.6e6 / 16777216, "e_pass": 798.6e6 / 16777216}
+
 
 def _peaks():
     try:
@@ -227,7 +232,10 @@ def run_ours(args):
                      "kernel_ms": {k: round(v, 4) for k, v in fp_prof.items()}},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "traffic": None, "bytes_per_launch": dom_bytes,
+                         "traffic": (round(MEASURED_TRAFFIC_PER_CELL[dom] * cells, 0)
+                                     if dom in MEASURED_TRAFFIC_PER_CELL else None),
+                         "traffic_source": "ncu dram bytes per cell at 256^3, scaled to this workload's cells",
+                         "bytes_per_launch": dom_bytes,
                          "step_bytes_per_cell": round(sp["stats"].bytes_per_cell_update, 2),
                          "kernel_ms": {k: round(v, 4) for k, v in per_launch.items()}},
             "gpu_launches": launches,

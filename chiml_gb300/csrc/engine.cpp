@@ -6,7 +6,6 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
-#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -564,10 +563,6 @@ private:
                 pass.nLor = static_cast<long long>(li.size());
                 pass.lorComp = mem_.upload(lc);
                 pass.lorCell = mem_.upload(li);
-            }
-            {
-                const char* sh = std::getenv("CHIML_P3SHAPE");
-                pass.shape = sh ? std::atoi(sh) : 0;
             }
         }
         (void)bytes;

@@ -92,7 +92,6 @@ struct Pass {
     // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
     int interior3d;
     int index64;            // grid too large for 32-bit cell indices
-    int shape;              // tile shape of the interior form
     // dispersive cells of the E pass, run by their own kernel in the interior form
     long long nLor;
     const int* lorComp;

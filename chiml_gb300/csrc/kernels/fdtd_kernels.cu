@@ -310,13 +310,7 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
         if (p.index64) {
             launch_pass3d<T, long long, 16, 2>(p, ePass, s);
         } else {
-            switch (p.shape) {
-            case 1: launch_pass3d<T, int, 16, 0>(p, ePass, s); break;
-            case 2: launch_pass3d<T, int, 32, 2>(p, ePass, s); break;
-            case 3: launch_pass3d<T, int, 32, 0>(p, ePass, s); break;
-            case 4: launch_pass3d<T, int, 8, 2>(p, ePass, s); break;
-            default: launch_pass3d<T, int, 16, 2>(p, ePass, s); break;
-            }
+            launch_pass3d<T, int, 16, 2>(p, ePass, s);
         }
         if (ePass && p.nLor > 0)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
