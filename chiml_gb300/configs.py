@@ -52,6 +52,38 @@ def drude_lorentz_pols(wp_ev, poles):
     return out
 
 
+def emitter_level(e_cen_ev, dist="Delta_Fxn", nstates=1, width_ev=None, levs=1):
+    """One Energy_Levels entry (parallelInputs.cpp:465-579): centre in eV, optional
+    broadening (a distribution sampled at nstates equispaced energies over +-2 widths)."""
+    d = {"E_cen": [e_cen_ev], "distribution": dist, "nstates": nstates, "levs_described": levs}
+    if width_ev is not None:
+        d["dist_width"] = [width_ev]
+        d["BandWith"] = 4.0 * width_ev
+    return d
+
+
+def emitter_obj(shape, loc, basis, levels, couplings, relax, mol_den, eps=1.0, dtc_levs=(), output_pol=None,
+                dtc_base="out/qe_", **geo):
+    """An object holding quantum emitters (parallelInputs.cpp:425-662): (l, m) basis,
+    energy levels, coupling matrix, relaxation channels (state_i, state_f, rate 1/s,
+    dephasing rate 1/s), molecular density (1/m^3), population detectors and the
+    polarisation output file."""
+    o = _obj(shape, loc, material="custom", eps=eps, pols=[], **geo)
+    o["Basis_Set"] = [{"l": l, "m": m} for (l, m) in basis]
+    o["mol_den"] = mol_den
+    o["Energy_Levels"] = list(levels)
+    o["couplings"] = [float(c) for c in couplings]
+    o["gam"] = []
+    o["RelaxationOperators"] = [{"state_i": i, "state_f": f, "rate": r, "dephasing_rate": d} for (i, f, r, d) in relax]
+    o["dtc_levs"] = list(dtc_levs)
+    o["levDTC_timeInt"] = 1
+    o["dtc_pop_fname_base"] = dtc_base
+    if output_pol:
+        o["output_pol"] = True
+        o["output_pol_filename"] = output_pol
+    return o
+
+
 def config1(n=400, pml=20, steps=4000, radius_cells=50, src_gap_cells=60, ndtc=8, nfreq=100):
     """2-D TMz (Ez, Hx, Hy), dielectric disk eps=2.25, Ez point source, 8 point detectors, flux line."""
     dx = 0.05

@@ -196,9 +196,7 @@ Object read_object(const JNode& node, const Inputs& ip) {
             o.coord[ii * 3 + jj] = dot / std::sqrt(s);
         }
     }
-    if (node.child("Basis_Set").size() > 0)
-        throw UnsupportedError("quantum-emitter objects (Basis_Set) are not supported by this build");
-    o.ML = false;
+    o.ML = node.child("Basis_Set").size() > 0;
     std::string s = node.get<std::string>("shape");
     if (s == "block") {
         o.shape = Shape::BLOCK;
@@ -225,6 +223,164 @@ Object read_object(const JNode& node, const Inputs& ip) {
     }
     o.geoML = o.geo;
     return o;
+}
+
+// Adds buffer cells around an emitter object so that the polarisation points, which sit
+// between grid points, are inside it (Obj::addMLBuff, OBJECTS/Obj.hpp:537,653,776,949).
+void add_ml_buffer(Object& o, double d) {
+    switch (o.shape) {
+        case Shape::SPHERE: o.geoML[0] += 3.0 * d; break;
+        case Shape::BLOCK:
+        case Shape::ELLIPSOID:
+            o.geoML[0] += 3.0 * d;
+            o.geoML[1] += 3.0 * d;
+            o.geoML[2] += 3.0 * d;
+            break;
+        case Shape::CYLINDER:
+            o.geoML[0] += 3.0 * d;
+            o.geoML[1] += 3.0 * d;
+            break;
+    }
+}
+
+// Inhomogeneous-broadening weight functions (UTIL/ML_Dist_Fxn.hpp): the normal density,
+// its log-normal and skew-normal forms.
+static double norm_dist(double x, double cen, double w) {
+    return 1.0 / std::sqrt(2 * M_PI * std::pow(w, 2.0)) * std::exp(-1.0 * std::pow(x - cen, 2.0) / (2.0 * std::pow(w, 2.0)));
+}
+static double log_norm_dist(double x, double cen, double w) {
+    return (x <= cen) ? 0.0
+                      : 1.0 / std::sqrt(2 * M_PI * std::pow(w * x, 2.0)) *
+                            std::exp(-1.0 * std::pow(std::log(x) - cen, 2.0) / (2.0 * std::pow(w, 2.0)));
+}
+static double skew_norm_dist(double x, double cen, double w, double skew) {
+    return norm_dist(x, cen, w) * 0.5 * (1.0 + std::erf(skew * (x - cen) / (std::sqrt(2.0) * w)));
+}
+
+enum class LevelDist { GAUSSIAN, DELTA, SKEW_NORMAL, LOG_NORMAL, EXP_POW, GEN_SKEW_NORMAL };
+
+// parallelProgramInputs::string2dist, parallelInputs.cpp:903-919
+static LevelDist string2dist(const std::string& d) {
+    if (d == "Gaussian" || d == "gaussian") return LevelDist::GAUSSIAN;
+    if (d == "delta_fxn" || d == "Delta_fxn" || d == "Delta_Fxn" || d == "delta_Fxn" || d == "DeltaFxn") return LevelDist::DELTA;
+    if (d == "skew_normal" || d == "Skew_Normal" || d == "Skew_normal" || d == "skew_Normal") return LevelDist::SKEW_NORMAL;
+    if (d == "log_normal" || d == "Log_Normal" || d == "Log_normal" || d == "log_Normal") return LevelDist::LOG_NORMAL;
+    if (d == "exp_pow" || d == "Exp_Pow" || d == "Exp_pow" || d == "exp_Pow") return LevelDist::EXP_POW;
+    if (d == "gen_skew_normal" || d == "Gen_Skew_Normal" || d == "Gen_Skew_normal" || d == "gen_skew_Normal")
+        return LevelDist::GEN_SKEW_NORMAL;
+    throw InputError("The distribution type " + d + " is not defined, please define it for me.");
+}
+
+// The emitter part of an object (parallelInputs.cpp:425-662): removes the points of earlier
+// emitters that this object covers, then, when the object has a basis set, reads its levels,
+// couplings, relaxation and outputs, lists its grid points and buffers its geometry.
+void read_emitter(const JNode& node, Object& o, Inputs& ip) {
+    std::vector<std::array<int, 2>> basis;
+    for (auto& kv : node.child("Basis_Set").kids)
+        basis.push_back({kv.second.get<int>("l"), kv.second.get<int>("m")});
+    const int nx = find_pt(ip.size[0], ip.d[0]) + 1;
+    const int ny = find_pt(ip.size[1], ip.d[1]) + 1;
+    const int nz = find_pt(ip.size[2], ip.d[2]) + 1;
+    const double dminAll = *std::min_element(ip.d.begin(), ip.d.end());
+    // points of earlier emitters inside this object are dropped (the position used here is
+    // one cell below the one used when the points were listed, as in the reference)
+    for (auto& em : ip.emitters) {
+        for (std::size_t ll = 0; ll < em.locs.size(); ++ll) {
+            std::array<double, 3> loc = {(em.locs[ll][0] - (nx - 1) / 2.0 - 1) * ip.d[0],
+                                         (em.locs[ll][1] - (ny - 1) / 2.0 - 1) * ip.d[1],
+                                         (em.locs[ll][2] - (nz - 1) / 2.0 - 1) * ip.d[2]};
+            if (o.isObj(loc, dminAll, o.geo)) {
+                em.locs.erase(em.locs.begin() + ll);
+                --ll;
+            }
+        }
+    }
+    if (basis.empty()) return;
+    if (!ip.emitters.empty())
+        throw UnsupportedError("more than one emitter object (the reference pools their energy levels)");
+    const double eConv = kElementaryCharge * kEps0 * std::pow(kSpeedOfLight / ip.I0, 2) / ip.a;
+    EmitterSpec em;
+    em.object = static_cast<int>(ip.objects.size());
+    em.basis = basis;
+    em.molDen = node.get<double>("mol_den", 1.0);
+    const int numElProportion = node.get<int>("numElectorn", 1);
+    for (auto& kv : node.child("Energy_Levels").kids) {
+        const JNode& lev = kv.second;
+        EnergyLevel level;
+        std::vector<double> eCen = as_vector(lev, "E_cen");
+        for (auto& e : eCen) e *= eConv;
+        std::vector<double> wVec = as_vector(lev, "weights", 1.0, static_cast<int>(eCen.size()));
+        const LevelDist dist = string2dist(lev.get<std::string>("distribution", "Delta_Fxn"));
+        const int nstates = lev.get<int>("nstates", 1);
+        const double top = lev.get<double>("highEdge", eCen[0] / eConv + lev.get<double>("BandWith", 0.0) / 2.0) * eConv;
+        const double bot = lev.get<double>("lowEdge", eCen[0] / eConv - lev.get<double>("BandWith", 0.0) / 2.0) * eConv;
+        const int numLevs = lev.get<int>("levs_described", 1);
+        if (dist == LevelDist::DELTA || nstates == 1) {
+            if (nstates > 1) throw InputError("The number of states is greater than one for a delta function distribution.");
+            level.weights = wVec;
+            level.energyStates = eCen;
+        } else {
+            double weightSum = 0.0;
+            for (int n = 0; n < nstates; ++n) level.energyStates.push_back(bot + n * (top - bot) / (nstates - 1.0));
+            for (double es : level.energyStates) {
+                std::vector<double> width = as_vector(lev, "dist_width");
+                for (auto& w : width) w *= eConv;
+                if (width.size() != eCen.size())
+                    throw InputError("The center frequency and distribution width is not the same size.");
+                double weight = 0.0;
+                if (dist == LevelDist::GAUSSIAN) {
+                    for (std::size_t i = 0; i < width.size(); ++i) weight += wVec[i] * norm_dist(es, eCen[i], width[i]);
+                } else if (dist == LevelDist::LOG_NORMAL) {
+                    for (std::size_t i = 0; i < width.size(); ++i) weight += wVec[i] * log_norm_dist(es, eCen[i], width[i]);
+                } else if (dist == LevelDist::SKEW_NORMAL) {
+                    std::vector<double> skew = as_vector(lev, "skew_factor");
+                    if (skew.size() != eCen.size())
+                        throw InputError("The center frequency and skew factor do not have the same size.");
+                    for (std::size_t i = 0; i < width.size(); ++i)
+                        weight += wVec[i] * skew_norm_dist(es, eCen[i], width[i], skew[i]);
+                } else {
+                    throw UnsupportedError("generalised skew-normal and exponential-power level distributions are not supported");
+                }
+                level.weights.push_back(weight);
+                weightSum += weight;
+            }
+            for (auto& w : level.weights) w /= weightSum / static_cast<double>(numElProportion);
+        }
+        level.levDescribed = numLevs;
+        ip.qeELevs.push_back(level);
+    }
+    for (auto& kv : node.child("couplings").kids)
+        em.couplings.push_back(kv.second.value<double>() * 1.0e-21 / std::pow(ip.a, 2.0) / ip.I0);
+    for (auto& kv : node.child("gam").kids) {
+        std::vector<double> g;
+        for (auto& gg : kv.second.child("g").kids) g.push_back(gg.second.value<double>() * ip.a / kSpeedOfLight);
+        em.gam.push_back(g);
+    }
+    // grid points of the object (parallelInputs.cpp:596-614)
+    for (int zz = 0; zz < nz; ++zz)
+        for (int yy = 0; yy < ny; ++yy)
+            for (int xx = 0; xx < nx; ++xx) {
+                std::array<double, 3> pt = {(xx - (nx - 1) / 2.0) * ip.d[0], (yy - (ny - 1) / 2.0) * ip.d[1],
+                                            (zz - (nz - 1) / 2.0) * ip.d[2]};
+                if (o.isObj(pt, dminAll, o.geo)) em.locs.push_back({xx, yy, zz});
+            }
+    for (auto& kv : node.child("RelaxationOperators").kids) {
+        RelaxOp r;
+        r.n0 = kv.second.get<int>("state_i");
+        r.nf = kv.second.get<int>("state_f");
+        r.rate = kv.second.get<double>("rate") * ip.a / kSpeedOfLight;
+        r.dephasing = kv.second.get<double>("dephasing_rate", 0.0) * ip.a / kSpeedOfLight;
+        em.relax.push_back(r);
+    }
+    em.outputPol = node.get<bool>("output_pol", false);
+    if (em.outputPol) em.polFile = node.get<std::string>("output_pol_filename");
+    for (auto& kv : node.child("dtc_levs").kids) em.dtcLevs.push_back(kv.second.value<int>());
+    em.dtcTimeInt = node.get<int>("levDTC_timeInt", 1);
+    const std::string base = node.get<std::string>("dtc_pop_fname_base", "output_data/qe_");
+    for (int lv : em.dtcLevs)
+        em.dtcFiles.push_back(base + std::to_string(ip.emitters.size()) + "_level_" + std::to_string(lv) + ".dat");
+    add_ml_buffer(o, *std::max_element(ip.d.begin(), ip.d.end()));
+    ip.emitters.push_back(em);
 }
 
 std::vector<double> read_freq_list(const JNode& n, const char* what) {
@@ -338,7 +494,11 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
     }
     // Objects, parallelInputs.cpp:410-666; objArr_[0] is the vacuum block of the whole cell
     ip.objects.push_back(make_vacuum_block(ip.size));
-    for (auto& kv : IP.child("ObjectList").kids) ip.objects.push_back(read_object(kv.second, ip));
+    for (auto& kv : IP.child("ObjectList").kids) {
+        Object o = read_object(kv.second, ip);
+        read_emitter(kv.second, o, ip);
+        ip.objects.push_back(o);
+    }
     // Detectors, parallelInputs.cpp:667-755
     int ii = 0;
     for (auto& kv : IP.child("DetectorList").kids) {

@@ -101,6 +101,39 @@ struct FluxSpec {
     std::string incdFile;
 };
 
+// One energy-level descriptor of the emitters (EnergyLevelDiscriptor; built in
+// parallelInputs.cpp:465-579): the energies it can take (FDTD units), their weights,
+// and how many basis levels it describes.
+struct EnergyLevel {
+    std::vector<double> energyStates;
+    std::vector<double> weights;
+    int levDescribed = 1;
+};
+
+// One relaxation channel of an emitter (relaxParams, ML/parallelQE.hpp:22-28); rates in FDTD units.
+struct RelaxOp {
+    int n0 = 0, nf = 0;
+    double rate = 0.0, dephasing = 0.0;
+};
+
+// A quantum-emitter object (parallelInputs.cpp:453-660): the object index, its
+// (l, m) basis, molecular density, transition-dipole couplings (FDTD units), the
+// relaxation matrix or channels, the grid points it holds, and its outputs.
+struct EmitterSpec {
+    int object = -1;
+    std::vector<std::array<int, 2>> basis;
+    double molDen = 1.0;
+    std::vector<double> couplings;
+    std::vector<std::vector<double>> gam;  // given relaxation matrix (may be empty)
+    std::vector<RelaxOp> relax;
+    std::vector<std::array<int, 3>> locs;  // physical grid points, z outermost then y then x
+    bool outputPol = false;
+    std::string polFile;
+    std::vector<int> dtcLevs;
+    std::vector<std::string> dtcFiles;
+    int dtcTimeInt = 1;
+};
+
 struct Inputs {
     std::string filename;
     Pol pol = Pol::EZ;
@@ -114,6 +147,9 @@ struct Inputs {
     std::vector<Object> objects;  // objects[0] is the vacuum cell block
     std::vector<DetectorSpec> detectors;
     std::vector<FluxSpec> fluxes;
+    // energy-level descriptors of all emitters together (the reference keeps one list, qeELevs_)
+    std::vector<EnergyLevel> qeELevs;
+    std::vector<EmitterSpec> emitters;
 
     int nSteps() const;
 };

@@ -1,5 +1,6 @@
 #include "outputs.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <fstream>
@@ -311,6 +312,44 @@ void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) 
                   << std::real(flux) << "\t" << std::setw(16) << std::setprecision(15) << std::imag(flux) << std::endl;
             else
                 f << std::endl;
+        }
+    }
+}
+
+void write_emitters(const Plan& P, const RunRecord& R, const std::string& outDir) {
+    for (std::size_t q = 0; q < P.emitters.size(); ++q) {
+        const EmitterPlan& e = P.emitters[q];
+        if (e.outputPol && q < R.emitterP.size()) {
+            const auto& tp = R.emitterP[q];
+            std::ofstream f(out_path(outDir, e.polFile));
+            if (!f) throw std::runtime_error("cannot open " + e.polFile);
+            const std::size_t iterMax = std::max(tp[0].size(), tp[2].size());
+            for (std::size_t ii = 0; ii < iterMax; ++ii) {
+                f << e.dt * static_cast<double>(ii);
+                double px = 0, py = 0, pz = 0;
+                if (!tp[0].empty()) {
+                    px += tp[0][ii];
+                    py += tp[1][ii];
+                    f << '\t' << px << '\t' << py;
+                }
+                if (!tp[2].empty()) {
+                    pz += tp[2][ii];
+                    f << '\t' << pz;
+                }
+                f << '\t' << std::sqrt(std::pow(px, 2) + std::pow(py, 2) + std::pow(pz, 2)) << '\n';
+            }
+        }
+        for (std::size_t d = 0; d < e.dtcFiles.size() && q < R.emitterPop.size() && d < R.emitterPop[q].size(); ++d) {
+            std::ofstream f(out_path(outDir, e.dtcFiles[d]));
+            if (!f) throw std::runtime_error("cannot open " + e.dtcFiles[d]);
+            const auto& pop = R.emitterPop[q][d];
+            for (std::size_t tt = 0; tt < pop.size(); ++tt) {
+                const cplx v = pop[tt];
+                f << std::setw(9) << std::setprecision(9) << static_cast<double>(tt) * e.dtcTimeInt * e.dt << "\t"
+                  << std::setw(16) << std::setprecision(16) << std::real(v) << "\t" << std::setw(16)
+                  << std::setprecision(16) << std::imag(v) << "\t" << std::setw(16) << std::setprecision(16)
+                  << std::abs(v) << std::endl;
+            }
         }
     }
 }

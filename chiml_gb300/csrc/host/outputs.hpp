@@ -17,6 +17,10 @@ struct RunRecord {
     // flux accumulators per flux: re/im [point][freq], and the number of DFT samples
     std::vector<std::vector<double>> fluxRe, fluxIm;
     std::vector<int> fluxSamples;
+    // per emitter: the total polarisation of each coupled component, one value per step
+    // (parallelQE.cpp:41-44 accumP_), and per population detector its events
+    std::vector<std::array<std::vector<double>, 3>> emitterP;
+    std::vector<std::vector<std::vector<cplx>>> emitterPop;
 };
 
 // Number of values one output event of detector k stores.
@@ -28,6 +32,10 @@ int detector_events(const DetectorPlan& dp, int nSteps);
 void write_detectors(const Plan& P, const RunRecord& R, const std::string& outDir, int stepsDone);
 // Combines the flux accumulators and writes "<name>.dat" (parallelFlux.hpp:325-560).
 void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir);
+
+// Writes the emitter polarisation file (parallelQEReal::outputPol, parallelQE.cpp:520-557) and
+// the population files (QEPopDtc::toFile, QEPopDtc.cpp:37-61).
+void write_emitters(const Plan& P, const RunRecord& R, const std::string& outDir);
 
 std::string out_path(const std::string& outDir, const std::string& name);
 

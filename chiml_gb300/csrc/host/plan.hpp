@@ -137,6 +137,43 @@ struct FluxPlan {
     bool real3D = false;
 };
 
+// The emitters of one object, ready to step (ML/parallelQE.hpp, parallelQE.cpp). Each
+// emitter cell holds one density matrix per ensemble member (one Hamiltonian per
+// combination of level energies, ML/Hamiltonian.cpp). Matrices are nlevel x nlevel,
+// stored flat as the reference does (element i + nlevel*j is row i, column j of the
+// column-major BLAS calls).
+struct EmitterPlan {
+    int nlevel = 0;
+    int nMembers = 0;
+    std::vector<double> h0;             // [member * nlevel + level]: diagonal energies (FDTD units)
+    std::vector<double> weight;         // [member]: initial rho[0]
+    std::array<std::vector<cplx>, 3> mu;     // x/y/z_expectation_ (coupling-scaled), nlevel^2 each
+    std::array<std::vector<cplx>, 3> negMu;  // neg_x/y/z_expectation_
+    std::array<bool, 3> addMu = {false, false, false};  // the operator has a nonzero element
+    // relaxation: for each flat index ii the (jj, rate) pairs, outDeriv[ii] += rho[jj] * rate
+    std::vector<std::vector<std::pair<int, double>>> gam;
+    double dt = 0.0, hbar = 0.0, na = 0.0;
+    int zOff = 0;
+    std::array<bool, 3> comp = {false, false, false};  // component c is coupled (E_c exists)
+    bool gatherZCopy = false;                          // Ez gathered by copy (2-D TMz) instead of averaging
+    // geometry in grid coordinates (halo included). P-box point (i, j, k) sits at grid point
+    // boxBase + (i, j, k); the cell at (x, y, z) from the emitters' lowest point has P-box
+    // point (x+1, y+1, z+zOff). E points boxBase + (i, j, k), i < addN, receive P.
+    std::array<int, 3> boxBase = {0, 0, 0};
+    std::array<int, 3> nCell = {1, 1, 1};     // cell box extent
+    std::vector<long long> cellGrid;          // per emitter cell (reference order): grid index
+    std::array<int, 3> pDims = {1, 1, 1};     // P box extents; P index i + px*(k + pz*j)
+    std::vector<int> cellP;                   // per emitter cell: P-box index of the cell
+    std::array<int, 3> addN = {1, 1, 1};
+    // outputs
+    int nPoints = 0;                          // emitter points (population normalisation)
+    bool outputPol = false;
+    std::string polFile;
+    std::vector<int> dtcLevs;
+    std::vector<std::string> dtcFiles;
+    int dtcTimeInt = 1;
+};
+
 struct Plan {
     Inputs in;
     Dims dims;
@@ -149,11 +186,23 @@ struct Plan {
     std::vector<SourcePlan> sources;
     std::vector<DetectorPlan> detectors;
     std::vector<FluxPlan> fluxes;
+    std::vector<EmitterPlan> emitters;
+    // relative permittivity on the cell-centred grid (epsRelOrDip_), where the emitter
+    // polarisation is divided into E; filled only when there are emitters
+    std::vector<double> epsP;
     // object pole coefficients, flattened: per object, per pole
     std::vector<std::vector<double>> alpha, xi, gamma;
 };
 
 // Builds the plan; throws InputError / UnsupportedError.
 Plan build_plan(const Inputs& in);
+
+// Emitter plans of the input (emitters.cpp); Epresent: which of Ex, Ey, Ez the grid has;
+// epsOrDip: the relative permittivity on the cell-centred grid.
+void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3],
+                    const std::vector<double>& epsOrDip, Plan& P);
+
+// Wigner 3j symbol for integer arguments (emitters.cpp).
+double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);
 
 }  // namespace chiml

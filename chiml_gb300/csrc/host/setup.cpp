@@ -1232,6 +1232,10 @@ Plan build_plan(const Inputs& in) {
     Plan P;
     Builder b(in, P);
     b.build();
+    if (!in.emitters.empty()) {
+        const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
+        build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v, P);
+    }
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)
     for (auto& fp : P.fluxes) {
         if (!fp.spec.crossSec) {

@@ -10,6 +10,8 @@
 //   soft sources         SOURCE/parallelSourceNormal.cpp:15-37
 //   DFT accumulation     DTC/parallelStorageFreqDTC.cpp:21-30, DTC/parallelFlux.hpp:296-314
 //   detector sampling    DTC/parallelStorageDTC.cpp:17-48
+//   emitters             ML/parallelQE.hpp:614-770 (addQE, updateDensity, denDeriv, PCABAM4),
+//                        UTIL/FDTD_up_eq.cpp:1367-1420 (addP, getE_TE/TM), ML/Hamiltonian.cpp:59-69
 // Its outputs are pinned by the golden files of the reference's own CPU build
 // (tests/golden). Only tests, the smoke check and the CPU-baseline leg of the
 // benchmark call it; the product path never does.
@@ -17,6 +19,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <numeric>
 #include <string>
 #include <vector>
 #ifdef _OPENMP
@@ -30,6 +33,159 @@ namespace {
 
 using namespace chiml;
 
+// One emitter object stepped as ML/parallelQE.hpp:674-770 does for one process:
+// addQE (P into E, then updateDensity: gather E, PCABAM4 per member and cell,
+// populations, P from rho). The BLAS calls are restated with the arithmetic order
+// of the reference build's BLAS (dot-product zgemm, element-wise zaxpy/zdotc).
+struct EmitterSim {
+    const EmitterPlan& e;
+    const Dims& D;
+    int N, n2, nm, nc;
+    std::vector<cplx> rho;                  // [member][cell][n2]
+    std::vector<cplx> kd[4];                // derivatives at n, n-1, n-2, n-3
+    std::vector<double> Pbox[3];
+    std::array<std::vector<double>, 3> totP;
+    std::vector<cplx> curPop;
+    std::vector<std::vector<cplx>> allPop;
+    int tstep = 0;
+    std::vector<cplx> H, pred, kp, tmp;
+
+    EmitterSim(const EmitterPlan& ep, const Dims& dd) : e(ep), D(dd) {
+        N = e.nlevel;
+        n2 = N * N;
+        nm = e.nMembers;
+        nc = static_cast<int>(e.cellGrid.size());
+        rho.assign(static_cast<std::size_t>(nm) * nc * n2, cplx(0.0, 0.0));
+        for (int m = 0; m < nm; ++m)
+            for (int c = 0; c < nc; ++c) rho[(static_cast<std::size_t>(m) * nc + c) * n2] = cplx(e.weight[m], 0.0);
+        for (auto& k : kd) k.assign(rho.size(), cplx(0.0, 0.0));
+        const std::size_t pb = static_cast<std::size_t>(e.pDims[0]) * e.pDims[1] * e.pDims[2];
+        for (auto& p : Pbox) p.assign(pb, 0.0);
+        curPop.assign(e.dtcLevs.size(), cplx(0.0, 0.0));
+        allPop.assign(e.dtcLevs.size(), {});
+        H.resize(n2);
+        pred.resize(n2);
+        kp.resize(n2);
+        tmp.resize(n2);
+    }
+
+    // Hamiltonian::getHam (Hamiltonian.cpp:59-69)
+    void getHam(int m, cplx ex, cplx ey, cplx ez) {
+        for (int i = 0; i < n2; ++i) H[i] = cplx(0.0, 0.0);
+        for (int i = 0; i < N; ++i) H[i * N + i] = cplx(e.h0[static_cast<std::size_t>(m) * N + i], 0.0);
+        if (ex == 0.0 && ey == 0.0 && ez == 0.0) return;
+        const cplx a[3] = {ex, ey, ez};
+        for (int c = 0; c < 3; ++c)
+            if (e.addMu[c])
+                for (int i = 0; i < n2; ++i) H[i] += a[c] * e.negMu[c][i];
+    }
+
+    // denDeriv, MKL form (parallelQE.hpp:727-744): temp = (i/hbar) H den, out = temp + temp^H, + relaxation
+    void denDeriv(const cplx* den, cplx* out) {
+        const cplx alpha(0.0, 1.0 / e.hbar);
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                cplx s = 0.0;
+                for (int l = 0; l < N; ++l) s += H[i + l * N] * den[l + j * N];
+                tmp[i + j * N] = cplx(0.0) + alpha * s;
+            }
+        const cplx one(1.0, 0.0);
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) out[i * N + j] = one * tmp[i * N + j] + one * std::conj(tmp[j * N + i]);
+        for (std::size_t ii = 0; ii < e.gam.size(); ++ii)
+            for (auto& g : e.gam[ii]) out[ii] += den[g.first] * g.second;
+    }
+
+    void axpy(double a, const cplx* x, cplx* y) {
+        const cplx ca(a, 0.0);
+        for (int i = 0; i < n2; ++i) y[i] += ca * x[i];
+    }
+
+    // PCABAM4 (parallelQE.hpp:751-770) for member m, cell c
+    void pcabam4(int m, int c, cplx ex, cplx ey, cplx ez) {
+        const std::size_t o = (static_cast<std::size_t>(m) * nc + c) * n2;
+        cplx* r = &rho[o];
+        cplx* k0 = &kd[0][o];
+        cplx* k1 = &kd[1][o];
+        cplx* k2 = &kd[2][o];
+        cplx* k3 = &kd[3][o];
+        const double dt = e.dt;
+        for (int i = 0; i < n2; ++i) pred[i] = r[i];
+        axpy(55.0 * dt / 24.0, k0, pred.data());
+        axpy(-59.0 * dt / 24.0, k1, pred.data());
+        axpy(37.0 * dt / 24.0, k2, pred.data());
+        axpy(-9.0 * dt / 24.0, k3, pred.data());
+        getHam(m, ex, ey, ez);
+        denDeriv(pred.data(), kp.data());
+        axpy(9.0 * dt / 24.0, kp.data(), r);
+        axpy(19.0 * dt / 24.0, k0, r);
+        axpy(-5.0 * dt / 24.0, k1, r);
+        axpy(dt / 24.0, k2, r);
+        for (int i = 0; i < n2; ++i) {
+            k3[i] = k2[i];
+            k2[i] = k1[i];
+            k1[i] = k0[i];
+        }
+        getHam(m, ex, ey, ez);
+        denDeriv(r, k0);
+    }
+
+    // addQE: P into E (MLUpdateFxnReal::addP, FDTD_up_eq.cpp:1367-1380), then updateDensity
+    void step(std::vector<double>* F, const std::vector<double>& eps) {
+        const int off[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, e.zOff}};
+        const int px = e.pDims[0], pz = e.pDims[2];
+        for (int c = 0; c < 3; ++c) {
+            if (!e.comp[c]) continue;
+            double* E = F[c].data();
+            for (int kk = 0; kk < e.addN[2]; ++kk)
+                for (int jj = 0; jj < e.addN[1]; ++jj)
+                    for (int ii = 0; ii < e.addN[0]; ++ii) {
+                        const long long g = D.idx(e.boxBase[0] + ii, e.boxBase[1] + jj, e.boxBase[2] + kk);
+                        const long long gb = D.idx(e.boxBase[0] + ii + off[c][0], e.boxBase[1] + jj + off[c][1],
+                                                   e.boxBase[2] + kk + off[c][2]);
+                        const double pa = Pbox[c][ii + px * (kk + pz * jj)];
+                        const double pb = Pbox[c][(ii + off[c][0]) + px * ((kk + off[c][2]) + pz * (jj + off[c][1]))];
+                        E[g] += -0.5 * pa / eps[g];
+                        E[g] += -0.5 * pb / eps[gb];
+                    }
+        }
+        // updateDensity (parallelQE.hpp:614-678)
+        const long long unit[3] = {1, static_cast<long long>(D.lx) * D.lz, D.lx};
+        std::vector<cplx> eAt(static_cast<std::size_t>(nc) * 3, cplx(0.0, 0.0));
+        for (int q = 0; q < nc; ++q) {
+            const long long g = e.cellGrid[q];
+            for (int c = 0; c < 3; ++c) {
+                if (!e.comp[c]) continue;
+                const double* E = F[c].data();
+                if (c == 2 && e.gatherZCopy) eAt[q * 3 + c] = cplx(E[g], 0.0);
+                else eAt[q * 3 + c] = cplx(0.5 * E[g] + 0.5 * E[g - unit[c]], 0.0);
+            }
+        }
+        for (auto& p : Pbox) std::fill(p.begin(), p.end(), 0.0);
+        for (int m = 0; m < nm; ++m)
+            for (int q = 0; q < nc; ++q) {
+                pcabam4(m, q, eAt[q * 3 + 0], eAt[q * 3 + 1], eAt[q * 3 + 2]);
+                const cplx* r = &rho[(static_cast<std::size_t>(m) * nc + q) * n2];
+                for (std::size_t d = 0; d < e.dtcLevs.size(); ++d)
+                    if (tstep % e.dtcTimeInt == 0) curPop[d] += r[e.dtcLevs[d]];
+                for (int c = 0; c < 3; ++c) {
+                    if (!e.comp[c]) continue;
+                    cplx s = 0.0;
+                    for (int i = 0; i < n2; ++i) s += std::conj(r[i]) * e.mu[c][i];
+                    Pbox[c][e.cellP[q]] += e.na * std::real(s);
+                }
+            }
+        if (e.outputPol)
+            for (int c = 0; c < 3; ++c)
+                if (e.comp[c]) totP[c].push_back(std::accumulate(Pbox[c].begin(), Pbox[c].end(), 0.0));
+        for (std::size_t d = 0; d < e.dtcLevs.size(); ++d) {
+            if (tstep % e.dtcTimeInt == 0) allPop[d].push_back(curPop[d] / static_cast<double>(e.nPoints));
+            curPop[d] = 0.0;
+        }
+        ++tstep;
+    }
+};
+
 struct OracleSim {
     Plan P;
     std::vector<double> F[6];
@@ -37,9 +193,11 @@ struct OracleSim {
     std::vector<double> psi[6][2];
     std::vector<std::vector<double>> lorP[3], prevP[3];
     RunRecord rec;
+    std::vector<std::unique_ptr<EmitterSim>> qe;
     int step = 0;
 
     explicit OracleSim(const Plan& plan) : P(plan) {
+        for (auto& ep : P.emitters) qe.emplace_back(new EmitterSim(ep, P.dims));
         const std::size_t N = static_cast<std::size_t>(P.dims.cells());
         for (int c = 0; c < 6; ++c) {
             if (!P.comp[c].present) continue;
@@ -211,6 +369,8 @@ struct OracleSim {
             if (P.comp[c].present) curl(c);
         for (int c = 0; c < 3; ++c)
             if (P.comp[c].present) d2e(c);
+        // emitters after D -> E (parallelFDTDField.hpp:1282-1283)
+        for (auto& q : qe) q->step(F, P.epsP);
         ++step;
         record(P.tcur[step]);
         dft(step);
@@ -279,6 +439,13 @@ int chiml_oracle_finalize(void* h, const char* out_dir) {
     try {
         write_detectors(s->P, s->rec, out_dir ? out_dir : "", s->step);
         write_fluxes(s->P, s->rec, out_dir ? out_dir : "");
+        s->rec.emitterP.clear();
+        s->rec.emitterPop.clear();
+        for (auto& q : s->qe) {
+            s->rec.emitterP.push_back(q->totP);
+            s->rec.emitterPop.push_back(q->allPop);
+        }
+        write_emitters(s->P, s->rec, out_dir ? out_dir : "");
         return 0;
     } catch (const std::exception& e) {
         g_err = e.what();

@@ -10,6 +10,12 @@ def read_output(path):
     if raw[:1] == b"#":
         rows = [l.split() for l in raw.decode().splitlines() if not l.startswith("#")]
         return "txt", None, np.array([[float(x) for x in r] for r in rows])
+    try:
+        # headerless numeric text: emitter population and polarisation files
+        rows = [l.split() for l in raw.decode("ascii").splitlines() if l.strip()]
+        return "txt", None, np.array([float(x) for r in rows for x in r])
+    except (UnicodeDecodeError, ValueError):
+        pass
     hdr = np.frombuffer(raw[:24], dtype=np.int32)
     return "bin", hdr, np.frombuffer(raw[24:], dtype=np.float64)
 

@@ -46,11 +46,65 @@ def _tm_lorentz():
     return cfg
 
 
+def _qe_pulse(amp=5e8):
+    return [configs._gauss(configs.ev2fdtd(2.0), 1.0 / (10e-15 / configs.T_UNIT), 5.0, 12e-15 / configs.T_UNIT, amp=amp)]
+
+
+def _qe_tm():
+    """2-D TMz with a block of two-level emitters (z dipoles), relaxation and dephasing."""
+    cfg = configs.config1(n=60, pml=8, steps=300, radius_cells=6, src_gap_cells=6, ndtc=2, nfreq=4)
+    lv = [configs.emitter_level(0.0), configs.emitter_level(2.0)]
+    cfg["ObjectList"] = [configs.emitter_obj("block", [0.0, 0.0, 0.0], [(0, 0), (1, 0)], lv, [1e5] * 4,
+                                             [(1, 0, 1e12, 2e13)], 1e21, eps=1.5, dtc_levs=[0, 3],
+                                             output_pol="out/qe_pol.dat", size=[0.4, 0.4, 0.0])]
+    cfg["SourceList"][0]["loc"] = [-0.3, 0.0, 0.0]
+    cfg["SourceList"][0]["PulseList"] = _qe_pulse()
+    return cfg
+
+
+def _qe_te():
+    """2-D TE (Ex, Ey, Hz) with a disk of emitters in an (l, m) = (0,0), (1,1), (1,-1) basis (x/y dipoles)."""
+    cfg = configs.config1(n=56, pml=8, steps=260, radius_cells=6, src_gap_cells=6, ndtc=2, nfreq=4)
+    cfg["CompCell"]["pol"] = "Hz"
+    cfg["SourceList"][0]["pol"] = "Ey"
+    cfg["SourceList"][0]["loc"] = [-0.6, 0.1, 0.0]
+    cfg["SourceList"][0]["PulseList"] = _qe_pulse()
+    for d in cfg["DetectorList"]:
+        d["type"] = "Ex"
+    lv = [configs.emitter_level(0.0), configs.emitter_level(2.0, levs=2)]
+    cfg["ObjectList"] = [configs.emitter_obj("sphere", [0.0, 0.0, 0.0], [(0, 0), (1, 1), (1, -1)], lv, [1e5] * 9,
+                                             [(1, 0, 1e12, 2e13), (2, 0, 1e12, 0.0)], 1e21, eps=1.3, dtc_levs=[0, 4, 8],
+                                             output_pol="out/qe_te_pol.dat", radius=0.25)]
+    cfg["FluxList"][0]["name"] = "out/qe_te_flux"
+    return cfg
+
+
+def _qe_3d():
+    """3-D ladder of three levels (z dipoles) with Gaussian-broadened upper levels (nine ensemble
+    members), Ez plane source, population detectors and the polarisation output."""
+    n, dx = 26, 0.05
+    cfg = configs.config2(n=n, pml=5, steps=90, nell=0, nfreq=4, metal_radius_cells=0)
+    cfg["ObjectList"] = []
+    lv = [configs.emitter_level(0.0), configs.emitter_level(2.0, "Gaussian", 3, 0.02),
+          configs.emitter_level(4.2, "Gaussian", 3, 0.02)]
+    cfg["ObjectList"].append(configs.emitter_obj("block", [0.0, 0.0, 0.05], [(0, 0), (1, 0), (2, 0)], lv, [1e5] * 9,
+                                                 [(1, 0, 1e12, 2e13), (2, 1, 1e12, 2e13)], 1e21, eps=1.2,
+                                                 dtc_levs=[0, 4, 8], output_pol="out/qe3d_pol.dat",
+                                                 size=[0.3, 0.3, 0.15]))
+    src = cfg["SourceList"][0]
+    src["pol"] = "Ez"
+    src["PulseList"] = _qe_pulse()
+    return cfg
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20),
     "te_dispersive": _te_dispersive,
     "tm_lorentz": _tm_lorentz,
+    "qe_tm": _qe_tm,
+    "qe_te": _qe_te,
+    "qe_3d": _qe_3d,
 }
 
 
