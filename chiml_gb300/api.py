@@ -56,6 +56,8 @@ class Stats(ctypes.Structure):
         ("bytes_dft", ctypes.c_double),
         ("h2d_bytes", ctypes.c_double),
         ("d2h_bytes", ctypes.c_double),
+        ("n_flux_regions", ctypes.c_int32),
+        ("n_emitters", ctypes.c_int32),
     ]
 
 
@@ -180,13 +182,16 @@ class Simulation:
         ns = ctypes.c_int()
         self._check(self._lib.chiml_profile_steps(self._h, int(n), ms, 64, ctypes.byref(ns)))
         names = ["h_pass", "sources", "e_pass", "step_counter", "records"]
+        ndft = self.stats().n_flux_regions
         out = {}
         for k in range(ns.value):
             if k < len(names):
                 out[names[k]] = ms[k]
-            else:
+            elif k < len(names) + 2 * ndft:
                 q, r = divmod(k - len(names), 2)
                 out["dft%d_%s" % (q, "sample" if r == 0 else "fold")] = ms[k]
+            else:
+                out["emitter%d" % (k - len(names) - 2 * ndft)] = ms[k]
         return out
 
     @property

@@ -17,6 +17,7 @@
 #include "host/outputs.hpp"
 #include "host/plan.hpp"
 #include "kernels/box_noalloc.hpp"
+#include "kernels/emitter_device.hpp"
 #include "kernels/fdtd_device.hpp"
 
 using namespace chiml;
@@ -161,8 +162,37 @@ public:
             R.fluxIm.push_back(std::move(im));
             R.fluxSamples.push_back(stepsDone_ / fp.spec.timeInt + 1);
         }
+        for (std::size_t q = 0; q < emit_.size(); ++q) {
+            const dev::EmitterDev& e = emit_[q];
+            const EmitterPlan& ep = P.emitters[q];
+            std::array<std::vector<double>, 3> tp;
+            if (e.totP) {
+                std::vector<double> all(3 * static_cast<std::size_t>(std::max(P.nSteps, 1)));
+                ck(cudaMemcpy(all.data(), e.totP, all.size() * sizeof(double), cudaMemcpyDeviceToHost), "D2H emitter P");
+                d2h_ += static_cast<double>(all.size() * sizeof(double));
+                for (int c = 0; c < 3; ++c)
+                    if (ep.comp[c])
+                        tp[c].assign(all.begin() + static_cast<long long>(c) * P.nSteps,
+                                     all.begin() + static_cast<long long>(c) * P.nSteps + stepsDone_);
+            }
+            R.emitterP.push_back(tp);
+            std::vector<std::vector<cplx>> pops(ep.dtcLevs.size());
+            if (e.nDtc > 0) {
+                std::vector<double2> all(static_cast<std::size_t>(e.nDtc) * e.nEvents);
+                ck(cudaMemcpy(all.data(), e.pop, all.size() * sizeof(double2), cudaMemcpyDeviceToHost), "D2H populations");
+                d2h_ += static_cast<double>(all.size() * sizeof(double2));
+                const int nev = stepsDone_ > 0 ? (stepsDone_ - 1) / ep.dtcTimeInt + 1 : 0;
+                for (int d = 0; d < e.nDtc; ++d)
+                    for (int v = 0; v < nev; ++v) {
+                        const double2 x = all[static_cast<std::size_t>(d) * e.nEvents + v];
+                        pops[d].emplace_back(x.x, x.y);
+                    }
+            }
+            R.emitterPop.push_back(pops);
+        }
         write_detectors(P, R, outDir_, stepsDone_);
         write_fluxes(P, R, outDir_);
+        write_emitters(P, R, outDir_);
         finalized_ = true;
     }
 
@@ -223,44 +253,64 @@ public:
         s->bytes_dft = dftBytes_;
         s->h2d_bytes = mem_.h2d;
         s->d2h_bytes = d2h_;
+        s->n_flux_regions = static_cast<int32_t>(dft_.size());
+        s->n_emitters = static_cast<int32_t>(emit_.size());
     }
 
     int profile(int nsteps, double* ms, int maxSlots) override {
         if (finalized_) throw std::logic_error("step after finalize");
-        const int nslots = 5 + 2 * static_cast<int>(dft_.size());
-        std::vector<cudaEvent_t> ev(static_cast<std::size_t>(nslots) + 1);
-        for (auto& e : ev) ck(cudaEventCreate(&e), "cudaEventCreate");
+        const int nDft = static_cast<int>(dft_.size());
+        const int nslots = 5 + 2 * nDft + static_cast<int>(emit_.size());
+        // a start and an end event per slot, recorded around that slot's launches
+        std::vector<cudaEvent_t> e0(static_cast<std::size_t>(nslots)), e1(static_cast<std::size_t>(nslots));
+        for (auto& e : e0) ck(cudaEventCreate(&e), "cudaEventCreate");
+        for (auto& e : e1) ck(cudaEventCreate(&e), "cudaEventCreate");
         std::vector<double> acc(static_cast<std::size_t>(nslots), 0.0);
         long long left = P.nSteps - stepsDone_;
         if (nsteps > left) nsteps = static_cast<int>(left);
+        auto mark = [&](std::vector<cudaEvent_t>& v, int k) { ck(cudaEventRecord(v[k], stream_), "cudaEventRecord"); };
         for (int st = 0; st < nsteps; ++st) {
             void* s = stream_;
-            ck(cudaEventRecord(ev[0], stream_), "cudaEventRecord");
+            mark(e0, 0);
             dev::launch_pass<T>(hPass_, false, s);
-            ck(cudaEventRecord(ev[1], stream_), "cudaEventRecord");
+            mark(e1, 0);
+            mark(e0, 1);
             dev::launch_sources<T>(src_, fields_, dStep_, s);
-            ck(cudaEventRecord(ev[2], stream_), "cudaEventRecord");
+            mark(e1, 1);
+            mark(e0, 2);
             dev::launch_pass<T>(ePass_, true, s);
-            ck(cudaEventRecord(ev[3], stream_), "cudaEventRecord");
-            dev::launch_increment(dStep_, s);
-            ck(cudaEventRecord(ev[4], stream_), "cudaEventRecord");
-            dev::launch_record<T>(recT_, fields_, dStep_, s);
-            ck(cudaEventRecord(ev[5], stream_), "cudaEventRecord");
-            for (std::size_t q = 0; q < dft_.size(); ++q) {
-                dev::launch_dft_sample<T>(dft_[q], fields_, dStep_, s);
-                ck(cudaEventRecord(ev[6 + 2 * q], stream_), "cudaEventRecord");
-                dev::launch_dft_fold<T>(dft_[q], dStep_, -1, 0, s);
-                ck(cudaEventRecord(ev[7 + 2 * q], stream_), "cudaEventRecord");
+            mark(e1, 2);
+            T* const ef[3] = {fields_.f[0], fields_.f[1], fields_.f[2]};
+            for (std::size_t q = 0; q < emit_.size(); ++q) {
+                const int k = 5 + 2 * nDft + static_cast<int>(q);
+                mark(e0, k);
+                dev::launch_emitter_step<T>(emit_[q], ef, dStep_, s);
+                mark(e1, k);
             }
-            ck(cudaEventSynchronize(ev[static_cast<std::size_t>(nslots)]), "cudaEventSynchronize");
+            mark(e0, 3);
+            dev::launch_increment(dStep_, s);
+            mark(e1, 3);
+            mark(e0, 4);
+            dev::launch_record<T>(recT_, fields_, dStep_, s);
+            mark(e1, 4);
+            for (int q = 0; q < nDft; ++q) {
+                mark(e0, 5 + 2 * q);
+                dev::launch_dft_sample<T>(dft_[q], fields_, dStep_, s);
+                mark(e1, 5 + 2 * q);
+                mark(e0, 6 + 2 * q);
+                dev::launch_dft_fold<T>(dft_[q], dStep_, -1, 0, s);
+                mark(e1, 6 + 2 * q);
+            }
+            ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
             for (int k = 0; k < nslots; ++k) {
                 float m = 0.f;
-                ck(cudaEventElapsedTime(&m, ev[k], ev[k + 1]), "cudaEventElapsedTime");
+                ck(cudaEventElapsedTime(&m, e0[k], e1[k]), "cudaEventElapsedTime");
                 acc[k] += m;
             }
             ++stepsDone_;
         }
-        for (auto& e : ev) cudaEventDestroy(e);
+        for (auto& e : e0) cudaEventDestroy(e);
+        for (auto& e : e1) cudaEventDestroy(e);
         int n = std::min(nslots, maxSlots);
         for (int k = 0; k < n; ++k) ms[k] = acc[k];
         return n;
@@ -281,6 +331,7 @@ private:
     dev::SourceTable src_{};
     dev::RecordTable recT_{};
     std::vector<dev::DftTable<T>> dft_;
+    std::vector<dev::EmitterDev> emit_;
     std::vector<long long> recBase_;
     std::size_t recTotal_ = 0;
     double* dRec_ = nullptr;
@@ -299,11 +350,114 @@ private:
         dev::launch_pass<T>(hPass_, false, s);
         dev::launch_sources<T>(src_, fields_, dStep_, s);
         dev::launch_pass<T>(ePass_, true, s);
+        launchEmitters(s);
         dev::launch_increment(dStep_, s);
         dev::launch_record<T>(recT_, fields_, dStep_, s);
         for (auto& d : dft_) {
             dev::launch_dft_sample<T>(d, fields_, dStep_, s);
             dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
+        }
+    }
+
+    // emitters after D -> E, before the step counter moves (parallelFDTDField.hpp:1281-1287)
+    void launchEmitters(void* s) {
+        T* const ef[3] = {fields_.f[0], fields_.f[1], fields_.f[2]};
+        for (auto& e : emit_) dev::launch_emitter_step<T>(e, ef, dStep_, s);
+    }
+
+    // Device state of the emitter objects: FP64 density matrices (one per cell and
+    // ensemble member) initialised to the member weight in rho[0], four zeroed derivative
+    // slots, the P boxes, and the constants of the plan.
+    void uploadEmitters() {
+        const Dims& D = P.dims;
+        for (const EmitterPlan& ep : P.emitters) {
+            if (ep.nlevel > dev::kMaxEmitterLevels) throw UnsupportedError("emitters with more than 8 levels");
+            if (ep.dtcLevs.size() > 8) throw UnsupportedError("more than 8 population detectors on one emitter");
+            dev::EmitterDev e{};
+            const int N = ep.nlevel, n2 = N * N;
+            e.N = N;
+            e.n2 = n2;
+            e.nm = ep.nMembers;
+            e.nc = static_cast<int>(ep.cellGrid.size());
+            e.h0 = mem_.upload(ep.h0);
+            std::vector<double2> mu(3 * n2), nmu(3 * n2);
+            for (int c = 0; c < 3; ++c)
+                for (int i = 0; i < n2; ++i) {
+                    mu[c * n2 + i] = make_double2(ep.mu[c][i].real(), ep.mu[c][i].imag());
+                    nmu[c * n2 + i] = make_double2(ep.negMu[c][i].real(), ep.negMu[c][i].imag());
+                }
+            e.mu = mem_.upload(mu);
+            e.negMu = mem_.upload(nmu);
+            for (int c = 0; c < 3; ++c) {
+                e.addMu[c] = ep.addMu[c] ? 1 : 0;
+                e.comp[c] = ep.comp[c] ? 1 : 0;
+            }
+            e.gatherZCopy = ep.gatherZCopy ? 1 : 0;
+            std::vector<int> row(n2 + 1, 0), col;
+            std::vector<double> val;
+            for (int ii = 0; ii < n2; ++ii) {
+                row[ii] = static_cast<int>(col.size());
+                if (ii < static_cast<int>(ep.gam.size()))
+                    for (auto& g : ep.gam[ii]) {
+                        col.push_back(g.first);
+                        val.push_back(g.second);
+                    }
+            }
+            row[n2] = static_cast<int>(col.size());
+            if (col.empty()) {
+                col.push_back(0);
+                val.push_back(0.0);
+            }
+            e.gamRow = mem_.upload(row);
+            e.gamCol = mem_.upload(col);
+            e.gamVal = mem_.upload(val);
+            e.dt = ep.dt;
+            e.hbar = ep.hbar;
+            e.na = ep.na;
+            e.cellGrid = mem_.upload(ep.cellGrid);
+            e.cellP = mem_.upload(ep.cellP);
+            e.unit[0] = 1;
+            e.unit[1] = static_cast<long long>(D.lx) * D.lz;
+            e.unit[2] = D.lx;
+            const std::size_t nstate = static_cast<std::size_t>(e.nm) * n2 * e.nc;
+            std::vector<double2> rho(nstate, make_double2(0.0, 0.0));
+            for (int m = 0; m < e.nm; ++m)
+                for (int q = 0; q < e.nc; ++q) rho[static_cast<std::size_t>(m) * n2 * e.nc + q] = make_double2(ep.weight[m], 0.0);
+            e.rho = static_cast<double2*>(mem_.upload(rho));
+            e.kd = mem_.alloc<double2>(4 * nstate);
+            e.pBox = ep.pDims[0] * ep.pDims[1] * ep.pDims[2];
+            e.P = mem_.alloc<double>(3 * static_cast<std::size_t>(e.pBox));
+            std::vector<double> epsBox(e.pBox, 1.0);
+            for (int j = 0; j < ep.pDims[1]; ++j)
+                for (int k = 0; k < ep.pDims[2]; ++k)
+                    for (int i = 0; i < ep.pDims[0]; ++i) {
+                        const int gx = ep.boxBase[0] + i, gy = ep.boxBase[1] + j, gz = ep.boxBase[2] + k;
+                        if (gx < D.lx && gy < D.ly && gz < D.lz)
+                            epsBox[i + ep.pDims[0] * (k + ep.pDims[2] * j)] = P.epsP[static_cast<std::size_t>(D.idx(gx, gy, gz))];
+                    }
+            e.epsBox = mem_.upload(epsBox);
+            for (int k = 0; k < 3; ++k) {
+                e.pDims[k] = ep.pDims[k];
+                e.addN[k] = ep.addN[k];
+                e.boxBase[k] = ep.boxBase[k];
+            }
+            e.zOff = ep.zOff;
+            e.lx = D.lx;
+            e.lz = D.lz;
+            e.nDtc = static_cast<int>(ep.dtcLevs.size());
+            std::vector<int> lev = ep.dtcLevs;
+            if (lev.empty()) lev.push_back(0);
+            e.dtcLev = mem_.upload(lev);
+            e.dtcTimeInt = ep.dtcTimeInt;
+            e.nPoints = static_cast<double>(ep.nPoints);
+            e.partialBlocks = (e.nc + 127) / 128;
+            e.popPartial = mem_.alloc<double2>(static_cast<std::size_t>(e.partialBlocks) * std::max(e.nDtc, 1));
+            e.totPartial = mem_.alloc<double>(static_cast<std::size_t>(e.partialBlocks) * 3);
+            e.nSteps = P.nSteps;
+            e.nEvents = P.nSteps > 0 ? (P.nSteps - 1) / ep.dtcTimeInt + 1 : 1;
+            e.pop = mem_.alloc<double2>(static_cast<std::size_t>(std::max(e.nDtc, 1)) * e.nEvents);
+            e.totP = ep.outputPol ? mem_.alloc<double>(3 * static_cast<std::size_t>(std::max(P.nSteps, 1))) : nullptr;
+            emit_.push_back(e);
         }
     }
 
@@ -662,6 +816,7 @@ private:
             d.im = mem_.alloc<double>(cell.size() * nf);
             dft_.push_back(d);
         }
+        uploadEmitters();
         bytesPerCell_ = algorithmicBytesPerCell();
         dStep_ = mem_.alloc<int>(1);
         dErr_ = mem_.alloc<unsigned int>(1);
@@ -670,7 +825,7 @@ private:
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
         kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size()) +
-                          (ePass_.nLor > 0 ? 1 : 0);
+                          (ePass_.nLor > 0 ? 1 : 0) + 3 * static_cast<int>(emit_.size());
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
         for (auto& d : dft_) dev::launch_dft_sample<T>(d, fields_, dStep_, stream_);

@@ -1,0 +1,58 @@
+// Device descriptor of one emitter object (the Maxwell-Liouville part of the E half
+// step); kernels in emitter_kernels.cu, host set-up in engine.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace chiml {
+namespace dev {
+
+constexpr int kMaxEmitterLevels = 8;
+
+// Density matrices and their derivative histories are FP64 in every precision form.
+// Layout: element e of member m of cell q is at (m * n2 + e) * nc + q, so that the
+// threads of a warp (consecutive cells) read consecutive addresses.
+struct EmitterDev {
+    int N, n2, nm, nc;            // levels, N*N, ensemble members, emitter cells
+    const double* h0;             // [nm][N] diagonal energies
+    const double2* mu;            // [3][n2] coupling-scaled dipole operators
+    const double2* negMu;         // [3][n2] their negatives
+    int addMu[3];                 // operator c has a nonzero element
+    int comp[3];                  // component c is coupled
+    int gatherZCopy;              // Ez gathered by copy (2-D TMz)
+    const int* gamRow;            // relaxation rows, CSR: [n2 + 1]
+    const int* gamCol;
+    const double* gamVal;
+    double dt, hbar, na;
+    const long long* cellGrid;    // [nc] grid index of each cell
+    const int* cellP;             // [nc] P-box index of each cell
+    long long unit[3];            // grid index step along x, y, z
+    double2* rho;                 // [nm * n2 * nc]
+    double2* kd;                  // 4 slots of derivatives, slot stride nm * n2 * nc
+    double* P;                    // [3][pBox] polarisation per component
+    const double* epsBox;         // [pBox] relative permittivity at the P-box points
+    int pDims[3], addN[3], boxBase[3], zOff;
+    int lx, lz;                   // grid extents for P-box -> grid indices
+    int pBox;
+    // outputs
+    int nDtc;
+    const int* dtcLev;
+    int dtcTimeInt;
+    double nPoints;               // emitter points (population normalisation)
+    double2* popPartial;          // [blocks][nDtc]
+    double* totPartial;           // [blocks][3]
+    int partialBlocks;
+    double2* pop;                 // [nDtc][nEvents]
+    int nEvents;
+    double* totP;                 // [3][nSteps], null when the polarisation is not written
+    int nSteps;
+};
+
+// P into E on the (n+1)-box (addP), then one density update of every cell and member
+// (updateDensity) and the output reductions. `step` is the device step counter, equal
+// to the number of completed steps when these run.
+template <typename T>
+void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream);
+
+}  // namespace dev
+}  // namespace chiml

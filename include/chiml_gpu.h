@@ -35,7 +35,7 @@ typedef enum chiml_status {
 
 typedef enum chiml_precision {
     CHIML_PREC_FP64 = 0,  /* every field, coefficient and accumulator in FP64 (the parity form) */
-    CHIML_PREC_SPLIT = 1  /* fields, CPML and polarisations in FP32; DFT accumulators in FP64 */
+    CHIML_PREC_SPLIT = 1  /* fields, CPML and polarisations in FP32; DFT accumulators and emitter density matrices in FP64 */
 } chiml_precision;
 
 typedef struct chiml_options {
@@ -61,6 +61,8 @@ typedef struct chiml_stats {
     double bytes_dft;              /* algorithmic HBM bytes of the DFT launches of one sampled step */
     double h2d_bytes;              /* bytes copied host to device so far */
     double d2h_bytes;              /* bytes copied device to host so far */
+    int32_t n_flux_regions;        /* DFT flux regions (two profile slots each) */
+    int32_t n_emitters;            /* emitter objects (one profile slot each) */
 } chiml_stats;
 
 /* Reads the JSON input (chiML schema), builds the update plan and uploads it. */
@@ -74,8 +76,9 @@ chiml_status chiml_step(chiml_sim* sim, int64_t nsteps);
 /* Waits for queued work. */
 chiml_status chiml_sync(chiml_sim* sim);
 
-/* Copies detector records and DFT accumulators to the host and writes the
- * detector and flux files in chiML's formats. */
+/* Copies detector records, DFT accumulators and emitter outputs to the host and
+ * writes the detector, flux, emitter polarisation and population files in chiML's
+ * formats. */
 chiml_status chiml_finalize(chiml_sim* sim);
 
 void chiml_destroy(chiml_sim* sim);
@@ -96,7 +99,8 @@ void* chiml_stream(chiml_sim* sim);
 /* Advances nsteps steps without graphs, timing every kernel launch with CUDA
  * events on the handle's stream. ms_out[k] receives the summed milliseconds of
  * kernel slot k: 0 H pass, 1 sources, 2 E pass, 3 step counter, 4 detector
- * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of flux region q.
+ * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of flux region q, then
+ * 5 + 2 * n_flux_regions + e the emitter step of emitter object e.
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 

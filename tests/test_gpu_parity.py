@@ -59,11 +59,12 @@ def test_fp64_fields_match_oracle_midrun(case, built_engine, built_oracle):
     assert checked >= 3
 
 
-def test_graph_replay_equals_eager_launches(built_engine, tmp_path):
+@pytest.mark.parametrize("case", ["c2_small", "qe_3d"])
+def test_graph_replay_equals_eager_launches(case, built_engine, tmp_path):
     a = tmp_path / "eager"
     b = tmp_path / "graph"
-    _run_gpu("c2_small", a, graph=0)
-    _run_gpu("c2_small", b, graph=16)
+    _run_gpu(case, a, graph=0)
+    _run_gpu(case, b, graph=16)
     for d, _, files in os.walk(a):
         for f in files:
             pa = os.path.join(d, f)
