@@ -116,9 +116,16 @@ def config1(n=400, pml=20, steps=4000, radius_cells=50, src_gap_cells=60, ndtc=8
     }
 
 
-def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal_radius_cells=30):
+def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal_radius_cells=30, aniso=True):
     """3-D dispersive scene: seeded ellipsoids, a Drude + 2 Lorentz metal sphere, a plane Ex
-    source sheet and a DFT flux box."""
+    source sheet and a DFT flux box.
+
+    With ``aniso`` each ellipsoid is uniaxial: eps_inf = eps_o plus one oriented-dipole
+    Lorentz pole along the random optic axis whose static strength is eps_e - eps_o, centred
+    far above the source band (5x its centre frequency), so that the permittivity along the
+    axis is eps_e and across it eps_o. The pair (eps_o, eps_e) is drawn as two uniforms on
+    [1.5, 4] ordered so that eps_e >= eps_o (the reader drops the direction of a pole with
+    negative strength)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     dx = 0.05
     dt = 0.5 * dx / math.sqrt(3.0)
@@ -128,8 +135,9 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
     objs = []
     for _ in range(nell):
         semi = rng.uniform(10, 40, size=3) * dx * (n / 256.0)
-        eps_o = float(rng.uniform(1.5, 4.0))
-        rng.uniform(1.5, 4.0)              # eps_e: the uniaxial part needs oriented-dipole poles
+        e1 = float(rng.uniform(1.5, 4.0))
+        e2 = float(rng.uniform(1.5, 4.0))
+        eps_o, eps_e = (min(e1, e2), max(e1, e2)) if aniso else (e1, e1)
         axis = rng.normal(size=3)
         axis /= np.linalg.norm(axis)
         lim = np.maximum(inner - semi.max(), 0.0)
@@ -139,8 +147,12 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
         u1 = np.cross(u0, tmp)
         u1 /= np.linalg.norm(u1)
         u2 = np.cross(u0, u1)
+        pols = []
+        if aniso and eps_e > eps_o:
+            pols = [{"gamma": 0.01, "omega": 5.0 * A / 550e-9, "sigma_p": eps_e - eps_o,
+                     "dipOrE": "unidirectional", "dirDipE": [float(v) for v in axis]}]
         objs.append(_obj("ellipsoid", [float(v) for v in c], size=[float(2 * s) for s in semi], material="custom",
-                         eps=eps_o, pols=[],
+                         eps=eps_o, pols=pols,
                          unit_vectors=[{"uvec": [float(v) for v in u]} for u in (u0, u1, u2)]))
     rm = metal_radius_cells * dx * (n / 256.0)
     objs.append(_obj("sphere", [0.0, 0.0, 0.0], radius=rm, material="custom", eps=6.0,

@@ -365,6 +365,38 @@ private:
         for (auto& e : emit_) dev::launch_emitter_step<T>(e, ef, dStep_, s);
     }
 
+    // Oriented-dipole polarisation entries, their dipole directions (entry-fastest per
+    // pole and axis) and the full-grid P / P_prev arrays per component and pole.
+    void uploadOrDip(dev::Pass<T>& pass) {
+        const OrDipPlan& od = P.ordip;
+        std::memset(&pass.od, 0, sizeof(pass.od));
+        if (!od.present || od.cells.empty()) return;
+        if (od.nPoles > dev::kMaxPoles) throw UnsupportedError("more than 8 oriented-dipole poles");
+        const std::size_t N = static_cast<std::size_t>(P.dims.cells());
+        const long long n = static_cast<long long>(od.cells.size());
+        pass.od.n = n;
+        pass.od.nPoles = od.nPoles;
+        pass.od.cell = mem_.upload(od.cells);
+        pass.od.obj = mem_.upload(od.obj);
+        std::vector<T> dip(static_cast<std::size_t>(od.nPoles) * 3 * n);
+        for (long long j = 0; j < n; ++j)
+            for (int pp = 0; pp < od.nPoles; ++pp)
+                for (int a = 0; a < 3; ++a)
+                    dip[(static_cast<std::size_t>(pp) * 3 + a) * n + j] = static_cast<T>(od.dip[j * od.nPoles + pp][a]);
+        pass.od.dip = mem_.upload(dip);
+        for (int c = 0; c < 3; ++c) {
+            pass.od.off[c] = od.offA[c];
+            for (int pp = 0; pp < od.nPoles; ++pp) {
+                pass.od.P[c][pp] = mem_.alloc<T>(N);
+                pass.od.Pprev[c][pp] = mem_.alloc<T>(N);
+            }
+        }
+        for (long long j = 0; j < n; ++j) {
+            const long long i = od.cells[j];
+            if (i - od.offA[1] < 0 || i >= static_cast<long long>(N)) throw InputError("oriented-dipole cell outside the grid");
+        }
+    }
+
     // Device state of the emitter objects: FP64 density matrices (one per cell and
     // ensemble member) initialised to the member weight in rho[0], four zeroed derivative
     // slots, the P boxes, and the constants of the plan.
@@ -649,8 +681,9 @@ private:
                         o.npsi[t] = k.npsi[t];
                         o.psiUpd[t] = k.psiUpd[t];
                     }
-                    if (k.ordip) throw UnsupportedError("oriented-dipole cells are not supported by the device engine");
-                    if ((k.lor || k.toD) && !cp.hasD) throw InputError("dispersive cell without a D field");
+                    o.ordip = k.ordip;
+                    o.odCoef = static_cast<T>(-0.5 / k.eps);
+                    if ((k.lor || k.toD || k.ordip) && !cp.hasD) throw InputError("dispersive cell without a D field");
                 }
                 dc.cls = mem_.upload(cls);
                 std::vector<dev::FastClass<T>> fcls(cp.classes.size());
@@ -671,6 +704,7 @@ private:
                         if (base != 0.0 || k.kflag[t] || (psiUpd && k.npsi[t])) write = true;
                     }
                     if (k.lor) o.flags |= dev::kFcLor;
+                    if (k.ordip) o.flags |= dev::kFcOrDip;
                     if (k.toD) o.flags |= dev::kFcToD;
                     if (write) o.flags |= dev::kFcWrite;
                 }
@@ -701,6 +735,7 @@ private:
                 bytes += 3.0 * sizeof(T) + 1.0;  // field read + write, neighbour read, code
             }
             setSlabsAndForm(pass, half == 1);
+            if (half == 1) uploadOrDip(pass);
             if (half == 1 && pass.interior3d) {
                 // dispersive cells leave the interior form for their own list kernel
                 std::vector<int> lc;
@@ -709,7 +744,7 @@ private:
                     const CompPlan& cp = P.comp[ci];
                     if (!cp.present) continue;
                     for (long long i = 0; i < static_cast<long long>(cp.code.size()); ++i)
-                        if (cp.code[i] && cp.classes[cp.code[i]].lor) {
+                        if (cp.code[i] && (cp.classes[cp.code[i]].lor || cp.classes[cp.code[i]].ordip)) {
                             lc.push_back(ci);
                             li.push_back(i);
                         }

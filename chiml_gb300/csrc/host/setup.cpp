@@ -814,6 +814,45 @@ struct Builder {
         cp.nPoles = (E && P.disp) ? np : 0;
     }
 
+    // Oriented-dipole polarisation cells (upOrDipP_): the cell-centred grid points whose
+    // object has oriented-dipole poles, from initializeList on physPOrDip_
+    // (parallelFDTDField.cpp:83-87 with getBlasLists / fillBlasLists), and the dipole
+    // direction of every pole there (setupDipMoments, parallelFDTDField.hpp:960-1048:
+    // isotropic 1, unidirectional the normalised direction).
+    void buildOrDip() {
+        OrDipPlan& od = P.ordip;
+        od = OrDipPlan();
+        int np = 0;
+        for (auto& o : objs)
+            if (o.orDip && o.gamma.size() > 0) np = std::max(np, static_cast<int>(o.gamma.size()));
+        if (np == 0) return;
+        od.present = true;
+        od.nPoles = np;
+        const Field3<int>& ph = phys[6];
+        for (int jj = 1; jj < D.ly - 1; ++jj)
+            for (int kk = 1; kk < D.lz - 1; ++kk)
+                for (int ii = 1; ii < D.lx - 1; ++ii) {
+                    const int o = ph.at(ii, jj, kk);
+                    if (o < 0) throw InputError("oriented-dipole list reaches a border cell");
+                    const Object& ob = objs[o];
+                    if (!(ob.orDip && ob.gamma.size() > 0)) continue;
+                    od.cells.push_back(D.idx(ii, jj, kk));
+                    od.obj.push_back(o);
+                    for (int pp = 0; pp < np; ++pp) {
+                        std::array<double, 3> dv = {0.0, 0.0, 0.0};
+                        if (pp < static_cast<int>(ob.dipOr.size())) {
+                            if (ob.dipOr[pp] == DipOr::ISOTROPIC) dv = {1.0, 1.0, 1.0};
+                            else dv = ob.dipE[pp];
+                        }
+                        od.dip.push_back(dv);
+                    }
+                }
+        // E_c at the cell and one cell below along c enter the averaged dot product
+        od.offA[0] = 1;
+        od.offA[1] = static_cast<long long>(D.lx) * D.lz;
+        od.offA[2] = D.lx;
+    }
+
     void build() {
         P.in = in;
         objs = in.objects;
@@ -856,8 +895,9 @@ struct Builder {
         if (te) P.comp[EX].present = P.comp[EY].present = P.comp[HZ].present = true;
         if (tm) P.comp[HX].present = P.comp[HY].present = P.comp[EZ].present = true;
         for (auto& o : objs)
-            if (o.orDip && o.gamma.size() > 0)
-                throw UnsupportedError("oriented-dipole (anisotropic) poles are not supported by this build");
+            if (o.orDip && o.gamma.size() > 0 && !D.threeD)
+                throw UnsupportedError("oriented-dipole poles need a 3-D grid (the reference allocates the 2-D "
+                                       "polarisation grids for the other polarisation)");
         // the reference's list order: TE (Hz, Ex, Ey) then TM (Ez, Hx, Hy)
         const int order[6] = {HZ, EX, EY, EZ, HX, HY};
         bool present[6];
@@ -865,6 +905,7 @@ struct Builder {
         for (int c : order)
             if (present[c]) buildComp(c);
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
+        buildOrDip();
         P.alpha.clear();
         P.xi.clear();
         P.gamma.clear();

@@ -23,7 +23,9 @@ struct Class {
     uint8_t kflag[2];
     uint8_t npsi[2];
     uint8_t psiUpd[2];
-    uint8_t pad[2];
+    uint8_t ordip;   // oriented-dipole D -> E: P averaged over two cell-centred points
+    uint8_t pad;
+    T odCoef;        // -0.5 / eps_inf (orDipDtoU)
 };
 
 // The same class in the shape the interior form's arithmetic uses: per term
@@ -46,6 +48,7 @@ constexpr uint32_t kFcSlab0 = 32u;   // term J needs the slab (profile or psi)
 constexpr uint32_t kFcSlab1 = 64u;   // term K needs the slab
 constexpr uint32_t kFcKp0 = 128u;    // term J adds its normal-slab profile kprof
 constexpr uint32_t kFcKp1 = 256u;    // term K adds its normal-slab profile kprof
+constexpr uint32_t kFcOrDip = 512u;  // oriented-dipole D -> E (E pass)
 
 template <typename T>
 struct Comp {
@@ -77,6 +80,21 @@ struct Comp {
     int slabHi[2];
 };
 
+// Oriented-dipole polarisations (UpdateLorPolOrDip): one entry per cell-centred grid
+// point inside an object with oriented-dipole poles. P and P_prev are full-grid arrays
+// per component and pole; the dipole directions are stored per entry, pole and axis.
+template <typename T>
+struct OrDipDev {
+    long long n;
+    int nPoles;
+    const long long* cell;
+    const int* obj;
+    const T* dip;                  // [(pole * 3 + axis) * n + entry]
+    T* P[3][kMaxPoles];
+    T* Pprev[3][kMaxPoles];
+    long long off[3];              // grid index step along x, y, z
+};
+
 template <typename T>
 struct Pass {
     Comp<T> c[3];
@@ -92,6 +110,7 @@ struct Pass {
     // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
     int interior3d;
     int index64;            // grid too large for 32-bit cell indices
+    OrDipDev<T> od;         // oriented-dipole polarisations (E pass)
     // dispersive cells of the E pass, run by their own kernel in the interior form
     long long nLor;
     const int* lorComp;

@@ -80,6 +80,62 @@ __device__ __forceinline__ void cellGeneric(const Pass<T>& p, int ci, long long 
         for (int q = 0; q < c.nPoles; ++q) e += k.negEpsInv * c.P[q][i];
         c.U[i] = e;
     }
+    if (EPASS && k.ordip) {
+        // orDipDtoU (FDTD_up_eq.cpp:862-875)
+        T e = c.D[i];
+        e *= k.epsInv;
+        const long long o = p.od.off[ci];
+        for (int q = 0; q < p.od.nPoles; ++q) {
+            e += k.odCoef * p.od.P[ci][q][i];
+            e += k.odCoef * p.od.P[ci][q][i + o];
+        }
+        c.U[i] = e;
+    }
+}
+
+// Oriented-dipole polarisations from E^n, before the E curl (UpdateLorPolOrDip,
+// UTIL/FDTD_up_eq.cpp:450-521): per pole P = alpha P + xi P_prev + gamma d (d . <E>),
+// <E_c> the average of E_c at the point and one cell below along c.
+template <typename T>
+__global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
+    const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+    const OrDipDev<T>& od = p.od;
+    if (j >= od.n) return;
+    const long long i = od.cell[j];
+    const int o = od.obj[j];
+    if (o < 0 || o >= p.nObj || p.poleCount[o] > od.nPoles) {
+        atomicOr(p.err, kErrPoleCount);
+        return;
+    }
+    const T* Ex = p.c[0].U;
+    const T* Ey = p.c[1].U;
+    const T* Ez = p.c[2].U;
+    const int s = p.poleStart[o];
+    const int np = p.poleCount[o];
+    for (int pp = 0; pp < np; ++pp) {
+        const T dx = od.dip[(pp * 3 + 0) * od.n + j];
+        const T dy = od.dip[(pp * 3 + 1) * od.n + j];
+        const T dz = od.dip[(pp * 3 + 2) * od.n + j];
+        const T jx = od.P[0][pp][i], jy = od.P[1][pp][i], jz = od.P[2][pp][i];
+        T px = p.alpha[s + pp] * jx;
+        px = px + p.xi[s + pp] * od.Pprev[0][pp][i];
+        T py = p.alpha[s + pp] * jy;
+        py = py + p.xi[s + pp] * od.Pprev[1][pp][i];
+        T pz = p.alpha[s + pp] * jz;
+        pz = pz + p.xi[s + pp] * od.Pprev[2][pp][i];
+        T dot = dx * Ex[i] / T(2);
+        dot += T(1) * (dx * Ex[i - od.off[0]] / T(2));
+        dot += T(1) * (dy * Ey[i] / T(2));
+        dot += T(1) * (dy * Ey[i - od.off[1]] / T(2));
+        dot += T(1) * (dz * Ez[i] / T(2));
+        dot += T(1) * (dz * Ez[i - od.off[2]] / T(2));
+        od.P[0][pp][i] = px + p.gamma[s + pp] * (dx * dot);
+        od.P[1][pp][i] = py + p.gamma[s + pp] * (dy * dot);
+        od.P[2][pp][i] = pz + p.gamma[s + pp] * (dz * dot);
+        od.Pprev[0][pp][i] = jx;
+        od.Pprev[1][pp][i] = jy;
+        od.Pprev[2][pp][i] = jz;
+    }
 }
 
 template <typename T, bool EPASS>
@@ -229,7 +285,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
         const FastClass<T>* kc = c.fcls + cd;
         const T coef0 = kc->coef[0], coef1 = kc->coef[1];
         const uint32_t fl = kc->flags;
-        if (EPASS && (fl & kFcLor)) continue;  // dispersive cells run in k_pass_lorentz
+        if (EPASS && (fl & (kFcLor | kFcOrDip))) continue;  // dispersive cells run in k_pass_lorentz
         if (((fl & kFcSlab0) && !in[0]) || ((fl & kFcSlab1) && !in[1])) {
             atomicOr(p.err, kErrSlab);
             continue;
@@ -306,6 +362,8 @@ static void launch_pass3d(const Pass<T>& p, bool ePass, cudaStream_t s) {
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ePass && p.od.n > 0)
+        k_ordip_pol<T><<<static_cast<unsigned>((p.od.n + 255) / 256), 256, 0, s>>>(p);
     if (p.interior3d) {
         if (p.index64) {
             launch_pass3d<T, long long, 16, 2>(p, ePass, s);

@@ -5,8 +5,8 @@
 //   step order           FDTD_MANAGER/parallelFDTDField.hpp:1228-1303
 //   curl updates         UTIL/FDTD_up_eq.cpp:10-35   (TwoCompCurl / OneCompCurlJ/K)
 //   CPML psi and terms   PML/parallelPML.cpp:12-40   (addPsi / addGridOnly / updatePsiField)
-//   Lorentz polarisation UTIL/FDTD_up_eq.cpp:425-448 (UpdateLorPol)
-//   D -> E               UTIL/FDTD_up_eq.cpp:838-848 (DtoU)
+//   Lorentz polarisation UTIL/FDTD_up_eq.cpp:425-448 (UpdateLorPol), 450-521 (UpdateLorPolOrDip)
+//   D -> E               UTIL/FDTD_up_eq.cpp:838-848 (DtoU), 862-875 (orDipDtoU)
 //   soft sources         SOURCE/parallelSourceNormal.cpp:15-37
 //   DFT accumulation     DTC/parallelStorageFreqDTC.cpp:21-30, DTC/parallelFlux.hpp:296-314
 //   detector sampling    DTC/parallelStorageDTC.cpp:17-48
@@ -192,6 +192,7 @@ struct OracleSim {
     std::vector<double> Dd[3];
     std::vector<double> psi[6][2];
     std::vector<std::vector<double>> lorP[3], prevP[3];
+    std::vector<std::vector<double>> odP[3], odPrev[3];  // oriented-dipole polarisations (cell-centred grid)
     RunRecord rec;
     std::vector<std::unique_ptr<EmitterSim>> qe;
     int step = 0;
@@ -213,6 +214,12 @@ struct OracleSim {
                 prevP[c].emplace_back(N, 0.0);
             }
         }
+        if (P.ordip.present)
+            for (int c = 0; c < 3; ++c)
+                for (int p = 0; p < P.ordip.nPoles; ++p) {
+                    odP[c].emplace_back(N, 0.0);
+                    odPrev[c].emplace_back(N, 0.0);
+                }
         rec.detectors.resize(P.detectors.size());
         for (auto& fp : P.fluxes) {
             std::size_t n = static_cast<std::size_t>(fp.npts) * fp.spec.freqList.size();
@@ -342,14 +349,72 @@ struct OracleSim {
         const Dims& D = P.dims;
         double* E = F[c].data();
         const double* Dc = Dd[c].data();
+        const long long off = P.ordip.offA[c];
 #pragma omp parallel for schedule(static)
         for (long long i = 0; i < D.cells(); ++i) {
             const ClassInfo& k = cp.classes[cp.code[i]];
+            if (k.ordip) {
+                // orDipDtoU (FDTD_up_eq.cpp:862-875): P averaged over the two cell-centred points
+                double e = Dc[i];
+                e *= 1.0 / k.eps;
+                for (int p = 0; p < P.ordip.nPoles; ++p) {
+                    e += (-0.5 / k.eps) * odP[c][p][i];
+                    e += (-0.5 / k.eps) * odP[c][p][i + off];
+                }
+                E[i] = e;
+                continue;
+            }
             if (!k.lor) continue;
             double e = Dc[i];
             e *= 1.0 / k.eps;
             for (int p = 0; p < cp.nPoles; ++p) e += (-1.0 / k.eps) * lorP[c][p][i];
             E[i] = e;
+        }
+    }
+
+    // UpdateLorPolOrDip (FDTD_up_eq.cpp:450-521): per pole, P = alpha P + xi P_prev
+    // + gamma d (d . <E>), where <E> averages each E component over the cell-centred
+    // point and the point one cell below along that component.
+    void orDipPolarisation() {
+        const OrDipPlan& od = P.ordip;
+        if (!od.present) return;
+        const double* Ex = F[0].data();
+        const double* Ey = F[1].data();
+        const double* Ez = F[2].data();
+        const long long ox = od.offA[0], oy = od.offA[1], oz = od.offA[2];
+        const int np = od.nPoles;
+#pragma omp parallel for schedule(static)
+        for (std::size_t j = 0; j < od.cells.size(); ++j) {
+            const long long i = od.cells[j];
+            const int o = od.obj[j];
+            const auto& al = P.alpha[o];
+            const auto& xi = P.xi[o];
+            const auto& ga = P.gamma[o];
+            for (std::size_t pp = 0; pp < al.size(); ++pp) {
+                const auto& dv = od.dip[j * np + pp];
+                double* Px = &odP[0][pp][i];
+                double* Py = &odP[1][pp][i];
+                double* Pz = &odP[2][pp][i];
+                const double jx = *Px, jy = *Py, jz = *Pz;
+                *Px = al[pp] * *Px;
+                *Px = *Px + xi[pp] * odPrev[0][pp][i];
+                *Py = al[pp] * *Py;
+                *Py = *Py + xi[pp] * odPrev[1][pp][i];
+                *Pz = al[pp] * *Pz;
+                *Pz = *Pz + xi[pp] * odPrev[2][pp][i];
+                double dot = dv[0] * Ex[i] / 2.0;
+                dot += 1.0 * (dv[0] * Ex[i - ox] / 2.0);
+                dot += 1.0 * (dv[1] * Ey[i] / 2.0);
+                dot += 1.0 * (dv[1] * Ey[i - oy] / 2.0);
+                dot += 1.0 * (dv[2] * Ez[i] / 2.0);
+                dot += 1.0 * (dv[2] * Ez[i - oz] / 2.0);
+                *Px = *Px + ga[pp] * (dv[0] * dot);
+                *Py = *Py + ga[pp] * (dv[1] * dot);
+                *Pz = *Pz + ga[pp] * (dv[2] * dot);
+                odPrev[0][pp][i] = jx;
+                odPrev[1][pp][i] = jy;
+                odPrev[2][pp][i] = jz;
+            }
         }
     }
 
@@ -362,7 +427,8 @@ struct OracleSim {
             double v = s.value[static_cast<std::size_t>(step)];
             for (long long id : s.cells) F[s.comp][id] += v;
         }
-        // E half step: polarisations from E^n, curl onto E or D, D -> E
+        // E half step: polarisations from E^n (oriented dipoles first, updatePolE), curl onto E or D, D -> E
+        orDipPolarisation();
         for (int c = 0; c < 3; ++c)
             if (P.comp[c].present) polarisation(c);
         for (int c = 0; c < 3; ++c)

@@ -97,9 +97,19 @@ def _qe_3d():
     return cfg
 
 
+def _c2_aniso():
+    """3-D with five uniaxial ellipsoids (oriented-dipole poles) and the metal sphere; a short
+    pulse so that the field reaches the objects within the run."""
+    cfg = configs.config2(n=36, pml=6, steps=160, nell=5, nfreq=6, metal_radius_cells=18)
+    width = 0.3e-15 / configs.T_UNIT
+    cfg["SourceList"][0]["PulseList"] = [configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)]
+    return cfg
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
-    "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20),
+    "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False),
+    "c2_aniso": _c2_aniso,
     "te_dispersive": _te_dispersive,
     "tm_lorentz": _tm_lorentz,
     "qe_tm": _qe_tm,
