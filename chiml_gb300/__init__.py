@@ -7,6 +7,7 @@ input, step ``ceil(tLim/dt)`` times, then write the flux and detector files.
 There is no CPU fallback: every entry point raises if the library is missing.
 """
 from .api import (  # noqa: F401
+    Batch,
     ChimlError,
     Simulation,
     Stats,

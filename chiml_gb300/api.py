@@ -75,6 +75,11 @@ EXPORTED = [
     "chiml_stream",
     "chiml_profile_steps",
     "chiml_get_box_noalloc",
+    "chiml_batch_create",
+    "chiml_batch_run",
+    "chiml_batch_finalize",
+    "chiml_batch_member",
+    "chiml_batch_destroy",
 ]
 
 BOX_NOALLOC_MAX_CELLS = 1048576
@@ -113,6 +118,17 @@ def load_library(path=None):
     lib.chiml_get_box_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int32),
                                           ctypes.POINTER(ctypes.c_double)]
     lib.chiml_get_box_noalloc.restype = ctypes.c_int
+    lib.chiml_batch_create.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(_Options),
+                                       ctypes.POINTER(ctypes.c_void_p)]
+    lib.chiml_batch_create.restype = ctypes.c_int
+    lib.chiml_batch_run.argtypes = [ctypes.c_void_p]
+    lib.chiml_batch_run.restype = ctypes.c_int
+    lib.chiml_batch_finalize.argtypes = [ctypes.c_void_p]
+    lib.chiml_batch_finalize.restype = ctypes.c_int
+    lib.chiml_batch_member.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.chiml_batch_member.restype = ctypes.c_void_p
+    lib.chiml_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.chiml_batch_destroy.restype = None
     if path is None:
         _lib = lib
     return lib
@@ -201,6 +217,65 @@ class Simulation:
     def close(self):
         if self._h:
             self._lib.chiml_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Batch:
+    """Independent simulations stepped together (chiml_batch_*): a parameter sweep."""
+
+    def __init__(self, json_paths, precision="fp64", device=0, steps_per_graph=20, out_dir=None):
+        """Members write their outputs under out_dir, or beside their own input files when it is None."""
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        prec = {"fp64": PREC_FP64, "split": PREC_SPLIT}[precision]
+        opt = _Options(prec, device, steps_per_graph, out_dir.encode() if out_dir else None)
+        arr = (ctypes.c_char_p * len(json_paths))(*[os.fsencode(p) for p in json_paths])
+        st = self._lib.chiml_batch_create(arr, len(json_paths), ctypes.byref(opt), ctypes.byref(self._h))
+        if st != 0:
+            raise ChimlError(st, self._lib.chiml_last_error(None).decode())
+        self.n = len(json_paths)
+
+    def _check(self, st):
+        if st != 0:
+            why = "batch call failed"
+            for i in range(self.n):
+                h = self._lib.chiml_batch_member(self._h, i)
+                msg = self._lib.chiml_last_error(ctypes.c_void_p(h)).decode()
+                if msg:
+                    why = "member %d: %s" % (i, msg)
+            raise ChimlError(st, why)
+
+    def run(self):
+        self._check(self._lib.chiml_batch_run(self._h))
+
+    def finalize(self):
+        self._check(self._lib.chiml_batch_finalize(self._h))
+
+    def member_stats(self, i):
+        h = self._lib.chiml_batch_member(self._h, i)
+        if not h:
+            raise IndexError(i)
+        s = Stats()
+        st = self._lib.chiml_query(ctypes.c_void_p(h), ctypes.byref(s))
+        if st != 0:
+            raise ChimlError(st, "query failed")
+        return s
+
+    def close(self):
+        if self._h:
+            self._lib.chiml_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -15,6 +15,8 @@ A = 1e-7                 # length unit (m)
 C0 = 2.9979245e8         # speed of light, as the reference defines it
 T_UNIT = A / C0          # one time unit in seconds
 SEED0 = 20261203
+C4_COUPLING = 1.0e2      # emitter coupling of the batched sweep (chiML's "couplings" units)
+C4_AMPLITUDE = 5.0e8     # peak source amplitude of the batched sweep
 
 
 def ev2fdtd(ev):
@@ -174,6 +176,63 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
         "FluxList": [{"name": "out/c2_flux", "loc": [0.0, 0.0, 0.0], "size": [fb, fb, fb],
                       "lamL": 4.0, "lamR": 7.0, "nfreq": nfreq, "SI": False}],
     }
+
+
+def config4_member(side, detuning_ev, mol_den, pml=16, steps=6000, sheet_cells=10, coupling=C4_COUPLING,
+                   nfreq=50, tag="c4"):
+    """One point of the batched sweep: a 2-D TMz square of ``side`` cells (dx = 5 nm) with a
+    ``sheet_cells``-thick sheet of two-level emitters (z dipoles) across the whole width,
+    transition at 2.0 eV + ``detuning_ev``, dephasing T2 = 30 fs and population decay
+    T1 = 1 ps; an Ez line source on one side, a point detector and a DFT flux line on the
+    other, and the upper-level population recorded every step."""
+    dx = 0.05
+    dt = dx / 2.0
+    size = (side - 1) * dx
+    half = size / 2
+    e0 = 2.0
+    width = 10e-15 / T_UNIT
+    lv = [emitter_level(0.0), emitter_level(e0 + detuning_ev)]
+    sheet_h = size - 2 * (pml + 2) * dx
+    obj = emitter_obj("block", [0.0, 0.0, 0.0], [(0, 0), (1, 0)], lv, [coupling] * 4,
+                      [(1, 0, 1e12, 1.0 / 30e-15)], mol_den, eps=1.0, dtc_levs=[3],
+                      output_pol=tag + "_pol.dat", dtc_base=tag + "_qe_",
+                      size=[sheet_cells * dx, sheet_h, 0.0])
+    src_x = -round((half - (pml + 4) * dx) / dx) * dx
+    out_x = round((half - (pml + 6) * dx) / dx) * dx
+    return {
+        "CompCell": {"size": [size, size, 0.0], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
+                     "a": A, "pol": "Ez", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
+        "PML": {"thickness": [pml * dx, pml * dx, 0.0], "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
+        "SourceList": [{"pol": "Ez", "loc": [src_x, 0.0, 0.0], "size": [0.0, sheet_h, 0.0],
+                        "PulseList": [_gauss(ev2fdtd(e0), 1.0 / width, 4.0, 3 * width, amp=C4_AMPLITUDE)]}],
+        "TFSF": [],
+        "ObjectList": [obj],
+        "DetectorList": [{"loc": [out_x, 0.0, 0.0], "size": [0.0, 0.0, 0.0], "type": "Ez", "fname": tag + "_pt",
+                          "dtc_class": "txt", "SI": False, "Time_Interval": dt}],
+        "FluxList": [{"name": tag + "_flux", "loc": [out_x, 0.0, 0.0], "size": [0.0, sheet_h, 0.0],
+                      "lamL": 5.0, "lamR": 7.5, "nfreq": nfreq, "SI": False}],
+    }
+
+
+def config4(n=96, sides=tuple(range(192, 769, 64)), steps=6000, seed=SEED0 + 4, pml=16):
+    """The batched sweep: ``n`` independent 2-D TMz emitter simulations. Square sides are
+    drawn by seed from ``sides``; detuning runs over -100..+100 meV and molecular density
+    over 1e25..1e26 m^-3 (log-spaced) on a grid of the two, in sweep order. Returns
+    [(name, cfg)]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nd = max(1, int(round(math.sqrt(n * 1.5))))
+    while n % nd:
+        nd -= 1
+    nn = n // nd
+    dets = np.linspace(-0.1, 0.1, nd) if nd > 1 else np.zeros(1)
+    dens = np.logspace(25, 26, nn) if nn > 1 else np.array([1e25])
+    out = []
+    for k in range(n):
+        side = int(rng.choice(np.asarray(sides)))
+        det, den = float(dets[k % nd]), float(dens[k // nd])
+        name = "c4_%03d" % k
+        out.append((name, config4_member(side, det, den, pml=pml, steps=steps, tag=name)))
+    return out
 
 
 def write_json(cfg, path):

@@ -1031,6 +1031,86 @@ chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out) {
     }
 }
 
+}  // extern "C"
+
+struct chiml_batch {
+    std::vector<chiml_sim*> members;
+    int graphSteps = 0;
+    ~chiml_batch() {
+        for (chiml_sim* m : members) chiml_destroy(m);
+    }
+};
+
+extern "C" {
+
+chiml_status chiml_batch_create(const char* const* json_paths, int n, const chiml_options* opt, chiml_batch** out) {
+    if (!out || !json_paths || n < 1) return CHIML_E_INPUT;
+    *out = nullptr;
+    std::unique_ptr<chiml_batch> b(new chiml_batch());
+    for (int i = 0; i < n; ++i) {
+        chiml_sim* m = nullptr;
+        // without an output directory, a member writes beside its own input file
+        chiml_options o = opt ? *opt : chiml_options{CHIML_PREC_FP64, 0, 0, nullptr};
+        std::string dir;
+        if (!o.out_dir && json_paths[i]) {
+            dir = json_paths[i];
+            const size_t slash = dir.find_last_of('/');
+            dir = slash == std::string::npos ? std::string(".") : dir.substr(0, slash + 1);
+            o.out_dir = dir.c_str();
+        }
+        const chiml_status st = chiml_create(json_paths[i], &o, &m);
+        if (st != CHIML_OK) {
+            g_createError = std::string("batch member ") + std::to_string(i) + " (" +
+                            (json_paths[i] ? json_paths[i] : "null") + "): " + g_createError;
+            return st;
+        }
+        b->members.push_back(m);
+    }
+    b->graphSteps = opt ? opt->steps_per_graph : 0;
+    *out = b.release();
+    return CHIML_OK;
+}
+
+chiml_status chiml_batch_run(chiml_batch* batch) {
+    if (!batch) return CHIML_E_STATE;
+    // queue one graph-sized chunk of every unfinished member in turn; members own
+    // separate streams, so the chunks run concurrently on the device
+    bool left = true;
+    while (left) {
+        left = false;
+        for (chiml_sim* m : batch->members) {
+            chiml_stats st;
+            m->h.sim->fillStats(&st);
+            if (st.steps_done >= st.steps_total) continue;
+            const int64_t chunk = batch->graphSteps > 0 ? 4LL * batch->graphSteps : 64;
+            const chiml_status s = chiml_step(m, chunk);
+            if (s != CHIML_OK) return s;
+            left = true;
+        }
+    }
+    for (chiml_sim* m : batch->members) {
+        const chiml_status s = chiml_sync(m);
+        if (s != CHIML_OK) return s;
+    }
+    return CHIML_OK;
+}
+
+chiml_status chiml_batch_finalize(chiml_batch* batch) {
+    if (!batch) return CHIML_E_STATE;
+    for (chiml_sim* m : batch->members) {
+        const chiml_status s = chiml_finalize(m);
+        if (s != CHIML_OK) return s;
+    }
+    return CHIML_OK;
+}
+
+chiml_sim* chiml_batch_member(chiml_batch* batch, int i) {
+    if (!batch || i < 0 || i >= static_cast<int>(batch->members.size())) return nullptr;
+    return batch->members[i];
+}
+
+void chiml_batch_destroy(chiml_batch* batch) { delete batch; }
+
 chiml_status chiml_get_box_noalloc(chiml_sim* sim, int comp, const int32_t box[6], double* out) {
     if (!sim || !box || !out) return CHIML_E_STATE;
     const int b[6] = {box[0], box[1], box[2], box[3], box[4], box[5]};

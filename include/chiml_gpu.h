@@ -104,6 +104,31 @@ void* chiml_stream(chiml_sim* sim);
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
+/* A batch of independent simulations stepped together (a parameter sweep): each
+ * member keeps its own plan, device state, stream and CUDA graph; chiml_batch_run
+ * queues the members' step graphs round-robin so that their kernels run
+ * concurrently. The reference runs such sweeps as separate processes. */
+typedef struct chiml_batch chiml_batch;
+
+/* Creates one member per input file, all with the same options, except that with
+ * opt->out_dir NULL each member's relative output names resolve against the
+ * directory of its own input file (one directory per sweep point, as separate
+ * reference runs would use). On failure no batch is returned and
+ * chiml_last_error(NULL) names the failing input; after a failed run or finalize,
+ * chiml_last_error of the failing member (chiml_batch_member) holds the reason. */
+chiml_status chiml_batch_create(const char* const* json_paths, int n, const chiml_options* opt, chiml_batch** out);
+
+/* Advances every member to its last step (ceil(tLim/dt) each) and waits. */
+chiml_status chiml_batch_run(chiml_batch* batch);
+
+/* Writes every member's output files (as chiml_finalize). */
+chiml_status chiml_batch_finalize(chiml_batch* batch);
+
+/* Member i of the batch (owned by the batch), or NULL when i is out of range. */
+chiml_sim* chiml_batch_member(chiml_batch* batch, int i);
+
+void chiml_batch_destroy(chiml_batch* batch);
+
 /* Largest box, in cells, that chiml_get_box_noalloc reads in one call. */
 #define CHIML_BOX_NOALLOC_MAX_CELLS 1048576
 

@@ -1,0 +1,124 @@
+"""The batched sweep (chiml_batch_*): independent 2-D TMz emitter simulations of uneven
+sizes stepped together.
+
+Batching changes only when each member's kernels run, never what they compute: every
+member of a batch must write the same files as the same input run alone (byte for
+byte), and in FP64 the oracle's files to the parity bar.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from compare import compare_dirs
+
+TOL_FP64 = 1e-10
+
+
+def _small_sweep(n=4, steps=240):
+    from chiml_gb300 import configs
+    return configs.config4(n=n, sides=(40, 48, 56, 64), steps=steps, pml=8)
+
+
+def _write_members(root, members):
+    from chiml_gb300 import configs
+    paths = []
+    for name, cfg in members:
+        d = os.path.join(str(root), name)
+        os.makedirs(d, exist_ok=True)
+        paths.append(configs.write_json(cfg, os.path.join(d, "in.json")))
+    return paths
+
+
+def _same_files(a, b):
+    n = 0
+    for d, _, files in os.walk(a):
+        for f in files:
+            if f == "in.json":
+                continue
+            pa = os.path.join(d, f)
+            pb = os.path.join(b, os.path.relpath(pa, a))
+            assert os.path.exists(pb), pb
+            assert open(pa, "rb").read() == open(pb, "rb").read(), f
+            n += 1
+    assert n >= 4
+    return n
+
+
+def test_config4_sweep_covers_the_grid():
+    from chiml_gb300 import configs
+    members = configs.config4()
+    assert len(members) == 96
+    sides, dets, dens = set(), set(), set()
+    for name, cfg in members:
+        cc = cfg["CompCell"]
+        side = int(round(cc["size"][0] / cc["stepSize"][0])) + 1
+        assert cc["size"][0] == cc["size"][1] and cc["size"][2] == 0.0 and cc["pol"] == "Ez"
+        assert side in range(192, 769, 64)
+        sides.add(side)
+        qe = cfg["ObjectList"][0]
+        dets.add(round(qe["Energy_Levels"][1]["E_cen"][0] - 2.0, 9))
+        dens.add(qe["mol_den"])
+        assert int(round(qe["size"][0] / cc["stepSize"][0])) == 10
+        assert cfg["PML"]["thickness"][0] == pytest.approx(16 * cc["stepSize"][0])
+        relax = qe["RelaxationOperators"][0]
+        assert relax["dephasing_rate"] == pytest.approx(1.0 / 30e-15)
+        steps = cfg["CompCell"]["tLim"] / cc["dt"]
+        assert abs(steps - 6000) < 1
+    assert len(sides) >= 6
+    assert min(dets) == pytest.approx(-0.1) and max(dets) == pytest.approx(0.1)
+    assert min(dens) == pytest.approx(1e25) and max(dens) == pytest.approx(1e26)
+    assert len(dets) * len(dens) == 96
+    # the same seed draws the same sizes
+    assert [c["CompCell"]["size"] for _, c in configs.config4()] == [c["CompCell"]["size"] for _, c in members]
+
+
+@pytest.mark.gpu
+def test_batch_fp64_matches_oracle(built_engine, built_oracle, tmp_path):
+    import oracle
+    from chiml_gb300 import Batch
+    members = _small_sweep()
+    paths = _write_members(tmp_path / "gpu", members)
+    with Batch(paths, precision="fp64", steps_per_graph=16) as b:
+        b.run()
+        b.finalize()
+        for i in range(len(paths)):
+            st = b.member_stats(i)
+            assert st.steps_done == st.steps_total > 0
+            assert st.n_emitters == 1
+    for (name, _), p in zip(members, paths):
+        ref = tmp_path / "oracle" / name
+        os.makedirs(ref)
+        oracle.run(p, str(ref))
+        res = compare_dirs(str(ref), os.path.dirname(p), TOL_FP64)
+        assert any("qe" in k for k in res) and any("flux" in k for k in res)
+
+
+@pytest.mark.gpu
+def test_batch_split_equals_members_run_alone(built_engine, tmp_path):
+    from chiml_gb300 import Batch, Simulation
+    members = _small_sweep(n=6, steps=200)
+    paths = _write_members(tmp_path / "batch", members)
+    with Batch(paths, precision="split", steps_per_graph=16) as b:
+        b.run()
+        b.finalize()
+    for name, cfg in members:
+        alone = tmp_path / "alone" / name
+        os.makedirs(alone)
+        sim = Simulation(os.path.join(str(tmp_path / "batch"), name, "in.json"), precision="split",
+                         steps_per_graph=16, out_dir=str(alone))
+        sim.step()
+        sim.finalize()
+        _same_files(str(tmp_path / "batch" / name), str(alone))
+
+
+@pytest.mark.gpu
+def test_batch_rejects_a_bad_member(built_engine, tmp_path):
+    from chiml_gb300 import Batch, ChimlError
+    members = _small_sweep(n=2, steps=10)
+    paths = _write_members(tmp_path, members)
+    bad = tmp_path / "bad.json"
+    bad.write_text("{ not json")
+    with pytest.raises(ChimlError) as ei:
+        Batch([paths[0], str(bad), paths[1]])
+    assert "batch member 1" in str(ei.value)
