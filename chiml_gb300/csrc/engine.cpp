@@ -3,6 +3,7 @@
 // and writes the outputs at finalize.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -318,6 +319,23 @@ public:
 
     double h2dBytes() const { return mem_.h2d; }
     double d2hBytes() const { return d2h_; }
+
+    // ---- batched sweep: the device descriptors of this member, for packed launches ----
+    const dev::Pass<T>& hPass() const { return hPass_; }
+    const dev::Pass<T>& ePass() const { return ePass_; }
+    const dev::Fields<T>& fields() const { return fields_; }
+    const dev::SourceTable& sources() const { return src_; }
+    const dev::RecordTable& records() const { return recT_; }
+    const std::vector<dev::DftTable<T>>& dftTables() const { return dft_; }
+    const std::vector<dev::EmitterDev>& emitters() const { return emit_; }
+    int* stepCounter() const { return dStep_; }
+    long long stepsLeft() const { return finalized_ ? 0 : static_cast<long long>(P.nSteps) - stepsDone_; }
+    // Counts n steps that a packed launch sequence queued for this member.
+    void stepsRunElsewhere(long long n) {
+        if (finalized_) throw std::logic_error("step after finalize");
+        if (n > stepsLeft()) throw std::logic_error("more steps than the member has left");
+        stepsDone_ += static_cast<int>(n);
+    }
 
 private:
     Plan P;
@@ -924,6 +942,143 @@ private:
     }
 };
 
+// Independent simulations of one precision stepped by packed launches: per step one
+// launch of each kind of work covers every member (H pass, sources, oriented-dipole P,
+// E pass, emitters, step counters, detector records, DFT sample and fold), in the order
+// of Sim::enqueueStep. The members' descriptors sit in device job arrays; a work table
+// per launch maps each block to {job, block of that job}. Members run the generic form
+// of the passes. The step is captured into a CUDA graph of `graphSteps` steps.
+template <typename T>
+class PackedBatch {
+public:
+    PackedBatch(const std::vector<Sim<T>*>& members, int device) : members_(members) {
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        ck(cudaStreamCreate(&stream_), "cudaStreamCreate");
+        std::vector<dev::Pass<T>> hp, ep;
+        std::vector<dev::SrcJob<T>> src;
+        std::vector<dev::RecJob<T>> rec;
+        std::vector<dev::DftJob<T>> dft;
+        std::vector<dev::EmitJob<T>> em;
+        std::vector<int*> steps;
+        std::vector<int2> passW, odW, srcW, recW, smpW, foldW, addW, updW[4];
+        auto add = [](std::vector<int2>& w, int job, long long blocks) {
+            for (long long b = 0; b < blocks; ++b) w.push_back(make_int2(job, static_cast<int>(b)));
+        };
+        for (Sim<T>* m : members) {
+            const int j = static_cast<int>(hp.size());
+            hp.push_back(m->hPass());
+            ep.push_back(m->ePass());
+            add(passW, j, dev::pass_blocks<T>(m->hPass()));
+            if (dev::pass_blocks<T>(m->ePass()) != dev::pass_blocks<T>(m->hPass()))
+                throw std::logic_error("H and E passes of a member differ in extent");
+            if (m->ePass().od.n > 0) add(odW, j, dev::ordip_blocks(m->ePass().od.n));
+            if (m->sources().n > 0) {
+                add(srcW, static_cast<int>(src.size()), dev::sources_blocks(m->sources().n));
+                src.push_back(dev::SrcJob<T>{m->sources(), m->fields(), m->stepCounter()});
+            }
+            if (m->records().n > 0) {
+                add(recW, static_cast<int>(rec.size()), dev::record_blocks(m->records().n));
+                rec.push_back(dev::RecJob<T>{m->records(), m->fields(), m->stepCounter()});
+            }
+            for (const auto& d : m->dftTables()) {
+                if (d.npts == 0) continue;
+                const int q = static_cast<int>(dft.size());
+                add(smpW, q, dev::dft_sample_blocks(d.npts));
+                add(foldW, q, dev::dft_fold_blocks(d.npts, d.nfreq));
+                dft.push_back(dev::DftJob<T>{d, m->fields(), m->stepCounter()});
+            }
+            for (const auto& e : m->emitters()) {
+                const int q = static_cast<int>(em.size());
+                add(addW, q, 3LL * dev::emitter_addp_blocks_per_comp(e));
+                add(updW[dev::emitter_level_group(e.N)], q, dev::emitter_update_blocks(e));
+                dev::EmitJob<T> jb{};
+                jb.e = e;
+                for (int c = 0; c < 3; ++c) jb.f[c] = m->fields().f[c];
+                jb.step = m->stepCounter();
+                em.push_back(jb);
+            }
+            steps.push_back(m->stepCounter());
+        }
+        auto map = [this](const std::vector<int2>& w) {
+            if (w.size() > 0x7fffffffULL) throw UnsupportedError("a packed launch of more than 2^31 blocks");
+            return dev::WorkMap{mem_.upload(w), static_cast<int>(w.size())};
+        };
+        dH_ = mem_.upload(hp);
+        dE_ = mem_.upload(ep);
+        dSrc_ = mem_.upload(src);
+        dRec_ = mem_.upload(rec);
+        dDft_ = mem_.upload(dft);
+        dEm_ = mem_.upload(em);
+        nEm_ = static_cast<int>(em.size());
+        dSteps_ = mem_.upload(steps);
+        nSteps_ = static_cast<int>(steps.size());
+        passMap_ = map(passW);
+        odMap_ = map(odW);
+        srcMap_ = map(srcW);
+        recMap_ = map(recW);
+        smpMap_ = map(smpW);
+        foldMap_ = map(foldW);
+        addMap_ = map(addW);
+        for (int g = 0; g < 4; ++g) updMap_[g] = map(updW[g]);
+        ck(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    }
+    ~PackedBatch() {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        if (stream_) {
+            cudaStreamSynchronize(stream_);
+            cudaStreamDestroy(stream_);
+        }
+    }
+
+    // Queues n steps of every member and waits for them.
+    void run(long long n, int graphSteps) {
+        for (Sim<T>* m : members_) ck(cudaStreamSynchronize(m->stream()), "cudaStreamSynchronize");
+        if (graphSteps > 0 && n >= graphSteps) {
+            if (!graph_) {
+                cudaGraph_t g;
+                ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+                for (int k = 0; k < graphSteps; ++k) enqueueStep();
+                ck(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
+                ck(cudaGraphInstantiate(&graph_, g, 0), "cudaGraphInstantiate");
+                cudaGraphDestroy(g);
+            }
+            for (; n >= graphSteps; n -= graphSteps) ck(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
+        }
+        for (; n > 0; --n) enqueueStep();
+        ck(cudaGetLastError(), "kernel launch");
+        ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    }
+
+private:
+    std::vector<Sim<T>*> members_;
+    DevMem mem_;
+    cudaStream_t stream_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    dev::Pass<T>* dH_ = nullptr;
+    dev::Pass<T>* dE_ = nullptr;
+    dev::SrcJob<T>* dSrc_ = nullptr;
+    dev::RecJob<T>* dRec_ = nullptr;
+    dev::DftJob<T>* dDft_ = nullptr;
+    dev::EmitJob<T>* dEm_ = nullptr;
+    int nEm_ = 0;
+    int** dSteps_ = nullptr;
+    int nSteps_ = 0;
+    dev::WorkMap passMap_{}, odMap_{}, srcMap_{}, recMap_{}, smpMap_{}, foldMap_{}, addMap_{}, updMap_[4]{};
+
+    void enqueueStep() {
+        void* s = stream_;
+        dev::launch_pass_packed<T>(dH_, passMap_, false, s);
+        dev::launch_sources_packed<T>(dSrc_, srcMap_, s);
+        dev::launch_ordip_packed<T>(dE_, odMap_, s);
+        dev::launch_pass_packed<T>(dE_, passMap_, true, s);
+        dev::launch_emitter_packed<T>(dEm_, nEm_, addMap_, updMap_, s);
+        dev::launch_increment_packed(dSteps_, nSteps_, s);
+        dev::launch_record_packed<T>(dRec_, recMap_, s);
+        dev::launch_dft_sample_packed<T>(dDft_, smpMap_, s);
+        dev::launch_dft_fold_packed<T>(dDft_, foldMap_, s);
+    }
+};
+
 struct Handle {
     std::unique_ptr<SimBase> sim;
     std::string err;
@@ -1036,10 +1191,47 @@ chiml_status chiml_get_field(chiml_sim* sim, int comp, double* out) {
 struct chiml_batch {
     std::vector<chiml_sim*> members;
     int graphSteps = 0;
+    int precision = CHIML_PREC_FP64;
+    int device = 0;
     ~chiml_batch() {
         for (chiml_sim* m : members) chiml_destroy(m);
     }
 };
+
+namespace {
+
+// Phases of packed steps: each phase runs the unfinished members for the fewest steps
+// any of them has left, so members with different step counts each stop at their own.
+template <typename T>
+chiml_status batch_run(chiml_batch* batch) {
+    std::vector<Sim<T>*> all;
+    for (chiml_sim* m : batch->members) {
+        auto* s = dynamic_cast<Sim<T>*>(m->h.sim.get());
+        if (!s) return CHIML_E_STATE;
+        all.push_back(s);
+    }
+    try {
+        for (;;) {
+            std::vector<Sim<T>*> live;
+            long long n = 0;
+            for (Sim<T>* s : all)
+                if (s->stepsLeft() > 0) {
+                    live.push_back(s);
+                    n = (n == 0) ? s->stepsLeft() : std::min(n, s->stepsLeft());
+                }
+            if (live.empty()) break;
+            PackedBatch<T> pb(live, batch->device);
+            pb.run(n, batch->graphSteps);
+            for (Sim<T>* s : live) s->stepsRunElsewhere(n);
+        }
+    } catch (const std::exception& e) {
+        batch->members[0]->h.err = std::string("batched step: ") + e.what();
+        return status_of(e);
+    }
+    return CHIML_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1067,30 +1259,23 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
         b->members.push_back(m);
     }
     b->graphSteps = opt ? opt->steps_per_graph : 0;
+    b->precision = opt ? opt->precision : CHIML_PREC_FP64;
+    b->device = opt ? opt->device : 0;
     *out = b.release();
     return CHIML_OK;
 }
 
 chiml_status chiml_batch_run(chiml_batch* batch) {
     if (!batch) return CHIML_E_STATE;
-    // queue one graph-sized chunk of every unfinished member in turn; members own
-    // separate streams, so the chunks run concurrently on the device
-    bool left = true;
-    while (left) {
-        left = false;
-        for (chiml_sim* m : batch->members) {
-            chiml_stats st;
-            m->h.sim->fillStats(&st);
-            if (st.steps_done >= st.steps_total) continue;
-            const int64_t chunk = batch->graphSteps > 0 ? 4LL * batch->graphSteps : 64;
-            const chiml_status s = chiml_step(m, chunk);
-            if (s != CHIML_OK) return s;
-            left = true;
-        }
-    }
+    const chiml_status st = batch->precision == CHIML_PREC_SPLIT ? batch_run<float>(batch) : batch_run<double>(batch);
+    if (st != CHIML_OK) return st;
     for (chiml_sim* m : batch->members) {
-        const chiml_status s = chiml_sync(m);
-        if (s != CHIML_OK) return s;
+        try {
+            m->h.sim->checkDeviceErrors();
+        } catch (const std::exception& e) {
+            m->h.err = e.what();
+            return status_of(e);
+        }
     }
     return CHIML_OK;
 }

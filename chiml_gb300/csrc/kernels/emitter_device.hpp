@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include "fdtd_device.hpp"
+
 namespace chiml {
 namespace dev {
 
@@ -53,6 +55,24 @@ struct EmitterDev {
 // to the number of completed steps when these run.
 template <typename T>
 void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream);
+
+// The same step for the emitter objects of many simulations (the batched sweep): the
+// addP launch and one density-update launch per level-count group (2, 3, 4 levels,
+// other), each over the packed blocks of its jobs, then one reduce block per job.
+template <typename T>
+struct EmitJob {
+    EmitterDev e;
+    T* f[3];
+    const int* step;
+};
+// addP blocks per component (3 components per job)
+__host__ __device__ inline int emitter_addp_blocks_per_comp(const EmitterDev& e) {
+    return (e.addN[0] * e.addN[1] * e.addN[2] + 255) / 256;
+}
+int emitter_update_blocks(const EmitterDev& e);
+int emitter_level_group(int N);                          // update group of an N-level emitter
+template <typename T>
+void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[4], void* stream);
 
 }  // namespace dev
 }  // namespace chiml

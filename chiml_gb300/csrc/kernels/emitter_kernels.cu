@@ -62,15 +62,15 @@ __device__ __forceinline__ void den_deriv(const EmitterDev& e, int N, const C2* 
         }
 }
 
+// addP of component c over points t = tBegin, tBegin + tStride, ...
 template <typename T>
-__global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex, T* Ey, T* Ez) {
-    const int c = blockIdx.y;
+__device__ __forceinline__ void addpRange(const EmitterDev& e, T* Ex, T* Ey, T* Ez, int c, int tBegin, int tStride) {
     if (!e.comp[c]) return;
     T* E = c == 0 ? Ex : (c == 1 ? Ey : Ez);
     const int ox = (c == 0), oy = (c == 1), oz = (c == 2) ? e.zOff : 0;
     const int n = e.addN[0] * e.addN[1] * e.addN[2];
     const double* P = e.P + static_cast<long long>(c) * e.pBox;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    for (int t = tBegin; t < n; t += tStride) {
         const int ii = t % e.addN[0];
         const int r = t / e.addN[0];
         const int jj = r % e.addN[1];
@@ -86,14 +86,19 @@ __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex,
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex, T* Ey, T* Ez) {
+    addpRange(e, Ex, Ey, Ez, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+// Block `blk` of the density update (cells kEmThreads * blk ...), writing partial row blk.
 template <typename T, int NT>
-__global__ void __launch_bounds__(kEmThreads) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
-                                                               const T* __restrict__ Ey, const T* __restrict__ Ez,
-                                                               const int* __restrict__ stepPtr) {
+__device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __restrict__ Ex, const T* __restrict__ Ey,
+                                            const T* __restrict__ Ez, const int* __restrict__ stepPtr, int blk) {
     constexpr int MAXN2 = (NT ? NT * NT : kMaxEmitterLevels * kMaxEmitterLevels);
     const int N = NT ? NT : e.N;
     const int n2 = N * N;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blk * kEmThreads + threadIdx.x;
     const int s = *stepPtr;
     const bool popStep = (s % e.dtcTimeInt) == 0;
     C2 popAcc[kMaxDtc];
@@ -177,12 +182,19 @@ __global__ void __launch_bounds__(kEmThreads) k_emitter_update(const EmitterDev 
     }
     if (threadIdx.x == 0) {
         for (int d = 0; d < e.nDtc; ++d)
-            e.popPartial[static_cast<long long>(blockIdx.x) * e.nDtc + d] = make_double2(red[2 * d][0], red[2 * d + 1][0]);
-        for (int c = 0; c < 3; ++c) e.totPartial[blockIdx.x * 3 + c] = red[2 * kMaxDtc + c][0];
+            e.popPartial[static_cast<long long>(blk) * e.nDtc + d] = make_double2(red[2 * d][0], red[2 * d + 1][0]);
+        for (int c = 0; c < 3; ++c) e.totPartial[blk * 3 + c] = red[2 * kMaxDtc + c][0];
     }
 }
 
-__global__ void __launch_bounds__(256) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
+template <typename T, int NT>
+__global__ void __launch_bounds__(kEmThreads) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
+                                                               const T* __restrict__ Ey, const T* __restrict__ Ez,
+                                                               const int* __restrict__ stepPtr) {
+    updateBlock<T, NT>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
+}
+
+__device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __restrict__ stepPtr) {
     const int s = *stepPtr;
     __shared__ double red[256];
     const bool popStep = (s % e.dtcTimeInt) == 0;
@@ -219,13 +231,59 @@ __global__ void __launch_bounds__(256) k_emitter_reduce(const EmitterDev e, cons
     }
 }
 
+__global__ void __launch_bounds__(256) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
+    reduceBody(e, stepPtr);
+}
+
+// ---- packed launches (batched sweep): work[b] = {job, block of that job} ----
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const EmitJob<T>& j = jobs[w.x];
+    const int bpc = emitter_addp_blocks_per_comp(j.e);
+    const int c = w.y / bpc, b = w.y % bpc;
+    addpRange(j.e, j.f[0], j.f[1], j.f[2], c, b * 256 + static_cast<int>(threadIdx.x), bpc * 256);
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(kEmThreads) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
+                                                                      const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const EmitJob<T>& j = jobs[w.x];
+    updateBlock<T, NT>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_emitter_reduce_packed(const EmitJob<T>* __restrict__ jobs) {
+    const EmitJob<T>& j = jobs[blockIdx.x];
+    reduceBody(j.e, j.step);
+}
+
 }  // namespace
+
+int emitter_update_blocks(const EmitterDev& e) { return (e.nc + kEmThreads - 1) / kEmThreads; }
+int emitter_level_group(int N) { return N == 2 ? 0 : (N == 3 ? 1 : (N == 4 ? 2 : 3)); }
+
+template <typename T>
+void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[4], void* stream) {
+    if (njobs <= 0) return;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (addp.blocks > 0) k_emitter_addp_packed<T><<<addp.blocks, 256, 0, s>>>(jobs, addp.work);
+    if (update[0].blocks > 0) k_emitter_update_packed<T, 2><<<update[0].blocks, kEmThreads, 0, s>>>(jobs, update[0].work);
+    if (update[1].blocks > 0) k_emitter_update_packed<T, 3><<<update[1].blocks, kEmThreads, 0, s>>>(jobs, update[1].work);
+    if (update[2].blocks > 0) k_emitter_update_packed<T, 4><<<update[2].blocks, kEmThreads, 0, s>>>(jobs, update[2].work);
+    if (update[3].blocks > 0) k_emitter_update_packed<T, 0><<<update[3].blocks, kEmThreads, 0, s>>>(jobs, update[3].work);
+    k_emitter_reduce_packed<T><<<njobs, 256, 0, s>>>(jobs);
+}
+
+template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[4], void*);
+template void launch_emitter_packed<double>(const EmitJob<double>*, int, WorkMap, const WorkMap[4], void*);
 
 template <typename T>
 void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const int nAdd = e.addN[0] * e.addN[1] * e.addN[2];
-    dim3 ga((nAdd + 255) / 256, 3);
+    dim3 ga(emitter_addp_blocks_per_comp(e), 3);
     k_emitter_addp<T><<<ga, 256, 0, s>>>(e, fields[0], fields[1], fields[2]);
     const int blocks = (e.nc + kEmThreads - 1) / kEmThreads;
     switch (e.N) {

@@ -171,6 +171,33 @@ struct DftTable {
     double* im;
 };
 
+// Packed launches of the batched sweep: one launch runs one kind of work for many
+// independent simulations (members). The job array holds each member's descriptor
+// in device memory; work[b] = {job, block of that job} for block b of the launch,
+// each job taking the blocks its own launch would have.
+template <typename T>
+struct SrcJob {
+    SourceTable s;
+    Fields<T> f;
+    const int* step;
+};
+template <typename T>
+struct RecJob {
+    RecordTable r;
+    Fields<T> f;
+    const int* step;
+};
+template <typename T>
+struct DftJob {
+    DftTable<T> d;
+    Fields<T> f;
+    const int* step;
+};
+struct WorkMap {
+    const int2* work;  // [blocks]
+    int blocks;
+};
+
 // Launchers (fdtd_kernels.cu). All run on the given stream.
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream);
@@ -186,6 +213,29 @@ void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step
 template <typename T>
 void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream);
 void launch_increment(int* step, void* stream);
+
+// Blocks each job of a packed launch takes (the grid of its own launch).
+template <typename T>
+long long pass_blocks(const Pass<T>& p);  // generic form
+long long ordip_blocks(long long n);
+int sources_blocks(int n);
+int record_blocks(int n);
+long long dft_sample_blocks(long long npts);
+long long dft_fold_blocks(long long npts, int nfreq);
+
+template <typename T>
+void launch_pass_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream);
+template <typename T>
+void launch_ordip_packed(const Pass<T>* jobs, WorkMap m, void* stream);
+template <typename T>
+void launch_sources_packed(const SrcJob<T>* jobs, WorkMap m, void* stream);
+template <typename T>
+void launch_record_packed(const RecJob<T>* jobs, WorkMap m, void* stream);
+template <typename T>
+void launch_dft_sample_packed(const DftJob<T>* jobs, WorkMap m, void* stream);
+template <typename T>
+void launch_dft_fold_packed(const DftJob<T>* jobs, WorkMap m, void* stream);
+void launch_increment_packed(int* const* steps, int n, void* stream);
 
 }  // namespace dev
 }  // namespace chiml

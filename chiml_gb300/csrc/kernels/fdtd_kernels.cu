@@ -97,8 +97,7 @@ __device__ __forceinline__ void cellGeneric(const Pass<T>& p, int ci, long long 
 // UTIL/FDTD_up_eq.cpp:450-521): per pole P = alpha P + xi P_prev + gamma d (d . <E>),
 // <E_c> the average of E_c at the point and one cell below along c.
 template <typename T>
-__global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
-    const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ __forceinline__ void ordipEntry(const Pass<T>& p, long long j) {
     const OrDipDev<T>& od = p.od;
     if (j >= od.n) return;
     const long long i = od.cell[j];
@@ -138,17 +137,28 @@ __global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
+    ordipEntry(p, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
+}
+
+// One cell of the generic form, every component of the pass.
 template <typename T, bool EPASS>
-__global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y * blockDim.y + threadIdx.y;
-    const int y = blockIdx.z * blockDim.z + threadIdx.z;
+__device__ __forceinline__ void passCell(const Pass<T>& p, int x, int y, int z) {
     if (x >= p.lx || z >= p.lz || y >= p.ly) return;
     const long long i = x + static_cast<long long>(p.lx) * (z + static_cast<long long>(p.lz) * y);
     const int coord[3] = {x, y, z};
 #pragma unroll
     for (int ci = 0; ci < 3; ++ci)
         if (p.c[ci].present) cellGeneric<T, EPASS>(p, ci, i, coord);
+}
+
+// Blocks of 32 (x) by 1 (z) by kGenBY (y) cells.
+constexpr int kGenBY = 8;
+
+template <typename T, bool EPASS>
+__global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
+    passCell<T, EPASS>(p, blockIdx.x * 32 + threadIdx.x, blockIdx.z * kGenBY + threadIdx.z, blockIdx.y);
 }
 
 // The dispersive (Lorentz) cells of the E pass, from a list: the interior form
@@ -375,21 +385,25 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     } else {
         // 2-D grids, and 3-D grids with updated halo cells: one thread per cell,
         // all components of the pass
-        dim3 block(32, 1, 8);
-        dim3 grid((p.lx + 31) / 32, p.lz, (p.ly + 7) / 8);
+        dim3 block(32, 1, kGenBY);
+        dim3 grid((p.lx + 31) / 32, p.lz, (p.ly + kGenBY - 1) / kGenBY);
         if (ePass) k_pass<T, true><<<grid, block, 0, s>>>(p);
         else k_pass<T, false><<<grid, block, 0, s>>>(p);
     }
 }
 
 template <typename T>
-__global__ void k_sources(const SourceTable s, const Fields<T> f, const int* __restrict__ step) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sourceEntry(const SourceTable& s, const Fields<T>& f, const int* step, int j) {
     if (j >= s.n) return;
     const int st = *step;
     if (st >= s.nSteps) return;
     const double v = s.value[static_cast<long long>(s.src[j]) * s.nSteps + st];
     atomicAdd(&f.f[s.comp[j]][s.cell[j]], static_cast<T>(v));
+}
+
+template <typename T>
+__global__ void k_sources(const SourceTable s, const Fields<T> f, const int* __restrict__ step) {
+    sourceEntry(s, f, step, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
@@ -399,8 +413,7 @@ void launch_sources(const SourceTable& s, const Fields<T>& f, const int* step, v
 }
 
 template <typename T>
-__global__ void k_record(const RecordTable r, const Fields<T> f, const int* __restrict__ step) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void recordEntry(const RecordTable& r, const Fields<T>& f, const int* step, int j) {
     if (j >= r.n) return;
     const int d = r.det[j];
     const int st = *step;
@@ -414,18 +427,27 @@ __global__ void k_record(const RecordTable r, const Fields<T> f, const int* __re
 }
 
 template <typename T>
+__global__ void k_record(const RecordTable r, const Fields<T> f, const int* __restrict__ step) {
+    recordEntry(r, f, step, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <typename T>
 void launch_record(const RecordTable& r, const Fields<T>& f, const int* step, void* stream) {
     if (r.n == 0) return;
     k_record<T><<<(r.n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(r, f, step);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_sample(const DftTable<T> d, const Fields<T> f, const int* __restrict__ step) {
-    const long long p = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+__device__ __forceinline__ void dftSampleEntry(const DftTable<T>& d, const Fields<T>& f, const int* step, long long p) {
     const int st = *step;
     if (st % d.timeInt != 0 || p >= d.npts) return;
     const int slot = (st / d.timeInt) & (d.K - 1);
     d.ring[static_cast<long long>(slot) * d.stride + p] = f.f[d.comp[p]][d.cell[p]];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_sample(const DftTable<T> d, const Fields<T> f, const int* __restrict__ step) {
+    dftSampleEntry(d, f, step, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
 
 template <typename T>
@@ -473,9 +495,10 @@ __device__ __forceinline__ void lds4(const double* p, double v[4]) {
     v[3] = b.y;
 }
 
+// Tiles tileBegin, tileBegin + tileStride, ... of one fold (all threads of the block).
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
-                                                  int firstSample) {
+__device__ __forceinline__ void foldTiles(const DftTable<T>& d, const int* step, int flushCount, int firstSample,
+                                          long long tileBegin, long long tileStride) {
     constexpr int KS = FoldCfg<T>::KS;
     constexpr int EV = 16 / sizeof(T);  // values per 16-byte copy
     __shared__ __align__(16) T smp[2][KS][kFoldTP];
@@ -498,7 +521,7 @@ __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int
     const int fTiles = (nf + kFoldTF - 1) / kFoldTF;
     const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * fTiles;
     const int stages = (count + KS - 1) / KS;
-    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    for (long long tile = tileBegin; tile < tiles; tile += tileStride) {
         const long long p0 = (tile / fTiles) * kFoldTP;
         const int f0 = static_cast<int>(tile % fTiles) * kFoldTF;
         // copies of stage s into buffer s & 1 (the ring pitch and the phasor rows are 16-byte multiples)
@@ -569,6 +592,12 @@ __global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int
 }
 
 template <typename T>
+__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
+                                                  int firstSample) {
+    foldTiles(d, step, flushCount, firstSample, blockIdx.x, gridDim.x);
+}
+
+template <typename T>
 void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream) {
     if (d.npts == 0) return;
     const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
@@ -579,6 +608,115 @@ void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int 
 __global__ void k_increment(int* step) { *step += 1; }
 
 void launch_increment(int* step, void* stream) { k_increment<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(step); }
+
+// ---- packed launches (batched sweep) ----
+
+template <typename T>
+long long pass_blocks(const Pass<T>& p) {
+    return static_cast<long long>((p.lx + 31) / 32) * p.lz * ((p.ly + kGenBY - 1) / kGenBY);
+}
+long long ordip_blocks(long long n) { return (n + 255) / 256; }
+int sources_blocks(int n) { return (n + 127) / 128; }
+int record_blocks(int n) { return (n + 127) / 128; }
+long long dft_sample_blocks(long long npts) { return (npts + 255) / 256; }
+long long dft_fold_blocks(long long npts, int nfreq) {
+    return ((npts + kFoldTP - 1) / kFoldTP) * ((nfreq + kFoldTF - 1) / kFoldTF);
+}
+
+// Block (bx, bz, by) of a member's generic pass grid from its linear block index.
+template <typename T, bool EPASS>
+__global__ void __launch_bounds__(256) k_pass_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const Pass<T>& p = jobs[w.x];
+    const int gx = (p.lx + 31) / 32;
+    const int bx = w.y % gx;
+    const int r = w.y / gx;
+    const int bz = r % p.lz;
+    const int by = r / p.lz;
+    passCell<T, EPASS>(p, bx * 32 + (threadIdx.x & 31), by * kGenBY + (threadIdx.x >> 5), bz);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_ordip_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    ordipEntry(jobs[w.x], w.y * 256LL + threadIdx.x);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_sources_packed(const SrcJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const SrcJob<T>& j = jobs[w.x];
+    sourceEntry(j.s, j.f, j.step, w.y * 128 + static_cast<int>(threadIdx.x));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_record_packed(const RecJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const RecJob<T>& j = jobs[w.x];
+    recordEntry(j.r, j.f, j.step, w.y * 128 + static_cast<int>(threadIdx.x));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_sample_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const DftJob<T>& j = jobs[w.x];
+    dftSampleEntry(j.d, j.f, j.step, w.y * 256LL + threadIdx.x);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_fold_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const DftJob<T>& j = jobs[w.x];
+    foldTiles(j.d, j.step, -1, 0, w.y, 1LL << 62);
+}
+
+__global__ void k_increment_packed(int* const* __restrict__ steps, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) *steps[j] += 1;
+}
+
+template <typename T>
+void launch_pass_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream) {
+    if (m.blocks <= 0) return;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ePass) k_pass_packed<T, true><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+    else k_pass_packed<T, false><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+}
+template <typename T>
+void launch_ordip_packed(const Pass<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_ordip_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+template <typename T>
+void launch_sources_packed(const SrcJob<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_sources_packed<T><<<m.blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+template <typename T>
+void launch_record_packed(const RecJob<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_record_packed<T><<<m.blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+template <typename T>
+void launch_dft_sample_packed(const DftJob<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_dft_sample_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+template <typename T>
+void launch_dft_fold_packed(const DftJob<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_dft_fold_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+void launch_increment_packed(int* const* steps, int n, void* stream) {
+    if (n > 0) k_increment_packed<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(steps, n);
+}
+
+#define CHIML_PACKED(T)                                                                   \
+    template long long pass_blocks<T>(const Pass<T>&);                                    \
+    template void launch_pass_packed<T>(const Pass<T>*, WorkMap, bool, void*);            \
+    template void launch_ordip_packed<T>(const Pass<T>*, WorkMap, void*);                 \
+    template void launch_sources_packed<T>(const SrcJob<T>*, WorkMap, void*);             \
+    template void launch_record_packed<T>(const RecJob<T>*, WorkMap, void*);              \
+    template void launch_dft_sample_packed<T>(const DftJob<T>*, WorkMap, void*);          \
+    template void launch_dft_fold_packed<T>(const DftJob<T>*, WorkMap, void*);
+CHIML_PACKED(float)
+CHIML_PACKED(double)
+#undef CHIML_PACKED
 
 template void launch_pass<double>(const Pass<double>&, bool, void*);
 template void launch_pass<float>(const Pass<float>&, bool, void*);

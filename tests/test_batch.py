@@ -1,13 +1,12 @@
-"""The batched sweep (chiml_batch_*): independent 2-D TMz emitter simulations of uneven
-sizes stepped together.
+"""The batched sweep (chiml_batch_*): independent simulations of uneven sizes (the sweep
+of 2-D TMz emitter sheets, and mixed members) stepped together by packed launches.
 
-Batching changes only when each member's kernels run, never what they compute: every
+Packing changes which launch runs a member's blocks, never what they compute: every
 member of a batch must write the same files as the same input run alone (byte for
-byte), and in FP64 the oracle's files to the parity bar.
+byte), and in FP64 the oracle's and the reference's files to the parity bar.
 """
 import os
 
-import numpy as np
 import pytest
 
 from compare import compare_dirs
@@ -110,6 +109,32 @@ def test_batch_split_equals_members_run_alone(built_engine, tmp_path):
         sim.step()
         sim.finalize()
         _same_files(str(tmp_path / "batch" / name), str(alone))
+
+
+@pytest.mark.gpu
+def test_batch_of_golden_cases_matches_reference_outputs(built_engine, tmp_path):
+    """Members of different dimensions, media and step counts in one batch (3-D anisotropic
+    and dispersive, 3-D and 2-D emitters, 2-D dielectric): the packed steps run in phases
+    that stop each member at its own last step, and every member still meets the FP64
+    parity bar against the reference's own outputs."""
+    import shutil
+    from conftest import GOLDEN, golden_cases
+    from chiml_gb300 import Batch
+    cases = [c for c in ["c2_aniso", "qe_3d", "qe_tm", "c1_small"] if c in golden_cases()]
+    assert len(cases) >= 3
+    paths = []
+    for c in cases:
+        d = tmp_path / c
+        os.makedirs(d)
+        shutil.copy(os.path.join(GOLDEN, c, "in.json"), d / "in.json")
+        paths.append(str(d / "in.json"))
+    with Batch(paths, precision="fp64", steps_per_graph=8) as b:
+        totals = [b.member_stats(i).steps_total for i in range(len(paths))]
+        assert len(set(totals)) > 1
+        b.run()
+        b.finalize()
+    for c in cases:
+        compare_dirs(os.path.join(GOLDEN, c, "ref"), str(tmp_path / c), TOL_FP64)
 
 
 @pytest.mark.gpu
