@@ -76,6 +76,7 @@ EXPORTED = [
     "chiml_profile_steps",
     "chiml_get_box_noalloc",
     "chiml_batch_create",
+    "chiml_batch_step",
     "chiml_batch_run",
     "chiml_batch_finalize",
     "chiml_batch_member",
@@ -121,6 +122,8 @@ def load_library(path=None):
     lib.chiml_batch_create.argtypes = [ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(_Options),
                                        ctypes.POINTER(ctypes.c_void_p)]
     lib.chiml_batch_create.restype = ctypes.c_int
+    lib.chiml_batch_step.argtypes = [ctypes.c_void_p, ctypes.c_int64]
+    lib.chiml_batch_step.restype = ctypes.c_int
     lib.chiml_batch_run.argtypes = [ctypes.c_void_p]
     lib.chiml_batch_run.restype = ctypes.c_int
     lib.chiml_batch_finalize.argtypes = [ctypes.c_void_p]
@@ -257,7 +260,12 @@ class Batch:
                     why = "member %d: %s" % (i, msg)
             raise ChimlError(st, why)
 
+    def step(self, n):
+        """Advances every unfinished member by n steps (each stops at its last) and waits."""
+        self._check(self._lib.chiml_batch_step(self._h, int(n)))
+
     def run(self):
+        """Advances every member to its last step and waits."""
         self._check(self._lib.chiml_batch_run(self._h))
 
     def finalize(self):

@@ -463,6 +463,16 @@ private:
             e.gamVal = mem_.upload(val);
             e.dt = ep.dt;
             e.hbar = ep.hbar;
+            // PCABAM4 weights (parallelQE.hpp:727-770), as the device formed them
+            e.abP[0] = 55.0 * ep.dt / 24.0;
+            e.abP[1] = -59.0 * ep.dt / 24.0;
+            e.abP[2] = 37.0 * ep.dt / 24.0;
+            e.abP[3] = -9.0 * ep.dt / 24.0;
+            e.abC[0] = 9.0 * ep.dt / 24.0;
+            e.abC[1] = 19.0 * ep.dt / 24.0;
+            e.abC[2] = -5.0 * ep.dt / 24.0;
+            e.abC[3] = ep.dt / 24.0;
+            e.invHbar = 1.0 / ep.hbar;
             e.na = ep.na;
             e.cellGrid = mem_.upload(ep.cellGrid);
             e.cellP = mem_.upload(ep.cellP);
@@ -485,7 +495,8 @@ private:
                         if (gx < D.lx && gy < D.ly && gz < D.lz)
                             epsBox[i + ep.pDims[0] * (k + ep.pDims[2] * j)] = P.epsP[static_cast<std::size_t>(D.idx(gx, gy, gz))];
                     }
-            e.epsBox = mem_.upload(epsBox);
+            for (double& v : epsBox) v = -0.5 / v;
+            e.negHalfInvEps = mem_.upload(epsBox);
             for (int k = 0; k < 3; ++k) {
                 e.pDims[k] = ep.pDims[k];
                 e.addN[k] = ep.addN[k];
@@ -520,17 +531,24 @@ private:
         cudaGraphDestroy(g);
     }
 
+    // A dispersive class whose object has Lorentz poles (the others only divide D by eps_inf).
+    bool lorHasPoles(const ClassInfo& k) const {
+        return k.obj < 0 || k.obj >= static_cast<int>(P.alpha.size()) || !P.alpha[k.obj].empty();
+    }
+
     // Per term, the coordinate bounds outside which no cell uses the term's CPML
     // profile or psi, and whether the 3-D interior kernel form applies.
     void setSlabsAndForm(dev::Pass<T>& pass, bool ePass) const {
         const Dims& D = P.dims;
-        bool interior = D.lz > 1;
+        const bool twoD = D.lz == 1;
+        bool interior = true;
         for (int ci = 0; ci < 3; ++ci) {
             const CompPlan& cp = P.comp[(ePass ? 0 : 3) + ci];
             dev::Comp<T>& dc = pass.c[ci];
             const int axes[2] = {(ci + 2) % 3, (ci + 1) % 3};
             if (!cp.present) {
-                interior = false;
+                // a 2-D grid has one polarisation: the other components are absent
+                if (!twoD) interior = false;
                 continue;
             }
             for (int t = 0; t < 2; ++t) {
@@ -538,6 +556,12 @@ private:
                 const int L = tp.axis == 0 ? D.lx : (tp.axis == 1 ? D.ly : D.lz);
                 dc.slabLo[t] = 0;
                 dc.slabHi[t] = L;
+                if (twoD && axes[t] == 2) {
+                    // the derivative along z of a 2-D grid: the term must be absent
+                    dc.slabHi[t] = 1;
+                    if (tp.present) interior = false;
+                    continue;
+                }
                 const int field = (ePass ? 3 : 0) + (t == 0 ? (ci + 1) % 3 : (ci + 2) % 3);
                 if (!tp.present || tp.axis != axes[t] || tp.field != field) {
                     interior = false;
@@ -572,11 +596,16 @@ private:
         // the interior form never visits halo cells: all of them must be inactive
         if (interior) {
             for (int ci = 0; ci < 3 && interior; ++ci) {
+                if (!P.comp[(ePass ? 0 : 3) + ci].present) continue;  // no code array
                 const std::vector<uint8_t>& code = P.comp[(ePass ? 0 : 3) + ci].code;
+                if (static_cast<long long>(code.size()) != D.cells()) {
+                    interior = false;
+                    break;
+                }
                 for (int y = 0; y < D.ly && interior; ++y)
                     for (int z = 0; z < D.lz && interior; ++z) {
                         const long long row = static_cast<long long>(D.lx) * (z + static_cast<long long>(D.lz) * y);
-                        const bool edge = (y == 0 || y == D.ly - 1 || z == 0 || z == D.lz - 1);
+                        const bool edge = (y == 0 || y == D.ly - 1 || (!twoD && (z == 0 || z == D.lz - 1)));
                         if (edge) {
                             for (int x = 0; x < D.lx; ++x)
                                 if (code[row + x]) interior = false;
@@ -586,7 +615,8 @@ private:
                     }
             }
         }
-        pass.interior3d = interior ? 1 : 0;
+        pass.interior3d = (interior && !twoD) ? 1 : 0;
+        pass.interior2d = (interior && twoD) ? 1 : 0;
         pass.index64 = D.cells() + 2LL * D.lx * D.lz >= (1LL << 31) ? 1 : 0;
     }
 
@@ -721,7 +751,11 @@ private:
                         if (k.kflag[t] || k.psiUpd[t]) o.flags |= (t == 0 ? dev::kFcSlab0 : dev::kFcSlab1);
                         if (base != 0.0 || k.kflag[t] || (psiUpd && k.npsi[t])) write = true;
                     }
-                    if (k.lor) o.flags |= dev::kFcLor;
+                    if (k.lor && lorHasPoles(k)) o.flags |= dev::kFcLor;
+                    if (k.lor && !lorHasPoles(k)) {
+                        o.flags |= dev::kFcDtoE;
+                        o.epsInv = static_cast<T>(1.0 / k.eps);
+                    }
                     if (k.ordip) o.flags |= dev::kFcOrDip;
                     if (k.toD) o.flags |= dev::kFcToD;
                     if (write) o.flags |= dev::kFcWrite;
@@ -754,7 +788,7 @@ private:
             }
             setSlabsAndForm(pass, half == 1);
             if (half == 1) uploadOrDip(pass);
-            if (half == 1 && pass.interior3d) {
+            if (half == 1 && (pass.interior3d || pass.interior2d)) {
                 // dispersive cells leave the interior form for their own list kernel
                 std::vector<int> lc;
                 std::vector<long long> li;
@@ -762,7 +796,8 @@ private:
                     const CompPlan& cp = P.comp[ci];
                     if (!cp.present) continue;
                     for (long long i = 0; i < static_cast<long long>(cp.code.size()); ++i)
-                        if (cp.code[i] && (cp.classes[cp.code[i]].lor || cp.classes[cp.code[i]].ordip)) {
+                        if (cp.code[i] && ((cp.classes[cp.code[i]].lor && lorHasPoles(cp.classes[cp.code[i]])) ||
+                                           cp.classes[cp.code[i]].ordip)) {
                             lc.push_back(ci);
                             li.push_back(i);
                         }
@@ -946,10 +981,16 @@ private:
 // launch of each kind of work covers every member (H pass, sources, oriented-dipole P,
 // E pass, emitters, step counters, detector records, DFT sample and fold), in the order
 // of Sim::enqueueStep. The members' descriptors sit in device job arrays; a work table
-// per launch maps each block to {job, block of that job}. Members run the generic form
-// of the passes. The step is captured into a CUDA graph of `graphSteps` steps.
+// per launch maps each block to {job, block of that job}. 2-D members whose halo carries
+// no update run the 2-D form of the passes (dispersive cells from their list), the
+// others the generic form. The step is captured into a CUDA graph of `graphSteps` steps.
+struct PackedBase {
+    virtual ~PackedBase() {}
+    virtual void run(long long n, int graphSteps) = 0;
+};
+
 template <typename T>
-class PackedBatch {
+class PackedBatch : public PackedBase {
 public:
     PackedBatch(const std::vector<Sim<T>*>& members, int device) : members_(members) {
         ck(cudaSetDevice(device), "cudaSetDevice");
@@ -960,7 +1001,7 @@ public:
         std::vector<dev::DftJob<T>> dft;
         std::vector<dev::EmitJob<T>> em;
         std::vector<int*> steps;
-        std::vector<int2> passW, odW, srcW, recW, smpW, foldW, addW, updW[4];
+        std::vector<int2> passW, p2W[2], lorW, odW, srcW, recW, smpW, foldW, addW, updW[4];
         auto add = [](std::vector<int2>& w, int job, long long blocks) {
             for (long long b = 0; b < blocks; ++b) w.push_back(make_int2(job, static_cast<int>(b)));
         };
@@ -968,9 +1009,22 @@ public:
             const int j = static_cast<int>(hp.size());
             hp.push_back(m->hPass());
             ep.push_back(m->ePass());
-            add(passW, j, dev::pass_blocks<T>(m->hPass()));
-            if (dev::pass_blocks<T>(m->ePass()) != dev::pass_blocks<T>(m->hPass()))
-                throw std::logic_error("H and E passes of a member differ in extent");
+            if (m->hPass().interior2d && m->ePass().interior2d) {
+                // 2-D form: blocks of the present components only
+                const dev::Pass<T>* ps[2] = {&m->hPass(), &m->ePass()};
+                for (int h = 0; h < 2; ++h) {
+                    const long long per = dev::pass2d_blocks_per_comp<T>(*ps[h]);
+                    for (int ci = 0; ci < 3; ++ci)
+                        if (ps[h]->c[ci].present)
+                            for (long long b = 0; b < per; ++b) p2W[h].push_back(make_int2(j, static_cast<int>(ci * per + b)));
+                }
+                if (m->ePass().nLor > 0) add(lorW, j, dev::lorentz_blocks(m->ePass().nLor));
+            } else {
+                // generic form (its E pass runs the dispersive cells itself)
+                add(passW, j, dev::pass_blocks<T>(m->hPass()));
+                if (dev::pass_blocks<T>(m->ePass()) != dev::pass_blocks<T>(m->hPass()))
+                    throw std::logic_error("H and E passes of a member differ in extent");
+            }
             if (m->ePass().od.n > 0) add(odW, j, dev::ordip_blocks(m->ePass().od.n));
             if (m->sources().n > 0) {
                 add(srcW, static_cast<int>(src.size()), dev::sources_blocks(m->sources().n));
@@ -989,7 +1043,10 @@ public:
             }
             for (const auto& e : m->emitters()) {
                 const int q = static_cast<int>(em.size());
-                add(addW, q, 3LL * dev::emitter_addp_blocks_per_comp(e));
+                const int bpc = dev::emitter_addp_blocks_per_comp(e);
+                for (int c = 0; c < 3; ++c)
+                    if (e.comp[c])
+                        for (int b = 0; b < bpc; ++b) addW.push_back(make_int2(q, c * bpc + b));
                 add(updW[dev::emitter_level_group(e.N)], q, dev::emitter_update_blocks(e));
                 dev::EmitJob<T> jb{};
                 jb.e = e;
@@ -1013,6 +1070,9 @@ public:
         dSteps_ = mem_.upload(steps);
         nSteps_ = static_cast<int>(steps.size());
         passMap_ = map(passW);
+        p2Map_[0] = map(p2W[0]);
+        p2Map_[1] = map(p2W[1]);
+        lorMap_ = map(lorW);
         odMap_ = map(odW);
         srcMap_ = map(srcW);
         recMap_ = map(recW);
@@ -1031,7 +1091,7 @@ public:
     }
 
     // Queues n steps of every member and waits for them.
-    void run(long long n, int graphSteps) {
+    void run(long long n, int graphSteps) override {
         for (Sim<T>* m : members_) ck(cudaStreamSynchronize(m->stream()), "cudaStreamSynchronize");
         if (graphSteps > 0 && n >= graphSteps) {
             if (!graph_) {
@@ -1063,14 +1123,17 @@ private:
     int nEm_ = 0;
     int** dSteps_ = nullptr;
     int nSteps_ = 0;
-    dev::WorkMap passMap_{}, odMap_{}, srcMap_{}, recMap_{}, smpMap_{}, foldMap_{}, addMap_{}, updMap_[4]{};
+    dev::WorkMap passMap_{}, p2Map_[2]{}, lorMap_{}, odMap_{}, srcMap_{}, recMap_{}, smpMap_{}, foldMap_{}, addMap_{}, updMap_[4]{};
 
     void enqueueStep() {
         void* s = stream_;
         dev::launch_pass_packed<T>(dH_, passMap_, false, s);
+        dev::launch_pass2d_packed<T>(dH_, p2Map_[0], false, s);
         dev::launch_sources_packed<T>(dSrc_, srcMap_, s);
         dev::launch_ordip_packed<T>(dE_, odMap_, s);
         dev::launch_pass_packed<T>(dE_, passMap_, true, s);
+        dev::launch_pass2d_packed<T>(dE_, p2Map_[1], true, s);
+        dev::launch_lorentz_packed<T>(dE_, lorMap_, s);
         dev::launch_emitter_packed<T>(dEm_, nEm_, addMap_, updMap_, s);
         dev::launch_increment_packed(dSteps_, nSteps_, s);
         dev::launch_record_packed<T>(dRec_, recMap_, s);
@@ -1193,17 +1256,23 @@ struct chiml_batch {
     int graphSteps = 0;
     int precision = CHIML_PREC_FP64;
     int device = 0;
+    // packed launches of the current set of unfinished members, kept between calls
+    std::unique_ptr<PackedBase> packed;
+    std::vector<const void*> packedSet;
     ~chiml_batch() {
+        packed.reset();  // waits for its stream before the members' memory goes
         for (chiml_sim* m : members) chiml_destroy(m);
     }
 };
 
 namespace {
 
-// Phases of packed steps: each phase runs the unfinished members for the fewest steps
-// any of them has left, so members with different step counts each stop at their own.
+// Up to maxSteps packed steps, in phases: each phase runs the unfinished members for the
+// fewest steps any of them has left (or what remains of maxSteps), so members with
+// different step counts each stop at their own. The packed launches are rebuilt only
+// when the set of unfinished members changes.
 template <typename T>
-chiml_status batch_run(chiml_batch* batch) {
+chiml_status batch_steps(chiml_batch* batch, long long maxSteps) {
     std::vector<Sim<T>*> all;
     for (chiml_sim* m : batch->members) {
         auto* s = dynamic_cast<Sim<T>*>(m->h.sim.get());
@@ -1211,18 +1280,25 @@ chiml_status batch_run(chiml_batch* batch) {
         all.push_back(s);
     }
     try {
-        for (;;) {
+        while (maxSteps > 0) {
             std::vector<Sim<T>*> live;
-            long long n = 0;
+            std::vector<const void*> set;
+            long long n = maxSteps;
             for (Sim<T>* s : all)
                 if (s->stepsLeft() > 0) {
                     live.push_back(s);
-                    n = (n == 0) ? s->stepsLeft() : std::min(n, s->stepsLeft());
+                    set.push_back(s);
+                    n = std::min(n, s->stepsLeft());
                 }
             if (live.empty()) break;
-            PackedBatch<T> pb(live, batch->device);
-            pb.run(n, batch->graphSteps);
+            if (!batch->packed || set != batch->packedSet) {
+                batch->packed.reset();
+                batch->packed.reset(new PackedBatch<T>(live, batch->device));
+                batch->packedSet = set;
+            }
+            batch->packed->run(n, batch->graphSteps);
             for (Sim<T>* s : live) s->stepsRunElsewhere(n);
+            maxSteps -= n;
         }
     } catch (const std::exception& e) {
         batch->members[0]->h.err = std::string("batched step: ") + e.what();
@@ -1265,9 +1341,11 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
     return CHIML_OK;
 }
 
-chiml_status chiml_batch_run(chiml_batch* batch) {
+chiml_status chiml_batch_step(chiml_batch* batch, int64_t nsteps) {
     if (!batch) return CHIML_E_STATE;
-    const chiml_status st = batch->precision == CHIML_PREC_SPLIT ? batch_run<float>(batch) : batch_run<double>(batch);
+    if (nsteps <= 0) return CHIML_OK;
+    const chiml_status st =
+        batch->precision == CHIML_PREC_SPLIT ? batch_steps<float>(batch, nsteps) : batch_steps<double>(batch, nsteps);
     if (st != CHIML_OK) return st;
     for (chiml_sim* m : batch->members) {
         try {
@@ -1278,6 +1356,17 @@ chiml_status chiml_batch_run(chiml_batch* batch) {
         }
     }
     return CHIML_OK;
+}
+
+chiml_status chiml_batch_run(chiml_batch* batch) {
+    if (!batch) return CHIML_E_STATE;
+    long long most = 0;
+    for (chiml_sim* m : batch->members) {
+        chiml_stats st;
+        m->h.sim->fillStats(&st);
+        most = std::max<long long>(most, static_cast<long long>(st.steps_total) - st.steps_done);
+    }
+    return chiml_batch_step(batch, most);
 }
 
 chiml_status chiml_batch_finalize(chiml_batch* batch) {

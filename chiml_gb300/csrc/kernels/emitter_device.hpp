@@ -26,13 +26,16 @@ struct EmitterDev {
     const int* gamCol;
     const double* gamVal;
     double dt, hbar, na;
+    // ABM4 step weights (predictor 55, -59, 37, -9; corrector 9, 19, -5, 1, each x dt/24)
+    // and 1/hbar, formed once on the host: FP64 division is slow on this GPU
+    double abP[4], abC[4], invHbar;
     const long long* cellGrid;    // [nc] grid index of each cell
     const int* cellP;             // [nc] P-box index of each cell
     long long unit[3];            // grid index step along x, y, z
     double2* rho;                 // [nm * n2 * nc]
     double2* kd;                  // 4 slots of derivatives, slot stride nm * n2 * nc
     double* P;                    // [3][pBox] polarisation per component
-    const double* epsBox;         // [pBox] relative permittivity at the P-box points
+    const double* negHalfInvEps;  // [pBox] -0.5 / eps at the P-box points (eps the relative permittivity)
     int pDims[3], addN[3], boxBase[3], zOff;
     int lx, lz;                   // grid extents for P-box -> grid indices
     int pBox;

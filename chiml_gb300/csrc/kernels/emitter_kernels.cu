@@ -31,7 +31,6 @@ struct C2 {
     double x, y;
 };
 __device__ __forceinline__ C2 c2(double a, double b) { return C2{a, b}; }
-__device__ __forceinline__ C2 cmul(C2 a, C2 b) { return C2{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 __device__ __forceinline__ C2 cadd(C2 a, C2 b) { return C2{a.x + b.x, a.y + b.y}; }
 __device__ __forceinline__ C2 cconj(C2 a) { return C2{a.x, -a.y}; }
 __device__ __forceinline__ C2 ld(const double2* p) {
@@ -39,27 +38,82 @@ __device__ __forceinline__ C2 ld(const double2* p) {
     return C2{v.x, v.y};
 }
 __device__ __forceinline__ void st(double2* p, C2 v) { *p = make_double2(v.x, v.y); }
-// y + (a, 0) * x, the complex axpy of a real step coefficient
-__device__ __forceinline__ C2 caxpy(double a, C2 x, C2 y) { return cadd(y, cmul(c2(a, 0.0), x)); }
+// y + (a, 0) * x, the complex axpy of a real step coefficient: the imaginary part of
+// (a, 0) contributes exact zeros, so two FMAs give the same value for finite operands.
+__device__ __forceinline__ C2 caxpy(double a, C2 x, C2 y) { return C2{fma(a, x.x, y.x), fma(a, x.y, y.y)}; }
+// s + a * b, four FMAs
+__device__ __forceinline__ C2 cmac(C2 a, C2 b, C2 s) {
+    s.x = fma(a.x, b.x, s.x);
+    s.x = fma(-a.y, b.y, s.x);
+    s.y = fma(a.x, b.y, s.y);
+    s.y = fma(a.y, b.x, s.y);
+    return s;
+}
 
-// (i/hbar) H den + its conjugate transpose, plus the relaxation rows (denDeriv, MKL form)
+// v[k] for a register array: with NT fixed, a chain of selects instead of a dynamic
+// index, which would move the array to local memory.
 template <int NT>
-__device__ __forceinline__ void den_deriv(const EmitterDev& e, int N, const C2* H, const C2* den, C2* out, C2* tmp) {
+__device__ __forceinline__ C2 pick(const C2* v, int k) {
+    if constexpr (NT == 0) {
+        return v[k];
+    } else {
+        C2 r = v[0];
+#pragma unroll
+        for (int i = 1; i < NT * NT; ++i)
+            if (k == i) r = v[i];
+        return r;
+    }
+}
+
+// (i/hbar) H den + its conjugate transpose, plus the relaxation rows (denDeriv, MKL form).
+// The factor i/hbar is purely imaginary: (0, w) * s = (-w s.y, w s.x) exactly. With
+// t(r, c) = (i/hbar) sum_l H[r + l n] den[l + c n], the element pair (i, j), (j, i) of the
+// result is t(i, j) + conj(t(j, i)) and its exact conjugate (the sum commutes and conj
+// is exact), so each pair i <= j is formed once.
+// FP64 issue rate is the bound of this kernel, so the complex products are FMA chains.
+template <int NT>
+__device__ __forceinline__ void den_deriv(const EmitterDev& e, int N, double invHbar, const C2* H, const C2* den, C2* out) {
     const int n = NT ? NT : N;
-    const C2 alpha = c2(0.0, 1.0 / e.hbar);
-    for (int j = 0; j < n; ++j)
-        for (int i = 0; i < n; ++i) {
-            C2 s = c2(0.0, 0.0);
-            for (int l = 0; l < n; ++l) s = cadd(s, cmul(H[i + l * n], den[l + j * n]));
-            tmp[i + j * n] = cmul(alpha, s);
+#pragma unroll
+    for (int i = 0; i < (NT ? NT : n); ++i)
+#pragma unroll
+        for (int j = i; j < (NT ? NT : n); ++j) {
+            C2 sij = c2(0.0, 0.0), sji = c2(0.0, 0.0);
+#pragma unroll
+            for (int l = 0; l < (NT ? NT : n); ++l) {
+                sij = cmac(H[i + l * n], den[l + j * n], sij);
+                if (j != i) sji = cmac(H[j + l * n], den[l + i * n], sji);
+            }
+            if (j == i) sji = sij;
+            const C2 tij = C2{-invHbar * sij.y, invHbar * sij.x};
+            const C2 tji = C2{-invHbar * sji.y, invHbar * sji.x};
+            // the MKL form stores t column-major and adds conj of the transpose:
+            // out[j * n + i] = t(i, j) + conj(t(j, i)), out[i * n + j] its conjugate
+            const C2 o = cadd(tij, cconj(tji));
+            out[j * n + i] = o;
+            if (j != i) out[i * n + j] = cconj(o);
         }
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) out[i * n + j] = cadd(tmp[i * n + j], cconj(tmp[j * n + i]));
-    for (int ii = 0; ii < n * n; ++ii)
+#pragma unroll
+    for (int ii = 0; ii < (NT ? NT * NT : n * n); ++ii)
         for (int p = e.gamRow[ii]; p < e.gamRow[ii + 1]; ++p) {
-            const C2 d = den[e.gamCol[p]];
-            out[ii] = cadd(out[ii], c2(d.x * e.gamVal[p], d.y * e.gamVal[p]));
+            const C2 d = pick<NT>(den, e.gamCol[p]);
+            const double g = e.gamVal[p];
+            out[ii] = C2{fma(d.x, g, out[ii].x), fma(d.y, g, out[ii].y)};
         }
+}
+
+// Sum over the block of one value per thread, in a fixed order (warp shuffle tree,
+// then the warps in order); the result is valid in thread 0.
+__device__ __forceinline__ double blockSum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < kEmThreads / 32; ++w) r += sh[w];
+    __syncthreads();
+    return r;
 }
 
 // addP of component c over points t = tBegin, tBegin + tStride, ...
@@ -80,8 +134,8 @@ __device__ __forceinline__ void addpRange(const EmitterDev& e, T* Ex, T* Ey, T* 
         const long long g = (e.boxBase[0] + ii) +
                             static_cast<long long>(e.lx) * ((e.boxBase[2] + kk) + static_cast<long long>(e.lz) * (e.boxBase[1] + jj));
         double v = static_cast<double>(E[g]);
-        v += -0.5 * P[pa] / e.epsBox[pa];
-        v += -0.5 * P[pb] / e.epsBox[pb];
+        v = fma(P[pa], e.negHalfInvEps[pa], v);  // -0.5 P / eps, the reciprocal formed on the host
+        v = fma(P[pb], e.negHalfInvEps[pb], v);
         E[g] = static_cast<T>(v);
     }
 }
@@ -102,6 +156,7 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
     const int s = *stepPtr;
     const bool popStep = (s % e.dtcTimeInt) == 0;
     C2 popAcc[kMaxDtc];
+#pragma unroll
     for (int d = 0; d < kMaxDtc; ++d) popAcc[d] = c2(0.0, 0.0);
     double Pc[3] = {0.0, 0.0, 0.0};
     if (q < e.nc) {
@@ -109,6 +164,7 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         const long long g = e.cellGrid[q];
         const T* Es[3] = {Ex, Ey, Ez};
         double Ec[3] = {0.0, 0.0, 0.0};
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (!e.comp[c]) continue;
             if (c == 2 && e.gatherZCopy) Ec[c] = static_cast<double>(Es[c][g]);
@@ -117,74 +173,114 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         const bool zeroE = (Ec[0] == 0.0 && Ec[1] == 0.0 && Ec[2] == 0.0);
         const long long slotStride = static_cast<long long>(e.nm) * n2 * e.nc;
         const int s0 = (s - 1) & 3, s1 = (s - 2) & 3, s2 = (s - 3) & 3, s3 = s & 3;  // k_n, k_n-1, k_n-2, k_n-3
-        const double dt = e.dt;
-        const double c55 = 55.0 * dt / 24.0, cm59 = -59.0 * dt / 24.0, c37 = 37.0 * dt / 24.0, cm9 = -9.0 * dt / 24.0;
-        const double c9 = 9.0 * dt / 24.0, c19 = 19.0 * dt / 24.0, cm5 = -5.0 * dt / 24.0, c1 = dt / 24.0;
-        C2 H[MAXN2], a[MAXN2], b[MAXN2], tmp[MAXN2];
+        const double c55 = e.abP[0], cm59 = e.abP[1], c37 = e.abP[2], cm9 = e.abP[3];
+        const double c9 = e.abC[0], c19 = e.abC[1], cm5 = e.abC[2], c1 = e.abC[3];
+        const double invHbar = e.invHbar;
+        const double2* __restrict__ k0 = e.kd + s0 * slotStride;
+        const double2* __restrict__ k1 = e.kd + s1 * slotStride;
+        const double2* __restrict__ k2 = e.kd + s2 * slotStride;
+        double2* __restrict__ k3 = e.kd + s3 * slotStride;
+        C2 H[MAXN2], a[MAXN2], b[MAXN2];
         for (int m = 0; m < e.nm; ++m) {
             // Hamiltonian::getHam
-            for (int i = 0; i < n2; ++i) H[i] = c2(0.0, 0.0);
-            for (int i = 0; i < N; ++i) H[i * N + i] = c2(e.h0[m * N + i], 0.0);
+#pragma unroll
+            for (int i = 0; i < (NT ? MAXN2 : n2); ++i) H[i] = c2(0.0, 0.0);
+#pragma unroll
+            for (int i = 0; i < (NT ? NT : N); ++i) H[i * N + i] = c2(e.h0[m * N + i], 0.0);
             if (!zeroE)
+#pragma unroll
                 for (int c = 0; c < 3; ++c)
                     if (e.addMu[c])
-                        for (int i = 0; i < n2; ++i) H[i] = cadd(H[i], cmul(c2(Ec[c], 0.0), ld(&e.negMu[c * n2 + i])));
+#pragma unroll
+                        for (int i = 0; i < (NT ? MAXN2 : n2); ++i) H[i] = caxpy(Ec[c], ld(&e.negMu[c * n2 + i]), H[i]);
             const long long base = static_cast<long long>(m) * n2 * e.nc + q;
-            // predictor
-            for (int i = 0; i < n2; ++i) {
+            // predictor; for two levels the history values stay in registers for the
+            // corrector, for more they are read again (cache hits)
+            constexpr bool KEEP = NT == 2;
+            constexpr int KN = KEEP ? MAXN2 : 1;
+            C2 r0[KN], h0v[KN], h1v[KN], h2v[KN];
+#pragma unroll
+            for (int i = 0; i < (NT ? MAXN2 : n2); ++i) {
                 const long long o = base + static_cast<long long>(i) * e.nc;
-                C2 p = ld(&e.rho[o]);
-                p = caxpy(c55, ld(&e.kd[s0 * slotStride + o]), p);
-                p = caxpy(cm59, ld(&e.kd[s1 * slotStride + o]), p);
-                p = caxpy(c37, ld(&e.kd[s2 * slotStride + o]), p);
-                p = caxpy(cm9, ld(&e.kd[s3 * slotStride + o]), p);
+                const C2 rr = ld(&e.rho[o]), x0 = ld(&k0[o]), x1 = ld(&k1[o]), x2 = ld(&k2[o]);
+                if constexpr (KEEP) {
+                    r0[i] = rr;
+                    h0v[i] = x0;
+                    h1v[i] = x1;
+                    h2v[i] = x2;
+                }
+                C2 p = caxpy(c55, x0, rr);
+                p = caxpy(cm59, x1, p);
+                p = caxpy(c37, x2, p);
+                p = caxpy(cm9, ld(&k3[o]), p);
                 a[i] = p;
             }
-            den_deriv<NT>(e, N, H, a, b, tmp);  // b = derivative at the prediction
+            den_deriv<NT>(e, N, invHbar, H, a, b);  // b = derivative at the prediction
             // corrector
-            for (int i = 0; i < n2; ++i) {
+#pragma unroll
+            for (int i = 0; i < (NT ? MAXN2 : n2); ++i) {
                 const long long o = base + static_cast<long long>(i) * e.nc;
-                C2 r = ld(&e.rho[o]);
-                r = caxpy(c9, b[i], r);
-                r = caxpy(c19, ld(&e.kd[s0 * slotStride + o]), r);
-                r = caxpy(cm5, ld(&e.kd[s1 * slotStride + o]), r);
-                r = caxpy(c1, ld(&e.kd[s2 * slotStride + o]), r);
+                C2 rr, x0, x1, x2;
+                if constexpr (KEEP) {
+                    rr = r0[i];
+                    x0 = h0v[i];
+                    x1 = h1v[i];
+                    x2 = h2v[i];
+                } else {
+                    rr = ld(&e.rho[o]);
+                    x0 = ld(&k0[o]);
+                    x1 = ld(&k1[o]);
+                    x2 = ld(&k2[o]);
+                }
+                C2 r = caxpy(c9, b[i], rr);
+                r = caxpy(c19, x0, r);
+                r = caxpy(cm5, x1, r);
+                r = caxpy(c1, x2, r);
                 a[i] = r;
                 st(&e.rho[o], r);
             }
-            den_deriv<NT>(e, N, H, a, b, tmp);  // derivative at the new density: the next k_n
-            for (int i = 0; i < n2; ++i) st(&e.kd[s3 * slotStride + base + static_cast<long long>(i) * e.nc], b[i]);
+            den_deriv<NT>(e, N, invHbar, H, a, b);  // derivative at the new density: the next k_n
+#pragma unroll
+            for (int i = 0; i < (NT ? MAXN2 : n2); ++i) st(&k3[base + static_cast<long long>(i) * e.nc], b[i]);
             if (popStep)
-                for (int d = 0; d < e.nDtc; ++d) popAcc[d] = cadd(popAcc[d], a[e.dtcLev[d]]);
+#pragma unroll
+                for (int d = 0; d < kMaxDtc; ++d)
+                    if (d < e.nDtc) popAcc[d] = cadd(popAcc[d], pick<NT>(a, e.dtcLev[d]));
+#pragma unroll
             for (int c = 0; c < 3; ++c) {
                 if (!e.comp[c]) continue;
-                C2 sdot = c2(0.0, 0.0);
-                for (int i = 0; i < n2; ++i) sdot = cadd(sdot, cmul(cconj(a[i]), ld(&e.mu[c * n2 + i])));
-                Pc[c] += e.na * sdot.x;
+                // Re(conj(a) . mu), the real part of zdotc
+                double sdot = 0.0;
+#pragma unroll
+                for (int i = 0; i < (NT ? MAXN2 : n2); ++i) {
+                    const C2 mu = ld(&e.mu[c * n2 + i]);
+                    sdot = fma(a[i].x, mu.x, sdot);
+                    sdot = fma(a[i].y, mu.y, sdot);
+                }
+                Pc[c] += e.na * sdot;
             }
         }
+#pragma unroll
         for (int c = 0; c < 3; ++c)
             if (e.comp[c]) e.P[static_cast<long long>(c) * e.pBox + e.cellP[q]] = Pc[c];
     }
-    // block partial sums, fixed tree order
-    constexpr int NQ = 2 * kMaxDtc + 3;
-    __shared__ double red[NQ][kEmThreads];
-    for (int d = 0; d < kMaxDtc; ++d) {
-        red[2 * d][threadIdx.x] = popAcc[d].x;
-        red[2 * d + 1][threadIdx.x] = popAcc[d].y;
-    }
-    for (int c = 0; c < 3; ++c) red[2 * kMaxDtc + c][threadIdx.x] = Pc[c];
-    __syncthreads();
-    for (int w = kEmThreads / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w)
-            for (int k = 0; k < NQ; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        for (int d = 0; d < e.nDtc; ++d)
-            e.popPartial[static_cast<long long>(blk) * e.nDtc + d] = make_double2(red[2 * d][0], red[2 * d + 1][0]);
-        for (int c = 0; c < 3; ++c) e.totPartial[blk * 3 + c] = red[2 * kMaxDtc + c][0];
-    }
+    // block partial sums of the quantities this step outputs (block-uniform conditions)
+    __shared__ double sh[kEmThreads / 32];
+    if (popStep)
+#pragma unroll
+        for (int d = 0; d < kMaxDtc; ++d) {
+            if (d >= e.nDtc) break;
+            const double sx = blockSum(popAcc[d].x, sh);
+            const double sy = blockSum(popAcc[d].y, sh);
+            if (threadIdx.x == 0) e.popPartial[static_cast<long long>(blk) * e.nDtc + d] = make_double2(sx, sy);
+        }
+    if (e.totP)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (!e.comp[c]) continue;
+            const double v = blockSum(Pc[c], sh);
+            if (threadIdx.x == 0) e.totPartial[blk * 3 + c] = v;
+        }
 }
 
 template <typename T, int NT>

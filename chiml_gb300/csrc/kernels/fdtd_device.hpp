@@ -38,6 +38,7 @@ struct alignas(16) FastClass {
     uint32_t flags;
     uint32_t pad0;
     T psiCoef[2];  // npsi * dbpsi
+    T epsInv;      // 1 / eps_inf of a D -> E cell without poles (kFcDtoE)
 };
 constexpr uint32_t kFcPsi0 = 1u;     // term J updates psi
 constexpr uint32_t kFcPsi1 = 2u;     // term K updates psi
@@ -49,6 +50,7 @@ constexpr uint32_t kFcSlab1 = 64u;   // term K needs the slab
 constexpr uint32_t kFcKp0 = 128u;    // term J adds its normal-slab profile kprof
 constexpr uint32_t kFcKp1 = 256u;    // term K adds its normal-slab profile kprof
 constexpr uint32_t kFcOrDip = 512u;  // oriented-dipole D -> E (E pass)
+constexpr uint32_t kFcDtoE = 1024u;  // D -> E of a cell whose object has no poles: E = D / eps_inf (E pass)
 
 template <typename T>
 struct Comp {
@@ -109,6 +111,7 @@ struct Pass {
     // 3-D interior form usable: every halo cell has code 0, term j of component c
     // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
     int interior3d;
+    int interior2d;         // the same conditions on a 2-D grid (lz == 1; the z terms absent)
     int index64;            // grid too large for 32-bit cell indices
     OrDipDev<T> od;         // oriented-dipole polarisations (E pass)
     // dispersive cells of the E pass, run by their own kernel in the interior form
@@ -217,6 +220,9 @@ void launch_increment(int* step, void* stream);
 // Blocks each job of a packed launch takes (the grid of its own launch).
 template <typename T>
 long long pass_blocks(const Pass<T>& p);  // generic form
+template <typename T>
+long long pass2d_blocks_per_comp(const Pass<T>& p);  // 2-D form, per component
+long long lorentz_blocks(long long n);
 long long ordip_blocks(long long n);
 int sources_blocks(int n);
 int record_blocks(int n);
@@ -225,6 +231,10 @@ long long dft_fold_blocks(long long npts, int nfreq);
 
 template <typename T>
 void launch_pass_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream);
+template <typename T>
+void launch_pass2d_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream);
+template <typename T>
+void launch_lorentz_packed(const Pass<T>* jobs, WorkMap m, void* stream);
 template <typename T>
 void launch_ordip_packed(const Pass<T>* jobs, WorkMap m, void* stream);
 template <typename T>

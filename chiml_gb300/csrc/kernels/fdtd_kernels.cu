@@ -191,19 +191,32 @@ __global__ void __launch_bounds__(256) k_pass_lorentz(const Pass<T> p) {
 // pass are left to k_pass_lorentz. Per cell the arithmetic is that of
 // cellGeneric.
 constexpr int kP3BZ = 8;
+#ifndef CHIML_MARCH_UNROLL
+#define CHIML_MARCH_UNROLL 1
+#endif
+constexpr int kMarchUnroll = CHIML_MARCH_UNROLL;  // planes of the march unrolled together
 
 __device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
 
-template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML>
+// D2: a 2-D grid (lz == 1), where the term along z is absent.
+template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false>
 __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1) {
     constexpr int A0 = (CI + 2) % 3;  // derivative axis of term J
     constexpr int A1 = (CI + 1) % 3;  // derivative axis of term K
+    constexpr bool P0 = !(D2 && A0 == 2);  // term J present
+    constexpr bool P1 = !(D2 && A1 == 2);  // term K present
     constexpr int TY = (A0 == 1) ? 0 : ((A1 == 1) ? 1 : -1);  // term along y, or none
     const Comp<T>& c = p.c[CI];
     const I plane = static_cast<I>(p.lx) * p.lz;
     I i = x + static_cast<I>(p.lx) * (z + static_cast<I>(p.lz) * y0);
     const T* __restrict__ G0 = c.G[0];
     const T* __restrict__ G1 = c.G[1];
+    // every array of the pass is its own allocation: no access aliases another
+    T* __restrict__ U = c.U;
+    T* __restrict__ Dd = c.D;
+    const uint8_t* __restrict__ code = c.code;
+    T* __restrict__ psi0 = c.psi[0];
+    T* __restrict__ psi1 = c.psi[1];
     const I off0 = static_cast<I>(c.off[0]);
     const I off1 = static_cast<I>(c.off[1]);
     // CPML profile of the terms along x or z at this thread's coordinate
@@ -213,7 +226,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
             const int ax = t == 0 ? A0 : A1;
-            if (ax == 1) continue;
+            if (ax == 1 || (D2 && ax == 2)) continue;
             const int a = ax == 0 ? x : z;
             inC[t] = a < c.slabLo[t] || a >= c.slabHi[t];
             if (inC[t]) {
@@ -229,17 +242,18 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
     T carry = T(0);
     if constexpr (TY >= 0) carry = EPASS ? c.G[TY][i - plane] : c.G[TY][i];
 
+#pragma unroll kMarchUnroll
     for (int y = y0; y < y1; ++y, i += plane) {
         if (PD > 0 && y + PD < y1) {
             const I ip = i + PD * plane;
-            prefetchL2(c.code + ip);
-            prefetchL2(c.U + ip);
-            prefetchL2(G0 + ip);
-            prefetchL2(G1 + ip);
+            prefetchL2(code + ip);
+            prefetchL2(U + ip);
+            if (P0) prefetchL2(G0 + ip);
+            if (P1) prefetchL2(G1 + ip);
         }
-        const uint8_t cd = c.code[i];
-        const T u = c.U[i];
-        T g[2], n[2];
+        const uint8_t cd = code[i];
+        const T u = U[i];
+        T g[2] = {T(0), T(0)}, n[2] = {T(0), T(0)};
         if (TY == 0) {
             if (EPASS) {
                 g[0] = G0[i];
@@ -250,7 +264,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
                 n[0] = G0[i + plane];
                 carry = n[0];
             }
-        } else {
+        } else if (P0) {
             g[0] = G0[i];
             n[0] = G0[i + off0];
         }
@@ -264,7 +278,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
                 n[1] = G1[i + plane];
                 carry = n[1];
             }
-        } else {
+        } else if (P1) {
             g[1] = G1[i];
             n[1] = G1[i + off1];
         }
@@ -285,7 +299,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
             }
 #pragma unroll
             for (int t = 0; t < 2; ++t)
-                if (c.hasPsi[t] && in[t]) ps[t] = c.psi[t][i];
+                if ((t == 0 ? P0 : P1) && c.hasPsi[t] && in[t]) ps[t] = (t == 0 ? psi0 : psi1)[i];
         }
         if (cd == 0) continue;
         if (cd >= c.ncls) {
@@ -305,22 +319,31 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
             const T coef[2] = {coef0, coef1};
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
+                if (!(t == 0 ? P0 : P1)) continue;
                 const T ct = (fl & (t == 0 ? kFcKp0 : kFcKp1)) ? coef[t] + kp[t] : coef[t];
                 const T diff = g[t] - n[t];
                 add += ct * diff;
                 if (fl & (t == 0 ? kFcPsi0 : kFcPsi1)) {
                     const T q = bq[t] * ps[t] + cq[t] * diff;
-                    c.psi[t][i] = q;
+                    (t == 0 ? psi0 : psi1)[i] = q;
                     add += kc->psiCoef[t] * q;
                 }
             }
         } else {
-            add += coef0 * (g[0] - n[0]);
-            add += coef1 * (g[1] - n[1]);
+            if (P0) add += coef0 * (g[0] - n[0]);
+            if (P1) add += coef1 * (g[1] - n[1]);
         }
-        if (fl & kFcWrite) {
-            if (fl & kFcToD) c.D[i] += add;
-            else c.U[i] = u + add;
+        if (EPASS && (fl & kFcDtoE)) {
+            // D -> E without poles: E = D / eps_inf (the P sum of cellGeneric adds zeros)
+            T d = Dd[i];
+            if (fl & kFcWrite) {
+                d += add;
+                Dd[i] = d;
+            }
+            U[i] = d * kc->epsInv;
+        } else if (fl & kFcWrite) {
+            if (fl & kFcToD) Dd[i] += add;
+            else U[i] = u + add;
         }
     }
 }
@@ -369,6 +392,45 @@ static void launch_pass3d(const Pass<T>& p, bool ePass, cudaStream_t s) {
     else k_pass3d<T, false, I, CY, PD><<<grid, block, 0, s>>>(p);
 }
 
+// 2-D form (lz == 1): a block of 32 x-columns by 8 warps; warp w of y-block by marches
+// CY rows along y from row 1 + (8 by + w) CY. The CPML decision is per warp.
+constexpr int kP2W = 8;
+#ifndef CHIML_P2CY
+#define CHIML_P2CY 16
+#endif
+
+template <typename T, bool EPASS, int CI, int CY, int PD>
+__device__ __forceinline__ void pass2d(const Pass<T>& p, int bx, int by) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int xa = 1 + bx * 32;
+    const int x = xa + lane;
+    const int y0 = 1 + (by * kP2W + w) * CY;
+    if (y0 > p.ly - 2) return;
+    const int y1 = min(y0 + CY, p.ly - 1);
+    const bool pml = blockTouchesSlab(p.c[CI], CI, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, 0, 0);
+    if (x > p.lx - 2) return;
+    if (pml) pass3dRun<T, EPASS, CI, int, CY, PD, true, true>(p, x, 0, y0, y1);
+    else pass3dRun<T, EPASS, CI, int, CY, PD, false, true>(p, x, 0, y0, y1);
+}
+
+template <typename T, bool EPASS, int CY>
+__device__ __forceinline__ void pass2dAny(const Pass<T>& p, int ci, int bx, int by) {
+    if (ci == 0) pass2d<T, EPASS, 0, CY, 2>(p, bx, by);
+    else if (ci == 1) pass2d<T, EPASS, 1, CY, 2>(p, bx, by);
+    else pass2d<T, EPASS, 2, CY, 2>(p, bx, by);
+}
+
+constexpr int kP2CY = CHIML_P2CY;
+
+template <typename T, bool EPASS>
+__global__ void __launch_bounds__(256) k_pass2d(const Pass<T> p) {
+    if (!p.c[blockIdx.z].present) return;
+    pass2dAny<T, EPASS, kP2CY>(p, blockIdx.z, blockIdx.x, blockIdx.y);
+}
+
+__host__ __device__ inline int pass2d_gx(int lx) { return (lx - 2 + 31) / 32; }
+__host__ __device__ inline int pass2d_gy(int ly) { return (ly - 2 + kP2W * kP2CY - 1) / (kP2W * kP2CY); }
+
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -380,6 +442,12 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
         } else {
             launch_pass3d<T, int, 16, 2>(p, ePass, s);
         }
+        if (ePass && p.nLor > 0)
+            k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
+    } else if (p.interior2d) {
+        dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
+        if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
+        else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
         if (ePass && p.nLor > 0)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else {
@@ -615,6 +683,11 @@ template <typename T>
 long long pass_blocks(const Pass<T>& p) {
     return static_cast<long long>((p.lx + 31) / 32) * p.lz * ((p.ly + kGenBY - 1) / kGenBY);
 }
+template <typename T>
+long long pass2d_blocks_per_comp(const Pass<T>& p) {
+    return static_cast<long long>(pass2d_gx(p.lx)) * pass2d_gy(p.ly);
+}
+long long lorentz_blocks(long long n) { return (n + 255) / 256; }
 long long ordip_blocks(long long n) { return (n + 255) / 256; }
 int sources_blocks(int n) { return (n + 127) / 128; }
 int record_blocks(int n) { return (n + 127) / 128; }
@@ -634,6 +707,30 @@ __global__ void __launch_bounds__(256) k_pass_packed(const Pass<T>* __restrict__
     const int bz = r % p.lz;
     const int by = r / p.lz;
     passCell<T, EPASS>(p, bx * 32 + (threadIdx.x & 31), by * kGenBY + (threadIdx.x >> 5), bz);
+}
+
+// 2-D form: the block index of a job encodes (component, y-block, x-block).
+template <typename T, bool EPASS>
+__global__ void __launch_bounds__(256) k_pass2d_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const Pass<T>& p = jobs[w.x];
+    const int gx = pass2d_gx(p.lx), gy = pass2d_gy(p.ly);
+    const int bx = w.y % gx;
+    const int r = w.y / gx;
+    pass2dAny<T, EPASS, kP2CY>(p, r / gy, bx, r % gy);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lorentz_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const Pass<T>& p = jobs[w.x];
+    const long long j = w.y * 256LL + threadIdx.x;
+    if (j >= p.nLor) return;
+    const long long i = p.lorCell[j];
+    const int x = static_cast<int>(i % p.lx);
+    const long long r = i / p.lx;
+    const int coord[3] = {x, static_cast<int>(r / p.lz), static_cast<int>(r % p.lz)};
+    cellGeneric<T, true>(p, p.lorComp[j], i, coord);
 }
 
 template <typename T>
@@ -683,6 +780,17 @@ void launch_pass_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream
     else k_pass_packed<T, false><<<m.blocks, 256, 0, s>>>(jobs, m.work);
 }
 template <typename T>
+void launch_pass2d_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream) {
+    if (m.blocks <= 0) return;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ePass) k_pass2d_packed<T, true><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+    else k_pass2d_packed<T, false><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+}
+template <typename T>
+void launch_lorentz_packed(const Pass<T>* jobs, WorkMap m, void* stream) {
+    if (m.blocks > 0) k_lorentz_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+}
+template <typename T>
 void launch_ordip_packed(const Pass<T>* jobs, WorkMap m, void* stream) {
     if (m.blocks > 0) k_ordip_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
 }
@@ -708,6 +816,9 @@ void launch_increment_packed(int* const* steps, int n, void* stream) {
 
 #define CHIML_PACKED(T)                                                                   \
     template long long pass_blocks<T>(const Pass<T>&);                                    \
+    template long long pass2d_blocks_per_comp<T>(const Pass<T>&);                         \
+    template void launch_pass2d_packed<T>(const Pass<T>*, WorkMap, bool, void*);          \
+    template void launch_lorentz_packed<T>(const Pass<T>*, WorkMap, void*);               \
     template void launch_pass_packed<T>(const Pass<T>*, WorkMap, bool, void*);            \
     template void launch_ordip_packed<T>(const Pass<T>*, WorkMap, void*);                 \
     template void launch_sources_packed<T>(const SrcJob<T>*, WorkMap, void*);             \

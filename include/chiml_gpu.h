@@ -104,10 +104,11 @@ void* chiml_stream(chiml_sim* sim);
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
-/* A batch of independent simulations stepped together (a parameter sweep): each
- * member keeps its own plan, device state, stream and CUDA graph; chiml_batch_run
- * queues the members' step graphs round-robin so that their kernels run
- * concurrently. The reference runs such sweeps as separate processes. */
+/* A batch of independent simulations stepped together (a parameter sweep), of
+ * uneven sizes: each member keeps its own plan and device state, and each kind of
+ * per-step work of all members runs as one packed launch, driven by a table that maps
+ * every block to a member and a block of that member's own launch. The reference runs
+ * such sweeps as separate processes. */
 typedef struct chiml_batch chiml_batch;
 
 /* Creates one member per input file, all with the same options, except that with
@@ -118,7 +119,12 @@ typedef struct chiml_batch chiml_batch;
  * chiml_last_error of the failing member (chiml_batch_member) holds the reason. */
 chiml_status chiml_batch_create(const char* const* json_paths, int n, const chiml_options* opt, chiml_batch** out);
 
-/* Advances every member to its last step (ceil(tLim/dt) each) and waits. */
+/* Advances every unfinished member by nsteps steps (each stops at its own last
+ * step, ceil(tLim/dt)) and waits: per step, one packed launch of each kind of work
+ * covers all members, the steps captured as CUDA graphs of opt->steps_per_graph steps. */
+chiml_status chiml_batch_step(chiml_batch* batch, int64_t nsteps);
+
+/* Advances every member to its last step and waits. */
 chiml_status chiml_batch_run(chiml_batch* batch);
 
 /* Writes every member's output files (as chiml_finalize). */

@@ -99,6 +99,10 @@ def test_batch_split_equals_members_run_alone(built_engine, tmp_path):
     members = _small_sweep(n=6, steps=200)
     paths = _write_members(tmp_path / "batch", members)
     with Batch(paths, precision="split", steps_per_graph=16) as b:
+        # partial advances reuse the packed launches; the rest runs as eager steps and graphs
+        b.step(37)
+        b.step(100)
+        assert all(b.member_stats(i).steps_done == 137 for i in range(len(paths)))
         b.run()
         b.finalize()
     for name, cfg in members:
