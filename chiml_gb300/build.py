@@ -18,7 +18,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HOST_SRCS = ["json.cpp", "inputs.cpp", "setup.cpp", "outputs.cpp", "emitters.cpp"]
+HOST_SRCS = ["json.cpp", "inputs.cpp", "setup.cpp", "outputs.cpp", "emitters.cpp", "tfsf.cpp"]
 
 LIB_ENGINE = os.path.join(BUILD, "libchiml_gb300.so")
 LIB_ORACLE = os.path.join(ORACLE, "_build", "libchiml_oracle.so")

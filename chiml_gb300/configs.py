@@ -118,9 +118,27 @@ def config1(n=400, pml=20, steps=4000, radius_cells=50, src_gap_cells=60, ndtc=8
     }
 
 
-def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal_radius_cells=30, aniso=True):
-    """3-D dispersive scene: seeded ellipsoids, a Drude + 2 Lorentz metal sphere, a plane Ex
-    source sheet and a DFT flux box.
+def tfsf_surface(box, fcen_a, width, psi_deg=0.0, theta_deg=0.0, phi_deg=90.0, m=None, circ=None, pml_thick=12,
+                 loc=(0.0, 0.0, 0.0)):
+    """One TFSF entry (parallelInputs.cpp:219-408): box size (a units), a Gaussian pulse at
+    fcen_a (1/a units) of 1/e time width ``width``, direction from theta/phi or an integer
+    vector m, polarisation angle psi (0 = along x for propagation along z), optional
+    circular polarisation ("L" / "R") and the thickness of its 1-D CPML."""
+    t = {"loc": list(loc), "size": list(box), "theta": theta_deg, "phi": phi_deg, "psi": psi_deg,
+         "PulseList": [_gauss(fcen_a, 1.0 / width, 4.0, 3 * width)], "pmlThick": pml_thick}
+    if m is not None:
+        t["m"] = list(m)
+    if circ:
+        t["circPol"] = circ
+    return t
+
+
+def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal_radius_cells=30, aniso=True,
+            tfsf=True):
+    """3-D dispersive scene: seeded ellipsoids, a Drude + 2 Lorentz metal sphere, an
+    x-polarised plane wave along +z and a DFT flux box. With ``tfsf`` the wave enters
+    through a TFSF box (4 cells inside the CPML) that holds every object and the flux box;
+    without it, through a soft Ex source sheet.
 
     With ``aniso`` each ellipsoid is uniaxial: eps_inf = eps_o plus one oriented-dipole
     Lorentz pole along the random optic axis whose static strength is eps_e - eps_o, centred
@@ -163,13 +181,16 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
     sheet = size - 2 * (pml + 1) * dx
     fb = 2 * (half - (pml + 5) * dx)
     width = 5e-15 / T_UNIT
+    tbox = 2 * (half - (pml + 4) * dx)
+    tf = [tfsf_surface([tbox] * 3, A / 550e-9, width, psi_deg=0.0, theta_deg=0.0)] if tfsf else []
+    srcs = [] if tfsf else [{"pol": "Ex", "loc": [0.0, 0.0, round(src_z / dx) * dx], "size": [sheet, sheet, 0.0],
+                             "PulseList": [_gauss(A / 550e-9, 1.0 / width, 4.0, 3 * width)]}]
     return {
         "CompCell": {"size": [size, size, size], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
                      "a": A, "pol": "Ex", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
         "PML": {"thickness": [pml * dx] * 3, "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
-        "SourceList": [{"pol": "Ex", "loc": [0.0, 0.0, round(src_z / dx) * dx], "size": [sheet, sheet, 0.0],
-                        "PulseList": [_gauss(A / 550e-9, 1.0 / width, 4.0, 3 * width)]}],
-        "TFSF": [],
+        "SourceList": srcs,
+        "TFSF": tf,
         "ObjectList": objs,
         "DetectorList": [{"loc": [0.0, 0.0, round((half - (pml + 8) * dx) / dx) * dx], "size": [0.0, 0.0, 0.0],
                           "type": "Ex", "fname": "out/c2_pt", "dtc_class": "txt", "SI": False, "Time_Interval": dt}],

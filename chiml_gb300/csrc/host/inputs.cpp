@@ -404,6 +404,71 @@ std::vector<double> read_freq_list(const JNode& n, const char* what) {
     return fl;
 }
 
+// One TFSF surface (parallelInputs.cpp:219-408): the box in grid points (odd sizes
+// unless the box is a plane), the propagation vector m from the angles or the angles
+// from m, the pulses with the amplitude appended as (0, Emax)
+// (parallelFDTDField.cpp:648), the polarisation and the 1-D CPML parameters.
+void read_tfsf(const JNode& tn, Inputs& ip) {
+    TfsfSpec t;
+    const std::array<double, 3> tempSz = as_arr3(tn, "size");
+    for (int i = 0; i < 3; ++i) t.sz[i] = find_pt(tempSz[i], ip.d[i]) + 1;
+    const bool anyOne = t.sz[0] == 1 || t.sz[1] == 1 || t.sz[2] == 1;
+    if ((ip.size[2] == 0 && t.sz[0] != 1 && t.sz[1] != 1) || (ip.size[2] != 0.0 && !anyOne))
+        for (int& v : t.sz) v -= (v - 1) % 2;
+    const std::array<double, 3> loc = as_arr3(tn, "loc");
+    for (int i = 0; i < 3; ++i)
+        t.loc[i] = (ip.size[i] != 0.0) ? find_pt(loc[i] + ip.size[i] / 2.0, ip.d[i]) - (t.sz[i] - (t.sz[i] % 2)) / 2 : 0;
+    for (int i = 0; i < 3; ++i)
+        if (ip.size[i] > 0.0 && (t.loc[i] + t.sz[i] / 2 > find_pt(ip.size[i], ip.d[i]) || t.loc[i] < 0))
+            if (t.loc[i] + t.sz[i] / 2.0 != 1) throw InputError("A TFSF surface is outside the FDTD cell.");
+    if (tn.has("m") && tn.child("m").size() > 0) {
+        int i = 0;
+        for (auto& mk : tn.child("m").kids) {
+            if (i < 3) t.m[i] = mk.second.value<int>();
+            ++i;
+        }
+        const int nz = (t.m[0] != 0) + (t.m[1] != 0) + (t.m[2] != 0);
+        if (nz == 1)
+            for (int& v : t.m)
+                if (v != 0) v /= std::abs(v);
+        t.phi = (t.m[0] == 0) ? ((t.m[1] > 0) ? M_PI / 2.0 : -1.0 * M_PI / 2.0)
+                              : std::atan(t.m[1] * ip.d[0] / (t.m[0] * ip.d[1]));
+        if (t.m[0] < 0) t.phi += M_PI;
+        else if (t.m[1] < 0) t.phi += 2.0 * M_PI;
+        t.theta = (t.m[2] == 0) ? M_PI / 2.0
+                                : std::atan(std::sqrt(std::pow(t.m[1] / ip.d[1], 2.0) + std::pow(t.m[0] / ip.d[0], 2.0)) /
+                                            (t.m[2] / ip.d[2]));
+        if (t.m[2] < 0) t.theta += M_PI;
+        t.psi = M_PI * tn.get<double>("psi", 90.0) / 180.0;
+    } else {
+        t.m = {0, 0, 0};
+        t.theta = M_PI * tn.get<double>("theta", 90.0) / 180.0;
+        if (t.theta < 0 || t.theta > M_PI) throw InputError("The theta value for the TFSF surfaces must be between 0 and 180 degrees.");
+        t.phi = M_PI * tn.get<double>("phi", 90.0) / 180.0;
+        t.psi = M_PI * tn.get<double>("psi", 90.0) / 180.0;
+        if (ip.size[2] == 0.0) {
+            t.theta = M_PI / 2.0;
+            t.psi = (ip.pol == Pol::EZ || ip.pol == Pol::HX || ip.pol == Pol::HY) ? M_PI / 2.0 : 0.0;
+        }
+        if (std::fmod(t.theta, M_PI) == 0.0) t.m[2] = t.theta == 0 ? 1 : -1;
+        else if (std::fmod(t.phi, M_PI) == 0.0) t.m[0] = (std::fmod(t.phi, 2 * M_PI) == 0.0) ? 1 : -1;
+        else if (std::fmod(t.phi, M_PI / 2.0) == 0.0) t.m[1] = (std::fmod(t.phi, 2 * M_PI) == M_PI / 2.0) ? 1 : -1;
+    }
+    if (t.m[0] == 0 && t.m[1] == 0 && t.m[2] == 0) throw InputError("TFSF surface must have a direction of propgation.");
+    for (auto& pk : tn.child("PulseList").kids) {
+        PulseSpec p = read_pulse(pk.second, ip.a, ip.I0);
+        p.param.back() = cplx(0.0, std::real(p.param.back()));
+        t.pulses.push_back(p);
+    }
+    t.circPol = string2pol(tn.get<std::string>("circPol", "Ex"));
+    t.kRatio = tn.get<double>("ellpiticalKRat", 1.0);
+    t.pmlThick = tn.get<int>("pmlThick", 20);
+    t.pmlAMax = tn.get<double>("pmlAMax", 0.0);
+    t.pmlM = tn.get<double>("pmlM", ip.pmlM);
+    t.pmlMa = tn.get<double>("pmlMa", ip.pmlMa);
+    ip.tfsf.push_back(t);
+}
+
 }  // namespace
 
 cplx PulseSpec::value(double tt) const {
@@ -458,7 +523,6 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
     ip.pmlAMax = IP.get<double>("PML.aMax", 0.00);
     ip.pmlMa = IP.get<double>("PML.ma", 1.0);
     ip.pmlM = IP.get<double>("PML.m", 3.0);
-    if (IP.child("TFSF").size() > 0) throw UnsupportedError("TFSF surfaces are not supported by this build");
     // parallelInputs.cpp:96-107
     if (ip.d[0] < 0 || ip.d[1] < 0 || ip.d[2] < 0) throw InputError("Please define a positive step size.");
     double stab = 0.0;
@@ -492,6 +556,8 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
         }
         ip.sources.push_back(s);
     }
+    // TFSF surfaces, parallelInputs.cpp:219-408
+    for (auto& kv : IP.child("TFSF").kids) read_tfsf(kv.second, ip);
     // Objects, parallelInputs.cpp:410-666; objArr_[0] is the vacuum block of the whole cell
     ip.objects.push_back(make_vacuum_block(ip.size));
     for (auto& kv : IP.child("ObjectList").kids) {

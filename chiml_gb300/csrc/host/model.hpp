@@ -8,6 +8,7 @@
 #pragma once
 
 #include <array>
+#include <cmath>
 #include <complex>
 #include <memory>
 #include <stdexcept>
@@ -80,6 +81,19 @@ struct SourceSpec {
     double phi = 90.0;
 };
 
+// A TFSF plane-wave surface (parallelInputs.cpp:219-408): box in grid points (lower
+// corner, 0-based physical coordinates, and size), integer propagation vector m, angles
+// in radians, pulses (amplitude appended as (0, Emax)), polarisation and the 1-D CPML.
+struct TfsfSpec {
+    std::array<int, 3> loc = {0, 0, 0}, sz = {1, 1, 1}, m = {0, 0, 0};
+    double theta = M_PI / 2.0, phi = 0.0, psi = 0.0;
+    std::vector<PulseSpec> pulses;
+    Pol circPol = Pol::EX;
+    double kRatio = 1.0;
+    int pmlThick = 20;
+    double pmlAMax = 0.0, pmlM = 3.0, pmlMa = 1.0;
+};
+
 struct DetectorSpec {
     DtcClass cls = DtcClass::TXT;
     DtcType type = DtcType::EZ;
@@ -144,6 +158,7 @@ struct Inputs {
     std::array<int, 3> pmlThickness = {0, 0, 0};
     double pmlSigOptRat = 1.0, pmlKappaMax = 1.0, pmlAMax = 0.0, pmlMa = 1.0, pmlM = 3.0;
     std::vector<SourceSpec> sources;
+    std::vector<TfsfSpec> tfsf;
     std::vector<Object> objects;  // objects[0] is the vacuum cell block
     std::vector<DetectorSpec> detectors;
     std::vector<FluxSpec> fluxes;

@@ -255,12 +255,18 @@ void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) 
         }
         f << std::setw(16) << "freq\tabs(total)\treal(total)\timag(total)\n";
         const double tInt = static_cast<double>(fp.spec.timeInt);
-        const std::size_t nIncd = 2 * (static_cast<std::size_t>(P.nSteps) + 1) + 2;
         for (int ff = 0; ff < nfreq; ++ff) {
             cx flux = 0.0;
-            // incident fields are zero without a TFSF surface; the transform is kept for its form
+            // transform of the recorded incident fields (zero without a TFSF surface): the even
+            // samples, then the odd ones, real parts only (parallelFlux.hpp:457-479)
             cx inc[6] = {0, 0, 0, 0, 0, 0};
-            (void)nIncd;
+            const std::vector<cplx>* incSer[6] = {&R.incE[0], &R.incE[1], &R.incE[2], &R.incH[0], &R.incH[1], &R.incH[2]};
+            const std::size_t nInc = incSer[0]->size();
+            for (int start = 0; start < 2; ++start)
+                for (std::size_t tt = start; tt < nInc; tt += 2) {
+                    const cx ph = std::exp(cx(0.0, fp.spec.freqList.at(ff) * static_cast<double>(tt / 2) * (P.dt / tInt)));
+                    for (int q = 0; q < 6; ++q) inc[q] += cx(std::real(0.5 * (*incSer[q])[tt]), 0.0) * ph;
+                }
             cx flux_incd = std::pow(fp.incdConv[0] * (inc[1] * std::conj(inc[5]) - inc[2] * std::conj(inc[4])) /
                                         (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
             flux_incd += std::pow(fp.incdConv[1] * (inc[2] * std::conj(inc[3]) - inc[0] * std::conj(inc[5])) /
@@ -268,7 +274,6 @@ void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) 
             flux_incd += std::pow(fp.incdConv[2] * (inc[0] * std::conj(inc[4]) - inc[1] * std::conj(inc[3])) /
                                       (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
             flux_incd = std::sqrt(flux_incd);
-            (void)tInt;
             f << std::setw(18) << std::setprecision(15) << fp.freqConv * fp.spec.freqList[ff] << "\t" << std::setw(16)
               << std::setprecision(15) << std::abs(flux_incd) << "\t" << std::setw(16) << std::setprecision(15)
               << std::abs(std::real(flux_incd)) << "\t" << std::setw(16) << std::setprecision(15) << std::imag(flux_incd)

@@ -21,6 +21,9 @@ struct RunRecord {
     // (parallelQE.cpp:41-44 accumP_), and per population detector its events
     std::vector<std::array<std::vector<double>, 3>> emitterP;
     std::vector<std::vector<std::vector<cplx>>> emitterPop;
+    // incident fields of the TFSF surface (E_incd_ / H_incd_, parallelFDTDField.hpp:1238-1255):
+    // per component two samples per step, 2 * (nSteps + 1) values; empty without a surface
+    std::array<std::vector<cplx>, 3> incE, incH;
 };
 
 // Number of values one output event of detector k stores.

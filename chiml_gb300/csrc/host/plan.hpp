@@ -174,6 +174,61 @@ struct EmitterPlan {
     int dtcTimeInt = 1;
 };
 
+// ---- TFSF plane-wave surfaces (SOURCE/parallelTFSF.*, PML/PML.*) ----
+// Incident fields live on 1-D complex grids ("lines"), one per field component the
+// main grid has; line c = 0..2 Ex..Ez, 3..5 Hx..Hy. Each line has the incident grid
+// (updated as D / B, then divided by eps / mu), its own CPML, and a short "pulse" grid
+// in the uniform surface material whose values are recorded for flux normalisation.
+
+// A run of equal material along a line (paramUpIncdField, parallelTFSF.hpp:17-38):
+// U[indI + r] += pj (J[posK + r] - J[negK + r]) + pk (K[posJ + r] - K[negJ + r]).
+struct TfsfRun {
+    int indI = 0, posJ = 0, negJ = 0, posK = 0, negK = 0, n = 0;
+    double pj = 0.0, pk = 0.0;
+};
+
+// One psi list of a line's CPML (IncdCPML::getUpList, PML/PML.hpp:222-271; addPsi and
+// updatePsiField, PML/PML.cpp:12-31): psi = b psi + c G[loc + d] + cOff G[locOff + d],
+// then U[gridLoc + d] += Db psi, for d < n. G is the neighbour line nbr.
+struct TfsfPsi {
+    int nbr = -1;
+    int loc = 0, locOff = 0, gridLoc = 0, n = 0;
+    double Db = 0.0;
+    std::vector<double> b, c, cOff;
+};
+
+struct TfsfLine {
+    bool present = false;
+    bool useJ = false, useK = false;  // the j / k neighbour lines take part in the curl
+    int nbrJ = -1, nbrK = -1;          // neighbour line ids (component (c+1)%3, (c+2)%3 of the other kind)
+    double epMu = 1.0;                 // uniform eps (E) or mu (H) of the line
+    std::vector<TfsfRun> runs;         // incident grid, length gridLen
+    std::vector<TfsfRun> pulseRuns;    // pulse grid, length pulseLen
+    std::vector<TfsfPsi> pml, pmlPulse;
+    std::vector<double> dist;          // per pulse point: distance from the source (distVecE/H)
+    cplx prefact = 0.0;                // pulse prefactor (prefactE_/prefactH_)
+    int recIdx = 0, recOffIdx = 0;     // pulse-grid points recorded each step
+};
+
+// Surface corrections of one main-grid cell, in the reference's order: each term adds
+// pref * Re(line[incd]) to the cell's field (toD: to its D field).
+struct TfsfCellAdds {
+    long long cell = 0;
+    int comp = 0;                      // main field component 0..5
+    std::vector<int> line, incd;
+    std::vector<double> pref;
+    std::vector<uint8_t> toD;
+};
+
+struct TfsfPlan {
+    int gridLen = 0, pulseLen = 0, mTot = 0, mMax = 0, pmlThick = 0, pulAddStart = 0;
+    std::array<int, 3> m = {0, 0, 0};
+    double dt = 0.0;
+    TfsfLine line[6];
+    std::vector<PulseSpec> pulses;
+    std::vector<TfsfCellAdds> addH, addE;  // applied before and after the 1-D step
+};
+
 struct Plan {
     Inputs in;
     Dims dims;
@@ -187,6 +242,7 @@ struct Plan {
     std::vector<DetectorPlan> detectors;
     std::vector<FluxPlan> fluxes;
     std::vector<EmitterPlan> emitters;
+    std::vector<TfsfPlan> tfsf;
     // relative permittivity on the cell-centred grid (epsRelOrDip_), where the emitter
     // polarisation is divided into E; filled only when there are emitters
     std::vector<double> epsP;
@@ -201,6 +257,11 @@ Plan build_plan(const Inputs& in);
 // epsOrDip: the relative permittivity on the cell-centred grid.
 void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3],
                     const std::vector<double>& epsOrDip, Plan& P);
+
+// TFSF plans of the input (tfsf.cpp); phys[c]: object id per cell of main component c
+// (0..5; null when absent), -1 on the halo.
+void build_tfsf(const Inputs& in, const Dims& D, double dt, const std::vector<int>* const phys[6],
+                const std::vector<Object>& objs, Plan& P);
 
 // Wigner 3j symbol for integer arguments (emitters.cpp).
 double wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);

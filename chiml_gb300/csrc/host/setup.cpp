@@ -1277,6 +1277,11 @@ Plan build_plan(const Inputs& in) {
         const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
         build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v, P);
     }
+    if (!in.tfsf.empty()) {
+        const std::vector<int>* ph[6];
+        for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? &b.phys[c].v : nullptr;
+        build_tfsf(in, P.dims, P.dt, ph, in.objects, P);
+    }
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)
     for (auto& fp : P.fluxes) {
         if (!fp.spec.crossSec) {

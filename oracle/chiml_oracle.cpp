@@ -10,6 +10,7 @@
 //   soft sources         SOURCE/parallelSourceNormal.cpp:15-37
 //   DFT accumulation     DTC/parallelStorageFreqDTC.cpp:21-30, DTC/parallelFlux.hpp:296-314
 //   detector sampling    DTC/parallelStorageDTC.cpp:17-48
+//   TFSF surfaces        SOURCE/parallelTFSF.hpp:1058-1186, SOURCE/parallelTFSF.cpp:11-94, PML/PML.cpp:12-31
 //   emitters             ML/parallelQE.hpp:614-770 (addQE, updateDensity, denDeriv, PCABAM4),
 //                        UTIL/FDTD_up_eq.cpp:1367-1420 (addP, getE_TE/TM), ML/Hamiltonian.cpp:59-69
 // Its outputs are pinned by the golden files of the reference's own CPU build
@@ -186,6 +187,96 @@ struct EmitterSim {
     }
 };
 
+// TFSF surface: the 1-D incident lines stepped with complex arithmetic, and the surface
+// corrections (parallelTFSFBase::updateFields / step, SOURCE/parallelTFSF.hpp:1058-1186;
+// updateIncdFieldJ/K/JK, incdD2U, fillPulseVec, addIncdFields, SOURCE/parallelTFSF.cpp:11-94;
+// IncdCPML addPsi / updatePsiField, PML/PML.cpp:12-31).
+struct TfsfSim {
+    const TfsfPlan& T;
+    std::vector<cplx> U[6], Dl[6], pul[6];  // incident field, its D / B, pulse grid
+    std::vector<std::vector<cplx>> psi[6], psiPul[6];
+    std::vector<cplx> pulseVec;
+    double tStep = 0.0;
+
+    explicit TfsfSim(const TfsfPlan& t) : T(t) {
+        for (int c = 0; c < 6; ++c) {
+            const TfsfLine& L = T.line[c];
+            if (!L.present) continue;
+            U[c].assign(T.gridLen, 0.0);
+            Dl[c].assign(T.gridLen, 0.0);
+            pul[c].assign(T.pulseLen, 0.0);
+            for (auto& p : L.pml) psi[c].emplace_back(p.n, 0.0);
+            for (auto& p : L.pmlPulse) psiPul[c].emplace_back(p.n, 0.0);
+        }
+        pulseVec.assign(T.mTot, 0.0);
+    }
+
+    cplx rec(int c, bool off) const { return T.line[c].present ? pul[c][off ? T.line[c].recOffIdx : T.line[c].recIdx] : cplx(0.0); }
+
+    static void addSurface(const std::vector<TfsfCellAdds>& adds, const std::vector<cplx>* lines, std::vector<double>* F,
+                           std::vector<double>* Dd) {
+        for (const TfsfCellAdds& a : adds)
+            for (std::size_t q = 0; q < a.line.size(); ++q) {
+                const double v = a.pref[q] * std::real(lines[a.line[q]][a.incd[q]]);
+                if (a.toD[q]) Dd[a.comp][a.cell] += v;
+                else F[a.comp][a.cell] += v;
+            }
+    }
+
+    // updateIncdField*: pulse, curl runs, then the line's CPML
+    void updateLine(int c, std::vector<cplx>& G, const std::vector<TfsfRun>& runs, const std::vector<TfsfPsi>& pml,
+                    std::vector<std::vector<cplx>>& ps, const std::vector<cplx>* nbr) {
+        const TfsfLine& L = T.line[c];
+        for (int r = 0; r < T.mTot; ++r) G[T.pulAddStart + r] = G[T.pulAddStart + r] + L.prefact * pulseVec[r];
+        for (const TfsfRun& run : runs) {
+            if (L.useJ) {
+                const std::vector<cplx>& J = nbr[L.nbrJ];
+                for (int r = 0; r < run.n; ++r) G[run.indI + r] += cplx(run.pj, 0.0) * J[run.posK + r];
+                for (int r = 0; r < run.n; ++r) G[run.indI + r] += cplx(-1.0 * run.pj, 0.0) * J[run.negK + r];
+            }
+            if (L.useK) {
+                const std::vector<cplx>& K = nbr[L.nbrK];
+                for (int r = 0; r < run.n; ++r) G[run.indI + r] += cplx(run.pk, 0.0) * K[run.posJ + r];
+                for (int r = 0; r < run.n; ++r) G[run.indI + r] += cplx(-1.0 * run.pk, 0.0) * K[run.negJ + r];
+            }
+        }
+        for (std::size_t q = 0; q < pml.size(); ++q) {
+            const TfsfPsi& p = pml[q];
+            std::vector<cplx>& s = ps[q];
+            const std::vector<cplx>& N = nbr[p.nbr];
+            for (int dd = 0; dd < p.n; ++dd) s[dd] = cplx(p.b[dd]) * s[dd];
+            for (int dd = 0; dd < p.n; ++dd) s[dd] = s[dd] + cplx(p.c[dd]) * N[p.loc + dd];
+            for (int dd = 0; dd < p.n; ++dd) s[dd] = s[dd] + cplx(p.cOff[dd]) * N[p.locOff + dd];
+            for (int dd = 0; dd < p.n; ++dd) G[p.gridLoc + dd] += cplx(p.Db, 0.0) * s[dd];
+        }
+    }
+
+    void fillPulse(int c) {
+        const TfsfLine& L = T.line[c];
+        for (int r = 0; r < T.mTot; ++r) pulseVec[r] = 0.0;
+        for (const PulseSpec& p : T.pulses)
+            for (int r = 0; r < T.mTot; ++r) pulseVec[r] = pulseVec[r] + p.value(tStep * T.dt - L.dist[r]);
+    }
+
+    void stepLines() {
+        for (int h = 3; h < 6; ++h) {
+            if (!T.line[h].present) continue;
+            fillPulse(h);
+            updateLine(h, Dl[h], T.line[h].runs, T.line[h].pml, psi[h], U);
+            updateLine(h, pul[h], T.line[h].pulseRuns, T.line[h].pmlPulse, psiPul[h], pul);
+            for (int x = 0; x < T.gridLen; ++x) U[h][x] = Dl[h][x] / T.line[h].epMu;
+        }
+        for (int e = 0; e < 3; ++e) {
+            if (!T.line[e].present) continue;
+            fillPulse(e);
+            updateLine(e, Dl[e], T.line[e].runs, T.line[e].pml, psi[e], U);
+            updateLine(e, pul[e], T.line[e].pulseRuns, T.line[e].pmlPulse, psiPul[e], pul);
+            for (int x = 0; x < T.gridLen; ++x) U[e][x] = Dl[e][x] / T.line[e].epMu;
+        }
+        tStep += 1.0;
+    }
+};
+
 struct OracleSim {
     Plan P;
     std::vector<double> F[6];
@@ -195,10 +286,17 @@ struct OracleSim {
     std::vector<std::vector<double>> odP[3], odPrev[3];  // oriented-dipole polarisations (cell-centred grid)
     RunRecord rec;
     std::vector<std::unique_ptr<EmitterSim>> qe;
+    std::vector<std::unique_ptr<TfsfSim>> tfsf;
     int step = 0;
 
     explicit OracleSim(const Plan& plan) : P(plan) {
         for (auto& ep : P.emitters) qe.emplace_back(new EmitterSim(ep, P.dims));
+        for (auto& tp : P.tfsf) tfsf.emplace_back(new TfsfSim(tp));
+        if (!P.tfsf.empty())
+            for (int c = 0; c < 3; ++c) {
+                rec.incE[c].assign(2 * (static_cast<std::size_t>(P.nSteps) + 1), 0.0);
+                rec.incH[c].assign(2 * (static_cast<std::size_t>(P.nSteps) + 1), 0.0);
+            }
         const std::size_t N = static_cast<std::size_t>(P.dims.cells());
         for (int c = 0; c < 6; ++c) {
             if (!P.comp[c].present) continue;
@@ -422,6 +520,21 @@ struct OracleSim {
         // H half step (updateH + H CPML)
         for (int c = 3; c < 6; ++c)
             if (P.comp[c].present) curl(c);
+        // TFSF after the H update: record H incident, H corrections, 1-D step, E corrections,
+        // record E incident (parallelFDTDField.hpp:1237-1255)
+        for (auto& t : tfsf) {
+            for (int c = 0; c < 3; ++c) {
+                rec.incH[c][2 * step + 0] = t->rec(3 + c, false);
+                rec.incH[c][2 * step + 1] = t->rec(3 + c, true);
+            }
+            TfsfSim::addSurface(t->T.addH, t->U, F, Dd);
+            t->stepLines();
+            TfsfSim::addSurface(t->T.addE, t->U, F, Dd);
+            for (int c = 0; c < 3; ++c) {
+                rec.incE[c][2 * step + 0] = t->rec(c, false);
+                rec.incE[c][2 * step + 1] = t->rec(c, true);
+            }
+        }
         // soft sources at t_n (after H, before E)
         for (auto& s : P.sources) {
             double v = s.value[static_cast<std::size_t>(step)];

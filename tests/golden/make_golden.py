@@ -83,7 +83,7 @@ def _qe_3d():
     """3-D ladder of three levels (z dipoles) with Gaussian-broadened upper levels (nine ensemble
     members), Ez plane source, population detectors and the polarisation output."""
     n, dx = 26, 0.05
-    cfg = configs.config2(n=n, pml=5, steps=90, nell=0, nfreq=4, metal_radius_cells=0)
+    cfg = configs.config2(n=n, pml=5, steps=90, nell=0, nfreq=4, metal_radius_cells=0, tfsf=False)
     cfg["ObjectList"] = []
     lv = [configs.emitter_level(0.0), configs.emitter_level(2.0, "Gaussian", 3, 0.02),
           configs.emitter_level(4.2, "Gaussian", 3, 0.02)]
@@ -100,21 +100,60 @@ def _qe_3d():
 def _c2_aniso():
     """3-D with five uniaxial ellipsoids (oriented-dipole poles) and the metal sphere; a short
     pulse so that the field reaches the objects within the run."""
-    cfg = configs.config2(n=36, pml=6, steps=160, nell=5, nfreq=6, metal_radius_cells=18)
+    cfg = configs.config2(n=36, pml=6, steps=160, nell=5, nfreq=6, metal_radius_cells=18, tfsf=False)
     width = 0.3e-15 / configs.T_UNIT
     cfg["SourceList"][0]["PulseList"] = [configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)]
     return cfg
 
 
+def _tfsf_disp():
+    """3-D TFSF plane wave along +z, x-polarised, onto three uniaxial ellipsoids and the
+    Drude-Lorentz sphere inside the total-field box; a short pulse that crosses the box."""
+    cfg = configs.config2(n=40, pml=6, steps=240, nell=2, nfreq=6, metal_radius_cells=36, tfsf=True)
+    width = 0.2e-15 / configs.T_UNIT
+    cfg["TFSF"][0]["PulseList"] = [configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)]
+    cfg["TFSF"][0]["pmlThick"] = 8
+    return cfg
+
+
+def _tfsf_oblique():
+    """3-D oblique TFSF (m = (1, 2, 1)), left circular polarisation, onto a dispersive sphere."""
+    cfg = configs.config2(n=32, pml=6, steps=160, nell=0, nfreq=5, metal_radius_cells=40, tfsf=True)
+    dx = 0.05
+    box = 2 * ((32 - 1) * dx / 2 - 10 * dx)
+    width = 0.2e-15 / configs.T_UNIT
+    cfg["TFSF"] = [configs.tfsf_surface([box] * 3, configs.A / 550e-9, width, psi_deg=20.0, m=(1, 2, 1), circ="L",
+                                        pml_thick=6)]
+    return cfg
+
+
+def _tfsf_2d_te():
+    """2-D TE (Ex, Ey, Hz) TFSF along m = (1, 1, 0) onto the dielectric disk, flux line inside."""
+    cfg = configs.config1(n=60, pml=8, steps=240, radius_cells=6, src_gap_cells=6, ndtc=2, nfreq=5)
+    cfg["CompCell"]["pol"] = "Hz"
+    cfg["SourceList"] = []
+    for d in cfg["DetectorList"]:
+        d["type"] = "Ey"
+    dx = 0.05
+    box = 2 * ((60 - 1) * dx / 2 - 12 * dx)
+    width = 0.3e-15 / configs.T_UNIT
+    cfg["TFSF"] = [configs.tfsf_surface([box, box, 0.0], configs.A / 550e-9, width, m=(1, 1, 0), pml_thick=10)]
+    return cfg
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
-    "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False),
+    "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
+                                          tfsf=False),
     "c2_aniso": _c2_aniso,
     "te_dispersive": _te_dispersive,
     "tm_lorentz": _tm_lorentz,
     "qe_tm": _qe_tm,
     "qe_te": _qe_te,
     "qe_3d": _qe_3d,
+    "tfsf_disp": _tfsf_disp,
+    "tfsf_oblique": _tfsf_oblique,
+    "tfsf_2d_te": _tfsf_2d_te,
 }
 
 
