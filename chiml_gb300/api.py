@@ -58,6 +58,7 @@ class Stats(ctypes.Structure):
         ("d2h_bytes", ctypes.c_double),
         ("n_flux_regions", ctypes.c_int32),
         ("n_emitters", ctypes.c_int32),
+        ("n_tfsf", ctypes.c_int32),
     ]
 
 
@@ -201,7 +202,8 @@ class Simulation:
         ns = ctypes.c_int()
         self._check(self._lib.chiml_profile_steps(self._h, int(n), ms, 64, ctypes.byref(ns)))
         names = ["h_pass", "sources", "e_pass", "step_counter", "records"]
-        ndft = self.stats().n_flux_regions
+        st = self.stats()
+        ndft, nem = st.n_flux_regions, st.n_emitters
         out = {}
         for k in range(ns.value):
             if k < len(names):
@@ -209,8 +211,10 @@ class Simulation:
             elif k < len(names) + 2 * ndft:
                 q, r = divmod(k - len(names), 2)
                 out["dft%d_%s" % (q, "sample" if r == 0 else "fold")] = ms[k]
-            else:
+            elif k < len(names) + 2 * ndft + nem:
                 out["emitter%d" % (k - len(names) - 2 * ndft)] = ms[k]
+            else:
+                out["tfsf%d" % (k - len(names) - 2 * ndft - nem)] = ms[k]
         return out
 
     @property

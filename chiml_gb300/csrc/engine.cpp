@@ -20,6 +20,7 @@
 #include "kernels/box_noalloc.hpp"
 #include "kernels/emitter_device.hpp"
 #include "kernels/fdtd_device.hpp"
+#include "kernels/tfsf_device.hpp"
 
 using namespace chiml;
 
@@ -191,6 +192,18 @@ public:
             }
             R.emitterPop.push_back(pops);
         }
+        if (!tfsf_.empty()) {
+            // incident values of the last surface (each surface overwrites them, parallelFDTDField.hpp:1238-1255)
+            const std::size_t n = 2 * (static_cast<std::size_t>(P.nSteps) + 1);
+            std::vector<double2> all(6 * n);
+            ck(cudaMemcpy(all.data(), tfsf_.back().rec, all.size() * sizeof(double2), cudaMemcpyDeviceToHost), "D2H incident");
+            d2h_ += static_cast<double>(all.size() * sizeof(double2));
+            for (int c = 0; c < 6; ++c) {
+                std::vector<cplx>& dst = c < 3 ? R.incE[c] : R.incH[c - 3];
+                dst.resize(n);
+                for (std::size_t k = 0; k < n; ++k) dst[k] = cplx(all[c * n + k].x, all[c * n + k].y);
+            }
+        }
         write_detectors(P, R, outDir_, stepsDone_);
         write_fluxes(P, R, outDir_);
         write_emitters(P, R, outDir_);
@@ -256,12 +269,13 @@ public:
         s->d2h_bytes = d2h_;
         s->n_flux_regions = static_cast<int32_t>(dft_.size());
         s->n_emitters = static_cast<int32_t>(emit_.size());
+        s->n_tfsf = static_cast<int32_t>(tfsf_.size());
     }
 
     int profile(int nsteps, double* ms, int maxSlots) override {
         if (finalized_) throw std::logic_error("step after finalize");
         const int nDft = static_cast<int>(dft_.size());
-        const int nslots = 5 + 2 * nDft + static_cast<int>(emit_.size());
+        const int nslots = 5 + 2 * nDft + static_cast<int>(emit_.size()) + static_cast<int>(tfsf_.size());
         // a start and an end event per slot, recorded around that slot's launches
         std::vector<cudaEvent_t> e0(static_cast<std::size_t>(nslots)), e1(static_cast<std::size_t>(nslots));
         for (auto& e : e0) ck(cudaEventCreate(&e), "cudaEventCreate");
@@ -275,6 +289,12 @@ public:
             mark(e0, 0);
             dev::launch_pass<T>(hPass_, false, s);
             mark(e1, 0);
+            for (std::size_t q = 0; q < tfsf_.size(); ++q) {
+                const int k = 5 + 2 * nDft + static_cast<int>(emit_.size() + q);
+                mark(e0, k);
+                launchTfsf(tfsf_[q], s);
+                mark(e1, k);
+            }
             mark(e0, 1);
             dev::launch_sources<T>(src_, fields_, dStep_, s);
             mark(e1, 1);
@@ -329,6 +349,11 @@ public:
     const std::vector<dev::DftTable<T>>& dftTables() const { return dft_; }
     const std::vector<dev::EmitterDev>& emitters() const { return emit_; }
     int* stepCounter() const { return dStep_; }
+    bool hasTfsf() const { return !tfsf_.empty(); }
+    // The member's TFSF kernels on the given stream (packed steps launch them per member).
+    void launchTfsfOn(void* s) {
+        for (auto& t : tfsf_) launchTfsf(t, s);
+    }
     long long stepsLeft() const { return finalized_ ? 0 : static_cast<long long>(P.nSteps) - stepsDone_; }
     // Counts n steps that a packed launch sequence queued for this member.
     void stepsRunElsewhere(long long n) {
@@ -350,6 +375,7 @@ private:
     dev::RecordTable recT_{};
     std::vector<dev::DftTable<T>> dft_;
     std::vector<dev::EmitterDev> emit_;
+    std::vector<dev::TfsfDev> tfsf_;
     std::vector<long long> recBase_;
     std::size_t recTotal_ = 0;
     double* dRec_ = nullptr;
@@ -366,6 +392,8 @@ private:
     void enqueueStep() {
         void* s = stream_;
         dev::launch_pass<T>(hPass_, false, s);
+        // TFSF after the H update, before the sources (parallelFDTDField.hpp:1237-1261)
+        for (auto& t : tfsf_) launchTfsf(t, s);
         dev::launch_sources<T>(src_, fields_, dStep_, s);
         dev::launch_pass<T>(ePass_, true, s);
         launchEmitters(s);
@@ -374,6 +402,127 @@ private:
         for (auto& d : dft_) {
             dev::launch_dft_sample<T>(d, fields_, dStep_, s);
             dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
+        }
+    }
+
+    void launchTfsf(const dev::TfsfDev& t, void* s) {
+        T* const f6[6] = {fields_.f[0], fields_.f[1], fields_.f[2], fields_.f[3], fields_.f[4], fields_.f[5]};
+        dev::launch_tfsf_step<T>(t, f6, dStep_, s);
+    }
+
+    // TFSF surfaces: the lines' two grids and psi lists (zeroed), the pulse table of
+    // every step, the record array and the surface corrections as per-cell term lists.
+    void uploadTfsf() {
+        for (const TfsfPlan& tp : P.tfsf) {
+            dev::TfsfDev t{};
+            t.gridLen = tp.gridLen;
+            t.pulseLen = tp.pulseLen;
+            t.mTot = tp.mTot;
+            t.pulAddStart = tp.pulAddStart;
+            t.nSteps = P.nSteps;
+            for (int c = 0; c < 6; ++c) {
+                const TfsfLine& L = tp.line[c];
+                dev::TfsfLineDev& d = t.line[c];
+                d.present = L.present ? 1 : 0;
+                if (!L.present) continue;
+                if (L.runs.size() != 1 || L.pulseRuns.size() != 1) throw UnsupportedError("TFSF line with several materials");
+                if (L.pml.size() > dev::kTfsfMaxPsi || L.pmlPulse.size() > dev::kTfsfMaxPsi)
+                    throw UnsupportedError("TFSF line CPML with more than four psi lists");
+                d.useJ = L.useJ ? 1 : 0;
+                d.useK = L.useK ? 1 : 0;
+                d.nbrJ = L.nbrJ;
+                d.nbrK = L.nbrK;
+                d.prefact = make_double2(L.prefact.real(), L.prefact.imag());
+                d.U = mem_.alloc<double2>(static_cast<std::size_t>(tp.gridLen));
+                d.pul = mem_.alloc<double2>(static_cast<std::size_t>(tp.pulseLen));
+                auto run = [](const TfsfRun& r) {
+                    return dev::TfsfRunDev{r.indI, r.n, r.posJ, r.negJ, r.posK, r.negK, r.pj, r.pk};
+                };
+                d.run = run(L.runs[0]);
+                d.pulseRun = run(L.pulseRuns[0]);
+                // every index a line element reads or writes stays inside its grid
+                auto inRange = [](long long lo, long long n, long long len) { return lo >= 0 && n >= 0 && lo + n <= len; };
+                const TfsfRun* rr[2] = {&L.runs[0], &L.pulseRuns[0]};
+                const long long lens[2] = {tp.gridLen, tp.pulseLen};
+                for (int g = 0; g < 2; ++g) {
+                    const TfsfRun& r = *rr[g];
+                    if (!inRange(r.indI, r.n, lens[g]) || !inRange(r.posJ, r.n, lens[g]) || !inRange(r.negJ, r.n, lens[g]) ||
+                        !inRange(r.posK, r.n, lens[g]) || !inRange(r.negK, r.n, lens[g]))
+                        throw InputError("TFSF run outside its line");
+                    const std::vector<TfsfPsi>& pl = g == 0 ? L.pml : L.pmlPulse;
+                    for (const TfsfPsi& q : pl)
+                        if (!inRange(q.loc, q.n, lens[g]) || !inRange(q.locOff, q.n, lens[g]) || !inRange(q.gridLoc, q.n, lens[g]) ||
+                            q.nbr < 0 || q.nbr > 5 || !tp.line[q.nbr].present || static_cast<int>(q.b.size()) != q.n ||
+                            static_cast<int>(q.c.size()) != q.n || static_cast<int>(q.cOff.size()) != q.n)
+                            throw InputError("TFSF CPML list outside its line");
+                }
+                if ((L.useJ && !tp.line[L.nbrJ].present) || (L.useK && !tp.line[L.nbrK].present) || L.recIdx < 0 ||
+                    L.recIdx >= tp.pulseLen || L.recOffIdx < 0 || L.recOffIdx >= tp.pulseLen || tp.pulAddStart < 0 ||
+                    tp.pulAddStart + tp.mTot > tp.pulseLen || static_cast<int>(L.dist.size()) != tp.mTot)
+                    throw InputError("TFSF line set-up inconsistent");
+                auto psiList = [&](const TfsfPsi& q) {
+                    dev::TfsfPsiDev o{};
+                    o.nbr = q.nbr;
+                    o.loc = q.loc;
+                    o.locOff = q.locOff;
+                    o.gridLoc = q.gridLoc;
+                    o.n = q.n;
+                    o.Db = q.Db;
+                    o.b = mem_.upload(q.b);
+                    o.c = mem_.upload(q.c);
+                    o.cOff = mem_.upload(q.cOff);
+                    o.psi = mem_.alloc<double2>(static_cast<std::size_t>(q.n));
+                    return o;
+                };
+                d.nPml = static_cast<int>(L.pml.size());
+                for (int q = 0; q < d.nPml; ++q) d.pml[q] = psiList(L.pml[q]);
+                d.nPmlPulse = static_cast<int>(L.pmlPulse.size());
+                for (int q = 0; q < d.nPmlPulse; ++q) d.pmlPulse[q] = psiList(L.pmlPulse[q]);
+                d.recIdx = L.recIdx;
+                d.recOffIdx = L.recOffIdx;
+            }
+            // fillPulseVec for every step (SOURCE/parallelTFSF.cpp:76-81) at t = step * dt
+            std::vector<double2> tab(static_cast<std::size_t>(std::max(P.nSteps, 1)) * 6 * tp.mTot, make_double2(0.0, 0.0));
+            for (int st = 0; st < P.nSteps; ++st)
+                for (int c = 0; c < 6; ++c) {
+                    if (!tp.line[c].present) continue;
+                    for (int r = 0; r < tp.mTot; ++r) {
+                        cplx v = 0.0;
+                        for (const PulseSpec& p : tp.pulses) v = v + p.value(static_cast<double>(st) * tp.dt - tp.line[c].dist[r]);
+                        tab[(static_cast<std::size_t>(st) * 6 + c) * tp.mTot + r] = make_double2(v.real(), v.imag());
+                    }
+                }
+            t.pulseTab = mem_.upload(tab);
+            t.rec = mem_.alloc<double2>(6 * 2 * (static_cast<std::size_t>(P.nSteps) + 1));
+            const std::vector<TfsfCellAdds>* adds[2] = {&tp.addH, &tp.addE};
+            for (int w = 0; w < 2; ++w) {
+                std::vector<long long> cell;
+                std::vector<int> comp, start, tl, ti;
+                std::vector<double> pref;
+                for (const TfsfCellAdds& a : *adds[w]) {
+                    cell.push_back(a.cell);
+                    comp.push_back(a.comp);
+                    start.push_back(static_cast<int>(tl.size()));
+                    for (std::size_t k = 0; k < a.line.size(); ++k) {
+                        if (a.toD[k]) throw UnsupportedError("TFSF corrections into D");
+                        if (!tp.line[a.line[k]].present || a.incd[k] < 0 || a.incd[k] >= tp.gridLen ||
+                            a.cell < 0 || a.cell >= P.dims.cells() || !P.comp[a.comp].present)
+                            throw InputError("TFSF correction outside its grids");
+                        tl.push_back(a.line[k]);
+                        ti.push_back(a.incd[k]);
+                        pref.push_back(a.pref[k]);
+                    }
+                }
+                start.push_back(static_cast<int>(tl.size()));
+                t.nCell[w] = static_cast<int>(cell.size());
+                t.cell[w] = mem_.upload(cell);
+                t.comp[w] = mem_.upload(comp);
+                t.start[w] = mem_.upload(start);
+                t.termLine[w] = mem_.upload(tl);
+                t.termIncd[w] = mem_.upload(ti);
+                t.termPref[w] = mem_.upload(pref);
+            }
+            tfsf_.push_back(t);
         }
     }
 
@@ -905,6 +1054,7 @@ private:
             dft_.push_back(d);
         }
         uploadEmitters();
+        uploadTfsf();
         bytesPerCell_ = algorithmicBytesPerCell();
         dStep_ = mem_.alloc<int>(1);
         dErr_ = mem_.alloc<unsigned int>(1);
@@ -913,7 +1063,7 @@ private:
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
         kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size()) +
-                          (ePass_.nLor > 0 ? 1 : 0) + 3 * static_cast<int>(emit_.size());
+                          (ePass_.nLor > 0 ? 1 : 0) + 3 * static_cast<int>(emit_.size()) + 3 * static_cast<int>(tfsf_.size());
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
         for (auto& d : dft_) dev::launch_dft_sample<T>(d, fields_, dStep_, stream_);
@@ -1129,6 +1279,8 @@ private:
         void* s = stream_;
         dev::launch_pass_packed<T>(dH_, passMap_, false, s);
         dev::launch_pass2d_packed<T>(dH_, p2Map_[0], false, s);
+        for (Sim<T>* m : members_)
+            if (m->hasTfsf()) m->launchTfsfOn(s);
         dev::launch_sources_packed<T>(dSrc_, srcMap_, s);
         dev::launch_ordip_packed<T>(dE_, odMap_, s);
         dev::launch_pass_packed<T>(dE_, passMap_, true, s);

@@ -1,0 +1,65 @@
+// Device descriptor of one TFSF surface: the 1-D incident lines (complex FP64), their
+// CPML psi lists, the pulse table and the surface corrections. Kernels in
+// tfsf_kernels.cu, host set-up in engine.cpp.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace chiml {
+namespace dev {
+
+constexpr int kTfsfMaxPsi = 4;
+
+// The single run of a vacuum line: U[indI + r] += pj (J[posK + r] - J[negK + r])
+// + pk (K[posJ + r] - K[negJ + r]) for r < n.
+struct TfsfRunDev {
+    int indI, n, posJ, negJ, posK, negK;
+    double pj, pk;
+};
+
+// One CPML psi list of a line: psi = b psi + c N[loc + d] + cOff N[locOff + d],
+// U[gridLoc + d] += Db psi, for d < n; N is line nbr (of the same grid kind).
+struct TfsfPsiDev {
+    int nbr, loc, locOff, gridLoc, n;
+    double Db;
+    const double* b;
+    const double* c;
+    const double* cOff;
+    double2* psi;
+};
+
+// A line: its incident grid and its pulse grid. In vacuum D / B equals the field
+// (division by eps = mu = 1 is exact), so one array per grid holds both.
+struct TfsfLineDev {
+    int present, useJ, useK, nbrJ, nbrK;
+    double2 prefact;
+    double2* U;    // [gridLen]
+    double2* pul;  // [pulseLen]
+    TfsfRunDev run, pulseRun;
+    int nPml, nPmlPulse;
+    TfsfPsiDev pml[kTfsfMaxPsi], pmlPulse[kTfsfMaxPsi];
+    int recIdx, recOffIdx;
+};
+
+struct TfsfDev {
+    int gridLen, pulseLen, mTot, pulAddStart, nSteps;
+    TfsfLineDev line[6];       // 0..2 Ex..Ez, 3..5 Hx..Hz
+    const double2* pulseTab;   // [step][line][mTot]: sum of the pulses at the line's pulse points
+    double2* rec;              // [line][2 (nSteps + 1)]: recorded incident values (flux normalisation)
+    // surface corrections, per cell (CSR over the terms): F[comp][cell] += pref * Re(line[incd])
+    int nCell[2];              // [0] H corrections, [1] E corrections
+    const long long* cell[2];
+    const int* comp[2];
+    const int* start[2];       // [nCell + 1]
+    const int* termLine[2];
+    const int* termIncd[2];
+    const double* termPref[2];
+};
+
+// Per step, after the H pass: H corrections, the 1-D step of every line (with the
+// incident records), E corrections. fields: the main grid's E (0..2) and H (3..5).
+template <typename T>
+void launch_tfsf_step(const TfsfDev& t, T* const fields[6], const int* step, void* stream);
+
+}  // namespace dev
+}  // namespace chiml

@@ -25,7 +25,7 @@ typedef struct chiml_sim chiml_sim;
 typedef enum chiml_status {
     CHIML_OK = 0,
     CHIML_E_INPUT = 1,       /* malformed or inconsistent input (the reference throws std::logic_error) */
-    CHIML_E_UNSUPPORTED = 2, /* a feature outside this engine (magnetic/chiral media, PBC, TFSF, ...) */
+    CHIML_E_UNSUPPORTED = 2, /* a feature outside this engine (magnetic/chiral media, PBC, ...) */
     CHIML_E_CUDA = 3,        /* a CUDA runtime error */
     CHIML_E_OOM = 4,         /* device memory exhausted */
     CHIML_E_NUMERIC = 5,     /* a NaN or Inf reached a monitored field value */
@@ -63,6 +63,7 @@ typedef struct chiml_stats {
     double d2h_bytes;              /* bytes copied device to host so far */
     int32_t n_flux_regions;        /* DFT flux regions (two profile slots each) */
     int32_t n_emitters;            /* emitter objects (one profile slot each) */
+    int32_t n_tfsf;                /* TFSF surfaces (one profile slot each) */
 } chiml_stats;
 
 /* Reads the JSON input (chiML schema), builds the update plan and uploads it. */
@@ -100,7 +101,8 @@ void* chiml_stream(chiml_sim* sim);
  * events on the handle's stream. ms_out[k] receives the summed milliseconds of
  * kernel slot k: 0 H pass, 1 sources, 2 E pass, 3 step counter, 4 detector
  * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of flux region q, then
- * 5 + 2 * n_flux_regions + e the emitter step of emitter object e.
+ * 5 + 2 * n_flux_regions + e the emitter step of emitter object e, then
+ * 5 + 2 * n_flux_regions + n_emitters + k the step of TFSF surface k.
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
