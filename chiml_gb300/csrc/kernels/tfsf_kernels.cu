@@ -4,15 +4,16 @@
 // IncdCPML addPsi / updatePsiField, PML/PML.cpp:12-31; surface adds, addIncdFields,
 // SOURCE/parallelTFSF.cpp:84-90).
 //
-//   k_tfsf_add    one thread per corrected main-grid cell, its terms in the reference's
-//                 order: F += pref * Re(incident line value)
-//   k_tfsf_lines  one block: records the H incident values, steps the H lines, then the
-//                 E lines, and records the E incident values. Within a phase every line
-//                 element is updated by one thread in the reference's per-element order
-//                 (pulse add, J and K curl terms, then each CPML psi list touching it):
-//                 the phase only reads lines of the other kind, so its elements are
-//                 independent. Complex FP64 in both precision forms (the lines are a
-//                 few thousand points).
+//   k_tfsf_half   launched twice per step. The first launch steps the H lines and adds
+//                 the H corrections (from the E lines), the second steps the E lines and
+//                 adds the E corrections (from the new H lines). Every line element is
+//                 updated by one thread in the reference's per-element order (pulse add,
+//                 J and K curl terms, then each CPML psi list touching it): a half only
+//                 reads lines of the other kind, so its elements are independent. Each
+//                 corrected main-grid cell is one thread that adds its terms in the
+//                 reference's order: F += pref * Re(incident line value).
+//   k_tfsf_record the incident values recorded for flux normalisation.
+// The lines are complex FP64 in both precision forms (a few thousand points).
 #include "tfsf_device.hpp"
 
 namespace chiml {
@@ -27,11 +28,10 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// Surface corrections of cell q of list `which` (0 H, 1 E).
 template <typename T>
-__global__ void __launch_bounds__(256) k_tfsf_add(const TfsfDev t, int which, T* F0, T* F1, T* F2, T* F3, T* F4, T* F5) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, T* const F[6]) {
     if (q >= t.nCell[which]) return;
-    T* const F[6] = {F0, F1, F2, F3, F4, F5};
     T* f = F[t.comp[which][q]];
     const long long cell = t.cell[which][q];
     double v = static_cast<double>(f[cell]);
@@ -76,37 +76,49 @@ __device__ __forceinline__ void lineElement(const TfsfDev& t, int c, bool pulseG
     G[x] = v;
 }
 
-// Every element of every grid of the lines c0 .. c0 + 2, strided over the block.
-__device__ __forceinline__ void linePhase(const TfsfDev& t, int c0, int s) {
+// Element e of the lines c0 .. c0 + 2 (incident grid, then pulse grid, per line).
+__device__ __forceinline__ void lineAny(const TfsfDev& t, int c0, int e, int s) {
     const int per = t.gridLen + t.pulseLen;
-    for (int e = threadIdx.x; e < 3 * per; e += blockDim.x) {
-        const int c = c0 + e / per;
-        if (!t.line[c].present) continue;
-        const int x = e % per;
-        if (x < t.gridLen) lineElement(t, c, false, x, s);
-        else lineElement(t, c, true, x - t.gridLen, s);
+    if (e >= 3 * per) return;
+    const int c = c0 + e / per;
+    if (!t.line[c].present) return;
+    const int x = e % per;
+    if (x < t.gridLen) lineElement(t, c, false, x, s);
+    else lineElement(t, c, true, x - t.gridLen, s);
+}
+
+constexpr int kTfsfThreads = 256;
+
+// One half of the TFSF step: blocks [0, lineBlocks) step the lines of kind c0 (3: H,
+// 0: E), the other blocks add the corrections of list `which` (0: H corrections, from
+// the E lines; 1: E corrections, from the H lines). The two parts touch disjoint data:
+// the corrections read the lines of the other kind, which this half does not write.
+template <typename T>
+__global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, T* F0, T* F1,
+                                                            T* F2, T* F3, T* F4, T* F5, const int* __restrict__ step) {
+    const int s = *step;
+    if (s >= t.nSteps) return;
+    if (static_cast<int>(blockIdx.x) < lineBlocks) {
+        lineAny(t, c0, blockIdx.x * kTfsfThreads + threadIdx.x, s);
+    } else {
+        T* const F[6] = {F0, F1, F2, F3, F4, F5};
+        addCell(t, which, (blockIdx.x - lineBlocks) * kTfsfThreads + threadIdx.x, F);
     }
 }
 
-__device__ __forceinline__ void record(const TfsfDev& t, int c0, int s) {
-    if (threadIdx.x >= 3) return;
-    const int c = c0 + threadIdx.x;
+// Incident records after the step: E values of this step and the H values the next step
+// starts from (the H lines do not change until then); step 0's H values are zero, and
+// like the reference no H values are kept for the step after the last.
+__global__ void k_tfsf_record(const TfsfDev t, const int* __restrict__ step) {
+    const int s = *step;
+    if (s >= t.nSteps || threadIdx.x >= 6) return;
+    const int c = threadIdx.x;
+    const int slot = c < 3 ? s : s + 1;
+    if (slot >= t.nSteps) return;  // slot nSteps is never a step's start: it stays zero
     const TfsfLineDev& L = t.line[c];
-    const long long base = static_cast<long long>(c) * 2 * (t.nSteps + 1) + 2LL * s;
+    const long long base = static_cast<long long>(c) * 2 * (t.nSteps + 1) + 2LL * slot;
     t.rec[base] = L.present ? L.pul[L.recIdx] : make_double2(0.0, 0.0);
     t.rec[base + 1] = L.present ? L.pul[L.recOffIdx] : make_double2(0.0, 0.0);
-}
-
-__global__ void __launch_bounds__(1024) k_tfsf_lines(const TfsfDev t, const int* __restrict__ step) {
-    const int s = *step;
-    if (s >= t.nSteps) return;
-    record(t, 3, s);  // H incident values before the step (parallelFDTDField.hpp:1240-1245)
-    __syncthreads();
-    linePhase(t, 3, s);
-    __syncthreads();
-    linePhase(t, 0, s);
-    __syncthreads();
-    record(t, 0, s);  // E incident values after it (parallelFDTDField.hpp:1249-1254)
 }
 
 }  // namespace
@@ -114,13 +126,13 @@ __global__ void __launch_bounds__(1024) k_tfsf_lines(const TfsfDev t, const int*
 template <typename T>
 void launch_tfsf_step(const TfsfDev& t, T* const fields[6], const int* step, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (t.nCell[0] > 0)
-        k_tfsf_add<T><<<(t.nCell[0] + 255) / 256, 256, 0, s>>>(t, 0, fields[0], fields[1], fields[2], fields[3], fields[4],
-                                                              fields[5]);
-    k_tfsf_lines<<<1, 1024, 0, s>>>(t, step);
-    if (t.nCell[1] > 0)
-        k_tfsf_add<T><<<(t.nCell[1] + 255) / 256, 256, 0, s>>>(t, 1, fields[0], fields[1], fields[2], fields[3], fields[4],
-                                                              fields[5]);
+    const int lineBlocks = (3 * (t.gridLen + t.pulseLen) + kTfsfThreads - 1) / kTfsfThreads;
+    for (int half = 0; half < 2; ++half) {
+        const int addBlocks = (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
+        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, fields[0], fields[1],
+                                                                        fields[2], fields[3], fields[4], fields[5], step);
+    }
+    k_tfsf_record<<<1, 32, 0, s>>>(t, step);
 }
 
 template void launch_tfsf_step<float>(const TfsfDev&, float* const[6], const int*, void*);

@@ -117,14 +117,15 @@ def test_batch_split_equals_members_run_alone(built_engine, tmp_path):
 
 @pytest.mark.gpu
 def test_batch_of_golden_cases_matches_reference_outputs(built_engine, tmp_path):
-    """Members of different dimensions, media and step counts in one batch (3-D anisotropic
-    and dispersive, 3-D and 2-D emitters, 2-D dielectric): the packed steps run in phases
+    """Members of different dimensions, media, sources and step counts in one batch (3-D
+    anisotropic and dispersive, 3-D and 2-D emitters, 2-D dielectric, 2-D and 3-D TFSF
+    plane waves): the packed steps run in phases
     that stop each member at its own last step, and every member still meets the FP64
     parity bar against the reference's own outputs."""
     import shutil
     from conftest import GOLDEN, golden_cases
     from chiml_gb300 import Batch
-    cases = [c for c in ["c2_aniso", "qe_3d", "qe_tm", "c1_small"] if c in golden_cases()]
+    cases = [c for c in ["c2_aniso", "qe_3d", "qe_tm", "c1_small", "tfsf_2d_te", "tfsf_disp"] if c in golden_cases()]
     assert len(cases) >= 3
     paths = []
     for c in cases:

@@ -59,7 +59,7 @@ def test_fp64_fields_match_oracle_midrun(case, built_engine, built_oracle):
     assert checked >= 3
 
 
-@pytest.mark.parametrize("case", ["c2_small", "qe_3d"])
+@pytest.mark.parametrize("case", ["c2_small", "qe_3d", "tfsf_oblique"])
 def test_graph_replay_equals_eager_launches(case, built_engine, tmp_path):
     a = tmp_path / "eager"
     b = tmp_path / "graph"
