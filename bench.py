@@ -2,8 +2,8 @@
 """Benchmark of chiML's time-step loop on GB300: Gcell-updates/s and HBM roofline.
 
 Workload: the 3-D dispersive configuration (256^3 cells, 12-cell CPML, 16
-seeded ellipsoids, a Drude + two-Lorentz metal sphere, a plane Ex source, a
-150-frequency DFT flux box), generated by chiml_gb300.configs.config2.
+seeded uniaxial ellipsoids, a Drude + two-Lorentz metal sphere, an x-polarised TFSF
+plane wave along +z, a 150-frequency DFT flux box), generated by chiml_gb300.configs.config2.
 One step is one full time step (H half + E half + detectors + DFT).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -105,9 +105,26 @@ def _dist():
     return world, rank, local
 
 
-def _workload(n, steps):
+# The workloads: the default is the 3-D anisotropic + dispersive scene the headline
+# metric is quoted on; c1 (2-D TMz), c3 (3-D Maxwell-Liouville) and c4 (batched sweep of
+# 2-D emitter sheets) are the other configurations, for design measurements.
+WORKLOADS = {
+    "c2": ("Gcell-updates/s (FP32/FP64-split, 3-D dispersive 256^3)",
+           "3-D anisotropic + dispersive: %d^3 cells, 12-cell CPML, 16 uniaxial ellipsoids, Drude+2-Lorentz sphere, "
+           "x-polarised TFSF plane wave at 550 nm, DFT flux box x 150 freqs", 256, "config2"),
+    "c1": ("Gcell-updates/s (FP32/FP64-split, 2-D TMz 400^2)",
+           "2-D TMz: %d^2 cells, 20-cell CPML, dielectric disk, Ez point source, 8 point detectors, flux line x 100 freqs",
+           400, "config1"),
+    "c3": ("Gcell-updates/s (FP32/FP64-split fields, FP64 density matrices, 3-D Maxwell-Liouville 192^3)",
+           "3-D Maxwell-Liouville: %d^3 cells, 12-cell CPML, 20-cell slab of 3-level ladder emitters (9 ensemble members "
+           "per cell from 20 meV Gaussian broadening), 1e26 m^-3, Ez plane source at 2.1 eV, flux plane x 50 freqs",
+           192, "config3"),
+}
+
+
+def _workload(n, steps, name="c2"):
     from chiml_gb300 import configs
-    return configs.config2(n=n, steps=steps)
+    return getattr(configs, WORKLOADS[name][3])(n=n, steps=steps)
 
 
 def _time_steps(sim, k, torch):
@@ -137,7 +154,7 @@ def run_ours(args):
     n = args.n
     total_steps = args.warmup + args.steps + args.profile_steps + 2
     work = tempfile.mkdtemp(prefix="chiml_bench_")
-    cfg_path = configs.write_json(_workload(n, total_steps), os.path.join(work, "in.json"))
+    cfg_path = configs.write_json(_workload(n, total_steps, args.workload), os.path.join(work, "in.json"))
     peak, peak_kind = _peaks()
     results = {}
     for prec in ("split", "fp64"):
@@ -206,7 +223,7 @@ def run_ours(args):
     if rank == 0:
         launches = sp["stats"].kernels_per_step * args.steps
         line = {
-            "metric": "Gcell-updates/s (FP32/FP64-split, 3-D dispersive 256^3)",
+            "metric": WORKLOADS[args.workload][0],
             "value": round(value, 3),
             "unit": "Gcell-updates/s",
             "n_gpus": world,
@@ -217,10 +234,9 @@ def run_ours(args):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f32 fields, f64 DFT accumulators",
-            "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.config2)",
+            "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.%s)" % WORKLOADS[args.workload][3],
             "config": {
-                "workload": "3-D dispersive: %d^3 cells, 12-cell CPML, 16 ellipsoids, Drude+2-Lorentz sphere, "
-                            "plane Ex source, DFT flux box x 150 freqs" % n,
+                "workload": WORKLOADS[args.workload][1] % n,
                 "cells": cells,
                 "precision": "split",
                 "l2": "inputs larger than L2 (%.0f MB of field state vs 129 MB L2)" % (sp["stats"].device_bytes / 1e6),
@@ -276,10 +292,10 @@ def run_reference(args):
     build.build_oracle()
     work = tempfile.mkdtemp(prefix="chiml_ref_")
     total = args.warmup + args.steps + 2
-    cfg_path = configs.write_json(_workload(args.n, total), os.path.join(work, "in.json"))
+    cfg_path = configs.write_json(_workload(args.n, total, args.workload), os.path.join(work, "in.json"))
     sim = oracle.OracleSim(cfg_path)
     sim.step(args.warmup)
-    cells = (args.n) ** 3
+    cells = (args.n) ** (2 if args.workload == "c1" else 3)
     per_step = []
     t_all = time.perf_counter()
     for _ in range(args.steps):
@@ -290,7 +306,7 @@ def run_reference(args):
     sim.close()
     v = cells * args.steps / total_s / 1e9
     line = {
-        "metric": "Gcell-updates/s (FP32/FP64-split, 3-D dispersive 256^3)",
+        "metric": WORKLOADS[args.workload][0],
         "value": round(v, 5),
         "unit": "Gcell-updates/s",
         "impl": "reference",
@@ -302,13 +318,159 @@ def run_reference(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.config2)",
-        "config": {"workload": "3-D dispersive: %d^3 cells, same input as the GPU arm" % args.n, "cells": cells},
+        "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.%s)" % WORKLOADS[args.workload][3],
+        "config": {"workload": WORKLOADS[args.workload][1] % args.n, "cells": cells},
         "cpu_baseline": {"value": round(v, 5), "unit": "Gcell-updates/s", "cores": oracle.threads(), "kind": "port",
                          "sample": "%d timed steps of the full workload after %d warm-up steps" % (args.steps, args.warmup)},
         "e2e": {"value": round(v, 5), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def _c4_members(work, n_members, steps):
+    from chiml_gb300 import configs
+    paths = []
+    for name, cfg in configs.config4(n=n_members, steps=steps):
+        d = os.path.join(work, name)
+        os.makedirs(d, exist_ok=True)
+        paths.append(configs.write_json(cfg, os.path.join(d, "in.json")))
+    return paths
+
+
+C4_METRIC = "aggregate Gcell-updates/s (FP32 fields, FP64 density matrices, batched sweep of 2-D emitter sheets)"
+C4_WORKLOAD = ("batched sweep: %d 2-D TMz simulations, sides drawn from {192..768}, 16-cell CPML, 10-cell sheet of "
+               "2-level emitters, detuning -100..+100 meV x density 1e25..1e26 m^-3, T2 = 30 fs")
+
+
+def run_batch(args):
+    """The sweep as one batch (packed launches per kind of work, graph-captured), against
+    the same members run one after another through the single-simulation API."""
+    world, rank, local = _dist()
+    import torch
+    from chiml_gb300 import Batch, Simulation
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    work = tempfile.mkdtemp(prefix="chiml_c4_")
+    total = args.warmup + args.steps
+    paths = _c4_members(work, args.members, total)
+    t0 = time.perf_counter()
+    b = Batch(paths, precision="split", device=local, steps_per_graph=args.graph)
+    t_create = time.perf_counter() - t0
+    sts = [b.member_stats(i) for i in range(len(paths))]
+    cells = sum(st.cells_physical for st in sts)
+    step_bytes = sum(st.bytes_per_cell_update * st.cells_physical for st in sts)
+    b.step(args.warmup)
+    sampler = ClockSampler(local)
+    sampler.start()
+    t0 = time.perf_counter()
+    b.step(args.steps)
+    t_batch = time.perf_counter() - t0
+    clocks = sampler.stop()
+    b.close()
+    value = cells * args.steps / t_batch / 1e9
+    peak, peak_kind = _peaks()
+    achieved = step_bytes * args.steps / t_batch / 1e9
+    # the members alone, one after another (each with its own graphs)
+    t_seq = 0.0
+    for p in paths:
+        sim = Simulation(p, precision="split", device=local, steps_per_graph=args.graph, out_dir=os.path.join(work, "seq"))
+        sim.step(args.warmup)
+        sim.sync()
+        t0 = time.perf_counter()
+        sim.step(args.steps)
+        sim.sync()
+        t_seq += time.perf_counter() - t0
+        sim.close()
+    seq_value = cells * args.steps / t_seq / 1e9
+    e2e = None
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        b2 = Batch(paths, precision="split", device=local, steps_per_graph=args.graph, out_dir=os.path.join(work, "e2e"))
+        b2.run()
+        b2.finalize()
+        t_e2e = time.perf_counter() - t0
+        s2 = [b2.member_stats(i) for i in range(len(paths))]
+        b2.close()
+        e2e = {"value": cells * total / t_e2e / 1e9, "unit": "Gcell-updates/s",
+               "h2d_bytes_per_step": sum(x.h2d_bytes for x in s2) / total,
+               "d2h_bytes_per_step": sum(x.d2h_bytes for x in s2) / total, "seconds": t_e2e,
+               "includes": "JSON reads, plans, uploads, %d steps of every member, downloads, file writes" % total}
+    cpu = None
+    if not args.no_cpu:
+        cpu = batch_cpu_sample(paths, args.cpu_seconds)
+    line = {
+        "metric": C4_METRIC, "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t_batch / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 fields, f64 density matrices and DFT accumulators",
+        "data": "synthetic (seeded PCG64 sizes and sweep values, chiml_gb300.configs.config4)",
+        "config": {"workload": C4_WORKLOAD % len(paths), "members": len(paths), "cells": cells,
+                   "graph_steps": args.graph, "create_s": round(t_create, 2),
+                   "l2": "inputs larger than L2 (%d cells of field state)" % cells},
+        "sequential": {"value": round(seq_value, 3), "unit": "Gcell-updates/s", "seconds": round(t_seq, 3),
+                       "batch_speedup": round(value / seq_value, 2)},
+        "roofline": {"bound": "hbm", "kernel": "whole packed step", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                     "bytes_per_step": step_bytes},
+        "gpu_launches": None, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+def batch_cpu_sample(paths, seconds):
+    """The oracle on the sweep's members in turn, a bounded number of steps each."""
+    import oracle
+    from chiml_gb300 import build
+    build.build_oracle()
+    cells_done, t_used, members = 0, 0.0, 0
+    per = max(seconds / len(paths), 0.05)
+    for p in paths:
+        sim = oracle.OracleSim(p)
+        sim.step(1)
+        st = sim.cells_physical()
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < per:
+            sim.step(1)
+            n += 1
+        t_used += time.perf_counter() - t0
+        cells_done += st * n
+        members += 1
+        sim.close()
+    return {"value": round(cells_done / t_used / 1e9, 5), "unit": "Gcell-updates/s", "cores": oracle.threads(),
+            "kind": "port", "sample": "every member of the sweep for %.2f s each (%d members)" % (per, members)}
+
+
+def run_batch_reference(args):
+    world, rank, local = _dist()
+    if rank != 0:
+        return
+    import oracle
+    from chiml_gb300 import build
+    build.build_oracle()
+    work = tempfile.mkdtemp(prefix="chiml_c4_ref_")
+    paths = _c4_members(work, args.members, args.warmup + args.steps)
+    cells, t_used = 0, 0.0
+    for p in paths:
+        sim = oracle.OracleSim(p)
+        sim.step(args.warmup)
+        t0 = time.perf_counter()
+        sim.step(args.steps)
+        t_used += time.perf_counter() - t0
+        cells += sim.cells_physical() * args.steps
+        sim.close()
+    v = cells / t_used / 1e9
+    print(json.dumps({
+        "metric": C4_METRIC, "value": round(v, 5), "unit": "Gcell-updates/s", "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t_used / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64 sizes and sweep values, chiml_gb300.configs.config4)",
+        "config": {"workload": C4_WORKLOAD % len(paths), "members": len(paths)},
+        "cpu_baseline": {"value": round(v, 5), "unit": "Gcell-updates/s", "cores": oracle.threads(), "kind": "port",
+                         "sample": "every member run alone for %d timed steps after %d warm-up steps" % (args.steps, args.warmup)},
+        "e2e": {"value": round(v, 5), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
 
 
 def main():
@@ -317,7 +479,10 @@ def main():
     ap.add_argument("--steps", type=int, default=512)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=N_DEFAULT, help="cells per side")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["c4"], default="c2",
+                    help="c2 (default, the headline), c1, c3, or c4 (the batched sweep)")
+    ap.add_argument("--n", type=int, default=None, help="cells per side (default: the workload's)")
+    ap.add_argument("--members", type=int, default=96, help="c4: simulations in the sweep")
     ap.add_argument("--graph", type=int, default=20, help="steps per CUDA graph")
     ap.add_argument("--profile-steps", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -326,6 +491,14 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
+    if args.n is None:
+        args.n = WORKLOADS[args.workload][2] if args.workload in WORKLOADS else 0
+    if args.workload == "c4":
+        if args.impl == "reference":
+            run_batch_reference(args)
+        else:
+            run_batch(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

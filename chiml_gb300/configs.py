@@ -199,6 +199,42 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
     }
 
 
+def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, coupling=C4_COUPLING, nfreq=50):
+    """3-D Maxwell-Liouville scene: a ``slab_cells``-thick slab (normal z) of three-level
+    ladder emitters across the cell inside the CPML, transitions at 2.0 and 2.2 eV with
+    Gaussian inhomogeneous broadening of 20 meV sampled at ``nstates`` energies per upper
+    level (nstates^2 ensemble members per cell), z dipoles, T1 = 1 ps and T2 = 50 fs on
+    both transitions, ground-state start; an Ez plane source sheet below the slab with a
+    Gaussian pulse at 2.1 eV, 10 fs wide, peak 5e8 V/m; a flux plane above
+    the slab, a point detector and the upper-level populations."""
+    dx = 0.05
+    dt = 0.5 * dx / math.sqrt(3.0)
+    size = (n - 1) * dx
+    half = size / 2
+    inner = size - 2 * (pml + 2) * dx
+    lv = [emitter_level(0.0), emitter_level(2.0, "Gaussian", nstates, 0.02), emitter_level(4.2, "Gaussian", nstates, 0.02)]
+    relax = [(1, 0, 1e12, 1.0 / 50e-15), (2, 1, 1e12, 1.0 / 50e-15)]
+    qe = emitter_obj("block", [0.0, 0.0, 0.0], [(0, 0), (1, 0), (2, 0)], lv, [coupling] * 9, relax, mol_den, eps=1.0,
+                     dtc_levs=[0, 4, 8], output_pol="c3_pol.dat", dtc_base="c3_qe_",
+                     size=[inner, inner, slab_cells * dx])
+    width = 10e-15 / T_UNIT
+    src_z = -round((half - (pml + 4) * dx) / dx) * dx
+    out_z = round((half - (pml + 6) * dx) / dx) * dx
+    return {
+        "CompCell": {"size": [size, size, size], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
+                     "a": A, "pol": "Ez", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
+        "PML": {"thickness": [pml * dx] * 3, "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
+        "SourceList": [{"pol": "Ez", "loc": [0.0, 0.0, src_z], "size": [inner, inner, 0.0],
+                        "PulseList": [_gauss(ev2fdtd(2.1), 1.0 / width, 4.0, 3 * width, amp=C4_AMPLITUDE)]}],
+        "TFSF": [],
+        "ObjectList": [qe],
+        "DetectorList": [{"loc": [0.0, 0.0, out_z], "size": [0.0, 0.0, 0.0], "type": "Ez", "fname": "c3_pt",
+                          "dtc_class": "txt", "SI": False, "Time_Interval": dt}],
+        "FluxList": [{"name": "c3_flux", "loc": [0.0, 0.0, out_z], "size": [inner, inner, 0.0],
+                      "lamL": 5.0, "lamR": 7.0, "nfreq": nfreq, "SI": False}],
+    }
+
+
 def config4_member(side, detuning_ev, mol_den, pml=16, steps=6000, sheet_cells=10, coupling=C4_COUPLING,
                    nfreq=50, tag="c4"):
     """One point of the batched sweep: a 2-D TMz square of ``side`` cells (dx = 5 nm) with a

@@ -65,6 +65,10 @@ class OracleSim:
     def step(self, n):
         return self._lib.chiml_oracle_step(self._h, int(n))
 
+    def cells_physical(self):
+        d = self.dims()
+        return d[3] * d[4] * d[5]
+
     def field(self, name):
         lx, ly, lz = self.dims()[:3]
         out = np.empty(lx * ly * lz, dtype=np.float64)
