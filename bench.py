@@ -270,11 +270,11 @@ def cpu_baseline(cfg_path, cells, seconds):
     from chiml_gb300 import build
     build.build_oracle()
     sim = oracle.OracleSim(cfg_path)
-    sim.step(1)
+    done = sim.step(1)
     t0 = time.perf_counter()
     n = 0
-    while time.perf_counter() - t0 < seconds:
-        sim.step(1)
+    while time.perf_counter() - t0 < seconds and done < sim.steps_total:
+        done = sim.step(1)
         n += 1
     dt = time.perf_counter() - t0
     sim.close()
@@ -427,12 +427,12 @@ def batch_cpu_sample(paths, seconds):
     per = max(seconds / len(paths), 0.05)
     for p in paths:
         sim = oracle.OracleSim(p)
-        sim.step(1)
+        done = sim.step(1)
         st = sim.cells_physical()
         t0 = time.perf_counter()
         n = 0
-        while time.perf_counter() - t0 < per:
-            sim.step(1)
+        while time.perf_counter() - t0 < per and done < sim.steps_total:
+            done = sim.step(1)
             n += 1
         t_used += time.perf_counter() - t0
         cells_done += st * n
