@@ -564,6 +564,31 @@ private:
         }
     }
 
+    // Whether the density matrices stay Hermitian with a real symmetric Hamiltonian: every
+    // dipole operator real and symmetric, and the relaxation rows map each element pair
+    // (r, c), (c, r) onto conjugate pairs with equal rates (then the mirrored row of a
+    // row holds the mirrored columns with the same values).
+    static bool hermitianForm(const EmitterPlan& ep) {
+        const int N = ep.nlevel;
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < N; ++r)
+                for (int k = 0; k < N; ++k) {
+                    const std::complex<double> a = ep.mu[c][r + k * N], b = ep.mu[c][k + r * N];
+                    if (a.imag() != 0.0 || b.imag() != 0.0 || a.real() != b.real()) return false;
+                }
+        auto mirror = [N](int i) { return (i / N) + (i % N) * N; };
+        std::vector<std::vector<std::pair<int, double>>> rows(static_cast<std::size_t>(N) * N);
+        for (std::size_t ii = 0; ii < ep.gam.size() && ii < rows.size(); ++ii) rows[ii] = ep.gam[ii];
+        for (int ii = 0; ii < N * N; ++ii)
+            for (const auto& g : rows[ii]) {
+                bool found = false;
+                for (const auto& h : rows[mirror(ii)])
+                    if (h.first == mirror(g.first) && h.second == g.second) found = true;
+                if (!found) return false;
+            }
+        return true;
+    }
+
     // Device state of the emitter objects: FP64 density matrices (one per cell and
     // ensemble member) initialised to the member weight in rho[0], four zeroed derivative
     // slots, the P boxes, and the constants of the plan.
@@ -607,6 +632,7 @@ private:
                 col.push_back(0);
                 val.push_back(0.0);
             }
+            e.herm = hermitianForm(ep) ? 1 : 0;
             e.gamRow = mem_.upload(row);
             e.gamCol = mem_.upload(col);
             e.gamVal = mem_.upload(val);
@@ -1151,7 +1177,7 @@ public:
         std::vector<dev::DftJob<T>> dft;
         std::vector<dev::EmitJob<T>> em;
         std::vector<int*> steps;
-        std::vector<int2> passW, p2W[2], lorW, odW, srcW, recW, smpW, foldW, addW, updW[4];
+        std::vector<int2> passW, p2W[2], lorW, odW, srcW, recW, smpW, foldW, addW, updW[7];
         auto add = [](std::vector<int2>& w, int job, long long blocks) {
             for (long long b = 0; b < blocks; ++b) w.push_back(make_int2(job, static_cast<int>(b)));
         };
@@ -1197,7 +1223,7 @@ public:
                 for (int c = 0; c < 3; ++c)
                     if (e.comp[c])
                         for (int b = 0; b < bpc; ++b) addW.push_back(make_int2(q, c * bpc + b));
-                add(updW[dev::emitter_level_group(e.N)], q, dev::emitter_update_blocks(e));
+                add(updW[dev::emitter_level_group(e.N, e.herm != 0)], q, dev::emitter_update_blocks(e));
                 dev::EmitJob<T> jb{};
                 jb.e = e;
                 for (int c = 0; c < 3; ++c) jb.f[c] = m->fields().f[c];
@@ -1229,7 +1255,7 @@ public:
         smpMap_ = map(smpW);
         foldMap_ = map(foldW);
         addMap_ = map(addW);
-        for (int g = 0; g < 4; ++g) updMap_[g] = map(updW[g]);
+        for (int g = 0; g < 7; ++g) updMap_[g] = map(updW[g]);
         ck(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
     }
     ~PackedBatch() {
@@ -1273,7 +1299,7 @@ private:
     int nEm_ = 0;
     int** dSteps_ = nullptr;
     int nSteps_ = 0;
-    dev::WorkMap passMap_{}, p2Map_[2]{}, lorMap_{}, odMap_{}, srcMap_{}, recMap_{}, smpMap_{}, foldMap_{}, addMap_{}, updMap_[4]{};
+    dev::WorkMap passMap_{}, p2Map_[2]{}, lorMap_{}, odMap_{}, srcMap_{}, recMap_{}, smpMap_{}, foldMap_{}, addMap_{}, updMap_[7]{};
 
     void enqueueStep() {
         void* s = stream_;

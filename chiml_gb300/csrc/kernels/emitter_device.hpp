@@ -26,6 +26,9 @@ struct EmitterDev {
     const int* gamCol;
     const double* gamVal;
     double dt, hbar, na;
+    // Hermitian form: real symmetric dipole operators and a relaxation that maps element
+    // pairs onto conjugate pairs; the update then needs only the upper triangle
+    int herm;
     // ABM4 step weights (predictor 55, -59, 37, -9; corrector 9, 19, -5, 1, each x dt/24)
     // and 1/hbar, formed once on the host: FP64 division is slow on this GPU
     double abP[4], abC[4], invHbar;
@@ -60,8 +63,9 @@ template <typename T>
 void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream);
 
 // The same step for the emitter objects of many simulations (the batched sweep): the
-// addP launch and one density-update launch per level-count group (2, 3, 4 levels,
-// other), each over the packed blocks of its jobs, then one reduce block per job.
+// addP launch and one density-update launch per group (general form for 2, 3, 4 levels
+// and other; Hermitian form for 2, 3, 4 levels), each over the packed blocks of its jobs,
+// then one reduce block per job.
 template <typename T>
 struct EmitJob {
     EmitterDev e;
@@ -73,9 +77,9 @@ __host__ __device__ inline int emitter_addp_blocks_per_comp(const EmitterDev& e)
     return (e.addN[0] * e.addN[1] * e.addN[2] + 255) / 256;
 }
 int emitter_update_blocks(const EmitterDev& e);
-int emitter_level_group(int N);                          // update group of an N-level emitter
+int emitter_level_group(int N, bool herm);               // update group: 0..3 general (N = 2, 3, 4, other), 4..6 Hermitian (N = 2, 3, 4)
 template <typename T>
-void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[4], void* stream);
+void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[7], void* stream);
 
 }  // namespace dev
 }  // namespace chiml

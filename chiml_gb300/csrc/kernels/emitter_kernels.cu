@@ -145,8 +145,161 @@ __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex,
     addpRange(e, Ex, Ey, Ez, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
+// ---- Hermitian form (EmitterDev::herm) ----
+// With real symmetric dipole operators and a relaxation that maps every element pair
+// (r, c), (c, r) onto conjugate pairs, the reference's density matrices stay Hermitian and
+// H = h0 - E . mu is real symmetric. The step then needs only the upper triangle: the
+// diagonal is real, (c, r) = conj (r, c). Element (r, c) has storage index r + c N.
+
+// Upper-triangle derivative: out(r, c) = t(r, c) + conj t(c, r) for r < c, and the real
+// diagonal t(r, r) + conj t(r, r) = 2 Re t(r, r); t = (i/hbar) H den, H real.
+template <int NT>
+__device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, double invHbar, const double* H, const C2* den,
+                                               C2* out) {
+#pragma unroll
+    for (int i = 0; i < NT; ++i) {
+        // Re t(i, i) = -Im(sum_l H(i, l) den(l, i)) / hbar
+        double sy = 0.0;
+#pragma unroll
+        for (int l = 0; l < NT; ++l) sy = fma(H[i + l * NT], den[l + i * NT].y, sy);
+        const double tx = -invHbar * sy;
+        out[i + i * NT] = C2{tx + tx, 0.0};
+#pragma unroll
+        for (int j = i + 1; j < NT; ++j) {
+            C2 sij = c2(0.0, 0.0), sji = c2(0.0, 0.0);
+#pragma unroll
+            for (int l = 0; l < NT; ++l) {
+                sij.x = fma(H[i + l * NT], den[l + j * NT].x, sij.x);
+                sij.y = fma(H[i + l * NT], den[l + j * NT].y, sij.y);
+                sji.x = fma(H[j + l * NT], den[l + i * NT].x, sji.x);
+                sji.y = fma(H[j + l * NT], den[l + i * NT].y, sji.y);
+            }
+            const C2 tij = C2{-invHbar * sij.y, invHbar * sij.x};
+            const C2 tji = C2{-invHbar * sji.y, invHbar * sji.x};
+            out[i + j * NT] = cadd(tij, cconj(tji));
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < NT * NT; ++ii) {
+        if ((ii % NT) > (ii / NT)) continue;  // lower triangle: the conjugate of its mirror
+        for (int p = e.gamRow[ii]; p < e.gamRow[ii + 1]; ++p) {
+            const C2 d = pick<NT>(den, e.gamCol[p]);
+            const double g = e.gamVal[p];
+            out[ii] = C2{fma(d.x, g, out[ii].x), (ii % NT) == (ii / NT) ? 0.0 : fma(d.y, g, out[ii].y)};
+        }
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void mirrorLower(C2* a) {
+#pragma unroll
+    for (int r = 0; r < NT; ++r)
+#pragma unroll
+        for (int c = r + 1; c < NT; ++c) a[c + r * NT] = cconj(a[r + c * NT]);
+}
+
+// One ensemble member of one cell in the Hermitian form: loads and stores the upper
+// triangle only (the diagonal's real part), about half the FP64 work and bytes of the
+// general form.
+template <int NT>
+__device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[3], bool zeroE, int m, long long base,
+                                           const double2* __restrict__ k0, const double2* __restrict__ k1,
+                                           const double2* __restrict__ k2, double2* __restrict__ k3, bool popStep,
+                                           C2* popAcc, double* Pc) {
+    constexpr int N2 = NT * NT;
+    const double c55 = e.abP[0], cm59 = e.abP[1], c37 = e.abP[2], cm9 = e.abP[3];
+    const double c9 = e.abC[0], c19 = e.abC[1], cm5 = e.abC[2], c1 = e.abC[3];
+    double H[N2];
+#pragma unroll
+    for (int i = 0; i < N2; ++i) H[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < NT; ++i) H[i * NT + i] = e.h0[m * NT + i];
+    if (!zeroE)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (e.addMu[c])
+#pragma unroll
+                for (int i = 0; i < N2; ++i) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
+    const double* rhoD = reinterpret_cast<const double*>(e.rho);
+    C2 a[N2], b[N2], r0[N2];
+    // predictor on the upper triangle
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) {
+                const double rr = rhoD[2 * o];
+                double p = fma(c55, reinterpret_cast<const double*>(k0)[2 * o], rr);
+                p = fma(cm59, reinterpret_cast<const double*>(k1)[2 * o], p);
+                p = fma(c37, reinterpret_cast<const double*>(k2)[2 * o], p);
+                p = fma(cm9, reinterpret_cast<const double*>(k3)[2 * o], p);
+                r0[i] = C2{rr, 0.0};
+                a[i] = C2{p, 0.0};
+            } else {
+                const C2 rr = ld(&e.rho[o]);
+                C2 p = caxpy(c55, ld(&k0[o]), rr);
+                p = caxpy(cm59, ld(&k1[o]), p);
+                p = caxpy(c37, ld(&k2[o]), p);
+                p = caxpy(cm9, ld(&k3[o]), p);
+                r0[i] = rr;
+                a[i] = p;
+            }
+        }
+    mirrorLower<NT>(a);
+    den_deriv_herm<NT>(e, e.invHbar, H, a, b);
+    // corrector
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) {
+                double v = fma(c9, b[i].x, r0[i].x);
+                v = fma(c19, reinterpret_cast<const double*>(k0)[2 * o], v);
+                v = fma(cm5, reinterpret_cast<const double*>(k1)[2 * o], v);
+                v = fma(c1, reinterpret_cast<const double*>(k2)[2 * o], v);
+                a[i] = C2{v, 0.0};
+                reinterpret_cast<double*>(e.rho)[2 * o] = v;
+            } else {
+                C2 v = caxpy(c9, b[i], r0[i]);
+                v = caxpy(c19, ld(&k0[o]), v);
+                v = caxpy(cm5, ld(&k1[o]), v);
+                v = caxpy(c1, ld(&k2[o]), v);
+                a[i] = v;
+                st(&e.rho[o], v);
+            }
+        }
+    mirrorLower<NT>(a);
+    den_deriv_herm<NT>(e, e.invHbar, H, a, b);  // derivative at the new density: the next k_n
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) reinterpret_cast<double*>(k3)[2 * o] = b[i].x;
+            else st(&k3[o], b[i]);
+        }
+    if (popStep)
+#pragma unroll
+        for (int d = 0; d < kMaxDtc; ++d)
+            if (d < e.nDtc) popAcc[d] = cadd(popAcc[d], pick<NT>(a, e.dtcLev[d]));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (!e.comp[c]) continue;
+        // Re(conj(a) . mu) with mu real
+        double sdot = 0.0;
+#pragma unroll
+        for (int i = 0; i < N2; ++i) sdot = fma(a[i].x, e.mu[c * N2 + i].x, sdot);
+        Pc[c] += e.na * sdot;
+    }
+}
+
 // Block `blk` of the density update (cells kEmThreads * blk ...), writing partial row blk.
-template <typename T, int NT>
+template <typename T, int NT, bool HERM = false>
 __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __restrict__ Ex, const T* __restrict__ Ey,
                                             const T* __restrict__ Ez, const int* __restrict__ stepPtr, int blk) {
     constexpr int MAXN2 = (NT ? NT * NT : kMaxEmitterLevels * kMaxEmitterLevels);
@@ -180,6 +333,11 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         const double2* __restrict__ k1 = e.kd + s1 * slotStride;
         const double2* __restrict__ k2 = e.kd + s2 * slotStride;
         double2* __restrict__ k3 = e.kd + s3 * slotStride;
+        if constexpr (HERM) {
+            for (int m = 0; m < e.nm; ++m)
+                memberHerm<NT>(e, Ec, zeroE, m, static_cast<long long>(m) * n2 * e.nc + q, k0, k1, k2, k3, popStep, popAcc,
+                               Pc);
+        } else {
         C2 H[MAXN2], a[MAXN2], b[MAXN2];
         for (int m = 0; m < e.nm; ++m) {
             // Hamiltonian::getHam
@@ -260,6 +418,7 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
                 Pc[c] += e.na * sdot;
             }
         }
+        }
 #pragma unroll
         for (int c = 0; c < 3; ++c)
             if (e.comp[c]) e.P[static_cast<long long>(c) * e.pBox + e.cellP[q]] = Pc[c];
@@ -283,11 +442,11 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         }
 }
 
-template <typename T, int NT>
+template <typename T, int NT, bool HERM = false>
 __global__ void __launch_bounds__(kEmThreads) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
                                                                const T* __restrict__ Ey, const T* __restrict__ Ez,
                                                                const int* __restrict__ stepPtr) {
-    updateBlock<T, NT>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
+    updateBlock<T, NT, HERM>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
 }
 
 __device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __restrict__ stepPtr) {
@@ -342,12 +501,12 @@ __global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* _
     addpRange(j.e, j.f[0], j.f[1], j.f[2], c, b * 256 + static_cast<int>(threadIdx.x), bpc * 256);
 }
 
-template <typename T, int NT>
+template <typename T, int NT, bool HERM = false>
 __global__ void __launch_bounds__(kEmThreads) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
                                                                       const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const EmitJob<T>& j = jobs[w.x];
-    updateBlock<T, NT>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
+    updateBlock<T, NT, HERM>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
 }
 
 template <typename T>
@@ -359,10 +518,13 @@ __global__ void __launch_bounds__(256) k_emitter_reduce_packed(const EmitJob<T>*
 }  // namespace
 
 int emitter_update_blocks(const EmitterDev& e) { return (e.nc + kEmThreads - 1) / kEmThreads; }
-int emitter_level_group(int N) { return N == 2 ? 0 : (N == 3 ? 1 : (N == 4 ? 2 : 3)); }
+int emitter_level_group(int N, bool herm) {
+    if (herm && N >= 2 && N <= 4) return 2 + N;  // 4, 5, 6: the Hermitian form
+    return N == 2 ? 0 : (N == 3 ? 1 : (N == 4 ? 2 : 3));
+}
 
 template <typename T>
-void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[4], void* stream) {
+void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[7], void* stream) {
     if (njobs <= 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (addp.blocks > 0) k_emitter_addp_packed<T><<<addp.blocks, 256, 0, s>>>(jobs, addp.work);
@@ -370,11 +532,17 @@ void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, cons
     if (update[1].blocks > 0) k_emitter_update_packed<T, 3><<<update[1].blocks, kEmThreads, 0, s>>>(jobs, update[1].work);
     if (update[2].blocks > 0) k_emitter_update_packed<T, 4><<<update[2].blocks, kEmThreads, 0, s>>>(jobs, update[2].work);
     if (update[3].blocks > 0) k_emitter_update_packed<T, 0><<<update[3].blocks, kEmThreads, 0, s>>>(jobs, update[3].work);
+    if (update[4].blocks > 0)
+        k_emitter_update_packed<T, 2, true><<<update[4].blocks, kEmThreads, 0, s>>>(jobs, update[4].work);
+    if (update[5].blocks > 0)
+        k_emitter_update_packed<T, 3, true><<<update[5].blocks, kEmThreads, 0, s>>>(jobs, update[5].work);
+    if (update[6].blocks > 0)
+        k_emitter_update_packed<T, 4, true><<<update[6].blocks, kEmThreads, 0, s>>>(jobs, update[6].work);
     k_emitter_reduce_packed<T><<<njobs, 256, 0, s>>>(jobs);
 }
 
-template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[4], void*);
-template void launch_emitter_packed<double>(const EmitJob<double>*, int, WorkMap, const WorkMap[4], void*);
+template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[7], void*);
+template void launch_emitter_packed<double>(const EmitJob<double>*, int, WorkMap, const WorkMap[7], void*);
 
 template <typename T>
 void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream) {
@@ -382,7 +550,11 @@ void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* ste
     dim3 ga(emitter_addp_blocks_per_comp(e), 3);
     k_emitter_addp<T><<<ga, 256, 0, s>>>(e, fields[0], fields[1], fields[2]);
     const int blocks = (e.nc + kEmThreads - 1) / kEmThreads;
-    switch (e.N) {
+    if (e.herm && e.N >= 2 && e.N <= 4) {
+        if (e.N == 2) k_emitter_update<T, 2, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        else if (e.N == 3) k_emitter_update<T, 3, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        else k_emitter_update<T, 4, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+    } else switch (e.N) {
         case 2: k_emitter_update<T, 2><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
         case 3: k_emitter_update<T, 3><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
         case 4: k_emitter_update<T, 4><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
