@@ -633,6 +633,15 @@ private:
                 val.push_back(0.0);
             }
             e.herm = hermitianForm(ep) ? 1 : 0;
+            // H = h0 - E . mu: the diagonal and the nonzero elements of the coupled operators
+            e.hmask = 0;
+            for (int i = 0; i < n2 && i < 32; ++i) {
+                bool nz = (i % N) == (i / N);
+                for (int c = 0; c < 3; ++c)
+                    if (ep.addMu[c] && ep.negMu[c][i] != std::complex<double>(0.0, 0.0)) nz = true;
+                if (nz) e.hmask |= 1u << i;
+            }
+            if (n2 > 32) e.herm = 0;
             e.gamRow = mem_.upload(row);
             e.gamCol = mem_.upload(col);
             e.gamVal = mem_.upload(val);

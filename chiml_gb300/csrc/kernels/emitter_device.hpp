@@ -29,6 +29,7 @@ struct EmitterDev {
     // Hermitian form: real symmetric dipole operators and a relaxation that maps element
     // pairs onto conjugate pairs; the update then needs only the upper triangle
     int herm;
+    unsigned hmask;               // Hermitian form: elements of H that can be nonzero (bit i, i < 32)
     // ABM4 step weights (predictor 55, -59, 37, -9; corrector 9, 19, -5, 1, each x dt/24)
     // and 1/hbar, formed once on the host: FP64 division is slow on this GPU
     double abP[4], abC[4], invHbar;

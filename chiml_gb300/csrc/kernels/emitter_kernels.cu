@@ -153,15 +153,19 @@ __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex,
 
 // Upper-triangle derivative: out(r, c) = t(r, c) + conj t(c, r) for r < c, and the real
 // diagonal t(r, r) + conj t(r, r) = 2 Re t(r, r); t = (i/hbar) H den, H real.
+// hmask: bit i set when element i of H can be nonzero (the diagonal, and wherever a coupled
+// dipole operator is nonzero); products with the other elements are exact zeros and are
+// skipped (the branch is uniform over the emitter). The diagonal of den is real.
 template <int NT>
 __device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, double invHbar, const double* H, const C2* den,
-                                               C2* out) {
+                                               C2* out, unsigned hmask) {
 #pragma unroll
     for (int i = 0; i < NT; ++i) {
-        // Re t(i, i) = -Im(sum_l H(i, l) den(l, i)) / hbar
+        // Re t(i, i) = -Im(sum_l H(i, l) den(l, i)) / hbar; den(i, i) is real
         double sy = 0.0;
 #pragma unroll
-        for (int l = 0; l < NT; ++l) sy = fma(H[i + l * NT], den[l + i * NT].y, sy);
+        for (int l = 0; l < NT; ++l)
+            if (l != i && (hmask >> (i + l * NT) & 1u)) sy = fma(H[i + l * NT], den[l + i * NT].y, sy);
         const double tx = -invHbar * sy;
         out[i + i * NT] = C2{tx + tx, 0.0};
 #pragma unroll
@@ -169,10 +173,14 @@ __device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, double invHb
             C2 sij = c2(0.0, 0.0), sji = c2(0.0, 0.0);
 #pragma unroll
             for (int l = 0; l < NT; ++l) {
-                sij.x = fma(H[i + l * NT], den[l + j * NT].x, sij.x);
-                sij.y = fma(H[i + l * NT], den[l + j * NT].y, sij.y);
-                sji.x = fma(H[j + l * NT], den[l + i * NT].x, sji.x);
-                sji.y = fma(H[j + l * NT], den[l + i * NT].y, sji.y);
+                if (hmask >> (i + l * NT) & 1u) {
+                    sij.x = fma(H[i + l * NT], den[l + j * NT].x, sij.x);
+                    if (l != j) sij.y = fma(H[i + l * NT], den[l + j * NT].y, sij.y);
+                }
+                if (hmask >> (j + l * NT) & 1u) {
+                    sji.x = fma(H[j + l * NT], den[l + i * NT].x, sji.x);
+                    if (l != i) sji.y = fma(H[j + l * NT], den[l + i * NT].y, sji.y);
+                }
             }
             const C2 tij = C2{-invHbar * sij.y, invHbar * sij.x};
             const C2 tji = C2{-invHbar * sji.y, invHbar * sji.x};
@@ -219,7 +227,8 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
         for (int c = 0; c < 3; ++c)
             if (e.addMu[c])
 #pragma unroll
-                for (int i = 0; i < N2; ++i) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
+                for (int i = 0; i < N2; ++i)
+                    if (e.hmask >> i & 1u) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
     const double* rhoD = reinterpret_cast<const double*>(e.rho);
     C2 a[N2], b[N2], r0[N2];
     // predictor on the upper triangle
@@ -248,7 +257,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             }
         }
     mirrorLower<NT>(a);
-    den_deriv_herm<NT>(e, e.invHbar, H, a, b);
+    den_deriv_herm<NT>(e, e.invHbar, H, a, b, e.hmask);
     // corrector
 #pragma unroll
     for (int c = 0; c < NT; ++c)
@@ -273,7 +282,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             }
         }
     mirrorLower<NT>(a);
-    den_deriv_herm<NT>(e, e.invHbar, H, a, b);  // derivative at the new density: the next k_n
+    den_deriv_herm<NT>(e, e.invHbar, H, a, b, e.hmask);  // derivative at the new density: the next k_n
 #pragma unroll
     for (int c = 0; c < NT; ++c)
 #pragma unroll
