@@ -495,11 +495,58 @@ private:
             t.pulseTab = mem_.upload(tab);
             t.rec = mem_.alloc<double2>(6 * 2 * (static_cast<std::size_t>(P.nSteps) + 1));
             const std::vector<TfsfCellAdds>* adds[2] = {&tp.addH, &tp.addE};
+            const std::vector<TfsfSegment>* segs[2] = {&tp.segH, &tp.segE};
             for (int w = 0; w < 2; ++w) {
+                // rows split into runs of single-term cells; the cells with several terms
+                // (face edges) go to the per-cell list
+                std::vector<long long> keys;
+                long long nTerms = 0;
+                for (const TfsfSegment& g : *segs[w])
+                    for (int r = 0; r < g.n; ++r) keys.push_back(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride);
+                nTerms = static_cast<long long>(keys.size());
+                std::sort(keys.begin(), keys.end());
+                auto multi = [&](long long key) {
+                    auto lo = std::lower_bound(keys.begin(), keys.end(), key);
+                    return (lo + 1) != keys.end() && *(lo + 1) == key;
+                };
+                std::vector<dev::TfsfSegDev> sd;
+                std::vector<int2> sw;
+                for (const TfsfSegment& g : *segs[w]) {
+                    int r = 0;
+                    while (r < g.n) {
+                        while (r < g.n && multi(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride)) ++r;
+                        const int r0 = r;
+                        while (r < g.n && !multi(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride)) ++r;
+                        if (r == r0) continue;
+                        dev::TfsfSegDev d{};
+                        d.cell0 = g.cell0 + r0 * g.cellStride;
+                        d.cellStride = g.cellStride;
+                        d.incd0 = g.incd0 + r0 * g.incdStride;
+                        d.incdStride = g.incdStride;
+                        d.n = r - r0;
+                        d.line = g.line;
+                        d.comp = g.comp;
+                        d.pref = g.pref;
+                        const long long lastCell = d.cell0 + static_cast<long long>(d.n - 1) * d.cellStride;
+                        const long long lastIncd = d.incd0 + static_cast<long long>(d.n - 1) * d.incdStride;
+                        if (d.cell0 < 0 || lastCell >= P.dims.cells() || d.incd0 < 0 || lastIncd >= tp.gridLen || d.cellStride < 0 ||
+                            d.incdStride < 0 || !tp.line[d.line].present || !P.comp[d.comp].present)
+                            throw InputError("TFSF surface row outside its grids");
+                        for (int c = 0; c * dev::kTfsfRowChunk < d.n; ++c) sw.push_back(make_int2(static_cast<int>(sd.size()), c));
+                        sd.push_back(d);
+                    }
+                }
+                t.seg[w] = mem_.upload(sd);
+                t.segWork[w] = mem_.upload(sw);
+                t.segBlocks[w] = static_cast<int>(sw.size());
                 std::vector<long long> cell;
                 std::vector<int> comp, start, tl, ti;
                 std::vector<double> pref;
+                long long listed = 0;
+                for (const TfsfCellAdds& a : *adds[w]) listed += static_cast<long long>(a.line.size());
+                if (listed != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
                 for (const TfsfCellAdds& a : *adds[w]) {
+                    if (a.line.size() < 2) continue;  // in a row
                     cell.push_back(a.cell);
                     comp.push_back(a.comp);
                     start.push_back(static_cast<int>(tl.size()));

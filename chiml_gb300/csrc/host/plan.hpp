@@ -220,6 +220,14 @@ struct TfsfCellAdds {
     std::vector<uint8_t> toD;
 };
 
+// One row of one surface (a daxpy of addIncdFields): cell cell0 + r * cellStride of
+// component comp gets pref * Re(line[incd0 + r * incdStride]), r < n.
+struct TfsfSegment {
+    long long cell0 = 0, cellStride = 0;
+    int incd0 = 0, incdStride = 0, n = 0, line = 0, comp = 0;
+    double pref = 0.0;
+};
+
 struct TfsfPlan {
     int gridLen = 0, pulseLen = 0, mTot = 0, mMax = 0, pmlThick = 0, pulAddStart = 0;
     std::array<int, 3> m = {0, 0, 0};
@@ -227,6 +235,7 @@ struct TfsfPlan {
     TfsfLine line[6];
     std::vector<PulseSpec> pulses;
     std::vector<TfsfCellAdds> addH, addE;  // applied before and after the 1-D step
+    std::vector<TfsfSegment> segH, segE;   // the same corrections as surface rows
 };
 
 struct Plan {

@@ -35,6 +35,7 @@ struct TfsfBuilder {
     int mTot = 0, mMax = 0, gridLen = 0, pmlThick = 0, quadrant = 0, mInd = -1;
     double theta = 0, phi = 0, psi = 0, alpha = 0, phiP = 0, psiP = 0, dr = -1;
     bool present[6] = {false, false, false, false, false, false};
+    std::vector<TfsfSegment>* segs = nullptr;  // where genSurface records its rows
 
     TfsfBuilder(const Inputs& i, const Dims& dd, double dtt, const TfsfSpec& tt, const std::vector<int>* const* ph, TfsfPlan& tp)
         : in(i), D(dd), dt(dtt), d(i.d), t(tt), phys(ph), T(tp) {}
@@ -147,8 +148,11 @@ struct TfsfBuilder {
         // surfaces (parallelTFSF.hpp:332-340)
         const bool pl = (theta == 0 || ((theta == M_PI / 2.0 && std::abs(quadrant) == 4) || std::abs(quadrant) == 1)) ? false : true;
         std::vector<SurfaceTerm> hTerms, eTerms;
+        segs = &T.segH;
         for (int i = 0; i < 3; ++i) addStructs(3 + i, false, pl, hTerms);
+        segs = &T.segE;
         for (int i = 0; i < 3; ++i) addStructs(i, true, pl, eTerms);
+        segs = nullptr;
         gather(hTerms, T.addH);
         gather(eTerms, T.addE);
         // the lines' CPMLs (parallelTFSF.hpp:342-378)
@@ -427,9 +431,22 @@ struct TfsfBuilder {
             mOffSet -= m[cor];
         const int mOff = static_cast<int>(std::floor(mOffSet - mOffHalf));
         const int ir = std::abs(m[0] * locRelOr[0]) + std::abs(m[1] * locRelOr[1]) + std::abs(m[2] * locRelOr[2]);
+        const long long cellStride = addVec1[0] + static_cast<long long>(D.lx) * (addVec1[2] + static_cast<long long>(D.lz) * addVec1[1]);
         for (int ll = 0; ll < sz1; ++ll) {
             // one run per row: the line material is uniform (vacuum), no poles: the U list
             const int incdStart = ir + pmlThick + mOff + 6 * mTot + ll * addIncdProp;
+            if (segs && sz0Max > 0) {
+                TfsfSegment sg;
+                sg.cell0 = D.idx(locTemp[0] + ll * addVec2[0], locTemp[1] + ll * addVec2[1], locTemp[2] + ll * addVec2[2]);
+                sg.cellStride = cellStride;
+                sg.incd0 = incdStart;
+                sg.incdStride = strideIncd;
+                sg.n = sz0Max;
+                sg.line = polIncd;
+                sg.comp = pol;
+                sg.pref = prefactor;
+                segs->push_back(sg);
+            }
             for (int s0 = 0; s0 < sz0Max; ++s0) {
                 const int x = locTemp[0] + ll * addVec2[0] + s0 * addVec1[0];
                 const int y = locTemp[1] + ll * addVec2[1] + s0 * addVec1[1];

@@ -9,6 +9,7 @@ namespace chiml {
 namespace dev {
 
 constexpr int kTfsfMaxPsi = 4;
+constexpr int kTfsfRowChunk = 256;  // cells of a correction row per block (the block size)
 
 // The single run of a vacuum line: U[indI + r] += pj (J[posK + r] - J[negK + r])
 // + pk (K[posJ + r] - K[negJ + r]) for r < n.
@@ -41,13 +42,25 @@ struct TfsfLineDev {
     int recIdx, recOffIdx;
 };
 
+struct TfsfSegDev {
+    long long cell0, cellStride;
+    int incd0, incdStride, n, line, comp;
+    double pref;
+};
+
 struct TfsfDev {
     int gridLen, pulseLen, mTot, pulAddStart, nSteps;
     TfsfLineDev line[6];       // 0..2 Ex..Ez, 3..5 Hx..Hz
     const double2* pulseTab;   // [step][line][mTot]: sum of the pulses at the line's pulse points
     double2* rec;              // [line][2 (nSteps + 1)]: recorded incident values (flux normalisation)
-    // surface corrections, per cell (CSR over the terms): F[comp][cell] += pref * Re(line[incd])
-    int nCell[2];              // [0] H corrections, [1] E corrections
+    // surface corrections: rows of cells that get one term each (the bulk of every face),
+    // one block per 256 cells of a row: F[comp][cell0 + r s] += pref * Re(line[incd0 + r t])
+    const TfsfSegDev* seg[2];  // [0] H corrections, [1] E corrections
+    const int2* segWork[2];    // per block: {row, chunk of 256 cells}
+    int segBlocks[2];
+    // cells that get several terms (face edges), per cell (CSR over the terms, in the
+    // reference's order): F[comp][cell] += pref * Re(line[incd])
+    int nCell[2];
     const long long* cell[2];
     const int* comp[2];
     const int* start[2];       // [nCell + 1]

@@ -9,9 +9,10 @@
 //                 adds the E corrections (from the new H lines). Every line element is
 //                 updated by one thread in the reference's per-element order (pulse add,
 //                 J and K curl terms, then each CPML psi list touching it): a half only
-//                 reads lines of the other kind, so its elements are independent. Each
-//                 corrected main-grid cell is one thread that adds its terms in the
-//                 reference's order: F += pref * Re(incident line value).
+//                 reads lines of the other kind, so its elements are independent. The
+//                 corrections: face rows of cells with one term each, one thread per cell
+//                 along the row; cells on face edges (several terms) one thread each,
+//                 adding their terms in the reference's order: F += pref * Re(line value).
 //   k_tfsf_record the incident values recorded for flux normalisation.
 // The lines are complex FP64 in both precision forms (a few thousand points).
 #include "tfsf_device.hpp"
@@ -87,7 +88,7 @@ __device__ __forceinline__ void lineAny(const TfsfDev& t, int c0, int e, int s) 
     else lineElement(t, c, true, x - t.gridLen, s);
 }
 
-constexpr int kTfsfThreads = 256;
+constexpr int kTfsfThreads = kTfsfRowChunk;
 
 // One half of the TFSF step: blocks [0, lineBlocks) step the lines of kind c0 (3: H,
 // 0: E), the other blocks add the corrections of list `which` (0: H corrections, from
@@ -98,12 +99,24 @@ __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int
                                                             T* F2, T* F3, T* F4, T* F5, const int* __restrict__ step) {
     const int s = *step;
     if (s >= t.nSteps) return;
-    if (static_cast<int>(blockIdx.x) < lineBlocks) {
-        lineAny(t, c0, blockIdx.x * kTfsfThreads + threadIdx.x, s);
-    } else {
-        T* const F[6] = {F0, F1, F2, F3, F4, F5};
-        addCell(t, which, (blockIdx.x - lineBlocks) * kTfsfThreads + threadIdx.x, F);
+    const int b = static_cast<int>(blockIdx.x);
+    if (b < lineBlocks) {
+        lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
+        return;
     }
+    T* const F[6] = {F0, F1, F2, F3, F4, F5};
+    const int sb = b - lineBlocks;
+    if (sb < t.segBlocks[which]) {
+        const int2 w = t.segWork[which][sb];
+        const TfsfSegDev& g = t.seg[which][w.x];
+        const int r = w.y * kTfsfThreads + static_cast<int>(threadIdx.x);
+        if (r >= g.n) return;
+        T* f = F[g.comp];
+        const long long cell = g.cell0 + r * g.cellStride;
+        f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * t.line[g.line].U[g.incd0 + r * g.incdStride].x);
+        return;
+    }
+    addCell(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
 }
 
 // Incident records after the step: E values of this step and the H values the next step
@@ -128,7 +141,7 @@ void launch_tfsf_step(const TfsfDev& t, T* const fields[6], const int* step, voi
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int lineBlocks = (3 * (t.gridLen + t.pulseLen) + kTfsfThreads - 1) / kTfsfThreads;
     for (int half = 0; half < 2; ++half) {
-        const int addBlocks = (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
+        const int addBlocks = t.segBlocks[half] + (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
         k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, fields[0], fields[1],
                                                                         fields[2], fields[3], fields[4], fields[5], step);
     }
