@@ -983,11 +983,10 @@ private:
                         if (base != 0.0 || k.kflag[t] || (psiUpd && k.npsi[t])) write = true;
                     }
                     if (k.lor && lorHasPoles(k)) o.flags |= dev::kFcLor;
-                    if (k.lor && !lorHasPoles(k)) {
-                        o.flags |= dev::kFcDtoE;
-                        o.epsInv = static_cast<T>(1.0 / k.eps);
-                    }
+                    if (k.lor && !lorHasPoles(k)) o.flags |= dev::kFcDtoE;
                     if (k.ordip) o.flags |= dev::kFcOrDip;
+                    o.epsInv = static_cast<T>(1.0 / k.eps);
+                    o.obj = static_cast<uint32_t>(k.obj < 0 ? 0x7fffffff : k.obj);
                     if (k.toD) o.flags |= dev::kFcToD;
                     if (write) o.flags |= dev::kFcWrite;
                 }
@@ -1019,7 +1018,7 @@ private:
             }
             setSlabsAndForm(pass, half == 1);
             if (half == 1) uploadOrDip(pass);
-            if (half == 1 && (pass.interior3d || pass.interior2d)) {
+            if (half == 1 && (pass.interior3d || pass.interior2d) && !dev::kInlineDispersive<T>) {
                 // dispersive cells leave the interior form for their own list kernel
                 std::vector<int> lc;
                 std::vector<long long> li;

@@ -198,6 +198,50 @@ constexpr int kMarchUnroll = CHIML_MARCH_UNROLL;  // planes of the march unrolle
 
 __device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
 
+// The dispersive part of one E-pass cell of the FP32 interior form, with cellGeneric's
+// arithmetic: the Lorentz ADE from E^n (u), D += curl, then D -> E with the pole sum
+// (UpdateLorPol, DtoU, orDipDtoU: UTIL/FDTD_up_eq.cpp:425-448, 838-875). -1/eps_inf and
+// -0.5/eps_inf are exact scalings of the class's 1/eps_inf.
+template <typename T>
+__device__ __forceinline__ void dispersiveCell(const Pass<T>& p, int ci, uint32_t fl, int obj, T epsInv, long long i, T u,
+                                               T add, bool write) {
+    const Comp<T>& c = p.c[ci];
+    if (fl & kFcLor) {
+        if (obj < 0 || obj >= p.nObj || p.poleCount[obj] > c.nPoles) {
+            atomicOr(p.err, kErrPoleCount);
+            return;
+        }
+        const int s = p.poleStart[obj];
+        const int n = p.poleCount[obj];
+        for (int q = 0; q < n; ++q) {
+            const T old = c.P[q][i];
+            T np = p.alpha[s + q] * old;
+            np += p.xi[s + q] * c.Pprev[q][i];
+            np += p.gamma[s + q] * u;
+            c.P[q][i] = np;
+            c.Pprev[q][i] = old;
+        }
+    }
+    T d = c.D[i];
+    if (write) {
+        d += add;
+        c.D[i] = d;
+    }
+    T e = d * epsInv;
+    if (fl & kFcLor) {
+        const T ne = -epsInv;
+        for (int q = 0; q < c.nPoles; ++q) e += ne * c.P[q][i];
+    } else {
+        const T oc = T(-0.5) * epsInv;
+        const long long o = p.od.off[ci];
+        for (int q = 0; q < p.od.nPoles; ++q) {
+            e += oc * p.od.P[ci][q][i];
+            e += oc * p.od.P[ci][q][i + o];
+        }
+    }
+    c.U[i] = e;
+}
+
 // D2: a 2-D grid (lz == 1), where the term along z is absent.
 template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false>
 __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1) {
@@ -309,7 +353,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
         const FastClass<T>* kc = c.fcls + cd;
         const T coef0 = kc->coef[0], coef1 = kc->coef[1];
         const uint32_t fl = kc->flags;
-        if (EPASS && (fl & (kFcLor | kFcOrDip))) continue;  // dispersive cells run in k_pass_lorentz
+        if (EPASS && !kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) continue;  // run by k_pass_lorentz
         if (((fl & kFcSlab0) && !in[0]) || ((fl & kFcSlab1) && !in[1])) {
             atomicOr(p.err, kErrSlab);
             continue;
@@ -333,7 +377,9 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
             if (P0) add += coef0 * (g[0] - n[0]);
             if (P1) add += coef1 * (g[1] - n[1]);
         }
-        if (EPASS && (fl & kFcDtoE)) {
+        if (EPASS && kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) {
+            dispersiveCell<T>(p, CI, fl, static_cast<int>(kc->obj), kc->epsInv, i, u, add, (fl & kFcWrite) != 0);
+        } else if (EPASS && (fl & kFcDtoE)) {
             // D -> E without poles: E = D / eps_inf (the P sum of cellGeneric adds zeros)
             T d = Dd[i];
             if (fl & kFcWrite) {
@@ -442,13 +488,13 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
         } else {
             launch_pass3d<T, int, 16, 2>(p, ePass, s);
         }
-        if (ePass && p.nLor > 0)
+        if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else if (p.interior2d) {
         dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
         if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
         else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
-        if (ePass && p.nLor > 0)
+        if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else {
         // 2-D grids, and 3-D grids with updated halo cells: one thread per cell,
