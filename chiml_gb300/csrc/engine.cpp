@@ -164,6 +164,19 @@ public:
             R.fluxIm.push_back(std::move(im));
             R.fluxSamples.push_back(stepsDone_ / fp.spec.timeInt + 1);
         }
+        for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
+            const dev::DftTable<T>& d = dft_[P.fluxes.size() + k];
+            const std::size_t n = static_cast<std::size_t>(d.npts) * P.freqDetectors[k].spec.freqList.size();
+            std::vector<double> re(n), im(n);
+            if (n) {
+                ck(cudaMemcpy(re.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
+                ck(cudaMemcpy(im.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
+            }
+            d2h_ += 2.0 * n * sizeof(double);
+            R.freqRe.push_back(std::move(re));
+            R.freqIm.push_back(std::move(im));
+            R.freqSamples.push_back(stepsDone_ / P.freqDetectors[k].timeInt + 1);
+        }
         for (std::size_t q = 0; q < emit_.size(); ++q) {
             const dev::EmitterDev& e = emit_[q];
             const EmitterPlan& ep = P.emitters[q];
@@ -206,6 +219,7 @@ public:
         }
         write_detectors(P, R, outDir_, stepsDone_);
         write_fluxes(P, R, outDir_);
+        write_freq_detectors(P, R, outDir_);
         write_emitters(P, R, outDir_);
         finalized_ = true;
     }
@@ -1097,9 +1111,8 @@ private:
             dRec_ = mem_.alloc<double>(recTotal_);
             recT_.rec = dRec_;
         }
-        // DFT flux: point tables, phasors per sample, ring of K samples, FP64 accumulators
+        // DFT tables: the flux regions, then the frequency-domain detectors
         for (auto& fp : P.fluxes) {
-            dev::DftTable<T> d{};
             std::vector<int> comp, cell;
             for (auto& st : fp.stores)
                 for (long long c : st.cells) {
@@ -1107,14 +1120,35 @@ private:
                     comp.push_back(st.comp);
                     cell.push_back(static_cast<int>(c));
                 }
-            const int nf = static_cast<int>(fp.spec.freqList.size());
-            const int ti = fp.spec.timeInt;
+            dft_.push_back(makeDft(comp, cell, fp.spec.freqList, fp.spec.timeInt));
+        }
+        for (auto& dp : P.freqDetectors) {
+            std::vector<int> comp, cell;
+            for (auto& F : dp.fields)
+                for (long long c : F.cells) {
+                    if (c < 0 || c > 0x7fffffffLL) throw UnsupportedError("frequency detector point outside 32-bit indices");
+                    comp.push_back(F.comp);
+                    cell.push_back(static_cast<int>(c));
+                }
+            dft_.push_back(makeDft(comp, cell, dp.spec.freqList, dp.timeInt));
+        }
+        uploadEmitters();
+        uploadTfsf();
+        uploadTail();
+    }
+
+    // One DFT table: point table (component, cell), phasors per sample from the accumulated
+    // time, a ring of K samples and FP64 accumulators [point][frequency].
+    dev::DftTable<T> makeDft(const std::vector<int>& comp, const std::vector<int>& cell, const std::vector<double>& freqs, int ti) {
+        dev::DftTable<T> d{};
+        {
+            const int nf = static_cast<int>(freqs.size());
             const int nSamples = P.nSteps / ti + 1;
             const int nfPad = (nf + 31) / 32 * 32;
             std::vector<T> ph(static_cast<std::size_t>(nSamples) * nfPad * 2, T(0));
             for (int n = 0; n < nSamples; ++n)
                 for (int f = 0; f < nf; ++f) {
-                    std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * fp.spec.freqList[f]));
+                    std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * freqs[f]));
                     ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 0] = static_cast<T>(e.real());
                     ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 1] = static_cast<T>(e.imag());
                 }
@@ -1132,10 +1166,11 @@ private:
             d.ring = mem_.alloc<T>(static_cast<std::size_t>(d.stride) * static_cast<std::size_t>(K));
             d.re = mem_.alloc<double>(cell.size() * nf);
             d.im = mem_.alloc<double>(cell.size() * nf);
-            dft_.push_back(d);
         }
-        uploadEmitters();
-        uploadTfsf();
+        return d;
+    }
+
+    void uploadTail() {
         bytesPerCell_ = algorithmicBytesPerCell();
         dStep_ = mem_.alloc<int>(1);
         dErr_ = mem_.alloc<unsigned int>(1);

@@ -580,7 +580,7 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
         else if (cls == "freq") d.cls = DtcClass::FREQ;
         else if (cls == "cout" || cls == "bmp") throw UnsupportedError("detector class '" + cls + "' is not supported");
         else throw InputError("DTCCLASS (DetectorList.class) for input file is not defined");
-        if (d.cls == DtcClass::FREQ) throw UnsupportedError("frequency-domain field detectors are not supported by this build");
+
         d.SI = dn.get<bool>("SI", true);
         d.timeInt = dn.get<double>("Time_Interval", ip.dt);
         std::array<double, 3> tempSz = as_arr3(dn, "size");
@@ -591,6 +591,7 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
                 throw InputError("A detector is outside the FDTD cell.");
             d.loc[i] = find_pt(loc[i] + ip.size[i] / 2.0 - tempSz[i] / 2.0, ip.d[i]);
         }
+        if (d.cls == DtcClass::FREQ) d.freqList = read_freq_list(dn, "The freq detector");
         ip.detectors.push_back(d);
     }
     // Flux regions, parallelInputs.cpp:756-838

@@ -359,4 +359,149 @@ void write_emitters(const Plan& P, const RunRecord& R, const std::string& outDir
     }
 }
 
+void write_freq_detectors(const Plan& P, const RunRecord& R, const std::string& outDir) {
+    typedef std::complex<double> cx;
+    for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
+        const DetectorPlan& dp = P.freqDetectors[k];
+        const DetectorSpec& ds = dp.spec;
+        const std::vector<double>& fl = ds.freqList;
+        const int nfreq = static_cast<int>(fl.size());
+        const long long szFreq = dp.szFreq;
+        const int nt = R.freqSamples[k];
+        const int ti = dp.timeInt;
+        // the collected fields, transposed: [field][point][freq] (fieldTranspose)
+        std::vector<std::vector<cx>> trans;
+        long long off = 0;
+        for (const auto& F : dp.fields) {
+            std::vector<cx> g(static_cast<std::size_t>(szFreq) * nfreq, cx(0.0, 0.0));
+            for (std::size_t p = 0; p < F.cells.size(); ++p)
+                for (int f = 0; f < nfreq; ++f) {
+                    const std::size_t a = static_cast<std::size_t>(off + static_cast<long long>(p)) * nfreq + f;
+                    g[p + static_cast<std::size_t>(szFreq) * f] = cx(R.freqRe[k][a], R.freqIm[k][a]);
+                }
+            off += static_cast<long long>(F.cells.size());
+            trans.push_back(std::move(g));
+        }
+        // the incident fields main.cpp passes for the detector type
+        std::vector<const std::vector<cplx>*> incd;
+        switch (ds.type) {
+            case DtcType::HPOW: incd = {&R.incH[0], &R.incH[1], &R.incH[2]}; break;
+            case DtcType::EPOW: incd = {&R.incE[0], &R.incE[1], &R.incE[2]}; break;
+            case DtcType::EX: incd = {&R.incE[0]}; break;
+            case DtcType::EY: incd = {&R.incE[1]}; break;
+            case DtcType::EZ: incd = {&R.incE[2]}; break;
+            case DtcType::HX: incd = {&R.incH[0]}; break;
+            case DtcType::HY: incd = {&R.incH[1]}; break;
+            case DtcType::HZ: incd = {&R.incH[2]}; break;
+            default: break;
+        }
+        const double conv = dp.convFactor / 2.0;
+        // toOutFile_: fieldOutFreqFunction / pwrOutFreqFunction (DTC/parallelDTCOutputFxn.cpp:9-18)
+        auto out = [&](const cx* col, long long n) {
+            cx sum(0.0, 0.0);
+            if (dp.power) {
+                for (long long p = 0; p < n; ++p) sum += col[p] * std::conj(col[p]);
+                return conv * sum / std::pow(static_cast<double>(nt), 2.0);
+            }
+            for (long long p = 0; p < n; ++p) sum += col[p];
+            return conv * sum / std::pow(static_cast<double>(nt), 1.0);
+        };
+        // incident spectra: even samples, then odd ones, real parts (parallelDTC_FREQ.hpp:416-428)
+        auto incident = [&](int ii) {
+            std::vector<cx> pts;
+            for (const std::vector<cplx>* field : incd) {
+                cx pt(0.0, 0.0);
+                for (int start = 0; start < 2; ++start)
+                    for (std::size_t tt = start; tt < field->size(); tt += 2)
+                        pt += std::real(0.5 * (*field)[tt]) *
+                              std::exp(cx(0.0, -1.0 * fl[ii] * static_cast<double>(tt / 2) * (P.dt / static_cast<double>(ti))));
+                pt /= static_cast<double>(nt * ti);
+                if (dp.power) pt *= std::conj(pt);
+                pt *= dp.convFactor / 2.0;
+                pts.push_back(pt);
+            }
+            return pts;
+        };
+        const std::size_t nField = trans.size();
+        if (!ds.outputMaps) {
+            const std::string path = out_path(outDir, ds.name);
+            std::ofstream f(path);
+            if (!f) throw InputError("cannot open detector output " + path);
+            f << "#" << std::setw(16) << "freq\tabs(incd)\treal(incd)\timag(incd)";
+            for (std::size_t nn = 1; nn < nField; ++nn) f << "\tabs(field " << nn << ")\treal(field " << nn << ")\timag(field " << nn << ")";
+            if (nField > 1) f << "\tabs(total)\treal(total)\timag(total)";
+            f << std::endl;
+            for (int ii = 0; ii < nfreq; ++ii) {
+                f << std::setw(16) << std::setprecision(12) << dp.freqConv * fl[ii];
+                cx incdField(0.0, 0.0);
+                for (const cx& pt : incident(ii)) {
+                    f << "\t" << std::setw(16) << std::setprecision(12) << std::real(pt) << "\t" << std::setw(16)
+                      << std::setprecision(12) << std::imag(pt) << "\t" << std::setw(16) << std::setprecision(12) << std::abs(pt);
+                    incdField += pt;
+                }
+                if (incd.size() > 2)
+                    f << "\t" << std::setw(16) << std::setprecision(12) << std::real(incdField) << "\t" << std::setw(16)
+                      << std::setprecision(12) << std::imag(incdField) << "\t" << std::setw(16) << std::setprecision(12)
+                      << std::abs(incdField);
+                cx freq(0.0, 0.0);
+                for (const auto& g : trans) {
+                    const cx pt = out(&g[static_cast<std::size_t>(szFreq) * ii], szFreq);
+                    f << "\t" << std::setw(16) << std::setprecision(12) << std::real(pt) << "\t" << std::setw(16)
+                      << std::setprecision(12) << std::imag(pt) << "\t" << std::setw(16) << std::setprecision(12) << std::abs(pt);
+                    freq += pt;
+                }
+                if (nField > 1)
+                    f << '\t' << std::setw(16) << std::setprecision(12) << std::real(freq) << "\t" << std::setw(16)
+                      << std::setprecision(12) << std::imag(freq) << "\t" << std::setw(16) << std::setprecision(12) << std::abs(freq)
+                      << std::endl;
+                else
+                    f << "\n";
+            }
+        } else {
+            for (int ii = 0; ii < nfreq; ++ii) {
+                const std::string path = out_path(outDir, ds.name + "." + std::to_string(dp.freqConv * fl[ii]));
+                std::ofstream f(path);
+                if (!f) throw InputError("cannot open detector output " + path);
+                f << "#" << std::setw(16) << "x\ty\tz\tabs(incd)\treal(incd)\timag(incd)";
+                for (std::size_t nn = 1; nn < nField; ++nn) f << "\tabs(field " << nn << ")\treal(field " << nn << ")\timag(field " << nn << ")";
+                if (nField > 1) f << "\tabs(total)\treal(total)\timag(total)";
+                f << std::endl;
+                std::vector<double> outIncd;
+                cx incdField(0.0, 0.0);
+                for (const cx& pt : incident(ii)) {
+                    outIncd.push_back(std::real(pt));
+                    outIncd.push_back(std::imag(pt));
+                    outIncd.push_back(std::abs(pt));
+                    incdField += pt;
+                }
+                if (incd.size() > 2) {
+                    outIncd.push_back(std::real(incdField));
+                    outIncd.push_back(std::imag(incdField));
+                    outIncd.push_back(std::abs(incdField));
+                }
+                for (int yy = 0; yy < ds.sz[1]; ++yy)
+                    for (int zz = 0; zz < ds.sz[2]; ++zz)
+                        for (int xx = 0; xx < ds.sz[0]; ++xx) {
+                            f << std::setw(16) << xx << '\t' << yy << '\t' << zz;
+                            for (double v : outIncd) f << "\t" << std::setw(16) << std::setprecision(12) << v;
+                            const long long jj = xx + static_cast<long long>(zz) * ds.sz[0] + static_cast<long long>(yy) * ds.sz[0] * ds.sz[2];
+                            cx freq(0.0, 0.0);
+                            for (const auto& g : trans) {
+                                const cx pt = out(&g[static_cast<std::size_t>(szFreq) * ii + jj], 1);
+                                f << "\t" << std::setw(16) << std::setprecision(12) << std::abs(pt) << "\t" << std::real(pt) << "\t"
+                                  << std::imag(pt);
+                                freq += pt;
+                            }
+                            if (nField > 1)
+                                f << '\t' << std::setw(16) << std::setprecision(12) << std::real(freq) << "\t" << std::setw(16)
+                                  << std::setprecision(12) << std::imag(freq) << "\t" << std::setw(16) << std::setprecision(12)
+                                  << std::abs(freq) << std::endl;
+                            else
+                                f << "\n";
+                        }
+            }
+        }
+    }
+}
+
 }  // namespace chiml

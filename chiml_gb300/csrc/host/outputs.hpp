@@ -24,6 +24,10 @@ struct RunRecord {
     // incident fields of the TFSF surface (E_incd_ / H_incd_, parallelFDTDField.hpp:1238-1255):
     // per component two samples per step, 2 * (nSteps + 1) values; empty without a surface
     std::array<std::vector<cplx>, 3> incE, incH;
+    // frequency-domain detectors: re/im [point][freq] over the concatenated fields of each
+    // detector, and its number of samples
+    std::vector<std::vector<double>> freqRe, freqIm;
+    std::vector<int> freqSamples;
 };
 
 // Number of values one output event of detector k stores.
@@ -35,6 +39,10 @@ int detector_events(const DetectorPlan& dp, int nSteps);
 void write_detectors(const Plan& P, const RunRecord& R, const std::string& outDir, int stepsDone);
 // Combines the flux accumulators and writes "<name>.dat" (parallelFlux.hpp:325-560).
 void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir);
+
+// Writes every frequency-domain detector (parallelDetectorFREQ_Base::toFile / toMap with the
+// incident fields, DTC/parallelDTC_FREQ.hpp:390-583, as main.cpp:73-105 calls them).
+void write_freq_detectors(const Plan& P, const RunRecord& R, const std::string& outDir);
 
 // Writes the emitter polarisation file (parallelQEReal::outputPol, parallelQE.cpp:520-557) and
 // the population files (QEPopDtc::toFile, QEPopDtc.cpp:37-61).

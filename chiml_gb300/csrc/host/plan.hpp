@@ -106,6 +106,11 @@ struct DetectorPlan {
     };
     std::vector<Field> fields;
     std::array<int, 3> sz = {1, 1, 1};
+    // frequency-domain detectors (parallelDetectorFREQ_Base, DTC/parallelDTC_FREQ.hpp): each
+    // field's DFT box (parallelStorageFreqDTC, no propagation direction) holds its points
+    // x fastest, then z, then y; `freqPts` of the szFreq = product of sz box points are stored
+    double freqConv = 1.0;
+    long long szFreq = 0;
 };
 
 // One DFT accumulator box (parallelStorageFreqDTC) of a flux region.
@@ -248,7 +253,8 @@ struct Plan {
     CompPlan comp[6];
     OrDipPlan ordip;
     std::vector<SourcePlan> sources;
-    std::vector<DetectorPlan> detectors;
+    std::vector<DetectorPlan> detectors;       // time-domain (text, binary)
+    std::vector<DetectorPlan> freqDetectors;   // frequency-domain
     std::vector<FluxPlan> fluxes;
     std::vector<EmitterPlan> emitters;
     std::vector<TfsfPlan> tfsf;

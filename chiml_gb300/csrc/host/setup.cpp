@@ -972,7 +972,9 @@ struct Builder {
             DetectorPlan dp;
             dp.spec = ds;
             dp.sz = ds.sz;
-            dp.timeInt = static_cast<int>(std::floor(ds.timeInt / dt));
+            const bool freq = ds.cls == DtcClass::FREQ;
+            // parallelFDTDField.cpp:1728 rounds a frequency detector's interval to the nearest step
+            dp.timeInt = freq ? static_cast<int>(std::floor(ds.timeInt / dt + 0.5)) : static_cast<int>(std::floor(ds.timeInt / dt));
             if (dp.timeInt == 0) throw InputError("The time step of a detector is less than the main grid or set to 0.");
             std::vector<std::pair<int, std::array<int, 3>>> flds;
             auto need = [&](int c) {
@@ -1024,6 +1026,11 @@ struct Builder {
             }
             dp.power = (ds.type == DtcType::EPOW || ds.type == DtcType::HPOW);
             if (dp.power) dp.convFactor *= dp.convFactor;
+            if (freq) {
+                freqDetector(dp, flds);
+                P.freqDetectors.push_back(std::move(dp));
+                continue;
+            }
             for (auto& f : flds) {
                 DetectorPlan::Field F;
                 F.comp = f.first;
@@ -1074,6 +1081,54 @@ struct Builder {
                             throw UnsupportedError("text detector of a staggered power field reads past its box (the reference aborts)");
             }
             P.detectors.push_back(std::move(dp));
+        }
+    }
+
+    // A frequency-domain detector (parallelDetectorFREQ_Base constructor,
+    // DTC/parallelDTC_FREQ.hpp:80-130): its own unit conversions, and per field the DFT box
+    // of parallelStorageFreqDTC without a propagation direction (genDatStruct, getLocalLocEl,
+    // getLocalSzEl: DTC/parallelStorageFreqDTC.hpp:168-320): points x fastest, then z, then
+    // y, from the detector corner; the field offsets of power detectors are not applied.
+    void freqDetector(DetectorPlan& dp, const std::vector<std::pair<int, std::array<int, 3>>>& flds) {
+        const DetectorSpec& ds = dp.spec;
+        dp.convFactor = 1.0;
+        dp.freqConv = 1.0;
+        if (ds.SI) {
+            dp.convFactor = in.I0 / in.a;
+            if (ds.type == DtcType::EX || ds.type == DtcType::EY || ds.type == DtcType::EZ)
+                dp.convFactor /= kEps0 * kSpeedOfLight;
+            dp.freqConv = kSpeedOfLight / in.a;
+        }
+        if (dp.power) dp.convFactor = std::pow(dp.convFactor, 2.0);
+        dp.freqConv /= (M_PI * 2.0);
+        dp.szFreq = static_cast<long long>(ds.sz[0]) * ds.sz[1] * ds.sz[2];
+        for (auto& f : flds) {
+            DetectorPlan::Field F;
+            F.comp = f.first;
+            F.off = f.second;
+            std::array<int, 3> ll{}, ls{0, 0, 0};
+            bool inside = true;
+            for (int ii = 0; ii < 3; ++ii) {
+                const int ln = lnv(ii);
+                if (ds.loc[ii] >= 0 && ds.loc[ii] < ln - 2) ll[ii] = ds.loc[ii] + 1;
+                else if (ds.loc[ii] == -1) ll[ii] = 0;
+                else if (ds.loc[ii] < 0 && ds.loc[ii] + ds.sz[ii] > 0) ll[ii] = 1;
+                else ll[ii] = -1;
+            }
+            if (D.lz == 1) ll[2] = 0;
+            for (int ii = 0; ii < 3; ++ii)
+                if (ll[ii] == -1) inside = false;
+            if (inside)
+                for (int ii = 0; ii < 3; ++ii) {
+                    const int ln = lnv(ii);
+                    ls[ii] = (ds.sz[ii] + ds.loc[ii] > ln - 2) ? ln - ll[ii] - 1 : ds.loc[ii] + ds.sz[ii] - (ll[ii] - 1);
+                }
+            F.outSz = ls;  // x, y, z sizes of the stored box
+            for (int y = 0; y < ls[1]; ++y)
+                for (int z = 0; z < ls[2]; ++z)
+                    for (int x = 0; x < ls[0]; ++x) F.cells.push_back(D.idx(ll[0] + x, ll[1] + y, ll[2] + z));
+            if (static_cast<long long>(F.cells.size()) > dp.szFreq) throw InputError("frequency detector box larger than the detector");
+            dp.fields.push_back(std::move(F));
         }
     }
 

@@ -61,7 +61,7 @@ typedef struct chiml_stats {
     double bytes_dft;              /* algorithmic HBM bytes of the DFT launches of one sampled step */
     double h2d_bytes;              /* bytes copied host to device so far */
     double d2h_bytes;              /* bytes copied device to host so far */
-    int32_t n_flux_regions;        /* DFT flux regions (two profile slots each) */
+    int32_t n_flux_regions;        /* DFT tables: flux regions, then frequency-domain detectors (two profile slots each) */
     int32_t n_emitters;            /* emitter objects (one profile slot each) */
     int32_t n_tfsf;                /* TFSF surfaces (one profile slot each) */
 } chiml_stats;
@@ -78,8 +78,8 @@ chiml_status chiml_step(chiml_sim* sim, int64_t nsteps);
 chiml_status chiml_sync(chiml_sim* sim);
 
 /* Copies detector records, DFT accumulators and emitter outputs to the host and
- * writes the detector, flux, emitter polarisation and population files in chiML's
- * formats. */
+ * writes the detector (time and frequency domain), flux, emitter polarisation and
+ * population files in chiML's formats. */
 chiml_status chiml_finalize(chiml_sim* sim);
 
 void chiml_destroy(chiml_sim* sim);
@@ -100,7 +100,8 @@ void* chiml_stream(chiml_sim* sim);
 /* Advances nsteps steps without graphs, timing every kernel launch with CUDA
  * events on the handle's stream. ms_out[k] receives the summed milliseconds of
  * kernel slot k: 0 H pass, 1 sources, 2 E pass, 3 step counter, 4 detector
- * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of flux region q, then
+ * records, 5 + 2q DFT sample gather and 6 + 2q DFT fold of DFT table q (flux
+ * regions, then frequency-domain detectors), then
  * 5 + 2 * n_flux_regions + e the emitter step of emitter object e, then
  * 5 + 2 * n_flux_regions + n_emitters + k the step of TFSF surface k.
  * *nslots receives the number of slots written (at most max_slots). */

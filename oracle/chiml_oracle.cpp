@@ -9,7 +9,7 @@
 //   D -> E               UTIL/FDTD_up_eq.cpp:838-848 (DtoU), 862-875 (orDipDtoU)
 //   soft sources         SOURCE/parallelSourceNormal.cpp:15-37
 //   DFT accumulation     DTC/parallelStorageFreqDTC.cpp:21-30, DTC/parallelFlux.hpp:296-314
-//   detector sampling    DTC/parallelStorageDTC.cpp:17-48
+//   detector sampling    DTC/parallelStorageDTC.cpp:17-48, DTC/parallelDTC_FREQ.hpp:258-264 (frequency domain)
 //   TFSF surfaces        SOURCE/parallelTFSF.hpp:1058-1186, SOURCE/parallelTFSF.cpp:11-94, PML/PML.cpp:12-31
 //   emitters             ML/parallelQE.hpp:614-770 (addQE, updateDensity, denDeriv, PCABAM4),
 //                        UTIL/FDTD_up_eq.cpp:1367-1420 (addP, getE_TE/TM), ML/Hamiltonian.cpp:59-69
@@ -325,6 +325,13 @@ struct OracleSim {
             rec.fluxIm.emplace_back(n, 0.0);
             rec.fluxSamples.push_back(0);
         }
+        for (auto& dp : P.freqDetectors) {
+            std::size_t npts = 0;
+            for (auto& F : dp.fields) npts += F.cells.size();
+            rec.freqRe.emplace_back(npts * dp.spec.freqList.size(), 0.0);
+            rec.freqIm.emplace_back(npts * dp.spec.freqList.size(), 0.0);
+            rec.freqSamples.push_back(0);
+        }
         // detectors and flux take their t = 0 sample at construction (parallelFDTDField.cpp:831-837)
         record(0.0);
         dft(0);
@@ -371,6 +378,34 @@ struct OracleSim {
                 }
             }
             rec.fluxSamples[q] += 1;
+        }
+        // frequency-domain detectors: parallelDetectorFREQ_Base::output (DTC/parallelDTC_FREQ.hpp:258-264)
+        for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
+            const DetectorPlan& dp = P.freqDetectors[k];
+            if (st % dp.timeInt != 0) continue;
+            const double tt = P.tcur[st];
+            const std::vector<double>& fl = dp.spec.freqList;
+            const std::size_t nf = fl.size();
+            std::vector<double> cr(nf), ci(nf);
+            for (std::size_t f = 0; f < nf; ++f) {
+                std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * tt * fl[f]));
+                cr[f] = e.real();
+                ci[f] = e.imag();
+            }
+            std::size_t off = 0;
+            for (const auto& F : dp.fields) {
+                const double* src = fieldOf(F.comp);
+                for (std::size_t p = 0; p < F.cells.size(); ++p) {
+                    const double v = src[F.cells[p]];
+                    const std::size_t base = (off + p) * nf;
+                    for (std::size_t f = 0; f < nf; ++f) {
+                        rec.freqRe[k][base + f] += cr[f] * v;
+                        rec.freqIm[k][base + f] += ci[f] * v;
+                    }
+                }
+                off += F.cells.size();
+            }
+            rec.freqSamples[k] += 1;
         }
     }
 
@@ -618,6 +653,7 @@ int chiml_oracle_finalize(void* h, const char* out_dir) {
     try {
         write_detectors(s->P, s->rec, out_dir ? out_dir : "", s->step);
         write_fluxes(s->P, s->rec, out_dir ? out_dir : "");
+        write_freq_detectors(s->P, s->rec, out_dir ? out_dir : "");
         s->rec.emitterP.clear();
         s->rec.emitterPop.clear();
         for (auto& q : s->qe) {

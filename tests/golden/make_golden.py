@@ -141,6 +141,29 @@ def _tfsf_2d_te():
     return cfg
 
 
+def _freq_dets(cfg, dets):
+    """Appends frequency-domain detectors (type, size, output_map, SI, interval in steps) at the centre."""
+    dt = cfg["CompCell"]["dt"]
+    for i, (typ, sz, maps, si, ti) in enumerate(dets):
+        cfg["DetectorList"].append({"loc": [0.0, 0.0, 0.0], "size": list(sz), "type": typ, "fname": "out/fq%d" % i,
+                                    "dtc_class": "freq", "SI": si, "Time_Interval": ti * dt, "lamL": 4.0, "lamR": 7.0,
+                                    "nfreq": 5, "output_map": maps})
+    return cfg
+
+
+def _freq_3d():
+    """Frequency-domain detectors in 3-D under a TFSF plane wave: an Ex box in SI units, an E power
+    box sampled every other step, an H power box written as per-frequency maps, an Hy plane."""
+    return _freq_dets(_tfsf_disp(), [("Ex", (0.2, 0.2, 0.2), False, True, 1), ("E_pow", (0.1, 0.15, 0.2), False, False, 2),
+                                     ("H_pow", (0.1, 0.1, 0.1), True, True, 1), ("Hy", (0.1, 0.0, 0.1), False, False, 3)])
+
+
+def _freq_2d():
+    """Frequency-domain detectors in 2-D TE (the reference's storage holds no points there:
+    the field columns are zero, the incident columns are not)."""
+    return _freq_dets(_tfsf_2d_te(), [("Ey", (0.2, 0.2, 0.0), False, False, 1), ("H_pow", (0.1, 0.1, 0.0), True, True, 1)])
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -154,6 +177,8 @@ CASES = {
     "tfsf_disp": _tfsf_disp,
     "tfsf_oblique": _tfsf_oblique,
     "tfsf_2d_te": _tfsf_2d_te,
+    "freq_3d": _freq_3d,
+    "freq_2d": _freq_2d,
 }
 
 
