@@ -227,14 +227,13 @@ public:
     void getField(int comp, double* out) override {
         if (comp < 0 || comp > 8 || !fields_.f[comp]) throw std::invalid_argument("field not present");
         ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
-        std::size_t N = static_cast<std::size_t>(P.dims.cells());
-        if (std::is_same<T, double>::value) {
-            ck(cudaMemcpy(out, fields_.f[comp], N * sizeof(double), cudaMemcpyDeviceToHost), "D2H field");
-        } else {
-            std::vector<T> tmp(N);
-            ck(cudaMemcpy(tmp.data(), fields_.f[comp], N * sizeof(T), cudaMemcpyDeviceToHost), "D2H field");
-            for (std::size_t i = 0; i < N; ++i) out[i] = static_cast<double>(tmp[i]);
-        }
+        // the device rows are padded to pitch_ values: copy them out and drop the padding
+        const Dims& D = P.dims;
+        std::vector<T> tmp(static_cast<std::size_t>(cellsPad_));
+        ck(cudaMemcpy(tmp.data(), fields_.f[comp], tmp.size() * sizeof(T), cudaMemcpyDeviceToHost), "D2H field");
+        const long long rows = static_cast<long long>(D.ly) * D.lz;
+        for (long long r = 0; r < rows; ++r)
+            for (int x = 0; x < D.lx; ++x) out[r * D.lx + x] = static_cast<double>(tmp[static_cast<std::size_t>(r * pitch_ + x)]);
     }
 
     // Validates the box and reads it through the fixed device array; no allocation.
@@ -257,7 +256,7 @@ public:
                   std::to_string(dev::kBoxScratchCells) + " cells of chiml_get_box_noalloc";
             return CHIML_E_INPUT;
         }
-        cudaError_t e = dev::gather_box_noalloc<T>(opt_.device, fields_.f[comp], D.lx, D.lz, box, out, stream_);
+        cudaError_t e = dev::gather_box_noalloc<T>(opt_.device, fields_.f[comp], static_cast<int>(pitch_), D.lz, box, out, stream_);
         if (e == cudaSuccess) return CHIML_OK;
         why = std::string("chiml_get_box_noalloc: ") + cudaGetErrorString(e);
         return CHIML_E_CUDA;
@@ -390,6 +389,8 @@ private:
     std::vector<dev::DftTable<T>> dft_;
     std::vector<dev::EmitterDev> emit_;
     std::vector<dev::TfsfDev> tfsf_;
+    long long pitch_ = 0;     // device row length (values): lx rounded up to a multiple of 4
+    long long cellsPad_ = 0;  // device grid size: pitch_ * ly * lz
     std::vector<long long> recBase_;
     std::size_t recTotal_ = 0;
     double* dRec_ = nullptr;
@@ -417,6 +418,40 @@ private:
             dev::launch_dft_sample<T>(d, fields_, dStep_, s);
             dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
         }
+    }
+
+    // ---- the device layout: rows padded from lx to pitch_ values ----
+    // Cell index of the device layout for a cell index of the plan (negative: unchanged).
+    long long pad(long long i) const {
+        if (i < 0) return i;
+        const long long lx = P.dims.lx;
+        return (i % lx) + pitch_ * (i / lx);
+    }
+    template <typename I>
+    std::vector<I> padCells(const std::vector<I>& v) const {
+        std::vector<I> o(v.size());
+        for (std::size_t k = 0; k < v.size(); ++k) o[k] = static_cast<I>(pad(static_cast<long long>(v[k])));
+        return o;
+    }
+    // A neighbour offset of the plan (dx + lx (dz + lz dy), |d*| <= 1) in the device layout.
+    long long padOffset(long long off) const {
+        const long long lx = P.dims.lx, lz = P.dims.lz;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dx = -1; dx <= 1; ++dx)
+                    if (dx + lx * (dz + lz * dy) == off) return dx + pitch_ * (dz + lz * dy);
+        throw InputError("neighbour offset of more than one cell");
+    }
+    // A whole-grid array of the plan in the device layout; the padding holds `fill`.
+    template <typename V>
+    std::vector<V> padGrid(const std::vector<V>& v, V fill) const {
+        const Dims& D = P.dims;
+        if (static_cast<long long>(v.size()) != D.cells()) throw InputError("grid array of the wrong size");
+        std::vector<V> o(static_cast<std::size_t>(cellsPad_), fill);
+        const long long rows = static_cast<long long>(D.ly) * D.lz;
+        for (long long r = 0; r < rows; ++r)
+            for (int x = 0; x < D.lx; ++x) o[static_cast<std::size_t>(r * pitch_ + x)] = v[static_cast<std::size_t>(r * D.lx + x)];
+        return o;
     }
 
     void launchTfsf(const dev::TfsfDev& t, void* s) {
@@ -533,8 +568,8 @@ private:
                         while (r < g.n && !multi(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride)) ++r;
                         if (r == r0) continue;
                         dev::TfsfSegDev d{};
-                        d.cell0 = g.cell0 + r0 * g.cellStride;
-                        d.cellStride = g.cellStride;
+                        d.cell0 = pad(g.cell0 + r0 * g.cellStride);
+                        d.cellStride = padOffset(g.cellStride);
                         d.incd0 = g.incd0 + r0 * g.incdStride;
                         d.incdStride = g.incdStride;
                         d.n = r - r0;
@@ -543,7 +578,7 @@ private:
                         d.pref = g.pref;
                         const long long lastCell = d.cell0 + static_cast<long long>(d.n - 1) * d.cellStride;
                         const long long lastIncd = d.incd0 + static_cast<long long>(d.n - 1) * d.incdStride;
-                        if (d.cell0 < 0 || lastCell >= P.dims.cells() || d.incd0 < 0 || lastIncd >= tp.gridLen || d.cellStride < 0 ||
+                        if (d.cell0 < 0 || lastCell >= cellsPad_ || d.incd0 < 0 || lastIncd >= tp.gridLen || d.cellStride < 0 ||
                             d.incdStride < 0 || !tp.line[d.line].present || !P.comp[d.comp].present)
                             throw InputError("TFSF surface row outside its grids");
                         for (int c = 0; c * dev::kTfsfRowChunk < d.n; ++c) sw.push_back(make_int2(static_cast<int>(sd.size()), c));
@@ -561,7 +596,7 @@ private:
                 if (listed != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
                 for (const TfsfCellAdds& a : *adds[w]) {
                     if (a.line.size() < 2) continue;  // in a row
-                    cell.push_back(a.cell);
+                    cell.push_back(pad(a.cell));
                     comp.push_back(a.comp);
                     start.push_back(static_cast<int>(tl.size()));
                     for (std::size_t k = 0; k < a.line.size(); ++k) {
@@ -600,11 +635,11 @@ private:
         std::memset(&pass.od, 0, sizeof(pass.od));
         if (!od.present || od.cells.empty()) return;
         if (od.nPoles > dev::kMaxPoles) throw UnsupportedError("more than 8 oriented-dipole poles");
-        const std::size_t N = static_cast<std::size_t>(P.dims.cells());
+        const std::size_t N = static_cast<std::size_t>(cellsPad_);
         const long long n = static_cast<long long>(od.cells.size());
         pass.od.n = n;
         pass.od.nPoles = od.nPoles;
-        pass.od.cell = mem_.upload(od.cells);
+        pass.od.cell = mem_.upload(padCells(od.cells));
         pass.od.obj = mem_.upload(od.obj);
         std::vector<T> dip(static_cast<std::size_t>(od.nPoles) * 3 * n);
         for (long long j = 0; j < n; ++j)
@@ -613,7 +648,7 @@ private:
                     dip[(static_cast<std::size_t>(pp) * 3 + a) * n + j] = static_cast<T>(od.dip[j * od.nPoles + pp][a]);
         pass.od.dip = mem_.upload(dip);
         for (int c = 0; c < 3; ++c) {
-            pass.od.off[c] = od.offA[c];
+            pass.od.off[c] = padOffset(od.offA[c]);
             for (int pp = 0; pp < od.nPoles; ++pp) {
                 pass.od.P[c][pp] = mem_.alloc<T>(N);
                 pass.od.Pprev[c][pp] = mem_.alloc<T>(N);
@@ -621,7 +656,7 @@ private:
         }
         for (long long j = 0; j < n; ++j) {
             const long long i = od.cells[j];
-            if (i - od.offA[1] < 0 || i >= static_cast<long long>(N)) throw InputError("oriented-dipole cell outside the grid");
+            if (i - od.offA[1] < 0 || i >= P.dims.cells()) throw InputError("oriented-dipole cell outside the grid");
         }
     }
 
@@ -719,11 +754,11 @@ private:
             e.abC[3] = ep.dt / 24.0;
             e.invHbar = 1.0 / ep.hbar;
             e.na = ep.na;
-            e.cellGrid = mem_.upload(ep.cellGrid);
+            e.cellGrid = mem_.upload(padCells(ep.cellGrid));
             e.cellP = mem_.upload(ep.cellP);
             e.unit[0] = 1;
-            e.unit[1] = static_cast<long long>(D.lx) * D.lz;
-            e.unit[2] = D.lx;
+            e.unit[1] = pitch_ * D.lz;
+            e.unit[2] = pitch_;
             const std::size_t nstate = static_cast<std::size_t>(e.nm) * n2 * e.nc;
             std::vector<double2> rho(nstate, make_double2(0.0, 0.0));
             for (int m = 0; m < e.nm; ++m)
@@ -748,7 +783,7 @@ private:
                 e.boxBase[k] = ep.boxBase[k];
             }
             e.zOff = ep.zOff;
-            e.lx = D.lx;
+            e.lx = static_cast<int>(pitch_);
             e.lz = D.lz;
             e.nDtc = static_cast<int>(ep.dtcLevs.size());
             std::vector<int> lev = ep.dtcLevs;
@@ -862,7 +897,7 @@ private:
         }
         pass.interior3d = (interior && !twoD) ? 1 : 0;
         pass.interior2d = (interior && twoD) ? 1 : 0;
-        pass.index64 = D.cells() + 2LL * D.lx * D.lz >= (1LL << 31) ? 1 : 0;
+        pass.index64 = cellsPad_ + 2LL * pitch_ * D.lz >= (1LL << 31) ? 1 : 0;
     }
 
     // Host-side bounds validation of every index the kernels will dereference.
@@ -906,7 +941,11 @@ private:
     void upload() {
         validatePlan();
         const Dims& D = P.dims;
-        const std::size_t N = static_cast<std::size_t>(D.cells());
+        // device rows of pitch_ >= lx values, a multiple of 4, so that every row starts on a
+        // 16-byte boundary (32 bytes in FP64)
+        pitch_ = (static_cast<long long>(D.lx) + 3) / 4 * 4;
+        cellsPad_ = pitch_ * D.ly * D.lz;
+        const std::size_t N = static_cast<std::size_t>(cellsPad_);
         // fields
         for (int c = 0; c < 6; ++c)
             if (P.comp[c].present) fields_.f[c] = mem_.alloc<T>(N);
@@ -940,6 +979,7 @@ private:
             pass.lx = D.lx;
             pass.ly = D.ly;
             pass.lz = D.lz;
+            pass.pitch = pitch_;
             pass.poleStart = dStart;
             pass.poleCount = dCount;
             pass.alpha = dAl;
@@ -955,7 +995,7 @@ private:
                 dc.present = 1;
                 dc.U = fields_.f[c];
                 dc.D = (c < 3) ? fields_.f[6 + c] : nullptr;
-                dc.code = mem_.upload(cp.code);
+                dc.code = mem_.upload(padGrid(cp.code, static_cast<uint8_t>(0)));
                 std::vector<dev::Class<T>> cls(cp.classes.size());
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
@@ -1017,7 +1057,7 @@ private:
                     dc.tpresent[t] = tp.present ? 1 : 0;
                     if (!tp.present) continue;
                     dc.axis[t] = tp.axis;
-                    dc.off[t] = tp.off;
+                    dc.off[t] = padOffset(tp.off);
                     dc.G[t] = fields_.f[tp.field];
                     dc.db[t] = static_cast<T>(tp.db);
                     dc.dbpsi[t] = static_cast<T>(tp.dbpsi);
@@ -1048,7 +1088,7 @@ private:
                 }
                 pass.nLor = static_cast<long long>(li.size());
                 pass.lorComp = mem_.upload(lc);
-                pass.lorCell = mem_.upload(li);
+                pass.lorCell = mem_.upload(padCells(li));
             }
         }
         (void)bytes;
@@ -1068,7 +1108,7 @@ private:
             }
             src_.n = static_cast<int>(cell.size());
             src_.comp = mem_.upload(comp);
-            src_.cell = mem_.upload(cell);
+            src_.cell = mem_.upload(padCells(cell));
             src_.src = mem_.upload(srcId);
             src_.value = mem_.upload(val);
             src_.nSteps = P.nSteps;
@@ -1102,7 +1142,7 @@ private:
             recT_.n = static_cast<int>(cell.size());
             recT_.det = mem_.upload(det);
             recT_.comp = mem_.upload(comp);
-            recT_.cell = mem_.upload(cell);
+            recT_.cell = mem_.upload(padCells(cell));
             recT_.outIndex = mem_.upload(outIdx);
             recT_.timeInt = mem_.upload(ti);
             recT_.nvals = mem_.upload(nvals);
@@ -1116,9 +1156,10 @@ private:
             std::vector<int> comp, cell;
             for (auto& st : fp.stores)
                 for (long long c : st.cells) {
-                    if (c > 0x7fffffffLL) throw UnsupportedError("grid too large for 32-bit flux point indices");
+                    const long long pc = pad(c);
+                    if (pc > 0x7fffffffLL) throw UnsupportedError("grid too large for 32-bit flux point indices");
                     comp.push_back(st.comp);
-                    cell.push_back(static_cast<int>(c));
+                    cell.push_back(static_cast<int>(pc));
                 }
             dft_.push_back(makeDft(comp, cell, fp.spec.freqList, fp.spec.timeInt));
         }
@@ -1126,9 +1167,10 @@ private:
             std::vector<int> comp, cell;
             for (auto& F : dp.fields)
                 for (long long c : F.cells) {
-                    if (c < 0 || c > 0x7fffffffLL) throw UnsupportedError("frequency detector point outside 32-bit indices");
+                    const long long pc = pad(c);
+                    if (c < 0 || pc > 0x7fffffffLL) throw UnsupportedError("frequency detector point outside 32-bit indices");
                     comp.push_back(F.comp);
-                    cell.push_back(static_cast<int>(c));
+                    cell.push_back(static_cast<int>(pc));
                 }
             dft_.push_back(makeDft(comp, cell, dp.spec.freqList, dp.timeInt));
         }

@@ -108,6 +108,7 @@ template <typename T>
 struct Pass {
     Comp<T> c[3];
     int lx, ly, lz;
+    long long pitch;        // device row length: cell (x, y, z) is x + pitch (z + lz y), pitch >= lx
     const int* poleStart;   // per object: first pole in the coefficient arrays
     const int* poleCount;   // per object: number of poles
     const T* alpha;

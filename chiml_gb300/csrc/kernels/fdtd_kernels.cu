@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
 template <typename T, bool EPASS>
 __device__ __forceinline__ void passCell(const Pass<T>& p, int x, int y, int z) {
     if (x >= p.lx || z >= p.lz || y >= p.ly) return;
-    const long long i = x + static_cast<long long>(p.lx) * (z + static_cast<long long>(p.lz) * y);
+    const long long i = x + p.pitch * (z + static_cast<long long>(p.lz) * y);
     const int coord[3] = {x, y, z};
 #pragma unroll
     for (int ci = 0; ci < 3; ++ci)
@@ -168,8 +168,8 @@ __global__ void __launch_bounds__(256) k_pass_lorentz(const Pass<T> p) {
     const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (j >= p.nLor) return;
     const long long i = p.lorCell[j];
-    const int x = static_cast<int>(i % p.lx);
-    const long long r = i / p.lx;
+    const int x = static_cast<int>(i % p.pitch);
+    const long long r = i / p.pitch;
     const int z = static_cast<int>(r % p.lz);
     const int y = static_cast<int>(r / p.lz);
     const int coord[3] = {x, y, z};
@@ -251,8 +251,8 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
     constexpr bool P1 = !(D2 && A1 == 2);  // term K present
     constexpr int TY = (A0 == 1) ? 0 : ((A1 == 1) ? 1 : -1);  // term along y, or none
     const Comp<T>& c = p.c[CI];
-    const I plane = static_cast<I>(p.lx) * p.lz;
-    I i = x + static_cast<I>(p.lx) * (z + static_cast<I>(p.lz) * y0);
+    const I plane = static_cast<I>(p.pitch) * p.lz;
+    I i = x + static_cast<I>(p.pitch) * (z + static_cast<I>(p.lz) * y0);
     const T* __restrict__ G0 = c.G[0];
     const T* __restrict__ G1 = c.G[1];
     // every array of the pass is its own allocation: no access aliases another
@@ -773,8 +773,8 @@ __global__ void __launch_bounds__(256) k_lorentz_packed(const Pass<T>* __restric
     const long long j = w.y * 256LL + threadIdx.x;
     if (j >= p.nLor) return;
     const long long i = p.lorCell[j];
-    const int x = static_cast<int>(i % p.lx);
-    const long long r = i / p.lx;
+    const int x = static_cast<int>(i % p.pitch);
+    const long long r = i / p.pitch;
     const int coord[3] = {x, static_cast<int>(r / p.lz), static_cast<int>(r % p.lz)};
     cellGeneric<T, true>(p, p.lorComp[j], i, coord);
 }
