@@ -203,13 +203,13 @@ __device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefet
 // (UpdateLorPol, DtoU, orDipDtoU: UTIL/FDTD_up_eq.cpp:425-448, 838-875). -1/eps_inf and
 // -0.5/eps_inf are exact scalings of the class's 1/eps_inf.
 template <typename T>
-__device__ __forceinline__ void dispersiveCell(const Pass<T>& p, int ci, uint32_t fl, int obj, T epsInv, long long i, T u,
-                                               T add, bool write) {
+__device__ __forceinline__ T dispersiveE(const Pass<T>& p, int ci, uint32_t fl, int obj, T epsInv, long long i, T u, T add,
+                                        bool write) {
     const Comp<T>& c = p.c[ci];
     if (fl & kFcLor) {
         if (obj < 0 || obj >= p.nObj || p.poleCount[obj] > c.nPoles) {
             atomicOr(p.err, kErrPoleCount);
-            return;
+            return u;
         }
         const int s = p.poleStart[obj];
         const int n = p.poleCount[obj];
@@ -239,7 +239,13 @@ __device__ __forceinline__ void dispersiveCell(const Pass<T>& p, int ci, uint32_
             e += oc * p.od.P[ci][q][i + o];
         }
     }
-    c.U[i] = e;
+    return e;
+}
+
+template <typename T>
+__device__ __forceinline__ void dispersiveCell(const Pass<T>& p, int ci, uint32_t fl, int obj, T epsInv, long long i, T u,
+                                               T add, bool write) {
+    p.c[ci].U[i] = dispersiveE<T>(p, ci, fl, obj, epsInv, i, u, add, write);
 }
 
 // D2: a 2-D grid (lz == 1), where the term along z is absent.
