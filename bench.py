@@ -106,25 +106,75 @@ def _dist():
 
 
 # The workloads: the default is the 3-D anisotropic + dispersive scene the headline
-# metric is quoted on; c1 (2-D TMz), c3 (3-D Maxwell-Liouville) and c4 (batched sweep of
-# 2-D emitter sheets) are the other configurations, for design measurements.
+# metric is quoted on; c1 (2-D TMz), c3 (3-D Maxwell-Liouville), c4 (batched sweep of
+# 2-D emitter sheets) and c5 (large 3-D mixed scene) are the other configurations.
 WORKLOADS = {
     "c2": ("Gcell-updates/s (FP32/FP64-split, 3-D dispersive 256^3)",
-           "3-D anisotropic + dispersive: %d^3 cells, 12-cell CPML, 16 uniaxial ellipsoids, Drude+2-Lorentz sphere, "
+           "3-D anisotropic + dispersive: %s cells, 12-cell CPML, 16 uniaxial ellipsoids, Drude+2-Lorentz sphere, "
            "x-polarised TFSF plane wave at 550 nm, DFT flux box x 150 freqs", 256, "config2"),
     "c1": ("Gcell-updates/s (FP32/FP64-split, 2-D TMz 400^2)",
-           "2-D TMz: %d^2 cells, 20-cell CPML, dielectric disk, Ez point source, 8 point detectors, flux line x 100 freqs",
+           "2-D TMz: %s cells, 20-cell CPML, dielectric disk, Ez point source, 8 point detectors, flux line x 100 freqs",
            400, "config1"),
     "c3": ("Gcell-updates/s (FP32/FP64-split fields, FP64 density matrices, 3-D Maxwell-Liouville 192^3)",
-           "3-D Maxwell-Liouville: %d^3 cells, 12-cell CPML, 20-cell slab of 3-level ladder emitters (9 ensemble members "
+           "3-D Maxwell-Liouville: %s cells, 12-cell CPML, 20-cell slab of 3-level ladder emitters (9 ensemble members "
            "per cell from 20 meV Gaussian broadening), 1e26 m^-3, Ez plane source at 2.1 eV, flux plane x 50 freqs",
            192, "config3"),
+    "c5": ("Gcell-updates/s (FP32/FP64-split fields, FP64 density matrices, 3-D mixed 640x640x320)",
+           "3-D mixed: %s cells, dx=4 nm, 16-cell CPML, 16 uniaxial ellipsoids, Drude film, 10-cell sheet of 4-level "
+           "emitters (1e26 m^-3), p-polarised TFSF pulse along (1,1,3) at 550 nm, 6 DFT flux planes x 200 freqs",
+           640, "config5"),
 }
+
+# Config 5's CPU samples and its FP64-vs-split error check run on a 160 x 160 x 80 crop of
+# the same scene (the full 131 M-cell grid needs minutes of host set-up per oracle run).
+C5_CROP = dict(n=160, nz=80, pml=8, nell=4, film_cells=4, sheet_cells=4)
+C5_CROP_STEPS = 1600  # the pulse has passed every flux plane of the crop by then
+
+
+def _dims(name, n):
+    if name == "c1":
+        return "%d^2" % n
+    if name == "c5":
+        return "%dx%dx%d" % (n, n, n // 2)
+    return "%d^3" % n
 
 
 def _workload(n, steps, name="c2"):
     from chiml_gb300 import configs
+    if name == "c5":
+        return configs.config5(n=n, nz=n // 2, steps=steps)
     return getattr(configs, WORKLOADS[name][3])(n=n, steps=steps)
+
+
+def _cpu_sample_config(args, work, cfg_path, steps):
+    """(config path, description) of the input the CPU legs time: the workload itself, or
+    for c5 the crop."""
+    if args.workload != "c5":
+        return cfg_path, "the full workload"
+    from chiml_gb300 import configs
+    path = configs.write_json(configs.config5(steps=steps, **C5_CROP), os.path.join(work, "crop.json"))
+    return path, "the %dx%dx%d crop of the workload" % (C5_CROP["n"], C5_CROP["n"], C5_CROP["nz"])
+
+
+def _crop_error(args, work, local):
+    """Config 5's accuracy check: the crop run to the end in the split form and in FP64;
+    returns the largest relative L2 difference over the flux spectra and over the emitter
+    outputs (populations, polarisation)."""
+    from chiml_gb300 import Simulation, configs
+    from chiml_gb300.outfiles import relative_errors
+    path = configs.write_json(configs.config5(steps=C5_CROP_STEPS, **C5_CROP), os.path.join(work, "crop_check.json"))
+    dirs = {}
+    for prec in ("fp64", "split"):
+        dirs[prec] = os.path.join(work, "crop_" + prec)
+        sim = Simulation(path, precision=prec, device=local, steps_per_graph=args.graph, out_dir=dirs[prec])
+        sim.step()
+        sim.finalize()
+        sim.close()
+    err = relative_errors(dirs["fp64"], dirs["split"])
+    flux = max(v for k, v in err.items() if "flux" in k)
+    emit = max(v for k, v in err.items() if "flux" not in k)
+    return {"crop": "%dx%dx%d" % (C5_CROP["n"], C5_CROP["n"], C5_CROP["nz"]), "steps": C5_CROP_STEPS,
+            "flux_rel_l2_max": float("%.3g" % flux), "emitter_rel_l2_max": float("%.3g" % emit)}
 
 
 def _time_steps(sim, k, torch):
@@ -218,7 +268,10 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(cfg_path, cells, args.cpu_seconds)
+        cpu_path, what = _cpu_sample_config(args, work, cfg_path, total_steps)
+        cpu = cpu_baseline(cpu_path, what, args.cpu_seconds)
+
+    crop = _crop_error(args, work, local) if (rank == 0 and args.workload == "c5") else None
 
     if rank == 0:
         launches = sp["stats"].kernels_per_step * args.steps
@@ -236,7 +289,7 @@ def run_ours(args):
             "dtype": "f32 fields, f64 DFT accumulators",
             "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.%s)" % WORKLOADS[args.workload][3],
             "config": {
-                "workload": WORKLOADS[args.workload][1] % n,
+                "workload": WORKLOADS[args.workload][1] % _dims(args.workload, n),
                 "cells": cells,
                 "precision": "split",
                 "l2": "inputs larger than L2 (%.0f MB of field state vs 129 MB L2)" % (sp["stats"].device_bytes / 1e6),
@@ -259,17 +312,21 @@ def run_ours(args):
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
+        if crop:
+            line["fp64_crop_error"] = crop
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
 
 
-def cpu_baseline(cfg_path, cells, seconds):
-    """The oracle (FP64 CPU port of the reference loop) on the machine's host cores, on a bounded sample."""
+def cpu_baseline(cfg_path, what, seconds):
+    """The oracle (FP64 CPU port of the reference loop) on the machine's host cores, on a bounded
+    sample: as many steps of cfg_path as fit in ``seconds``."""
     import oracle
     from chiml_gb300 import build
     build.build_oracle()
     sim = oracle.OracleSim(cfg_path)
+    cells = sim.cells_physical()
     done = sim.step(1)
     t0 = time.perf_counter()
     n = 0
@@ -280,7 +337,7 @@ def cpu_baseline(cfg_path, cells, seconds):
     sim.close()
     v = cells * n / dt / 1e9
     return {"value": round(v, 5), "unit": "Gcell-updates/s", "cores": oracle.threads(), "kind": "port",
-            "sample": "%d steps of the full %d-cell workload in FP64 (setup excluded), %.1f s" % (n, cells, dt)}
+            "sample": "%d steps of %s (%d cells) in FP64 (setup excluded), %.1f s" % (n, what, cells, dt)}
 
 
 def run_reference(args):
@@ -293,9 +350,10 @@ def run_reference(args):
     work = tempfile.mkdtemp(prefix="chiml_ref_")
     total = args.warmup + args.steps + 2
     cfg_path = configs.write_json(_workload(args.n, total, args.workload), os.path.join(work, "in.json"))
+    cfg_path, what = _cpu_sample_config(args, work, cfg_path, total)
     sim = oracle.OracleSim(cfg_path)
     sim.step(args.warmup)
-    cells = (args.n) ** (2 if args.workload == "c1" else 3)
+    cells = sim.cells_physical()
     per_step = []
     t_all = time.perf_counter()
     for _ in range(args.steps):
@@ -319,9 +377,9 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.%s)" % WORKLOADS[args.workload][3],
-        "config": {"workload": WORKLOADS[args.workload][1] % args.n, "cells": cells},
+        "config": {"workload": WORKLOADS[args.workload][1] % _dims(args.workload, args.n), "cells": cells},
         "cpu_baseline": {"value": round(v, 5), "unit": "Gcell-updates/s", "cores": oracle.threads(), "kind": "port",
-                         "sample": "%d timed steps of the full workload after %d warm-up steps" % (args.steps, args.warmup)},
+                         "sample": "%d timed steps of %s after %d warm-up steps" % (args.steps, what, args.warmup)},
         "e2e": {"value": round(v, 5), "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

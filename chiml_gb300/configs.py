@@ -119,13 +119,13 @@ def config1(n=400, pml=20, steps=4000, radius_cells=50, src_gap_cells=60, ndtc=8
 
 
 def tfsf_surface(box, fcen_a, width, psi_deg=0.0, theta_deg=0.0, phi_deg=90.0, m=None, circ=None, pml_thick=12,
-                 loc=(0.0, 0.0, 0.0)):
+                 loc=(0.0, 0.0, 0.0), amp=1.0):
     """One TFSF entry (parallelInputs.cpp:219-408): box size (a units), a Gaussian pulse at
     fcen_a (1/a units) of 1/e time width ``width``, direction from theta/phi or an integer
     vector m, polarisation angle psi (0 = along x for propagation along z), optional
-    circular polarisation ("L" / "R") and the thickness of its 1-D CPML."""
+    circular polarisation ("L" / "R"), the thickness of its 1-D CPML and the peak amplitude."""
     t = {"loc": list(loc), "size": list(box), "theta": theta_deg, "phi": phi_deg, "psi": psi_deg,
-         "PulseList": [_gauss(fcen_a, 1.0 / width, 4.0, 3 * width)], "pmlThick": pml_thick}
+         "PulseList": [_gauss(fcen_a, 1.0 / width, 4.0, 3 * width, amp=amp)], "pmlThick": pml_thick}
     if m is not None:
         t["m"] = list(m)
     if circ:
@@ -232,6 +232,83 @@ def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, c
                           "dtc_class": "txt", "SI": False, "Time_Interval": dt}],
         "FluxList": [{"name": "c3_flux", "loc": [0.0, 0.0, out_z], "size": [inner, inner, 0.0],
                       "lamL": 5.0, "lamR": 7.0, "nfreq": nfreq, "SI": False}],
+    }
+
+
+def config5(n=640, nz=320, pml=16, steps=20000, nell=16, nfreq=200, seed=SEED0 + 5, coupling=C4_COUPLING,
+            mol_den=1e26, sheet_cells=10, film_cells=10, amp=C4_AMPLITUDE):
+    """Large 3-D mixed scene (dx = 4 nm, fields in FP32 in the split form): n x n x nz cells.
+
+    Inside the total-field box of a TFSF surface (``pml`` + 4 cells in from the edges): a
+    ``film_cells``-thick Drude metal film (wp = 9 eV, gamma = 0.07 eV) below the middle, a
+    ``sheet_cells``-thick sheet of four-level ladder emitters above it (transitions at 1.9,
+    2.0 and 2.3 eV, FP64 density matrices, z dipoles whose adjacent-level couplings are drawn
+    from 0.5-1.5 x ``coupling``, the seeded stand-in for 5-15 D dipoles; the reference has one
+    dipole operator per emitter object, so the draw is per transition, not per cell), and
+    ``nell`` seeded uniaxial ellipsoids between the two, built as in config 2. The wave is a
+    p-polarised Gaussian pulse at 550 nm along m = (1, 1, 3) (25 degrees off the film
+    normal, so its E field has a z component that drives the emitters), peak ``amp``. Six
+    DFT flux planes of ``nfreq`` frequencies, three below the film and three above the
+    sheet."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    dx = 0.04
+    dt = 0.5 * dx / math.sqrt(3.0)
+    sx = (n - 1) * dx
+    sz = (nz - 1) * dx
+    hx, hz = sx / 2, sz / 2
+    box_x = hx - (pml + 4) * dx           # half sizes of the TFSF box
+    box_z = hz - (pml + 4) * dx
+    cell = lambda v: round(v / dx) * dx
+    film_z = cell(-0.55 * box_z)
+    sheet_z = cell(0.55 * box_z)
+    lateral = 2 * (hx - (pml + 12) * dx)
+    inner_x = hx - (pml + 6) * dx
+    room_z = 0.55 * box_z - 0.5 * max(film_cells, sheet_cells) * dx - dx
+    objs = []
+    for _ in range(nell):
+        semi = rng.uniform(10, 40, size=3) * dx * (n / 640.0)
+        e1, e2 = float(rng.uniform(1.5, 4.0)), float(rng.uniform(1.5, 4.0))
+        eps_o, eps_e = min(e1, e2), max(e1, e2)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        lim = np.maximum(np.array([inner_x, inner_x, room_z]) - semi.max(), 0.0)
+        c = rng.uniform(-lim, lim)
+        tmp = np.array([1.0, 0.0, 0.0]) if abs(axis[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        u1 = np.cross(axis, tmp)
+        u1 /= np.linalg.norm(u1)
+        u2 = np.cross(axis, u1)
+        pols = [{"gamma": 0.01, "omega": 5.0 * A / 550e-9, "sigma_p": eps_e - eps_o, "dipOrE": "unidirectional",
+                 "dirDipE": [float(v) for v in axis]}] if eps_e > eps_o else []
+        objs.append(_obj("ellipsoid", [float(v) for v in c], size=[float(2 * s) for s in semi], material="custom",
+                         eps=eps_o, pols=pols, unit_vectors=[{"uvec": [float(v) for v in u]} for u in (axis, u1, u2)]))
+    objs.append(_obj("block", [0.0, 0.0, film_z], size=[lateral, lateral, film_cells * dx], material="custom",
+                     eps=1.0, pols=drude_lorentz_pols(9.0, [(1.0, 0.07, 0.0)])))
+    nlev = 4
+    cpl = np.zeros((nlev, nlev))
+    for a in range(nlev - 1):
+        cpl[a, a + 1] = cpl[a + 1, a] = coupling * float(rng.uniform(0.5, 1.5))
+    lv = [emitter_level(0.0), emitter_level(1.9), emitter_level(3.9), emitter_level(6.2)]
+    relax = [(1, 0, 1e12, 2e13), (2, 1, 1e12, 2e13), (3, 2, 1e12, 2e13)]
+    objs.append(emitter_obj("block", [0.0, 0.0, sheet_z], [(0, 0), (1, 0), (2, 0), (3, 0)], lv,
+                            [float(v) for v in cpl.ravel()], relax, mol_den, eps=1.0, dtc_levs=[5, 10, 15],
+                            output_pol="c5_pol.dat", dtc_base="c5_qe_", size=[lateral, lateral, sheet_cells * dx]))
+    width = 5e-15 / T_UNIT
+    fl = 2 * (hx - (pml + 6) * dx)
+    planes = []
+    for k, zf in enumerate((-0.94, -0.87, -0.8, 0.8, 0.87, 0.94)):
+        planes.append({"name": "c5_flux%d" % k, "loc": [0.0, 0.0, cell(zf * box_z)], "size": [fl, fl, 0.0],
+                       "lamL": 4.0, "lamR": 7.0, "nfreq": nfreq, "SI": False})
+    tf = tfsf_surface([2 * box_x, 2 * box_x, 2 * box_z], A / 550e-9, width, psi_deg=90.0, m=(1, 1, 3),
+                      pml_thick=pml, amp=amp)
+    return {
+        "CompCell": {"size": [sx, sx, sz], "stepSize": [dx, dx, dx], "dt": dt, "tLim": _tlim(steps, dt),
+                     "a": A, "pol": "Ex", "PBC": False, "InputMaps_x": [], "InputMaps_y": [], "InputMaps_z": []},
+        "PML": {"thickness": [pml * dx] * 3, "m": 3.0, "ma": 1.0, "sigOptRat": 1.0, "kappaMax": 1.0, "aMax": 0.0},
+        "SourceList": [],
+        "TFSF": [tf],
+        "ObjectList": objs,
+        "DetectorList": [],
+        "FluxList": planes,
     }
 
 

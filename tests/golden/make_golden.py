@@ -164,6 +164,12 @@ def _freq_2d():
     return _freq_dets(_tfsf_2d_te(), [("Ey", (0.2, 0.2, 0.0), False, False, 1), ("H_pow", (0.1, 0.1, 0.0), True, True, 1)])
 
 
+def _c5_small():
+    """Config 5 in miniature: three uniaxial ellipsoids, the Drude film, the four-level emitter
+    sheet, the oblique p-polarised TFSF wave and the six flux planes, at 40 x 40 x 48 cells."""
+    return configs.config5(n=40, nz=48, pml=6, steps=480, nell=3, nfreq=5, sheet_cells=2, film_cells=2)
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -179,6 +185,7 @@ CASES = {
     "tfsf_2d_te": _tfsf_2d_te,
     "freq_3d": _freq_3d,
     "freq_2d": _freq_2d,
+    "c5_small": _c5_small,
 }
 
 
