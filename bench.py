@@ -264,7 +264,9 @@ def run_ours(args):
         sim.close()
         e2e = {"value": cells * args.steps / (t1 - t0) / 1e9, "unit": "Gcell-updates/s",
                "h2d_bytes_per_step": s.h2d_bytes / args.steps, "d2h_bytes_per_step": s.d2h_bytes / args.steps,
-               "seconds": t1 - t0, "includes": "JSON read, plan build, upload, steps, download, file writes"}
+               "seconds": t1 - t0, "includes": "JSON read, plan build, upload, steps, flux integration, download, file writes",
+               "seconds_plan": round(s.seconds_plan, 3), "seconds_upload": round(s.seconds_upload, 3),
+               "seconds_finalize": round(s.seconds_finalize, 3)}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

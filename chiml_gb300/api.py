@@ -59,6 +59,10 @@ class Stats(ctypes.Structure):
         ("n_flux_regions", ctypes.c_int32),
         ("n_emitters", ctypes.c_int32),
         ("n_tfsf", ctypes.c_int32),
+        ("reserved2", ctypes.c_int32),
+        ("seconds_plan", ctypes.c_double),
+        ("seconds_upload", ctypes.c_double),
+        ("seconds_finalize", ctypes.c_double),
     ]
 
 

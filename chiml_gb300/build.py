@@ -55,7 +55,7 @@ def build_engine(force=False):
         return LIB_ENGINE
     objs = []
     jobs = []
-    for name in ("fdtd_kernels", "box_noalloc", "emitter_kernels", "tfsf_kernels"):
+    for name in ("fdtd_kernels", "box_noalloc", "emitter_kernels", "tfsf_kernels", "flux_kernels"):
         cu = os.path.join(CSRC, "kernels", name + ".cu")
         o = os.path.join(BUILD, name + ".o")
         jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu, "-o", o])

@@ -20,6 +20,7 @@
 #include "kernels/box_noalloc.hpp"
 #include "kernels/emitter_device.hpp"
 #include "kernels/fdtd_device.hpp"
+#include "kernels/flux_device.hpp"
 #include "kernels/tfsf_device.hpp"
 
 using namespace chiml;
@@ -152,17 +153,11 @@ public:
         }
         ck(cudaStreamSynchronize(stream_), "DFT flush");
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
-            const FluxPlan& fp = P.fluxes[q];
-            std::size_t n = static_cast<std::size_t>(fp.npts) * fp.spec.freqList.size();
-            std::vector<double> re(n), im(n);
-            if (n) {
-                ck(cudaMemcpy(re.data(), dft_[q].re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H flux");
-                ck(cudaMemcpy(im.data(), dft_[q].im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H flux");
-            }
-            d2h_ += 2.0 * n * sizeof(double);
-            R.fluxRe.push_back(std::move(re));
-            R.fluxIm.push_back(std::move(im));
-            R.fluxSamples.push_back(stepsDone_ / fp.spec.timeInt + 1);
+            const int nt = stepsDone_ / P.fluxes[q].spec.timeInt + 1;
+            R.fluxFaces.push_back(fluxFacesOnDevice(q, nt));
+            R.fluxRe.emplace_back();
+            R.fluxIm.emplace_back();
+            R.fluxSamples.push_back(nt);
         }
         for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
             const dev::DftTable<T>& d = dft_[P.fluxes.size() + k];
@@ -222,6 +217,55 @@ public:
         write_freq_detectors(P, R, outDir_);
         write_emitters(P, R, outDir_);
         finalized_ = true;
+    }
+
+    // The integrated flux of every face of flux q, [freq * nFaces + face], evaluated from the
+    // accumulators on the device; only these values are copied back.
+    std::vector<cplx> fluxFacesOnDevice(std::size_t q, int nt) {
+        const FluxPlan& fp = P.fluxes[q];
+        const int nfreq = static_cast<int>(fp.spec.freqList.size());
+        const std::vector<FluxFaceMap> maps = flux_face_maps(P, q);
+        const int nFaces = static_cast<int>(maps.size());
+        std::vector<cplx> res(static_cast<std::size_t>(nfreq) * nFaces, cplx(0.0, 0.0));
+        if (nFaces == 0 || nfreq == 0) return res;
+        DevMem tmp;  // freed on return
+        std::vector<dev::FluxFaceDev> faces(static_cast<std::size_t>(nFaces));
+        std::vector<int4> tiles;
+        for (int v = 0; v < nFaces; ++v) {
+            const FluxFaceMap& m = maps[v];
+            dev::FluxFaceDev& F = faces[v];
+            F.nx = m.nx;
+            F.sz = m.sz;
+            for (int w = 0; w < 4; ++w) {
+                F.has[w] = m.has[w] ? 1 : 0;
+                F.start[w] = m.has[w] ? tmp.upload(m.start[w]) : nullptr;
+                F.pt[w] = m.has[w] ? tmp.upload(m.pt[w]) : nullptr;
+                F.scale[w] = m.has[w] ? tmp.upload(m.scale[w]) : nullptr;
+                for (long long p : m.pt[w])
+                    if (p < 0 || p >= fp.npts) throw std::logic_error("flux map point outside the accumulators");
+            }
+            F.wx = tmp.upload(m.wx);
+            F.wy = tmp.upload(m.wy);
+            F.pref = m.pref;
+            F.firstTile = static_cast<int>(tiles.size());
+            for (int s0 = 0; s0 < m.sz; s0 += dev::kFluxTile) tiles.push_back(make_int4(v, s0, std::min(m.sz, s0 + dev::kFluxTile), 0));
+            F.nTiles = static_cast<int>(tiles.size()) - F.firstTile;
+        }
+        const dev::FluxFaceDev* dFaces = tmp.upload(faces);
+        const int4* dTiles = tmp.upload(tiles);
+        double2* partial = tmp.alloc<double2>(tiles.size() * static_cast<std::size_t>(nfreq), false);
+        double2* out = tmp.alloc<double2>(res.size(), false);
+        const double nt2 = std::pow(static_cast<double>(nt), 2.0);
+        dev::launch_flux_faces(dFaces, nFaces, dTiles, static_cast<int>(tiles.size()), nfreq, dft_[q].re, dft_[q].im, nt2, partial,
+                               out, stream_);
+        ck(cudaGetLastError(), "flux integration launch");
+        ck(cudaStreamSynchronize(stream_), "flux integration");
+        std::vector<double2> h(res.size());
+        ck(cudaMemcpy(h.data(), out, h.size() * sizeof(double2), cudaMemcpyDeviceToHost), "D2H flux faces");
+        d2h_ += static_cast<double>(h.size() * sizeof(double2));
+        mem_.h2d += tmp.h2d;
+        for (std::size_t i = 0; i < h.size(); ++i) res[i] = cplx(h[i].x, h[i].y);
+        return res;
     }
 
     void getField(int comp, double* out) override {
@@ -1456,7 +1500,12 @@ struct Handle {
     std::unique_ptr<SimBase> sim;
     std::string err;
     double h2d = 0, d2h = 0;
+    double tPlan = 0, tUpload = 0, tFinalize = 0;  // wall seconds of create and finalize
 };
+
+double wall_seconds() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 chiml_status status_of(const std::exception& e) {
     if (dynamic_cast<const UnsupportedError*>(&e)) return CHIML_E_UNSUPPORTED;
@@ -1488,12 +1537,16 @@ chiml_status chiml_create(const char* json_path, const chiml_options* opt, chiml
     if (opt) o = *opt;
     try {
         if (!json_path) throw InputError("no input file");
+        const double t0 = wall_seconds();
         Inputs in = read_inputs_file(json_path);
         Plan P = build_plan(in);
+        const double t1 = wall_seconds();
         std::unique_ptr<chiml_sim> s(new chiml_sim());
         if (o.precision == CHIML_PREC_FP64) s->h.sim.reset(new Sim<double>(std::move(P), o));
         else if (o.precision == CHIML_PREC_SPLIT) s->h.sim.reset(new Sim<float>(std::move(P), o));
         else throw InputError("unknown precision mode");
+        s->h.tPlan = t1 - t0;
+        s->h.tUpload = wall_seconds() - t1;
         *out = s.release();
         return CHIML_OK;
     } catch (const std::exception& e) {
@@ -1527,7 +1580,9 @@ chiml_status chiml_sync(chiml_sim* sim) {
 chiml_status chiml_finalize(chiml_sim* sim) {
     if (!sim) return CHIML_E_STATE;
     try {
+        const double t0 = wall_seconds();
         sim->h.sim->finalize();
+        sim->h.tFinalize = wall_seconds() - t0;
         return CHIML_OK;
     } catch (const std::exception& e) {
         sim->h.err = e.what();
@@ -1545,6 +1600,9 @@ const char* chiml_last_error(const chiml_sim* sim) {
 chiml_status chiml_query(const chiml_sim* sim, chiml_stats* out) {
     if (!sim || !out) return CHIML_E_STATE;
     sim->h.sim->fillStats(out);
+    out->seconds_plan = sim->h.tPlan;
+    out->seconds_upload = sim->h.tUpload;
+    out->seconds_finalize = sim->h.tFinalize;
     return CHIML_OK;
 }
 

@@ -156,116 +156,206 @@ cx simps2D(CGrid& g) {
 
 }  // namespace
 
-void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) {
+std::vector<double> simps_weights(int n, double d) {
+    std::vector<double> w(static_cast<std::size_t>(std::max(n, 0)), 0.0);
+    if (n == 1) {
+        w[0] = d;
+    } else if (n % 2 == 0) {
+        for (int ii = 0; ii < (n - 2) / 2; ii++) {
+            w[ii * 2] += d / 6.0;
+            w[ii * 2 + 1] += d / 6.0 * 4.0;
+            w[(ii + 1) * 2] += d / 6.0;
+        }
+        for (int ii = 1; ii < n / 2; ii++) {
+            w[ii * 2 - 1] += d / 6.0;
+            w[ii * 2] += d / 6.0 * 4.0;
+            w[ii * 2 + 1] += d / 6.0;
+        }
+        for (int k : {0, 1, n - 1, n - 2}) w[k] += d / 4.0;
+    } else {
+        for (int ii = 0; ii < (n - 1) / 2; ii++) {
+            w[ii * 2] += d / 3.0;
+            w[ii * 2 + 1] += d / 3.0 * 4.0;
+            w[(ii + 1) * 2] += d / 3.0;
+        }
+    }
+    return w;
+}
+
+std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
     const Dims& D = P.dims;
     auto lnv = [&](int ax) { return ax == 0 ? D.lx : (ax == 1 ? D.ly : D.lz); };
+    const FluxPlan& fp = P.fluxes[q];
+    const auto& loc_ = fp.spec.loc;
+    std::vector<FluxFaceMap> maps;
+    for (const FluxFace& f : fp.faces) {
+        FluxFaceMap m;
+        // the face grids are (freq, y = faceSz[transCor1], z = faceSz[cor]); the product grid
+        // of the integration is (x = faceSz[cor], y = faceSz[transCor1])
+        m.nx = f.faceSz[f.cor];
+        m.ny = f.faceSz[f.transCor1];
+        m.dx = P.in.d[f.cor];
+        m.dy = P.in.d[f.transCor1];
+        m.sz = f.sz;
+        m.pref = fp.fluxConv * f.weight;
+        if (static_cast<long long>(m.sz) > static_cast<long long>(m.nx) * m.ny)
+            throw InputError("flux face larger than its integration grid");
+        const long long npt = static_cast<long long>(m.nx) * m.ny;
+        std::array<int, 2> addIndex = {std::max(0, 0 - loc_[f.transCor1]), std::max(0, 0 - loc_[f.cor])};
+        const std::vector<int>* lists[4] = {&f.Ej, &f.Ek, &f.Hj, &f.Hk};
+        int ej, ek, hj, hk;
+        if (f.corI == 0) { ej = EY; hj = HY; ek = EZ; hk = HZ; }
+        else if (f.corI == 1) { ej = EZ; hj = HZ; ek = EX; hk = HX; }
+        else { ej = EX; hj = HX; ek = EY; hk = HY; }
+        const int comps[4] = {ej, ek, hj, hk};
+        const int oth[4] = {1, 0, 3, 2};
+        for (int w = 0; w < 4; ++w) {
+            if (lists[w]->empty()) continue;
+            m.has[w] = true;
+            // act / trans fields and the J/K coordinate of constructSzProcOffsetLists (Real
+            // flux): the complementary field exists when its component is present
+            const int corJK = (w == 0 || w == 3) ? f.corJ : f.corK;
+            const bool act = P.comp[comps[w]].present;
+            const bool trans = P.comp[comps[oth[w]]].present;
+            std::vector<std::vector<std::pair<long long, double>>> cellTerms(static_cast<std::size_t>(npt));
+            const std::vector<int>& lst = *lists[w];
+            const double scaleDen = static_cast<double>(lst.size());
+            for (std::size_t dd = 0; dd < lst.size(); ++dd) {
+                const FreqStore& st = fp.stores[lst[dd]];
+                if (st.outN[0] == 0) continue;  // outside the grid: no out grid
+                std::vector<std::array<int, 9>> so;
+                const int oy = st.outN[1], oz = st.outN[2];
+                if (act && trans) {
+                    so.assign(2, {0, oy, oz, 0, 0, 0, 0, 0, 0});
+                    if (f.cor == corJK) {
+                        if (addIndex[1] == 0) {
+                            so[1][6] = 1;
+                            so[1][4] = 1;
+                        } else {
+                            so[0][8] = 1;
+                        }
+                        if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][4] = 1;
+                    } else if (f.transCor1 == corJK) {
+                        if (addIndex[0] == 0) {
+                            so[1][5] = 1;
+                            so[1][3] = 1;
+                        } else {
+                            so[0][7] = 1;
+                        }
+                        if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][3] = 1;
+                    }
+                } else {
+                    so.assign(1, {0, oy, oz, 0, 0, 0, 0, 0, 0});
+                }
+                const double scale = 1.0 / (scaleDen * static_cast<double>(so.size()));
+                for (auto& o : so)
+                    for (int jj = 0; jj < o[2] - o[4]; ++jj)
+                        for (int ii = 0; ii < o[1] - o[3]; ++ii) {
+                            const long long pt = st.accOffset + (jj + o[6]) + static_cast<long long>(ii + o[5]) * oz;
+                            const int y = ii + addIndex[0] + o[7], z = jj + addIndex[1] + o[8];
+                            if (y < 0 || z < 0 || y >= m.ny || z >= m.nx)
+                                throw InputError("flux combination index out of range (the reference asserts here)");
+                            cellTerms[static_cast<std::size_t>(z + static_cast<long long>(m.nx) * y)].emplace_back(pt, scale);
+                        }
+            }
+            m.start[w].assign(static_cast<std::size_t>(npt) + 1, 0);
+            for (long long c = 0; c < npt; ++c) m.start[w][c + 1] = m.start[w][c] + static_cast<long long>(cellTerms[c].size());
+            m.pt[w].reserve(static_cast<std::size_t>(m.start[w][npt]));
+            m.scale[w].reserve(static_cast<std::size_t>(m.start[w][npt]));
+            for (auto& ct : cellTerms)
+                for (auto& t : ct) {
+                    m.pt[w].push_back(t.first);
+                    m.scale[w].push_back(t.second);
+                }
+        }
+        // getFlux pairs the E grid with the complementary H grid: Ej with Hk, Ek with Hj
+        if (!(m.has[0] || m.has[1]) || (m.has[0] && !m.has[3]) || (!m.has[0] && !m.has[2]) || (m.has[1] && !m.has[2]))
+            throw InputError("flux face without field pairs");
+        if (m.nx <= 1 && m.ny <= 1) throw UnsupportedError("a single-point flux face has no defined integral in the reference");
+        m.wx = m.nx > 1 ? simps_weights(m.nx, m.dx) : std::vector<double>(1, 1.0);
+        m.wy = m.ny > 1 ? simps_weights(m.ny, m.dy) : std::vector<double>(1, 1.0);
+        maps.push_back(std::move(m));
+    }
+    return maps;
+}
+
+std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps,
+                                   const std::vector<double>& re, const std::vector<double>& im, int nt) {
+    const FluxPlan& fp = P.fluxes[q];
+    const int nfreq = static_cast<int>(fp.spec.freqList.size());
+    const std::size_t nFaces = maps.size();
+    std::vector<cplx> out(static_cast<std::size_t>(nfreq) * nFaces, cplx(0.0, 0.0));
+    const double nt2 = std::pow(static_cast<double>(nt), 2.0);
+    for (std::size_t vv = 0; vv < nFaces; ++vv) {
+        const FluxFaceMap& m = maps[vv];
+        const long long npt = static_cast<long long>(m.nx) * m.ny;
+        // the face grids [point][freq], summed in the reference's order
+        std::vector<cx> g[4];
+        for (int w = 0; w < 4; ++w) {
+            if (!m.has[w]) continue;
+            g[w].assign(static_cast<std::size_t>(npt) * nfreq, cx(0.0, 0.0));
+#pragma omp parallel for schedule(static)
+            for (long long c = 0; c < npt; ++c)
+                for (long long k = m.start[w][c]; k < m.start[w][c + 1]; ++k) {
+                    const std::size_t b = static_cast<std::size_t>(m.pt[w][k]) * nfreq;
+                    for (int fq = 0; fq < nfreq; ++fq)
+                        g[w][static_cast<std::size_t>(c) * nfreq + fq] += m.scale[w][k] * cx(re[b + fq], im[b + fq]);
+                }
+        }
+        const cx* Ej = m.has[0] ? g[0].data() : nullptr;
+        const cx* Ek = m.has[1] ? g[1].data() : nullptr;
+        const cx* Hj = m.has[2] ? g[2].data() : nullptr;
+        const cx* Hk = m.has[3] ? g[3].data() : nullptr;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int ff = 0; ff < nfreq; ++ff) {
+            CGrid ijk(m.nx, m.ny, 1, m.dx, m.dy, 1.0);
+            CGrid ikj(ijk.nx, ijk.ny, 1, ijk.dx, ijk.dy, 1.0);
+            if (Ej)
+                for (int s = 0; s < m.sz; ++s) {
+                    cx e = Ej[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                    cx h = Hk[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                    ijk.v[s] = e * std::conj(h) / nt2;
+                }
+            if (Ek) {
+                for (int s = 0; s < m.sz; ++s) {
+                    cx e = Ek[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                    cx h = Hj[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
+                    ikj.v[s] = e * std::conj(h) / nt2;
+                }
+                for (std::size_t s = 0; s < ijk.v.size(); ++s) ijk.v[s] += cx(-1.0) * ikj.v[s];
+            }
+            out[static_cast<std::size_t>(ff) * nFaces + vv] = fp.fluxConv * fp.faces[vv].weight * simps2D(ijk);
+        }
+    }
+    return out;
+}
+
+void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) {
     for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
         const FluxPlan& fp = P.fluxes[q];
         const int nfreq = static_cast<int>(fp.spec.freqList.size());
-        const std::vector<double>& re = R.fluxRe[q];
-        const std::vector<double>& im = R.fluxIm[q];
-        const int nt = R.fluxSamples[q];
-        const auto& loc_ = fp.spec.loc;
-        std::vector<std::unique_ptr<CGrid>> Ef[2], Hf[2];  // [J/K][face]
-        for (const FluxFace& f : fp.faces) {
-            std::array<int, 2> addIndex = {std::max(0, 0 - loc_[f.transCor1]), std::max(0, 0 - loc_[f.cor])};
-            const std::vector<int>* lists[4] = {&f.Ej, &f.Ek, &f.Hj, &f.Hk};
-            std::unique_ptr<CGrid> grids[4];
-            for (int w = 0; w < 4; ++w) {
-                if (lists[w]->empty()) continue;
-                grids[w].reset(new CGrid(nfreq, f.faceSz[f.transCor1], f.faceSz[f.cor], fp.dLam, P.in.d[f.transCor1], P.in.d[f.cor]));
-                // act / trans fields and the J/K coordinate of constructSzProcOffsetLists (Real flux)
-                bool act = true, trans = false;
-                int corJK = 0;
-                int actComp = P.fluxes[q].stores[(*lists[w])[0]].comp;
-                (void)actComp;
-                const std::vector<int>* other = nullptr;
-                if (w == 0) { other = lists[1]; corJK = f.corJ; }
-                if (w == 1) { other = lists[0]; corJK = f.corK; }
-                if (w == 2) { other = lists[3]; corJK = f.corK; }
-                if (w == 3) { other = lists[2]; corJK = f.corJ; }
-                // the complementary field exists when its component is present
-                {
-                    int ej, ek, hj, hk;
-                    if (f.corI == 0) { ej = EY; hj = HY; ek = EZ; hk = HZ; }
-                    else if (f.corI == 1) { ej = EZ; hj = HZ; ek = EX; hk = HX; }
-                    else { ej = EX; hj = HX; ek = EY; hk = HY; }
-                    int comps[4] = {ej, ek, hj, hk};
-                    int oth[4] = {1, 0, 3, 2};
-                    act = P.comp[comps[w]].present;
-                    trans = P.comp[comps[oth[w]]].present;
-                }
-                (void)other;
-                const std::vector<int>& lst = *lists[w];
-                const double scaleDen = static_cast<double>(lst.size());
-                for (std::size_t dd = 0; dd < lst.size(); ++dd) {
-                    const FreqStore& st = fp.stores[lst[dd]];
-                    if (st.outN[0] == 0) continue;  // outside the grid: no out grid
-                    std::vector<std::array<int, 9>> so;
-                    const int oy = st.outN[1], oz = st.outN[2];
-                    if (act && trans) {
-                        so.assign(2, {0, oy, oz, 0, 0, 0, 0, 0, 0});
-                        if (f.cor == corJK) {
-                            if (addIndex[1] == 0) {
-                                so[1][6] = 1;
-                                so[1][4] = 1;
-                            } else {
-                                so[0][8] = 1;
-                            }
-                            if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][4] = 1;
-                        } else if (f.transCor1 == corJK) {
-                            if (addIndex[0] == 0) {
-                                so[1][5] = 1;
-                                so[1][3] = 1;
-                            } else {
-                                so[0][7] = 1;
-                            }
-                            if ((0 <= st.loc[corJK] + st.sz[corJK] - 1) && (st.loc[corJK] + st.sz[corJK] - 1 < lnv(corJK) - 2)) so[0][3] = 1;
-                        }
-                    } else {
-                        so.assign(1, {0, oy, oz, 0, 0, 0, 0, 0, 0});
-                    }
-                    const double scale = 1.0 / (scaleDen * static_cast<double>(so.size()));
-                    for (auto& o : so)
-                        for (int jj = 0; jj < o[2] - o[4]; ++jj)
-                            for (int ii = 0; ii < o[1] - o[3]; ++ii) {
-                                long long pt = st.accOffset + (jj + o[6]) + static_cast<long long>(ii + o[5]) * oz;
-                                for (int fq = 0; fq < nfreq; ++fq) {
-                                    cx v(re[static_cast<std::size_t>(pt) * nfreq + fq], im[static_cast<std::size_t>(pt) * nfreq + fq]);
-                                    grids[w]->at(fq, ii + addIndex[0] + o[7], jj + addIndex[1] + o[8]) += scale * v;
-                                }
-                            }
-                }
-            }
-            Ef[0].push_back(std::move(grids[0]));
-            Ef[1].push_back(std::move(grids[1]));
-            Hf[0].push_back(std::move(grids[2]));
-            Hf[1].push_back(std::move(grids[3]));
-        }
-        // getFlux (parallelFlux.hpp:406-545)
-        const std::string path = out_path(outDir, fp.spec.name + ".dat");
-        std::ofstream f(path);
-        if (!f) throw InputError("cannot open flux output " + path);
         const std::size_t nFaces = fp.faces.size();
-        f << "#" << std::setw(16) << "freq\tabs(incd)\treal(incd)\timag(incd)";
-        if (nFaces > 1) {
-            f << std::setw(16) << "\tabs(right)\treal(right)\timag(right)\tabs(left)\treal(left)\timag(left)\tabs(top)\treal(top)\timag(top)\tabs(bot)\treal(bot)\timag(bot)";
-            if (fp.spec.sz[0] > 1 && fp.spec.sz[1] > 1 && fp.spec.sz[2] > 1)
-                f << std::setw(16) << "\tabs(front)\treal(front)\timag(front)\tabs(back)\treal(back)\timag(back)";
+        std::vector<cplx> faceVal;
+        if (q < R.fluxFaces.size() && !R.fluxFaces[q].empty()) {
+            faceVal = R.fluxFaces[q];
+        } else {
+            faceVal = flux_face_values(P, q, flux_face_maps(P, q), R.fluxRe[q], R.fluxIm[q], R.fluxSamples[q]);
         }
-        f << std::setw(16) << "freq\tabs(total)\treal(total)\timag(total)\n";
+        if (faceVal.size() != static_cast<std::size_t>(nfreq) * nFaces) throw InputError("flux face values of the wrong size");
+        const int nt = R.fluxSamples[q];
+        // transform of the recorded incident fields (zero without a TFSF surface): the even
+        // samples, then the odd ones, real parts only (parallelFlux.hpp:457-479)
+        std::vector<cx> incd(static_cast<std::size_t>(nfreq));
+        const std::vector<cplx>* incSer[6] = {&R.incE[0], &R.incE[1], &R.incE[2], &R.incH[0], &R.incH[1], &R.incH[2]};
+        const std::size_t nInc = incSer[0]->size();
         const double tInt = static_cast<double>(fp.spec.timeInt);
+#pragma omp parallel for schedule(dynamic, 1)
         for (int ff = 0; ff < nfreq; ++ff) {
-            cx flux = 0.0;
-            // transform of the recorded incident fields (zero without a TFSF surface): the even
-            // samples, then the odd ones, real parts only (parallelFlux.hpp:457-479)
             cx inc[6] = {0, 0, 0, 0, 0, 0};
-            const std::vector<cplx>* incSer[6] = {&R.incE[0], &R.incE[1], &R.incE[2], &R.incH[0], &R.incH[1], &R.incH[2]};
-            const std::size_t nInc = incSer[0]->size();
             for (int start = 0; start < 2; ++start)
                 for (std::size_t tt = start; tt < nInc; tt += 2) {
                     const cx ph = std::exp(cx(0.0, fp.spec.freqList.at(ff) * static_cast<double>(tt / 2) * (P.dt / tInt)));
-                    for (int q = 0; q < 6; ++q) inc[q] += cx(std::real(0.5 * (*incSer[q])[tt]), 0.0) * ph;
+                    for (int c = 0; c < 6; ++c) inc[c] += cx(std::real(0.5 * (*incSer[c])[tt]), 0.0) * ph;
                 }
             cx flux_incd = std::pow(fp.incdConv[0] * (inc[1] * std::conj(inc[5]) - inc[2] * std::conj(inc[4])) /
                                         (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
@@ -273,40 +363,28 @@ void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) 
                                       (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
             flux_incd += std::pow(fp.incdConv[2] * (inc[0] * std::conj(inc[4]) - inc[1] * std::conj(inc[3])) /
                                       (std::pow(static_cast<double>(nt * fp.spec.timeInt), 2.0)), 2.0);
-            flux_incd = std::sqrt(flux_incd);
+            incd[ff] = std::sqrt(flux_incd);
+        }
+        // getFlux output (parallelFlux.hpp:406-545)
+        const std::string path = out_path(outDir, fp.spec.name + ".dat");
+        std::ofstream f(path);
+        if (!f) throw InputError("cannot open flux output " + path);
+        f << "#" << std::setw(16) << "freq\tabs(incd)\treal(incd)\timag(incd)";
+        if (nFaces > 1) {
+            f << std::setw(16) << "\tabs(right)\treal(right)\timag(right)\tabs(left)\treal(left)\timag(left)\tabs(top)\treal(top)\timag(top)\tabs(bot)\treal(bot)\timag(bot)";
+            if (fp.spec.sz[0] > 1 && fp.spec.sz[1] > 1 && fp.spec.sz[2] > 1)
+                f << std::setw(16) << "\tabs(front)\treal(front)\timag(front)\tabs(back)\treal(back)\timag(back)";
+        }
+        f << std::setw(16) << "freq\tabs(total)\treal(total)\timag(total)\n";
+        for (int ff = 0; ff < nfreq; ++ff) {
+            const cx flux_incd = incd[ff];
             f << std::setw(18) << std::setprecision(15) << fp.freqConv * fp.spec.freqList[ff] << "\t" << std::setw(16)
               << std::setprecision(15) << std::abs(flux_incd) << "\t" << std::setw(16) << std::setprecision(15)
               << std::abs(std::real(flux_incd)) << "\t" << std::setw(16) << std::setprecision(15) << std::imag(flux_incd)
               << "\t";
+            cx flux = 0.0;
             for (std::size_t vv = 0; vv < nFaces; ++vv) {
-                CGrid* Ej = Ef[0][vv].get();
-                CGrid* Ek = Ef[1][vv].get();
-                CGrid* Hj = Hf[0][vv].get();
-                CGrid* Hk = Hf[1][vv].get();
-                CGrid* gE = Ej ? Ej : Ek;
-                CGrid* gH = Ej ? Hk : Hj;
-                if (!gE || !gH) throw InputError("flux face without field pairs");
-                // flux grids are (x = sz[cor], y = sz[transCor1]), spacing (d[cor], d[transCor1])
-                CGrid ijk(gE->nz, gE->ny, 1, gE->dz, gE->dy, 1.0);
-                CGrid ikj(ijk.nx, ijk.ny, 1, ijk.dx, ijk.dy, 1.0);
-                const double nt2 = std::pow(static_cast<double>(nt), 2.0);
-                const int sz = fp.faces[vv].sz;
-                if (Ej) {
-                    for (int s = 0; s < sz; ++s) {
-                        cx e = Ej->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
-                        cx h = Hk->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
-                        ijk.v[s] = e * std::conj(h) / nt2;
-                    }
-                }
-                if (Ek) {
-                    for (int s = 0; s < sz; ++s) {
-                        cx e = Ek->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
-                        cx h = Hj->v[static_cast<std::size_t>(ff) + static_cast<std::size_t>(nfreq) * s];
-                        ikj.v[s] = e * std::conj(h) / nt2;
-                    }
-                    for (std::size_t s = 0; s < ijk.v.size(); ++s) ijk.v[s] += cx(-1.0) * ikj.v[s];
-                }
-                cx tempFlux = fp.fluxConv * fp.faces[vv].weight * simps2D(ijk);
+                const cx tempFlux = faceVal[static_cast<std::size_t>(ff) * nFaces + vv];
                 flux += tempFlux;
                 f << std::setw(16) << std::setprecision(15) << std::abs(tempFlux) << "\t" << std::setw(16)
                   << std::setprecision(15) << std::real(tempFlux) << "\t" << std::setw(16) << std::setprecision(15)

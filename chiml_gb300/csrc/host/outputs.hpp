@@ -17,6 +17,9 @@ struct RunRecord {
     // flux accumulators per flux: re/im [point][freq], and the number of DFT samples
     std::vector<std::vector<double>> fluxRe, fluxIm;
     std::vector<int> fluxSamples;
+    // per flux, optionally: the integrated flux of every face, [freq * nFaces + face]
+    // (computed on the device); when present the accumulators are not needed
+    std::vector<std::vector<cplx>> fluxFaces;
     // per emitter: the total polarisation of each coupled component, one value per step
     // (parallelQE.cpp:41-44 accumP_), and per population detector its events
     std::vector<std::array<std::vector<double>, 3>> emitterP;
@@ -37,7 +40,35 @@ int detector_events(const DetectorPlan& dp, int nSteps);
 
 // Writes every detector file (TXT: parallelDTC_TXT.cpp:13-55; BIN: parallelDTC_BIN.cpp:12-50).
 void write_detectors(const Plan& P, const RunRecord& R, const std::string& outDir, int stepsDone);
-// Combines the flux accumulators and writes "<name>.dat" (parallelFlux.hpp:325-560).
+// The combination and integration of one flux face as data (parallelFlux.hpp:325-405 combine
+// the accumulated points into four face grids Ej, Ek, Hj, Hk; getFlux, :406-545, integrates
+// (Ej conj(Hk) - Ek conj(Hj)) / nt^2 over the face with simps2D). Grid point c = x + nx * y
+// (x along the face's cor axis, y along transCor1) takes, for grid w, the terms
+// [start[w][c], start[w][c + 1]) of (accumulator point, scale), in the reference's order.
+struct FluxFaceMap {
+    int nx = 0, ny = 0, sz = 0;  // integration grid and the points the product fills
+    double dx = 0.0, dy = 0.0;
+    double pref = 1.0;            // fluxConv * face weight
+    bool has[4] = {false, false, false, false};
+    std::vector<long long> start[4];
+    std::vector<long long> pt[4];
+    std::vector<double> scale[4];
+    // simps2D as a linear form: weight of point (x, y) = wx[x] * wy[y] (length 1, weight 1,
+    // along an axis of one point)
+    std::vector<double> wx, wy;
+};
+
+// The weights w with simps(v, n, d) = sum_i w[i] v[i] (parallelFlux.hpp:548-576).
+std::vector<double> simps_weights(int n, double d);
+// The maps of the faces of flux q. Throws where the reference's combination or integration
+// would fail.
+std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q);
+// The integrated flux of every face of flux q from its accumulators, [freq * nFaces + face],
+// in the reference's arithmetic.
+std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps,
+                                   const std::vector<double>& re, const std::vector<double>& im, int nt);
+// Writes "<name>.dat" of every flux (parallelFlux.hpp:325-560) from R.fluxFaces, or from the
+// accumulators where those are absent.
 void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir);
 
 // Writes every frequency-domain detector (parallelDetectorFREQ_Base::toFile / toMap with the

@@ -8,10 +8,13 @@
 // is then checked cell by cell against the literal accumulation.
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <map>
 #include <numeric>
 #include <set>
 #include <tuple>
+
+#include <omp.h>
 
 #include "plan.hpp"
 
@@ -652,7 +655,6 @@ struct Builder {
         std::vector<uint8_t> psiUpd[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
         std::vector<uint8_t> nplain[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
         std::vector<uint8_t> kflag[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
-        std::vector<double> kval[2] = {std::vector<double>(N, 0.0), std::vector<double>(N, 0.0)};
         auto coordOf = [&](long long id, int ax) {
             long long x = id % D.lx;
             long long r = id / D.lx;
@@ -672,7 +674,6 @@ struct Builder {
                     if (e.slab == T.axis) {
                         if (kflag[t][id]) throw UnsupportedError("overlapping CPML slabs along one axis");
                         kflag[t][id] = 1;
-                        kval[t][id] = e.DbField;
                         int a = coordOf(id, T.axis);
                         if (T.kprof[a] != 0.0 && T.kprof[a] != e.DbField)
                             throw UnsupportedError("CPML coefficient is not a function of the normal coordinate");
@@ -704,103 +705,149 @@ struct Builder {
             }
         }
 
-        // build classes
+        // build classes: each cell's class (its update terms and coefficients) is looked up
+        // by key; class ids are given in order of first appearance in the scan order
+        // (y, z, x). Rows of y are scanned in parallel chunks with chunk-local ids, merged
+        // in chunk order (which reproduces the scan order's first appearances) and remapped.
         cp.present = true;
         cp.isE = E;
-        std::map<std::array<double, 16>, int> index;  // key -> class id
+        typedef std::array<double, 16> Key;
         cp.code.assign(N, 0);
         cp.classes.clear();
+        std::map<Key, int> index;  // key -> class id
         {
             // class 0: cells no list updates (the halo and staggered borders); the
             // kernels skip them without touching any neighbour
             ClassInfo none;
             cp.classes.push_back(none);
-            std::array<double, 16> key;
+            Key key;
             key.fill(0.0);
             key[4] = 1.0;  // eps as normalised below for non-dispersive classes
             index[key] = 0;
         }
-        bool anyD = false;
-        std::array<double, 16> lastKey;
-        lastKey.fill(-1.0);
-        int lastId = -1;
-        for (int y = 0; y < D.ly; ++y)
-            for (int z = 0; z < D.lz; ++z)
-                for (int x = 0; x < D.lx; ++x) {
-                    std::size_t id = static_cast<std::size_t>(D.idx(x, y, z));
-                    ClassInfo c;
-                    int o = ph.at(x, y, z);
-                    c.obj = (o < 0) ? 0 : o;
-                    double cellEps = ep.at(x, y, z);
-                    uint8_t kind = curlKind[id];
-                    bool pmlCell = false;
-                    for (int t = 0; t < 2; ++t) pmlCell = pmlCell || npsi[t][id] > 0 || (coef[t][id] != 0.0);
-                    if (kind == L_U || kind == L_D) {
-                        double em = (kind == L_U) ? cellEps : 1.0;
-                        double pref1 = -1.0 * dt / (em * dj), pref2 = -1.0 * dt / (em * dk);
-                        if (tp[0].present) c.cint[0] = pref2;
-                        if (tp[1].present) c.cint[1] = -pref1;
-                        c.toD = (kind == L_D) ? 1 : 0;
-                    }
-                    if (pmlCell) {
-                        uint8_t pmlToD = (E && matInPML) ? 1 : 0;
-                        if (kind != L_NONE && c.toD != pmlToD)
-                            throw UnsupportedError("a cell's interior and CPML updates target different fields");
-                        c.toD = pmlToD;
-                    }
-                    c.lor = lorFlag[id];
-                    c.ordip = ordipFlag[id];
-                    if (c.lor || c.ordip) c.eps = cellEps;
-                    if (c.toD || c.lor || c.ordip) anyD = true;
-                    for (int t = 0; t < 2; ++t) {
-                        if (!tp[t].present) {
-                            if (coef[t][id] != 0.0 || npsi[t][id] || psiUpd[t][id])
-                                throw InputError("CPML term without a neighbour field");
-                            continue;
+        const int nChunks = std::max(1, std::min(D.ly, 64));
+        std::vector<std::vector<std::pair<Key, ClassInfo>>> local(static_cast<std::size_t>(nChunks));
+        std::vector<std::exception_ptr> chunkErr(static_cast<std::size_t>(nChunks));
+        std::vector<char> chunkAnyD(static_cast<std::size_t>(nChunks), 0);
+        auto chunkRows = [&](int ch, int& y0, int& y1) {
+            y0 = static_cast<int>(static_cast<long long>(D.ly) * ch / nChunks);
+            y1 = static_cast<int>(static_cast<long long>(D.ly) * (ch + 1) / nChunks);
+        };
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int ch = 0; ch < nChunks; ++ch) {
+            try {
+                int y0, y1;
+                chunkRows(ch, y0, y1);
+                std::map<Key, int> lindex;
+                std::vector<std::pair<Key, ClassInfo>>& lcls = local[ch];
+                Key lastKey;
+                lastKey.fill(-1.0);
+                int lastId = -1;
+                for (int y = y0; y < y1; ++y)
+                    for (int z = 0; z < D.lz; ++z)
+                        for (int x = 0; x < D.lx; ++x) {
+                            std::size_t id = static_cast<std::size_t>(D.idx(x, y, z));
+                            ClassInfo c;
+                            int o = ph.at(x, y, z);
+                            c.obj = (o < 0) ? 0 : o;
+                            double cellEps = ep.at(x, y, z);
+                            uint8_t kind = curlKind[id];
+                            bool pmlCell = false;
+                            for (int t = 0; t < 2; ++t) pmlCell = pmlCell || npsi[t][id] > 0 || (coef[t][id] != 0.0);
+                            if (kind == L_U || kind == L_D) {
+                                double em = (kind == L_U) ? cellEps : 1.0;
+                                double pref1 = -1.0 * dt / (em * dj), pref2 = -1.0 * dt / (em * dk);
+                                if (tp[0].present) c.cint[0] = pref2;
+                                if (tp[1].present) c.cint[1] = -pref1;
+                                c.toD = (kind == L_D) ? 1 : 0;
+                            }
+                            if (pmlCell) {
+                                uint8_t pmlToD = (E && matInPML) ? 1 : 0;
+                                if (kind != L_NONE && c.toD != pmlToD)
+                                    throw UnsupportedError("a cell's interior and CPML updates target different fields");
+                                c.toD = pmlToD;
+                            }
+                            c.lor = lorFlag[id];
+                            c.ordip = ordipFlag[id];
+                            if (c.lor || c.ordip) c.eps = cellEps;
+                            if (c.toD || c.lor || c.ordip) chunkAnyD[ch] = 1;
+                            for (int t = 0; t < 2; ++t) {
+                                if (!tp[t].present) {
+                                    if (coef[t][id] != 0.0 || npsi[t][id] || psiUpd[t][id])
+                                        throw InputError("CPML term without a neighbour field");
+                                    continue;
+                                }
+                                c.nplain[t] = nplain[t][id];
+                                c.kflag[t] = kflag[t][id];
+                                c.npsi[t] = npsi[t][id];
+                                c.psiUpd[t] = psiUpd[t][id];
+                            }
+                            Key key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
+                                       c.cint[0], c.cint[1], double(c.nplain[0]), double(c.nplain[1]),
+                                       double(c.kflag[0]), double(c.kflag[1]), double(c.npsi[0]),
+                                       double(c.npsi[1]), double(c.psiUpd[0]), double(c.psiUpd[1]), 0.0};
+                            if (!(c.lor || c.ordip)) key[4] = 1.0, c.eps = 1.0;
+                            if (!c.lor) key[3] = 0.0, c.obj = 0;
+                            int lid;
+                            if (key == lastKey) {
+                                lid = lastId;
+                            } else {
+                                auto it = lindex.find(key);
+                                if (it == lindex.end()) {
+                                    lid = static_cast<int>(lcls.size());
+                                    // a chunk's classes are a subset of the whole component's
+                                    if (lid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
+                                    lcls.emplace_back(key, c);
+                                    lindex[key] = lid;
+                                } else {
+                                    lid = it->second;
+                                }
+                                lastKey = key;
+                                lastId = lid;
+                            }
+                            cp.code[id] = static_cast<uint8_t>(lid);
+                            // check the compressed CPML coefficient against the literal sum
+                            for (int t = 0; t < 2; ++t) {
+                                if (!tp[t].present) continue;
+                                const int a = coordOf(static_cast<long long>(id), tp[t].axis);
+                                double comp = c.nplain[t] * tp[t].db + (c.kflag[t] ? tp[t].kprof[a] : 0.0);
+                                double lit = coef[t][id];
+                                if (std::abs(comp - lit) > 1e-14 * std::max(1.0, std::abs(lit)) * std::abs(dt))
+                                    throw UnsupportedError("compressed CPML coefficient differs from the list sum");
+                            }
                         }
-                        c.nplain[t] = nplain[t][id];
-                        c.kflag[t] = kflag[t][id];
-                        c.npsi[t] = npsi[t][id];
-                        c.psiUpd[t] = psiUpd[t][id];
-                    }
-                    std::array<double, 16> key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
-                                               c.cint[0], c.cint[1], double(c.nplain[0]), double(c.nplain[1]),
-                                               double(c.kflag[0]), double(c.kflag[1]), double(c.npsi[0]),
-                                               double(c.npsi[1]), double(c.psiUpd[0]), double(c.psiUpd[1]), 0.0};
-                    if (!(c.lor || c.ordip)) key[4] = 1.0, c.eps = 1.0;
-                    if (!c.lor) key[3] = 0.0, c.obj = 0;
-                    int cid;
-                    if (key == lastKey) {
-                        cid = lastId;
-                        cp.code[id] = static_cast<uint8_t>(cid);
-                        goto check;
-                    }
-                    {
-                    auto it = index.find(key);
-                    if (it == index.end()) {
-                        cid = static_cast<int>(cp.classes.size());
-                        if (cid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
-                        cp.classes.push_back(c);
-                        index[key] = cid;
-                    } else {
-                        cid = it->second;
-                    }
-                    }
-                    lastKey = key;
-                    lastId = cid;
-                    cp.code[id] = static_cast<uint8_t>(cid);
-                check:
-                    // check the compressed CPML coefficient against the literal sum
-                    for (int t = 0; t < 2; ++t) {
-                        if (!tp[t].present) continue;
-                        int a = (t == 0) ? 0 : 0;
-                        a = coordOf(static_cast<long long>(id), tp[t].axis);
-                        double comp = c.nplain[t] * tp[t].db + (c.kflag[t] ? tp[t].kprof[a] : 0.0);
-                        double lit = coef[t][id];
-                        if (std::abs(comp - lit) > 1e-14 * std::max(1.0, std::abs(lit)) * std::abs(dt))
-                            throw UnsupportedError("compressed CPML coefficient differs from the list sum");
-                    }
+            } catch (...) {
+                chunkErr[ch] = std::current_exception();
+            }
+        }
+        for (int ch = 0; ch < nChunks; ++ch)
+            if (chunkErr[ch]) std::rethrow_exception(chunkErr[ch]);
+        bool anyD = false;
+        std::vector<std::vector<uint8_t>> remap(static_cast<std::size_t>(nChunks));
+        for (int ch = 0; ch < nChunks; ++ch) {
+            anyD = anyD || chunkAnyD[ch];
+            for (auto& kc : local[ch]) {
+                auto it = index.find(kc.first);
+                int cid;
+                if (it == index.end()) {
+                    cid = static_cast<int>(cp.classes.size());
+                    if (cid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
+                    cp.classes.push_back(kc.second);
+                    index[kc.first] = cid;
+                } else {
+                    cid = it->second;
                 }
+                remap[ch].push_back(static_cast<uint8_t>(cid));
+            }
+        }
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int ch = 0; ch < nChunks; ++ch) {
+            int y0, y1;
+            chunkRows(ch, y0, y1);
+            const std::vector<uint8_t>& rm = remap[ch];
+            const std::size_t b = static_cast<std::size_t>(D.idx(0, y0, 0)), e = static_cast<std::size_t>(D.idx(0, y1, 0));
+            for (std::size_t id = b; id < e; ++id) cp.code[id] = rm[cp.code[id]];
+        }
         for (std::size_t q = 1; q < cp.classes.size(); ++q) {
             const ClassInfo& k = cp.classes[q];
             bool acts = k.toD || k.lor || k.ordip;
@@ -899,11 +946,28 @@ struct Builder {
                 throw UnsupportedError("oriented-dipole poles need a 3-D grid (the reference allocates the 2-D "
                                        "polarisation grids for the other polarisation)");
         // the reference's list order: TE (Hz, Ex, Ey) then TM (Ez, Hx, Hy)
+        // Each component's lists depend only on the material maps and on which components
+        // exist, so the components are built concurrently; the first error in the order
+        // above is the one reported.
         const int order[6] = {HZ, EX, EY, EZ, HX, HY};
         bool present[6];
         for (int c = 0; c < 6; ++c) present[c] = P.comp[c].present;
-        for (int c : order)
-            if (present[c]) buildComp(c);
+        // Each component's row loops are parallel too (nested; the caller's setting is put back).
+        std::exception_ptr err[6];
+        const int prevLevels = omp_get_max_active_levels();
+        omp_set_max_active_levels(std::max(prevLevels, 2));
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int q = 0; q < 6; ++q) {
+            if (!present[order[q]]) continue;
+            try {
+                buildComp(order[q]);
+            } catch (...) {
+                err[q] = std::current_exception();
+            }
+        }
+        omp_set_max_active_levels(prevLevels);
+        for (int q = 0; q < 6; ++q)
+            if (err[q]) std::rethrow_exception(err[q]);
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
         buildOrDip();
         P.alpha.clear();

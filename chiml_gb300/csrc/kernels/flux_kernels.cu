@@ -1,0 +1,88 @@
+// Flux integration on the device (parallelFlux.hpp:325-545 as a gather plus a weighted sum).
+//
+//   k_flux_partial  one block per (tile of kFluxTile integration points, 128 frequencies):
+//                   each thread forms the four face-grid values of its frequency at every
+//                   point of the tile from the accumulators (the threads of a warp read
+//                   consecutive frequencies of one point), the integrand and its Simpson
+//                   weight, and writes the tile's partial sum.
+//   k_flux_sum      sums a face's partials in tile order (a fixed order: the result does not
+//                   depend on scheduling) and scales by fluxConv * face weight.
+#include "flux_device.hpp"
+
+namespace chiml {
+namespace dev {
+
+namespace {
+
+__device__ __forceinline__ double2 gridValue(const FluxFaceDev& F, int w, int s, int ff, int nfreq, const double* __restrict__ re,
+                                             const double* __restrict__ im) {
+    double2 g = make_double2(0.0, 0.0);
+    const long long k1 = F.start[w][s + 1];
+    for (long long k = F.start[w][s]; k < k1; ++k) {
+        const long long idx = F.pt[w][k] * nfreq + ff;
+        const double sc = F.scale[w][k];
+        g.x += sc * re[idx];
+        g.y += sc * im[idx];
+    }
+    return g;
+}
+
+// a * conj(b) / d
+__device__ __forceinline__ double2 mulConjDiv(double2 a, double2 b, double d) {
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+__global__ void __launch_bounds__(kFluxThreads) k_flux_partial(const FluxFaceDev* __restrict__ faces, const int4* __restrict__ tiles,
+                                                               int nfreq, const double* __restrict__ re, const double* __restrict__ im,
+                                                               double nt2, double2* __restrict__ partial) {
+    const int ff = blockIdx.y * kFluxThreads + threadIdx.x;
+    if (ff >= nfreq) return;
+    const int4 t = tiles[blockIdx.x];
+    const FluxFaceDev& F = faces[t.x];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s = t.y; s < t.z; ++s) {
+        double2 v = make_double2(0.0, 0.0);
+        if (F.has[0]) v = mulConjDiv(gridValue(F, 0, s, ff, nfreq, re, im), gridValue(F, 3, s, ff, nfreq, re, im), nt2);
+        if (F.has[1]) {
+            const double2 u = mulConjDiv(gridValue(F, 1, s, ff, nfreq, re, im), gridValue(F, 2, s, ff, nfreq, re, im), nt2);
+            v.x -= u.x;
+            v.y -= u.y;
+        }
+        const double w = F.wx[s % F.nx] * F.wy[s / F.nx];
+        acc.x += w * v.x;
+        acc.y += w * v.y;
+    }
+    partial[static_cast<long long>(blockIdx.x) * nfreq + ff] = acc;
+}
+
+__global__ void k_flux_sum(const FluxFaceDev* __restrict__ faces, int nFaces, int nfreq, const double2* __restrict__ partial,
+                           double2* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nFaces * nfreq) return;
+    const int face = i / nfreq, ff = i % nfreq;
+    const FluxFaceDev& F = faces[face];
+    double2 s = make_double2(0.0, 0.0);
+    for (int t = 0; t < F.nTiles; ++t) {
+        const double2 p = partial[static_cast<long long>(F.firstTile + t) * nfreq + ff];
+        s.x += p.x;
+        s.y += p.y;
+    }
+    out[static_cast<long long>(ff) * nFaces + face] = make_double2(F.pref * s.x, F.pref * s.y);
+}
+
+}  // namespace
+
+void launch_flux_faces(const FluxFaceDev* faces, int nFaces, const int4* tiles, int nTiles, int nfreq, const double* re,
+                       const double* im, double nt2, double2* partial, double2* out, void* stream) {
+    if (nFaces == 0 || nfreq == 0) return;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nTiles > 0) {
+        const dim3 grid(static_cast<unsigned>(nTiles), static_cast<unsigned>((nfreq + kFluxThreads - 1) / kFluxThreads));
+        k_flux_partial<<<grid, kFluxThreads, 0, s>>>(faces, tiles, nfreq, re, im, nt2, partial);
+    }
+    const int n = nFaces * nfreq;
+    k_flux_sum<<<(n + 127) / 128, 128, 0, s>>>(faces, nFaces, nfreq, partial, out);
+}
+
+}  // namespace dev
+}  // namespace chiml

@@ -64,6 +64,10 @@ typedef struct chiml_stats {
     int32_t n_flux_regions;        /* DFT tables: flux regions, then frequency-domain detectors (two profile slots each) */
     int32_t n_emitters;            /* emitter objects (one profile slot each) */
     int32_t n_tfsf;                /* TFSF surfaces (one profile slot each) */
+    int32_t reserved2;
+    double seconds_plan;           /* chiml_create: reading the input and building the plan (host) */
+    double seconds_upload;         /* chiml_create: device allocation and upload */
+    double seconds_finalize;       /* chiml_finalize: flux integration, downloads and file writes */
 } chiml_stats;
 
 /* Reads the JSON input (chiML schema), builds the update plan and uploads it. */
