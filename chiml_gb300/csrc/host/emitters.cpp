@@ -124,7 +124,7 @@ void level_combos(const std::vector<EnergyLevel>& levs, std::size_t depth, std::
 
 }  // namespace
 
-void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3], const std::vector<double>& epsOrDip,
+void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3], const double* epsOrDip,
                     Plan& P) {
     for (const EmitterSpec& em : in.emitters) {
         EmitterPlan e;
@@ -236,7 +236,7 @@ void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epres
         if (e.dtcTimeInt < 1) throw InputError("levDTC_timeInt must be positive");
         P.emitters.push_back(std::move(e));
     }
-    if (!P.emitters.empty()) P.epsP = epsOrDip;
+    if (!P.emitters.empty()) P.epsP.assign(epsOrDip, epsOrDip + D.cells());
 }
 
 }  // namespace chiml

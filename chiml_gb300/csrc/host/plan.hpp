@@ -271,11 +271,11 @@ Plan build_plan(const Inputs& in);
 // Emitter plans of the input (emitters.cpp); Epresent: which of Ex, Ey, Ez the grid has;
 // epsOrDip: the relative permittivity on the cell-centred grid.
 void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3],
-                    const std::vector<double>& epsOrDip, Plan& P);
+                    const double* epsOrDip, Plan& P);
 
 // TFSF plans of the input (tfsf.cpp); phys[c]: object id per cell of main component c
 // (0..5; null when absent), -1 on the halo.
-void build_tfsf(const Inputs& in, const Dims& D, double dt, const std::vector<int>* const phys[6],
+void build_tfsf(const Inputs& in, const Dims& D, double dt, const int* const phys[6],
                 const std::vector<Object>& objs, Plan& P);
 
 // Wigner 3j symbol for integer arguments (emitters.cpp).

@@ -13,6 +13,7 @@
 #include <numeric>
 #include <set>
 #include <tuple>
+#include <utility>
 
 #include <omp.h>
 
@@ -29,12 +30,45 @@ bool ClassInfo::operator==(const ClassInfo& o) const {
 
 namespace {
 
+// Host buffers of one value per grid cell: the vector leaves its elements uninitialised
+// and filled() writes them in parallel (first touch spread over the threads).
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        typedef UninitAlloc<U> other;
+    };
+    UninitAlloc() = default;
+    template <typename U>
+    UninitAlloc(const UninitAlloc<U>&) {}
+    template <typename U>
+    void construct(U* p) noexcept {
+        ::new (static_cast<void*>(p)) U;
+    }
+    template <typename U, typename... A>
+    void construct(U* p, A&&... a) {
+        ::new (static_cast<void*>(p)) U(std::forward<A>(a)...);
+    }
+};
+template <typename T>
+using Buf = std::vector<T, UninitAlloc<T>>;
+
+template <typename T>
+Buf<T> filled(std::size_t n, T init, int threads) {
+    Buf<T> v(n);
+    T* p = v.data();
+    const long long m = static_cast<long long>(n);
+#pragma omp parallel for schedule(static) num_threads(threads)
+    for (long long i = 0; i < m; ++i) p[i] = init;
+    return v;
+}
+
 template <typename T>
 struct Field3 {
     Dims d;
-    std::vector<T> v;
+    Buf<T> v;
     Field3() {}
-    Field3(const Dims& dd, T init) : d(dd), v(static_cast<std::size_t>(dd.cells()), init) {}
+    Field3(const Dims& dd, T init) : d(dd), v(filled<T>(static_cast<std::size_t>(dd.cells()), init, omp_get_max_threads())) {}
     T& at(int x, int y, int z) { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
     T at(int x, int y, int z) const { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
 };
@@ -189,6 +223,7 @@ struct Builder {
                 mx[q] = static_cast<int>(static_cast<double>(nvec[q]) / 2);
             }
             mx[ci] = static_cast<int>(in.pmlThickness[ci] - nvec[ci] / 2.0);
+            bool carried = false;
             for (std::size_t oo = 0; oo < objs.size(); ++oo) {
                 const Object& o = objs[oo];
                 if (o.epsInf == 1.0 && o.gamma.size() < 1 && !o.ML) continue;
@@ -199,30 +234,49 @@ struct Builder {
                     for (int q = 0; q < 3; ++q) s2 += (pt[q] - o.loc[q]) * (pt[q] - o.loc[q]);
                     return s2 <= rad * rad;
                 };
-                for (int jj = mn[cj]; jj < mx[cj]; ++jj)
-                    for (int kk = mn[ck]; kk < mx[ck]; ++kk) {
-                        for (int pass = 0; pass < 2; ++pass) {
-                            if (pass == 1) {
-                                mn[ci] = nvec[ci] / 2 - in.pmlThickness[ci];
-                                mx[ci] = nvec[ci] / 2;
-                            }
-                            for (int ii = mn[ci]; ii < mx[ci]; ++ii) {
-                                std::array<double, 3> pt = {0, 0, 0};
-                                pt[ci] = static_cast<double>(ii) * d[ci];
-                                pt[cj] = static_cast<double>(jj) * d[cj];
-                                pt[ck] = static_cast<double>(kk) * d[ck];
-                                pt[0] += d[0] / 2.0;
-                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
-                                pt[1] += d[1] / 2.0;
-                                pt[0] -= d[0] / 2.0;
-                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
-                                pt[2] += d[2] / 2.0;
-                                pt[1] -= d[0] / 2.0;
-                                if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
-                                pt[0] += d[2] / 2.0;
-                            }
-                        }
+                // one (jj, kk) row of points over ii in [a, b): three staggered points each
+                auto row = [&](int jj, int kk, int a, int b) {
+                    for (int ii = a; ii < b && !matInPML; ++ii) {
+                        std::array<double, 3> pt = {0, 0, 0};
+                        pt[ci] = static_cast<double>(ii) * d[ci];
+                        pt[cj] = static_cast<double>(jj) * d[cj];
+                        pt[ck] = static_cast<double>(kk) * d[ck];
+                        pt[0] += d[0] / 2.0;
+                        if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                        pt[1] += d[1] / 2.0;
+                        pt[0] -= d[0] / 2.0;
+                        if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
+                        pt[2] += d[2] / 2.0;
+                        pt[1] -= d[0] / 2.0;
+                        if (!matInPML && maybeIn(pt) && o.isObj(pt, d[0], o.geo)) matInPML = dielc;
                     }
+                };
+                // The reference's loops reset the ii bounds to the plus-side slab in the second
+                // pass of the first (jj, kk) iteration and never restore them: the first row's
+                // first pass covers the minus-side slab, every later pass the plus side.
+                if (mn[cj] >= mx[cj] || mn[ck] >= mx[ck]) continue;
+                if (!carried) {
+                    row(mn[cj], mn[ck], mn[ci], mx[ci]);
+                    mn[ci] = nvec[ci] / 2 - in.pmlThickness[ci];
+                    mx[ci] = nvec[ci] / 2;
+                    carried = true;
+                }
+                // points outside the bounding sphere fail maybeIn: scan only its index box
+                // (every staggered point lies within half a cell of its row's point)
+                auto box = [&](int ax, int m0, int m1, int& a, int& b) {
+                    a = m0;
+                    b = m1;
+                    if (!(rad < 1e300)) return;
+                    const double reach = rad + std::max(std::max(d[0], d[1]), d[2]);
+                    a = std::max(m0, static_cast<int>(std::floor((o.loc[ax] - reach) / d[ax])) - 1);
+                    b = std::min(m1, static_cast<int>(std::ceil((o.loc[ax] + reach) / d[ax])) + 2);
+                };
+                int ja, jb, ka, kb, ia, ib;
+                box(cj, mn[cj], mx[cj], ja, jb);
+                box(ck, mn[ck], mx[ck], ka, kb);
+                box(ci, mn[ci], mx[ci], ia, ib);
+                for (int jj = ja; jj < jb; ++jj)
+                    for (int kk = ka; kk < kb; ++kk) row(jj, kk, ia, ib);
             }
         }
     }
@@ -537,6 +591,7 @@ struct Builder {
         lnPlOut[comp] = p.lnPl;
     }
     std::array<int, 3> lnMnOut[6], lnPlOut[6];
+    int innerThreads_ = 1;  // threads of each component's row loops
 
     // ---- update lists (parallelFDTDField.hpp:628-856) ----
     enum ListKind { L_NONE = 0, L_U = 1, L_D = 2 };
@@ -574,16 +629,22 @@ struct Builder {
         mx[1] -= fieldEnd[1];
 
         // per-cell list membership
-        std::vector<uint8_t> curlKind(static_cast<std::size_t>(D.cells()), L_NONE);
-        std::vector<uint8_t> lorFlag(static_cast<std::size_t>(D.cells()), 0);
-        std::vector<uint8_t> ordipFlag(static_cast<std::size_t>(D.cells()), 0);
+        const int nt = innerThreads_;
+        Buf<uint8_t> curlKind = filled<uint8_t>(static_cast<std::size_t>(D.cells()), L_NONE, nt);
+        Buf<uint8_t> lorFlag = filled<uint8_t>(static_cast<std::size_t>(D.cells()), 0, nt);
+        Buf<uint8_t> ordipFlag = filled<uint8_t>(static_cast<std::size_t>(D.cells()), 0, nt);
 
         auto classify = [&](std::array<int, 3> a, std::array<int, 3> b, bool includeU, bool finalFill) {
+            int border = 0;  // rows write disjoint cells
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(| : border)
             for (int jj = a[1]; jj < b[1]; ++jj)
                 for (int kk = a[2]; kk < b[2]; ++kk)
                     for (int ii = a[0]; ii < b[0]; ++ii) {
                         int o = ph.at(ii, jj, kk);
-                        if (o < 0) throw InputError("update list reaches a border cell");
+                        if (o < 0) {
+                            border = 1;
+                            continue;
+                        }
                         const Object& ob = objs[o];
                         std::size_t id = static_cast<std::size_t>(D.idx(ii, jj, kk));
                         bool orDipCell = ob.orDip && (E && ob.gamma.size() > 0);
@@ -596,6 +657,7 @@ struct Builder {
                             else if (!uCell) lorFlag[id] = 1;
                         }
                     }
+            if (border) throw InputError("update list reaches a border cell");
         };
         // getBlasLists
         bool pmlMat = (E && matInPML);
@@ -650,11 +712,11 @@ struct Builder {
 
         // literal per-cell accumulation of every list (for the check) and compression
         const std::size_t N = static_cast<std::size_t>(D.cells());
-        std::vector<double> coef[2] = {std::vector<double>(N, 0.0), std::vector<double>(N, 0.0)};
-        std::vector<uint8_t> npsi[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
-        std::vector<uint8_t> psiUpd[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
-        std::vector<uint8_t> nplain[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
-        std::vector<uint8_t> kflag[2] = {std::vector<uint8_t>(N, 0), std::vector<uint8_t>(N, 0)};
+        Buf<double> coef[2] = {filled<double>(N, 0.0, nt), filled<double>(N, 0.0, nt)};
+        Buf<uint8_t> npsi[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
+        Buf<uint8_t> psiUpd[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
+        Buf<uint8_t> nplain[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
+        Buf<uint8_t> kflag[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
         auto coordOf = [&](long long id, int ax) {
             long long x = id % D.lx;
             long long r = id / D.lx;
@@ -733,7 +795,7 @@ struct Builder {
             y0 = static_cast<int>(static_cast<long long>(D.ly) * ch / nChunks);
             y1 = static_cast<int>(static_cast<long long>(D.ly) * (ch + 1) / nChunks);
         };
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
         for (int ch = 0; ch < nChunks; ++ch) {
             try {
                 int y0, y1;
@@ -840,7 +902,7 @@ struct Builder {
                 remap[ch].push_back(static_cast<uint8_t>(cid));
             }
         }
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
         for (int ch = 0; ch < nChunks; ++ch) {
             int y0, y1;
             chunkRows(ch, y0, y1);
@@ -954,9 +1016,13 @@ struct Builder {
         for (int c = 0; c < 6; ++c) present[c] = P.comp[c].present;
         // Each component's row loops are parallel too (nested; the caller's setting is put back).
         std::exception_ptr err[6];
+        int nComp = 0;
+        for (int c = 0; c < 6; ++c) nComp += present[c] ? 1 : 0;
+        const int nThreads = omp_get_max_threads();
+        innerThreads_ = std::max(1, nThreads / std::max(1, nComp));
         const int prevLevels = omp_get_max_active_levels();
         omp_set_max_active_levels(std::max(prevLevels, 2));
-#pragma omp parallel for schedule(dynamic, 1)
+#pragma omp parallel for schedule(dynamic, 1) num_threads(std::min(nThreads, std::max(1, nComp)))
         for (int q = 0; q < 6; ++q) {
             if (!present[order[q]]) continue;
             try {
@@ -1394,11 +1460,11 @@ Plan build_plan(const Inputs& in) {
     b.build();
     if (!in.emitters.empty()) {
         const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
-        build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v, P);
+        build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v.data(), P);
     }
     if (!in.tfsf.empty()) {
-        const std::vector<int>* ph[6];
-        for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? &b.phys[c].v : nullptr;
+        const int* ph[6];
+        for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? b.phys[c].v.data() : nullptr;
         build_tfsf(in, P.dims, P.dt, ph, in.objects, P);
     }
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)

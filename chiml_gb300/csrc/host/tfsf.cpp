@@ -26,7 +26,7 @@ struct TfsfBuilder {
     double dt;
     std::array<double, 3> d;
     const TfsfSpec& t;
-    const std::vector<int>* const* phys;
+    const int* const* phys;
     TfsfPlan& T;
 
     bool twoD = false;
@@ -37,7 +37,7 @@ struct TfsfBuilder {
     bool present[6] = {false, false, false, false, false, false};
     std::vector<TfsfSegment>* segs = nullptr;  // where genSurface records its rows
 
-    TfsfBuilder(const Inputs& i, const Dims& dd, double dtt, const TfsfSpec& tt, const std::vector<int>* const* ph, TfsfPlan& tp)
+    TfsfBuilder(const Inputs& i, const Dims& dd, double dtt, const TfsfSpec& tt, const int* const* ph, TfsfPlan& tp)
         : in(i), D(dd), dt(dtt), d(i.d), t(tt), phys(ph), T(tp) {}
 
     // ---- parallelTFSFBase constructor, parallelTFSF.hpp:179-380 ----
@@ -171,7 +171,7 @@ struct TfsfBuilder {
         const int indStart = twoD ? 2 : 0;
         for (int c = 0; c < 6; ++c) {
             if (!phys[c]) continue;
-            const std::vector<int>& ph = *phys[c];
+            const int* ph = phys[c];
             for (int ii = indStart; ii < 6; ++ii) {
                 if (ii % 2 == 0) continue;  // only the plus surfaces are sampled
                 const int s = surInds[ii];
@@ -511,7 +511,7 @@ struct TfsfBuilder {
 
 }  // namespace
 
-void build_tfsf(const Inputs& in, const Dims& D, double dt, const std::vector<int>* const phys[6],
+void build_tfsf(const Inputs& in, const Dims& D, double dt, const int* const phys[6],
                 const std::vector<Object>& objs, Plan& P) {
     (void)objs;
     for (const TfsfSpec& t : in.tfsf) {
