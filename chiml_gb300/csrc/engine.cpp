@@ -587,7 +587,7 @@ private:
                 }
             t.pulseTab = mem_.upload(tab);
             t.rec = mem_.alloc<double2>(6 * 2 * (static_cast<std::size_t>(P.nSteps) + 1));
-            const std::vector<TfsfCellAdds>* adds[2] = {&tp.addH, &tp.addE};
+            const TfsfAdds* adds[2] = {&tp.addH, &tp.addE};
             const std::vector<TfsfSegment>* segs[2] = {&tp.segH, &tp.segE};
             for (int w = 0; w < 2; ++w) {
                 // rows split into runs of single-term cells; the cells with several terms
@@ -635,18 +635,17 @@ private:
                 std::vector<long long> cell;
                 std::vector<int> comp, start, tl, ti;
                 std::vector<double> pref;
-                long long listed = 0;
-                for (const TfsfCellAdds& a : *adds[w]) listed += static_cast<long long>(a.line.size());
-                if (listed != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
-                for (const TfsfCellAdds& a : *adds[w]) {
-                    if (a.line.size() < 2) continue;  // in a row
-                    cell.push_back(pad(a.cell));
-                    comp.push_back(a.comp);
+                const TfsfAdds& a = *adds[w];
+                if (static_cast<long long>(a.terms()) != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
+                for (std::size_t q = 0; q < a.cells(); ++q) {
+                    if (a.start[q + 1] - a.start[q] < 2) continue;  // in a row
+                    cell.push_back(pad(a.cell[q]));
+                    comp.push_back(a.comp[q]);
                     start.push_back(static_cast<int>(tl.size()));
-                    for (std::size_t k = 0; k < a.line.size(); ++k) {
+                    for (long long k = a.start[q]; k < a.start[q + 1]; ++k) {
                         if (a.toD[k]) throw UnsupportedError("TFSF corrections into D");
                         if (!tp.line[a.line[k]].present || a.incd[k] < 0 || a.incd[k] >= tp.gridLen ||
-                            a.cell < 0 || a.cell >= P.dims.cells() || !P.comp[a.comp].present)
+                            a.cell[q] < 0 || a.cell[q] >= P.dims.cells() || !P.comp[a.comp[q]].present)
                             throw InputError("TFSF correction outside its grids");
                         tl.push_back(a.line[k]);
                         ti.push_back(a.incd[k]);

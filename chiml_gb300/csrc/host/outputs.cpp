@@ -217,9 +217,11 @@ std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
             const int corJK = (w == 0 || w == 3) ? f.corJ : f.corK;
             const bool act = P.comp[comps[w]].present;
             const bool trans = P.comp[comps[oth[w]]].present;
-            std::vector<std::vector<std::pair<long long, double>>> cellTerms(static_cast<std::size_t>(npt));
             const std::vector<int>& lst = *lists[w];
             const double scaleDen = static_cast<double>(lst.size());
+            // every (grid point, accumulator point, scale) term in the reference's order,
+            // visited twice: to count the terms per grid point, then to place them
+            auto visit = [&](auto&& fn) {
             for (std::size_t dd = 0; dd < lst.size(); ++dd) {
                 const FreqStore& st = fp.stores[lst[dd]];
                 if (st.outN[0] == 0) continue;  // outside the grid: no out grid
@@ -255,18 +257,22 @@ std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
                             const int y = ii + addIndex[0] + o[7], z = jj + addIndex[1] + o[8];
                             if (y < 0 || z < 0 || y >= m.ny || z >= m.nx)
                                 throw InputError("flux combination index out of range (the reference asserts here)");
-                            cellTerms[static_cast<std::size_t>(z + static_cast<long long>(m.nx) * y)].emplace_back(pt, scale);
+                            fn(z + static_cast<long long>(m.nx) * y, pt, scale);
                         }
             }
-            m.start[w].assign(static_cast<std::size_t>(npt) + 1, 0);
-            for (long long c = 0; c < npt; ++c) m.start[w][c + 1] = m.start[w][c] + static_cast<long long>(cellTerms[c].size());
-            m.pt[w].reserve(static_cast<std::size_t>(m.start[w][npt]));
-            m.scale[w].reserve(static_cast<std::size_t>(m.start[w][npt]));
-            for (auto& ct : cellTerms)
-                for (auto& t : ct) {
-                    m.pt[w].push_back(t.first);
-                    m.scale[w].push_back(t.second);
-                }
+            };
+            std::vector<long long>& start = m.start[w];
+            start.assign(static_cast<std::size_t>(npt) + 1, 0);
+            visit([&](long long c, long long, double) { ++start[static_cast<std::size_t>(c) + 1]; });
+            for (long long c = 0; c < npt; ++c) start[c + 1] += start[c];
+            m.pt[w].resize(static_cast<std::size_t>(start[npt]));
+            m.scale[w].resize(static_cast<std::size_t>(start[npt]));
+            std::vector<long long> cursor(start.begin(), start.end() - 1);
+            visit([&](long long c, long long pt, double scale) {
+                const long long k = cursor[static_cast<std::size_t>(c)]++;
+                m.pt[w][k] = pt;
+                m.scale[w][k] = scale;
+            });
         }
         // getFlux pairs the E grid with the complementary H grid: Ej with Hk, Ek with Hj
         if (!(m.has[0] || m.has[1]) || (m.has[0] && !m.has[3]) || (!m.has[0] && !m.has[2]) || (m.has[1] && !m.has[2]))

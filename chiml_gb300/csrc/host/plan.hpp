@@ -217,12 +217,18 @@ struct TfsfLine {
 
 // Surface corrections of one main-grid cell, in the reference's order: each term adds
 // pref * Re(line[incd]) to the cell's field (toD: to its D field).
-struct TfsfCellAdds {
-    long long cell = 0;
-    int comp = 0;                      // main field component 0..5
+// The surface terms of every main-grid cell that gets some, cells in the order of their
+// first term, terms of cell q in [start[q], start[q + 1]) in the reference's order:
+// F[comp[q]][cell[q]] (or D where toD) += pref * Re(line[line][incd]).
+struct TfsfAdds {
+    std::vector<long long> cell;
+    std::vector<int> comp;              // main field component 0..5
+    std::vector<long long> start{0};    // [cells + 1]
     std::vector<int> line, incd;
     std::vector<double> pref;
     std::vector<uint8_t> toD;
+    std::size_t cells() const { return cell.size(); }
+    std::size_t terms() const { return line.size(); }
 };
 
 // One row of one surface (a daxpy of addIncdFields): cell cell0 + r * cellStride of
@@ -239,7 +245,7 @@ struct TfsfPlan {
     double dt = 0.0;
     TfsfLine line[6];
     std::vector<PulseSpec> pulses;
-    std::vector<TfsfCellAdds> addH, addE;  // applied before and after the 1-D step
+    TfsfAdds addH, addE;  // applied before and after the 1-D step
     std::vector<TfsfSegment> segH, segE;   // the same corrections as surface rows
 };
 

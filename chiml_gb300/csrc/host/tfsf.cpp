@@ -482,8 +482,7 @@ struct TfsfBuilder {
     }
 
     // Terms grouped by main cell, cells in order of their first term.
-    void gather(const std::vector<SurfaceTerm>& terms, std::vector<TfsfCellAdds>& out) const {
-        std::vector<std::pair<long long, int>> key;  // (comp * cells + cell, first index)
+    void gather(const std::vector<SurfaceTerm>& terms, TfsfAdds& out) const {
         std::vector<long long> k(terms.size());
         for (std::size_t q = 0; q < terms.size(); ++q) k[q] = terms[q].comp * D.cells() + terms[q].cell;
         std::vector<std::size_t> order(terms.size());
@@ -493,18 +492,25 @@ struct TfsfBuilder {
         for (std::size_t p = 0; p < order.size(); ++p)
             if (p == 0 || k[order[p]] != k[order[p - 1]]) groups.push_back({order[p], p});
         std::sort(groups.begin(), groups.end());
+        out = TfsfAdds();
+        out.cell.reserve(groups.size());
+        out.comp.reserve(groups.size());
+        out.start.reserve(groups.size() + 1);
+        out.line.reserve(terms.size());
+        out.incd.reserve(terms.size());
+        out.pref.reserve(terms.size());
+        out.toD.reserve(terms.size());
         for (auto& g : groups) {
-            TfsfCellAdds a;
-            a.cell = terms[g.first].cell;
-            a.comp = terms[g.first].comp;
+            out.cell.push_back(terms[g.first].cell);
+            out.comp.push_back(terms[g.first].comp);
             for (std::size_t p = g.second; p < order.size() && k[order[p]] == k[g.first]; ++p) {
                 const SurfaceTerm& st = terms[order[p]];
-                a.line.push_back(st.line);
-                a.incd.push_back(st.incd);
-                a.pref.push_back(st.pref);
-                a.toD.push_back(st.toD ? 1 : 0);
+                out.line.push_back(st.line);
+                out.incd.push_back(st.incd);
+                out.pref.push_back(st.pref);
+                out.toD.push_back(st.toD ? 1 : 0);
             }
-            out.push_back(std::move(a));
+            out.start.push_back(static_cast<long long>(out.line.size()));
         }
     }
 };

@@ -213,13 +213,12 @@ struct TfsfSim {
 
     cplx rec(int c, bool off) const { return T.line[c].present ? pul[c][off ? T.line[c].recOffIdx : T.line[c].recIdx] : cplx(0.0); }
 
-    static void addSurface(const std::vector<TfsfCellAdds>& adds, const std::vector<cplx>* lines, std::vector<double>* F,
-                           std::vector<double>* Dd) {
-        for (const TfsfCellAdds& a : adds)
-            for (std::size_t q = 0; q < a.line.size(); ++q) {
+    static void addSurface(const TfsfAdds& a, const std::vector<cplx>* lines, std::vector<double>* F, std::vector<double>* Dd) {
+        for (std::size_t c = 0; c < a.cells(); ++c)
+            for (long long q = a.start[c]; q < a.start[c + 1]; ++q) {
                 const double v = a.pref[q] * std::real(lines[a.line[q]][a.incd[q]]);
-                if (a.toD[q]) Dd[a.comp][a.cell] += v;
-                else F[a.comp][a.cell] += v;
+                if (a.toD[q]) Dd[a.comp[c]][a.cell[c]] += v;
+                else F[a.comp[c]][a.cell[c]] += v;
             }
     }
 
