@@ -493,6 +493,7 @@ private:
         if (static_cast<long long>(v.size()) != D.cells()) throw InputError("grid array of the wrong size");
         std::vector<V> o(static_cast<std::size_t>(cellsPad_), fill);
         const long long rows = static_cast<long long>(D.ly) * D.lz;
+#pragma omp parallel for schedule(static)
         for (long long r = 0; r < rows; ++r)
             for (int x = 0; x < D.lx; ++x) o[static_cast<std::size_t>(r * pitch_ + x)] = v[static_cast<std::size_t>(r * D.lx + x)];
         return o;
@@ -944,15 +945,13 @@ private:
     }
 
     // Host-side bounds validation of every index the kernels will dereference.
-    void validatePlan() const {
+    void validatePlan() {
         const Dims& D = P.dims;
         const long long N = D.cells();
         for (int c = 0; c < 6; ++c) {
             const CompPlan& cp = P.comp[c];
             if (!cp.present) continue;
             if (static_cast<long long>(cp.code.size()) != N) throw InputError("class code array size");
-            for (uint8_t k : cp.code)
-                if (k >= cp.classes.size()) throw InputError("class code outside the class table");
             for (int t = 0; t < 2; ++t) {
                 const TermPlan& tp = cp.term[t];
                 if (!tp.present) continue;
@@ -960,13 +959,28 @@ private:
                 if (static_cast<int>(tp.kprof.size()) != L || static_cast<int>(tp.b.size()) != L) throw InputError("profile size");
                 if (!P.comp[tp.field].present) throw InputError("neighbour field absent");
             }
-            // every coded cell's neighbour stays inside the grid
-            for (long long i = 0; i < N; ++i) {
-                if (cp.code[i] == 0) continue;
-                for (int t = 0; t < 2; ++t)
-                    if (cp.term[t].present && (i + cp.term[t].off < 0 || i + cp.term[t].off >= N))
-                        throw InputError("stencil neighbour outside the grid");
+            // every code indexes the class table and every coded cell's neighbour stays
+            // inside the grid; the cells of each class are counted on the way
+            const int ncls = static_cast<int>(cp.classes.size());
+            const long long off0 = cp.term[0].present ? cp.term[0].off : 0, off1 = cp.term[1].present ? cp.term[1].off : 0;
+            std::vector<long long> count(256, 0);
+            int bad = 0;
+#pragma omp parallel
+            {
+                std::vector<long long> local(256, 0);
+#pragma omp for schedule(static) reduction(| : bad)
+                for (long long i = 0; i < N; ++i) {
+                    const uint8_t k = cp.code[i];
+                    ++local[k];
+                    if (k >= ncls) bad |= 1;
+                    else if (k != 0 && (i + off0 < 0 || i + off0 >= N || i + off1 < 0 || i + off1 >= N)) bad |= 2;
+                }
+#pragma omp critical
+                for (int q = 0; q < 256; ++q) count[q] += local[q];
             }
+            if (bad & 1) throw InputError("class code outside the class table");
+            if (bad & 2) throw InputError("stencil neighbour outside the grid");
+            classCount_[c].assign(count.begin(), count.begin() + ncls);
         }
         for (auto& s : P.sources)
             for (long long c : s.cells)
@@ -1255,6 +1269,8 @@ private:
         return d;
     }
 
+    std::vector<long long> classCount_[6];  // cells of each class, per component
+
     void uploadTail() {
         bytesPerCell_ = algorithmicBytesPerCell();
         dStep_ = mem_.alloc<int>(1);
@@ -1305,8 +1321,7 @@ private:
                 const int c = (half ? 0 : 3) + ci;
                 const CompPlan& cp = P.comp[c];
                 if (!cp.present) continue;
-                std::vector<long long> count(cp.classes.size(), 0);
-                for (uint8_t k : cp.code) count[k]++;
+                const std::vector<long long>& count = classCount_[c];
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
                     for (int tt = 0; tt < 2; ++tt)

@@ -356,14 +356,20 @@ void read_emitter(const JNode& node, Object& o, Inputs& ip) {
         for (auto& gg : kv.second.child("g").kids) g.push_back(gg.second.value<double>() * ip.a / kSpeedOfLight);
         em.gam.push_back(g);
     }
-    // grid points of the object (parallelInputs.cpp:596-614)
-    for (int zz = 0; zz < nz; ++zz)
-        for (int yy = 0; yy < ny; ++yy)
-            for (int xx = 0; xx < nx; ++xx) {
-                std::array<double, 3> pt = {(xx - (nx - 1) / 2.0) * ip.d[0], (yy - (ny - 1) / 2.0) * ip.d[1],
-                                            (zz - (nz - 1) / 2.0) * ip.d[2]};
-                if (o.isObj(pt, dminAll, o.geo)) em.locs.push_back({xx, yy, zz});
-            }
+    // grid points of the object (parallelInputs.cpp:596-614), in (z, y, x) order; the z
+    // planes are scanned in parallel and concatenated in order
+    {
+        std::vector<std::vector<std::array<int, 3>>> plane(static_cast<std::size_t>(std::max(nz, 0)));
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int zz = 0; zz < nz; ++zz)
+            for (int yy = 0; yy < ny; ++yy)
+                for (int xx = 0; xx < nx; ++xx) {
+                    std::array<double, 3> pt = {(xx - (nx - 1) / 2.0) * ip.d[0], (yy - (ny - 1) / 2.0) * ip.d[1],
+                                                (zz - (nz - 1) / 2.0) * ip.d[2]};
+                    if (o.isObj(pt, dminAll, o.geo)) plane[zz].push_back({xx, yy, zz});
+                }
+        for (auto& pl : plane) em.locs.insert(em.locs.end(), pl.begin(), pl.end());
+    }
     for (auto& kv : node.child("RelaxationOperators").kids) {
         RelaxOp r;
         r.n0 = kv.second.get<int>("state_i");

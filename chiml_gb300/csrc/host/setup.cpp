@@ -93,8 +93,6 @@ struct Builder {
 
     Builder(const Inputs& i, Plan& p) : in(i), P(p) {}
 
-    // Index range [lo, hi) per axis that contains every cell whose sample point can
-    // lie inside the object (isObj is only ever true within the object's extent).
     // Radius of a sphere about o.loc that contains every point isObj accepts
     // (with geo or geoML), or 1e300 when no finite bound is known.
     double boundingRadius(const Object& o) const {
@@ -118,34 +116,50 @@ struct Builder {
         return r;
     }
 
-    void objectIndexBox(const Object& o, std::array<double, 3> offPt, int lo[3], int hi[3]) const {
-        double r = 0.0;
-        switch (o.shape) {
-            case Shape::SPHERE: r = o.geoML[0]; break;
-            case Shape::ELLIPSOID: r = 0.5 * std::max(std::max(std::abs(o.geoML[0]), std::abs(o.geoML[1])), std::abs(o.geoML[2])); break;
-            case Shape::BLOCK: r = 0.5 * std::sqrt(o.geoML[0] * o.geoML[0] + o.geoML[1] * o.geoML[1] + o.geoML[2] * o.geoML[2]); break;
-            case Shape::CYLINDER: r = std::sqrt(o.geoML[0] * o.geoML[0] + 0.25 * o.geoML[1] * o.geoML[1]); break;
-        }
-        if (!(r < 1e300)) r = 1e300;  // NaN or huge: no narrowing
-        if (o.shape != Shape::SPHERE) {
-            // the object-space distance equals the real-space one only for orthonormal axes
+    // Half extents h[q] about o.loc, along each grid axis, of every point isObj accepts with
+    // geo or geoML (the object's axis box rotated into the grid frame); false when no bound
+    // is known (axes that are not orthonormal, unbounded sizes).
+    bool objectExtent(const Object& o, std::array<double, 3>& h) const {
+        if (o.shape != Shape::SPHERE)
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) {
                     double dot = 0.0;
                     for (int k = 0; k < 3; ++k) dot += o.coord[a * 3 + k] * o.coord[b * 3 + k];
-                    if (!(std::abs(dot - (a == b ? 1.0 : 0.0)) < 1e-9)) r = 1e300;
+                    if (!(std::abs(dot - (a == b ? 1.0 : 0.0)) < 1e-9)) return false;
                 }
-        }
+        auto g = [&](int i) { return std::max(std::abs(o.geo[i]), std::abs(o.geoML[i])); };
+        auto R = [&](int i, int q) { return o.coord[i * 3 + q]; };  // t_i = sum_q R(i, q) (p - loc)_q
         for (int q = 0; q < 3; ++q) {
-            const double pad = 2.0 * d[q] + 1e-9 * std::abs(r);
-            const double c0 = (nvec[q] - nvec[q] % 2) / 2.0 - offPt[q] + 1.0;  // index of the origin
-            if (d[q] <= 0 || r >= 1e300) {
+            switch (o.shape) {
+                case Shape::SPHERE: h[q] = std::max(o.geoML[0], o.geo[0]); break;
+                case Shape::BLOCK: h[q] = 0.5 * (std::abs(R(0, q)) * g(0) + std::abs(R(1, q)) * g(1) + std::abs(R(2, q)) * g(2)); break;
+                case Shape::ELLIPSOID:
+                    h[q] = 0.5 * std::sqrt(std::pow(R(0, q) * g(0), 2) + std::pow(R(1, q) * g(1), 2) + std::pow(R(2, q) * g(2), 2));
+                    break;
+                case Shape::CYLINDER:
+                    h[q] = 0.5 * std::abs(R(1, q)) * g(1) + g(0) * std::sqrt(R(0, q) * R(0, q) + R(2, q) * R(2, q));
+                    break;
+            }
+            if (!(h[q] < 1e300)) return false;
+        }
+        return true;
+    }
+
+    // Index range [lo, hi) per axis that contains every cell whose sample point can
+    // lie inside the object (isObj is only ever true within the object's extent).
+    void objectIndexBox(const Object& o, std::array<double, 3> offPt, int lo[3], int hi[3]) const {
+        std::array<double, 3> h;
+        const bool bounded = objectExtent(o, h);
+        for (int q = 0; q < 3; ++q) {
+            if (d[q] <= 0 || !bounded) {
                 lo[q] = -1;
                 hi[q] = 1 << 30;
                 continue;
             }
-            lo[q] = static_cast<int>(std::floor((o.loc[q] - r - pad) / d[q] + c0)) - 1;
-            hi[q] = static_cast<int>(std::ceil((o.loc[q] + r + pad) / d[q] + c0)) + 2;
+            const double pad = 2.0 * d[q] + 1e-9 * std::abs(h[q]);
+            const double c0 = (nvec[q] - nvec[q] % 2) / 2.0 - offPt[q] + 1.0;  // index of the origin
+            lo[q] = static_cast<int>(std::floor((o.loc[q] - h[q] - pad) / d[q] + c0)) - 1;
+            hi[q] = static_cast<int>(std::ceil((o.loc[q] + h[q] + pad) / d[q] + c0)) + 2;
         }
     }
 
@@ -261,13 +275,17 @@ struct Builder {
                     mx[ci] = nvec[ci] / 2;
                     carried = true;
                 }
-                // points outside the bounding sphere fail maybeIn: scan only its index box
-                // (every staggered point lies within half a cell of its row's point)
+                // points outside the bounding sphere fail maybeIn and points outside the
+                // object's extent fail isObj: scan only the index box of both (every
+                // staggered point lies within half a cell of its row's point)
+                std::array<double, 3> ext;
+                const bool bounded = objectExtent(o, ext);
                 auto box = [&](int ax, int m0, int m1, int& a, int& b) {
                     a = m0;
                     b = m1;
-                    if (!(rad < 1e300)) return;
-                    const double reach = rad + std::max(std::max(d[0], d[1]), d[2]);
+                    if (!(rad < 1e300) && !bounded) return;
+                    const double r = bounded ? std::min(rad, ext[ax]) : rad;
+                    const double reach = r + std::max(std::max(d[0], d[1]), d[2]);
                     a = std::max(m0, static_cast<int>(std::floor((o.loc[ax] - reach) / d[ax])) - 1);
                     b = std::min(m1, static_cast<int>(std::ceil((o.loc[ax] + reach) / d[ax])) + 2);
                 };
