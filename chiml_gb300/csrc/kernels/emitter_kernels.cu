@@ -50,6 +50,17 @@ __device__ __forceinline__ C2 cmac(C2 a, C2 b, C2 s) {
     return s;
 }
 
+// Per-thread population sums over the ensemble members of a density-update block, kept in
+// shared memory rather than registers (the update needs every register it can get):
+// gPopSh[d * kEmThreads + thread] for population detector d.
+__shared__ double2 gPopSh[kMaxDtc * kEmThreads];
+
+__device__ __forceinline__ void addPop(int d, double x, double y) {
+    double2& p = gPopSh[d * kEmThreads + threadIdx.x];
+    p.x += x;
+    p.y += y;
+}
+
 // v[k] for a register array: with NT fixed, a chain of selects instead of a dynamic
 // index, which would move the array to local memory.
 template <int NT>
@@ -213,7 +224,7 @@ template <int NT>
 __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[3], bool zeroE, int m, long long base,
                                            const double2* __restrict__ k0, const double2* __restrict__ k1,
                                            const double2* __restrict__ k2, double2* __restrict__ k3, bool popStep,
-                                           C2* popAcc, double* Pc) {
+                                           double* Pc) {
     constexpr int N2 = NT * NT;
     const double c55 = e.abP[0], cm59 = e.abP[1], c37 = e.abP[2], cm9 = e.abP[3];
     const double c9 = e.abC[0], c19 = e.abC[1], cm5 = e.abC[2], c1 = e.abC[3];
@@ -230,7 +241,10 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
                 for (int i = 0; i < N2; ++i)
                     if (e.hmask >> i & 1u) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
     const double* rhoD = reinterpret_cast<const double*>(e.rho);
-    C2 a[N2], b[N2], r0[N2];
+    // up to three levels the current density stays in registers for the corrector; above,
+    // it is read again (an L1 hit) to leave the registers to the derivative
+    constexpr bool KEEP = NT <= 3;
+    C2 a[N2], b[N2], r0[KEEP ? N2 : 1];
     // predictor on the upper triangle
 #pragma unroll
     for (int c = 0; c < NT; ++c)
@@ -244,7 +258,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
                 p = fma(cm59, reinterpret_cast<const double*>(k1)[2 * o], p);
                 p = fma(c37, reinterpret_cast<const double*>(k2)[2 * o], p);
                 p = fma(cm9, reinterpret_cast<const double*>(k3)[2 * o], p);
-                r0[i] = C2{rr, 0.0};
+                if constexpr (KEEP) r0[i] = C2{rr, 0.0};
                 a[i] = C2{p, 0.0};
             } else {
                 const C2 rr = ld(&e.rho[o]);
@@ -252,7 +266,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
                 p = caxpy(cm59, ld(&k1[o]), p);
                 p = caxpy(c37, ld(&k2[o]), p);
                 p = caxpy(cm9, ld(&k3[o]), p);
-                r0[i] = rr;
+                if constexpr (KEEP) r0[i] = rr;
                 a[i] = p;
             }
         }
@@ -266,14 +280,14 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             const int i = r + c * NT;
             const long long o = base + static_cast<long long>(i) * e.nc;
             if (r == c) {
-                double v = fma(c9, b[i].x, r0[i].x);
+                double v = fma(c9, b[i].x, KEEP ? r0[KEEP ? i : 0].x : rhoD[2 * o]);
                 v = fma(c19, reinterpret_cast<const double*>(k0)[2 * o], v);
                 v = fma(cm5, reinterpret_cast<const double*>(k1)[2 * o], v);
                 v = fma(c1, reinterpret_cast<const double*>(k2)[2 * o], v);
                 a[i] = C2{v, 0.0};
                 reinterpret_cast<double*>(e.rho)[2 * o] = v;
             } else {
-                C2 v = caxpy(c9, b[i], r0[i]);
+                C2 v = caxpy(c9, b[i], KEEP ? r0[KEEP ? i : 0] : ld(&e.rho[o]));
                 v = caxpy(c19, ld(&k0[o]), v);
                 v = caxpy(cm5, ld(&k1[o]), v);
                 v = caxpy(c1, ld(&k2[o]), v);
@@ -295,7 +309,10 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
     if (popStep)
 #pragma unroll
         for (int d = 0; d < kMaxDtc; ++d)
-            if (d < e.nDtc) popAcc[d] = cadd(popAcc[d], pick<NT>(a, e.dtcLev[d]));
+            if (d < e.nDtc) {
+                const C2 v = pick<NT>(a, e.dtcLev[d]);
+                addPop(d, v.x, v.y);
+            }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         if (!e.comp[c]) continue;
@@ -317,9 +334,10 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
     const int q = blk * kEmThreads + threadIdx.x;
     const int s = *stepPtr;
     const bool popStep = (s % e.dtcTimeInt) == 0;
-    C2 popAcc[kMaxDtc];
+    if (popStep)
 #pragma unroll
-    for (int d = 0; d < kMaxDtc; ++d) popAcc[d] = c2(0.0, 0.0);
+        for (int d = 0; d < kMaxDtc; ++d)
+            if (d < e.nDtc) gPopSh[d * kEmThreads + threadIdx.x] = make_double2(0.0, 0.0);
     double Pc[3] = {0.0, 0.0, 0.0};
     if (q < e.nc) {
         // E at the cell centre
@@ -344,7 +362,7 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         double2* __restrict__ k3 = e.kd + s3 * slotStride;
         if constexpr (HERM) {
             for (int m = 0; m < e.nm; ++m)
-                memberHerm<NT>(e, Ec, zeroE, m, static_cast<long long>(m) * n2 * e.nc + q, k0, k1, k2, k3, popStep, popAcc,
+                memberHerm<NT>(e, Ec, zeroE, m, static_cast<long long>(m) * n2 * e.nc + q, k0, k1, k2, k3, popStep,
                                Pc);
         } else {
         C2 H[MAXN2], a[MAXN2], b[MAXN2];
@@ -412,7 +430,10 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
             if (popStep)
 #pragma unroll
                 for (int d = 0; d < kMaxDtc; ++d)
-                    if (d < e.nDtc) popAcc[d] = cadd(popAcc[d], pick<NT>(a, e.dtcLev[d]));
+                    if (d < e.nDtc) {
+                        const C2 v = pick<NT>(a, e.dtcLev[d]);
+                        addPop(d, v.x, v.y);
+                    }
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 if (!e.comp[c]) continue;
@@ -438,8 +459,9 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
 #pragma unroll
         for (int d = 0; d < kMaxDtc; ++d) {
             if (d >= e.nDtc) break;
-            const double sx = blockSum(popAcc[d].x, sh);
-            const double sy = blockSum(popAcc[d].y, sh);
+            const double2 v = gPopSh[d * kEmThreads + threadIdx.x];
+            const double sx = blockSum(v.x, sh);
+            const double sy = blockSum(v.y, sh);
             if (threadIdx.x == 0) e.popPartial[static_cast<long long>(blk) * e.nDtc + d] = make_double2(sx, sy);
         }
     if (e.totP)
@@ -452,7 +474,7 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
 }
 
 template <typename T, int NT, bool HERM = false>
-__global__ void __launch_bounds__(kEmThreads) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
+__global__ void __launch_bounds__(kEmThreads, 1) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
                                                                const T* __restrict__ Ey, const T* __restrict__ Ez,
                                                                const int* __restrict__ stepPtr) {
     updateBlock<T, NT, HERM>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
