@@ -163,39 +163,38 @@ __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex,
 // diagonal is real, (c, r) = conj (r, c). Element (r, c) has storage index r + c N.
 
 // Upper-triangle derivative: out(r, c) = t(r, c) + conj t(c, r) for r < c, and the real
-// diagonal t(r, r) + conj t(r, r) = 2 Re t(r, r); t = (i/hbar) H den, H real.
+// diagonal t(r, r) + conj t(r, r) = 2 Re t(r, r); t = i Hs den with Hs = H / hbar real
+// (scaled once per step). With s(i, j) = sum_l Hs(i, l) den(l, j):
+//   out(i, j) = (-(Im s(i, j) + Im s(j, i)), Re s(i, j) - Re s(j, i)),
+// each sum formed in one FMA chain.
 // hmask: bit i set when element i of H can be nonzero (the diagonal, and wherever a coupled
 // dipole operator is nonzero); products with the other elements are exact zeros and are
 // skipped (the branch is uniform over the emitter). The diagonal of den is real.
 template <int NT>
-__device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, double invHbar, const double* H, const C2* den,
-                                               C2* out, unsigned hmask) {
+__device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, const double* Hs, const C2* den, C2* out, unsigned hmask) {
 #pragma unroll
     for (int i = 0; i < NT; ++i) {
-        // Re t(i, i) = -Im(sum_l H(i, l) den(l, i)) / hbar; den(i, i) is real
+        // Re t(i, i) = -Im s(i, i); den(i, i) is real
         double sy = 0.0;
 #pragma unroll
         for (int l = 0; l < NT; ++l)
-            if (l != i && (hmask >> (i + l * NT) & 1u)) sy = fma(H[i + l * NT], den[l + i * NT].y, sy);
-        const double tx = -invHbar * sy;
-        out[i + i * NT] = C2{tx + tx, 0.0};
+            if (l != i && (hmask >> (i + l * NT) & 1u)) sy = fma(Hs[i + l * NT], den[l + i * NT].y, sy);
+        out[i + i * NT] = C2{-2.0 * sy, 0.0};
 #pragma unroll
         for (int j = i + 1; j < NT; ++j) {
-            C2 sij = c2(0.0, 0.0), sji = c2(0.0, 0.0);
+            double ox = 0.0, oy = 0.0;
 #pragma unroll
             for (int l = 0; l < NT; ++l) {
                 if (hmask >> (i + l * NT) & 1u) {
-                    sij.x = fma(H[i + l * NT], den[l + j * NT].x, sij.x);
-                    if (l != j) sij.y = fma(H[i + l * NT], den[l + j * NT].y, sij.y);
+                    if (l != j) ox = fma(-Hs[i + l * NT], den[l + j * NT].y, ox);
+                    oy = fma(Hs[i + l * NT], den[l + j * NT].x, oy);
                 }
                 if (hmask >> (j + l * NT) & 1u) {
-                    sji.x = fma(H[j + l * NT], den[l + i * NT].x, sji.x);
-                    if (l != i) sji.y = fma(H[j + l * NT], den[l + i * NT].y, sji.y);
+                    if (l != i) ox = fma(-Hs[j + l * NT], den[l + i * NT].y, ox);
+                    oy = fma(-Hs[j + l * NT], den[l + i * NT].x, oy);
                 }
             }
-            const C2 tij = C2{-invHbar * sij.y, invHbar * sij.x};
-            const C2 tji = C2{-invHbar * sji.y, invHbar * sji.x};
-            out[i + j * NT] = cadd(tij, cconj(tji));
+            out[i + j * NT] = C2{ox, oy};
         }
     }
 #pragma unroll
@@ -240,6 +239,9 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
 #pragma unroll
                 for (int i = 0; i < N2; ++i)
                     if (e.hmask >> i & 1u) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
+#pragma unroll
+    for (int i = 0; i < N2; ++i)
+        if (e.hmask >> i & 1u) H[i] *= e.invHbar;
     const double* rhoD = reinterpret_cast<const double*>(e.rho);
     // up to three levels the current density stays in registers for the corrector; above,
     // it is read again (an L1 hit) to leave the registers to the derivative
@@ -271,7 +273,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             }
         }
     mirrorLower<NT>(a);
-    den_deriv_herm<NT>(e, e.invHbar, H, a, b, e.hmask);
+    den_deriv_herm<NT>(e, H, a, b, e.hmask);
     // corrector
 #pragma unroll
     for (int c = 0; c < NT; ++c)
@@ -296,7 +298,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             }
         }
     mirrorLower<NT>(a);
-    den_deriv_herm<NT>(e, e.invHbar, H, a, b, e.hmask);  // derivative at the new density: the next k_n
+    den_deriv_herm<NT>(e, H, a, b, e.hmask);  // derivative at the new density: the next k_n
 #pragma unroll
     for (int c = 0; c < NT; ++c)
 #pragma unroll
@@ -315,11 +317,13 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        if (!e.comp[c]) continue;
-        // Re(conj(a) . mu) with mu real
+        // Re(conj(a) . mu) with mu real: zero for an operator without nonzero elements, and
+        // only the elements hmask marks can be nonzero
+        if (!e.comp[c] || !e.addMu[c]) continue;
         double sdot = 0.0;
 #pragma unroll
-        for (int i = 0; i < N2; ++i) sdot = fma(a[i].x, e.mu[c * N2 + i].x, sdot);
+        for (int i = 0; i < N2; ++i)
+            if (e.hmask >> i & 1u) sdot = fma(a[i].x, e.mu[c * N2 + i].x, sdot);
         Pc[c] += e.na * sdot;
     }
 }
