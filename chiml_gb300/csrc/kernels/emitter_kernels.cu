@@ -162,6 +162,28 @@ __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex,
 // H = h0 - E . mu is real symmetric. The step then needs only the upper triangle: the
 // diagonal is real, (c, r) = conj (r, c). Element (r, c) has storage index r + c N.
 
+// Element (r, c) of a Hermitian matrix of which only the upper triangle (r <= c) is held,
+// at storage index r + c NT; the lower triangle is the conjugate of its mirror. With r and
+// c known at compile time the lower elements cost no registers.
+template <int NT>
+__device__ __forceinline__ C2 hel(const C2* a, int r, int c) {
+    return r <= c ? a[r + c * NT] : C2{a[c + r * NT].x, -a[c + r * NT].y};
+}
+// Element (r, c) of a real symmetric matrix held as its upper triangle.
+template <int NT>
+__device__ __forceinline__ double sel(const double* h, int r, int c) {
+    return r <= c ? h[r + c * NT] : h[c + r * NT];
+}
+// hel at a flat index k = r + c NT known only at run time: a chain of selects.
+template <int NT>
+__device__ __forceinline__ C2 pickHerm(const C2* a, int k) {
+    C2 r = a[0];
+#pragma unroll
+    for (int i = 1; i < NT * NT; ++i)
+        if (k == i) r = hel<NT>(a, i % NT, i / NT);
+    return r;
+}
+
 // Upper-triangle derivative: out(r, c) = t(r, c) + conj t(c, r) for r < c, and the real
 // diagonal t(r, r) + conj t(r, r) = 2 Re t(r, r); t = i Hs den with Hs = H / hbar real
 // (scaled once per step). With s(i, j) = sum_l Hs(i, l) den(l, j):
@@ -178,7 +200,7 @@ __device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, const double
         double sy = 0.0;
 #pragma unroll
         for (int l = 0; l < NT; ++l)
-            if (l != i && (hmask >> (i + l * NT) & 1u)) sy = fma(Hs[i + l * NT], den[l + i * NT].y, sy);
+            if (l != i && (hmask >> (i + l * NT) & 1u)) sy = fma(sel<NT>(Hs, i, l), hel<NT>(den, l, i).y, sy);
         out[i + i * NT] = C2{-2.0 * sy, 0.0};
 #pragma unroll
         for (int j = i + 1; j < NT; ++j) {
@@ -186,12 +208,14 @@ __device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, const double
 #pragma unroll
             for (int l = 0; l < NT; ++l) {
                 if (hmask >> (i + l * NT) & 1u) {
-                    if (l != j) ox = fma(-Hs[i + l * NT], den[l + j * NT].y, ox);
-                    oy = fma(Hs[i + l * NT], den[l + j * NT].x, oy);
+                    const C2 d = hel<NT>(den, l, j);
+                    if (l != j) ox = fma(-sel<NT>(Hs, i, l), d.y, ox);
+                    oy = fma(sel<NT>(Hs, i, l), d.x, oy);
                 }
                 if (hmask >> (j + l * NT) & 1u) {
-                    if (l != i) ox = fma(-Hs[j + l * NT], den[l + i * NT].y, ox);
-                    oy = fma(-Hs[j + l * NT], den[l + i * NT].x, oy);
+                    const C2 d = hel<NT>(den, l, i);
+                    if (l != i) ox = fma(-sel<NT>(Hs, j, l), d.y, ox);
+                    oy = fma(-sel<NT>(Hs, j, l), d.x, oy);
                 }
             }
             out[i + j * NT] = C2{ox, oy};
@@ -201,19 +225,11 @@ __device__ __forceinline__ void den_deriv_herm(const EmitterDev& e, const double
     for (int ii = 0; ii < NT * NT; ++ii) {
         if ((ii % NT) > (ii / NT)) continue;  // lower triangle: the conjugate of its mirror
         for (int p = e.gamRow[ii]; p < e.gamRow[ii + 1]; ++p) {
-            const C2 d = pick<NT>(den, e.gamCol[p]);
+            const C2 d = pickHerm<NT>(den, e.gamCol[p]);
             const double g = e.gamVal[p];
             out[ii] = C2{fma(d.x, g, out[ii].x), (ii % NT) == (ii / NT) ? 0.0 : fma(d.y, g, out[ii].y)};
         }
     }
-}
-
-template <int NT>
-__device__ __forceinline__ void mirrorLower(C2* a) {
-#pragma unroll
-    for (int r = 0; r < NT; ++r)
-#pragma unroll
-        for (int c = r + 1; c < NT; ++c) a[c + r * NT] = cconj(a[r + c * NT]);
 }
 
 // One ensemble member of one cell in the Hermitian form: loads and stores the upper
@@ -227,6 +243,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
     constexpr int N2 = NT * NT;
     const double c55 = e.abP[0], cm59 = e.abP[1], c37 = e.abP[2], cm9 = e.abP[3];
     const double c9 = e.abC[0], c19 = e.abC[1], cm5 = e.abC[2], c1 = e.abC[3];
+    // H / hbar, upper triangle (H is real symmetric)
     double H[N2];
 #pragma unroll
     for (int i = 0; i < N2; ++i) H[i] = 0.0;
@@ -238,10 +255,10 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
             if (e.addMu[c])
 #pragma unroll
                 for (int i = 0; i < N2; ++i)
-                    if (e.hmask >> i & 1u) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
+                    if ((i % NT) <= (i / NT) && (e.hmask >> i & 1u)) H[i] = fma(Ec[c], e.negMu[c * N2 + i].x, H[i]);
 #pragma unroll
     for (int i = 0; i < N2; ++i)
-        if (e.hmask >> i & 1u) H[i] *= e.invHbar;
+        if ((i % NT) <= (i / NT) && (e.hmask >> i & 1u)) H[i] *= e.invHbar;
     const double* rhoD = reinterpret_cast<const double*>(e.rho);
     // up to three levels the current density stays in registers for the corrector; above,
     // it is read again (an L1 hit) to leave the registers to the derivative
@@ -272,7 +289,6 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
                 a[i] = p;
             }
         }
-    mirrorLower<NT>(a);
     den_deriv_herm<NT>(e, H, a, b, e.hmask);
     // corrector
 #pragma unroll
@@ -297,7 +313,6 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
                 st(&e.rho[o], v);
             }
         }
-    mirrorLower<NT>(a);
     den_deriv_herm<NT>(e, H, a, b, e.hmask);  // derivative at the new density: the next k_n
 #pragma unroll
     for (int c = 0; c < NT; ++c)
@@ -312,7 +327,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
 #pragma unroll
         for (int d = 0; d < kMaxDtc; ++d)
             if (d < e.nDtc) {
-                const C2 v = pick<NT>(a, e.dtcLev[d]);
+                const C2 v = pickHerm<NT>(a, e.dtcLev[d]);
                 addPop(d, v.x, v.y);
             }
 #pragma unroll
@@ -323,7 +338,7 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
         double sdot = 0.0;
 #pragma unroll
         for (int i = 0; i < N2; ++i)
-            if (e.hmask >> i & 1u) sdot = fma(a[i].x, e.mu[c * N2 + i].x, sdot);
+            if (e.hmask >> i & 1u) sdot = fma(hel<NT>(a, i % NT, i / NT).x, e.mu[c * N2 + i].x, sdot);
         Pc[c] += e.na * sdot;
     }
 }
