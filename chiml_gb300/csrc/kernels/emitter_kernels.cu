@@ -113,20 +113,6 @@ __device__ __forceinline__ void den_deriv(const EmitterDev& e, int N, double inv
         }
 }
 
-// Sum over the block of one value per thread, in a fixed order (warp shuffle tree,
-// then the warps in order); the result is valid in thread 0.
-__device__ __forceinline__ double blockSum(double v, double* sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int w = 0; w < kEmThreads / 32; ++w) r += sh[w];
-    __syncthreads();
-    return r;
-}
-
 // addP of component c over points t = tBegin, tBegin + tStride, ...
 template <typename T>
 __device__ __forceinline__ void addpRange(const EmitterDev& e, T* Ex, T* Ey, T* Ez, int c, int tBegin, int tStride) {
@@ -472,24 +458,39 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         for (int c = 0; c < 3; ++c)
             if (e.comp[c]) e.P[static_cast<long long>(c) * e.pBox + e.cellP[q]] = Pc[c];
     }
-    // block partial sums of the quantities this step outputs (block-uniform conditions)
-    __shared__ double sh[kEmThreads / 32];
-    if (popStep)
+    // Block partial sums of the quantities this step outputs (block-uniform conditions): each
+    // quantity's kEmThreads per-thread values sit in shared memory; four threads sum 32 of
+    // them each and two shuffles combine the four (a quarter of the additions of a tree over
+    // every thread, on the FP64 pipe this kernel is bound by).
+    static_assert(4 * (2 * kMaxDtc + 3) <= kEmThreads, "four threads per summed quantity");
+    __shared__ double pSh[3 * kEmThreads];
+    const bool doP = e.totP != nullptr;
+    if (!popStep && !doP) return;
 #pragma unroll
-        for (int d = 0; d < kMaxDtc; ++d) {
-            if (d >= e.nDtc) break;
-            const double2 v = gPopSh[d * kEmThreads + threadIdx.x];
-            const double sx = blockSum(v.x, sh);
-            const double sy = blockSum(v.y, sh);
-            if (threadIdx.x == 0) e.popPartial[static_cast<long long>(blk) * e.nDtc + d] = make_double2(sx, sy);
+    for (int c = 0; c < 3; ++c) pSh[c * kEmThreads + threadIdx.x] = Pc[c];
+    __syncthreads();
+    const int nPop = popStep ? 2 * e.nDtc : 0;  // tasks: populations (x, y), then P x, y, z
+    const int nTask = nPop + (doP ? 3 : 0);
+    const int task = threadIdx.x >> 2, part = threadIdx.x & 3;
+    double sum = 0.0;
+    if (task < nTask) {
+        const bool pop = task < nPop;
+        const double* src = pop ? reinterpret_cast<const double*>(gPopSh) + 2 * (task >> 1) * kEmThreads + (task & 1)
+                                : pSh + (task - nPop) * kEmThreads;
+        const int stride = pop ? 2 : 1;
+#pragma unroll 8
+        for (int j = part * (kEmThreads / 4); j < (part + 1) * (kEmThreads / 4); ++j) sum += src[j * stride];
+    }
+    sum += __shfl_down_sync(0xffffffffu, sum, 2, 4);
+    sum += __shfl_down_sync(0xffffffffu, sum, 1, 4);
+    if (part == 0 && task < nTask) {
+        if (task < nPop) {
+            double* dst = reinterpret_cast<double*>(&e.popPartial[static_cast<long long>(blk) * e.nDtc + (task >> 1)]);
+            dst[task & 1] = sum;
+        } else if (e.comp[task - nPop]) {
+            e.totPartial[blk * 3 + (task - nPop)] = sum;
         }
-    if (e.totP)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            if (!e.comp[c]) continue;
-            const double v = blockSum(Pc[c], sh);
-            if (threadIdx.x == 0) e.totPartial[blk * 3 + c] = v;
-        }
+    }
 }
 
 template <typename T, int NT, bool HERM = false>
