@@ -160,14 +160,21 @@ template <int NT>
 __device__ __forceinline__ double sel(const double* h, int r, int c) {
     return r <= c ? h[r + c * NT] : h[c + r * NT];
 }
-// hel at a flat index k = r + c NT known only at run time: a chain of selects.
+// hel at a flat index k = r + c NT known only at run time: a chain of selects over the
+// upper triangle, and for a lower element the sign of the imaginary part flipped by an
+// integer operation (keeping the FP64 pipe, which bounds the update, free of it).
 template <int NT>
 __device__ __forceinline__ C2 pickHerm(const C2* a, int k) {
-    C2 r = a[0];
+    const int r = k % NT, c = k / NT;
+    const bool lower = r > c;
+    const int ku = lower ? c + r * NT : k;
+    C2 v = a[0];
 #pragma unroll
     for (int i = 1; i < NT * NT; ++i)
-        if (k == i) r = hel<NT>(a, i % NT, i / NT);
-    return r;
+        if ((i % NT) <= (i / NT) && ku == i) v = a[i];
+    const unsigned long long flip = lower ? 0x8000000000000000ULL : 0ULL;
+    v.y = __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(__double_as_longlong(v.y)) ^ flip));
+    return v;
 }
 
 // Upper-triangle derivative: out(r, c) = t(r, c) + conj t(c, r) for r < c, and the real
