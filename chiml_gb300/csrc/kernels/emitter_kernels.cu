@@ -507,45 +507,52 @@ __global__ void __launch_bounds__(kEmThreads, 1) k_emitter_update(const EmitterD
     updateBlock<T, NT, HERM>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
 }
 
-__device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __restrict__ stepPtr) {
+// Quantity k of the step's outputs (populations x / y per detector, then total P x, y, z)
+// summed over the block partials by one block, in a fixed order: thread t takes partials
+// t, t + 256, ... into four accumulators in turn, then a tree over the threads.
+constexpr int kReduceQuantities = 2 * kMaxDtc + 3;
+__device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __restrict__ stepPtr, int k) {
     const int s = *stepPtr;
     __shared__ double red[256];
     const bool popStep = (s % e.dtcTimeInt) == 0;
-    const int nq = 2 * e.nDtc + 3;
-    for (int k = 0; k < nq; ++k) {
-        const bool isPop = k < 2 * e.nDtc;
-        if (isPop && !popStep) continue;
-        if (!isPop && (!e.totP || s >= e.nSteps)) continue;
-        double v = 0.0;
-        for (int b = threadIdx.x; b < e.partialBlocks; b += blockDim.x) {
-            if (isPop) {
-                const double2 p = e.popPartial[static_cast<long long>(b) * e.nDtc + k / 2];
-                v += (k & 1) ? p.y : p.x;
-            } else {
-                v += e.totPartial[b * 3 + (k - 2 * e.nDtc)];
-            }
+    if (k >= 2 * e.nDtc + 3) return;
+    const bool isPop = k < 2 * e.nDtc;
+    if (isPop && !popStep) return;
+    if (!isPop && (!e.totP || s >= e.nSteps)) return;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    int q = 0;
+    for (int b = threadIdx.x; b < e.partialBlocks; b += blockDim.x, q = (q + 1) & 3) {
+        double x;
+        if (isPop) {
+            const double2 p = e.popPartial[static_cast<long long>(b) * e.nDtc + k / 2];
+            x = (k & 1) ? p.y : p.x;
+        } else {
+            x = e.totPartial[b * 3 + (k - 2 * e.nDtc)];
         }
-        red[threadIdx.x] = v;
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+            if (a == q) v[a] += x;
+    }
+    red[threadIdx.x] = (v[0] + v[1]) + (v[2] + v[3]);
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (isPop) {
+            double* dst = reinterpret_cast<double*>(&e.pop[static_cast<long long>(k / 2) * e.nEvents + s / e.dtcTimeInt]);
+            dst[k & 1] = red[0] / e.nPoints;
+        } else {
+            const int c = k - 2 * e.nDtc;
+            if (e.comp[c]) e.totP[static_cast<long long>(c) * e.nSteps + s] = red[0];
         }
-        if (threadIdx.x == 0) {
-            if (isPop) {
-                double* dst = reinterpret_cast<double*>(&e.pop[static_cast<long long>(k / 2) * e.nEvents + s / e.dtcTimeInt]);
-                dst[k & 1] = red[0] / e.nPoints;
-            } else {
-                const int c = k - 2 * e.nDtc;
-                if (e.comp[c]) e.totP[static_cast<long long>(c) * e.nSteps + s] = red[0];
-            }
-        }
-        __syncthreads();
     }
 }
 
+// one block per output quantity (blockIdx.y)
 __global__ void __launch_bounds__(256) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
-    reduceBody(e, stepPtr);
+    reduceBody(e, stepPtr, blockIdx.y);
 }
 
 // ---- packed launches (batched sweep): work[b] = {job, block of that job} ----
@@ -570,7 +577,7 @@ __global__ void __launch_bounds__(kEmThreads) k_emitter_update_packed(const Emit
 template <typename T>
 __global__ void __launch_bounds__(256) k_emitter_reduce_packed(const EmitJob<T>* __restrict__ jobs) {
     const EmitJob<T>& j = jobs[blockIdx.x];
-    reduceBody(j.e, j.step);
+    reduceBody(j.e, j.step, blockIdx.y);
 }
 
 }  // namespace
@@ -596,7 +603,7 @@ void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, cons
         k_emitter_update_packed<T, 3, true><<<update[5].blocks, kEmThreads, 0, s>>>(jobs, update[5].work);
     if (update[6].blocks > 0)
         k_emitter_update_packed<T, 4, true><<<update[6].blocks, kEmThreads, 0, s>>>(jobs, update[6].work);
-    k_emitter_reduce_packed<T><<<njobs, 256, 0, s>>>(jobs);
+    k_emitter_reduce_packed<T><<<dim3(njobs, kReduceQuantities), 256, 0, s>>>(jobs);
 }
 
 template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[7], void*);
@@ -618,7 +625,7 @@ void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* ste
         case 4: k_emitter_update<T, 4><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
         default: k_emitter_update<T, 0><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
     }
-    k_emitter_reduce<<<1, 256, 0, s>>>(e, step);
+    k_emitter_reduce<<<dim3(1, kReduceQuantities), 256, 0, s>>>(e, step);
 }
 
 template void launch_emitter_step<float>(const EmitterDev&, float* const[3], const int*, void*);
