@@ -37,6 +37,9 @@ N_DEFAULT = 256
 MEASURED_TRAFFIC_PER_CELL = {"h_pass": 749.6e6 / 16777216, "e_pass": 798.6e6 / 16777216}
 
 
+NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e nominal bandwidth, reported beside the measured copy peak
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -303,6 +306,7 @@ def run_ours(args):
                      "kernel_ms": {k: round(v, 4) for k, v in fp_prof.items()}},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "frac_of_nominal": round(achieved / NOMINAL_HBM_GBS, 4),
                          "traffic": (round(MEASURED_TRAFFIC_PER_CELL[dom] * cells, 0)
                                      if dom in MEASURED_TRAFFIC_PER_CELL else None),
                          "traffic_source": "ncu dram bytes per cell at 256^3, scaled to this workload's cells",
@@ -471,7 +475,8 @@ def run_batch(args):
         "sequential": {"value": round(seq_value, 3), "unit": "Gcell-updates/s", "seconds": round(t_seq, 3),
                        "batch_speedup": round(value / seq_value, 2)},
         "roofline": {"bound": "hbm", "kernel": "whole packed step", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "frac_of_nominal": round(achieved / NOMINAL_HBM_GBS, 4), "traffic": None,
                      "bytes_per_step": step_bytes},
         "gpu_launches": None, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
     }
