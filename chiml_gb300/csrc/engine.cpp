@@ -592,17 +592,15 @@ private:
             const std::vector<TfsfSegment>* segs[2] = {&tp.segH, &tp.segE};
             for (int w = 0; w < 2; ++w) {
                 // rows split into runs of single-term cells; the cells with several terms
-                // (face edges) go to the per-cell list
-                std::vector<long long> keys;
+                // (face edges, few) go to the per-cell list
+                const TfsfAdds& a = *adds[w];
                 long long nTerms = 0;
-                for (const TfsfSegment& g : *segs[w])
-                    for (int r = 0; r < g.n; ++r) keys.push_back(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride);
-                nTerms = static_cast<long long>(keys.size());
-                std::sort(keys.begin(), keys.end());
-                auto multi = [&](long long key) {
-                    auto lo = std::lower_bound(keys.begin(), keys.end(), key);
-                    return (lo + 1) != keys.end() && *(lo + 1) == key;
-                };
+                for (const TfsfSegment& g : *segs[w]) nTerms += g.n;
+                std::vector<long long> multiKeys;
+                for (std::size_t q = 0; q < a.cells(); ++q)
+                    if (a.start[q + 1] - a.start[q] > 1) multiKeys.push_back(a.comp[q] * P.dims.cells() + a.cell[q]);
+                std::sort(multiKeys.begin(), multiKeys.end());
+                auto multi = [&](long long key) { return std::binary_search(multiKeys.begin(), multiKeys.end(), key); };
                 std::vector<dev::TfsfSegDev> sd;
                 std::vector<int2> sw;
                 for (const TfsfSegment& g : *segs[w]) {
@@ -636,7 +634,6 @@ private:
                 std::vector<long long> cell;
                 std::vector<int> comp, start, tl, ti;
                 std::vector<double> pref;
-                const TfsfAdds& a = *adds[w];
                 if (static_cast<long long>(a.terms()) != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
                 for (std::size_t q = 0; q < a.cells(); ++q) {
                     if (a.start[q + 1] - a.start[q] < 2) continue;  // in a row
