@@ -1245,8 +1245,8 @@ private:
             for (int n = 0; n < nSamples; ++n)
                 for (int f = 0; f < nf; ++f) {
                     std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * freqs[f]));
-                    ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 0] = static_cast<T>(e.real());
-                    ph[(static_cast<std::size_t>(n) * nfPad + f) * 2 + 1] = static_cast<T>(e.imag());
+                    ph[(static_cast<std::size_t>(n) * 2 + 0) * nfPad + f] = static_cast<T>(e.real());
+                    ph[(static_cast<std::size_t>(n) * 2 + 1) * nfPad + f] = static_cast<T>(e.imag());
                 }
             const int K = dftBlockLength(static_cast<long long>(cell.size()), nSamples);
             d.npts = static_cast<long long>(cell.size());

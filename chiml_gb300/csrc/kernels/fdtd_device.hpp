@@ -176,7 +176,7 @@ struct DftTable {
     long long stride;           // ring row pitch: points rounded up to a multiple of 128
     const int* comp;            // per point
     const int* cell;            // per point (grid index)
-    const T* phasor;            // [(sample * nfreqPad + f) * 2 + {0: cos, 1: -sin}]
+    const T* phasor;            // [(sample * 2 + {0: cos, 1: -sin}) * nfreqPad + f]
     T* ring;                    // [K][stride]
     double* re;                 // [pt * nfreq + f]
     double* im;

@@ -622,7 +622,7 @@ __device__ __forceinline__ void foldTiles(const DftTable<T>& d, const int* step,
     constexpr int KS = FoldCfg<T>::KS;
     constexpr int EV = 16 / sizeof(T);  // values per 16-byte copy
     __shared__ __align__(16) T smp[2][KS][kFoldTP];
-    __shared__ __align__(16) T ph[2][KS][kFoldTF * 2];  // cos, -sin pairs
+    __shared__ __align__(16) T ph[2][KS][kFoldTF * 2];  // per sample: kFoldTF cos, then kFoldTF -sin
     int count, first;
     if (flushCount > 0) {
         count = flushCount;
@@ -658,9 +658,10 @@ __device__ __forceinline__ void foldTiles(const DftTable<T>& d, const int* step,
             }
             for (int q = threadIdx.x; q < KS * (kFoldTF * 2 / EV); q += blockDim.x) {
                 const int k = q / (kFoldTF * 2 / EV), c = q % (kFoldTF * 2 / EV);
+                const int plane = c / (kFoldTF / EV), cc = c % (kFoldTF / EV);
                 if (k < kn)
-                    cpAsync16(&ph[b][k][c * EV],
-                              d.phasor + (static_cast<long long>(first + k0 + k) * d.nfreqPad + f0) * 2 + c * EV);
+                    cpAsync16(&ph[b][k][plane * kFoldTF + cc * EV],
+                              d.phasor + (static_cast<long long>(first + k0 + k) * 2 + plane) * d.nfreqPad + f0 + cc * EV);
             }
             cpAsyncCommit();
         };
@@ -679,12 +680,12 @@ __device__ __forceinline__ void foldTiles(const DftTable<T>& d, const int* step,
             const int b = sg & 1;
             const int kn = min(KS, count - sg * KS);
             for (int k = 0; k < kn; ++k) {
-                T v[4], cs0[4], cs1[4];
+                // the eight threads of a point group read consecutive 16-byte chunks of each
+                // phasor plane: no bank conflicts
+                T v[4], c[4], sn[4];
                 lds4(&smp[b][k][4 * tp], v);
-                lds4(&ph[b][k][8 * tf], cs0);      // cos f, -sin f, cos f+1, -sin f+1
-                lds4(&ph[b][k][8 * tf + 4], cs1);  // f+2, f+3
-                const T c[4] = {cs0[0], cs0[2], cs1[0], cs1[2]};
-                const T sn[4] = {cs0[1], cs0[3], cs1[1], cs1[3]};
+                lds4(&ph[b][k][4 * tf], c);             // cos of frequencies 4 tf .. 4 tf + 3
+                lds4(&ph[b][k][kFoldTF + 4 * tf], sn);  // -sin
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
 #pragma unroll
