@@ -508,34 +508,44 @@ __global__ void __launch_bounds__(kEmThreads, 1) k_emitter_update(const EmitterD
 }
 
 // Quantity k of the step's outputs (populations x / y per detector, then total P x, y, z)
-// summed over the block partials by one block, in a fixed order: thread t takes partials
-// t, t + 256, ... into four accumulators in turn, then a tree over the threads.
+// summed over the block partials by one block, in a fixed order: thread t takes the
+// partials t + j * kReduceThreads, four independent loads at a time into four
+// accumulators, then a tree over the threads.
 constexpr int kReduceQuantities = 2 * kMaxDtc + 3;
+constexpr int kReduceThreads = 1024;
+__device__ __forceinline__ double reducePartial(const EmitterDev& e, bool isPop, int k, int b) {
+    if (isPop) {
+        const double2 p = e.popPartial[static_cast<long long>(b) * e.nDtc + k / 2];
+        return (k & 1) ? p.y : p.x;
+    }
+    return e.totPartial[b * 3 + (k - 2 * e.nDtc)];
+}
 __device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __restrict__ stepPtr, int k) {
     const int s = *stepPtr;
-    __shared__ double red[256];
+    __shared__ double red[kReduceThreads];
     const bool popStep = (s % e.dtcTimeInt) == 0;
     if (k >= 2 * e.nDtc + 3) return;
     const bool isPop = k < 2 * e.nDtc;
     if (isPop && !popStep) return;
     if (!isPop && (!e.totP || s >= e.nSteps)) return;
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
-    int q = 0;
-    for (int b = threadIdx.x; b < e.partialBlocks; b += blockDim.x, q = (q + 1) & 3) {
-        double x;
-        if (isPop) {
-            const double2 p = e.popPartial[static_cast<long long>(b) * e.nDtc + k / 2];
-            x = (k & 1) ? p.y : p.x;
-        } else {
-            x = e.totPartial[b * 3 + (k - 2 * e.nDtc)];
-        }
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-            if (a == q) v[a] += x;
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+    const int n = e.partialBlocks;
+    constexpr int R = kReduceThreads;
+    int b = threadIdx.x;
+    for (; b + 3 * R < n; b += 4 * R) {
+        const double x0 = reducePartial(e, isPop, k, b), x1 = reducePartial(e, isPop, k, b + R);
+        const double x2 = reducePartial(e, isPop, k, b + 2 * R), x3 = reducePartial(e, isPop, k, b + 3 * R);
+        v0 += x0;
+        v1 += x1;
+        v2 += x2;
+        v3 += x3;
     }
-    red[threadIdx.x] = (v[0] + v[1]) + (v[2] + v[3]);
+    if (b < n) v0 += reducePartial(e, isPop, k, b);
+    if (b + R < n) v1 += reducePartial(e, isPop, k, b + R);
+    if (b + 2 * R < n) v2 += reducePartial(e, isPop, k, b + 2 * R);
+    red[threadIdx.x] = (v0 + v1) + (v2 + v3);
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = R / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
@@ -551,7 +561,7 @@ __device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __res
 }
 
 // one block per output quantity (blockIdx.y)
-__global__ void __launch_bounds__(256) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
+__global__ void __launch_bounds__(kReduceThreads) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
     reduceBody(e, stepPtr, blockIdx.y);
 }
 
@@ -575,7 +585,7 @@ __global__ void __launch_bounds__(kEmThreads) k_emitter_update_packed(const Emit
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_emitter_reduce_packed(const EmitJob<T>* __restrict__ jobs) {
+__global__ void __launch_bounds__(kReduceThreads) k_emitter_reduce_packed(const EmitJob<T>* __restrict__ jobs) {
     const EmitJob<T>& j = jobs[blockIdx.x];
     reduceBody(j.e, j.step, blockIdx.y);
 }
@@ -603,7 +613,7 @@ void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, cons
         k_emitter_update_packed<T, 3, true><<<update[5].blocks, kEmThreads, 0, s>>>(jobs, update[5].work);
     if (update[6].blocks > 0)
         k_emitter_update_packed<T, 4, true><<<update[6].blocks, kEmThreads, 0, s>>>(jobs, update[6].work);
-    k_emitter_reduce_packed<T><<<dim3(njobs, kReduceQuantities), 256, 0, s>>>(jobs);
+    k_emitter_reduce_packed<T><<<dim3(njobs, kReduceQuantities), kReduceThreads, 0, s>>>(jobs);
 }
 
 template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[7], void*);
@@ -625,7 +635,7 @@ void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* ste
         case 4: k_emitter_update<T, 4><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
         default: k_emitter_update<T, 0><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
     }
-    k_emitter_reduce<<<dim3(1, kReduceQuantities), 256, 0, s>>>(e, step);
+    k_emitter_reduce<<<dim3(1, kReduceQuantities), kReduceThreads, 0, s>>>(e, step);
 }
 
 template void launch_emitter_step<float>(const EmitterDev&, float* const[3], const int*, void*);
