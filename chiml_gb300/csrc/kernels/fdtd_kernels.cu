@@ -428,8 +428,18 @@ __device__ __forceinline__ void pass3d(const Pass<T>& p) {
     else pass3dRun<T, EPASS, CI, I, CY, PD, false>(p, x, z, y0, y1);
 }
 
+// Resident blocks per SM the register budget is sized for: full occupancy (32 registers)
+// for the FP32 forms with 32-bit indices.
+#ifndef CHIML_E_MINB
+#define CHIML_E_MINB 8
+#endif
+template <typename T, bool EPASS, typename I>
+constexpr int passMinBlocks() {
+    return sizeof(T) == 4 ? (sizeof(I) == 4 ? (EPASS ? CHIML_E_MINB : 8) : 6) : 4;
+}
+
 template <typename T, bool EPASS, typename I, int CY, int PD>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (sizeof(I) == 4 ? 8 : 6) : 4) k_pass3d(const Pass<T> p) {
+__global__ void __launch_bounds__(256, passMinBlocks<T, EPASS, I>()) k_pass3d(const Pass<T> p) {
     const int ci = blockIdx.z % 3;
     if (ci == 0) pass3d<T, EPASS, 0, I, CY, PD>(p);
     else if (ci == 1) pass3d<T, EPASS, 1, I, CY, PD>(p);
