@@ -746,15 +746,20 @@ struct Builder {
             TermPlan& T = tp[t];
             double base = 0.0;
             for (auto& e : grid[t]) {
+                // a run moves along one grid axis: its coordinate along T.axis is c0 + q dq
+                const int c0 = coordOf(e.ind, T.axis);
+                const int dq = e.n > 1 ? coordOf(e.ind + e.stride, T.axis) - c0 : 0;
+                if (e.n > 1 && coordOf(e.ind + (e.n - 1) * e.stride, T.axis) != c0 + (e.n - 1) * dq)
+                    throw InputError("CPML run does not follow one grid axis");
+                if (e.indOff - e.ind != T.off) throw InputError("CPML offset does not match the curl offset");
                 for (int q = 0; q < e.n; ++q) {
                     long long id = e.ind + q * e.stride;
-                    if (e.indOff + q * e.stride - id != T.off) throw InputError("CPML offset does not match the curl offset");
                     coef[t][id] += e.DbField;
                     npsi[t][id] += 1;
                     if (e.slab == T.axis) {
                         if (kflag[t][id]) throw UnsupportedError("overlapping CPML slabs along one axis");
                         kflag[t][id] = 1;
-                        int a = coordOf(id, T.axis);
+                        int a = c0 + q * dq;
                         if (T.kprof[a] != 0.0 && T.kprof[a] != e.DbField)
                             throw UnsupportedError("CPML coefficient is not a function of the normal coordinate");
                         T.kprof[a] = e.DbField;
@@ -768,9 +773,9 @@ struct Builder {
             }
             T.db = base;
             for (auto& e : psi[t]) {
+                if (e.indOff - e.ind != T.off) throw InputError("psi offset does not match the curl offset");
                 for (int q = 0; q < e.n; ++q) {
                     long long id = e.ind + q * e.stride;
-                    if (e.indOff + q * e.stride - id != T.off) throw InputError("psi offset does not match the curl offset");
                     if (psiUpd[t][id]) throw UnsupportedError("a psi cell is updated twice");
                     psiUpd[t][id] = 1;
                     int a = e.normCoord;
@@ -889,7 +894,7 @@ struct Builder {
                             // check the compressed CPML coefficient against the literal sum
                             for (int t = 0; t < 2; ++t) {
                                 if (!tp[t].present) continue;
-                                const int a = coordOf(static_cast<long long>(id), tp[t].axis);
+                                const int a = tp[t].axis == 0 ? x : (tp[t].axis == 1 ? y : z);
                                 double comp = c.nplain[t] * tp[t].db + (c.kflag[t] ? tp[t].kprof[a] : 0.0);
                                 double lit = coef[t][id];
                                 if (std::abs(comp - lit) > 1e-14 * std::max(1.0, std::abs(lit)) * std::abs(dt))
