@@ -456,12 +456,9 @@ private:
         dev::launch_sources<T>(src_, fields_, dStep_, s);
         dev::launch_pass<T>(ePass_, true, s);
         launchEmitters(s);
-        dev::launch_increment(dStep_, s);
-        dev::launch_record<T>(recT_, fields_, dStep_, s);
-        for (auto& d : dft_) {
-            dev::launch_dft_sample<T>(d, fields_, dStep_, s);
-            dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
-        }
+        // records, DFT samples and the step counter in one launch, then the folds
+        dev::launch_step_tail<T>(tail_, s);
+        for (auto& d : dft_) dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
     }
 
     // ---- the device layout: rows padded from lx to pitch_ values ----
@@ -588,6 +585,7 @@ private:
                 }
             t.pulseTab = mem_.upload(tab);
             t.rec = mem_.alloc<double2>(6 * 2 * (static_cast<std::size_t>(P.nSteps) + 1));
+            t.ticket = mem_.alloc<unsigned int>(1);
             const TfsfAdds* adds[2] = {&tp.addH, &tp.addE};
             const std::vector<TfsfSegment>* segs[2] = {&tp.segH, &tp.segE};
             for (int w = 0; w < 2; ++w) {
@@ -1267,6 +1265,7 @@ private:
     }
 
     std::vector<long long> classCount_[6];  // cells of each class, per component
+    dev::StepTail<T> tail_{};
 
     void uploadTail() {
         bytesPerCell_ = algorithmicBytesPerCell();
@@ -1276,8 +1275,21 @@ private:
         ePass_.err = dErr_;
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
-        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + (recT_.n ? 1 : 0) + 2 * static_cast<int>(dft_.size()) +
-                          (ePass_.nLor > 0 ? 1 : 0) + 3 * static_cast<int>(emit_.size()) + 3 * static_cast<int>(tfsf_.size());
+        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + static_cast<int>(dft_.size()) + (ePass_.nLor > 0 ? 1 : 0) + (ePass_.od.n > 0 ? 1 : 0) +
+                          3 * static_cast<int>(emit_.size()) + 2 * static_cast<int>(tfsf_.size());
+        // the step tail: record blocks, then each DFT table's sample blocks
+        tail_ = dev::StepTail<T>{};
+        tail_.rec = recT_;
+        tail_.recBlocks = (recT_.n + 255) / 256;
+        tail_.nDft = static_cast<int>(dft_.size());
+        std::vector<int> start(1, 0);
+        for (auto& d : dft_) start.push_back(start.back() + static_cast<int>((d.npts + 255) / 256));
+        tail_.dft = mem_.upload(dft_);
+        tail_.dftStart = mem_.upload(start);
+        tail_.f = fields_;
+        tail_.step = dStep_;
+        tail_.ticket = mem_.alloc<unsigned int>(1);
+        tail_.blocks = std::max(1, tail_.recBlocks + start.back());
         // t = 0 samples (parallelFDTDField.cpp:831-837)
         dev::launch_record<T>(recT_, fields_, dStep_, stream_);
         for (auto& d : dft_) dev::launch_dft_sample<T>(d, fields_, dStep_, stream_);

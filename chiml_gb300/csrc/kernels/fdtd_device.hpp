@@ -209,6 +209,23 @@ struct WorkMap {
     int blocks;
 };
 
+// The end of a step in one launch: the detector records and the DFT samples of the
+// step after the counter's increment, then the increment itself, done by the block that
+// finishes last (a ticket counter, no waiting). Blocks [0, recBlocks) record, then the
+// DFT tables' sample blocks follow in order, table q from dftStart[q].
+template <typename T>
+struct StepTail {
+    RecordTable rec;
+    int recBlocks;
+    int nDft;
+    const DftTable<T>* dft;  // [nDft] (device)
+    const int* dftStart;     // [nDft + 1] block offsets after the record blocks (device)
+    Fields<T> f;
+    int* step;
+    unsigned int* ticket;    // zero between launches
+    int blocks;              // recBlocks + the sample blocks of every table (at least 1)
+};
+
 // Launchers (fdtd_kernels.cu). All run on the given stream.
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream);
@@ -224,6 +241,8 @@ void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step
 template <typename T>
 void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream);
 void launch_increment(int* step, void* stream);
+template <typename T>
+void launch_step_tail(const StepTail<T>& t, void* stream);
 
 // Blocks each job of a packed launch takes (the grid of its own launch).
 template <typename T>

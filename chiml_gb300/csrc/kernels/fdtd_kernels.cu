@@ -738,7 +738,38 @@ void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int 
 
 __global__ void k_increment(int* step) { *step += 1; }
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_step_tail(const StepTail<T> t) {
+    __shared__ int next;  // the step number after this step's increment
+    if (threadIdx.x == 0) next = *t.step + 1;
+    __syncthreads();
+    const int b = static_cast<int>(blockIdx.x);
+    if (b < t.recBlocks) {
+        recordEntry(t.rec, t.f, &next, b * 256 + static_cast<int>(threadIdx.x));
+    } else if (t.nDft > 0) {
+        const int sb = b - t.recBlocks;
+        int q = 0;
+        while (q + 1 < t.nDft && t.dftStart[q + 1] <= sb) ++q;
+        dftSampleEntry(t.dft[q], t.f, &next, (sb - t.dftStart[q]) * 256LL + threadIdx.x);
+    }
+    // every block has read the counter before it takes its ticket; the last one advances it
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(t.ticket, 1u) == gridDim.x - 1) {
+            *t.step = next;
+            *t.ticket = 0u;
+            __threadfence();
+        }
+    }
+}
+
 void launch_increment(int* step, void* stream) { k_increment<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(step); }
+
+template <typename T>
+void launch_step_tail(const StepTail<T>& t, void* stream) {
+    k_step_tail<T><<<static_cast<unsigned>(t.blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(t);
+}
 
 // ---- packed launches (batched sweep) ----
 
@@ -896,6 +927,8 @@ template void launch_pass<double>(const Pass<double>&, bool, void*);
 template void launch_pass<float>(const Pass<float>&, bool, void*);
 template void launch_sources<double>(const SourceTable&, const Fields<double>&, const int*, void*);
 template void launch_sources<float>(const SourceTable&, const Fields<float>&, const int*, void*);
+template void launch_step_tail<double>(const StepTail<double>&, void*);
+template void launch_step_tail<float>(const StepTail<float>&, void*);
 template void launch_record<double>(const RecordTable&, const Fields<double>&, const int*, void*);
 template void launch_record<float>(const RecordTable&, const Fields<float>&, const int*, void*);
 template void launch_dft_sample<double>(const DftTable<double>&, const Fields<double>&, const int*, void*);

@@ -53,6 +53,7 @@ struct TfsfDev {
     TfsfLineDev line[6];       // 0..2 Ex..Ez, 3..5 Hx..Hz
     const double2* pulseTab;   // [step][line][mTot]: sum of the pulses at the line's pulse points
     double2* rec;              // [line][2 (nSteps + 1)]: recorded incident values (flux normalisation)
+    unsigned int* ticket;      // blocks finished in the current E half (zero between launches)
     // surface corrections: rows of cells that get one term each (the bulk of every face),
     // one block per 256 cells of a row: F[comp][cell0 + r s] += pref * Re(line[incd0 + r t])
     const TfsfSegDev* seg[2];  // [0] H corrections, [1] E corrections

@@ -13,7 +13,8 @@
 //                 corrections: face rows of cells with one term each, one thread per cell
 //                 along the row; cells on face edges (several terms) one thread each,
 //                 adding their terms in the reference's order: F += pref * Re(line value).
-//   k_tfsf_record the incident values recorded for flux normalisation.
+//                 The second launch also writes the incident values recorded for flux
+//                 normalisation, from the block that finishes last.
 // The lines are complex FP64 in both precision forms (a few thousand points).
 #include "tfsf_device.hpp"
 
@@ -90,48 +91,61 @@ __device__ __forceinline__ void lineAny(const TfsfDev& t, int c0, int e, int s) 
 
 constexpr int kTfsfThreads = kTfsfRowChunk;
 
-// One half of the TFSF step: blocks [0, lineBlocks) step the lines of kind c0 (3: H,
-// 0: E), the other blocks add the corrections of list `which` (0: H corrections, from
-// the E lines; 1: E corrections, from the H lines). The two parts touch disjoint data:
-// the corrections read the lines of the other kind, which this half does not write.
-template <typename T>
-__global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, T* F0, T* F1,
-                                                            T* F2, T* F3, T* F4, T* F5, const int* __restrict__ step) {
-    const int s = *step;
-    if (s >= t.nSteps) return;
-    const int b = static_cast<int>(blockIdx.x);
-    if (b < lineBlocks) {
-        lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
-        return;
-    }
-    T* const F[6] = {F0, F1, F2, F3, F4, F5};
-    const int sb = b - lineBlocks;
-    if (sb < t.segBlocks[which]) {
-        const int2 w = t.segWork[which][sb];
-        const TfsfSegDev& g = t.seg[which][w.x];
-        const int r = w.y * kTfsfThreads + static_cast<int>(threadIdx.x);
-        if (r >= g.n) return;
-        T* f = F[g.comp];
-        const long long cell = g.cell0 + r * g.cellStride;
-        f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * t.line[g.line].U[g.incd0 + r * g.incdStride].x);
-        return;
-    }
-    addCell(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
-}
-
 // Incident records after the step: E values of this step and the H values the next step
 // starts from (the H lines do not change until then); step 0's H values are zero, and
 // like the reference no H values are kept for the step after the last.
-__global__ void k_tfsf_record(const TfsfDev t, const int* __restrict__ step) {
-    const int s = *step;
-    if (s >= t.nSteps || threadIdx.x >= 6) return;
-    const int c = threadIdx.x;
+__device__ __forceinline__ void recordIncident(const TfsfDev& t, int s, int c) {
     const int slot = c < 3 ? s : s + 1;
     if (slot >= t.nSteps) return;  // slot nSteps is never a step's start: it stays zero
     const TfsfLineDev& L = t.line[c];
     const long long base = static_cast<long long>(c) * 2 * (t.nSteps + 1) + 2LL * slot;
     t.rec[base] = L.present ? L.pul[L.recIdx] : make_double2(0.0, 0.0);
     t.rec[base + 1] = L.present ? L.pul[L.recOffIdx] : make_double2(0.0, 0.0);
+}
+
+// One half of the TFSF step: blocks [0, lineBlocks) step the lines of kind c0 (3: H,
+// 0: E), the other blocks add the corrections of list `which` (0: H corrections, from
+// the E lines; 1: E corrections, from the H lines). The two parts touch disjoint data:
+// the corrections read the lines of the other kind, which this half does not write.
+// With `record`, the block that finishes last (a ticket counter, no waiting) writes the
+// incident records once every line of the half has been stepped.
+template <typename T>
+__global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, int record, T* F0,
+                                                            T* F1, T* F2, T* F3, T* F4, T* F5, const int* __restrict__ step) {
+    const int s = *step;
+    if (s >= t.nSteps) return;
+    const int b = static_cast<int>(blockIdx.x);
+    if (b < lineBlocks) {
+        lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
+    } else {
+        T* const F[6] = {F0, F1, F2, F3, F4, F5};
+        const int sb = b - lineBlocks;
+        if (sb < t.segBlocks[which]) {
+            const int2 w = t.segWork[which][sb];
+            const TfsfSegDev& g = t.seg[which][w.x];
+            const int r = w.y * kTfsfThreads + static_cast<int>(threadIdx.x);
+            if (r < g.n) {
+                T* f = F[g.comp];
+                const long long cell = g.cell0 + r * g.cellStride;
+                f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * t.line[g.line].U[g.incd0 + r * g.incdStride].x);
+            }
+        } else {
+            addCell(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
+        }
+    }
+    if (!record) return;
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();  // this block's line values are visible before its ticket
+        last = atomicAdd(t.ticket, 1u) == gridDim.x - 1;
+        if (last) {
+            *t.ticket = 0u;
+            __threadfence();
+        }
+    }
+    __syncthreads();
+    if (last && threadIdx.x < 6) recordIncident(t, s, threadIdx.x);
 }
 
 }  // namespace
@@ -142,10 +156,9 @@ void launch_tfsf_step(const TfsfDev& t, T* const fields[6], const int* step, voi
     const int lineBlocks = (3 * (t.gridLen + t.pulseLen) + kTfsfThreads - 1) / kTfsfThreads;
     for (int half = 0; half < 2; ++half) {
         const int addBlocks = t.segBlocks[half] + (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
-        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, fields[0], fields[1],
-                                                                        fields[2], fields[3], fields[4], fields[5], step);
+        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, fields[0],
+                                                                        fields[1], fields[2], fields[3], fields[4], fields[5], step);
     }
-    k_tfsf_record<<<1, 32, 0, s>>>(t, step);
 }
 
 template void launch_tfsf_step<float>(const TfsfDev&, float* const[6], const int*, void*);

@@ -108,6 +108,8 @@ void* chiml_stream(chiml_sim* sim);
  * regions, then frequency-domain detectors), then
  * 5 + 2 * n_flux_regions + e the emitter step of emitter object e, then
  * 5 + 2 * n_flux_regions + n_emitters + k the step of TFSF surface k.
+ * chiml_step runs the counter, the records and every table's sample gather as one
+ * launch; here they run as separate launches so that each has its own time.
  * *nslots receives the number of slots written (at most max_slots). */
 chiml_status chiml_profile_steps(chiml_sim* sim, int nsteps, double* ms_out, int max_slots, int* nslots);
 
