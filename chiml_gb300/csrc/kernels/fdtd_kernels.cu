@@ -484,14 +484,19 @@ __device__ __forceinline__ void pass2dAny(const Pass<T>& p, int ci, int bx, int 
 
 constexpr int kP2CY = CHIML_P2CY;
 
-template <typename T, bool EPASS>
+// A grid this small (cells) marches kP2CYSmall rows per warp instead of kP2CY: a march is
+// a chain of dependent row loads, and a small grid has too few warps to hide it.
+constexpr int kP2CYSmall = 2;
+constexpr long long kP2SmallCells = 1LL << 22;
+
+template <typename T, bool EPASS, int CY = kP2CY>
 __global__ void __launch_bounds__(256) k_pass2d(const Pass<T> p) {
     if (!p.c[blockIdx.z].present) return;
-    pass2dAny<T, EPASS, kP2CY>(p, blockIdx.z, blockIdx.x, blockIdx.y);
+    pass2dAny<T, EPASS, CY>(p, blockIdx.z, blockIdx.x, blockIdx.y);
 }
 
 __host__ __device__ inline int pass2d_gx(int lx) { return (lx - 2 + 31) / 32; }
-__host__ __device__ inline int pass2d_gy(int ly) { return (ly - 2 + kP2W * kP2CY - 1) / (kP2W * kP2CY); }
+__host__ __device__ inline int pass2d_gy(int ly, int cy = kP2CY) { return (ly - 2 + kP2W * cy - 1) / (kP2W * cy); }
 
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
@@ -507,9 +512,15 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else if (p.interior2d) {
-        dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
-        if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
-        else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
+        if (static_cast<long long>(p.lx) * p.ly < kP2SmallCells) {
+            dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly, kP2CYSmall), 3);
+            if (ePass) k_pass2d<T, true, kP2CYSmall><<<grid, 256, 0, s>>>(p);
+            else k_pass2d<T, false, kP2CYSmall><<<grid, 256, 0, s>>>(p);
+        } else {
+            dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
+            if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
+            else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
+        }
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else {
