@@ -213,7 +213,11 @@ __device__ __forceinline__ T dispersiveE(const Pass<T>& p, int ci, uint32_t fl, 
         }
         const int s = p.poleStart[obj];
         const int n = p.poleCount[obj];
-        for (int q = 0; q < n; ++q) {
+        // unrolled to the pole bound with guards, so that the loads of every pole are in
+        // flight together
+#pragma unroll
+        for (int q = 0; q < kMaxPoles; ++q) {
+            if (q >= n) break;
             const T old = c.P[q][i];
             T np = p.alpha[s + q] * old;
             np += p.xi[s + q] * c.Pprev[q][i];
@@ -230,11 +234,17 @@ __device__ __forceinline__ T dispersiveE(const Pass<T>& p, int ci, uint32_t fl, 
     T e = d * epsInv;
     if (fl & kFcLor) {
         const T ne = -epsInv;
-        for (int q = 0; q < c.nPoles; ++q) e += ne * c.P[q][i];
+#pragma unroll
+        for (int q = 0; q < kMaxPoles; ++q) {
+            if (q >= c.nPoles) break;
+            e += ne * c.P[q][i];
+        }
     } else {
         const T oc = T(-0.5) * epsInv;
         const long long o = p.od.off[ci];
-        for (int q = 0; q < p.od.nPoles; ++q) {
+#pragma unroll
+        for (int q = 0; q < kMaxPoles; ++q) {
+            if (q >= p.od.nPoles) break;
             e += oc * p.od.P[ci][q][i];
             e += oc * p.od.P[ci][q][i + o];
         }
