@@ -543,13 +543,25 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     }
 }
 
+// f.f[c] for a component c known only at run time, as a chain of selects over the
+// parameter array: a dynamic index into a kernel parameter array would copy the whole
+// array to local memory in every thread.
+template <typename T>
+__device__ __forceinline__ T* fieldOf(const Fields<T>& f, int c) {
+    T* r = f.f[0];
+#pragma unroll
+    for (int k = 1; k < 9; ++k)
+        if (c == k) r = f.f[k];
+    return r;
+}
+
 template <typename T>
 __device__ __forceinline__ void sourceEntry(const SourceTable& s, const Fields<T>& f, const int* step, int j) {
     if (j >= s.n) return;
     const int st = *step;
     if (st >= s.nSteps) return;
     const double v = s.value[static_cast<long long>(s.src[j]) * s.nSteps + st];
-    atomicAdd(&f.f[s.comp[j]][s.cell[j]], static_cast<T>(v));
+    atomicAdd(&fieldOf(f, s.comp[j])[s.cell[j]], static_cast<T>(v));
 }
 
 template <typename T>
@@ -573,7 +585,7 @@ __device__ __forceinline__ void recordEntry(const RecordTable& r, const Fields<T
     const int ev = st / ti;
     if (ev >= r.nEvents[d]) return;
     const long long c = r.cell[j];
-    const double v = (c < 0) ? 0.0 : static_cast<double>(f.f[r.comp[j]][c]);
+    const double v = (c < 0) ? 0.0 : static_cast<double>(fieldOf(f, r.comp[j])[c]);
     r.rec[r.recBase[d] + static_cast<long long>(ev) * r.nvals[d] + r.outIndex[j]] = v;
 }
 
@@ -593,7 +605,7 @@ __device__ __forceinline__ void dftSampleEntry(const DftTable<T>& d, const Field
     const int st = *step;
     if (st % d.timeInt != 0 || p >= d.npts) return;
     const int slot = (st / d.timeInt) & (d.K - 1);
-    d.ring[static_cast<long long>(slot) * d.stride + p] = f.f[d.comp[p]][d.cell[p]];
+    d.ring[static_cast<long long>(slot) * d.stride + p] = fieldOf(f, d.comp[p])[d.cell[p]];
 }
 
 template <typename T>

@@ -30,9 +30,30 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// The main-grid field of component c (0..5), selected without a dynamic index into an
+// array (which would live in local memory).
+template <typename T>
+struct Fields6 {
+    T* f0;
+    T* f1;
+    T* f2;
+    T* f3;
+    T* f4;
+    T* f5;
+    __device__ __forceinline__ T* operator[](int c) const {
+        T* r = f0;
+        r = c == 1 ? f1 : r;
+        r = c == 2 ? f2 : r;
+        r = c == 3 ? f3 : r;
+        r = c == 4 ? f4 : r;
+        r = c == 5 ? f5 : r;
+        return r;
+    }
+};
+
 // Surface corrections of cell q of list `which` (0 H, 1 E).
 template <typename T>
-__device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, T* const F[6]) {
+__device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, const Fields6<T>& F) {
     if (q >= t.nCell[which]) return;
     T* f = F[t.comp[which][q]];
     const long long cell = t.cell[which][q];
@@ -118,7 +139,7 @@ __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int
     if (b < lineBlocks) {
         lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
     } else {
-        T* const F[6] = {F0, F1, F2, F3, F4, F5};
+        const Fields6<T> F{F0, F1, F2, F3, F4, F5};
         const int sb = b - lineBlocks;
         if (sb < t.segBlocks[which]) {
             const int2 w = t.segWork[which][sb];
