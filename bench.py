@@ -7,12 +7,18 @@ plane wave along +z, a 150-frequency DFT flux box), generated by chiml_gb300.con
 One step is one full time step (H half + E half + detectors + DFT).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload c2|c1|c3|c4|c5]
+
+The other workloads: c1 (2-D TMz 400^2), c3 (3-D Maxwell-Liouville 192^3), c4 (batched
+sweep of 96 2-D emitter sheets), c5 (3-D mixed scene 640x640x320 with a four-level emitter
+sheet; its CPU legs run a 160x160x80 crop, and its line adds the FP64-vs-split comparison
+on that crop).
 
 `value` is the FP32/FP64-split form (fields, CPML and polarisations in FP32,
 DFT accumulators in FP64) with all state resident in HBM; `fp64` is the same
 workload in FP64 (the parity form). `e2e` times the public C ABI end to end:
-chiml_create (JSON read, plan, upload), the K steps, chiml_finalize (download
-and file writes). Under torchrun every rank runs its own replica (the
+chiml_create (JSON read, plan, upload), the K steps, chiml_finalize (flux integration
+on the device, download and file writes). Under torchrun every rank runs its own replica (the
 single-domain path does not shard); value sums cells x steps over ranks and
 divides by the slowest rank's time.
 """
