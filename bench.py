@@ -39,8 +39,9 @@ N_DEFAULT = 256
 
 # DRAM bytes of one launch per physical cell, split form of this workload, measured with
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum, --cache-control none) at 256^3:
-# H pass 749.6 MB, E pass (main kernel 757.5 MB + dispersive-cell list 41.1 MB) 798.6 MB.
-MEASURED_TRAFFIC_PER_CELL = {"h_pass": 749.6e6 / 16777216, "e_pass": 798.6e6 / 16777216}
+# H pass 736.8 MB; E pass 946.3 MB (oriented-dipole P kernel 97.4 MB + the pass with its
+# inline dispersive cells 848.9 MB).
+MEASURED_TRAFFIC_PER_CELL = {"h_pass": 736.8e6 / 16777216, "e_pass": 946.3e6 / 16777216}
 
 
 NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e nominal bandwidth, reported beside the measured copy peak
