@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <numeric>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -161,12 +162,20 @@ public:
         }
         for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
             const dev::DftTable<T>& d = dft_[P.fluxes.size() + k];
-            const std::size_t n = static_cast<std::size_t>(d.npts) * P.freqDetectors[k].spec.freqList.size();
-            std::vector<double> re(n), im(n);
+            const std::size_t nf = P.freqDetectors[k].spec.freqList.size();
+            const std::size_t n = static_cast<std::size_t>(d.npts) * nf;
+            std::vector<double> dre(n), dim(n), re(n), im(n);
             if (n) {
-                ck(cudaMemcpy(re.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
-                ck(cudaMemcpy(im.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
+                ck(cudaMemcpy(dre.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
+                ck(cudaMemcpy(dim.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
             }
+            // back to the plan's point order
+            const std::vector<int>& pos = dftPos_[P.fluxes.size() + k];
+            for (std::size_t p = 0; p < pos.size(); ++p)
+                for (std::size_t f = 0; f < nf; ++f) {
+                    re[p * nf + f] = dre[static_cast<std::size_t>(pos[p]) * nf + f];
+                    im[p * nf + f] = dim[static_cast<std::size_t>(pos[p]) * nf + f];
+                }
             d2h_ += 2.0 * n * sizeof(double);
             R.freqRe.push_back(std::move(re));
             R.freqIm.push_back(std::move(im));
@@ -239,10 +248,14 @@ public:
             for (int w = 0; w < 4; ++w) {
                 F.has[w] = m.has[w] ? 1 : 0;
                 F.start[w] = m.has[w] ? tmp.upload(m.start[w]) : nullptr;
-                F.pt[w] = m.has[w] ? tmp.upload(m.pt[w]) : nullptr;
-                F.scale[w] = m.has[w] ? tmp.upload(m.scale[w]) : nullptr;
-                for (long long p : m.pt[w])
+                std::vector<long long> devPt(m.pt[w].size());
+                for (std::size_t k = 0; k < devPt.size(); ++k) {
+                    const long long p = m.pt[w][k];
                     if (p < 0 || p >= fp.npts) throw std::logic_error("flux map point outside the accumulators");
+                    devPt[k] = dftPos_[q][static_cast<std::size_t>(p)];
+                }
+                F.pt[w] = m.has[w] ? tmp.upload(devPt) : nullptr;
+                F.scale[w] = m.has[w] ? tmp.upload(m.scale[w]) : nullptr;
             }
             F.wx = tmp.upload(m.wx);
             F.wy = tmp.upload(m.wy);
@@ -1233,7 +1246,25 @@ private:
 
     // One DFT table: point table (component, cell), phasors per sample from the accumulated
     // time, a ring of K samples and FP64 accumulators [point][frequency].
-    dev::DftTable<T> makeDft(const std::vector<int>& comp, const std::vector<int>& cell, const std::vector<double>& freqs, int ti) {
+    // Position of each plan point of every DFT table in the device point order (points sorted
+    // by component and cell, so that a warp's gathers share sectors: the two planes of a
+    // face's averaged pair are neighbours in x). Accumulators, ring and tables are in the
+    // device order; the flux maps and the frequency-detector downloads are translated.
+    std::vector<std::vector<int>> dftPos_;
+
+    dev::DftTable<T> makeDft(const std::vector<int>& comp0, const std::vector<int>& cell0, const std::vector<double>& freqs, int ti) {
+        std::vector<int> order(cell0.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return comp0[a] != comp0[b] ? comp0[a] < comp0[b] : cell0[a] < cell0[b];
+        });
+        std::vector<int> comp(cell0.size()), cell(cell0.size()), pos(cell0.size());
+        for (std::size_t k = 0; k < order.size(); ++k) {
+            comp[k] = comp0[order[k]];
+            cell[k] = cell0[order[k]];
+            pos[order[k]] = static_cast<int>(k);
+        }
+        dftPos_.push_back(std::move(pos));
         dev::DftTable<T> d{};
         {
             const int nf = static_cast<int>(freqs.size());
