@@ -1045,6 +1045,13 @@ struct Builder {
         innerThreads_ = std::max(1, nThreads / std::max(1, nComp));
         const int prevLevels = omp_get_max_active_levels();
         omp_set_max_active_levels(std::max(prevLevels, 2));
+        // older runtimes (a host application may bring its own) also gate nesting on the
+        // OpenMP 3 switch
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
+        const int prevNested = omp_get_nested();
+        omp_set_nested(1);
+#pragma GCC diagnostic pop
 #pragma omp parallel for schedule(dynamic, 1) num_threads(std::min(nThreads, std::max(1, nComp)))
         for (int q = 0; q < 6; ++q) {
             if (!present[order[q]]) continue;
@@ -1055,6 +1062,10 @@ struct Builder {
             }
         }
         omp_set_max_active_levels(prevLevels);
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
+        omp_set_nested(prevNested);
+#pragma GCC diagnostic pop
         for (int q = 0; q < 6; ++q)
             if (err[q]) std::rethrow_exception(err[q]);
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
