@@ -1,37 +1,124 @@
-"""Readers for chiML's output files (text detectors, flux spectra, emitter population and
-polarisation files, binary detectors) and a per-file relative-error comparison of two
-output directories."""
+"""Readers for chiML's output files and a per-column relative-error comparison of two output
+directories.
+
+The files and their column layouts (what is a coordinate and what is data):
+
+* text detectors (`DTC/parallelDTC_TXT.cpp:20-53`): header ``# time x y z field``, then one
+  row per sample: t, x, y, z, and the values of every point of the box;
+* binary detectors (`DTC/parallelDTC_BIN.cpp:12-50`): six int32 (box size, location), then
+  per sample t and sz[0]*sz[1]*sz[2] FP64 values;
+* flux spectra (`DTC/parallelFlux.hpp:444-540`): header ``#freq ...``, then per frequency the
+  frequency and (abs, real, imag) triples: incident, each face, total;
+* frequency-domain detectors (`DTC/parallelDTC_FREQ.hpp:390-450`): ``#freq ...`` files with
+  triples (incident fields, their sum, each field, the total), and per-frequency maps
+  ``#x y z ...`` with three coordinate columns before the triples;
+* emitter populations (`ML/QEPopDtc.cpp:37-61`): headerless rows t, re, im, abs;
+* emitter polarisation (`ML/parallelQE.cpp:520-557`): headerless rows t, then Px, Py and/or
+  Pz and |P|.
+
+The comparison leaves coordinates out of the error (they must agree, or the files do not
+describe the same samples) and takes the relative L2 error of every data group on its own:
+each (abs, real, imag) triple of the spectra, the point values of a detector, the population
+triple, the polarisation columns. A file's error is the worst group's, so a small column
+is not hidden by a large one (a time column of O(100) next to fields of O(1e-4), a
+frequency column next to fluxes of O(1e-10)).
+"""
 import os
 
 import numpy as np
 
+COORD_TOL = 1e-9  # coordinate columns (time, x/y/z, frequency) must agree to this relative L2
+
 
 def read_output(path):
-    """Returns (kind, header, values) for a detector or flux file: kind "txt" with the numbers
-    of a text file (rows of a '#'-headed file, or every number of a headerless one), or "bin"
-    with the 6-int header and the FP64 payload of a binary detector."""
+    """Returns (kind, header, values): kind "txt" with the header line (None for headerless
+    files) and the rows of a text file as a 2-D array; or kind "bin" with the six-int header
+    and the FP64 payload of a binary detector."""
     raw = open(path, "rb").read()
-    if raw[:1] == b"#":
-        rows = [l.split() for l in raw.decode().splitlines() if not l.startswith("#")]
-        return "txt", None, np.array([[float(x) for x in r] for r in rows])
     try:
-        rows = [l.split() for l in raw.decode("ascii").splitlines() if l.strip()]
-        return "txt", None, np.array([float(x) for r in rows for x in r])
-    except (UnicodeDecodeError, ValueError):
-        pass
+        text = raw.decode("ascii")
+    except UnicodeDecodeError:
+        text = None
+    if text is not None:
+        header = None
+        rows = []
+        ok = True
+        for line in text.splitlines():
+            if line.startswith("#"):
+                if header is None:
+                    header = line
+                continue
+            if not line.strip():
+                continue
+            try:
+                rows.append([float(x) for x in line.split()])
+            except ValueError:
+                ok = False
+                break
+        if ok and (header is not None or rows):
+            width = max((len(r) for r in rows), default=0)
+            if any(len(r) != width for r in rows):
+                raise ValueError("%s: ragged rows" % path)
+            return "txt", header, np.array(rows, dtype=np.float64).reshape(len(rows), width)
     hdr = np.frombuffer(raw[:24], dtype=np.int32)
     return "bin", hdr, np.frombuffer(raw[24:], dtype=np.float64)
 
 
 def rel_l2(a, b):
     """||a - b|| / ||a|| (the absolute norm when a is zero)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
     den = np.linalg.norm(a)
     return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
 
 
-def relative_errors(ref_dir, out_dir):
-    """{relative path: rel_l2(ref, out)} for every file under ref_dir. Raises ValueError when
-    a file is missing on the out_dir side or its kind, header or shape differ."""
+def split_columns(kind, header, values):
+    """(coordinates, [(group name, data array)]) of one parsed output file."""
+    if kind == "bin":
+        npts = int(np.prod(header[:3])) if header.size >= 3 else 0
+        rec = npts + 1
+        if npts <= 0 or values.size % rec:
+            return None, [("payload", values)]
+        v = values.reshape(-1, rec)
+        return v[:, 0], [("points", v[:, 1:])]
+    v = values
+    if v.ndim != 2 or v.shape[1] == 0:
+        return None, [("values", v)]
+    h = (header or "").lstrip("#").strip()
+    if h.startswith("time"):                    # text detector: t, x, y, z, point values
+        return v[:, :4], [("points", v[:, 4:])]
+    if h.startswith("x"):                       # frequency map: x, y, z, triples
+        ncoord = 3
+    elif h.startswith("freq"):                  # flux spectrum / frequency detector: f, triples
+        ncoord = 1
+    else:                                       # headerless emitter files: t, then values
+        return v[:, :1], [("values", v[:, 1:])]
+    data = v[:, ncoord:]
+    if data.shape[1] % 3:
+        return v[:, :ncoord], [("values", data)]
+    return v[:, :ncoord], [("triple%d" % (k // 3), data[:, k:k + 3]) for k in range(0, data.shape[1], 3)]
+
+
+def column_errors(ref_path, out_path):
+    """{group name: relative L2} of one file against its reference. Raises ValueError when the
+    kinds, headers, shapes or coordinate columns differ."""
+    ka, ha, a = read_output(ref_path)
+    kb, hb, b = read_output(out_path)
+    if ka != kb or a.shape != b.shape:
+        raise ValueError("%s: kind or shape differ (%s vs %s)" % (out_path, a.shape, b.shape))
+    if ka == "bin" and not np.array_equal(ha, hb):
+        raise ValueError("%s: binary header differs" % out_path)
+    ca, ga = split_columns(ka, ha, a)
+    cb, gb = split_columns(kb, hb, b)
+    if ca is not None and rel_l2(ca, cb) > COORD_TOL:
+        raise ValueError("%s: coordinate columns differ (relative L2 %.3e)" % (out_path, rel_l2(ca, cb)))
+    return {name: rel_l2(x, y) for (name, x), (_, y) in zip(ga, gb)}
+
+
+def relative_errors(ref_dir, out_dir, detail=False):
+    """{relative path: worst data-group relative L2} for every file under ref_dir (with
+    detail=True, {relative path: {group: relative L2}}). Raises ValueError when a file is
+    missing on the out_dir side or its kind, header, shape or coordinates differ."""
     res = {}
     for d, _, files in os.walk(ref_dir):
         for f in files:
@@ -40,9 +127,26 @@ def relative_errors(ref_dir, out_dir):
             q = os.path.join(out_dir, rel)
             if not os.path.exists(q):
                 raise ValueError("missing output " + rel)
-            ka, ha, a = read_output(p)
-            kb, hb, b = read_output(q)
-            if ka != kb or (ha is not None and not np.array_equal(ha, hb)) or a.shape != b.shape:
-                raise ValueError("%s: kind, header or shape differ (%s vs %s)" % (rel, a.shape, b.shape))
-            res[rel] = rel_l2(a, b)
+            errs = column_errors(p, q)
+            res[rel] = errs if detail else max(errs.values(), default=0.0)
     return res
+
+
+def file_class(rel):
+    """'flux', 'emitter' or 'field' for an output file name (for error summaries)."""
+    name = os.path.basename(rel)
+    if "flux" in name:
+        return "flux"
+    if "_level_" in name or "pol" in name:
+        return "emitter"
+    return "field"
+
+
+def error_summary(ref_dir, out_dir):
+    """Worst relative L2 per class of output file: {"fields", "flux", "populations"} (None
+    where a class has no file)."""
+    worst = {"field": None, "flux": None, "emitter": None}
+    for rel, e in relative_errors(ref_dir, out_dir).items():
+        c = file_class(rel)
+        worst[c] = e if worst[c] is None else max(worst[c], e)
+    return {"fields": worst["field"], "flux": worst["flux"], "populations": worst["emitter"]}
