@@ -11,8 +11,12 @@ One step is one full time step (H half + E half + detectors + DFT).
 
 The other workloads: c1 (2-D TMz 400^2), c3 (3-D Maxwell-Liouville 192^3), c4 (batched
 sweep of 96 2-D emitter sheets), c5 (3-D mixed scene 640x640x320 with a four-level emitter
-sheet; its CPU legs run a 160x160x80 crop, and its line adds the FP64-vs-split comparison
-on that crop).
+sheet; its CPU legs run a 160x160x80 crop).
+
+Every line carries `fp64_error`: the split form against the FP64 form on the workload's
+scene run to its last step (c1 and the c4 members at full size, c2 at 128^3, c3 at 96^3,
+c5 on the crop), the worst relative L2 of each data column group of the detector, flux and
+emitter output files.
 
 `value` is the FP32/FP64-split form (fields, CPML and polarisations in FP32,
 DFT accumulators in FP64) with all state resident in HBM; `fp64` is the same
@@ -42,6 +46,7 @@ N_DEFAULT = 256
 # H pass 736.8 MB; E pass 946.3 MB (oriented-dipole P kernel 97.4 MB + the pass with its
 # inline dispersive cells 848.9 MB).
 MEASURED_TRAFFIC_PER_CELL = {"h_pass": 736.8e6 / 16777216, "e_pass": 946.3e6 / 16777216}
+TRAFFIC_CAPTURE = "256^3, split form"
 
 
 NOMINAL_HBM_GBS = 7900.0  # GB300 HBM3e nominal bandwidth, reported beside the measured copy peak
@@ -135,10 +140,20 @@ WORKLOADS = {
            640, "config5"),
 }
 
-# Config 5's CPU samples and its FP64-vs-split error check run on a 160 x 160 x 80 crop of
-# the same scene (the full 131 M-cell grid needs minutes of host set-up per oracle run).
+# Config 5's CPU samples run on a 160 x 160 x 80 crop of the same scene (the full 131 M-cell
+# grid needs minutes of host set-up per oracle run).
 C5_CROP = dict(n=160, nz=80, pml=8, nell=4, film_cells=4, sheet_cells=4)
 C5_CROP_STEPS = 1600  # the pulse has passed every flux plane of the crop by then
+
+# The FP64-vs-split accuracy check of each workload: the same scene at a size both forms
+# run to its last step in seconds, compared per data column of every output file.
+# c1 and the c4 members run at their full size and step count.
+ERROR_SCENES = {
+    "c1": ("the full workload (400^2, 4000 steps)", "config1", {}),
+    "c2": ("the scene at 128^3, 5000 steps", "config2", dict(n=128, steps=5000)),
+    "c3": ("the scene at 96^3 (20-cell emitter slab), 8000 steps", "config3", dict(n=96, steps=8000)),
+    "c5": ("the 160x160x80 crop of the scene, 1600 steps", "config5", dict(steps=C5_CROP_STEPS, **C5_CROP)),
+}
 
 
 def _dims(name, n):
@@ -166,25 +181,43 @@ def _cpu_sample_config(args, work, cfg_path, steps):
     return path, "the %dx%dx%d crop of the workload" % (C5_CROP["n"], C5_CROP["n"], C5_CROP["nz"])
 
 
-def _crop_error(args, work, local):
-    """Config 5's accuracy check: the crop run to the end in the split form and in FP64;
-    returns the largest relative L2 difference over the flux spectra and over the emitter
-    outputs (populations, polarisation)."""
-    from chiml_gb300 import Simulation, configs
-    from chiml_gb300.outfiles import relative_errors
-    path = configs.write_json(configs.config5(steps=C5_CROP_STEPS, **C5_CROP), os.path.join(work, "crop_check.json"))
-    dirs = {}
-    for prec in ("fp64", "split"):
-        dirs[prec] = os.path.join(work, "crop_" + prec)
-        sim = Simulation(path, precision=prec, device=local, steps_per_graph=args.graph, out_dir=dirs[prec])
-        sim.step()
-        sim.finalize()
-        sim.close()
-    err = relative_errors(dirs["fp64"], dirs["split"])
-    flux = max(v for k, v in err.items() if "flux" in k)
-    emit = max(v for k, v in err.items() if "flux" not in k)
-    return {"crop": "%dx%dx%d" % (C5_CROP["n"], C5_CROP["n"], C5_CROP["nz"]), "steps": C5_CROP_STEPS,
-            "flux_rel_l2_max": float("%.3g" % flux), "emitter_rel_l2_max": float("%.3g" % emit)}
+def _run_both(paths, work, local, graph, tag):
+    """Runs every input to its last step in FP64 and in the split form; returns the
+    per-class worst relative L2 of the split outputs against the FP64 ones."""
+    from chiml_gb300 import Simulation
+    from chiml_gb300.outfiles import error_summary
+    worst = {"fields": None, "flux": None, "populations": None}
+    for i, path in enumerate(paths):
+        dirs = {}
+        for prec in ("fp64", "split"):
+            dirs[prec] = os.path.join(work, "%s_%d_%s" % (tag, i, prec))
+            sim = Simulation(path, precision=prec, device=local, steps_per_graph=graph, out_dir=dirs[prec])
+            sim.step()
+            sim.finalize()
+            sim.close()
+        for k, v in error_summary(dirs["fp64"], dirs["split"]).items():
+            if v is not None:
+                worst[k] = v if worst[k] is None else max(worst[k], v)
+    return {k: (float("%.3g" % v) if v is not None else None) for k, v in worst.items()}
+
+
+def fp64_error(workload, work, local, graph, members=4):
+    """The split form's error against the FP64 form on the workload's scene (ERROR_SCENES;
+    for c4, the first ``members`` members of the sweep at full size): worst relative L2 per
+    data column group over the detector fields, the flux spectra and the emitter outputs."""
+    from chiml_gb300 import configs
+    t0 = time.perf_counter()
+    if workload == "c4":
+        what = "the first %d members of the sweep, full size, 6000 steps" % members
+        paths = _c4_members(os.path.join(work, "err_c4"), members, 6000)
+    else:
+        what, fn, kw = ERROR_SCENES[workload]
+        paths = [configs.write_json(getattr(configs, fn)(**kw), os.path.join(work, "err_%s.json" % workload))]
+    out = _run_both(paths, work, local, graph, "err_" + workload)
+    out["scene"] = what
+    out["compared"] = "split vs FP64 outputs, relative L2 of each data column group (worst per class)"
+    out["seconds"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def _time_steps(sim, k, torch):
@@ -257,6 +290,11 @@ def run_ours(args):
     dom_ms = dft_ms if dom == "dft" else per_launch[dom]
     dom_bytes = sp["stats"].bytes_dft if dom == "dft" else kbytes[dom]
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    # DRAM traffic is known from an ncu capture of this workload's scene only (c2)
+    traffic, traffic_src = None, "no ncu DRAM capture of this workload's pass kernels"
+    if args.workload == "c2" and dom in MEASURED_TRAFFIC_PER_CELL:
+        traffic = round(MEASURED_TRAFFIC_PER_CELL[dom] * cells, 0)
+        traffic_src = "ncu dram bytes per cell of this scene (captured at %s), times this run's cells" % TRAFFIC_CAPTURE
     fp = results["fp64"]
     fp_value = cells * args.steps / (fp["ms"] * 1e-3) / 1e9
     fp_prof = {k: v / nprof for k, v in fp["prof"].items()}
@@ -283,7 +321,7 @@ def run_ours(args):
         cpu_path, what = _cpu_sample_config(args, work, cfg_path, total_steps)
         cpu = cpu_baseline(cpu_path, what, args.cpu_seconds)
 
-    crop = _crop_error(args, work, local) if (rank == 0 and args.workload == "c5" and not args.no_check) else None
+    err = fp64_error(args.workload, work, local, args.graph) if (rank == 0 and not args.no_check) else None
 
     if rank == 0:
         launches = sp["stats"].kernels_per_step * args.steps
@@ -306,6 +344,9 @@ def run_ours(args):
                 "precision": "split",
                 "l2": "inputs larger than L2 (%.0f MB of field state vs 129 MB L2)" % (sp["stats"].device_bytes / 1e6),
                 "graph_steps": args.graph,
+                "dft_fold": ("staggered: the point tiles of each DFT table fold in K/4 groups, one group every 4 "
+                             "samples (K = 256 samples per fold), so any window of steps carries its share of the "
+                             "fold; %d steps carry %d group folds" % (args.steps, args.steps // 4)),
                 "parallelism": "replicas" if world > 1 else "single GPU",
             },
             "fp64": {"value": round(fp_value, 3), "unit": "Gcell-updates/s", "ms_per_step": round(fp["ms"] / args.steps, 4),
@@ -314,9 +355,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "frac_of_nominal": round(achieved / NOMINAL_HBM_GBS, 4),
-                         "traffic": (round(MEASURED_TRAFFIC_PER_CELL[dom] * cells, 0)
-                                     if dom in MEASURED_TRAFFIC_PER_CELL else None),
-                         "traffic_source": "ncu dram bytes per cell at 256^3, scaled to this workload's cells",
+                         "traffic": traffic,
+                         "traffic_source": traffic_src,
                          "bytes_per_launch": dom_bytes,
                          "step_bytes_per_cell": round(sp["stats"].bytes_per_cell_update, 2),
                          "kernel_ms": {k: round(v, 4) for k, v in per_launch.items()}},
@@ -325,8 +365,8 @@ def run_ours(args):
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
-        if crop:
-            line["fp64_crop_error"] = crop
+        if err:
+            line["fp64_error"] = err
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
@@ -470,6 +510,7 @@ def run_batch(args):
     cpu = None
     if not args.no_cpu:
         cpu = batch_cpu_sample(paths, args.cpu_seconds)
+    err = None if args.no_check else fp64_error("c4", work, local, args.graph)
     line = {
         "metric": C4_METRIC, "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t_batch / args.steps, 4),
@@ -487,6 +528,8 @@ def run_batch(args):
                      "bytes_per_step": step_bytes},
         "gpu_launches": None, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
     }
+    if err:
+        line["fp64_error"] = err
     print(json.dumps(line))
 
 
@@ -560,7 +603,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-check", action="store_true", help="c5: skip the FP64-vs-split crop check")
+    ap.add_argument("--no-check", action="store_true", help="skip the FP64-vs-split accuracy check")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -82,9 +82,12 @@ def build_oracle(force=False):
     return LIB_ORACLE
 
 
-def build_reference(ref_dir="/root/reference"):
-    """One-process CPU build of the chiML sources, only where they exist (never on the GPU host)."""
-    if not os.path.isdir(os.path.join(ref_dir, "src")):
+def build_reference(ref_dir=None):
+    """One-process CPU build of the chiML sources, only where they exist (never on the GPU
+    host). The checkout is ``ref_dir``, else the CHIML_REF_SRC environment variable; without
+    either nothing is built."""
+    ref_dir = ref_dir or os.environ.get("CHIML_REF_SRC")
+    if not ref_dir or not os.path.isdir(os.path.join(ref_dir, "src")):
         return None
     if shutil.which("make") is None:
         return None
@@ -92,11 +95,11 @@ def build_reference(ref_dir="/root/reference"):
     return os.path.join(ORACLE, "_ref", "chiml_ref")
 
 
-def build_all(force=False):
+def build_all(force=False, ref_dir=None):
     with cf.ThreadPoolExecutor(max_workers=3) as ex:
         fe = ex.submit(build_engine, force)
         fo = ex.submit(build_oracle, force)
-        fr = ex.submit(build_reference)
+        fr = ex.submit(build_reference, ref_dir)
         return fe.result(), fo.result(), fr.result()
 
 

@@ -91,7 +91,12 @@ public:
         // the legacy default stream.
         ck(cudaStreamCreate(&stream_), "cudaStreamCreate");
         outDir_ = opt.out_dir ? opt.out_dir : "";
+        // the fixed array of chiml_get_box_noalloc is placed on the device now, before
+        // this handle's uploads, so that no read-back has to place it later
+        ck(dev::box_noalloc_setup(opt.device), "chiml_get_box_noalloc set-up");
         upload();
+        // the step graph is captured and instantiated here, so that no step call pays for it
+        if (opt_.steps_per_graph > 0 && P.nSteps >= opt_.steps_per_graph) buildGraph(opt_.steps_per_graph);
     }
     ~Sim() override {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -145,12 +150,10 @@ public:
                 R.detectors[k].emplace_back(b, b + nv);
             }
         }
-        // fold the samples of the last, partial block into the accumulators
+        // fold every group's pending samples into the accumulators
         for (std::size_t q = 0; q < dft_.size(); ++q) {
             const dev::DftTable<T>& d = dft_[q];
-            const int samples = stepsDone_ / d.timeInt + 1;
-            const int pending = samples % d.K;
-            if (pending > 0) dev::launch_dft_fold<T>(d, dStep_, pending, samples - pending, stream_);
+            dev::launch_dft_flush<T>(d, stepsDone_ / d.timeInt + 1, stream_);
         }
         ck(cudaStreamSynchronize(stream_), "DFT flush");
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
@@ -389,7 +392,7 @@ public:
                 dev::launch_dft_sample<T>(dft_[q], fields_, dStep_, s);
                 mark(e1, 5 + 2 * q);
                 mark(e0, 6 + 2 * q);
-                dev::launch_dft_fold<T>(dft_[q], dStep_, -1, 0, s);
+                dev::launch_dft_fold<T>(dft_[q], dStep_, s);
                 mark(e1, 6 + 2 * q);
             }
             ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
@@ -471,7 +474,7 @@ private:
         launchEmitters(s);
         // records, DFT samples and the step counter in one launch, then the folds
         dev::launch_step_tail<T>(tail_, s);
-        for (auto& d : dft_) dev::launch_dft_fold<T>(d, dStep_, -1, 0, s);
+        for (auto& d : dft_) dev::launch_dft_fold<T>(d, dStep_, s);
     }
 
     // ---- the device layout: rows padded from lx to pitch_ values ----
@@ -1398,7 +1401,7 @@ struct PackedBase {
 template <typename T>
 class PackedBatch : public PackedBase {
 public:
-    PackedBatch(const std::vector<Sim<T>*>& members, int device) : members_(members) {
+    PackedBatch(const std::vector<Sim<T>*>& members, int device, int graphSteps) : members_(members) {
         ck(cudaSetDevice(device), "cudaSetDevice");
         ck(cudaStreamCreate(&stream_), "cudaStreamCreate");
         std::vector<dev::Pass<T>> hp, ep;
@@ -1487,6 +1490,8 @@ public:
         addMap_ = map(addW);
         for (int g = 0; g < 7; ++g) updMap_[g] = map(updW[g]);
         ck(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        // the packed step graph is made with the launches, not in the first run that uses it
+        if (graphSteps > 0) buildGraph(graphSteps);
     }
     ~PackedBatch() {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -1500,14 +1505,7 @@ public:
     void run(long long n, int graphSteps) override {
         for (Sim<T>* m : members_) ck(cudaStreamSynchronize(m->stream()), "cudaStreamSynchronize");
         if (graphSteps > 0 && n >= graphSteps) {
-            if (!graph_) {
-                cudaGraph_t g;
-                ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-                for (int k = 0; k < graphSteps; ++k) enqueueStep();
-                ck(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
-                ck(cudaGraphInstantiate(&graph_, g, 0), "cudaGraphInstantiate");
-                cudaGraphDestroy(g);
-            }
+            if (!graph_ || graphSteps != graphSteps_) buildGraph(graphSteps);
             for (; n >= graphSteps; n -= graphSteps) ck(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
         }
         for (; n > 0; --n) enqueueStep();
@@ -1516,7 +1514,20 @@ public:
     }
 
 private:
+    void buildGraph(int graphSteps) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        cudaGraph_t g;
+        ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        for (int k = 0; k < graphSteps; ++k) enqueueStep();
+        ck(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
+        ck(cudaGraphInstantiate(&graph_, g, 0), "cudaGraphInstantiate");
+        cudaGraphDestroy(g);
+        graphSteps_ = graphSteps;
+    }
+
     std::vector<Sim<T>*> members_;
+    int graphSteps_ = 0;
     DevMem mem_;
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
@@ -1715,7 +1726,7 @@ chiml_status batch_steps(chiml_batch* batch, long long maxSteps) {
             if (live.empty()) break;
             if (!batch->packed || set != batch->packedSet) {
                 batch->packed.reset();
-                batch->packed.reset(new PackedBatch<T>(live, batch->device));
+                batch->packed.reset(new PackedBatch<T>(live, batch->device, batch->graphSteps));
                 batch->packedSet = set;
             }
             batch->packed->run(n, batch->graphSteps);
@@ -1741,6 +1752,7 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
         chiml_sim* m = nullptr;
         // without an output directory, a member writes beside its own input file
         chiml_options o = opt ? *opt : chiml_options{CHIML_PREC_FP64, 0, 0, nullptr};
+        o.steps_per_graph = 0;  // members step through the batch's packed graph, not their own
         std::string dir;
         if (!o.out_dir && json_paths[i]) {
             dir = json_paths[i];

@@ -108,6 +108,102 @@ PulseSpec read_pulse(const JNode& pul, double a, double I0) {
     return p;
 }
 
+// Inverse of an n x n column-major matrix in place by LU with partial pivoting
+// (LAPACK dgetrf + dgetri semantics, unblocked: the same operation order as the
+// one-process reference build). Returns the determinant of the factors as
+// UTIL/utilityFxns.hpp:108-116 (getLUFactMatDet) forms it.
+double lu_invert(int n, double* a) {
+    std::vector<int> ipiv(static_cast<std::size_t>(n));
+    for (int j = 0; j < n; ++j) {
+        int p = j;
+        for (int i = j + 1; i < n; ++i)
+            if (std::abs(a[i + j * n]) > std::abs(a[p + j * n])) p = i;
+        ipiv[static_cast<std::size_t>(j)] = p + 1;
+        if (a[p + j * n] == 0.0) continue;
+        if (p != j)
+            for (int k = 0; k < n; ++k) std::swap(a[j + k * n], a[p + k * n]);
+        for (int i = j + 1; i < n; ++i) a[i + j * n] /= a[j + j * n];
+        for (int k = j + 1; k < n; ++k)
+            for (int i = j + 1; i < n; ++i) a[i + k * n] -= a[i + j * n] * a[j + k * n];
+    }
+    double det = 1.0;
+    for (int jj = 1; jj <= n; ++jj)
+        det *= (ipiv[static_cast<std::size_t>(jj - 1)] != jj) ? -1.0 * a[(jj - 1) * (n + 1)] : a[(jj - 1) * (n + 1)];
+    if (det == 0.0) return det;
+    std::vector<double> inv(static_cast<std::size_t>(n) * n, 0.0), e(static_cast<std::size_t>(n));
+    for (int col = 0; col < n; ++col) {
+        std::fill(e.begin(), e.end(), 0.0);
+        e[static_cast<std::size_t>(col)] = 1.0;
+        for (int i = 0; i < n; ++i) std::swap(e[static_cast<std::size_t>(i)], e[static_cast<std::size_t>(ipiv[static_cast<std::size_t>(i)] - 1)]);
+        for (int i = 0; i < n; ++i)
+            for (int k = 0; k < i; ++k) e[static_cast<std::size_t>(i)] -= a[i + k * n] * e[static_cast<std::size_t>(k)];
+        for (int i = n - 1; i >= 0; --i) {
+            for (int k = i + 1; k < n; ++k) e[static_cast<std::size_t>(i)] -= a[i + k * n] * e[static_cast<std::size_t>(k)];
+            e[static_cast<std::size_t>(i)] /= a[i + i * n];
+        }
+        for (int i = 0; i < n; ++i) inv[static_cast<std::size_t>(i + col * n)] = e[static_cast<std::size_t>(i)];
+    }
+    std::copy(inv.begin(), inv.end(), a);
+    return det;
+}
+
+// Object-space coordinates of p, t_i = sum_k coord[i][k] (p - loc)_k (Obj::RealSpace2ObjectSpace).
+std::array<double, 3> to_object(const Object& o, const std::array<double, 3>& p) {
+    std::array<double, 3> c = {p[0] - o.loc[0], p[1] - o.loc[1], p[2] - o.loc[2]};
+    std::array<double, 3> t;
+    for (int i = 0; i < 3; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) s += o.coord[i * 3 + k] * c[k];
+        t[i] = s;
+    }
+    return t;
+}
+
+// Triangular prism from its three 2-D vertices (Obj.cpp:147-200): the vertices are moved
+// to their centroid, which is added to the location, and the vertex matrix rows
+// (x, y, 1) are inverted for the barycentric test.
+void setup_prism(Object& o, const std::array<std::array<double, 2>, 3>& v) {
+    std::array<double, 3> cen = {0.0, 0.0, 0.0};
+    for (int ii = 0; ii < 3; ++ii)
+        for (int k = 0; k < 2; ++k) cen[k] = cen[k] + v[ii][k] / 3.0;
+    for (int k = 0; k < 3; ++k) o.loc[k] = o.loc[k] + cen[k];
+    double m[9];
+    for (int k = 0; k < 9; ++k) m[k] = 1.0;
+    for (int ii = 0; ii < 3; ++ii) {
+        o.verts[ii] = {v[ii][0] - cen[0], v[ii][1] - cen[1], 0.0};
+        m[ii] = o.verts[ii][0];
+        m[ii + 3] = o.verts[ii][1];
+    }
+    if (lu_invert(3, m) == 0.0) throw InputError("The triangular base is a line.");
+    std::copy(m, m + 9, o.invVert.begin());
+}
+
+// Tetrahedron from four real-space vertices (Obj.cpp:215-272): rows (x, y, z, 1) inverted.
+void setup_tetrahedron(Object& o) {
+    double m[16];
+    for (int k = 0; k < 16; ++k) m[k] = 1.0;
+    for (int ii = 0; ii < 4; ++ii)
+        for (int k = 0; k < 3; ++k) m[ii + 4 * k] = o.verts[ii][k];
+    if (lu_invert(4, m) == 0.0) throw InputError("The tetrahedron is planer.");
+    std::copy(m, m + 16, o.invVert.begin());
+}
+
+// Barycentric coordinates of the point (p, 1) with respect to the inverted vertex
+// matrix (UTIL/utilityFxns.hpp:130-141, cart2bary): lambda_i = sum_j inv[i n + j] p_j.
+template <int N>
+std::array<double, N> to_bary(const std::array<double, 16>& inv, const double* p) {
+    std::array<double, N> pad;
+    for (int j = 0; j < N - 1; ++j) pad[j] = p[j];
+    pad[N - 1] = 1.0;
+    std::array<double, N> b;
+    for (int i = 0; i < N; ++i) {
+        double t = 0.0;
+        for (int j = 0; j < N; ++j) t += inv[static_cast<std::size_t>(i * N + j)] * pad[j];
+        b[i] = t;
+    }
+    return b;
+}
+
 Object make_vacuum_block(const std::array<double, 3>& size) {
     Object o;
     o.shape = Shape::BLOCK;
@@ -117,7 +213,7 @@ Object make_vacuum_block(const std::array<double, 3>& size) {
 }
 
 // parallelProgramInputs::ptreeToObject, parallelInputs.cpp:1263-1623 (custom materials,
-// sphere / block / ellipsoid / cylinder).
+// every shape of OBJECTS/Obj.hpp).
 Object read_object(const JNode& node, const Inputs& ip) {
     Object o;
     o.loc = as_arr3(node, "loc");
@@ -197,12 +293,23 @@ Object read_object(const JNode& node, const Inputs& ip) {
         }
     }
     o.ML = node.child("Basis_Set").size() > 0;
+    // shapes and their parameters (parallelInputs.cpp:1468-1622, string2shape :921-951)
     std::string s = node.get<std::string>("shape");
+    auto geoTail = [&]() { o.geoML = o.geo; };
     if (s == "block") {
-        o.shape = Shape::BLOCK;
         o.geo = as_vector(node, "size");
-        if (node.get<double>("rad_curve", 0.0) != 0.0) throw UnsupportedError("rounded blocks are not supported");
-        o.geo.push_back(0.0);
+        o.geo.push_back(node.get<double>("rad_curve", 0.0));
+        if (o.geo.back() == 0.0) {
+            o.shape = Shape::BLOCK;
+        } else {
+            // rounded_block (Obj.cpp:133-145): the centres of curvature of the eight corners
+            o.shape = Shape::ROUNDED_BLOCK;
+            const double rc = o.geo.back();
+            for (int c = 0; c < 8; ++c)
+                for (int k = 0; k < 3; ++k)
+                    o.curveCens[c][k] = ((c >> k) & 1) ? -1.0 * o.geo[k] / 2.0 + rc : o.geo[k] / 2.0 - rc;
+        }
+        geoTail();
     } else if (s == "ellipsoid") {
         o.shape = Shape::ELLIPSOID;
         o.geo = as_vector(node, "size");
@@ -212,34 +319,169 @@ Object read_object(const JNode& node, const Inputs& ip) {
         for (int nn = 0; nn < 3; ++nn)
             if (std::abs(o.cutNeg[nn]) > 1.0 || std::abs(o.cutPos[nn]) > 1.0 || std::abs(o.cutGlobal[nn]) > 1.0)
                 throw InputError("abs(ellipsoid cutoff) must be <= 1.0");
-    } else if (s == "sphere") {
-        o.shape = Shape::SPHERE;
+        geoTail();
+    } else if (s == "hemiellipsoid") {
+        o.shape = Shape::HEMIELLIPSOID;
+        o.geo = as_vector(node, "size");
+        geoTail();
+    } else if (s == "sphere" || s == "hemisphere") {
+        o.shape = s == "sphere" ? Shape::SPHERE : Shape::HEMISPHERE;
         o.geo = {node.get<double>("radius", 0.0)};
+        geoTail();
     } else if (s == "cylinder") {
         o.shape = Shape::CYLINDER;
         o.geo = {node.get<double>("radius", 0.0), node.get<double>("length", 0.0)};
+        geoTail();
+    } else if (s == "cone") {
+        o.shape = Shape::CONE;
+        const double rad1 = node.get<double>("radSmall", 0.0);
+        const double rad2 = node.get<double>("radLarge", 0.0);
+        if (rad2 <= rad1) throw InputError("radLarge for a cone must be greater than radSmall.");
+        const double len = node.get<double>("height", 0.0);
+        const double raiseAng = std::atan((rad2 - rad1) / len);
+        o.geo = {rad2, len, rad2 * std::tan(raiseAng)};
+        geoTail();
+    } else if (s == "trapezoid_prism") {
+        o.shape = Shape::TRI_PRISM;
+        const double base1 = node.get<double>("base1", 0.0);
+        const double base2 = node.get<double>("base2", 0.0);
+        const double base = std::max(base1, base2);
+        const double height = node.get<double>("height", 0.0);
+        const double heightTri = base * 2.0 * height / (base1 - base2);
+        std::array<std::array<double, 2>, 3> v = {{{0, 0.5 * heightTri}, {0.5 * base, -0.5 * heightTri}, {-0.5 * base, -0.5 * heightTri}}};
+        o.geo = {std::abs(height / heightTri), 1.0, 1.0, node.get<double>("length", 0.0)};
+        geoTail();
+        setup_prism(o, v);
+    } else if (s == "triangle_prism") {
+        o.shape = Shape::TRI_PRISM;
+        // the vertex form; any failure in it falls back to the base/height form, as the
+        // reference's try block does
+        bool done = false;
+        const std::array<double, 3> loc0 = o.loc;
+        try {
+            const JNode& vl = node.child("vertLocs");
+            std::vector<double> g = as_vector(node, "barry_center_cutoff", 1.0, 3);
+            g.push_back(node.get<double>("length", 0.0));
+            std::array<std::array<double, 2>, 3> v{};
+            int cc = 0;
+            for (auto& kv : vl.kids) {
+                if (cc > 2) throw InputError("A triangle has exactly 3 verticies.");
+                const std::array<double, 3> p3 = as_arr3(kv.second, "vert", 0.0);
+                v[cc] = {p3[0], p3[1]};
+                ++cc;
+            }
+            if (cc != 3) throw InputError("A triangle has exactly 3 verticies.");
+            o.geo = g;
+            geoTail();
+            setup_prism(o, v);
+            done = true;
+        } catch (const std::exception&) {
+            o.loc = loc0;
+        }
+        if (!done) {
+            // base/height form (Obj.cpp:147-174): vertices (b/2, -h/2), (-b/2, -h/2), (0, h/2)
+            const double base = node.get<double>("base", 0.0), height = node.get<double>("height", 0.0);
+            o.geo = {base, height, 1.0, node.get<double>("length", 0.0)};
+            geoTail();
+            std::array<std::array<double, 2>, 3> v = {{{0.5 * base, -0.5 * height}, {-0.5 * base, -0.5 * height}, {0.0, 0.5 * height}}};
+            setup_prism(o, v);
+            o.geo = {1.0, 1.0, 1.0, o.geo[3]};
+        }
+    } else if (s == "ters_tip") {
+        o.shape = Shape::TERS_TIP;
+        o.geo = {2.0 * node.get<double>("rad_curve", 0.0), node.get<double>("base", 0.0), node.get<double>("length", 0.0)};
+        o.radCen = {0.0, 0.0, -1.0 * o.geo[2] / 2.0 + o.geo[0] / 2.0};
+        geoTail();
+    } else if (s == "paraboloid") {
+        o.shape = Shape::PARABOLOID;
+        const double rc = node.get<double>("rad_curve", 0.0);
+        o.geo = {node.get<double>("a", 1.0 / (2.0 * rc)), node.get<double>("b", 1.0 / (2.0 * rc)), node.get<double>("length", 0.0)};
+        geoTail();
+    } else if (s == "torus") {
+        o.shape = Shape::TORUS;
+        o.geo = {node.get<double>("rad_Ring", 0.0), node.get<double>("rad_CrossSec", 0.0),
+                 node.get<double>("phiMin", 0.0) * M_PI / 180.0, node.get<double>("phiMax", 360.0) * M_PI / 180.0};
+        geoTail();
+    } else if (s == "tetrahedron") {
+        o.shape = Shape::TETRAHEDRON;
+        if (o.ML) throw UnsupportedError("emitters in a tetrahedron are not supported");
+        bool done = false;
+        const std::array<double, 3> loc0 = o.loc;
+        const std::array<double, 9> coord0 = o.coord;
+        try {
+            const JNode& vl = node.child("vertLocs");
+            std::vector<double> g = as_vector(node, "barry_center_cutoff", 1.0, 4);
+            int cc = 0;
+            for (auto& kv : vl.kids) {
+                if (cc > 3) throw InputError("A tetrahedron has exactly 4 verticies.");
+                o.verts[cc] = as_arr3(kv.second, "vert");
+                ++cc;
+            }
+            if (cc != 4) throw InputError("A tetrahedron has exactly 4 verticies.");
+            // real-space vertices: location and unit vectors are reset (parallelInputs.cpp:1602-1606)
+            o.loc = {0.0, 0.0, 0.0};
+            o.coord = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+            o.geo = g;
+            geoTail();
+            setup_tetrahedron(o);
+            done = true;
+        } catch (const std::exception&) {
+            o.loc = loc0;
+            o.coord = coord0;
+        }
+        if (!done) {
+            // regular tetrahedron of side sideLen about the location (Obj.cpp:215-252)
+            o.geo = {node.get<double>("sideLen", 2.0 / std::sqrt(3.0) * node.get<double>("perpBiSect", -1.0))};
+            if (o.geo[0] == -1) throw InputError("please give a side length or prepindicular bisector length for the tetrahedron.");
+            o.geo.push_back(node.get<double>("height", std::sqrt(2.0 / 3.0) * o.geo[0]));
+            geoTail();
+            const double unit[4][3] = {{std::sqrt(8.0 / 9.0), 0, -1.0 / 3.0},
+                                       {-1.0 * std::sqrt(2.0 / 9.0), std::sqrt(2.0 / 3.0), -1.0 / 3.0},
+                                       {-1.0 * std::sqrt(2.0 / 9.0), -1.0 * std::sqrt(2.0 / 3.0), -1.0 / 3.0},
+                                       {0, 0, 1}};
+            for (int v = 0; v < 4; ++v) {
+                for (int i = 0; i < 3; ++i) {
+                    double t = 0.0;
+                    for (int k = 0; k < 3; ++k) t += o.coord[i * 3 + k] * unit[v][k];
+                    o.verts[v][i] = t;
+                }
+                for (int i = 0; i < 3; ++i) o.verts[v][i] *= o.geo[0] * std::sqrt(3.0 / 8.0);
+                for (int i = 0; i < 3; ++i) o.verts[v][i] = 1.0 * o.loc[i] + o.verts[v][i];
+            }
+            setup_tetrahedron(o);
+            // the fourth cut-off: the barycentric weight of vertex 4 at the requested height
+            const double heightRat = (o.geo[1] / (o.geo[0] * std::sqrt(2.0 / 3.0)) * (5.0 / 4.0)) - 1.0 / 4.0;
+            double v4[3];
+            for (int i = 0; i < 3; ++i) v4[i] = heightRat * o.verts[3][i] + o.loc[i];
+            const std::array<double, 4> b = to_bary<4>(o.invVert, v4);
+            o.geo = {1.0, 1.0, 1.0, b[3]};
+        }
     } else {
-        throw UnsupportedError("shape '" + s + "' is not supported");
+        throw InputError("A shape in the ObjectList is not defined in the code");
     }
-    o.geoML = o.geo;
     return o;
 }
 
 // Adds buffer cells around an emitter object so that the polarisation points, which sit
 // between grid points, are inside it (Obj::addMLBuff, OBJECTS/Obj.hpp:537,653,776,949).
 void add_ml_buffer(Object& o, double d) {
+    auto add = [&](std::initializer_list<int> idx) {
+        for (int i : idx) o.geoML[static_cast<std::size_t>(i)] += 3.0 * d;
+    };
     switch (o.shape) {
-        case Shape::SPHERE: o.geoML[0] += 3.0 * d; break;
+        case Shape::SPHERE:
+        case Shape::HEMISPHERE: add({0}); break;
         case Shape::BLOCK:
+        case Shape::ROUNDED_BLOCK:
         case Shape::ELLIPSOID:
-            o.geoML[0] += 3.0 * d;
-            o.geoML[1] += 3.0 * d;
-            o.geoML[2] += 3.0 * d;
-            break;
+        case Shape::HEMIELLIPSOID:
+        case Shape::TRI_PRISM:
+        case Shape::TERS_TIP: add({0, 1, 2}); break;
+        case Shape::CONE: add({1}); break;
         case Shape::CYLINDER:
-            o.geoML[0] += 3.0 * d;
-            o.geoML[1] += 3.0 * d;
-            break;
+        case Shape::PARABOLOID:
+        case Shape::TORUS: add({0, 1}); break;
+        case Shape::TETRAHEDRON: break;  // emitters in a tetrahedron are rejected when read
     }
 }
 
@@ -369,6 +611,7 @@ void read_emitter(const JNode& node, Object& o, Inputs& ip) {
                     if (o.isObj(pt, dminAll, o.geo)) plane[zz].push_back({xx, yy, zz});
                 }
         for (auto& pl : plane) em.locs.insert(em.locs.end(), pl.begin(), pl.end());
+        if (o.baryFault->load()) throw InputError("The sum of the boundary checks for a triangular base does not equal the determinant of the verticies");
     }
     for (auto& kv : node.child("RelaxationOperators").kids) {
         RelaxOp r;
@@ -650,32 +893,51 @@ void Object::setUpConsts(double dt) {
     }
 }
 
-// Shape tests, Obj.cpp:373-540
+// Shape tests, Obj.cpp:373-540 (isObj of every shape), with the reference's tolerances and
+// arithmetic as written (including its quirks: the cone's radius test compares a distance
+// with a squared length, the TERS tip takes the cosine of its apex diameter, and the
+// torus's azimuth is NaN on its axis, where every test against it is false).
 bool Object::isObj(const std::array<double, 3>& v, double dx, const std::vector<double>& geo_) const {
-    auto toObj = [&](const std::array<double, 3>& p) {
-        std::array<double, 3> c = {p[0] - loc[0], p[1] - loc[1], p[2] - loc[2]};
-        std::array<double, 3> t;
-        for (int i = 0; i < 3; ++i) {
-            double s = 0.0;
-            for (int k = 0; k < 3; ++k) s += coord[i * 3 + k] * c[k];
-            t[i] = s;
-        }
-        return t;
+    auto distTo = [](const std::array<double, 3>& a, const std::array<double, 3>& b) {
+        double sum = 0.0;
+        for (int cc = 0; cc < 3; ++cc) sum += std::pow((a[cc] - b[cc]), 2);
+        return std::sqrt(sum);
     };
+    const std::array<double, 3> zero = {0.0, 0.0, 0.0};
     switch (shape) {
-        case Shape::SPHERE: {
-            double sum = 0.0;
-            for (int cc = 0; cc < 3; ++cc) sum += std::pow((v[cc] - loc[cc]), 2);
-            return !(std::sqrt(sum) > geo_[0] + dx / 1.0e6);
+        case Shape::SPHERE: return !(distTo(v, loc) > geo_[0] + dx / 1.0e6);
+        case Shape::HEMISPHERE: {
+            if (distTo(v, loc) > geo_[0] + dx / 1.0e6) return false;
+            return !(to_object(*this, v)[0] > dx / 1e6);
         }
         case Shape::BLOCK: {
-            std::array<double, 3> t = toObj(v);
+            std::array<double, 3> t = to_object(*this, v);
             for (int i = 0; i < 3; ++i)
                 if ((t[i] > geo_[i] / 2.0 + dx / 1.0e6) || (t[i] < -1.0 * geo_[i] / 2.0 - dx / 1.0e6)) return false;
             return true;
         }
+        case Shape::ROUNDED_BLOCK: {
+            std::array<double, 3> t = to_object(*this, v);
+            const double rc = geo_.back();
+            for (int i = 0; i < 3; ++i)
+                if ((t[i] > geo_[i] / 2.0 + dx / 1.0e6) || (t[i] < -1.0 * geo_[i] / 2.0 - dx / 1.0e6)) return false;
+            auto outer = [&](int i) { return (t[i] > geo_[i] / 2.0 - rc + dx / 1.0e6) || (t[i] < -1.0 * geo_[i] / 2.0 + rc - dx / 1.0e6); };
+            auto inner = [&](int i) { return (t[i] < geo_[i] / 2.0 - rc + dx / 1.0e6) && (t[i] > -1.0 * geo_[i] / 2.0 + rc - dx / 1.0e6); };
+            if (outer(0) || outer(1) || outer(2)) {
+                for (int cc = 0; cc < 8; ++cc) {
+                    const auto& c = curveCens[cc];
+                    if ((std::sqrt(std::pow(t[0] - c[0], 2.0) + std::pow(t[1] - c[1], 2.0)) < rc + dx / 1.0e6) ||
+                        (std::sqrt(std::pow(t[2] - c[2], 2.0) + std::pow(t[1] - c[1], 2.0)) < rc + dx / 1.0e6) ||
+                        (std::sqrt(std::pow(t[0] - c[0], 2.0) + std::pow(t[2] - c[2], 2.0)) < rc + dx / 1.0e6))
+                        return true;
+                }
+                if ((inner(0) && inner(1)) || (inner(2) && inner(1)) || (inner(0) && inner(2))) return true;
+                return false;
+            }
+            return true;
+        }
         case Shape::ELLIPSOID: {
-            std::array<double, 3> t = toObj(v);
+            std::array<double, 3> t = to_object(*this, v);
             double ptSum = 0.0;
             for (int i = 0; i < (geo_[2] != 0.0 ? 3 : 2); ++i) ptSum += std::pow((t[i] - dx / 1.0e6) / (geo_[i] / 2.0), 2.0);
             if (1.0 < ptSum) return false;
@@ -686,11 +948,71 @@ bool Object::isObj(const std::array<double, 3>& v, double dx, const std::vector<
             }
             return true;
         }
+        case Shape::HEMIELLIPSOID: {
+            std::array<double, 3> t = to_object(*this, v);
+            if (t[0] > dx / 1e6) return false;
+            double ptSum = 0.0;
+            for (int i = 0; i < (geo_[2] != 0.0 ? 3 : 2); ++i) ptSum += std::pow((t[i] - dx / 1.0e6) / (geo_[i] / 2.0), 2.0);
+            return !(1.0 < ptSum);
+        }
         case Shape::CYLINDER: {
-            std::array<double, 3> t = toObj(v);
+            std::array<double, 3> t = to_object(*this, v);
             if ((t[1] < -1.0 * geo_[1] / 2.0 - dx * 1e-6) || (t[1] > geo_[1] / 2.0 + dx * 1e-6)) return false;
-            double s = std::sqrt(std::pow(t[0], 2) + std::pow(0.0, 2) + std::pow(t[2], 2));
-            if (s > geo_[0] + 1.0e-6 * dx) return false;
+            if (distTo({t[0], 0.0, t[2]}, zero) > geo_[0] + 1.0e-6 * dx) return false;
+            return true;
+        }
+        case Shape::CONE: {
+            std::array<double, 3> t = to_object(*this, v);
+            if ((t[1] < -1.0 * geo_[1] / 2.0 - dx * 1e-6) || (t[1] > geo_[1] / 2.0 + dx * 1e-6)) return false;
+            if (distTo({t[0], 0.0, t[2]}, zero) > std::pow(geo_[0] / geo_[2] * (t[2] - geo_[1] / 2.0), 2.0)) return false;
+            return true;
+        }
+        case Shape::TRI_PRISM: {
+            std::array<double, 3> t = to_object(*this, v);
+            if ((t[2] < -1.0 * geo_[3] / 2.0 - dx * 1e-6) || (t[2] > geo_[3] / 2.0 + dx * 1e-6)) return false;
+            const std::array<double, 3> b = to_bary<3>(invVert, t.data());
+            for (int i = 0; i < 3; ++i)
+                if (b[i] < -1e-13 || b[i] > geo_[i] + 1e-13) return false;
+            if (std::abs(1 - (b[0] + b[1] + b[2])) > 1e-14) {
+                baryFault->store(true);
+                return false;
+            }
+            return true;
+        }
+        case Shape::TETRAHEDRON: {
+            const std::array<double, 4> b = to_bary<4>(invVert, v.data());
+            for (int i = 0; i < 4; ++i)
+                if (b[i] < -1e-6 * dx || (b[i] + dx * 1e-6) > geo_[i]) return false;
+            if (std::abs(1 - (b[0] + b[1] + b[2] + b[3])) > 1e-14) {
+                baryFault->store(true);
+                return false;
+            }
+            return true;
+        }
+        case Shape::TERS_TIP: {
+            std::array<double, 3> t = to_object(*this, v);
+            if (distTo(t, radCen) < geo_[0] / 2.0) return true;
+            if ((t[2] < geo_[0] - geo_[2] / 2.0 - dx * 1e-6) || (t[2] > geo_[1] / 2.0 + dx * 1e-6)) return false;
+            if ((std::pow(t[0], 2.0) + std::pow(t[1], 2.0)) * std::pow(std::cos(geo_[0]), 2.0) - std::pow(t[2] * std::sin(geo_[0]), 2.0) >
+                dx * 1e-6)
+                return false;
+            return true;
+        }
+        case Shape::PARABOLOID: {
+            std::array<double, 3> t = to_object(*this, v);
+            t[1] += geo_[2] / 2.0;
+            if (t[1] > geo_[2]) return false;
+            if (std::pow(t[0] / geo_[0], 2.0) + std::pow(t[2] / geo_[1], 2.0) > t[1]) return false;
+            return true;
+        }
+        case Shape::TORUS: {
+            std::array<double, 3> t = to_object(*this, v);
+            if (std::pow(std::sqrt(std::pow(t[0], 2.0) + std::pow(t[1], 2.0)) - geo_[0], 2.0) > std::pow(geo_[1], 2.0) - std::pow(t[2], 2.0))
+                return false;
+            double phiPt = t[0] != 0 ? std::atan(t[1] / t[0]) : t[1] / std::abs(t[1]) * M_PI / 2.0;
+            if (t[0] < 0) phiPt += M_PI;
+            else if (t[1] < 0) phiPt += 2.0 * M_PI;
+            if (phiPt < geo_[2] || phiPt > geo_[3]) return false;
             return true;
         }
     }

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <memory>
@@ -33,7 +34,22 @@ extern const double kHbar;
 
 enum class Pol { EX, EY, EZ, HX, HY, HZ, L, R };
 enum class PulseShape { GAUSSIAN, CONTINUOUS, RICKER, RAMP_CONT, BH, RECT };
-enum class Shape { SPHERE, BLOCK, ELLIPSOID, CYLINDER };
+// OBJECTS/Obj.hpp:491-1290 (TRI_PRISM covers the reference's triangle and trapezoid prisms)
+enum class Shape {
+    SPHERE,
+    BLOCK,
+    ELLIPSOID,
+    CYLINDER,
+    HEMISPHERE,
+    ROUNDED_BLOCK,
+    HEMIELLIPSOID,
+    CONE,
+    TRI_PRISM,
+    TERS_TIP,
+    PARABOLOID,
+    TORUS,
+    TETRAHEDRON
+};
 enum class DipOr { REL_TO_NORM, ISOTROPIC, UNIDIRECTIONAL, LONG_TAN, LAT_TAN };
 enum class DtcClass { TXT, BIN, FREQ };
 // Same ordering as DTCTYPE (UTIL/enum.hpp:17)
@@ -56,6 +72,14 @@ struct Object {
     std::array<double, 3> loc = {0.0, 0.0, 0.0};
     std::array<double, 9> coord = {1, 0, 0, 0, 1, 0, 0, 0, 1};  // rows: normalised unit vectors
     std::array<double, 3> cutNeg = {-1, -1, -1}, cutPos = {1, 1, 1}, cutGlobal = {1, 1, 1};
+    // shape data built from geo when the object is read (Obj.cpp:133-272)
+    std::array<std::array<double, 3>, 8> curveCens{};  // rounded block: corner centres of curvature
+    std::array<std::array<double, 3>, 4> verts{};      // prism: 2-D vertices about the centroid; tetrahedron: 3-D vertices
+    std::array<double, 16> invVert{};                  // inverse of the vertex matrix (column-major, order 3 or 4)
+    std::array<double, 3> radCen{};                    // TERS tip: centre of the apex sphere
+    // Set when a barycentric test of a prism or tetrahedron fails its sum check (the
+    // reference throws there); shared by the copies of the object.
+    std::shared_ptr<std::atomic<bool>> baryFault = std::make_shared<std::atomic<bool>>(false);
     std::vector<Oscillator> pols;
     // derived per time step (setUpConsts)
     bool orDip = false;

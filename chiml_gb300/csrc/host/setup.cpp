@@ -102,10 +102,15 @@ struct Builder {
             case Shape::ELLIPSOID: r = 0.5 * std::max(std::max(std::abs(o.geoML[0]), std::abs(o.geoML[1])), std::abs(o.geoML[2])); break;
             case Shape::BLOCK: r = 0.5 * std::sqrt(o.geoML[0] * o.geoML[0] + o.geoML[1] * o.geoML[1] + o.geoML[2] * o.geoML[2]); break;
             case Shape::CYLINDER: r = std::sqrt(o.geoML[0] * o.geoML[0] + 0.25 * o.geoML[1] * o.geoML[1]); break;
+            case Shape::HEMISPHERE: r = std::max(o.geoML[0], o.geo[0]); break;
+            case Shape::HEMIELLIPSOID: r = 0.5 * std::max(std::max(std::abs(o.geoML[0]), std::abs(o.geoML[1])), std::abs(o.geoML[2])); break;
+            case Shape::ROUNDED_BLOCK: r = 0.5 * std::sqrt(o.geoML[0] * o.geoML[0] + o.geoML[1] * o.geoML[1] + o.geoML[2] * o.geoML[2]); break;
+            case Shape::TORUS: r = torusRadius(o); break;
+            default: return 1e300;  // cone (unbounded along its axis), prism, tip, paraboloid, tetrahedron
         }
         r += 2.0 * std::max(std::max(d[0], d[1]), d[2]) + 1e-9 * std::abs(r);
         if (!(r < 1e300)) return 1e300;
-        if (o.shape == Shape::ELLIPSOID && o.geo[2] == 0.0 && D.threeD) return 1e300;
+        if ((o.shape == Shape::ELLIPSOID || o.shape == Shape::HEMIELLIPSOID) && o.geo[2] == 0.0 && D.threeD) return 1e300;
         if (o.shape != Shape::SPHERE)
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) {
@@ -114,6 +119,13 @@ struct Builder {
                     if (!(std::abs(dot - (a == b ? 1.0 : 0.0)) < 1e-9)) return 1e300;
                 }
         return r;
+    }
+
+    // Radius about o.loc of a torus: (rho - R)^2 <= r^2 - t_z^2 bounds rho by R + r and |t_z| by r.
+    static double torusRadius(const Object& o) {
+        const double R = std::max(std::abs(o.geo[0]), std::abs(o.geoML[0]));
+        const double rc = std::max(std::abs(o.geo[1]), std::abs(o.geoML[1]));
+        return std::sqrt((R + rc) * (R + rc) + rc * rc);
     }
 
     // Half extents h[q] about o.loc, along each grid axis, of every point isObj accepts with
@@ -139,6 +151,13 @@ struct Builder {
                 case Shape::CYLINDER:
                     h[q] = 0.5 * std::abs(R(1, q)) * g(1) + g(0) * std::sqrt(R(0, q) * R(0, q) + R(2, q) * R(2, q));
                     break;
+                case Shape::HEMISPHERE: h[q] = std::max(o.geoML[0], o.geo[0]); break;
+                case Shape::ROUNDED_BLOCK: h[q] = 0.5 * (std::abs(R(0, q)) * g(0) + std::abs(R(1, q)) * g(1) + std::abs(R(2, q)) * g(2)); break;
+                case Shape::HEMIELLIPSOID:
+                    h[q] = 0.5 * std::sqrt(std::pow(R(0, q) * g(0), 2) + std::pow(R(1, q) * g(1), 2) + std::pow(R(2, q) * g(2), 2));
+                    break;
+                case Shape::TORUS: h[q] = torusRadius(o); break;
+                default: return false;  // no bound kept: the whole grid is scanned
             }
             if (!(h[q] < 1e300)) return false;
         }
@@ -1015,6 +1034,12 @@ struct Builder {
         setupPhys(3, false, {0.0, 0.5, 0.5}, {0, 1, 1});
         setupPhys(4, false, {0.5, 0.0, 0.5}, {1, 0, 1});
         setupPhys(5, false, {0.5, 0.5, 0.0}, {1, 1, 0});
+        // a barycentric test whose weights do not sum to one (Obj.cpp:485-489, 502-506)
+        for (const auto& o : objs)
+            if (o.baryFault->load())
+                throw InputError(o.shape == Shape::TETRAHEDRON
+                                     ? "The sum of the boundary checks for a tetrahedron does not equal the determinant of the verticies"
+                                     : "The sum of the boundary checks for a triangular base does not equal the determinant of the verticies");
         scanPML();
         bool disp = false;
         for (auto& o : objs)
@@ -1043,15 +1068,19 @@ struct Builder {
         for (int c = 0; c < 6; ++c) nComp += present[c] ? 1 : 0;
         const int nThreads = omp_get_max_threads();
         innerThreads_ = std::max(1, nThreads / std::max(1, nComp));
-        const int prevLevels = omp_get_max_active_levels();
-        omp_set_max_active_levels(std::max(prevLevels, 2));
-        // older runtimes (a host application may bring its own) also gate nesting on the
-        // OpenMP 3 switch
+        // Both settings are read before either is changed: in libgomp omp_set_nested(1)
+        // raises max-active-levels to its maximum and omp_set_nested(0) drops it to 1, so
+        // the switch is set first and the level count after it, and on the way out the
+        // switch is restored first and the level count last.
 #pragma GCC diagnostic push
 #pragma GCC diagnostic ignored "-Wdeprecated-declarations"
         const int prevNested = omp_get_nested();
+        const int prevLevels = omp_get_max_active_levels();
+        // older runtimes (a host application may bring its own) also gate nesting on the
+        // OpenMP 3 switch
         omp_set_nested(1);
 #pragma GCC diagnostic pop
+        omp_set_max_active_levels(std::max(prevLevels, 2));
 #pragma omp parallel for schedule(dynamic, 1) num_threads(std::min(nThreads, std::max(1, nComp)))
         for (int q = 0; q < 6; ++q) {
             if (!present[order[q]]) continue;
@@ -1061,11 +1090,11 @@ struct Builder {
                 err[q] = std::current_exception();
             }
         }
-        omp_set_max_active_levels(prevLevels);
 #pragma GCC diagnostic push
 #pragma GCC diagnostic ignored "-Wdeprecated-declarations"
         omp_set_nested(prevNested);
 #pragma GCC diagnostic pop
+        omp_set_max_active_levels(prevLevels);
         for (int q = 0; q < 6; ++q)
             if (err[q]) std::rethrow_exception(err[q]);
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;

@@ -9,6 +9,13 @@
 // runs its own memory pool does not let a library call cudaMalloc/cudaFree
 // (which also synchronise the whole device) behind its back.
 //
+// The array's device address is looked up when a handle is created on a device
+// (box_noalloc_setup, called before the handle's own uploads), once per device.
+// That lookup is what loads this file's module, and with it the array, under
+// lazy module loading; the gather kernels are loaded at the same time. A read
+// therefore neither places the array nor loads code: it launches one kernel and
+// copies.
+//
 // The array is shared by every call on a device and keeps the last call's
 // contents. A call writes every element it copies back before the copy, so no
 // element needs clearing; elements past the box hold older values and are not
@@ -30,20 +37,6 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setupMutex;
 double* g_scratch[kMaxDevices] = {};
 
-// Device address of the array on `device` (which is current); looked up once per device.
-cudaError_t scratch_address(int device, double** out) {
-    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_setupMutex);
-    if (!g_scratch[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_boxScratch);
-        if (e != cudaSuccess) return e;
-        g_scratch[device] = static_cast<double*>(p);
-    }
-    *out = g_scratch[device];
-    return cudaSuccess;
-}
-
 template <typename T>
 __global__ void k_gather_box(const T* __restrict__ U, long long lx, long long lz, int x0, int y0, int z0, int bx,
                              int bz, long long n, double* __restrict__ out) {
@@ -57,17 +50,65 @@ __global__ void k_gather_box(const T* __restrict__ U, long long lx, long long lz
     }
 }
 
+// Device address of the array on `device` (which is current); looked up once per device.
+cudaError_t scratch_address(int device, double** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_setupMutex);
+    if (!g_scratch[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_boxScratch);
+        if (e != cudaSuccess) return e;
+        // load the gather kernels now as well, so that a read loads no code
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, k_gather_box<float>);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_gather_box<double>);
+        if (e != cudaSuccess) return e;
+        g_scratch[device] = static_cast<double*>(p);
+    }
+    *out = g_scratch[device];
+    return cudaSuccess;
+}
+
+// Makes `device` current for its lifetime when it is not already, and puts the caller's
+// current device back on destruction.
+class DeviceGuard {
+public:
+    explicit DeviceGuard(int device) {
+        status_ = cudaGetDevice(&prev_);
+        if (status_ == cudaSuccess && prev_ != device) {
+            status_ = cudaSetDevice(device);
+            switched_ = status_ == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (switched_) cudaSetDevice(prev_);
+    }
+    cudaError_t status() const { return status_; }
+
+private:
+    int prev_ = 0;
+    bool switched_ = false;
+    cudaError_t status_ = cudaSuccess;
+};
+
 }  // namespace
+
+cudaError_t box_noalloc_setup(int device) {
+    DeviceGuard guard(device);
+    if (guard.status() != cudaSuccess) return guard.status();
+    double* scratch = nullptr;
+    return scratch_address(device, &scratch);
+}
 
 template <typename T>
 cudaError_t gather_box_noalloc(int device, const T* U, int lx, int lz, const int box[6], double* hostOut,
                                cudaStream_t stream) {
     const long long n = static_cast<long long>(box[3]) * box[4] * box[5];
     if (n <= 0 || n > kBoxScratchCells) return cudaErrorInvalidValue;
-    cudaError_t e = cudaSetDevice(device);
-    if (e != cudaSuccess) return e;
+    DeviceGuard guard(device);
+    if (guard.status() != cudaSuccess) return guard.status();
     double* scratch = nullptr;
-    e = scratch_address(device, &scratch);
+    cudaError_t e = scratch_address(device, &scratch);
     if (e != cudaSuccess) return e;
     const int threads = 256;
     const long long blocks = std::min<long long>((n + threads - 1) / threads, 152LL * 8);

@@ -160,8 +160,9 @@ struct RecordTable {
 };
 
 // Time-blocked DFT of one flux region. Every sampled step gathers the field
-// value of each accumulated point into a ring of K samples; every K samples one
-// launch folds the ring into the FP64 accumulators:
+// value of each accumulated point into a ring of K samples; every point folds the
+// ring into the FP64 accumulators once per K samples (the point tiles in groups
+// whose folds are staggered, one group every 4 samples):
 //   re[pt][f] += sum_k cos(w_f t_k) F_k[pt],  im[pt][f] += sum_k -sin(w_f t_k) F_k[pt]
 // which is the per-step update of parallelStorageFreqDTCReal::fieldIn
 // (DTC/parallelStorageFreqDTC.cpp:21-30) regrouped over K steps.
@@ -235,11 +236,13 @@ template <typename T>
 void launch_record(const RecordTable& r, const Fields<T>& f, const int* step, void* stream);
 template <typename T>
 void launch_dft_sample(const DftTable<T>& d, const Fields<T>& f, const int* step, void* stream);
-// Folds the ring into the accumulators when the current sample completes a block
-// (flushCount < 0), or unconditionally folds the first flushCount ring slots,
-// taken as samples [firstSample, firstSample + flushCount) (flushCount > 0).
+// Folds the ring into the accumulators for the group of point tiles whose turn comes
+// with the current sample (one group every 4 samples; nothing at the other steps).
 template <typename T>
-void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream);
+void launch_dft_fold(const DftTable<T>& d, const int* step, void* stream);
+// End of a run: folds every group's pending samples, `samples` being the samples taken.
+template <typename T>
+void launch_dft_flush(const DftTable<T>& d, int samples, void* stream);
 void launch_increment(int* step, void* stream);
 template <typename T>
 void launch_step_tail(const StepTail<T>& t, void* stream);

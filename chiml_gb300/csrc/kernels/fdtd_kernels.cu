@@ -658,115 +658,177 @@ __device__ __forceinline__ void lds4(const double* p, double v[4]) {
     v[3] = b.y;
 }
 
-// Tiles tileBegin, tileBegin + tileStride, ... of one fold (all threads of the block).
+// Staggered folds. The point tiles of a table are split into G = K / kFoldStagger
+// groups (point tile q belongs to group q mod G), and every kFoldStagger-th sample one
+// group folds: group g folds at the samples n with n + 1 = (g + 1 + m G) kFoldStagger,
+// each time taking the samples since its previous fold (K of them, or n + 1 at its
+// first fold). Every sample is folded by every group within K samples of being
+// written, so the ring of K slots suffices, and each step carries 1 / kFoldStagger of
+// a group fold: the fold work is spread evenly over the steps instead of arriving as
+// one launch every K samples.
+constexpr int kFoldStagger = 4;
+
+// The sample range one group still has to fold after sample `last` (the flush at the
+// end of a run): first sample and count (count 0 when nothing is pending).
+__device__ __forceinline__ void foldPending(int K, int group, int last, int& first, int& count) {
+    const int n0 = group * kFoldStagger + kFoldStagger - 1;  // the group's first fold
+    int folded = -1;  // last sample the group has folded
+    if (last >= n0) folded = n0 + ((last - n0) / K) * K;
+    first = folded + 1;
+    count = last - folded;
+}
+
+// One tile (kFoldTP points from p0, kFoldTF frequencies from f0) over `count` samples
+// from sample `first` (all threads of the block).
 template <typename T>
-__device__ __forceinline__ void foldTiles(const DftTable<T>& d, const int* step, int flushCount, int firstSample,
-                                          long long tileBegin, long long tileStride) {
+__device__ __forceinline__ void foldTile(const DftTable<T>& d, long long p0, int f0, int first, int count) {
     constexpr int KS = FoldCfg<T>::KS;
     constexpr int EV = 16 / sizeof(T);  // values per 16-byte copy
     __shared__ __align__(16) T smp[2][KS][kFoldTP];
     __shared__ __align__(16) T ph[2][KS][kFoldTF * 2];  // per sample: kFoldTF cos, then kFoldTF -sin
-    int count, first;
-    if (flushCount > 0) {
-        count = flushCount;
-        first = firstSample;
-    } else {
-        const int st = *step;
-        if (st % d.timeInt != 0) return;
-        const int n = st / d.timeInt;
-        if (n % d.K != d.K - 1) return;
-        count = d.K;
-        first = n - (d.K - 1);
-    }
     const int nf = d.nfreq;
     const int tf = threadIdx.x & 7;   // frequencies 4*tf .. 4*tf+3 of the tile
     const int tp = threadIdx.x >> 3;  // points 4*tp .. 4*tp+3 of the tile
-    const int fTiles = (nf + kFoldTF - 1) / kFoldTF;
-    const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * fTiles;
     const int stages = (count + KS - 1) / KS;
-    for (long long tile = tileBegin; tile < tiles; tile += tileStride) {
-        const long long p0 = (tile / fTiles) * kFoldTP;
-        const int f0 = static_cast<int>(tile % fTiles) * kFoldTF;
-        // copies of stage s into buffer s & 1 (the ring pitch and the phasor rows are 16-byte multiples)
-        auto issue = [&](int sg) {
-            const int b = sg & 1;
-            const int k0 = sg * KS;
-            const int kn = min(KS, count - k0);
-            for (int q = threadIdx.x; q < KS * (kFoldTP / EV); q += blockDim.x) {
-                const int k = q / (kFoldTP / EV), c = q % (kFoldTP / EV);
-                if (k < kn) {
-                    const int slot = (first + k0 + k) & (d.K - 1);
-                    cpAsync16(&smp[b][k][c * EV], d.ring + static_cast<long long>(slot) * d.stride + p0 + c * EV);
-                }
+    // copies of stage s into buffer s & 1 (the ring pitch and the phasor rows are 16-byte multiples)
+    auto issue = [&](int sg) {
+        const int b = sg & 1;
+        const int k0 = sg * KS;
+        const int kn = min(KS, count - k0);
+        for (int q = threadIdx.x; q < KS * (kFoldTP / EV); q += blockDim.x) {
+            const int k = q / (kFoldTP / EV), c = q % (kFoldTP / EV);
+            if (k < kn) {
+                const int slot = (first + k0 + k) & (d.K - 1);
+                cpAsync16(&smp[b][k][c * EV], d.ring + static_cast<long long>(slot) * d.stride + p0 + c * EV);
             }
-            for (int q = threadIdx.x; q < KS * (kFoldTF * 2 / EV); q += blockDim.x) {
-                const int k = q / (kFoldTF * 2 / EV), c = q % (kFoldTF * 2 / EV);
-                const int plane = c / (kFoldTF / EV), cc = c % (kFoldTF / EV);
-                if (k < kn)
-                    cpAsync16(&ph[b][k][plane * kFoldTF + cc * EV],
-                              d.phasor + (static_cast<long long>(first + k0 + k) * 2 + plane) * d.nfreqPad + f0 + cc * EV);
-            }
-            cpAsyncCommit();
-        };
-        T are[4][4], aim[4][4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int m = 0; m < 4; ++m) are[j][m] = aim[j][m] = T(0);
-        __syncthreads();  // the previous tile's last stage is no longer read
-        issue(0);
-        for (int sg = 0; sg < stages; ++sg) {
-            if (sg + 1 < stages) issue(sg + 1);
-            else cpAsyncCommit();
-            cpAsyncWait1();
-            __syncthreads();
-            const int b = sg & 1;
-            const int kn = min(KS, count - sg * KS);
-            for (int k = 0; k < kn; ++k) {
-                // the eight threads of a point group read consecutive 16-byte chunks of each
-                // phasor plane: no bank conflicts
-                T v[4], c[4], sn[4];
-                lds4(&smp[b][k][4 * tp], v);
-                lds4(&ph[b][k][4 * tf], c);             // cos of frequencies 4 tf .. 4 tf + 3
-                lds4(&ph[b][k][kFoldTF + 4 * tf], sn);  // -sin
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-#pragma unroll
-                    for (int m = 0; m < 4; ++m) {
-                        are[j][m] += c[m] * v[j];
-                        aim[j][m] += sn[m] * v[j];
-                    }
-            }
-            __syncthreads();  // buffer b is free for stage sg + 2
         }
-        cpAsyncWait0();
+        for (int q = threadIdx.x; q < KS * (kFoldTF * 2 / EV); q += blockDim.x) {
+            const int k = q / (kFoldTF * 2 / EV), c = q % (kFoldTF * 2 / EV);
+            const int plane = c / (kFoldTF / EV), cc = c % (kFoldTF / EV);
+            if (k < kn)
+                cpAsync16(&ph[b][k][plane * kFoldTF + cc * EV],
+                          d.phasor + (static_cast<long long>(first + k0 + k) * 2 + plane) * d.nfreqPad + f0 + cc * EV);
+        }
+        cpAsyncCommit();
+    };
+    T are[4][4], aim[4][4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const long long p = p0 + 4 * tp + j;
-            if (p >= d.npts) continue;
+    for (int j = 0; j < 4; ++j)
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const int f = f0 + 4 * tf + m;
-                if (f >= nf) continue;
-                d.re[p * nf + f] += static_cast<double>(are[j][m]);
-                d.im[p * nf + f] += static_cast<double>(aim[j][m]);
-            }
+        for (int m = 0; m < 4; ++m) are[j][m] = aim[j][m] = T(0);
+    __syncthreads();  // the previous tile's last stage is no longer read
+    issue(0);
+    for (int sg = 0; sg < stages; ++sg) {
+        if (sg + 1 < stages) issue(sg + 1);
+        else cpAsyncCommit();
+        cpAsyncWait1();
+        __syncthreads();
+        const int b = sg & 1;
+        const int kn = min(KS, count - sg * KS);
+        for (int k = 0; k < kn; ++k) {
+            // the eight threads of a point group read consecutive 16-byte chunks of each
+            // phasor plane: no bank conflicts
+            T v[4], c[4], sn[4];
+            lds4(&smp[b][k][4 * tp], v);
+            lds4(&ph[b][k][4 * tf], c);             // cos of frequencies 4 tf .. 4 tf + 3
+            lds4(&ph[b][k][kFoldTF + 4 * tf], sn);  // -sin
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    are[j][m] += c[m] * v[j];
+                    aim[j][m] += sn[m] * v[j];
+                }
+        }
+        __syncthreads();  // buffer b is free for stage sg + 2
+    }
+    cpAsyncWait0();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const long long p = p0 + 4 * tp + j;
+        if (p >= d.npts) continue;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const int f = f0 + 4 * tf + m;
+            if (f >= nf) continue;
+            d.re[p * nf + f] += static_cast<double>(are[j][m]);
+            d.im[p * nf + f] += static_cast<double>(aim[j][m]);
         }
     }
 }
 
+// The group that folds after the sample of the current step, with its first sample and
+// count; false when no group folds at this step.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step, int flushCount,
-                                                  int firstSample) {
-    foldTiles(d, step, flushCount, firstSample, blockIdx.x, gridDim.x);
+__device__ __forceinline__ bool foldGroupNow(const DftTable<T>& d, const int* step, int& group, int& first, int& count) {
+    const int st = *step;
+    if (st % d.timeInt != 0) return false;
+    const int n = st / d.timeInt;
+    if ((n + 1) % kFoldStagger != 0) return false;
+    group = ((n + 1) / kFoldStagger - 1) % (d.K / kFoldStagger);
+    count = min(d.K, n + 1);
+    first = n + 1 - count;
+    return true;
+}
+
+// Step fold: the tiles of the group that folds now, tileBegin, tileBegin + tileStride, ...
+// counted within the group.
+template <typename T>
+__device__ __forceinline__ void foldStep(const DftTable<T>& d, const int* step, long long tileBegin, long long tileStride) {
+    int g, first, count;
+    if (!foldGroupNow(d, step, g, first, count)) return;
+    const int G = d.K / kFoldStagger;
+    const int fTiles = (d.nfreq + kFoldTF - 1) / kFoldTF;
+    const long long pTiles = (d.npts + kFoldTP - 1) / kFoldTP;
+    if (g >= pTiles) return;
+    const long long tiles = ((pTiles - g + G - 1) / G) * fTiles;  // point tiles g, g + G, ... of the group
+    for (long long j = tileBegin; j < tiles; j += tileStride) {
+        const long long q = g + static_cast<long long>(G) * (j / fTiles);
+        foldTile(d, q * kFoldTP, static_cast<int>(j % fTiles) * kFoldTF, first, count);
+    }
+}
+
+// Flush at the end of a run: every tile folds what its group has pending after sample
+// `last`; tiles tileBegin, tileBegin + tileStride, ... of the whole table.
+template <typename T>
+__device__ __forceinline__ void foldFlush(const DftTable<T>& d, int last, long long tileBegin, long long tileStride) {
+    const int G = d.K / kFoldStagger;
+    const int fTiles = (d.nfreq + kFoldTF - 1) / kFoldTF;
+    const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * fTiles;
+    for (long long t = tileBegin; t < tiles; t += tileStride) {
+        const long long q = t / fTiles;
+        int first, count;
+        foldPending(d.K, static_cast<int>(q % G), last, first, count);
+        if (count > 0) foldTile(d, q * kFoldTP, static_cast<int>(t % fTiles) * kFoldTF, first, count);
+    }
 }
 
 template <typename T>
-void launch_dft_fold(const DftTable<T>& d, const int* step, int flushCount, int firstSample, void* stream) {
+__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step) {
+    foldStep(d, step, blockIdx.x, gridDim.x);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft_flush(const DftTable<T> d, int last) {
+    foldFlush(d, last, blockIdx.x, gridDim.x);
+}
+
+template <typename T>
+void launch_dft_fold(const DftTable<T>& d, const int* step, void* stream) {
     if (d.npts == 0) return;
+    const long long pTiles = (d.npts + kFoldTP - 1) / kFoldTP;
+    const long long G = d.K / kFoldStagger;
+    const long long tiles = ((pTiles + G - 1) / G) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
+    const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
+    k_dft_fold<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, step);
+}
+
+template <typename T>
+void launch_dft_flush(const DftTable<T>& d, int samples, void* stream) {
+    if (d.npts == 0 || samples <= 0) return;
     const long long tiles = ((d.npts + kFoldTP - 1) / kFoldTP) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
     const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
-    k_dft_fold<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, step, flushCount, firstSample);
+    k_dft_flush<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, samples - 1);
 }
 
 __global__ void k_increment(int* step) { *step += 1; }
@@ -891,7 +953,12 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_dft_fold_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const DftJob<T>& j = jobs[w.x];
-    foldTiles(j.d, j.step, -1, 0, w.y, 1LL << 62);
+    int g, first, count;
+    if (!foldGroupNow(j.d, j.step, g, first, count)) return;
+    const int fTiles = (j.d.nfreq + kFoldTF - 1) / kFoldTF;
+    const long long q = w.y / fTiles;  // point tile of this block
+    if (q % (j.d.K / kFoldStagger) != g) return;
+    foldTile(j.d, q * kFoldTP, static_cast<int>(w.y % fTiles) * kFoldTF, first, count);
 }
 
 __global__ void k_increment_packed(int* const* __restrict__ steps, int n) {
@@ -966,8 +1033,10 @@ template void launch_record<double>(const RecordTable&, const Fields<double>&, c
 template void launch_record<float>(const RecordTable&, const Fields<float>&, const int*, void*);
 template void launch_dft_sample<double>(const DftTable<double>&, const Fields<double>&, const int*, void*);
 template void launch_dft_sample<float>(const DftTable<float>&, const Fields<float>&, const int*, void*);
-template void launch_dft_fold<double>(const DftTable<double>&, const int*, int, int, void*);
-template void launch_dft_fold<float>(const DftTable<float>&, const int*, int, int, void*);
+template void launch_dft_fold<double>(const DftTable<double>&, const int*, void*);
+template void launch_dft_fold<float>(const DftTable<float>&, const int*, void*);
+template void launch_dft_flush<double>(const DftTable<double>&, int, void*);
+template void launch_dft_flush<float>(const DftTable<float>&, int, void*);
 
 }  // namespace dev
 }  // namespace chiml

@@ -159,12 +159,14 @@ void chiml_batch_destroy(chiml_batch* batch);
  * device) from a library. The values pass through one fixed device array of
  * CHIML_BOX_NOALLOC_MAX_CELLS doubles (8 MiB) per device; a larger box, or one
  * outside the grid, returns CHIML_E_INPUT with the reason in chiml_last_error.
- * The first call on a device looks up that array's address (the only set-up);
- * make that first call before any stream capture on the device. Every call
- * shares the array and leaves its values there; each call writes every value
- * it returns before copying, so nothing needs clearing. The call waits for its
- * copy. Calls that overlap on the GPU (handles of one device used from several
- * host threads at once) race on the array. */
+ * The array is placed on a device, and its address looked up, when the first
+ * handle on that device is created (chiml_create, before the handle's own
+ * uploads), so a read places nothing and loads no code. Every call shares the
+ * array and leaves its values there; each call writes every value it returns
+ * before copying, so nothing needs clearing. The call waits for its copy, and
+ * leaves the calling thread's current device as it found it. Calls that
+ * overlap on the GPU (handles of one device used from several host threads at
+ * once) race on the array. */
 chiml_status chiml_get_box_noalloc(chiml_sim* sim, int comp, const int32_t box[6], double* out);
 
 #ifdef __cplusplus

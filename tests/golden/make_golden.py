@@ -170,6 +170,85 @@ def _c5_small():
     return configs.config5(n=40, nz=48, pml=6, steps=480, nell=3, nfreq=5, sheet_cells=2, film_cells=2)
 
 
+def _bin_planes(cfg, planes, every=20):
+    """Binary snapshot detectors of Ex over planes through the objects (box size, fname)."""
+    dt = cfg["CompCell"]["dt"]
+    for k, (typ, size) in enumerate(planes):
+        cfg["DetectorList"].append({"loc": [0.0, 0.0, 0.0], "size": list(size), "type": typ, "fname": "out/plane%d" % k,
+                                    "dtc_class": "bin", "SI": False, "Time_Interval": every * dt})
+    return cfg
+
+
+def _shape(shape, loc, eps, pols=None, **kw):
+    return configs._obj(shape, loc, material="custom", eps=eps, pols=pols or [], **kw)
+
+
+def _rot(theta_deg, phi_deg):
+    """unit_vectors of a frame rotated by theta about y, then phi about z."""
+    import math
+    t, p = math.radians(theta_deg), math.radians(phi_deg)
+    u0 = [math.cos(t) * math.cos(p), math.cos(t) * math.sin(p), -math.sin(t)]
+    u1 = [-math.sin(p), math.cos(p), 0.0]
+    u2 = [math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)]
+    return [{"uvec": u} for u in (u0, u1, u2)]
+
+
+def _shapes_a():
+    """3-D: the cone (first, so the others overwrite it: the reference's cone test bounds it in
+    y only), a hemisphere, a rotated hemiellipsoid, a rounded block, a partial torus and a
+    paraboloid, one of them with a Lorentz pole; Ex plane source, flux box, two BIN planes."""
+    cfg = configs.config2(n=44, pml=6, steps=200, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    lor = configs.drude_lorentz_pols(5.0, [(0.6, 0.3, 2.4)])
+    cfg["ObjectList"] = [
+        _shape("cone", [-0.4, 0.35, 0.0], 1.4, radSmall=0.05, radLarge=0.15, height=0.3),
+        _shape("hemisphere", [-0.4, -0.3, 0.0], 2.0, radius=0.16, orPhi=30.0),
+        _shape("hemiellipsoid", [0.0, -0.3, 0.05], 2.5, size=[0.3, 0.22, 0.26], unit_vectors=_rot(25.0, 40.0)),
+        _shape("block", [0.4, -0.3, 0.0], 3.0, size=[0.3, 0.26, 0.22], rad_curve=0.06, unit_vectors=_rot(10.0, 15.0)),
+        _shape("torus", [0.0, 0.3, 0.0], 2.2, pols=lor, rad_Ring=0.13, rad_CrossSec=0.06, phiMin=20.0, phiMax=290.0,
+               unit_vectors=_rot(30.0, 0.0)),
+        _shape("paraboloid", [0.4, 0.3, 0.0], 1.8, a=0.28, b=0.2, length=0.3, orTheta=60.0, orPhi=20.0),
+    ]
+    return _bin_planes(cfg, [("Ex", (1.5, 1.5, 0.0)), ("Ey", (0.0, 1.5, 1.5))])
+
+
+def _shapes_b():
+    """3-D: triangular prisms from base/height and from vertices, a trapezoidal prism, a TERS
+    tip, a regular tetrahedron and one from real-space vertices; Ex plane source, flux box,
+    two BIN planes."""
+    cfg = configs.config2(n=44, pml=6, steps=200, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    lor = configs.drude_lorentz_pols(5.0, [(0.6, 0.3, 2.4)])
+    verts = [{"vert": [0.01, 0.16]}, {"vert": [0.15, -0.1]}, {"vert": [-0.13, -0.07]}]
+    tet = [{"vert": [0.31, 0.17, -0.12]}, {"vert": [0.57, 0.23, -0.06]}, {"vert": [0.41, 0.46, 0.01]},
+           {"vert": [0.43, 0.29, 0.21]}]
+    cfg["ObjectList"] = [
+        _shape("triangle_prism", [-0.4, -0.3, 0.0], 2.0, base=0.3, height=0.26, length=0.3, unit_vectors=_rot(20.0, 30.0)),
+        _shape("triangle_prism", [0.0, -0.3, 0.02], 2.6, vertLocs=verts, length=0.25),
+        _shape("trapezoid_prism", [0.4, -0.3, 0.0], 1.7, pols=lor, base1=0.3, base2=0.14, height=0.21, length=0.26,
+               orPhi=15.0),
+        _shape("ters_tip", [-0.4, 0.3, 0.0], 3.2, rad_curve=0.1, base=0.3, length=0.3),
+        _shape("tetrahedron", [0.0, 0.3, 0.0], 2.4, sideLen=0.34, unit_vectors=_rot(15.0, 35.0)),
+        _shape("tetrahedron", [0.0, 0.0, 0.0], 1.9, vertLocs=tet),
+    ]
+    return _bin_planes(cfg, [("Ex", (1.5, 1.5, 0.0)), ("Ey", (0.0, 1.5, 1.5))])
+
+
+def _shapes_2d():
+    """2-D TMz: partial torus, paraboloid, hemisphere, rounded block and triangular prism (in
+    2-D the third unit vector is zero, so the reference's object-frame z is NaN and every test
+    on it passes: the torus fills its azimuth range and the paraboloid a half-plane, so they
+    come first and the others overwrite them); point source, text detectors, flux line, one
+    BIN plane."""
+    cfg = configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=3, nfreq=8)
+    cfg["ObjectList"] = [
+        _shape("torus", [-0.6, -0.6, 0.0], 1.8, rad_Ring=0.25, rad_CrossSec=0.1, phiMin=0.0, phiMax=250.0),
+        _shape("paraboloid", [0.0, 0.0, 0.0], 2.2, a=0.5, b=0.4, length=0.5, orPhi=90.0),
+        _shape("hemisphere", [0.5, 0.6, 0.0], 2.0, radius=0.3, orPhi=45.0),
+        _shape("block", [-0.6, 0.7, 0.0], 2.5, size=[0.6, 0.4, 0.0], rad_curve=0.1, orPhi=20.0),
+        _shape("triangle_prism", [0.7, -0.6, 0.0], 3.0, base=0.5, height=0.45, length=0.0, orPhi=-30.0),
+    ]
+    return _bin_planes(cfg, [("Ez", (3.0, 3.0, 0.0))])
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -186,6 +265,9 @@ CASES = {
     "freq_3d": _freq_3d,
     "freq_2d": _freq_2d,
     "c5_small": _c5_small,
+    "shapes_a": _shapes_a,
+    "shapes_b": _shapes_b,
+    "shapes_2d": _shapes_2d,
 }
 
 

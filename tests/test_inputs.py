@@ -27,7 +27,8 @@ def _base():
     (lambda c: c["CompCell"].__setitem__("cplxFields", True), 2),
     (lambda c: c["ObjectList"][0].__setitem__("mu", 2.0), 2),
     (lambda c: c["ObjectList"][0].__setitem__("material", "Au"), 2),
-    (lambda c: c["ObjectList"][0].__setitem__("shape", "torus"), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("shape", "dodecahedron"), 1),
+    (lambda c: c["ObjectList"][0].update(shape="cone", radSmall=0.2, radLarge=0.1, height=0.3), 1),
     (lambda c: c["DetectorList"][0].__setitem__("dtc_class", "bmp"), 2),
     (lambda c: c["DetectorList"][0].__setitem__("type", "Mx"), 2),
     (lambda c: c["CompCell"].__setitem__("dt", 1.0), 1),

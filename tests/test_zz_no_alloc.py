@@ -2,9 +2,11 @@
 against chiml_get_field on the same handle.
 
 Two calls in a row on one handle, with steps between them and a smaller second box,
-so that the second call runs on an array that still holds the first call's values.
+so that the second call runs on an array that still holds the first call's values; and
+the device's free memory, read through the driver, unchanged by a series of calls.
 Collected last so that it runs both after the other GPU tests and alone.
 """
+import ctypes
 import os
 
 import numpy as np
@@ -77,5 +79,49 @@ def test_box_noalloc_rejects_bad_boxes(built_engine, tmp_path):
         got = sim.box_noalloc("Ez", (0, 0, 0), (lx, rows, 1))
         ref = _slice(sim.field("Ez"), (0, 0, 0), (lx, rows, 1))
         assert _rel_l2(got, ref) <= TOL
+    finally:
+        sim.close()
+
+
+def _device_free_bytes(device=0):
+    """Free memory of the device as the driver reports it (cuMemGetInfo in the device's
+    primary context, the context the engine's runtime calls use)."""
+    cuda = ctypes.CDLL("libcuda.so.1")
+    assert cuda.cuInit(0) == 0
+    dev = ctypes.c_int()
+    assert cuda.cuDeviceGet(ctypes.byref(dev), device) == 0
+    ctx = ctypes.c_void_p()
+    assert cuda.cuDevicePrimaryCtxRetain(ctypes.byref(ctx), dev) == 0
+    try:
+        assert cuda.cuCtxPushCurrent_v2(ctx) == 0
+        free, total = ctypes.c_size_t(), ctypes.c_size_t()
+        rc = cuda.cuMemGetInfo_v2(ctypes.byref(free), ctypes.byref(total))
+        cuda.cuCtxPopCurrent_v2(ctypes.byref(ctypes.c_void_p()))
+        assert rc == 0
+        return free.value
+    finally:
+        cuda.cuDevicePrimaryCtxRelease_v2(dev)
+
+
+def test_box_noalloc_allocates_nothing(built_engine, tmp_path):
+    """Free device memory after the handle is created and stepped equals free memory after
+    several reads, the largest allowed box among them."""
+    from chiml_gb300 import Simulation
+    from chiml_gb300.api import BOX_NOALLOC_MAX_CELLS
+    sim = Simulation(os.path.join(GOLDEN, "c2_small", "in.json"), precision="split", out_dir=str(tmp_path))
+    try:
+        s = sim.stats()
+        lx, ly = s.nx + 2, s.ny + 2
+        lz = s.cells // (lx * ly)
+        sim.step(3)
+        sim.sync()
+        before = _device_free_bytes()
+        rows = min(ly, BOX_NOALLOC_MAX_CELLS // (lx * lz))
+        boxes = [("Ez", (0, 0, 0), (lx, rows, lz)), ("Hx", (1, 2, 3), (4, 5, 6)), ("Ey", (0, 0, 0), (lx, 1, lz))]
+        got = [sim.box_noalloc(name, origin, shape) for name, origin, shape in boxes]
+        after = _device_free_bytes()
+        assert after == before, "free device memory changed by %d bytes" % (before - after)
+        for (name, origin, shape), g in zip(boxes, got):
+            assert _rel_l2(g, _slice(sim.field(name), origin, shape)) <= TOL
     finally:
         sim.close()
