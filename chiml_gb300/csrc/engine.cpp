@@ -1026,8 +1026,9 @@ private:
             pStart.push_back(static_cast<int>(al.size()));
             pCount.push_back(static_cast<int>(P.alpha[o].size()));
             for (std::size_t q = 0; q < P.alpha[o].size(); ++q) {
-                al.push_back(static_cast<T>(P.alpha[o][q]));
-                xi.push_back(static_cast<T>(P.xi[o][q]));
+                // the FP32 kernels take the increment form's coefficients (kIncrementPoles)
+                al.push_back(static_cast<T>(dev::kIncrementPoles<T> ? P.alphaInc[o][q] : P.alpha[o][q]));
+                xi.push_back(static_cast<T>(dev::kIncrementPoles<T> ? -1.0 * P.xi[o][q] : P.xi[o][q]));
                 ga.push_back(static_cast<T>(P.gamma[o][q]));
             }
         }
@@ -1050,8 +1051,8 @@ private:
             pass.pitch = pitch_;
             pass.poleStart = dStart;
             pass.poleCount = dCount;
-            pass.alpha = dAl;
-            pass.xi = dXi;
+            pass.poleA = dAl;
+            pass.poleB = dXi;
             pass.gamma = dGa;
             pass.nObj = static_cast<int>(pCount.size());
             for (int ci = 0; ci < 3; ++ci) {

@@ -212,6 +212,102 @@ Object make_vacuum_block(const std::array<double, 3>& size) {
     return o;
 }
 
+
+// Named materials (getMater, parallelInputs.cpp:1066-1179). The Lorentz-Drude parameter
+// sets are the published ones the reference tabulates (UTIL/dielectric_params.hpp): the
+// Rakic et al. sets (Appl. Opt. 37, 5271 (1998)) as {omega_p, then (f, Gamma, omega) per
+// oscillator, omega = 0 for the Drude term}, all in eV; the "JM" sets in the same layout
+// with the oscillator strength given directly; two quantum-dot resonances. eps_inf is the
+// reference's, including the 1 + k 1e-14 of the metals (which keeps them from counting as
+// vacuum). The numbers have to be the reference's: they are the material constants.
+enum class PoleForm { NONE, RAKIC, JM };
+struct NamedMaterial {
+    std::vector<std::string> names;
+    double epsInf;
+    PoleForm form;
+    std::vector<double> params;
+};
+
+const std::vector<NamedMaterial>& named_materials() {
+    static const std::vector<NamedMaterial> table = {
+        {{"Au", "au", "AU"}, 1.0 + 1.0e-14, PoleForm::RAKIC,
+         {9.03, 0.760, 0.053, 0.0, 0.024, 0.241, 0.415, 0.010, 0.345, 0.830, 0.071, 0.870, 2.969, 0.601, 2.494, 4.304, 4.384, 2.214, 13.32}},
+        {{"Ag", "ag", "AG"}, 1.0 + 1.1e-14, PoleForm::RAKIC,
+         {9.01, 0.845, 0.048, 0.0, 0.065, 3.886, 0.816, 0.124, 0.452, 4.481, 0.011, 0.065, 8.185, 0.840, 0.916, 9.083, 5.646, 2.419, 20.29}},
+        {{"Al", "al", "AL"}, 1.0 + 1.2e-14, PoleForm::RAKIC,
+         {14.98, 0.523, 0.047, 0.0, 0.227, 0.333, 0.162, 0.050, 0.312, 1.544, 0.166, 1.351, 1.808, 0.030, 3.382, 3.473}},
+        {{"Cu", "cu", "CU"}, 1.0 + 1.3e-14, PoleForm::RAKIC,
+         {10.83, 0.575, 0.030, 0.0, 0.061, 0.378, 0.291, 0.104, 1.056, 2.957, 0.723, 2.213, 5.300, 0.638, 4.305, 11.18}},
+        {{"Be", "be", "BE"}, 1.0 + 1.4e-14, PoleForm::RAKIC,
+         {18.51, 0.084, 0.035, 0.0, 0.031, 1.664, 0.100, 0.140, 3.395, 1.032, 0.530, 4.454, 3.183, 0.130, 1.802, 4.604}},
+        {{"Cr", "cr", "CR"}, 1.0 + 1.5e-14, PoleForm::RAKIC,
+         {10.75, 0.168, 0.047, 0.0, 0.151, 3.175, 0.121, 0.150, 1.305, 0.543, 1.149, 2.676, 1.970, 0.825, 1.335, 8.775}},
+        {{"Ni", "ni", "NI"}, 1.0 + 1.6e-14, PoleForm::RAKIC,
+         {15.92, 0.096, 0.048, 0.0, 0.100, 4.511, 0.174, 0.135, 1.334, 0.582, 0.106, 2.178, 1.597, 0.729, 6.292, 6.089}},
+        {{"Pt", "pt", "PT"}, 1.0 + 1.7e-14, PoleForm::RAKIC,
+         {9.59, 0.333, 0.080, 0.0, 0.191, 0.517, 0.780, 0.659, 1.838, 1.314, 0.547, 3.668, 3.141, 3.576, 8.517, 9.249}},
+        {{"Pd", "pd", "PD"}, 1.0 + 1.8e-14, PoleForm::RAKIC,
+         {9.72, 0.330, 0.008, 0.0, 0.649, 2.950, 0.336, 0.121, 0.555, 0.501, 0.638, 4.621, 1.659, 0.453, 3.236, 5.715}},
+        {{"Ti", "ti", "TI"}, 1.0 + 1.9e-14, PoleForm::RAKIC,
+         {7.29, 0.148, 0.082, 0.0, 0.899, 2.276, 0.777, 0.393, 2.518, 1.545, 0.187, 1.663, 2.509, 0.001, 1.762, 19.43}},
+        {{"W", "w"}, 1.0 + 2.0e-14, PoleForm::RAKIC,
+         {13.22, 0.206, 0.064, 0.0, 0.054, 0.530, 1.004, 0.166, 1.281, 1.917, 0.706, 3.332, 3.580, 2.590, 5.836, 7.498}},
+        {{"TiO2"}, 6.20001, PoleForm::NONE, {}},
+        {{"SiO2"}, 2.1025, PoleForm::NONE, {}},
+        {{"Si"}, 11.8336, PoleForm::NONE, {}},
+        {{"CdSe"}, 6.20, PoleForm::NONE, {}},
+        {{"CdSeQD"}, 6.20, PoleForm::RAKIC, {2.03253, 0.65, 0.140, 2.03253}},
+        {{"PbS"}, 17.20, PoleForm::NONE, {}},
+        {{"PbSQD"}, 17.20, PoleForm::RAKIC, {1.45864, 5.00, 0.26, 1.45864}},
+        {{"vac", "Vac", "VAC"}, 1.0, PoleForm::NONE, {}},
+        {{"JM_Ag", "JM_ag", "JM_AG"}, 1.256, PoleForm::JM, {9.219, 1.0, 0.000, 0.0, 2.244, 0.133, 5.456, 0.187, 0.407, 2.014}},
+        {{"JM_Au", "JM_au", "JM_AU"}, 5.513, PoleForm::JM, {9.013, 1.0, 0.000, 0.0, 1.857, 0.714, 3.658, 1.004, 0.399, 2.833}},
+        {{"JM_Al", "JM_al", "JM_AL"}, 1.000 + 2.1e-14, PoleForm::JM, {14.344, 1.0, 0.651, 0.0, 4.283, 0.203, 1.645, 0.069, 0.036, 3.933}},
+        {{"JM_Ga", "JM_ga", "JM_GA"}, 1.000 + 2.2e-14, PoleForm::JM, {9.954, 1.0, 1.796, 0.0, 30.615, 0.912, 1.863, 3.440, 0.215, 2.136}},
+        {{"JM_Sn", "JM_sn", "JM_SN"}, 1.203, PoleForm::JM, {12.439, 1.0, 0.757, 0.0, 0.560, 1.546, 6.699, 0.902, 0.563, 4.011}},
+        {{"JM_Tl", "JM_tl", "JM_TL"}, 1.456, PoleForm::JM, {6.314, 1.0, 0.000, 0.0, 0.527, 0.989, 5.332, 52.200, 0.763, 1.378}},
+        {{"JM_Pb", "JM_pb", "JM_PB"}, 1.000 + 2.3e-14, PoleForm::JM, {9.210, 1.0, 0.157, 0.0, 1.602, 14.011, 16.755, 17.903, 1.138, 2.449}},
+        {{"JM_Bi", "JM_bi", "JM_BI"}, 3.702, PoleForm::JM, {9.004, 1.0, 0.878, 0.0, 5.244, 1.833, 2.914, 5.161, 0.308, 1.484}},
+    };
+    return table;
+}
+
+// Oscillators of a named material's parameter set (getMetal / getMetalJM,
+// parallelInputs.cpp:1186-1261): energies in eV to FDTD frequencies (ev2FDTD); a zero
+// centre is the Drude term, given a 1e-20 eV centre. Rakic: sigma = f (wp / omega)^2,
+// gamma_in = Gamma; JM: the Drude term as Rakic's with f = 1, the others sigma = f and
+// gamma_in = 2 Gamma. The stored values are gamma_in pi and omega 2 pi, as for custom poles.
+std::vector<Oscillator> named_poles(const NamedMaterial& m, double a) {
+    std::vector<Oscillator> out;
+    if (m.form == PoleForm::NONE) return out;
+    auto ev2fdtd = [a](double ev) { return ev / 4.135666e-15 * a / kSpeedOfLight; };
+    const std::vector<double>& par = m.params;
+    const double wp = ev2fdtd(par[0]);
+    for (std::size_t ii = 0; ii < (par.size() - 1) / 3; ++ii) {
+        Oscillator osc;
+        osc.dipOrE = DipOr::ISOTROPIC;
+        osc.uVecDipE = {1.0, 1.0, 1.0};
+        const double f = par[3 * ii + 1];
+        const double GAM = ev2fdtd(par[3 * ii + 2]);
+        double OMG = ev2fdtd(par[3 * ii + 3]);
+        bool drude = false;
+        if (OMG == 0.0) {
+            drude = true;
+            OMG = ev2fdtd(1.0e-20);
+        }
+        if (m.form == PoleForm::RAKIC) {
+            osc.sigP = f * std::pow(wp / OMG, 2);
+            osc.gam = GAM * M_PI;
+        } else {
+            osc.sigP = drude ? std::pow(wp / OMG, 2.0) : f;
+            osc.gam = drude ? GAM * M_PI : 2.0 * GAM * M_PI;
+        }
+        osc.omg = OMG * 2.0 * M_PI;
+        out.push_back(osc);
+    }
+    return out;
+}
+
 // parallelProgramInputs::ptreeToObject, parallelInputs.cpp:1263-1623 (custom materials,
 // every shape of OBJECTS/Obj.hpp).
 Object read_object(const JNode& node, const Inputs& ip) {
@@ -219,11 +315,15 @@ Object read_object(const JNode& node, const Inputs& ip) {
     o.loc = as_arr3(node, "loc");
     std::string material = node.get<std::string>("material");
     if (material != "custom") {
-        if (material == "vac" || material == "Vac" || material == "VAC") {
-            o.epsInf = 1.0;
-        } else {
-            throw UnsupportedError("named material '" + material + "' is not supported; give a custom material");
-        }
+        const NamedMaterial* m = nullptr;
+        for (const NamedMaterial& nm : named_materials())
+            for (const std::string& n : nm.names)
+                if (n == material) m = &nm;
+        if (!m)
+            throw InputError("The material name " + material +
+                             " is not a predefined material. Please give me all the parameters or select from one of our predefined materials");
+        o.epsInf = m->epsInf;
+        o.pols = named_poles(*m, ip.a);
     } else {
         o.epsInf = node.get<double>("eps", 1.00);
         if (node.get<double>("mu", 1.0) != 1.0)
@@ -878,6 +978,7 @@ void Object::setUpConsts(double dt) {
     alpha.clear();
     xi.clear();
     gamma.clear();
+    alphaInc.clear();
     dipOr.clear();
     dipE.clear();
     orDip = false;
@@ -889,6 +990,7 @@ void Object::setUpConsts(double dt) {
             alpha.push_back(((2 - std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
             xi.push_back(((p.gam * dt - 1) / (1 + p.gam * dt)));
             gamma.push_back(((p.sigP * std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
+            alphaInc.push_back(-1.0 * std::pow(p.omg * dt, 2.0) / (1 + p.gam * dt));
         }
     }
 }

@@ -84,6 +84,7 @@ struct Object {
     // derived per time step (setUpConsts)
     bool orDip = false;
     std::vector<double> alpha, xi, gamma;
+    std::vector<double> alphaInc;  // -(omega dt)^2 / (1 + gamma dt) = alpha + xi - 1, formed without cancellation
     std::vector<DipOr> dipOr;
     std::vector<std::array<double, 3>> dipE;
 

@@ -267,8 +267,9 @@ struct Plan {
     // relative permittivity on the cell-centred grid (epsRelOrDip_), where the emitter
     // polarisation is divided into E; filled only when there are emitters
     std::vector<double> epsP;
-    // object pole coefficients, flattened: per object, per pole
-    std::vector<std::vector<double>> alpha, xi, gamma;
+    // object pole coefficients, flattened: per object, per pole; alphaInc is alpha + xi - 1
+    // formed directly (the increment form of the FP32 kernels)
+    std::vector<std::vector<double>> alpha, xi, gamma, alphaInc;
 };
 
 // Builds the plan; throws InputError / UnsupportedError.

@@ -1102,10 +1102,12 @@ struct Builder {
         P.alpha.clear();
         P.xi.clear();
         P.gamma.clear();
+        P.alphaInc.clear();
         for (auto& o : objs) {
             P.alpha.push_back(o.alpha);
             P.xi.push_back(o.xi);
             P.gamma.push_back(o.gamma);
+            P.alphaInc.push_back(o.alphaInc);
         }
         P.in.objects = objs;
         buildSources();

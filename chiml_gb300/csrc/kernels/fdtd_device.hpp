@@ -52,6 +52,16 @@ constexpr uint32_t kFcKp1 = 256u;    // term K adds its normal-slab profile kpro
 constexpr uint32_t kFcOrDip = 512u;  // oriented-dipole D -> E (E pass)
 constexpr uint32_t kFcDtoE = 1024u;  // D -> E of a cell whose object has no poles: E = D / eps_inf (E pass)
 
+// Form of the Lorentz / Drude recursion (UpdateLorPol, UTIL/FDTD_up_eq.cpp:425-448).
+// FP64 keeps the reference's form, P+ = alpha P + xi P- + gamma E, with Pprev holding P-.
+// FP32 uses the increment form: Pprev holds J = P - P-, and
+//   J+ = b J + a P + gamma E,  P+ = P + J+,  a = alpha + xi - 1 = -(w dt)^2 / (1 + g dt),  b = -xi,
+// which is the same recursion without its cancellation: alpha ~ 2 and xi ~ -1, so alpha P
+// + xi P- subtracts two nearly equal values, and in FP32 the rounding of that difference
+// accumulates over the run (a Drude pole integrates it twice).
+template <typename T>
+constexpr bool kIncrementPoles = sizeof(T) == 4;
+
 // The FP32 interior kernels update the dispersive (Lorentz, oriented-dipole) cells
 // themselves; the FP64 ones, whose register budget the extra path would exceed, leave
 // them to the list kernel (measured: FP32 E pass 0.25 ms inline vs 0.30 ms with the list
@@ -70,7 +80,7 @@ struct Comp {
     int present;
     int nPoles;
     T* P[kMaxPoles];
-    T* Pprev[kMaxPoles];
+    T* Pprev[kMaxPoles];   // P- (FP64 form) or J = P - P- (increment form)
     // neighbour terms J (uses grid_j) and K (uses grid_k)
     int tpresent[2];
     int axis[2];
@@ -100,7 +110,7 @@ struct OrDipDev {
     const int* obj;
     const T* dip;                  // [(pole * 3 + axis) * n + entry]
     T* P[3][kMaxPoles];
-    T* Pprev[3][kMaxPoles];
+    T* Pprev[3][kMaxPoles];        // P- (FP64 form) or J = P - P- (increment form)
     long long off[3];              // grid index step along x, y, z
 };
 
@@ -111,8 +121,8 @@ struct Pass {
     long long pitch;        // device row length: cell (x, y, z) is x + pitch (z + lz y), pitch >= lx
     const int* poleStart;   // per object: first pole in the coefficient arrays
     const int* poleCount;   // per object: number of poles
-    const T* alpha;
-    const T* xi;
+    const T* poleA;         // per pole: alpha (FP64 form) or a (increment form, kIncrementPoles)
+    const T* poleB;         // per pole: xi (FP64 form) or b = -xi (increment form)
     const T* gamma;
     int nObj;
     unsigned int* err;      // device error word (kErr* bits); the kernel skips the cell instead of faulting

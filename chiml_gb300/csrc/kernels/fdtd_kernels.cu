@@ -17,6 +17,26 @@
 namespace chiml {
 namespace dev {
 
+// One pole of the Lorentz recursion at one point: p (P, updated) and pm (P- or J, see
+// kIncrementPoles), from the drive term g = gamma E (or gamma d (d . <E>)).
+template <typename T>
+__device__ __forceinline__ void poleStep(T& p, T& pm, T A, T B, T g) {
+    if (kIncrementPoles<T>) {
+        T j = B * pm;
+        j += A * p;
+        j += g;
+        p = p + j;
+        pm = j;
+    } else {
+        const T old = p;
+        T np = A * old;
+        np += B * pm;
+        np += g;
+        p = np;
+        pm = old;
+    }
+}
+
 // One component of one cell, any class (the arithmetic every pass form shares).
 template <typename T, bool EPASS>
 __device__ __forceinline__ void cellGeneric(const Pass<T>& p, int ci, long long i, const int coord[3]) {
@@ -37,12 +57,10 @@ __device__ __forceinline__ void cellGeneric(const Pass<T>& p, int ci, long long 
         const int s = p.poleStart[k.obj];
         const int n = p.poleCount[k.obj];
         for (int q = 0; q < n; ++q) {
-            const T old = c.P[q][i];
-            T np = p.alpha[s + q] * old;
-            np += p.xi[s + q] * c.Pprev[q][i];
-            np += p.gamma[s + q] * e;
-            c.P[q][i] = np;
-            c.Pprev[q][i] = old;
+            T pq = c.P[q][i], pm = c.Pprev[q][i];
+            poleStep(pq, pm, p.poleA[s + q], p.poleB[s + q], p.gamma[s + q] * e);
+            c.P[q][i] = pq;
+            c.Pprev[q][i] = pm;
         }
     }
     T add = T(0);
@@ -115,25 +133,30 @@ __device__ __forceinline__ void ordipEntry(const Pass<T>& p, long long j) {
         const T dx = od.dip[(pp * 3 + 0) * od.n + j];
         const T dy = od.dip[(pp * 3 + 1) * od.n + j];
         const T dz = od.dip[(pp * 3 + 2) * od.n + j];
-        const T jx = od.P[0][pp][i], jy = od.P[1][pp][i], jz = od.P[2][pp][i];
-        T px = p.alpha[s + pp] * jx;
-        px = px + p.xi[s + pp] * od.Pprev[0][pp][i];
-        T py = p.alpha[s + pp] * jy;
-        py = py + p.xi[s + pp] * od.Pprev[1][pp][i];
-        T pz = p.alpha[s + pp] * jz;
-        pz = pz + p.xi[s + pp] * od.Pprev[2][pp][i];
         T dot = dx * Ex[i] / T(2);
         dot += T(1) * (dx * Ex[i - od.off[0]] / T(2));
         dot += T(1) * (dy * Ey[i] / T(2));
         dot += T(1) * (dy * Ey[i - od.off[1]] / T(2));
         dot += T(1) * (dz * Ez[i] / T(2));
         dot += T(1) * (dz * Ez[i - od.off[2]] / T(2));
-        od.P[0][pp][i] = px + p.gamma[s + pp] * (dx * dot);
-        od.P[1][pp][i] = py + p.gamma[s + pp] * (dy * dot);
-        od.P[2][pp][i] = pz + p.gamma[s + pp] * (dz * dot);
-        od.Pprev[0][pp][i] = jx;
-        od.Pprev[1][pp][i] = jy;
-        od.Pprev[2][pp][i] = jz;
+        const T A = p.poleA[s + pp], B = p.poleB[s + pp], g = p.gamma[s + pp];
+        const T dd[3] = {dx, dy, dz};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            T pa = od.P[a][pp][i], pm = od.Pprev[a][pp][i];
+            if (kIncrementPoles<T>) {
+                poleStep(pa, pm, A, B, g * (dd[a] * dot));
+            } else {
+                // UpdateLorPolOrDip's order: alpha P + xi P-, then + gamma d (d . <E>)
+                const T old = pa;
+                T np = A * old;
+                np = np + B * pm;
+                pa = np + g * (dd[a] * dot);
+                pm = old;
+            }
+            od.P[a][pp][i] = pa;
+            od.Pprev[a][pp][i] = pm;
+        }
     }
 }
 
@@ -218,12 +241,10 @@ __device__ __forceinline__ T dispersiveE(const Pass<T>& p, int ci, uint32_t fl, 
 #pragma unroll
         for (int q = 0; q < kMaxPoles; ++q) {
             if (q >= n) break;
-            const T old = c.P[q][i];
-            T np = p.alpha[s + q] * old;
-            np += p.xi[s + q] * c.Pprev[q][i];
-            np += p.gamma[s + q] * u;
-            c.P[q][i] = np;
-            c.Pprev[q][i] = old;
+            T pq = c.P[q][i], pm = c.Pprev[q][i];
+            poleStep(pq, pm, p.poleA[s + q], p.poleB[s + q], p.gamma[s + q] * u);
+            c.P[q][i] = pq;
+            c.Pprev[q][i] = pm;
         }
     }
     T d = c.D[i];

@@ -249,6 +249,40 @@ def _shapes_2d():
     return _bin_planes(cfg, [("Ez", (3.0, 3.0, 0.0))])
 
 
+def _named(shape, loc, material, **kw):
+    return configs._obj(shape, loc, material=material, **kw)
+
+
+def _named_3d():
+    """3-D: named materials (Rakic Au and W, JM Ag, TiO2, Si, the CdSe quantum-dot
+    resonance); Ex plane source, flux box, two BIN planes."""
+    cfg = configs.config2(n=44, pml=6, steps=220, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    cfg["ObjectList"] = [
+        _named("block", [-0.35, -0.3, 0.0], "TiO2", size=[0.3, 0.25, 0.3]),
+        _named("sphere", [0.0, 0.0, 0.0], "Au", radius=0.18),
+        _named("ellipsoid", [0.38, -0.3, 0.05], "JM_Ag", size=[0.3, 0.2, 0.24]),
+        _named("cylinder", [-0.35, 0.35, 0.0], "CdSeQD", radius=0.12, length=0.3),
+        _named("sphere", [0.38, 0.35, 0.0], "Si", radius=0.13),
+        _named("hemisphere", [0.0, -0.45, 0.0], "w", radius=0.12),
+    ]
+    return _bin_planes(cfg, [("Ex", (1.5, 1.5, 0.0)), ("Ey", (0.0, 1.5, 1.5))])
+
+
+def _named_2d():
+    """2-D TMz: Rakic Ag and Al, JM Au and Sn, the PbS quantum-dot resonance, SiO2; point
+    source, text detectors, flux line, one BIN plane."""
+    cfg = configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=3, nfreq=8)
+    cfg["ObjectList"] = [
+        _named("sphere", [0.0, 0.0, 0.0], "AG", radius=0.35),
+        _named("block", [0.8, 0.6, 0.0], "JM_Au", size=[0.4, 0.3, 0.0]),
+        _named("block", [-0.8, 0.6, 0.0], "al", size=[0.3, 0.5, 0.0]),
+        _named("sphere", [0.7, -0.7, 0.0], "PbSQD", radius=0.2),
+        _named("sphere", [-0.7, -0.7, 0.0], "JM_sn", radius=0.2),
+        _named("block", [0.0, 1.0, 0.0], "SiO2", size=[0.8, 0.2, 0.0]),
+    ]
+    return _bin_planes(cfg, [("Ez", (3.0, 3.0, 0.0))])
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -268,6 +302,8 @@ CASES = {
     "shapes_a": _shapes_a,
     "shapes_b": _shapes_b,
     "shapes_2d": _shapes_2d,
+    "named_3d": _named_3d,
+    "named_2d": _named_2d,
 }
 
 

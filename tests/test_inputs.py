@@ -26,7 +26,7 @@ def _base():
     (lambda c: c["CompCell"].__setitem__("PBC", True), 2),
     (lambda c: c["CompCell"].__setitem__("cplxFields", True), 2),
     (lambda c: c["ObjectList"][0].__setitem__("mu", 2.0), 2),
-    (lambda c: c["ObjectList"][0].__setitem__("material", "Au"), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("material", "Unobtainium"), 1),
     (lambda c: c["ObjectList"][0].__setitem__("shape", "dodecahedron"), 1),
     (lambda c: c["ObjectList"][0].update(shape="cone", radSmall=0.2, radLarge=0.1, height=0.3), 1),
     (lambda c: c["DetectorList"][0].__setitem__("dtc_class", "bmp"), 2),
