@@ -638,8 +638,13 @@ void read_emitter(const JNode& node, Object& o, Inputs& ip) {
         }
     }
     if (basis.empty()) return;
+    // A second emitter object: the reference pools the energy levels of every emitter
+    // object (qeELevs_, parallelInputs.cpp:578) and builds each object's Hamiltonians from
+    // the pooled list (parallelFDTDField.cpp:423), whose diagonal then disagrees with the
+    // ensemble energies, and parallelQE's constructor throws (ML/parallelQE.hpp:220-228).
     if (!ip.emitters.empty())
-        throw UnsupportedError("more than one emitter object (the reference pools their energy levels)");
+        throw InputError("The energy for the weight and the Hamiltonian at index 0 do not match, please fix this error. "
+                         "(a second emitter object: the reference pools the energy levels of all emitter objects)");
     const double eConv = kElementaryCharge * kEps0 * std::pow(kSpeedOfLight / ip.I0, 2) / ip.a;
     EmitterSpec em;
     em.object = static_cast<int>(ip.objects.size());

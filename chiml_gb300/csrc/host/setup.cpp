@@ -1053,8 +1053,8 @@ struct Builder {
         if (tm) P.comp[HX].present = P.comp[HY].present = P.comp[EZ].present = true;
         for (auto& o : objs)
             if (o.orDip && o.gamma.size() > 0 && !D.threeD)
-                throw UnsupportedError("oriented-dipole poles need a 3-D grid (the reference allocates the 2-D "
-                                       "polarisation grids for the other polarisation)");
+                throw UnsupportedError("oriented-dipole poles need a 3-D grid (the reference stops on a grid index "
+                                       "assertion, GRID/parallelGrid.hpp:563, while it builds their 2-D lists)");
         // the reference's list order: TE (Hz, Ex, Ey) then TM (Ez, Hx, Hy)
         // Each component's lists depend only on the material maps and on which components
         // exist, so the components are built concurrently; the first error in the order

@@ -307,6 +307,44 @@ CASES = {
 }
 
 
+def _qe_two_objects():
+    """Two emitter objects (the qe_tm block and a disk of two-level emitters). The reference
+    pools every emitter object's energy levels into one list (qeELevs_) and builds each
+    object's Hamiltonians from it, so the first object's Hamiltonian diagonal no longer
+    matches its ensemble energies and parallelQE's constructor throws."""
+    cfg = _qe_tm()
+    lv = [configs.emitter_level(0.0), configs.emitter_level(2.1)]
+    cfg["ObjectList"].append(configs.emitter_obj("sphere", [0.4, 0.3, 0.0], [(0, 0), (1, 0)], lv, [1e5] * 4,
+                                                 [(1, 0, 1e12, 2e13)], 1e21, eps=1.2, dtc_levs=[3],
+                                                 output_pol="out/qe2_pol.dat", radius=0.15))
+    return cfg
+
+
+def _ordip_2d(pol):
+    """A 2-D disk with one unidirectional (oriented-dipole) pole; the reference stops on a
+    grid index assertion while it builds the oriented-dipole lists in 2-D."""
+    def make():
+        cfg = configs.config1(n=60, pml=8, steps=200, radius_cells=8, src_gap_cells=6, ndtc=2, nfreq=4)
+        cfg["CompCell"]["pol"] = pol
+        if pol == "Hz":
+            cfg["SourceList"][0]["pol"] = "Ey"
+            for d in cfg["DetectorList"]:
+                d["type"] = "Ey"
+        cfg["ObjectList"][0]["pols"] = [{"gamma": 0.01, "omega": 5.0 * configs.A / 550e-9, "sigma_p": 1.5,
+                                         "dipOrE": "unidirectional", "dirDipE": [0.6, 0.8, 0.0]}]
+        return cfg
+    return make
+
+
+# Inputs the reference build does not finish: <case>/ref_error.txt keeps the last line it
+# printed, and the engine must reject the input instead of running it.
+FAILING = {
+    "qe_two_objects": _qe_two_objects,
+    "ordip_2d_tm": _ordip_2d("Ez"),
+    "ordip_2d_te": _ordip_2d("Hz"),
+}
+
+
 def main(names=None):
     ref = os.path.join(ROOT, "oracle", "_ref", "chiml_ref")
     if not os.path.exists(ref):
@@ -333,6 +371,24 @@ def main(names=None):
                     os.makedirs(os.path.dirname(dst), exist_ok=True)
                     shutil.copy(src, dst)
         print(name, "ok")
+    for name, make in FAILING.items():
+        if names and name not in names:
+            continue
+        case = os.path.join(HERE, name)
+        shutil.rmtree(case, ignore_errors=True)
+        os.makedirs(case)
+        configs.write_json(make(), os.path.join(case, "in.json"))
+        with tempfile.TemporaryDirectory() as tmp:
+            shutil.copy(os.path.join(case, "in.json"), os.path.join(tmp, "in.json"))
+            r = subprocess.run([ref, "in.json"], cwd=tmp, capture_output=True, text=True)
+            if r.returncode == 0:
+                raise SystemExit("%s: the reference finished; it is expected to fail" % name)
+            last = (r.stderr.strip().splitlines() or ["exit status %d" % r.returncode])[-1]
+            # the reference's own source path in an assertion message is not part of the record
+            last = last.replace(os.path.join(os.environ.get("CHIML_REF_SRC", ""), ""), "")
+            with open(os.path.join(case, "ref_error.txt"), "w") as f:
+                f.write("exit status %d\n%s\n" % (r.returncode, last))
+        print(name, "fails in the reference, as expected")
 
 
 if __name__ == "__main__":

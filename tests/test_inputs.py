@@ -60,3 +60,17 @@ def test_step_count_is_ceil_of_tlim_over_dt(built_oracle, tmp_path):
     cfg["CompCell"]["tLim"] = 10.2 * cfg["CompCell"]["dt"]
     p = configs.write_json(cfg, str(tmp_path / "in.json"))
     assert oracle.OracleSim(p).steps_total == 11
+
+
+def _reference_failures():
+    return sorted(d for d in os.listdir(GOLDEN) if os.path.exists(os.path.join(GOLDEN, d, "ref_error.txt")))
+
+
+@pytest.mark.parametrize("case", _reference_failures())
+def test_inputs_the_reference_cannot_run_are_rejected(built_engine, case):
+    """The reference build stops on these inputs (its last message is in ref_error.txt): the
+    engine rejects them at chiml_create instead of running them."""
+    from chiml_gb300 import ChimlError, Simulation
+    with pytest.raises(ChimlError) as ei:
+        Simulation(os.path.join(GOLDEN, case, "in.json"))
+    assert ei.value.status in (1, 2), str(ei.value)
