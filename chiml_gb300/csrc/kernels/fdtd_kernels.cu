@@ -218,6 +218,14 @@ constexpr int kP3BZ = 8;
 #define CHIML_MARCH_UNROLL 1
 #endif
 constexpr int kMarchUnroll = CHIML_MARCH_UNROLL;  // planes of the march unrolled together
+#ifndef CHIML_P3_CY
+#define CHIML_P3_CY 16
+#endif
+#ifndef CHIML_P3_PD
+#define CHIML_P3_PD 2
+#endif
+constexpr int kP3CY = CHIML_P3_CY;  // planes marched per block
+constexpr int kP3PD = CHIML_P3_PD;  // planes ahead of the march that are prefetched into L2
 
 __device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
 
@@ -277,6 +285,66 @@ template <typename T>
 __device__ __forceinline__ void dispersiveCell(const Pass<T>& p, int ci, uint32_t fl, int obj, T epsInv, long long i, T u,
                                                T add, bool write) {
     p.c[ci].U[i] = dispersiveE<T>(p, ci, fl, obj, epsInv, i, u, add, write);
+}
+
+// The update of one cell of component CI from its loaded values (class code cd, field u,
+// the two curl terms' cell and neighbour values g and n, and in the CPML blocks the slab
+// state of each term): class lookup, curl and CPML terms, the inline dispersive update of
+// the FP32 E pass, and the stores.
+template <typename T, bool EPASS, int CI, typename I, bool PML, bool P0, bool P1>
+__device__ __forceinline__ void cellTail(const Pass<T>& p, I i, uint8_t cd, T u, const T g[2], const T n[2],
+                                         const bool in[2], const T kp[2], const T bq[2], const T cq[2], const T ps[2]) {
+    const Comp<T>& c = p.c[CI];
+    T* __restrict__ U = c.U;
+    T* __restrict__ Dd = c.D;
+    T* __restrict__ psi0 = c.psi[0];
+    T* __restrict__ psi1 = c.psi[1];
+    if (cd == 0) return;
+    if (cd >= c.ncls) {
+        atomicOr(p.err, kErrClassCode);
+        return;
+    }
+    const FastClass<T>* kc = c.fcls + cd;
+    const T coef0 = kc->coef[0], coef1 = kc->coef[1];
+    const uint32_t fl = kc->flags;
+    if (EPASS && !kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) return;  // run by k_pass_lorentz
+    if (((fl & kFcSlab0) && !in[0]) || ((fl & kFcSlab1) && !in[1])) {
+        atomicOr(p.err, kErrSlab);
+        return;
+    }
+    T add = T(0);
+    if (PML) {
+        const T coef[2] = {coef0, coef1};
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            if (!(t == 0 ? P0 : P1)) continue;
+            const T ct = (fl & (t == 0 ? kFcKp0 : kFcKp1)) ? coef[t] + kp[t] : coef[t];
+            const T diff = g[t] - n[t];
+            add += ct * diff;
+            if (fl & (t == 0 ? kFcPsi0 : kFcPsi1)) {
+                const T q = bq[t] * ps[t] + cq[t] * diff;
+                (t == 0 ? psi0 : psi1)[i] = q;
+                add += kc->psiCoef[t] * q;
+            }
+        }
+    } else {
+        if (P0) add += coef0 * (g[0] - n[0]);
+        if (P1) add += coef1 * (g[1] - n[1]);
+    }
+    if (EPASS && kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) {
+        dispersiveCell<T>(p, CI, fl, static_cast<int>(kc->obj), kc->epsInv, i, u, add, (fl & kFcWrite) != 0);
+    } else if (EPASS && (fl & kFcDtoE)) {
+        // D -> E without poles: E = D / eps_inf (the P sum of cellGeneric adds zeros)
+        T d = Dd[i];
+        if (fl & kFcWrite) {
+            d += add;
+            Dd[i] = d;
+        }
+        U[i] = d * kc->epsInv;
+    } else if (fl & kFcWrite) {
+        if (fl & kFcToD) Dd[i] += add;
+        else U[i] = u + add;
+    }
 }
 
 // D2: a 2-D grid (lz == 1), where the term along z is absent.
@@ -382,52 +450,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
             for (int t = 0; t < 2; ++t)
                 if ((t == 0 ? P0 : P1) && c.hasPsi[t] && in[t]) ps[t] = (t == 0 ? psi0 : psi1)[i];
         }
-        if (cd == 0) continue;
-        if (cd >= c.ncls) {
-            atomicOr(p.err, kErrClassCode);
-            continue;
-        }
-        const FastClass<T>* kc = c.fcls + cd;
-        const T coef0 = kc->coef[0], coef1 = kc->coef[1];
-        const uint32_t fl = kc->flags;
-        if (EPASS && !kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) continue;  // run by k_pass_lorentz
-        if (((fl & kFcSlab0) && !in[0]) || ((fl & kFcSlab1) && !in[1])) {
-            atomicOr(p.err, kErrSlab);
-            continue;
-        }
-        T add = T(0);
-        if (PML) {
-            const T coef[2] = {coef0, coef1};
-#pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                if (!(t == 0 ? P0 : P1)) continue;
-                const T ct = (fl & (t == 0 ? kFcKp0 : kFcKp1)) ? coef[t] + kp[t] : coef[t];
-                const T diff = g[t] - n[t];
-                add += ct * diff;
-                if (fl & (t == 0 ? kFcPsi0 : kFcPsi1)) {
-                    const T q = bq[t] * ps[t] + cq[t] * diff;
-                    (t == 0 ? psi0 : psi1)[i] = q;
-                    add += kc->psiCoef[t] * q;
-                }
-            }
-        } else {
-            if (P0) add += coef0 * (g[0] - n[0]);
-            if (P1) add += coef1 * (g[1] - n[1]);
-        }
-        if (EPASS && kInlineDispersive<T> && (fl & (kFcLor | kFcOrDip))) {
-            dispersiveCell<T>(p, CI, fl, static_cast<int>(kc->obj), kc->epsInv, i, u, add, (fl & kFcWrite) != 0);
-        } else if (EPASS && (fl & kFcDtoE)) {
-            // D -> E without poles: E = D / eps_inf (the P sum of cellGeneric adds zeros)
-            T d = Dd[i];
-            if (fl & kFcWrite) {
-                d += add;
-                Dd[i] = d;
-            }
-            U[i] = d * kc->epsInv;
-        } else if (fl & kFcWrite) {
-            if (fl & kFcToD) Dd[i] += add;
-            else U[i] = u + add;
-        }
+        cellTail<T, EPASS, CI, I, PML, P0, P1>(p, i, cd, u, g, n, in, kp, bq, cq, ps);
     }
 }
 
@@ -535,11 +558,8 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     if (ePass && p.od.n > 0)
         k_ordip_pol<T><<<static_cast<unsigned>((p.od.n + 255) / 256), 256, 0, s>>>(p);
     if (p.interior3d) {
-        if (p.index64) {
-            launch_pass3d<T, long long, 16, 2>(p, ePass, s);
-        } else {
-            launch_pass3d<T, int, 16, 2>(p, ePass, s);
-        }
+        if (p.index64) launch_pass3d<T, long long, kP3CY, kP3PD>(p, ePass, s);
+        else launch_pass3d<T, int, kP3CY, kP3PD>(p, ePass, s);
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else if (p.interior2d) {
