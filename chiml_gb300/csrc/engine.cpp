@@ -818,8 +818,44 @@ private:
             std::vector<double2> rho(nstate, make_double2(0.0, 0.0));
             for (int m = 0; m < e.nm; ++m)
                 for (int q = 0; q < e.nc; ++q) rho[static_cast<std::size_t>(m) * n2 * e.nc + q] = make_double2(ep.weight[m], 0.0);
-            e.rho = static_cast<double2*>(mem_.upload(rho));
-            e.kd = mem_.alloc<double2>(4 * nstate);
+            // FP32 fields with the Hermitian form: the split update (float-float state, FP32
+            // histories; emitter_kernels.cu, memberHermSplit); otherwise FP64 state and histories
+            e.split = (sizeof(T) == 4 && e.herm && N >= 2 && N <= 4) ? 1 : 0;
+            if (e.split) {
+                auto pair = [](double v) {
+                    const float hi = static_cast<float>(v);
+                    return std::make_pair(hi, static_cast<float>(v - static_cast<double>(hi)));
+                };
+                std::vector<float4> rf(nstate);
+                for (std::size_t k = 0; k < nstate; ++k) {
+                    const auto re = pair(rho[k].x), im = pair(rho[k].y);
+                    rf[k] = make_float4(re.first, re.second, im.first, im.second);
+                }
+                e.rhoF = mem_.upload(rf);
+                e.kdF = mem_.alloc<float2>(4 * nstate);
+                std::vector<float2> dl(static_cast<std::size_t>(e.nm) * n2, make_float2(0.f, 0.f));
+                for (int m = 0; m < e.nm; ++m)
+                    for (int i = 0; i < N; ++i)
+                        for (int j = 0; j < N; ++j) {
+                            const double d = (ep.h0[static_cast<std::size_t>(m) * N + i] - ep.h0[static_cast<std::size_t>(m) * N + j]) / ep.hbar;
+                            const auto pr = pair(d);
+                            dl[static_cast<std::size_t>(m) * n2 + i + j * N] = make_float2(pr.first, pr.second);
+                        }
+                e.dlevF = mem_.upload(dl);
+                std::vector<float> nmh(3 * n2), gv(val.size());
+                for (int c = 0; c < 3; ++c)
+                    for (int i = 0; i < n2; ++i) nmh[c * n2 + i] = static_cast<float>(ep.negMu[c][i].real() / ep.hbar);
+                for (std::size_t k = 0; k < val.size(); ++k) gv[k] = static_cast<float>(val[k]);
+                e.negMuHF = mem_.upload(nmh);
+                e.gamValF = mem_.upload(gv);
+                for (int k = 0; k < 4; ++k) {
+                    e.abPf[k] = static_cast<float>(e.abP[k]);
+                    e.abCf[k] = static_cast<float>(e.abC[k]);
+                }
+            } else {
+                e.rho = static_cast<double2*>(mem_.upload(rho));
+                e.kd = mem_.alloc<double2>(4 * nstate);
+            }
             e.pBox = ep.pDims[0] * ep.pDims[1] * ep.pDims[2];
             e.P = mem_.alloc<double>(3 * static_cast<std::size_t>(e.pBox));
             std::vector<double> epsBox(e.pBox, 1.0);

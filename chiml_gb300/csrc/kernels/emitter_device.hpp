@@ -55,6 +55,17 @@ struct EmitterDev {
     int nEvents;
     double* totP;                 // [3][nSteps], null when the polarisation is not written
     int nSteps;
+    // Split form of the Hermitian update (FP32 fields): the density matrices as float-float
+    // pairs (hi + lo, a 48-bit significand), the derivative histories in FP32, the level
+    // energy differences (h0_i - h0_j) / hbar as float-float pairs, the coupling and the
+    // relaxation in FP32. Set when the fields are FP32 and the Hermitian form applies.
+    int split;
+    float4* rhoF;                 // [nm * n2 * nc] (re hi, re lo, im hi, im lo), layout as rho
+    float2* kdF;                  // 4 slots of derivatives, layout as kd
+    const float2* dlevF;          // [nm][n2] (h0_i - h0_j) / hbar at element i + j N, hi/lo
+    const float* negMuHF;         // [3][n2] Re(-mu) / hbar
+    const float* gamValF;         // relaxation values (CSR of gamRow / gamCol)
+    float abPf[4], abCf[4];       // ABM4 weights in FP32
 };
 
 // P into E on the (n+1)-box (addP), then one density update of every cell and member

@@ -13,11 +13,16 @@
 //                     of P for the outputs
 //   k_emitter_reduce  fixed-order sum of the block partials (deterministic run to run)
 //
-// All density-matrix arithmetic is FP64 in both precision forms. The four derivative
-// histories rotate through four slots by step number instead of being copied.
+// The FP64 form keeps all density-matrix arithmetic in FP64; with FP32 fields the Hermitian
+// update runs in FP32 with the state as float-float pairs (memberHermSplit). The four
+// derivative histories rotate through four slots by step number instead of being copied.
 #include <cstdint>
 
 #include "emitter_device.hpp"
+
+#ifndef CHIML_EM_SPLIT_MINB
+#define CHIML_EM_SPLIT_MINB 4
+#endif
 
 namespace chiml {
 namespace dev {
@@ -336,8 +341,219 @@ __device__ __forceinline__ void memberHerm(const EmitterDev& e, const double Ec[
     }
 }
 
+// ---- Split form of the Hermitian update ----
+//
+// With FP32 fields the density update runs on the FP32 pipe, which has 64 times the FP64
+// pipe's issue rate on this GPU. Each real of the density matrix is held as a float-float
+// pair (hi + lo with |lo| <= ulp(hi) / 2, a 48-bit significand: Dekker's double-length
+// representation), so that the state loses nothing over 10^5 steps; the four derivative
+// histories are FP32. A step forms each ABM4 increment (a weighted sum of derivatives times
+// dt) in FP32 and adds it to the pair exactly (Knuth's TwoSum, then a renormalising
+// FastTwoSum). The derivative itself, i [H / hbar, rho] + Gamma rho, is evaluated in FP32
+// on rho's hi part, except for its largest and most regular term, the free precession
+// i (h0_i - h0_j) / hbar rho_ij: the level difference is a float-float pair, so that the
+// precession frequency carries no rounding that would add up to a phase drift over a
+// long run. Population outputs are read from the pairs in FP64.
+struct F2 {
+    float x, y;
+};
+
+// hi + lo as an FP64 value
+__device__ __forceinline__ double dfToDouble(float hi, float lo) { return static_cast<double>(hi) + static_cast<double>(lo); }
+
+// (hi, lo) + v exactly, renormalised
+__device__ __forceinline__ void dfAdd(float& hi, float& lo, float v) {
+    const float s = hi + v;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (v - bb);  // TwoSum error of hi + v
+    const float l2 = lo + err;
+    const float h = s + l2;                        // FastTwoSum(s, l2), |s| >= |l2|
+    lo = l2 - (h - s);
+    hi = h;
+}
+
+// Upper-triangle derivative of the split form (the arrangement of den_deriv_herm): HE the
+// coupling -E . mu / hbar (real symmetric, upper triangle, FP32), den the density's hi
+// parts, dl the level differences of this member, cmask the nonzero elements of HE.
+template <int NT>
+__device__ __forceinline__ void den_deriv_split(const EmitterDev& e, const float* HE, const F2* den, const float2* dl,
+                                                F2* out, unsigned cmask) {
+#pragma unroll
+    for (int i = 0; i < NT; ++i) {
+        float sy = 0.f;
+#pragma unroll
+        for (int l = 0; l < NT; ++l)
+            if (l != i && (cmask >> (i + l * NT) & 1u)) {
+                const float h = (i <= l) ? HE[i + l * NT] : HE[l + i * NT];
+                const float dy = (l <= i) ? den[l + i * NT].y : -den[i + l * NT].y;
+                sy = fmaf(h, dy, sy);
+            }
+        out[i + i * NT] = F2{-2.f * sy, 0.f};
+#pragma unroll
+        for (int j = i + 1; j < NT; ++j) {
+            float ox = 0.f, oy = 0.f;
+#pragma unroll
+            for (int l = 0; l < NT; ++l) {
+                if (cmask >> (i + l * NT) & 1u) {
+                    const float h = (i <= l) ? HE[i + l * NT] : HE[l + i * NT];
+                    const F2 d = (l <= j) ? den[l + j * NT] : F2{den[j + l * NT].x, -den[j + l * NT].y};
+                    if (l != j) ox = fmaf(-h, d.y, ox);
+                    oy = fmaf(h, d.x, oy);
+                }
+                if (cmask >> (j + l * NT) & 1u) {
+                    const float h = (j <= l) ? HE[j + l * NT] : HE[l + j * NT];
+                    const F2 d = (l <= i) ? den[l + i * NT] : F2{den[i + l * NT].x, -den[i + l * NT].y};
+                    if (l != i) ox = fmaf(-h, d.y, ox);
+                    oy = fmaf(-h, d.x, oy);
+                }
+            }
+            // free precession i (d_i - d_j) rho_ij with the difference as hi + lo
+            const float2 dd = dl[i + j * NT];
+            const F2 r = den[i + j * NT];
+            ox = ox - fmaf(dd.y, r.y, dd.x * r.y);
+            oy = oy + fmaf(dd.y, r.x, dd.x * r.x);
+            out[i + j * NT] = F2{ox, oy};
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < NT * NT; ++ii) {
+        if ((ii % NT) > (ii / NT)) continue;
+        for (int p = e.gamRow[ii]; p < e.gamRow[ii + 1]; ++p) {
+            const int k = e.gamCol[p];
+            const int r = k % NT, c = k / NT;
+            const bool lower = r > c;
+            const int ku = lower ? c + r * NT : k;
+            F2 d = den[0];
+#pragma unroll
+            for (int t = 1; t < NT * NT; ++t)
+                if ((t % NT) <= (t / NT) && ku == t) d = den[t];
+            if (lower) d.y = -d.y;
+            const float g = e.gamValF[p];
+            out[ii] = F2{fmaf(d.x, g, out[ii].x), (ii % NT) == (ii / NT) ? 0.f : fmaf(d.y, g, out[ii].y)};
+        }
+    }
+}
+
+// One ensemble member of one cell in the split form (the upper triangle, as memberHerm).
+template <int NT>
+__device__ __forceinline__ void memberHermSplit(const EmitterDev& e, const float* HE, int m, long long base,
+                                                const float2* __restrict__ k0, const float2* __restrict__ k1,
+                                                const float2* __restrict__ k2, float2* __restrict__ k3, bool popStep,
+                                                double* Pc, unsigned cmask) {
+    constexpr int N2 = NT * NT;
+    const float c55 = e.abPf[0], cm59 = e.abPf[1], c37 = e.abPf[2], cm9 = e.abPf[3];
+    const float c9 = e.abCf[0], c19 = e.abCf[1], cm5 = e.abCf[2], c1 = e.abCf[3];
+    const float2* dl = e.dlevF + m * N2;
+    float4 r0[N2];  // the state (hi, lo pairs)
+    F2 a[N2], b[N2];
+    // predictor: rho + increment, in FP32 on the hi parts (the derivative's input)
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) {
+                const float2 rr = *reinterpret_cast<const float2*>(&e.rhoF[o]);
+                float inc = c55 * reinterpret_cast<const float*>(k0)[2 * o];
+                inc = fmaf(cm59, reinterpret_cast<const float*>(k1)[2 * o], inc);
+                inc = fmaf(c37, reinterpret_cast<const float*>(k2)[2 * o], inc);
+                inc = fmaf(cm9, reinterpret_cast<const float*>(k3)[2 * o], inc);
+                r0[i] = make_float4(rr.x, rr.y, 0.f, 0.f);
+                a[i] = F2{rr.x + inc, 0.f};
+            } else {
+                const float4 rr = e.rhoF[o];
+                const float2 x0 = k0[o], x1 = k1[o], x2 = k2[o], x3 = k3[o];
+                float ix = c55 * x0.x, iy = c55 * x0.y;
+                ix = fmaf(cm59, x1.x, ix);
+                iy = fmaf(cm59, x1.y, iy);
+                ix = fmaf(c37, x2.x, ix);
+                iy = fmaf(c37, x2.y, iy);
+                ix = fmaf(cm9, x3.x, ix);
+                iy = fmaf(cm9, x3.y, iy);
+                r0[i] = rr;
+                a[i] = F2{rr.x + ix, rr.z + iy};
+            }
+        }
+    den_deriv_split<NT>(e, HE, a, dl, b, cmask);
+    // corrector: rho + increment exactly into the pairs
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) {
+                float inc = c9 * b[i].x;
+                inc = fmaf(c19, reinterpret_cast<const float*>(k0)[2 * o], inc);
+                inc = fmaf(cm5, reinterpret_cast<const float*>(k1)[2 * o], inc);
+                inc = fmaf(c1, reinterpret_cast<const float*>(k2)[2 * o], inc);
+                float hi = r0[i].x, lo = r0[i].y;
+                dfAdd(hi, lo, inc);
+                r0[i] = make_float4(hi, lo, 0.f, 0.f);
+                *reinterpret_cast<float2*>(&e.rhoF[o]) = make_float2(hi, lo);
+                a[i] = F2{hi, 0.f};
+            } else {
+                const float2 x0 = k0[o], x1 = k1[o], x2 = k2[o];
+                float ix = c9 * b[i].x, iy = c9 * b[i].y;
+                ix = fmaf(c19, x0.x, ix);
+                iy = fmaf(c19, x0.y, iy);
+                ix = fmaf(cm5, x1.x, ix);
+                iy = fmaf(cm5, x1.y, iy);
+                ix = fmaf(c1, x2.x, ix);
+                iy = fmaf(c1, x2.y, iy);
+                float4 v = r0[i];
+                dfAdd(v.x, v.y, ix);
+                dfAdd(v.z, v.w, iy);
+                r0[i] = v;
+                e.rhoF[o] = v;
+                a[i] = F2{v.x, v.z};
+            }
+        }
+    den_deriv_split<NT>(e, HE, a, dl, b, cmask);  // derivative at the new density: the next k_n
+#pragma unroll
+    for (int c = 0; c < NT; ++c)
+#pragma unroll
+        for (int r = 0; r <= c; ++r) {
+            const int i = r + c * NT;
+            const long long o = base + static_cast<long long>(i) * e.nc;
+            if (r == c) reinterpret_cast<float*>(k3)[2 * o] = b[i].x;
+            else k3[o] = make_float2(b[i].x, b[i].y);
+        }
+    if (popStep)
+#pragma unroll
+        for (int d = 0; d < kMaxDtc; ++d)
+            if (d < e.nDtc) {
+                const int k = e.dtcLev[d];
+                const int r = k % NT, c = k / NT;
+                const bool lower = r > c;
+                const int ku = lower ? c + r * NT : k;
+                float4 v = r0[0];
+#pragma unroll
+                for (int t = 1; t < N2; ++t)
+                    if ((t % NT) <= (t / NT) && ku == t) v = r0[t];
+                const double im = dfToDouble(v.z, v.w);
+                addPop(d, dfToDouble(v.x, v.y), lower ? -im : im);
+            }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        // Re(conj(a) . mu) with mu real, over the elements hmask marks
+        if (!e.comp[c] || !e.addMu[c]) continue;
+        float sdot = 0.f;
+#pragma unroll
+        for (int i = 0; i < N2; ++i)
+            if (e.hmask >> i & 1u) {
+                const int r = i % NT, cc = i / NT;
+                const float ax = r <= cc ? a[i].x : a[cc + r * NT].x;
+                sdot = fmaf(ax, static_cast<float>(e.mu[c * N2 + i].x), sdot);
+            }
+        Pc[c] += e.na * static_cast<double>(sdot);
+    }
+}
+
 // Block `blk` of the density update (cells kEmThreads * blk ...), writing partial row blk.
-template <typename T, int NT, bool HERM = false>
+// SPLIT: the split form of the Hermitian update (T = float, memberHermSplit).
+template <typename T, int NT, bool HERM = false, bool SPLIT = false>
 __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __restrict__ Ex, const T* __restrict__ Ey,
                                             const T* __restrict__ Ez, const int* __restrict__ stepPtr, int blk) {
     constexpr int MAXN2 = (NT ? NT * NT : kMaxEmitterLevels * kMaxEmitterLevels);
@@ -372,7 +588,33 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
         const double2* __restrict__ k1 = e.kd + s1 * slotStride;
         const double2* __restrict__ k2 = e.kd + s2 * slotStride;
         double2* __restrict__ k3 = e.kd + s3 * slotStride;
-        if constexpr (HERM) {
+        if constexpr (HERM && SPLIT) {
+            // the coupling -E . mu / hbar once per cell (it does not depend on the member)
+            constexpr int N2 = NT * NT;
+            float HE[N2];
+            unsigned cmask = 0;
+#pragma unroll
+            for (int i = 0; i < N2; ++i) HE[i] = 0.f;
+            if (!zeroE)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    if (e.addMu[c])
+#pragma unroll
+                        for (int i = 0; i < N2; ++i)
+                            if ((i % NT) <= (i / NT) && (e.hmask >> i & 1u))
+                                HE[i] = fmaf(static_cast<float>(Ec[c]), e.negMuHF[c * N2 + i], HE[i]);
+            // the nonzero couplings, mirrored (HE is symmetric)
+#pragma unroll
+            for (int i = 0; i < N2; ++i)
+                if ((i % NT) <= (i / NT) && HE[i] != 0.f) cmask |= (1u << i) | (1u << ((i / NT) + (i % NT) * NT));
+            const float2* __restrict__ f0 = e.kdF + s0 * slotStride;
+            const float2* __restrict__ f1 = e.kdF + s1 * slotStride;
+            const float2* __restrict__ f2 = e.kdF + s2 * slotStride;
+            float2* __restrict__ f3 = e.kdF + s3 * slotStride;
+            for (int m = 0; m < e.nm; ++m)
+                memberHermSplit<NT>(e, HE, m, static_cast<long long>(m) * n2 * e.nc + q, f0, f1, f2, f3, popStep, Pc,
+                                    cmask);
+        } else if constexpr (HERM) {
             for (int m = 0; m < e.nm; ++m)
                 memberHerm<NT>(e, Ec, zeroE, m, static_cast<long long>(m) * n2 * e.nc + q, k0, k1, k2, k3, popStep,
                                Pc);
@@ -500,11 +742,19 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
     }
 }
 
-template <typename T, int NT, bool HERM = false>
-__global__ void __launch_bounds__(kEmThreads, 1) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
+// Resident blocks per SM the register budget is sized for: the FP64 forms are bound by the
+// FP64 pipe and keep every register; the split form runs on the FP32 pipe and is closer to
+// the memory bound, where more resident cells hide more latency.
+template <bool SPLIT>
+constexpr int emitterMinBlocks() {
+    return SPLIT ? CHIML_EM_SPLIT_MINB : 1;
+}
+
+template <typename T, int NT, bool HERM = false, bool SPLIT = false>
+__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<SPLIT>()) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
                                                                const T* __restrict__ Ey, const T* __restrict__ Ez,
                                                                const int* __restrict__ stepPtr) {
-    updateBlock<T, NT, HERM>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
+    updateBlock<T, NT, HERM, SPLIT>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
 }
 
 // Quantity k of the step's outputs (populations x / y per detector, then total P x, y, z)
@@ -576,12 +826,13 @@ __global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* _
     addpRange(j.e, j.f[0], j.f[1], j.f[2], c, b * 256 + static_cast<int>(threadIdx.x), bpc * 256);
 }
 
+// The Hermitian form of a batch in FP32 fields is the split form (EmitterDev::split).
 template <typename T, int NT, bool HERM = false>
-__global__ void __launch_bounds__(kEmThreads) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
+__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<HERM && sizeof(T) == 4>()) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
                                                                       const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const EmitJob<T>& j = jobs[w.x];
-    updateBlock<T, NT, HERM>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
+    updateBlock<T, NT, HERM, HERM && sizeof(T) == 4>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
 }
 
 template <typename T>
@@ -625,10 +876,12 @@ void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* ste
     dim3 ga(emitter_addp_blocks_per_comp(e), 3);
     k_emitter_addp<T><<<ga, 256, 0, s>>>(e, fields[0], fields[1], fields[2]);
     const int blocks = (e.nc + kEmThreads - 1) / kEmThreads;
+    // the Hermitian form in FP32 fields is the split form (EmitterDev::split)
+    constexpr bool SPLIT = sizeof(T) == 4;
     if (e.herm && e.N >= 2 && e.N <= 4) {
-        if (e.N == 2) k_emitter_update<T, 2, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
-        else if (e.N == 3) k_emitter_update<T, 3, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
-        else k_emitter_update<T, 4, true><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        if (e.N == 2) k_emitter_update<T, 2, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        else if (e.N == 3) k_emitter_update<T, 3, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        else k_emitter_update<T, 4, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
     } else switch (e.N) {
         case 2: k_emitter_update<T, 2><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
         case 3: k_emitter_update<T, 3><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
