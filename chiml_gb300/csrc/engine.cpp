@@ -158,28 +158,21 @@ public:
         ck(cudaStreamSynchronize(stream_), "DFT flush");
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
             const int nt = stepsDone_ / P.fluxes[q].spec.timeInt + 1;
-            R.fluxFaces.push_back(fluxFacesOnDevice(q, nt));
             R.fluxRe.emplace_back();
             R.fluxIm.emplace_back();
+            if (P.fluxes[q].spec.save || P.fluxes[q].spec.load) {
+                // saving or loading the face grids: combine and integrate on the host from
+                // the accumulators (write_fluxes), which the grids are made from
+                R.fluxFaces.emplace_back();
+                downloadDft(q, P.fluxes[q].spec.freqList.size(), R.fluxRe.back(), R.fluxIm.back());
+            } else {
+                R.fluxFaces.push_back(fluxFacesOnDevice(q, nt));
+            }
             R.fluxSamples.push_back(nt);
         }
         for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
-            const dev::DftTable<T>& d = dft_[P.fluxes.size() + k];
-            const std::size_t nf = P.freqDetectors[k].spec.freqList.size();
-            const std::size_t n = static_cast<std::size_t>(d.npts) * nf;
-            std::vector<double> dre(n), dim(n), re(n), im(n);
-            if (n) {
-                ck(cudaMemcpy(dre.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
-                ck(cudaMemcpy(dim.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H frequency detector");
-            }
-            // back to the plan's point order
-            const std::vector<int>& pos = dftPos_[P.fluxes.size() + k];
-            for (std::size_t p = 0; p < pos.size(); ++p)
-                for (std::size_t f = 0; f < nf; ++f) {
-                    re[p * nf + f] = dre[static_cast<std::size_t>(pos[p]) * nf + f];
-                    im[p * nf + f] = dim[static_cast<std::size_t>(pos[p]) * nf + f];
-                }
-            d2h_ += 2.0 * n * sizeof(double);
+            std::vector<double> re, im;
+            downloadDft(P.fluxes.size() + k, P.freqDetectors[k].spec.freqList.size(), re, im);
             R.freqRe.push_back(std::move(re));
             R.freqIm.push_back(std::move(im));
             R.freqSamples.push_back(stepsDone_ / P.freqDetectors[k].timeInt + 1);
@@ -229,6 +222,26 @@ public:
         write_freq_detectors(P, R, outDir_);
         write_emitters(P, R, outDir_);
         finalized_ = true;
+    }
+
+    // The accumulators of DFT table q (nf frequencies) in the plan's point order, [point][freq].
+    void downloadDft(std::size_t q, std::size_t nf, std::vector<double>& re, std::vector<double>& im) {
+        const dev::DftTable<T>& d = dft_[q];
+        const std::size_t n = static_cast<std::size_t>(d.npts) * nf;
+        std::vector<double> dre(n), dim(n);
+        re.assign(n, 0.0);
+        im.assign(n, 0.0);
+        if (n) {
+            ck(cudaMemcpy(dre.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H DFT accumulators");
+            ck(cudaMemcpy(dim.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H DFT accumulators");
+        }
+        const std::vector<int>& pos = dftPos_[q];
+        for (std::size_t p = 0; p < pos.size(); ++p)
+            for (std::size_t f = 0; f < nf; ++f) {
+                re[p * nf + f] = dre[static_cast<std::size_t>(pos[p]) * nf + f];
+                im[p * nf + f] = dim[static_cast<std::size_t>(pos[p]) * nf + f];
+            }
+        d2h_ += 2.0 * n * sizeof(double);
     }
 
     // The integrated flux of every face of flux q, [freq * nFaces + face], evaluated from the

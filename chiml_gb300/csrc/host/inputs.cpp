@@ -970,7 +970,9 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
         f.incdFile = fn.get<std::string>("incd_fileds", "");
         f.save = fn.get<bool>("save", false);
         f.load = fn.get<bool>("load", false);
-        if (f.load) throw UnsupportedError("loading saved flux fields is not supported by this build");
+        if (f.load && f.incdFile == "")
+            throw InputError("Trying to load in file without a valid path, in the " + std::to_string(ip.fluxes.size()) +
+                             " flux detector");
         ip.fluxes.push_back(f);
     }
     return ip;

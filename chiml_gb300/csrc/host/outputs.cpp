@@ -286,7 +286,8 @@ std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
 }
 
 std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps,
-                                   const std::vector<double>& re, const std::vector<double>& im, int nt) {
+                                   const std::vector<double>& re, const std::vector<double>& im, int nt,
+                                   const FluxGrids* seed, FluxGrids* grids) {
     const FluxPlan& fp = P.fluxes[q];
     const int nfreq = static_cast<int>(fp.spec.freqList.size());
     const std::size_t nFaces = maps.size();
@@ -299,7 +300,8 @@ std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vect
         std::vector<cx> g[4];
         for (int w = 0; w < 4; ++w) {
             if (!m.has[w]) continue;
-            g[w].assign(static_cast<std::size_t>(npt) * nfreq, cx(0.0, 0.0));
+            if (seed) g[w] = (*seed)[vv][w];  // the grid starts from the loaded field (loadFields)
+            else g[w].assign(static_cast<std::size_t>(npt) * nfreq, cx(0.0, 0.0));
 #pragma omp parallel for schedule(static)
             for (long long c = 0; c < npt; ++c)
                 for (long long k = m.start[w][c]; k < m.start[w][c + 1]; ++k) {
@@ -307,6 +309,10 @@ std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vect
                     for (int fq = 0; fq < nfreq; ++fq)
                         g[w][static_cast<std::size_t>(c) * nfreq + fq] += m.scale[w][k] * cx(re[b + fq], im[b + fq]);
                 }
+        }
+        if (grids) {
+            if (grids->size() < nFaces) grids->resize(nFaces);
+            for (int w = 0; w < 4; ++w) (*grids)[vv][w] = g[w];
         }
         const cx* Ej = m.has[0] ? g[0].data() : nullptr;
         const cx* Ek = m.has[1] ? g[1].data() : nullptr;
@@ -336,13 +342,94 @@ std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vect
     return out;
 }
 
+namespace {
+
+// n_vec of a face grid as the reference's Grid holds it: {nfreq, transCor1 points, cor points}
+std::array<int, 3> flux_grid_dims(int nfreq, const FluxFaceMap& m) { return {nfreq, m.ny, m.nx}; }
+
+}  // namespace
+
+void write_flux_fields(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps, const FluxGrids& grids,
+                       const std::string& path) {
+    const FluxPlan& fp = P.fluxes[q];
+    const int nfreq = static_cast<int>(fp.spec.freqList.size());
+    for (std::size_t vv = 0; vv < maps.size(); ++vv)
+        for (int w = 0; w < 4; ++w)
+            if (!maps[vv].has[w])
+                throw UnsupportedError("saving the fields of a flux face without all four field grids (the reference "
+                                       "dereferences the missing grid)");
+    std::ofstream f(path, std::ios::binary | std::ios::out);
+    if (!f) throw InputError("cannot open flux fields output " + path);
+    auto put = [&](int v) { f.write(reinterpret_cast<const char*>(&v), sizeof(v)); };
+    put(nfreq);
+    for (int k = 0; k < 3; ++k) put(fp.spec.sz[k]);
+    const int nFaces = static_cast<int>(maps.size());
+    for (int w = 0; w < 4; ++w) put(nFaces);
+    for (int w = 0; w < 4; ++w)
+        for (std::size_t vv = 0; vv < maps.size(); ++vv) {
+            const std::array<int, 3> n = flux_grid_dims(nfreq, maps[vv]);
+            for (int k = 0; k < 3; ++k) put(n[k]);
+            const std::vector<cplx>& g = grids[vv][w];
+            f.write(reinterpret_cast<const char*>(g.data()), static_cast<std::streamsize>(g.size() * sizeof(cplx)));
+        }
+}
+
+FluxGrids read_flux_fields(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps, const std::string& path,
+                           double weight) {
+    const FluxPlan& fp = P.fluxes[q];
+    const int nfreq = static_cast<int>(fp.spec.freqList.size());
+    std::ifstream f(path, std::ios::binary | std::ios::in);
+    if (!f) throw InputError("cannot open the flux fields file " + path);
+    auto get = [&]() {
+        int v = 0;
+        if (!f.read(reinterpret_cast<char*>(&v), sizeof(v))) throw InputError("flux fields file " + path + " is truncated");
+        return v;
+    };
+    const int nf = get(), nx = get(), ny = get(), nz = get();
+    int counts[4];
+    for (int w = 0; w < 4; ++w) counts[w] = get();
+    if (nf != nfreq || nx != fp.spec.sz[0] || ny != fp.spec.sz[1] || nz != fp.spec.sz[2])
+        throw InputError("Given incident fields do not match size and frequency numbers for the current calculations");
+    for (int w = 0; w < 4; ++w)
+        if (counts[w] != static_cast<int>(maps.size()))
+            throw InputError("The size of the field vectors of the saved fields are not the same as those in the current calculation");
+    FluxGrids g(maps.size());
+    static const char* names[4] = {"Ej_freq_", "Ek_freq_", "Hj_freq_", "Hk_freq_"};
+    for (int w = 0; w < 4; ++w)
+        for (std::size_t vv = 0; vv < maps.size(); ++vv) {
+            const std::array<int, 3> n = flux_grid_dims(nfreq, maps[vv]);
+            for (int k = 0; k < 3; ++k)
+                if (get() != n[k])
+                    throw InputError(std::string("When loading in a ") + names[w] +
+                                     " field in a flux region, one of the size elements did not agree with the file.");
+            std::vector<cplx>& v = g[vv][w];
+            v.assign(static_cast<std::size_t>(n[0]) * n[1] * n[2], cplx(0.0, 0.0));
+            if (!f.read(reinterpret_cast<char*>(v.data()), static_cast<std::streamsize>(v.size() * sizeof(cplx))))
+                throw InputError("flux fields file " + path + " is truncated");
+            for (cplx& x : v) x *= weight;
+            if (!maps[vv].has[w]) v.clear();
+        }
+    return g;
+}
+
 void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) {
     for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
         const FluxPlan& fp = P.fluxes[q];
         const int nfreq = static_cast<int>(fp.spec.freqList.size());
         const std::size_t nFaces = fp.faces.size();
         std::vector<cplx> faceVal;
-        if (q < R.fluxFaces.size() && !R.fluxFaces[q].empty()) {
+        FluxGrids saved;
+        if (fp.spec.save || fp.spec.load) {
+            // the face grids start from minus the loaded incident field (parallelFlux.cpp:69-70,
+            // loadFields(-1.0)) and are written after the flux (parallelFlux.hpp:535-536)
+            if (q >= R.fluxRe.size() || R.fluxRe[q].empty())
+                throw std::logic_error("flux save or load needs the accumulators on the host");
+            const std::vector<FluxFaceMap> maps = flux_face_maps(P, q);
+            FluxGrids seed;
+            if (fp.spec.load) seed = read_flux_fields(P, q, maps, out_path(outDir, fp.spec.incdFile), -1.0);
+            faceVal = flux_face_values(P, q, maps, R.fluxRe[q], R.fluxIm[q], R.fluxSamples[q], fp.spec.load ? &seed : nullptr,
+                                       fp.spec.save ? &saved : nullptr);
+        } else if (q < R.fluxFaces.size() && !R.fluxFaces[q].empty()) {
             faceVal = R.fluxFaces[q];
         } else {
             faceVal = flux_face_values(P, q, flux_face_maps(P, q), R.fluxRe[q], R.fluxIm[q], R.fluxSamples[q]);
@@ -402,6 +489,8 @@ void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir) 
             else
                 f << std::endl;
         }
+        f.close();
+        if (fp.spec.save) write_flux_fields(P, q, flux_face_maps(P, q), saved, out_path(outDir, fp.spec.name + "_fields.dat"));
     }
 }
 

@@ -2,6 +2,7 @@
 // written in chiML's formats.
 #pragma once
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -63,10 +64,26 @@ std::vector<double> simps_weights(int n, double d);
 // The maps of the faces of flux q. Throws where the reference's combination or integration
 // would fail.
 std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q);
+// The four combined frequency-domain grids of each face of a flux, [face][Ej, Ek, Hj, Hk],
+// each [point][freq] in the reference's Grid order (frequency fastest, then the face's cor
+// axis, then transCor1); a grid the face does not have is empty.
+typedef std::vector<std::array<std::vector<cplx>, 4>> FluxGrids;
 // The integrated flux of every face of flux q from its accumulators, [freq * nFaces + face],
-// in the reference's arithmetic.
+// in the reference's arithmetic. With `seed`, each grid starts from the seed's values instead
+// of zero (a loaded incident field, negated); with `grids`, the combined grids are kept.
 std::vector<cplx> flux_face_values(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps,
-                                   const std::vector<double>& re, const std::vector<double>& im, int nt);
+                                   const std::vector<double>& re, const std::vector<double>& im, int nt,
+                                   const FluxGrids* seed = nullptr, FluxGrids* grids = nullptr);
+// The flux fields file of parallelFluxDTC::saveFields / loadFields (parallelFlux.hpp:616-720):
+// int nfreq, the flux region's size (3 ints), the number of faces for each of Ej, Ek, Hj, Hk
+// (4 ints), then every face's Ej grid, every face's Ek, Hj and Hk grids, each as its size
+// (3 ints: nfreq, points along transCor1, along cor) and its complex values.
+void write_flux_fields(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps, const FluxGrids& grids,
+                       const std::string& path);
+// Reads such a file, checks it against flux q as loadFields does, and returns its grids
+// scaled by `weight` (the reference loads with -1).
+FluxGrids read_flux_fields(const Plan& P, std::size_t q, const std::vector<FluxFaceMap>& maps, const std::string& path,
+                           double weight);
 // Writes "<name>.dat" of every flux (parallelFlux.hpp:325-560) from R.fluxFaces, or from the
 // accumulators where those are absent.
 void write_fluxes(const Plan& P, const RunRecord& R, const std::string& outDir);

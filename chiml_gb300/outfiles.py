@@ -14,7 +14,9 @@ The files and their column layouts (what is a coordinate and what is data):
   ``#x y z ...`` with three coordinate columns before the triples;
 * emitter populations (`ML/QEPopDtc.cpp:37-61`): headerless rows t, re, im, abs;
 * emitter polarisation (`ML/parallelQE.cpp:520-557`): headerless rows t, then Px, Py and/or
-  Pz and |P|.
+  Pz and |P|;
+* saved flux fields (`DTC/parallelFlux.hpp:616-660`, `<flux>_fields.dat`): integers (sizes)
+  that must agree exactly, and one complex grid per face and field, each a data group.
 
 The comparison leaves coordinates out of the error (they must agree, or the files do not
 describe the same samples) and takes the relative L2 error of every data group on its own:
@@ -30,11 +32,35 @@ import numpy as np
 COORD_TOL = 1e-9  # coordinate columns (time, x/y/z, frequency) must agree to this relative L2
 
 
+def read_flux_fields(raw):
+    """(ints, [complex grids]) of a flux fields file (parallelFluxDTC::saveFields,
+    DTC/parallelFlux.hpp:616-660): int nfreq and the flux size (4 ints), the number of faces of
+    each of Ej, Ek, Hj, Hk (4 ints), then per grid its 3-int size and its complex values."""
+    head = np.frombuffer(raw[:32], dtype=np.int32)
+    ints = list(head)
+    grids = []
+    pos = 32
+    for _ in range(int(head[4:8].sum())):
+        n = np.frombuffer(raw[pos:pos + 12], dtype=np.int32)
+        ints.extend(int(v) for v in n)
+        pos += 12
+        cnt = int(np.prod(n))
+        grids.append(np.frombuffer(raw[pos:pos + 16 * cnt], dtype=np.complex128))
+        pos += 16 * cnt
+    if pos != len(raw):
+        raise ValueError("flux fields file of unexpected length")
+    return np.array(ints, dtype=np.int64), grids
+
+
 def read_output(path):
     """Returns (kind, header, values): kind "txt" with the header line (None for headerless
-    files) and the rows of a text file as a 2-D array; or kind "bin" with the six-int header
-    and the FP64 payload of a binary detector."""
+    files) and the rows of a text file as a 2-D array; kind "bin" with the six-int header
+    and the FP64 payload of a binary detector; or kind "fields" with the integers and the
+    complex grids of a saved flux fields file."""
     raw = open(path, "rb").read()
+    if path.endswith("_fields.dat"):
+        ints, grids = read_flux_fields(raw)
+        return "fields", ints, grids
     try:
         text = raw.decode("ascii")
     except UnicodeDecodeError:
@@ -66,14 +92,17 @@ def read_output(path):
 
 def rel_l2(a, b):
     """||a - b|| / ||a|| (the absolute norm when a is zero)."""
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    dt = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a = np.asarray(a, dtype=dt)
+    b = np.asarray(b, dtype=dt)
     den = np.linalg.norm(a)
     return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
 
 
 def split_columns(kind, header, values):
     """(coordinates, [(group name, data array)]) of one parsed output file."""
+    if kind == "fields":
+        return header.astype(np.float64), [("grid%d" % k, g) for k, g in enumerate(values)]
     if kind == "bin":
         npts = int(np.prod(header[:3])) if header.size >= 3 else 0
         rec = npts + 1
@@ -104,7 +133,11 @@ def column_errors(ref_path, out_path):
     kinds, headers, shapes or coordinate columns differ."""
     ka, ha, a = read_output(ref_path)
     kb, hb, b = read_output(out_path)
-    if ka != kb or a.shape != b.shape:
+    if ka == "fields" and kb == "fields":
+        if not np.array_equal(ha, hb) or len(a) != len(b):
+            raise ValueError("%s: flux fields header or grid sizes differ" % out_path)
+        return {"grid%d" % k: rel_l2(x, y) for k, (x, y) in enumerate(zip(a, b))}
+    if ka != kb or getattr(a, "shape", None) != getattr(b, "shape", None):
         raise ValueError("%s: kind or shape differ (%s vs %s)" % (out_path, a.shape, b.shape))
     if ka == "bin" and not np.array_equal(ha, hb):
         raise ValueError("%s: binary header differs" % out_path)

@@ -304,6 +304,8 @@ CASES = {
     "shapes_2d": _shapes_2d,
     "named_3d": _named_3d,
     "named_2d": _named_2d,
+    "flux_save": lambda: _flux_scene(save=True),
+    "flux_load": lambda: _flux_scene(load="incident_fields.dat"),
 }
 
 
@@ -336,6 +338,30 @@ def _ordip_2d(pol):
     return make
 
 
+def _flux_scene(objects=True, save=False, load=None):
+    """3-D: a dielectric sphere (eps 2.5) in a 30^3 cell, an Ex plane source below it, a flux
+    box around it; optionally saving the flux fields, or loading incident fields."""
+    cfg = configs.config2(n=30, pml=5, steps=160, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    width = 0.3e-15 / configs.T_UNIT
+    cfg["SourceList"][0]["PulseList"] = [configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)]
+    cfg["ObjectList"] = [configs._obj("sphere", [0.0, 0.0, 0.0], radius=0.15, material="custom", eps=2.5, pols=[])] if objects else []
+    fl = cfg["FluxList"][0]
+    if save:
+        fl["save"] = True
+    if load:
+        fl["load"] = True
+        fl["incd_fileds"] = load
+    return cfg
+
+
+# Files a case needs beside its input, made by a reference run of another input: the
+# case's inputs/ directory holds them, and runs of the case start with them in their
+# working (output) directory.
+INPUT_FILES = {
+    "flux_load": ("incident_fields.dat", lambda: _flux_scene(objects=False, save=True), "out/c2_flux_fields.dat"),
+}
+
+
 # Inputs the reference build does not finish: <case>/ref_error.txt keeps the last line it
 # printed, and the engine must reject the input instead of running it.
 FAILING = {
@@ -356,8 +382,21 @@ def main(names=None):
         shutil.rmtree(case, ignore_errors=True)
         os.makedirs(case)
         configs.write_json(make(), os.path.join(case, "in.json"))
+        staged = []
+        if name in INPUT_FILES:
+            fname, make_src, produced = INPUT_FILES[name]
+            with tempfile.TemporaryDirectory() as tmp:
+                configs.write_json(make_src(), os.path.join(tmp, "in.json"))
+                r = subprocess.run([ref, "in.json"], cwd=tmp, capture_output=True, text=True)
+                if r.returncode != 0:
+                    raise SystemExit("%s (input file) failed:\n%s%s" % (name, r.stdout, r.stderr))
+                os.makedirs(os.path.join(case, "inputs"))
+                shutil.copy(os.path.join(tmp, produced), os.path.join(case, "inputs", fname))
+            staged = [fname]
         with tempfile.TemporaryDirectory() as tmp:
             shutil.copy(os.path.join(case, "in.json"), os.path.join(tmp, "in.json"))
+            for fname in staged:
+                shutil.copy(os.path.join(case, "inputs", fname), os.path.join(tmp, fname))
             r = subprocess.run([ref, "in.json"], cwd=tmp, capture_output=True, text=True)
             if r.returncode != 0:
                 raise SystemExit("%s failed:\n%s%s" % (name, r.stdout, r.stderr))
@@ -365,7 +404,7 @@ def main(names=None):
                 for f in files:
                     src = os.path.join(d, f)
                     rel = os.path.relpath(src, tmp)
-                    if rel == "in.json" or f == "levelDist.dat":
+                    if rel == "in.json" or f == "levelDist.dat" or rel in staged:
                         continue
                     dst = os.path.join(case, "ref", rel)
                     os.makedirs(os.path.dirname(dst), exist_ok=True)

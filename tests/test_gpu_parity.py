@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from compare import compare_dirs, rel_l2
-from conftest import GOLDEN, golden_cases
+from conftest import GOLDEN, golden_cases, stage_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -22,6 +22,7 @@ TOL_SPLIT = 1e-4
 
 def _run_gpu(case, out_dir, precision="fp64", graph=0):
     from chiml_gb300 import Simulation
+    stage_inputs(case, out_dir)
     sim = Simulation(os.path.join(GOLDEN, case, "in.json"), precision=precision, steps_per_graph=graph, out_dir=str(out_dir))
     sim.step()
     sim.finalize()

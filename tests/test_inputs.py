@@ -35,6 +35,7 @@ def _base():
     (lambda c: c["CompCell"].__setitem__("pol", "Q"), 1),
     (lambda c: c["ObjectList"][0].pop("Basis_Set"), 1),
     (lambda c: c.pop("FluxList"), 1),
+    (lambda c: c["FluxList"][0].update(load=True), 1),
 ])
 def test_rejections_are_reported_with_status(built_engine, tmp_path, mutate, status):
     cfg = copy.deepcopy(_base())

@@ -105,3 +105,24 @@ def test_relative_errors_and_mismatches(tmp_path):
     (a / "g.dat").write_text("1 2\n")
     with pytest.raises(ValueError):
         relative_errors(str(a), str(b))
+
+
+def test_flux_fields_files_compare_per_grid(tmp_path):
+    """Saved flux fields: the integer header must agree exactly, each complex grid is a group."""
+    def write(path, grids, nf=2):
+        ints = [nf, 3, 3, 3, 1, 1, 1, 1]
+        body = b""
+        for g in grids:
+            body += np.array([nf, 1, len(g) // nf], dtype=np.int32).tobytes() + np.asarray(g, dtype=np.complex128).tobytes()
+        path.write_bytes(np.array(ints, dtype=np.int32).tobytes() + body)
+    g = [np.arange(4) + 1j, np.ones(4) * (2 - 1j), np.arange(4) * 1j, np.ones(4)]
+    write(tmp_path / "a_fields.dat", g)
+    h = [x.copy() for x in g]
+    h[2] = h[2] * (1 + 1e-3)
+    write(tmp_path / "b_fields.dat", h)
+    e = column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "b_fields.dat"))
+    assert list(e) == ["grid0", "grid1", "grid2", "grid3"]
+    assert e["grid0"] == 0.0 and e["grid2"] == pytest.approx(1e-3, rel=1e-6)
+    write(tmp_path / "c_fields.dat", g, nf=1)
+    with pytest.raises(ValueError):
+        column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "c_fields.dat"))
