@@ -60,7 +60,10 @@ def build_engine(force=False):
         o = os.path.join(BUILD, name + ".o")
         jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", cu, "-o", o])
         objs.append(o)
-    cxx = ["g++", "-std=c++17", "-O2", "-fPIC", "-fopenmp", "-I" + os.path.join(CUDA_HOME, "include")]
+    # The host plan (cell classes, shape tests, source cells) is built without contracting
+    # a*b+c into fused multiply-adds, which aarch64 gcc does by default, so that its
+    # inside/outside decisions are the same on x86_64 and aarch64 hosts.
+    cxx = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-fopenmp", "-I" + os.path.join(CUDA_HOME, "include")]
     for f in ["engine.cpp"] + ["host/" + h for h in HOST_SRCS]:
         o = os.path.join(BUILD, os.path.basename(f).replace(".cpp", ".o"))
         jobs.append(cxx + ["-c", os.path.join(CSRC, f), "-o", o])
@@ -78,7 +81,7 @@ def build_oracle(force=False):
     deps = srcs + [os.path.join(CSRC, "host", h) for h in os.listdir(os.path.join(CSRC, "host")) if h.endswith(".hpp")]
     if not force and _newer(LIB_ORACLE, deps):
         return LIB_ORACLE
-    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB_ORACLE] + srcs)
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", "-o", LIB_ORACLE] + srcs)
     return LIB_ORACLE
 
 

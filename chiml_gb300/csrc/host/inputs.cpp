@@ -892,13 +892,12 @@ Inputs read_inputs(const JNode& IP, const std::string& filename) {
         const JNode& sn = kv.second;
         SourceSpec s;
         s.pol = string2pol(sn.get<std::string>("pol"));
-        if (s.pol == Pol::L || s.pol == Pol::R) throw UnsupportedError("circularly polarised soft sources are not supported");
         for (auto& pk : sn.child("PulseList").kids) s.pulses.push_back(read_pulse(pk.second, ip.a, ip.I0));
         std::array<double, 3> tempSz = as_arr3(sn, "size");
         for (int cc = 0; cc < 3; ++cc) s.sz[cc] = find_pt(tempSz[cc], ip.d[cc]) + 1;
+        // "psi" and "ellpiticalKRat" of an L/R source only feed prefactors that its pulses
+        // never read (setup.cpp, buildSources, says why); "theta" is not read.
         s.phi = sn.get<double>("phi", 90);
-        if (static_cast<int>(std::round(s.phi)) % 90 != 0)
-            throw UnsupportedError("oblique soft sources are not supported");
         std::array<double, 3> loc = as_arr3(sn, "loc");
         for (int i = 0; i < 3; ++i) {
             if (loc[i] + tempSz[i] / 2.0 > ip.size[i] / 2.0 || loc[i] - tempSz[i] / 2.0 < -1.0 * ip.size[i] / 2.0)

@@ -1115,10 +1115,27 @@ struct Builder {
         buildFluxes();
     }
 
-    // ---- sources (parallelSourceNormal.hpp:60-150, parallelSourceNormal.cpp:15-37) ----
+    // ---- sources (parallelFDTDField.cpp:455-620) ----
+    // A source along a grid axis (phi a multiple of 90 degrees after rounding) is a normal
+    // source (parallelSourceNormal.cpp:15-37): dt * Re(sum of pulses) on every cell of its
+    // box. Any other phi is an oblique source (parallelSourceOblique.hpp:88-165), whose
+    // cells each add scalefact * Re(sum of pulses at t - t_off) without the factor dt; an
+    // oblique E_x/E_y (H_x/H_y) source acts on both in-plane components. A circularly
+    // polarised source (L/R) is two normal sources on the two E components across the
+    // source's thinnest axis (parallelFDTDField.cpp:548-618): the reference scales each
+    // pulse by its polarisation prefactors and phase in a parameter slot past the one the
+    // pulse functions read (UTIL/PulseFxn.hpp:19-89 read the amplitude at a fixed index), so
+    // both components carry the unscaled pulse.
     void buildSources() {
         for (auto& s : in.sources) {
-            SourcePlan sp;
+            if (s.pol == Pol::L || s.pol == Pol::R) {
+                int amin = 0;  // isamin_: the first axis of the smallest size
+                for (int ii = 1; ii < 3; ++ii)
+                    if (s.sz[ii] < s.sz[amin]) amin = ii;
+                const int pairs[3][2] = {{EY, EZ}, {EX, EZ}, {EX, EY}};
+                for (int c : pairs[amin]) addNormalSource(s, c);
+                continue;
+            }
             int comp = EX;
             switch (s.pol) {
                 case Pol::EX: comp = EX; break;
@@ -1129,33 +1146,129 @@ struct Builder {
                 case Pol::HZ: comp = HZ; break;
                 default: throw UnsupportedError("source polarisation");
             }
-            if (!P.comp[comp].present) throw InputError("a source acts on a field that this polarisation does not have");
-            sp.comp = comp;
-            std::array<int, 3> lloc, lsz = {0, 0, 0};
-            bool inside = true;
+            if (static_cast<int>(std::round(s.phi)) % 90 == 0) {
+                addNormalSource(s, comp);
+            } else if (comp == EX || comp == EY) {
+                addObliqueSource(s, EX);
+                addObliqueSource(s, EY);
+            } else if (comp == HX || comp == HY) {
+                // parallelFDTDField.cpp:523-536 builds the H_y part first for an H_x source
+                addObliqueSource(s, comp == HX ? HY : HX);
+                addObliqueSource(s, comp);
+            } else {
+                addObliqueSource(s, comp);
+            }
+        }
+    }
+
+    // One normal source of component comp: the box of the source (parallelSourceNormal.hpp:60-150).
+    void addNormalSource(const SourceSpec& s, int comp) {
+        if (!P.comp[comp].present) throw InputError("a source acts on a field that this polarisation does not have");
+        SourcePlan sp;
+        sp.comp = comp;
+        std::array<int, 3> lloc, lsz = {0, 0, 0};
+        bool inside = true;
+        for (int ii = 0; ii < 3; ++ii) {
+            int ln = lnv(ii);
+            if (s.loc[ii] >= 0 && s.loc[ii] < ln - 2) lloc[ii] = s.loc[ii] + 1;
+            else if (s.loc[ii] < 0 && s.loc[ii] + s.sz[ii] > 0) lloc[ii] = 1;
+            else lloc[ii] = -1;
+        }
+        if (D.lz == 1) lloc[2] = 0;
+        if (lloc[0] == -1 || lloc[1] == -1 || lloc[2] == -1) inside = false;
+        if (inside) {
             for (int ii = 0; ii < 3; ++ii) {
                 int ln = lnv(ii);
-                if (s.loc[ii] >= 0 && s.loc[ii] < ln - 2) lloc[ii] = s.loc[ii] + 1;
-                else if (s.loc[ii] < 0 && s.loc[ii] + s.sz[ii] > 0) lloc[ii] = 1;
-                else lloc[ii] = -1;
+                lsz[ii] = (s.sz[ii] + s.loc[ii] > ln - 2) ? ln - lloc[ii] - 1 : s.loc[ii] + s.sz[ii] - (lloc[ii] - 1);
             }
-            if (D.lz == 1) lloc[2] = 0;
-            if (lloc[0] == -1 || lloc[1] == -1 || lloc[2] == -1) inside = false;
-            if (inside) {
-                for (int ii = 0; ii < 3; ++ii) {
-                    int ln = lnv(ii);
-                    lsz[ii] = (s.sz[ii] + s.loc[ii] > ln - 2) ? ln - lloc[ii] - 1 : s.loc[ii] + s.sz[ii] - (lloc[ii] - 1);
+            if (D.lz == 1) lsz[2] = 1;
+            for (int z = 0; z < lsz[2]; ++z)
+                for (int y = 0; y < lsz[1]; ++y)
+                    for (int x = 0; x < lsz[0]; ++x) sp.cells.push_back(D.idx(lloc[0] + x, lloc[1] + y, lloc[2] + z));
+        }
+        sp.value.resize(static_cast<std::size_t>(P.nSteps));
+        for (int st = 0; st < P.nSteps; ++st) {
+            cplx v = 0.0;
+            for (auto& pul : s.pulses) v += pul.value(P.tcur[st]);
+            sp.value[st] = dt * std::real(v);
+        }
+        P.sources.push_back(std::move(sp));
+    }
+
+    // One oblique source acting on component comp (parallelSourceOblique.hpp:54-165): the
+    // cells of the box around the source's centre whose offset from it lies within dx/sqrt(2)
+    // of the plane normal to the propagation direction. The reference never reads a polar
+    // angle for soft sources (srcTheta_ stays 90, parallelInputs.cpp:44), so in 3-D the
+    // plane's normal is z and in 2-D (theta forced to 90 degrees) it lies in the xy plane
+    // at phi. Cells with equal (scalefact, t_off) share one time series.
+    void addObliqueSource(const SourceSpec& s, int comp) {
+        if (!P.comp[comp].present) throw InputError("a source acts on a field that this polarisation does not have");
+        const bool twoD = D.lz == 1;
+        const double phiA = std::fmod(s.phi, 360.0) * M_PI / 180.0;
+        double thetaA = std::fmod(90.0, 360.0) * M_PI / 180.0 - M_PI / 2.0;
+        if (twoD) thetaA = M_PI / 2.0;
+        const double phi = std::fmod(phiA + M_PI / 2.0, 2.0 * M_PI);
+        const double theta = (thetaA >= M_PI / 2) ? thetaA - M_PI / 2.0 : thetaA + M_PI / 2.0;
+        double nv[3] = {std::sin(thetaA) * std::cos(phiA), std::sin(thetaA) * std::sin(phiA), std::cos(thetaA)};
+        const double nrm = 1.0 / std::sqrt(std::pow(nv[0], 2.0) + std::pow(nv[1], 2.0) + std::pow(nv[2], 2.0));
+        for (double& v : nv) v *= nrm;
+        const double dx = in.d[0], dy = in.d[1], dz = twoD ? 1.0 : in.d[2];
+        const std::array<int, 3>& loc = s.loc;
+        const std::array<int, 3>& sz = s.sz;
+        auto half = [](double v) { return std::fabs(static_cast<int>(std::round(v / 2.0))); };
+        auto tilt = [](int m, double v) { return static_cast<int>(std::fabs(std::round(m + v))); };
+        int xMin = static_cast<int>(loc[0] - half(sz[0] * std::cos(phi)));
+        xMin = std::min(xMin, tilt(xMin, sz[1] * std::cos(phi) * std::sin(theta)));
+        int yMin = static_cast<int>(loc[1] - half(sz[0] * std::sin(phi)));
+        yMin = std::min(yMin, tilt(yMin, sz[1] * std::sin(phi) * std::sin(theta)));
+        int xMax = static_cast<int>(loc[0] + half(sz[0] * std::cos(phi)));
+        xMax = std::min(xMax, tilt(xMax, sz[1] * std::cos(phi) * std::sin(theta)));
+        int yMax = static_cast<int>(loc[1] + half(sz[0] * std::sin(phi)));
+        yMax = std::min(yMax, tilt(yMax, sz[1] * std::sin(phi) * std::sin(theta)));
+        int zMin = 0, zMax = 0;
+        if (!twoD) {
+            zMin = static_cast<int>(loc[2] - half(sz[1] * std::cos(theta)));
+            zMax = static_cast<int>(loc[2] + half(sz[1] * std::cos(theta)));
+        }
+        double off[3] = {0.0, 0.0, 0.0};
+        if (comp == EX || comp == HY || comp == HZ) off[0] = 0.5;
+        if (comp == HX || comp == EY || comp == HZ) off[1] = 0.5;
+        if (!twoD && (comp == HX || comp == HY || comp == EZ)) off[2] = 0.5;
+        double scale;
+        if (comp == EX || comp == HX) scale = std::cos(phi) * std::sin(thetaA);
+        else if (comp == EY || comp == HY) scale = std::sin(phi) * std::sin(thetaA);
+        else scale = std::cos(thetaA);
+        const double reach = dx / std::sqrt(2.0);
+        std::vector<double> offsets;           // distinct t_off, in the order first met
+        std::vector<std::vector<long long>> cells;
+        for (int xx = xMin; xx <= xMax; ++xx)
+            for (int yy = yMin; yy <= yMax; ++yy)
+                for (int zz = zMin; zz <= zMax; ++zz) {
+                    const double pt[3] = {(xx - loc[0] + off[0]) * dx, (yy - loc[1] + off[1]) * dy, (zz - loc[2] + off[2]) * dz};
+                    double dot = 0.0;  // the summation order of the one-process build's ddot_
+                    for (int k = 0; k < 3; ++k) dot += pt[k] * nv[k];
+                    if (std::fabs(dot) > reach) continue;
+                    if (xx < 0 || xx >= D.nx || yy < 0 || yy >= D.ny || (!twoD && (zz < 0 || zz >= D.nz)))
+                        throw InputError("An oblique source reaches outside the FDTD cell");
+                    double toff = 0.0;
+                    for (int k = 0; k < 3; ++k) toff += nv[k] * pt[k];
+                    std::size_t g = 0;
+                    while (g < offsets.size() && offsets[g] != toff) ++g;
+                    if (g == offsets.size()) {
+                        offsets.push_back(toff);
+                        cells.emplace_back();
+                    }
+                    cells[g].push_back(D.idx(xx + 1, yy + 1, twoD ? 0 : zz + 1));
                 }
-                if (D.lz == 1) lsz[2] = 1;
-                for (int z = 0; z < lsz[2]; ++z)
-                    for (int y = 0; y < lsz[1]; ++y)
-                        for (int x = 0; x < lsz[0]; ++x) sp.cells.push_back(D.idx(lloc[0] + x, lloc[1] + y, lloc[2] + z));
-            }
+        for (std::size_t g = 0; g < offsets.size(); ++g) {
+            SourcePlan sp;
+            sp.comp = comp;
+            sp.cells = std::move(cells[g]);
             sp.value.resize(static_cast<std::size_t>(P.nSteps));
             for (int st = 0; st < P.nSteps; ++st) {
                 cplx v = 0.0;
-                for (auto& pul : s.pulses) v += pul.value(P.tcur[st]);
-                sp.value[st] = dt * std::real(v);
+                for (auto& pul : s.pulses) v += pul.value(P.tcur[st] - offsets[g]);
+                sp.value[st] = scale * std::real(v);
             }
             P.sources.push_back(std::move(sp));
         }

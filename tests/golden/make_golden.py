@@ -283,6 +283,65 @@ def _named_2d():
     return _bin_planes(cfg, [("Ez", (3.0, 3.0, 0.0))])
 
 
+def _src(pol, loc, size, pulse, phi=None, **kw):
+    s = {"pol": pol, "loc": loc, "size": size, "PulseList": [pulse]}
+    if phi is not None:
+        s["phi"] = phi
+    s.update(kw)
+    return s
+
+
+def _src_oblique_2d():
+    """2-D TMz: an Ez line source at phi = 30 degrees (an oblique source: every cell adds the
+    pulse delayed by its distance along the direction of travel) onto the dielectric disk."""
+    cfg = configs.config1(n=72, pml=8, steps=260, radius_cells=7, src_gap_cells=8, ndtc=3, nfreq=8)
+    pulse = cfg["SourceList"][0]["PulseList"][0]
+    cfg["SourceList"] = [_src("Ez", [-0.8, -0.2, 0.0], [1.0, 0.0, 0.0], pulse, phi=30)]
+    return cfg
+
+
+def _src_oblique_te():
+    """2-D TE (Ex, Ey, Hz): an oblique Ey line source at phi = 60 degrees (it acts on Ex and
+    Ey) and an oblique Hz line source at phi = -45 degrees, onto a Drude-Lorentz disk."""
+    cfg = configs.config1(n=72, pml=8, steps=260, radius_cells=7, src_gap_cells=8, ndtc=3, nfreq=8)
+    cfg["CompCell"]["pol"] = "Hz"
+    pulse = cfg["SourceList"][0]["PulseList"][0]
+    cfg["SourceList"] = [_src("Ey", [-0.7, -0.5, 0.0], [0.8, 0.0, 0.0], pulse, phi=60),
+                         _src("Hz", [0.6, 0.7, 0.0], [0.6, 0.0, 0.0], pulse, phi=-45)]
+    cfg["ObjectList"][0]["pols"] = configs.drude_lorentz_pols(4.0, [(1.0, 0.2, 0.0), (0.6, 0.3, 2.4)])
+    for d in cfg["DetectorList"]:
+        d["type"] = "Hz"
+    cfg["DetectorList"].append({"loc": [0.3, -0.4, 0.0], "size": [0.0, 0.0, 0.0], "type": "Ex",
+                                "fname": "out/te_ex", "dtc_class": "txt", "SI": False, "Time_Interval": cfg["CompCell"]["dt"]})
+    return cfg
+
+
+def _src_3d(srcs):
+    cfg = configs.config2(n=30, pml=5, steps=150, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    width = 0.3e-15 / configs.T_UNIT
+    pulse = configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)
+    cfg["SourceList"] = [_src(pol, loc, size, pulse, **kw) for pol, loc, size, kw in srcs]
+    cfg["ObjectList"] = [configs._obj("sphere", [0.05, 0.0, 0.1], radius=0.2, material="custom", eps=2.5,
+                                      pols=configs.drude_lorentz_pols(3.0, [(0.8, 0.3, 2.2)]))]
+    cfg["DetectorList"].append({"loc": [0.2, -0.15, 0.3], "size": [0.0, 0.0, 0.0], "type": "Ez",
+                                "fname": "out/c2_ez", "dtc_class": "txt", "SI": False, "Time_Interval": cfg["CompCell"]["dt"]})
+    return cfg
+
+
+def _src_oblique_3d():
+    """3-D: oblique Ez and Hx sheets (phi = 45 and 120 degrees). The reference reads no polar
+    angle for soft sources, so in 3-D the plane of an oblique source is normal to z."""
+    return _src_3d([("Ez", [0.0, 0.0, -0.4], [0.5, 0.5, 0.0], {"phi": 45}),
+                    ("Hx", [0.1, -0.1, -0.3], [0.4, 0.4, 0.0], {"phi": 120})])
+
+
+def _src_circ_3d():
+    """3-D: a left circularly polarised xy sheet (Ex and Ey) and a right circularly polarised
+    yz sheet (Ey and Ez) with polarisation angles and an axis ratio."""
+    return _src_3d([("L", [0.0, 0.0, -0.4], [0.6, 0.6, 0.0], {"psi": 30.0}),
+                    ("R", [-0.45, 0.0, 0.0], [0.0, 0.5, 0.4], {"psi": 10.0, "ellpiticalKRat": 0.5})])
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -306,6 +365,10 @@ CASES = {
     "named_2d": _named_2d,
     "flux_save": lambda: _flux_scene(save=True),
     "flux_load": lambda: _flux_scene(load="incident_fields.dat"),
+    "src_oblique_2d": _src_oblique_2d,
+    "src_oblique_te": _src_oblique_te,
+    "src_oblique_3d": _src_oblique_3d,
+    "src_circ_3d": _src_circ_3d,
 }
 
 
