@@ -16,7 +16,8 @@ The files and their column layouts (what is a coordinate and what is data):
 * emitter polarisation (`ML/parallelQE.cpp:520-557`): headerless rows t, then Px, Py and/or
   Pz and |P|;
 * saved flux fields (`DTC/parallelFlux.hpp:616-660`, `<flux>_fields.dat`): integers (sizes)
-  that must agree exactly, and one complex grid per face and field, each a data group.
+  that must agree exactly, and one complex grid per face and field (all faces' Ej, then Ek,
+  Hj, Hk); the four grids of a face, from which its flux is formed, are one data group.
 
 The comparison leaves coordinates out of the error (they must agree, or the files do not
 describe the same samples) and takes the relative L2 error of every data group on its own:
@@ -99,10 +100,23 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / den) if den > 0 else float(np.linalg.norm(a - b))
 
 
+def fields_groups(ints, grids):
+    """[(group name, values)] of a flux fields file: per face the concatenation of its Ej, Ek,
+    Hj and Hk grids. A face's flux is Re(Ej Hk* - Ek Hj*) summed over the face, so a grid
+    that is near zero by symmetry (3e-3 next to 1.5 on the same face) counts against its
+    face's field, not against its own size. Files whose four field counts differ are
+    compared per grid."""
+    counts = [int(v) for v in ints[4:8]]
+    n = counts[0]
+    if n == 0 or counts != [n] * 4 or len(grids) != 4 * n:
+        return [("grid%d" % k, g) for k, g in enumerate(grids)]
+    return [("face%d" % f, np.concatenate([grids[f + k * n] for k in range(4)])) for f in range(n)]
+
+
 def split_columns(kind, header, values):
     """(coordinates, [(group name, data array)]) of one parsed output file."""
     if kind == "fields":
-        return header.astype(np.float64), [("grid%d" % k, g) for k, g in enumerate(values)]
+        return header.astype(np.float64), fields_groups(header, values)
     if kind == "bin":
         npts = int(np.prod(header[:3])) if header.size >= 3 else 0
         rec = npts + 1
@@ -136,7 +150,7 @@ def column_errors(ref_path, out_path):
     if ka == "fields" and kb == "fields":
         if not np.array_equal(ha, hb) or len(a) != len(b):
             raise ValueError("%s: flux fields header or grid sizes differ" % out_path)
-        return {"grid%d" % k: rel_l2(x, y) for k, (x, y) in enumerate(zip(a, b))}
+        return {name: rel_l2(x, y) for (name, x), (_, y) in zip(fields_groups(ha, a), fields_groups(hb, b))}
     if ka != kb or getattr(a, "shape", None) != getattr(b, "shape", None):
         raise ValueError("%s: kind or shape differ (%s vs %s)" % (out_path, a.shape, b.shape))
     if ka == "bin" and not np.array_equal(ha, hb):

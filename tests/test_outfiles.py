@@ -107,22 +107,31 @@ def test_relative_errors_and_mismatches(tmp_path):
         relative_errors(str(a), str(b))
 
 
-def test_flux_fields_files_compare_per_grid(tmp_path):
-    """Saved flux fields: the integer header must agree exactly, each complex grid is a group."""
-    def write(path, grids, nf=2):
-        ints = [nf, 3, 3, 3, 1, 1, 1, 1]
+def test_flux_fields_files_compare_per_face(tmp_path):
+    """Saved flux fields: the integer header must agree exactly; the four grids of a face
+    (Ej, Ek, Hj, Hk, stored field by field over all faces) are one group, so an error in a
+    grid that is small next to its face's other grids is weighed against the face."""
+    def write(path, grids, nf=2, faces=2):
+        ints = [nf, 3, 3, 3] + [faces] * 4
         body = b""
         for g in grids:
             body += np.array([nf, 1, len(g) // nf], dtype=np.int32).tobytes() + np.asarray(g, dtype=np.complex128).tobytes()
         path.write_bytes(np.array(ints, dtype=np.int32).tobytes() + body)
-    g = [np.arange(4) + 1j, np.ones(4) * (2 - 1j), np.arange(4) * 1j, np.ones(4)]
+    rng = np.random.default_rng(3)
+    g = [rng.normal(size=4) + 1j * rng.normal(size=4) for _ in range(8)]
+    g[5] = g[5] * 1e-3                      # face 1's Hj: near zero
     write(tmp_path / "a_fields.dat", g)
     h = [x.copy() for x in g]
-    h[2] = h[2] * (1 + 1e-3)
+    h[5] = h[5] * (1 + 1e-2)
     write(tmp_path / "b_fields.dat", h)
     e = column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "b_fields.dat"))
-    assert list(e) == ["grid0", "grid1", "grid2", "grid3"]
-    assert e["grid0"] == 0.0 and e["grid2"] == pytest.approx(1e-3, rel=1e-6)
-    write(tmp_path / "c_fields.dat", g, nf=1)
+    assert list(e) == ["face0", "face1"] and e["face0"] == 0.0
+    face1 = np.concatenate([g[1], g[3], g[5], g[7]])
+    assert e["face1"] == pytest.approx(np.linalg.norm(g[5]) * 1e-2 / np.linalg.norm(face1), rel=1e-6)
+    h[3] = h[3] * (1 + 1e-3)                # a 1e-3 error in face 1's Ek shows as ~1e-3
+    write(tmp_path / "c_fields.dat", h)
+    e = column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "c_fields.dat"))
+    assert 1e-4 < e["face1"] < 1e-3
+    write(tmp_path / "d_fields.dat", g, nf=1)
     with pytest.raises(ValueError):
-        column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "c_fields.dat"))
+        column_errors(str(tmp_path / "a_fields.dat"), str(tmp_path / "d_fields.dat"))
