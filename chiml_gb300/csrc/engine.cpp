@@ -86,6 +86,7 @@ template <typename T>
 class Sim : public SimBase {
 public:
     Sim(Plan&& plan, const chiml_options& opt) : P(std::move(plan)), opt_(opt) {
+        PhaseClock clk;
         ck(cudaSetDevice(opt.device), "cudaSetDevice");
         // A blocking stream: ordered after the uploads and memsets that run on
         // the legacy default stream.
@@ -94,9 +95,12 @@ public:
         // the fixed array of chiml_get_box_noalloc is placed on the device now, before
         // this handle's uploads, so that no read-back has to place it later
         ck(dev::box_noalloc_setup(opt.device), "chiml_get_box_noalloc set-up");
+        clk.mark("device-setup");
         upload();
+        clk.mark("upload");
         // the step graph is captured and instantiated here, so that no step call pays for it
         if (opt_.steps_per_graph > 0 && P.nSteps >= opt_.steps_per_graph) buildGraph(opt_.steps_per_graph);
+        clk.mark("graph");
     }
     ~Sim() override {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -135,6 +139,7 @@ public:
     }
 
     void finalize() override {
+        PhaseClock clk;
         checkDeviceErrors();
         RunRecord R;
         R.detectors.resize(P.detectors.size());
@@ -156,6 +161,7 @@ public:
             dev::launch_dft_flush<T>(d, stepsDone_ / d.timeInt + 1, stream_);
         }
         ck(cudaStreamSynchronize(stream_), "DFT flush");
+        clk.mark("fin-records");
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
             const int nt = stepsDone_ / P.fluxes[q].spec.timeInt + 1;
             R.fluxRe.emplace_back();
@@ -170,6 +176,7 @@ public:
             }
             R.fluxSamples.push_back(nt);
         }
+        clk.mark("fin-flux");
         for (std::size_t k = 0; k < P.freqDetectors.size(); ++k) {
             std::vector<double> re, im;
             downloadDft(P.fluxes.size() + k, P.freqDetectors[k].spec.freqList.size(), re, im);
@@ -217,10 +224,12 @@ public:
                 for (std::size_t k = 0; k < n; ++k) dst[k] = cplx(all[c * n + k].x, all[c * n + k].y);
             }
         }
+        clk.mark("fin-downloads");
         write_detectors(P, R, outDir_, stepsDone_);
         write_fluxes(P, R, outDir_);
         write_freq_detectors(P, R, outDir_);
         write_emitters(P, R, outDir_);
+        clk.mark("fin-writes");
         finalized_ = true;
     }
 
@@ -1056,7 +1065,9 @@ private:
     }
 
     void upload() {
+        PhaseClock clk;
         validatePlan();
+        clk.mark("up-validate");
         const Dims& D = P.dims;
         // device rows of pitch_ >= lx values, a multiple of 4, so that every row starts on a
         // 16-byte boundary (32 bytes in FP64)
@@ -1086,6 +1097,7 @@ private:
             xi.push_back(0);
             ga.push_back(0);
         }
+        clk.mark("up-fields");
         const int* dStart = mem_.upload(pStart);
         const int* dCount = mem_.upload(pCount);
         const T* dAl = mem_.upload(al);
@@ -1210,6 +1222,7 @@ private:
             }
         }
         (void)bytes;
+        clk.mark("up-passes");
         // sources
         {
             std::vector<int> comp, srcId;
@@ -1269,6 +1282,7 @@ private:
             dRec_ = mem_.alloc<double>(recTotal_);
             recT_.rec = dRec_;
         }
+        clk.mark("up-src-rec");
         // DFT tables: the flux regions, then the frequency-domain detectors
         for (auto& fp : P.fluxes) {
             std::vector<int> comp, cell;
@@ -1292,9 +1306,13 @@ private:
                 }
             dft_.push_back(makeDft(comp, cell, dp.spec.freqList, dp.timeInt));
         }
+        clk.mark("up-dft");
         uploadEmitters();
+        clk.mark("up-emitters");
         uploadTfsf();
+        clk.mark("up-tfsf");
         uploadTail();
+        clk.mark("up-tail");
     }
 
     // One DFT table: point table (component, cell), phasors per sample from the accumulated
@@ -1653,7 +1671,9 @@ chiml_status chiml_create(const char* json_path, const chiml_options* opt, chiml
     try {
         if (!json_path) throw InputError("no input file");
         const double t0 = wall_seconds();
+        PhaseClock clk;
         Inputs in = read_inputs_file(json_path);
+        clk.mark("read-inputs");
         Plan P = build_plan(in);
         const double t1 = wall_seconds();
         std::unique_ptr<chiml_sim> s(new chiml_sim());

@@ -18,13 +18,29 @@
 #pragma once
 
 #include <array>
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
 #include "model.hpp"
 
 namespace chiml {
+
+// With CHIML_HOST_TIMES set in the environment, mark() prints the wall seconds since the
+// previous mark (or construction) to stderr: the phases of the plan build and of finalize.
+struct PhaseClock {
+    bool on = std::getenv("CHIML_HOST_TIMES") != nullptr;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    void mark(const char* what) {
+        if (!on) return;
+        const auto t1 = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "host %-14s %8.4f s\n", what, std::chrono::duration<double>(t1 - t0).count());
+        t0 = t1;
+    }
+};
 
 // Grid layout kept from chiML's Grid (GRID/Grid.hpp:201-205): x fastest, then z,
 // then y, with a one-cell halo on every side (2-D: lz == 1, no z halo).

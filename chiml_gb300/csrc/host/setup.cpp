@@ -7,6 +7,7 @@
 // cell, and compressed into the class-code form of plan.hpp. The compressed form
 // is then checked cell by cell against the literal accumulation.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <exception>
 #include <map>
@@ -634,6 +635,7 @@ struct Builder {
     enum ListKind { L_NONE = 0, L_U = 1, L_D = 2 };
 
     void buildComp(int comp) {
+        PhaseClock clk;
         CompPlan& cp = P.comp[comp];
         const bool E = comp < 3;
         const int i = comp % 3;
@@ -667,9 +669,9 @@ struct Builder {
 
         // per-cell list membership
         const int nt = innerThreads_;
-        Buf<uint8_t> curlKind = filled<uint8_t>(static_cast<std::size_t>(D.cells()), L_NONE, nt);
-        Buf<uint8_t> lorFlag = filled<uint8_t>(static_cast<std::size_t>(D.cells()), 0, nt);
-        Buf<uint8_t> ordipFlag = filled<uint8_t>(static_cast<std::size_t>(D.cells()), 0, nt);
+        // one byte per cell: the curl list kind (bits 0-1), the Lorentz list (bit 2) and the
+        // oriented-dipole list (bit 3)
+        Buf<uint8_t> cellLists = filled<uint8_t>(static_cast<std::size_t>(D.cells()), L_NONE, nt);
 
         auto classify = [&](std::array<int, 3> a, std::array<int, 3> b, bool includeU, bool finalFill) {
             int border = 0;  // rows write disjoint cells
@@ -686,12 +688,12 @@ struct Builder {
                         std::size_t id = static_cast<std::size_t>(D.idx(ii, jj, kk));
                         bool orDipCell = ob.orDip && (E && ob.gamma.size() > 0);
                         bool uCell = includeU && ((!E) || (E && ob.gamma.size() < 1 && !ob.ML));
+                        uint8_t& cl = cellLists[id];
                         if (finalFill) {
-                            if (!orDipCell && uCell) curlKind[id] = L_U;
-                            else curlKind[id] = L_D;
+                            cl = static_cast<uint8_t>((cl & ~3u) | ((!orDipCell && uCell) ? L_U : L_D));
                         } else {
-                            if (orDipCell) ordipFlag[id] = 1;
-                            else if (!uCell) lorFlag[id] = 1;
+                            if (orDipCell) cl |= 8u;
+                            else if (!uCell) cl |= 4u;
                         }
                     }
             if (border) throw InputError("update list reaches a border cell");
@@ -724,6 +726,7 @@ struct Builder {
         fmx[2] -= lnMn[2];  // lnz_front() returns the minus-side thickness
         if (lnMn[2] != 0) fmx[2] += fieldEnd[2];
         classify(fmn, fmx, true, true);
+        clk.mark("comp-lists");
 
         // term geometry: J uses grid_j (derivative along k), K uses grid_k (derivative along j)
         TermPlan* tp = cp.term;
@@ -747,13 +750,18 @@ struct Builder {
             T.cpsi.assign(L, 0.0);
         }
 
-        // literal per-cell accumulation of every list (for the check) and compression
+        // Per cell and term, one byte of CPML list membership: the number of grid-list
+        // entries on the cell (bits 0-1; the reference's npsi count), how many of them come
+        // from slabs across the term's axis (bits 2-3), whether one comes from the slab along
+        // it (bit 4), whether a psi entry updates the cell (bit 5) and whether any of its
+        // grid-list coefficients is nonzero (bit 6). The compressed coefficient of a cell,
+        // nplain * db + kflag * kprof[normal coordinate], equals the sum of its entries up
+        // to rounding: every transverse entry carries db and the one entry along the axis
+        // carries kprof at its coordinate (both checked per entry below), and the entries of
+        // one component's term share the sign of (1/kappa - 1), so that their sum is nonzero
+        // exactly when one of them is.
         const std::size_t N = static_cast<std::size_t>(D.cells());
-        Buf<double> coef[2] = {filled<double>(N, 0.0, nt), filled<double>(N, 0.0, nt)};
-        Buf<uint8_t> npsi[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
-        Buf<uint8_t> psiUpd[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
-        Buf<uint8_t> nplain[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
-        Buf<uint8_t> kflag[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
+        Buf<uint8_t> termBits[2] = {filled<uint8_t>(N, 0, nt), filled<uint8_t>(N, 0, nt)};
         auto coordOf = [&](long long id, int ax) {
             long long x = id % D.lx;
             long long r = id / D.lx;
@@ -763,6 +771,7 @@ struct Builder {
         };
         for (int t = 0; t < 2; ++t) {
             TermPlan& T = tp[t];
+            uint8_t* tb = termBits[t].data();
             double base = 0.0;
             for (auto& e : grid[t]) {
                 // a run moves along one grid axis: its coordinate along T.axis is c0 + q dq
@@ -771,22 +780,25 @@ struct Builder {
                 if (e.n > 1 && coordOf(e.ind + (e.n - 1) * e.stride, T.axis) != c0 + (e.n - 1) * dq)
                     throw InputError("CPML run does not follow one grid axis");
                 if (e.indOff - e.ind != T.off) throw InputError("CPML offset does not match the curl offset");
+                const bool along = e.slab == T.axis;
+                if (!along && e.n > 0) {
+                    if (base == 0.0) base = e.DbField;
+                    if (e.DbField != base) throw UnsupportedError("CPML transverse coefficient varies");
+                }
+                const uint8_t nz = (e.DbField != 0.0) ? 0x40 : 0;
                 for (int q = 0; q < e.n; ++q) {
-                    long long id = e.ind + q * e.stride;
-                    coef[t][id] += e.DbField;
-                    npsi[t][id] += 1;
-                    if (e.slab == T.axis) {
-                        if (kflag[t][id]) throw UnsupportedError("overlapping CPML slabs along one axis");
-                        kflag[t][id] = 1;
-                        int a = c0 + q * dq;
-                        if (T.kprof[a] != 0.0 && T.kprof[a] != e.DbField)
+                    uint8_t& b = tb[e.ind + q * e.stride];
+                    if ((b & 3u) == 3u) throw UnsupportedError("more than three CPML entries on one cell");
+                    b = static_cast<uint8_t>(b + 1u) | nz;
+                    if (along) {
+                        if (b & 0x10u) throw UnsupportedError("overlapping CPML slabs along one axis");
+                        b |= 0x10u;
+                        int ac = c0 + q * dq;
+                        if (T.kprof[ac] != 0.0 && T.kprof[ac] != e.DbField)
                             throw UnsupportedError("CPML coefficient is not a function of the normal coordinate");
-                        T.kprof[a] = e.DbField;
+                        T.kprof[ac] = e.DbField;
                     } else {
-                        double db = e.DbField;
-                        if (base == 0.0) base = db;
-                        if (db != base) throw UnsupportedError("CPML transverse coefficient varies");
-                        nplain[t][id] += 1;
+                        b = static_cast<uint8_t>(b + 4u);
                     }
                 }
             }
@@ -794,21 +806,21 @@ struct Builder {
             for (auto& e : psi[t]) {
                 if (e.indOff - e.ind != T.off) throw InputError("psi offset does not match the curl offset");
                 for (int q = 0; q < e.n; ++q) {
-                    long long id = e.ind + q * e.stride;
-                    if (psiUpd[t][id]) throw UnsupportedError("a psi cell is updated twice");
-                    psiUpd[t][id] = 1;
-                    int a = e.normCoord;
-                    if ((T.b[a] != 0.0 || T.cpsi[a] != 0.0) && (T.b[a] != e.b || T.cpsi[a] != e.c))
+                    uint8_t& b = tb[e.ind + q * e.stride];
+                    if (b & 0x20u) throw UnsupportedError("a psi cell is updated twice");
+                    b |= 0x20u;
+                    int ac = e.normCoord;
+                    if ((T.b[ac] != 0.0 || T.cpsi[ac] != 0.0) && (T.b[ac] != e.b || T.cpsi[ac] != e.c))
                         throw UnsupportedError("psi coefficients are not a function of the normal coordinate");
-                    T.b[a] = e.b;
-                    T.cpsi[a] = e.c;
+                    T.b[ac] = e.b;
+                    T.cpsi[ac] = e.c;
                 }
             }
             if (!T.hasPsi) {
-                std::fill(npsi[t].begin(), npsi[t].end(), 0);
+#pragma omp parallel for schedule(static) num_threads(nt)
+                for (long long id = 0; id < static_cast<long long>(N); ++id) tb[id] &= static_cast<uint8_t>(~3u);
             }
         }
-
         // build classes: each cell's class (its update terms and coefficients) is looked up
         // by key; class ids are given in order of first appearance in the scan order
         // (y, z, x). Rows of y are scanned in parallel chunks with chunk-local ids, merged
@@ -844,20 +856,35 @@ struct Builder {
                 chunkRows(ch, y0, y1);
                 std::map<Key, int> lindex;
                 std::vector<std::pair<Key, ClassInfo>>& lcls = local[ch];
-                Key lastKey;
-                lastKey.fill(-1.0);
+                // A cell's class depends only on its object, permittivity, list byte and the
+                // two term bytes; runs of cells with the same five reuse the last class id.
+                uint64_t lastSig = ~0ull, lastEpsBits = 0;
                 int lastId = -1;
+                const uint8_t* tb0 = termBits[0].data();
+                const uint8_t* tb1 = termBits[1].data();
                 for (int y = y0; y < y1; ++y)
                     for (int z = 0; z < D.lz; ++z)
                         for (int x = 0; x < D.lx; ++x) {
                             std::size_t id = static_cast<std::size_t>(D.idx(x, y, z));
+                            const int o = ph.at(x, y, z);
+                            const double cellEps = ep.at(x, y, z);
+                            const uint8_t lists = cellLists[id];
+                            const uint8_t tbit[2] = {tb0[id], tb1[id]};
+                            const uint64_t sig = static_cast<uint64_t>(static_cast<uint32_t>(o)) |
+                                                 (static_cast<uint64_t>(lists) << 32) |
+                                                 (static_cast<uint64_t>(tbit[0]) << 40) |
+                                                 (static_cast<uint64_t>(tbit[1]) << 48);
+                            uint64_t epsBits;
+                            std::memcpy(&epsBits, &cellEps, sizeof epsBits);
+                            if (sig == lastSig && epsBits == lastEpsBits) {
+                                cp.code[id] = static_cast<uint8_t>(lastId);
+                                continue;
+                            }
                             ClassInfo c;
-                            int o = ph.at(x, y, z);
                             c.obj = (o < 0) ? 0 : o;
-                            double cellEps = ep.at(x, y, z);
-                            uint8_t kind = curlKind[id];
+                            const uint8_t kind = lists & 3u;
                             bool pmlCell = false;
-                            for (int t = 0; t < 2; ++t) pmlCell = pmlCell || npsi[t][id] > 0 || (coef[t][id] != 0.0);
+                            for (int t = 0; t < 2; ++t) pmlCell = pmlCell || (tbit[t] & 3u) || (tbit[t] & 0x40u);
                             if (kind == L_U || kind == L_D) {
                                 double em = (kind == L_U) ? cellEps : 1.0;
                                 double pref1 = -1.0 * dt / (em * dj), pref2 = -1.0 * dt / (em * dk);
@@ -871,20 +898,19 @@ struct Builder {
                                     throw UnsupportedError("a cell's interior and CPML updates target different fields");
                                 c.toD = pmlToD;
                             }
-                            c.lor = lorFlag[id];
-                            c.ordip = ordipFlag[id];
+                            c.lor = (lists >> 2) & 1u;
+                            c.ordip = (lists >> 3) & 1u;
                             if (c.lor || c.ordip) c.eps = cellEps;
                             if (c.toD || c.lor || c.ordip) chunkAnyD[ch] = 1;
                             for (int t = 0; t < 2; ++t) {
                                 if (!tp[t].present) {
-                                    if (coef[t][id] != 0.0 || npsi[t][id] || psiUpd[t][id])
-                                        throw InputError("CPML term without a neighbour field");
+                                    if (tbit[t] & 0x63u) throw InputError("CPML term without a neighbour field");
                                     continue;
                                 }
-                                c.nplain[t] = nplain[t][id];
-                                c.kflag[t] = kflag[t][id];
-                                c.npsi[t] = npsi[t][id];
-                                c.psiUpd[t] = psiUpd[t][id];
+                                c.nplain[t] = (tbit[t] >> 2) & 3u;
+                                c.kflag[t] = (tbit[t] >> 4) & 1u;
+                                c.npsi[t] = tbit[t] & 3u;
+                                c.psiUpd[t] = (tbit[t] >> 5) & 1u;
                             }
                             Key key = {double(c.toD), double(c.lor), double(c.ordip), double(c.obj), c.eps,
                                        c.cint[0], c.cint[1], double(c.nplain[0]), double(c.nplain[1]),
@@ -893,32 +919,20 @@ struct Builder {
                             if (!(c.lor || c.ordip)) key[4] = 1.0, c.eps = 1.0;
                             if (!c.lor) key[3] = 0.0, c.obj = 0;
                             int lid;
-                            if (key == lastKey) {
-                                lid = lastId;
+                            auto it = lindex.find(key);
+                            if (it == lindex.end()) {
+                                lid = static_cast<int>(lcls.size());
+                                // a chunk's classes are a subset of the whole component's
+                                if (lid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
+                                lcls.emplace_back(key, c);
+                                lindex[key] = lid;
                             } else {
-                                auto it = lindex.find(key);
-                                if (it == lindex.end()) {
-                                    lid = static_cast<int>(lcls.size());
-                                    // a chunk's classes are a subset of the whole component's
-                                    if (lid > 255) throw UnsupportedError("more than 255 distinct cell classes in one component");
-                                    lcls.emplace_back(key, c);
-                                    lindex[key] = lid;
-                                } else {
-                                    lid = it->second;
-                                }
-                                lastKey = key;
-                                lastId = lid;
+                                lid = it->second;
                             }
+                            lastSig = sig;
+                            lastEpsBits = epsBits;
+                            lastId = lid;
                             cp.code[id] = static_cast<uint8_t>(lid);
-                            // check the compressed CPML coefficient against the literal sum
-                            for (int t = 0; t < 2; ++t) {
-                                if (!tp[t].present) continue;
-                                const int a = tp[t].axis == 0 ? x : (tp[t].axis == 1 ? y : z);
-                                double comp = c.nplain[t] * tp[t].db + (c.kflag[t] ? tp[t].kprof[a] : 0.0);
-                                double lit = coef[t][id];
-                                if (std::abs(comp - lit) > 1e-14 * std::max(1.0, std::abs(lit)) * std::abs(dt))
-                                    throw UnsupportedError("compressed CPML coefficient differs from the list sum");
-                            }
                         }
             } catch (...) {
                 chunkErr[ch] = std::current_exception();
@@ -926,6 +940,7 @@ struct Builder {
         }
         for (int ch = 0; ch < nChunks; ++ch)
             if (chunkErr[ch]) std::rethrow_exception(chunkErr[ch]);
+        clk.mark("comp-classes");
         bool anyD = false;
         std::vector<std::vector<uint8_t>> remap(static_cast<std::size_t>(nChunks));
         for (int ch = 0; ch < nChunks; ++ch) {
@@ -1005,6 +1020,7 @@ struct Builder {
     }
 
     void build() {
+        PhaseClock clk;
         P.in = in;
         objs = in.objects;
         d = in.d;
@@ -1034,6 +1050,7 @@ struct Builder {
         setupPhys(3, false, {0.0, 0.5, 0.5}, {0, 1, 1});
         setupPhys(4, false, {0.5, 0.0, 0.5}, {1, 0, 1});
         setupPhys(5, false, {0.5, 0.5, 0.0}, {1, 1, 0});
+        clk.mark("materials");
         // a barycentric test whose weights do not sum to one (Obj.cpp:485-489, 502-506)
         for (const auto& o : objs)
             if (o.baryFault->load())
@@ -1041,6 +1058,7 @@ struct Builder {
                                      ? "The sum of the boundary checks for a tetrahedron does not equal the determinant of the verticies"
                                      : "The sum of the boundary checks for a triangular base does not equal the determinant of the verticies");
         scanPML();
+        clk.mark("pml-scan");
         bool disp = false;
         for (auto& o : objs)
             if (o.gamma.size() > 0 || o.ML || o.epsInf > 1.0) disp = true;
@@ -1097,6 +1115,7 @@ struct Builder {
         omp_set_max_active_levels(prevLevels);
         for (int q = 0; q < 6; ++q)
             if (err[q]) std::rethrow_exception(err[q]);
+        clk.mark("components");
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
         buildOrDip();
         P.alpha.clear();
@@ -1110,9 +1129,11 @@ struct Builder {
             P.alphaInc.push_back(o.alphaInc);
         }
         P.in.objects = objs;
+        clk.mark("dipoles");
         buildSources();
         buildDetectors();
         buildFluxes();
+        clk.mark("io");
     }
 
     // ---- sources (parallelFDTDField.cpp:455-620) ----
@@ -1636,14 +1657,17 @@ Plan build_plan(const Inputs& in) {
     Plan P;
     Builder b(in, P);
     b.build();
+    PhaseClock clk;
     if (!in.emitters.empty()) {
         const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
         build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v.data(), P);
+        clk.mark("emitters");
     }
     if (!in.tfsf.empty()) {
         const int* ph[6];
         for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? b.phys[c].v.data() : nullptr;
         build_tfsf(in, P.dims, P.dt, ph, in.objects, P);
+        clk.mark("tfsf");
     }
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)
     for (auto& fp : P.fluxes) {
