@@ -200,6 +200,9 @@ struct Builder {
             const int i0 = std::max(1, lo[0]), i1 = std::min(D.lx - 1, hi[0]);
             const int j0 = std::max(1, lo[1]), j1 = std::min(D.ly - 1, hi[1]);
             const int k0 = twoD ? zmin : std::max(zmin, lo[2]), k1 = twoD ? zmax : std::min(zmax, hi[2]);
+            // without an emitter buffer both tests are the same test
+            const bool sameGeo = o.geoML == o.geo;
+            const double epsHere = E ? o.epsInf : 1.0;
 #pragma omp parallel for schedule(dynamic, 4)
             for (int jj = j0; jj < j1; ++jj)
                 for (int ii = i0; ii < i1; ++ii)
@@ -208,8 +211,9 @@ struct Builder {
                         pt[0] = ((ii - 1) + offPt[0] + 0 - (nvec[0] - nvec[0] % 2) / 2.0) * d[0];
                         pt[1] = ((jj - 1) + offPt[1] + 0 - (nvec[1] - nvec[1] % 2) / 2.0) * d[1];
                         pt[2] = ((kk - 1) + offPt[2] + 0 - (nvec[2] - nvec[2] % 2) / 2.0) * d[2];
-                        if (o.isObj(pt, d[0], o.geoML)) ph.at(ii, jj, kk) = static_cast<int>(oo);
-                        if (o.isObj(pt, d[0], o.geo)) ep.at(ii, jj, kk) = E ? o.epsInf : 1.0;
+                        const bool inML = o.isObj(pt, d[0], o.geoML);
+                        if (inML) ph.at(ii, jj, kk) = static_cast<int>(oo);
+                        if (sameGeo ? inML : o.isObj(pt, d[0], o.geo)) ep.at(ii, jj, kk) = epsHere;
                     }
         }
         zmin = 0;
