@@ -34,6 +34,11 @@ struct DeviceStateError : public std::runtime_error {
     explicit DeviceStateError(const std::string& w) : std::runtime_error(w) {}
 };
 
+// A detector or DFT point read a NaN or Inf (the run has diverged).
+struct NumericError : public std::runtime_error {
+    explicit NumericError(const std::string& w) : std::runtime_error(w) {}
+};
+
 struct CudaError : public std::runtime_error {
     cudaError_t code;
     CudaError(cudaError_t c, const std::string& w) : std::runtime_error(w), code(c) {}
@@ -135,7 +140,8 @@ public:
         ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
         unsigned int e = 0;
         ck(cudaMemcpy(&e, dErr_, sizeof(e), cudaMemcpyDeviceToHost), "D2H error word");
-        if (e) throw DeviceStateError("device bounds check failed (code " + std::to_string(e) + ")");
+        if (e & ~dev::kErrNumeric) throw DeviceStateError("device bounds check failed (code " + std::to_string(e) + ")");
+        if (e) throw NumericError("a detector or flux point sampled a NaN or Inf field value");
     }
 
     void finalize() override {
@@ -1375,6 +1381,8 @@ private:
         dErr_ = mem_.alloc<unsigned int>(1);
         hPass_.err = dErr_;
         ePass_.err = dErr_;
+        recT_.err = dErr_;
+        for (auto& d : dft_) d.err = dErr_;
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
         kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + static_cast<int>(dft_.size()) + (ePass_.nLor > 0 ? 1 : 0) + (ePass_.od.n > 0 ? 1 : 0) +
@@ -1646,7 +1654,8 @@ chiml_status status_of(const std::exception& e) {
     if (auto* c = dynamic_cast<const CudaError*>(&e))
         return c->code == cudaErrorMemoryAllocation ? CHIML_E_OOM : CHIML_E_CUDA;
     if (dynamic_cast<const std::bad_alloc*>(&e)) return CHIML_E_OOM;
-    if (dynamic_cast<const DeviceStateError*>(&e)) return CHIML_E_NUMERIC;
+    if (dynamic_cast<const NumericError*>(&e)) return CHIML_E_NUMERIC;
+    if (dynamic_cast<const DeviceStateError*>(&e)) return CHIML_E_STATE;
     if (dynamic_cast<const std::logic_error*>(&e)) return CHIML_E_STATE;
     return CHIML_E_INPUT;
 }

@@ -141,6 +141,7 @@ struct Pass {
 constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class table
 constexpr unsigned int kErrPoleCount = 2u;   // a class asks for more poles than its component stores
 constexpr unsigned int kErrSlab = 4u;        // a class uses a CPML term outside its term's slab bounds
+constexpr unsigned int kErrNumeric = 8u;     // a sampled field value (detector or DFT point) is NaN or Inf
 
 template <typename T>
 struct Fields {
@@ -167,6 +168,7 @@ struct RecordTable {
     const long long* recBase;   // per detector: offset of event 0 in rec
     const int* nEvents;         // per detector
     double* rec;
+    unsigned int* err;          // error word: kErrNumeric for a value that is not finite
 };
 
 // Time-blocked DFT of one flux region. Every sampled step gathers the field
@@ -191,6 +193,7 @@ struct DftTable {
     T* ring;                    // [K][stride]
     double* re;                 // [pt * nfreq + f]
     double* im;
+    unsigned int* err;          // error word: kErrNumeric for a sample that is not finite
 };
 
 // Packed launches of the batched sweep: one launch runs one kind of work for many

@@ -628,6 +628,7 @@ __device__ __forceinline__ void recordEntry(const RecordTable& r, const Fields<T
     const long long c = r.cell[j];
     const double v = (c < 0) ? 0.0 : static_cast<double>(fieldOf(f, r.comp[j])[c]);
     r.rec[r.recBase[d] + static_cast<long long>(ev) * r.nvals[d] + r.outIndex[j]] = v;
+    if (!isfinite(v)) atomicOr(r.err, kErrNumeric);
 }
 
 template <typename T>
@@ -646,7 +647,9 @@ __device__ __forceinline__ void dftSampleEntry(const DftTable<T>& d, const Field
     const int st = *step;
     if (st % d.timeInt != 0 || p >= d.npts) return;
     const int slot = (st / d.timeInt) & (d.K - 1);
-    d.ring[static_cast<long long>(slot) * d.stride + p] = fieldOf(f, d.comp[p])[d.cell[p]];
+    const T v = fieldOf(f, d.comp[p])[d.cell[p]];
+    d.ring[static_cast<long long>(slot) * d.stride + p] = v;
+    if (!isfinite(v)) atomicOr(d.err, kErrNumeric);
 }
 
 template <typename T>

@@ -28,9 +28,10 @@ typedef enum chiml_status {
     CHIML_E_UNSUPPORTED = 2, /* a feature outside this engine (magnetic/chiral media, PBC, ...) */
     CHIML_E_CUDA = 3,        /* a CUDA runtime error */
     CHIML_E_OOM = 4,         /* device memory exhausted */
-    CHIML_E_NUMERIC = 5,     /* a NaN or Inf reached a monitored field value */
-    CHIML_E_TIMEOUT = 6,     /* a bounded device wait gave up */
-    CHIML_E_STATE = 7        /* call out of order (e.g. step after finalize) */
+    CHIML_E_NUMERIC = 5,     /* a detector or flux/DFT point sampled a NaN or Inf field value */
+    CHIML_E_TIMEOUT = 6,     /* reserved: no kernel of this engine spins on a flag or barrier */
+    CHIML_E_STATE = 7        /* call out of order (e.g. step after finalize), or a device-side
+                                bounds check of the plan failed */
 } chiml_status;
 
 typedef enum chiml_precision {
