@@ -332,14 +332,35 @@ Object read_object(const JNode& node, const Inputs& ip) {
             throw UnsupportedError("Tellegen media are not supported");
         for (auto& kv : node.child("pols").kids) {
             const JNode& pn = kv.second;
-            if (pn.get<bool>("tanIso", false)) throw UnsupportedError("tangential-isotropic poles are not supported");
+            // a tangential-isotropic pole needs relative electric and magnetic orientations
+            // (parallelInputs.cpp:1290-1295); magnetic orientations are rejected below, so
+            // with tanIso set the reference's own check is the one that applies
+            if (pn.get<bool>("tanIso", false))
+                throw InputError("Object can't be isotropic in tangential directions and unidirectional or isotropic");
             if (pn.get<bool>("molecular_trans", false)) throw UnsupportedError("molecular-transition poles are not supported");
             Oscillator osc;
-            osc.dipOrE = string2dipor(pn.get<std::string>("dipOrE", "isotropic"));
+            const std::string dipOrName = pn.get<std::string>("dipOrE", "isotropic");
+            osc.dipOrE = string2dipor(dipOrName);
             if (string2dipor(pn.get<std::string>("dipOrM", "isotropic")) != DipOr::ISOTROPIC)
                 throw UnsupportedError("magnetic dipole orientations are not supported");
-            if (osc.dipOrE != DipOr::ISOTROPIC && osc.dipOrE != DipOr::UNIDIRECTIONAL)
-                throw UnsupportedError("surface-relative dipole orientations are not supported");
+            // dipoles relative to the surface normal (parallelInputs.cpp:1330-1357): polar
+            // angle from the normal and azimuth in the tangent plane, fixed by the named forms
+            double polAng = pn.get<double>("polAngRelNormE", 45.0);
+            double azAng = pn.get<double>("azAngRelNormE", 45.0);
+            if (dipOrName == "normal") {
+                polAng = 0.0;
+            } else if (dipOrName == "tangent") {
+                polAng = 90.0;
+            } else if (osc.dipOrE == DipOr::LONG_TAN) {
+                polAng = 90.0;
+                azAng = 0.0;
+            } else if (osc.dipOrE == DipOr::LAT_TAN) {
+                polAng = 90.0;
+                azAng = 90.0;
+            }
+            osc.normW = std::cos(polAng * M_PI / 180.0);
+            osc.latW = std::sin(polAng * M_PI / 180.0) * std::sin(azAng * M_PI / 180.0);
+            osc.longW = std::sin(polAng * M_PI / 180.0) * std::cos(azAng * M_PI / 180.0);
             osc.gam = pn.get<double>("gamma") * M_PI;
             osc.omg = pn.get<double>("omega") * 2 * M_PI;
             osc.sigP = pn.get<double>("sigma_p", 0.0);
@@ -987,12 +1008,14 @@ void Object::setUpConsts(double dt) {
     alphaInc.clear();
     dipOr.clear();
     dipE.clear();
+    dipW.clear();
     orDip = false;
     for (auto& p : pols) {
         if (p.dipOrE != DipOr::ISOTROPIC) orDip = true;
         if (std::abs(p.sigP) != 0.0) {
             dipOr.push_back(p.dipOrE);
             dipE.push_back(p.uVecDipE);
+            dipW.push_back({p.normW, p.latW, p.longW});
             alpha.push_back(((2 - std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
             xi.push_back(((p.gam * dt - 1) / (1 + p.gam * dt)));
             gamma.push_back(((p.sigP * std::pow(p.omg * dt, 2.0)) / (1 + p.gam * dt)));
@@ -1088,6 +1111,12 @@ bool Object::isObj(const std::array<double, 3>& v, double dx, const std::vector<
             return true;
         }
         case Shape::TETRAHEDRON: {
+            // The regular form keeps its two-entry size (side, height) as the emitter-buffer
+            // geometry with which the material index is tested (geoParamML_ is copied before
+            // the constructor replaces geoParam_, Obj.cpp:63-72 and 215-252), and the
+            // reference reads four entries of it. No point passes that test in the
+            // reference's runs (shapes_b, dip_surface_b); here it is false without the read.
+            if (geo_.size() < 4) return false;
             const std::array<double, 4> b = to_bary<4>(invVert, v.data());
             for (int i = 0; i < 4; ++i)
                 if (b[i] < -1e-6 * dx || (b[i] + dx * 1e-6) > geo_[i]) return false;
@@ -1125,6 +1154,181 @@ bool Object::isObj(const std::array<double, 3>& v, double dx, const std::vector<
         }
     }
     return false;
+}
+
+// ---- surface directions (Obj::findGradient, OBJECTS/Obj.cpp:585-878) ----
+namespace {
+
+double sumSq(const std::array<double, 3>& v) { return ((0.0 + v[0] * v[0]) + v[1] * v[1]) + v[2] * v[2]; }
+
+void normalize3(std::array<double, 3>& v) {
+    const double n = std::sqrt(sumSq(v));
+    for (auto& x : v) x = x / n;
+}
+
+// BLAS i?amin / i?amax: the first index (0-based here) of the smallest / largest |x|.
+template <std::size_t N>
+int first_abs_min(const std::array<double, N>& x) {
+    int b = 0;
+    for (int i = 1; i < static_cast<int>(N); ++i)
+        if (std::abs(x[i]) < std::abs(x[b])) b = i;
+    return b;
+}
+template <std::size_t N>
+int first_abs_max(const std::array<double, N>& x) {
+    int b = 0;
+    for (int i = 1; i < static_cast<int>(N); ++i)
+        if (std::abs(x[i]) > std::abs(x[b])) b = i;
+    return b;
+}
+
+// Obj::ObjectSpace2RealSpace (Obj.cpp:24-34): the inverse of the unit-vector matrix (LU
+// inverse, as the reference's constructor forms it) applied, then normalised (zero for a
+// vector of squared length below 1e-20).
+std::array<double, 3> to_real_normalised(const Object& o, const std::array<double, 3>& g) {
+    double inv[9];
+    std::copy(o.coord.begin(), o.coord.end(), inv);
+    if (lu_invert(3, inv) == 0.0) throw InputError("The invCoordTransform_ can't be calculated!");
+    std::array<double, 3> r;
+    for (int i = 0; i < 3; ++i) {
+        double t = 0.0;
+        for (int k = 0; k < 3; ++k) t += inv[k + 3 * i] * g[k];
+        r[i] = t;
+    }
+    if (sumSq(r) < 1e-20) return {0.0, 0.0, 0.0};
+    normalize3(r);
+    return r;
+}
+
+}  // namespace
+
+std::array<double, 3> Object::gradient(const std::array<double, 3>& pt) const {
+    const std::vector<double>& g = geo;
+    switch (shape) {
+        case Shape::SPHERE:
+        case Shape::HEMISPHERE: {
+            std::array<double, 3> r = {pt[0] - loc[0], pt[1] - loc[1], pt[2] - loc[2]};
+            if (sumSq(r) < 1e-20) return {0.0, 0.0, 0.0};
+            normalize3(r);
+            return r;
+        }
+        case Shape::ELLIPSOID:
+        case Shape::HEMIELLIPSOID: {
+            std::array<double, 3> v = to_object(*this, pt);
+            for (int i = 0; i < 3; ++i) v[i] = v[i] / std::pow(g[i], 2.0);
+            return to_real_normalised(*this, v);
+        }
+        case Shape::CONE: {
+            const std::array<double, 3> v = to_object(*this, pt);
+            const double zp = v[2] + g[1] / 2.0;
+            const double c = g[0] / g[2];
+            const double z0 = zp * (1.0 + std::sqrt((std::pow(v[0], 2.0) + std::pow(v[1], 2.0)) / std::pow(c, 2.0)));
+            std::array<double, 3> r = {2.0 * v[0], 2.0 * v[1], -2.0 * std::pow(c, 2.0) * (zp - z0)};
+            if (std::abs(v[2]) == std::abs(z0 / 2.0)) r = {0.0, 0.0, -2.0 * v[2] / g[1]};
+            return to_real_normalised(*this, r);
+        }
+        case Shape::CYLINDER: {
+            const std::array<double, 3> v = to_object(*this, pt);
+            const double r = std::sqrt(std::pow(v[0], 2.0) + std::pow(v[2], 2.0));
+            const double len = g[1] * (r / g[0]);
+            std::array<double, 3> d = {v[0], 0.0, v[2]};
+            if (std::abs(v[1]) >= len / 2.0) d = {0.0, v[1] / std::abs(v[1]), 0.0};
+            return to_real_normalised(*this, d);
+        }
+        case Shape::BLOCK:
+        case Shape::ROUNDED_BLOCK: {
+            const std::array<double, 3> v = to_object(*this, pt);
+            std::array<double, 3> rat;
+            for (int i = 0; i < 3; ++i) rat[i] = v[i] / g[i];
+            const int m = first_abs_max(rat);
+            std::array<double, 3> d = {0.0, 0.0, 0.0};
+            bool corner = false;
+            if (shape == Shape::ROUNDED_BLOCK) {
+                const double t = rat[m];
+                corner = true;
+                for (int i = 0; i < 3; ++i)
+                    if (v[i] - t * (g[i] - g[3]) <= 0) corner = false;
+                if (corner) {
+                    // the reference takes |pt| of the real-space point here
+                    const std::array<double, 3> ab = {std::abs(pt[0]), std::abs(pt[1]), std::abs(pt[2])};
+                    const std::array<double, 3>& cen = curveCens[0];
+                    double dot = 0.0;
+                    for (int k = 0; k < 3; ++k) dot += ab[k] * cen[k];
+                    const double cenMag = sumSq(cen), ptMag = sumSq(ab);
+                    const double tt = 1.0 / (cenMag - std::pow(g[3], 2.0)) *
+                                      (std::pow(dot, 2.0) - std::sqrt(std::pow(dot, 2.0) - ptMag * (cenMag - std::pow(g[3], 2.0))));
+                    for (int k = 0; k < 3; ++k) d[k] = ab[k] - tt * cen[k];
+                    for (int k = 0; k < 3; ++k) d[k] = d[k] * pt[k] / std::abs(pt[k]);
+                }
+            }
+            if (!corner)
+                for (int i = 0; i < 3; ++i)
+                    if (rat[i] == rat[m]) d[i] = v[i] >= 0 ? 1.0 : -1.0;
+            return to_real_normalised(*this, d);
+        }
+        case Shape::TETRAHEDRON: {
+            const std::array<double, 4> b = to_bary<4>(invVert, pt.data());
+            std::array<double, 4> baseRat, truncRat;
+            for (int i = 0; i < 4; ++i) {
+                baseRat[i] = b[i] / g[i];
+                truncRat[i] = (g[i] - b[i]) / g[i];
+            }
+            const int iB = first_abs_min(baseRat) + 1, iT = first_abs_min(truncRat) + 1;
+            const int closest = (truncRat[iT - 1] < baseRat[iB - 1]) ? -1 * iT : iB;
+            const double dist = (closest < 0) ? truncRat[iT - 1] : baseRat[iB - 1];
+            std::vector<int> faces;
+            for (int i = 0; i < 4; ++i) {
+                if (baseRat[i] == dist) faces.push_back(i + 1);
+                if (truncRat[i] == dist) faces.push_back(-1 * i - 1);
+            }
+            std::array<double, 3> d = {0.0, 0.0, 0.0};
+            for (int f : faces) {
+                // the face's vertices, ordered so that the cross product points outwards
+                std::vector<int> act;
+                const int af = std::abs(f);
+                for (int ii = 0; ii < 4; ++ii) {
+                    int index = (static_cast<int>(std::pow(-1, af - 1) * ii) % 4) * static_cast<int>(f / af);
+                    index += (index < 0) ? 4 : 0;
+                    if (index != af - 1) act.push_back(index);
+                }
+                std::array<double, 3> v1, v2;
+                for (int k = 0; k < 3; ++k) {
+                    v1[k] = verts[act[1]][k] - verts[act[0]][k];
+                    v2[k] = verts[act[2]][k] - verts[act[1]][k];
+                }
+                std::array<double, 3> n = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+                normalize3(n);
+                for (int k = 0; k < 3; ++k) d[k] = n[k] + d[k];
+            }
+            if (std::abs(sumSq(d)) < 1.0e-20) return {0.0, 0.0, 0.0};
+            normalize3(d);
+            return d;
+        }
+        case Shape::PARABOLOID: {
+            std::array<double, 3> v = to_object(*this, pt);
+            v[1] += g[2] / 2.0;
+            std::array<double, 3> d = {2 * v[0] / std::pow(g[0], 2.0), -1.0, 2.0 * v[2] / std::pow(g[2], 2.0)};
+            normalize3(d);
+            return d;
+        }
+        case Shape::TORUS: {
+            const std::array<double, 3> v = to_object(*this, pt);
+            const double ring = std::sqrt(std::pow(v[0], 2.0) + std::pow(v[1], 2.0));
+            const double term = (ring - g[0]) / ring;
+            std::array<double, 3> d = {2.0 * v[0] * term, 2.0 * v[1] * term, 2.0 * v[2]};
+            normalize3(d);
+            return d;
+        }
+        case Shape::TERS_TIP:
+            throw InputError("Gradient is not defined for this object yet defined");
+        case Shape::TRI_PRISM:
+            // tri_prism::findGradient (Obj.cpp:700-792) indexes its three vertices with a
+            // 1-based face number, and with a negative one for the truncated faces, so its
+            // result depends on memory past the vertex array
+            throw UnsupportedError("dipoles relative to the surface of a triangular prism are not supported (the "
+                                   "reference's prism gradient reads past its vertex array)");
+    }
+    return {0.0, 0.0, 0.0};
 }
 
 }  // namespace chiml

@@ -60,6 +60,9 @@ struct Oscillator {
     DipOr dipOrE = DipOr::ISOTROPIC;
     double omg = 0.0, gam = 0.0, sigP = 0.0;
     std::array<double, 3> uVecDipE = {1.0, 1.0, 1.0};
+    // weights of a dipole relative to the local surface (normCompWeightE_,
+    // tangentLatCompWeightE_, tangentLongCompWeightE_; parallelInputs.cpp:1330-1357)
+    double normW = 1.0, latW = 0.0, longW = 0.0;
 };
 
 // A geometric object with its material; coefficients from Obj::setUpConsts (Obj.cpp:299-370).
@@ -87,8 +90,11 @@ struct Object {
     std::vector<double> alphaInc;  // -(omega dt)^2 / (1 + gamma dt) = alpha + xi - 1, formed without cancellation
     std::vector<DipOr> dipOr;
     std::vector<std::array<double, 3>> dipE;
+    std::vector<std::array<double, 3>> dipW;  // per pole: normal, latitudinal, longitudinal weights
 
     bool isObj(const std::array<double, 3>& v, double dx, const std::vector<double>& g) const;
+    // Outward surface direction at a real-space point (Obj::findGradient, Obj.cpp:585-878).
+    std::array<double, 3> gradient(const std::array<double, 3>& pt) const;
     bool isVacuum() const { return !(gamma.size() > 0 || epsInf != 1.0 || ML); }
     void setUpConsts(double dt);
 };

@@ -989,6 +989,25 @@ struct Builder {
     // (parallelFDTDField.cpp:83-87 with getBlasLists / fillBlasLists), and the dipole
     // direction of every pole there (setupDipMoments, parallelFDTDField.hpp:960-1048:
     // isotropic 1, unidirectional the normalised direction).
+    // getTangentDip (parallelFDTDField.hpp:1058-1091), 3-D form: the tangent rotated from the
+    // normal by pi/2 in polar angle (longitudinal) and its cross product with the normal
+    // (latitudinal), weighted.
+    static std::array<double, 3> tangentDip(const std::array<double, 3>& n, double latF, double longF) {
+        const double mag = std::sqrt(((0.0 + n[0] * n[0]) + n[1] * n[1]) + n[2] * n[2]);
+        std::array<double, 3> sph = {mag, std::acos(n[2] / mag), std::atan(n[1] / n[0])};
+        if (n[0] == 0.0) sph[2] = n[1] >= 0.0 ? M_PI / 2.0 : -1.0 * M_PI / 2.0;
+        if (n[0] < 0) sph[2] += M_PI;
+        if (mag < 1e-20) sph = {0.0, 0.0, 0.0};
+        const double pol = sph[1] + M_PI / 2.0, az = sph[2];
+        const std::array<double, 3> lng = {mag * std::sin(pol) * std::cos(az), mag * std::sin(pol) * std::sin(az), mag * std::cos(pol)};
+        std::array<double, 3> out;
+        for (int i = 0; i < 3; ++i) {
+            const double lat = n[(i + 1) % 3] * lng[(i + 2) % 3] - n[(i + 2) % 3] * lng[(i + 1) % 3];
+            out[i] = longF * lng[i] + latF * lat;
+        }
+        return out;
+    }
+
     void buildOrDip() {
         OrDipPlan& od = P.ordip;
         od = OrDipPlan();
@@ -1011,8 +1030,22 @@ struct Builder {
                     for (int pp = 0; pp < np; ++pp) {
                         std::array<double, 3> dv = {0.0, 0.0, 0.0};
                         if (pp < static_cast<int>(ob.dipOr.size())) {
-                            if (ob.dipOr[pp] == DipOr::ISOTROPIC) dv = {1.0, 1.0, 1.0};
-                            else dv = ob.dipE[pp];
+                            const DipOr dor = ob.dipOr[pp];
+                            if (dor == DipOr::ISOTROPIC) {
+                                dv = {1.0, 1.0, 1.0};
+                            } else if (dor == DipOr::UNIDIRECTIONAL) {
+                                dv = ob.dipE[pp];
+                            } else if (dor == DipOr::REL_TO_NORM) {
+                                const std::array<double, 3> pt = {((ii - 1) - (nvec[0] - nvec[0] % 2) / 2.0) * d[0],
+                                                                  ((jj - 1) - (nvec[1] - nvec[1] % 2) / 2.0) * d[1],
+                                                                  ((kk - 1) - (nvec[2] - nvec[2] % 2) / 2.0) * d[2]};
+                                const std::array<double, 3> n = ob.gradient(pt);
+                                const std::array<double, 3>& w = ob.dipW[static_cast<std::size_t>(pp)];
+                                const std::array<double, 3> tan = tangentDip(n, w[1], w[2]);
+                                for (int c = 0; c < 3; ++c) dv[c] = w[0] * n[c] + tan[c];
+                            }
+                            // the lat_tangent and long_tangent forms leave the reference's
+                            // dipole grid at zero (setupDipMoments has no branch for them)
                         }
                         od.dip.push_back(dv);
                     }

@@ -44,6 +44,29 @@ def test_rejections_are_reported_with_status(built_engine, tmp_path, mutate, sta
     assert err.status == status, str(err)
 
 
+def _relpole(kind, **kw):
+    p = {"gamma": 0.01, "omega": 1.0, "sigma_p": 1.0, "dipOrE": kind}
+    p.update(kw)
+    return p
+
+
+@pytest.mark.parametrize("obj,status,msg", [
+    # tanIso needs relative magnetic dipoles too; with the default isotropic ones the
+    # reference's own check throws (parallelInputs.cpp:1290-1295)
+    (dict(shape="sphere", radius=0.2, pols=[_relpole("normal", tanIso=True)]), 1, "isotropic in tangential"),
+    # the reference's prism gradient reads past its vertex array
+    (dict(shape="triangle_prism", base=0.3, height=0.2, length=0.3, pols=[_relpole("normal")]), 2, "triangular prism"),
+    # the reference's TERS tip has no gradient and throws this message
+    (dict(shape="ters_tip", rad_curve=0.1, base=0.3, length=0.3, pols=[_relpole("tangent")]), 1, "Gradient is not defined"),
+])
+def test_surface_relative_dipoles_that_cannot_run(built_engine, tmp_path, obj, status, msg):
+    cfg = configs.config2(n=24, pml=4, steps=10, nell=0, nfreq=3, metal_radius_cells=0, tfsf=False)
+    o = configs._obj(obj.pop("shape"), [0.0, 0.0, 0.0], material="custom", eps=2.0, pols=obj.pop("pols"), **obj)
+    cfg["ObjectList"] = [o]
+    err = _create(built_engine, cfg, tmp_path)
+    assert err.status == status and msg in str(err), str(err)
+
+
 def test_comments_are_stripped(built_oracle, tmp_path):
     import oracle
     src = open(os.path.join(GOLDEN, "c1_small", "in.json")).read().splitlines()
