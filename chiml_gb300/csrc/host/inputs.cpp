@@ -606,8 +606,8 @@ void add_ml_buffer(Object& o, double d) {
     }
 }
 
-// Inhomogeneous-broadening weight functions (UTIL/ML_Dist_Fxn.hpp): the normal density,
-// its log-normal and skew-normal forms.
+// Inhomogeneous-broadening weight functions (UTIL/ML_Dist_Fxn.hpp:14-50): the normal density,
+// its log-normal, skew-normal, exponential-power and generalised skew-normal forms.
 static double norm_dist(double x, double cen, double w) {
     return 1.0 / std::sqrt(2 * M_PI * std::pow(w, 2.0)) * std::exp(-1.0 * std::pow(x - cen, 2.0) / (2.0 * std::pow(w, 2.0)));
 }
@@ -618,6 +618,19 @@ static double log_norm_dist(double x, double cen, double w) {
 }
 static double skew_norm_dist(double x, double cen, double w, double skew) {
     return norm_dist(x, cen, w) * 0.5 * (1.0 + std::erf(skew * (x - cen) / (std::sqrt(2.0) * w)));
+}
+// exponential-power (generalised normal) density of shape s: s / (2 w Gamma(1/s)) exp(-(|x - c| / w)^s)
+static double exp_pow_dist(double x, double cen, double w, double s) {
+    return s / (2 * w * std::tgamma(1.0 / s)) * std::exp(-1.0 * std::pow(std::abs(x - cen) / w, s));
+}
+// generalised skew-normal of shape k as the reference writes it: zero beyond c + w / k, else
+// the standard normal density at y = -log(1 - k^2 (x - c) / w) / k over (w - k (x - c))
+// (the reference's argument carries k twice); the normal density for k = 0
+static double gen_skew_norm_dist(double x, double cen, double w, double k) {
+    if (k == 0.0) return norm_dist(x, cen, w);
+    if ((k < 0 && x < cen + w / k) || (k > 0 && x > cen + w / k)) return 0.0;
+    const double y = -1.0 / k * std::log(1 - k * (k * (x - cen) / w));
+    return norm_dist(y, 0.0, 1.0) / (w - k * (x - cen));
 }
 
 enum class LevelDist { GAUSSIAN, DELTA, SKEW_NORMAL, LOG_NORMAL, EXP_POW, GEN_SKEW_NORMAL };
@@ -707,7 +720,13 @@ void read_emitter(const JNode& node, Object& o, Inputs& ip) {
                     for (std::size_t i = 0; i < width.size(); ++i)
                         weight += wVec[i] * skew_norm_dist(es, eCen[i], width[i], skew[i]);
                 } else {
-                    throw UnsupportedError("generalised skew-normal and exponential-power level distributions are not supported");
+                    // GEN_SKEW_NORMAL and EXP_POW: one shape factor per centre
+                    std::vector<double> shape = as_vector(lev, "shape_factor");
+                    if (shape.size() != eCen.size())
+                        throw InputError("The center frequency and shape factor do not have the same size.");
+                    for (std::size_t i = 0; i < width.size(); ++i)
+                        weight += wVec[i] * (dist == LevelDist::EXP_POW ? exp_pow_dist(es, eCen[i], width[i], shape[i])
+                                                                        : gen_skew_norm_dist(es, eCen[i], width[i], shape[i]));
                 }
                 level.weights.push_back(weight);
                 weightSum += weight;

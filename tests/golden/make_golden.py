@@ -396,6 +396,34 @@ def _dip_surface_b():
     return _bin_planes(cfg, [("Ex", (1.5, 1.5, 0.0)), ("Ey", (0.0, 1.5, 1.5))])
 
 
+def _level(e_cen_ev, dist, nstates, width_ev, **factors):
+    lv = configs.emitter_level(e_cen_ev, dist, nstates, width_ev)
+    lv.update({k: [v] for k, v in factors.items()})
+    return lv
+
+
+def _qe_dists_3d():
+    """qe_3d's three-level ladder with a skew-normal (skew 2) and an exponential-power
+    (shape 1.5) broadened upper level, three sampled energies each."""
+    cfg = _qe_3d()
+    lv = [configs.emitter_level(0.0), _level(2.0, "skew_normal", 3, 0.02, skew_factor=2.0),
+          _level(4.2, "exp_pow", 3, 0.02, shape_factor=1.5)]
+    cfg["ObjectList"][0]["Energy_Levels"] = lv
+    return cfg
+
+
+def _qe_dists_2d():
+    """qe_tm's two-level block with a generalised skew-normal (shape 0.3) broadened upper
+    level sampled at four energies."""
+    cfg = _qe_tm()
+    lv = [configs.emitter_level(0.0), _level(2.0, "gen_skew_normal", 4, 0.03, shape_factor=0.3)]
+    o = cfg["ObjectList"][0]
+    o["Energy_Levels"] = lv
+    n = 2
+    o["couplings"] = [1e5] * (n * n)
+    return cfg
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -425,6 +453,8 @@ CASES = {
     "src_circ_3d": _src_circ_3d,
     "dip_surface_a": _dip_surface_a,
     "dip_surface_b": _dip_surface_b,
+    "qe_dists_3d": _qe_dists_3d,
+    "qe_dists_2d": _qe_dists_2d,
 }
 
 

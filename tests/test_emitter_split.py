@@ -22,7 +22,7 @@ TOL_EMIT = 1e-5    # relative L2 per data group of the emitter files, split vs F
 TOL_TRACE = 1e-7   # relative drift of the summed populations over the long run (split: 1.2e-8)
 TOL_LONG = 1e-5    # final populations, split vs FP64, after 10^5 steps
 
-EMITTER_CASES = ["qe_tm", "qe_te", "qe_3d", "c5_small"]
+EMITTER_CASES = ["qe_tm", "qe_te", "qe_3d", "qe_dists_3d", "qe_dists_2d", "c5_small"]
 
 
 def _run(path, precision, out_dir):
