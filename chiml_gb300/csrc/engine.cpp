@@ -250,11 +250,18 @@ public:
             ck(cudaMemcpy(dre.data(), d.re, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H DFT accumulators");
             ck(cudaMemcpy(dim.data(), d.im, n * sizeof(double), cudaMemcpyDeviceToHost), "D2H DFT accumulators");
         }
+        // the split form's float-float pairs become doubles (hi + lo is exact in FP64)
+        auto value = [](const std::vector<double>& a, std::size_t i) {
+            if (!dev::kFloatFloatAcc<T>) return a[i];
+            float pr[2];
+            std::memcpy(pr, &a[i], sizeof pr);
+            return static_cast<double>(pr[0]) + static_cast<double>(pr[1]);
+        };
         const std::vector<int>& pos = dftPos_[q];
         for (std::size_t p = 0; p < pos.size(); ++p)
             for (std::size_t f = 0; f < nf; ++f) {
-                re[p * nf + f] = dre[static_cast<std::size_t>(pos[p]) * nf + f];
-                im[p * nf + f] = dim[static_cast<std::size_t>(pos[p]) * nf + f];
+                re[p * nf + f] = value(dre, static_cast<std::size_t>(pos[p]) * nf + f);
+                im[p * nf + f] = value(dim, static_cast<std::size_t>(pos[p]) * nf + f);
             }
         d2h_ += 2.0 * n * sizeof(double);
     }
@@ -300,8 +307,8 @@ public:
         double2* partial = tmp.alloc<double2>(tiles.size() * static_cast<std::size_t>(nfreq), false);
         double2* out = tmp.alloc<double2>(res.size(), false);
         const double nt2 = std::pow(static_cast<double>(nt), 2.0);
-        dev::launch_flux_faces(dFaces, nFaces, dTiles, static_cast<int>(tiles.size()), nfreq, dft_[q].re, dft_[q].im, nt2, partial,
-                               out, stream_);
+        dev::launch_flux_faces(dFaces, nFaces, dTiles, static_cast<int>(tiles.size()), nfreq, dft_[q].re, dft_[q].im,
+                               dev::kFloatFloatAcc<T>, nt2, partial, out, stream_);
         ck(cudaGetLastError(), "flux integration launch");
         ck(cudaStreamSynchronize(stream_), "flux integration");
         std::vector<double2> h(res.size());

@@ -372,6 +372,30 @@ __device__ __forceinline__ void dfAdd(float& hi, float& lo, float v) {
     hi = h;
 }
 
+// (hi, lo) + (bh, bl), renormalised (the pair sum of Dekker's double-length arithmetic)
+__device__ __forceinline__ void dfAddPair(float& hi, float& lo, float bh, float bl) {
+    const float s = hi + bh;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (bh - bb);
+    const float l2 = (lo + bl) + err;
+    const float h = s + l2;
+    lo = l2 - (h - s);
+    hi = h;
+}
+
+// The split form sums each cell's members on the FP32 pipe: the population of detector d
+// as a (re hi, re lo, im hi, im lo) float4 in the 16 bytes of gPopSh[d][thread], turned
+// into the double2 the block reduction reads once the cell's members are done.
+__device__ __forceinline__ void addPopSplit(int d, float4 v) {
+    float4& p = reinterpret_cast<float4&>(gPopSh[d * kEmThreads + threadIdx.x]);
+    dfAddPair(p.x, p.y, v.x, v.y);
+    dfAddPair(p.z, p.w, v.z, v.w);
+}
+__device__ __forceinline__ void popSplitToDouble(int d) {
+    const float4 p = reinterpret_cast<const float4&>(gPopSh[d * kEmThreads + threadIdx.x]);
+    gPopSh[d * kEmThreads + threadIdx.x] = make_double2(dfToDouble(p.x, p.y), dfToDouble(p.z, p.w));
+}
+
 // Upper-triangle derivative of the split form (the arrangement of den_deriv_herm): HE the
 // coupling -E . mu / hbar (real symmetric, upper triangle, FP32), den the density's hi
 // parts, dl the level differences of this member, cmask the nonzero elements of HE.
@@ -439,7 +463,7 @@ template <int NT>
 __device__ __forceinline__ void memberHermSplit(const EmitterDev& e, const float* HE, int m, long long base,
                                                 const float2* __restrict__ k0, const float2* __restrict__ k1,
                                                 const float2* __restrict__ k2, float2* __restrict__ k3, bool popStep,
-                                                double* Pc, unsigned cmask) {
+                                                float2* PcF, unsigned cmask) {
     constexpr int N2 = NT * NT;
     const float c55 = e.abPf[0], cm59 = e.abPf[1], c37 = e.abPf[2], cm9 = e.abPf[3];
     const float c9 = e.abCf[0], c19 = e.abCf[1], cm5 = e.abCf[2], c1 = e.abCf[3];
@@ -532,8 +556,8 @@ __device__ __forceinline__ void memberHermSplit(const EmitterDev& e, const float
 #pragma unroll
                 for (int t = 1; t < N2; ++t)
                     if ((t % NT) <= (t / NT) && ku == t) v = r0[t];
-                const double im = dfToDouble(v.z, v.w);
-                addPop(d, dfToDouble(v.x, v.y), lower ? -im : im);
+                if (lower) v.z = -v.z, v.w = -v.w;
+                addPopSplit(d, v);
             }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -547,7 +571,7 @@ __device__ __forceinline__ void memberHermSplit(const EmitterDev& e, const float
                 const float ax = r <= cc ? a[i].x : a[cc + r * NT].x;
                 sdot = fmaf(ax, static_cast<float>(e.mu[c * N2 + i].x), sdot);
             }
-        Pc[c] += e.na * static_cast<double>(sdot);
+        dfAdd(PcF[c].x, PcF[c].y, sdot);  // the sum over members; times na once per cell
     }
 }
 
@@ -575,8 +599,14 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             if (!e.comp[c]) continue;
-            if (c == 2 && e.gatherZCopy) Ec[c] = static_cast<double>(Es[c][g]);
-            else Ec[c] = 0.5 * static_cast<double>(Es[c][g]) + 0.5 * static_cast<double>(Es[c][g - e.unit[c]]);
+            if constexpr (SPLIT) {
+                // FP32 fields, FP32 coupling: the average on the FP32 pipe
+                if (c == 2 && e.gatherZCopy) Ec[c] = static_cast<double>(Es[c][g]);
+                else Ec[c] = static_cast<double>(0.5f * static_cast<float>(Es[c][g]) + 0.5f * static_cast<float>(Es[c][g - e.unit[c]]));
+            } else {
+                if (c == 2 && e.gatherZCopy) Ec[c] = static_cast<double>(Es[c][g]);
+                else Ec[c] = 0.5 * static_cast<double>(Es[c][g]) + 0.5 * static_cast<double>(Es[c][g - e.unit[c]]);
+            }
         }
         const bool zeroE = (Ec[0] == 0.0 && Ec[1] == 0.0 && Ec[2] == 0.0);
         const long long slotStride = static_cast<long long>(e.nm) * n2 * e.nc;
@@ -611,9 +641,17 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
             const float2* __restrict__ f1 = e.kdF + s1 * slotStride;
             const float2* __restrict__ f2 = e.kdF + s2 * slotStride;
             float2* __restrict__ f3 = e.kdF + s3 * slotStride;
+            float2 PcF[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
             for (int m = 0; m < e.nm; ++m)
-                memberHermSplit<NT>(e, HE, m, static_cast<long long>(m) * n2 * e.nc + q, f0, f1, f2, f3, popStep, Pc,
+                memberHermSplit<NT>(e, HE, m, static_cast<long long>(m) * n2 * e.nc + q, f0, f1, f2, f3, popStep, PcF,
                                     cmask);
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (e.comp[c] && e.addMu[c]) Pc[c] = e.na * dfToDouble(PcF[c].x, PcF[c].y);
+            if (popStep)
+#pragma unroll
+                for (int d = 0; d < kMaxDtc; ++d)
+                    if (d < e.nDtc) popSplitToDouble(d);
         } else if constexpr (HERM) {
             for (int m = 0; m < e.nm; ++m)
                 memberHerm<NT>(e, Ec, zeroE, m, static_cast<long long>(m) * n2 * e.nc + q, k0, k1, k2, k3, popStep,

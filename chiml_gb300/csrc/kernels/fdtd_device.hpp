@@ -178,6 +178,12 @@ struct RecordTable {
 //   re[pt][f] += sum_k cos(w_f t_k) F_k[pt],  im[pt][f] += sum_k -sin(w_f t_k) F_k[pt]
 // which is the per-step update of parallelStorageFreqDTCReal::fieldIn
 // (DTC/parallelStorageFreqDTC.cpp:21-30) regrouped over K steps.
+// The split form's DFT accumulators are float-float pairs (48-bit significands): the fold
+// adds its FP32 partial sums with FP32 TwoSum arithmetic instead of FP64 adds, which the
+// GB300's FP64 rate (1/64 of FP32) made a third of the fold's issue time.
+template <typename T>
+constexpr bool kFloatFloatAcc = sizeof(T) == 4;
+
 template <typename T>
 struct DftTable {
     long long npts;
@@ -191,7 +197,9 @@ struct DftTable {
     const int* cell;            // per point (grid index)
     const T* phasor;            // [(sample * 2 + {0: cos, 1: -sin}) * nfreqPad + f]
     T* ring;                    // [K][stride]
-    double* re;                 // [pt * nfreq + f]
+    // [pt * nfreq + f], 8 bytes per value: FP64 in the FP64 form; in the split form a
+    // float-float pair (hi, lo) as a float2 (kFloatFloatAcc), summed on the FP32 pipe
+    double* re;
     double* im;
     unsigned int* err;          // error word: kErrNumeric for a sample that is not finite
 };

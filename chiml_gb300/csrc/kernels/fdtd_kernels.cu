@@ -702,6 +702,17 @@ __device__ __forceinline__ void lds4(const double* p, double v[4]) {
     v[3] = b.y;
 }
 
+// (hi, lo) + v with FP32 TwoSum arithmetic, renormalised: Dekker's double-length sum.
+__device__ __forceinline__ void ffAdd(float& hi, float& lo, float v) {
+    const float s = hi + v;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (v - bb);
+    const float l2 = lo + err;
+    const float h = s + l2;
+    lo = l2 - (h - s);
+    hi = h;
+}
+
 // Staggered folds. The point tiles of a table are split into G = K / kFoldStagger
 // groups (point tile q belongs to group q mod G), and every kFoldStagger-th sample one
 // group folds: group g folds at the samples n with n + 1 = (g + 1 + m G) kFoldStagger,
@@ -795,8 +806,18 @@ __device__ __forceinline__ void foldTile(const DftTable<T>& d, long long p0, int
         for (int m = 0; m < 4; ++m) {
             const int f = f0 + 4 * tf + m;
             if (f >= nf) continue;
-            d.re[p * nf + f] += static_cast<double>(are[j][m]);
-            d.im[p * nf + f] += static_cast<double>(aim[j][m]);
+            if constexpr (kFloatFloatAcc<T>) {
+                float2* r = reinterpret_cast<float2*>(d.re) + p * nf + f;
+                float2* q = reinterpret_cast<float2*>(d.im) + p * nf + f;
+                float2 a = *r, b = *q;
+                ffAdd(a.x, a.y, static_cast<float>(are[j][m]));
+                ffAdd(b.x, b.y, static_cast<float>(aim[j][m]));
+                *r = a;
+                *q = b;
+            } else {
+                d.re[p * nf + f] += static_cast<double>(are[j][m]);
+                d.im[p * nf + f] += static_cast<double>(aim[j][m]);
+            }
         }
     }
 }

@@ -29,9 +29,10 @@ struct FluxFaceDev {
 
 // Integrated flux of every face: out[f * nFaces + face] (host memory layout of the writer).
 // faces and tiles ({face, s0, s1, unused}) are device arrays; partial holds
-// nTiles * nfreq values; re / im are the accumulators [point][freq].
+// nTiles * nfreq values; re / im are the accumulators [point][freq], FP64 or (pairs)
+// float-float pairs in the same 8 bytes.
 void launch_flux_faces(const FluxFaceDev* faces, int nFaces, const int4* tiles, int nTiles, int nfreq, const double* re,
-                       const double* im, double nt2, double2* partial, double2* out, void* stream);
+                       const double* im, bool pairs, double nt2, double2* partial, double2* out, void* stream);
 
 }  // namespace dev
 }  // namespace chiml

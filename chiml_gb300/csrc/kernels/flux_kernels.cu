@@ -14,15 +14,22 @@ namespace dev {
 
 namespace {
 
+// One accumulator value: FP64, or a float-float pair (hi, lo) in the same 8 bytes.
+__device__ __forceinline__ double accValue(const double* __restrict__ a, long long idx, bool ff) {
+    if (!ff) return a[idx];
+    const float2 v = reinterpret_cast<const float2*>(a)[idx];
+    return static_cast<double>(v.x) + static_cast<double>(v.y);
+}
+
 __device__ __forceinline__ double2 gridValue(const FluxFaceDev& F, int w, int s, int ff, int nfreq, const double* __restrict__ re,
-                                             const double* __restrict__ im) {
+                                             const double* __restrict__ im, bool pairs) {
     double2 g = make_double2(0.0, 0.0);
     const long long k1 = F.start[w][s + 1];
     for (long long k = F.start[w][s]; k < k1; ++k) {
         const long long idx = F.pt[w][k] * nfreq + ff;
         const double sc = F.scale[w][k];
-        g.x += sc * re[idx];
-        g.y += sc * im[idx];
+        g.x += sc * accValue(re, idx, pairs);
+        g.y += sc * accValue(im, idx, pairs);
     }
     return g;
 }
@@ -34,7 +41,7 @@ __device__ __forceinline__ double2 mulConjDiv(double2 a, double2 b, double d) {
 
 __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(const FluxFaceDev* __restrict__ faces, const int4* __restrict__ tiles,
                                                                int nfreq, const double* __restrict__ re, const double* __restrict__ im,
-                                                               double nt2, double2* __restrict__ partial) {
+                                                               bool pairs, double nt2, double2* __restrict__ partial) {
     const int ff = blockIdx.y * kFluxThreads + threadIdx.x;
     if (ff >= nfreq) return;
     const int4 t = tiles[blockIdx.x];
@@ -42,9 +49,11 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(const FluxFaceDev
     double2 acc = make_double2(0.0, 0.0);
     for (int s = t.y; s < t.z; ++s) {
         double2 v = make_double2(0.0, 0.0);
-        if (F.has[0]) v = mulConjDiv(gridValue(F, 0, s, ff, nfreq, re, im), gridValue(F, 3, s, ff, nfreq, re, im), nt2);
+        if (F.has[0])
+            v = mulConjDiv(gridValue(F, 0, s, ff, nfreq, re, im, pairs), gridValue(F, 3, s, ff, nfreq, re, im, pairs), nt2);
         if (F.has[1]) {
-            const double2 u = mulConjDiv(gridValue(F, 1, s, ff, nfreq, re, im), gridValue(F, 2, s, ff, nfreq, re, im), nt2);
+            const double2 u =
+                mulConjDiv(gridValue(F, 1, s, ff, nfreq, re, im, pairs), gridValue(F, 2, s, ff, nfreq, re, im, pairs), nt2);
             v.x -= u.x;
             v.y -= u.y;
         }
@@ -73,12 +82,12 @@ __global__ void k_flux_sum(const FluxFaceDev* __restrict__ faces, int nFaces, in
 }  // namespace
 
 void launch_flux_faces(const FluxFaceDev* faces, int nFaces, const int4* tiles, int nTiles, int nfreq, const double* re,
-                       const double* im, double nt2, double2* partial, double2* out, void* stream) {
+                       const double* im, bool pairs, double nt2, double2* partial, double2* out, void* stream) {
     if (nFaces == 0 || nfreq == 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (nTiles > 0) {
         const dim3 grid(static_cast<unsigned>(nTiles), static_cast<unsigned>((nfreq + kFluxThreads - 1) / kFluxThreads));
-        k_flux_partial<<<grid, kFluxThreads, 0, s>>>(faces, tiles, nfreq, re, im, nt2, partial);
+        k_flux_partial<<<grid, kFluxThreads, 0, s>>>(faces, tiles, nfreq, re, im, pairs, nt2, partial);
     }
     const int n = nFaces * nfreq;
     k_flux_sum<<<(n + 127) / 128, 128, 0, s>>>(faces, nFaces, nfreq, partial, out);
