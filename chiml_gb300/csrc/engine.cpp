@@ -534,17 +534,17 @@ private:
                     if (dx + lx * (dz + lz * dy) == off) return dx + pitch_ * (dz + lz * dy);
         throw InputError("neighbour offset of more than one cell");
     }
-    // A whole-grid array of the plan in the device layout; the padding holds `fill`.
-    template <typename V>
-    std::vector<V> padGrid(const std::vector<V>& v, V fill) const {
+    // A whole-grid byte array of the plan, copied row by row into the device layout (rows of
+    // pitch_ values, the padding zero).
+    const uint8_t* uploadPadded(const std::vector<uint8_t>& v) {
         const Dims& D = P.dims;
         if (static_cast<long long>(v.size()) != D.cells()) throw InputError("grid array of the wrong size");
-        std::vector<V> o(static_cast<std::size_t>(cellsPad_), fill);
-        const long long rows = static_cast<long long>(D.ly) * D.lz;
-#pragma omp parallel for schedule(static)
-        for (long long r = 0; r < rows; ++r)
-            for (int x = 0; x < D.lx; ++x) o[static_cast<std::size_t>(r * pitch_ + x)] = v[static_cast<std::size_t>(r * D.lx + x)];
-        return o;
+        uint8_t* d = mem_.alloc<uint8_t>(static_cast<std::size_t>(cellsPad_));
+        ck(cudaMemcpy2D(d, static_cast<std::size_t>(pitch_), v.data(), static_cast<std::size_t>(D.lx), static_cast<std::size_t>(D.lx),
+                        static_cast<std::size_t>(D.ly) * D.lz, cudaMemcpyHostToDevice),
+           "cudaMemcpy2D H2D");
+        mem_.h2d += static_cast<double>(v.size());
+        return d;
     }
 
     void launchTfsf(const dev::TfsfDev& t, void* s) {
@@ -985,12 +985,15 @@ private:
                 }
                 if (!anyUse) continue;  // empty slab: no a satisfies a < 0 or a >= L
                 int lo = 0, hi = L;
+                const uint8_t* code = cp.code.data();
+                const int ax = tp.axis;
+#pragma omp parallel for schedule(static) reduction(max : lo) reduction(min : hi)
                 for (int y = 0; y < D.ly; ++y)
                     for (int z = 0; z < D.lz; ++z) {
                         const long long row = static_cast<long long>(D.lx) * (z + static_cast<long long>(D.lz) * y);
                         for (int x = 0; x < D.lx; ++x) {
-                            if (!uses[cp.code[row + x]]) continue;
-                            const int a = tp.axis == 0 ? x : (tp.axis == 1 ? y : z);
+                            if (!uses[code[row + x]]) continue;
+                            const int a = ax == 0 ? x : (ax == 1 ? y : z);
                             if (2 * a < L) lo = std::max(lo, a + 1);
                             else hi = std::min(hi, a);
                         }
@@ -1138,7 +1141,7 @@ private:
                 dc.present = 1;
                 dc.U = fields_.f[c];
                 dc.D = (c < 3) ? fields_.f[6 + c] : nullptr;
-                dc.code = mem_.upload(padGrid(cp.code, static_cast<uint8_t>(0)));
+                dc.code = uploadPadded(cp.code);
                 std::vector<dev::Class<T>> cls(cp.classes.size());
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
