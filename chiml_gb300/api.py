@@ -50,7 +50,7 @@ class Stats(ctypes.Structure):
         ("bytes_per_cell_update", ctypes.c_double),
         ("device_bytes", ctypes.c_double),
         ("kernels_per_step", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("persistent", ctypes.c_int32),
         ("bytes_h_pass", ctypes.c_double),
         ("bytes_e_pass", ctypes.c_double),
         ("bytes_dft", ctypes.c_double),
@@ -86,6 +86,7 @@ EXPORTED = [
     "chiml_batch_finalize",
     "chiml_batch_member",
     "chiml_batch_destroy",
+    "chiml_barrier_selftest",
 ]
 
 BOX_NOALLOC_MAX_CELLS = 1048576
@@ -137,9 +138,21 @@ def load_library(path=None):
     lib.chiml_batch_member.restype = ctypes.c_void_p
     lib.chiml_batch_destroy.argtypes = [ctypes.c_void_p]
     lib.chiml_batch_destroy.restype = None
+    lib.chiml_barrier_selftest.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double]
+    lib.chiml_barrier_selftest.restype = ctypes.c_int
     if path is None:
         _lib = lib
     return lib
+
+
+def barrier_selftest(device=0, blocks=8, missing=0, limit_seconds=0.2):
+    """Runs the persistent step's grid barrier alone (chiml_barrier_selftest); returns the
+    status code: 0 when every block arrived, 6 (CHIML_E_TIMEOUT) when the wait gave up."""
+    lib = load_library()
+    st = lib.chiml_barrier_selftest(int(device), int(blocks), int(missing), float(limit_seconds))
+    if st not in (0, 6):
+        raise ChimlError(st, lib.chiml_last_error(None).decode())
+    return st
 
 
 class Simulation:

@@ -142,6 +142,7 @@ constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class ta
 constexpr unsigned int kErrPoleCount = 2u;   // a class asks for more poles than its component stores
 constexpr unsigned int kErrSlab = 4u;        // a class uses a CPML term outside its term's slab bounds
 constexpr unsigned int kErrNumeric = 8u;     // a sampled field value (detector or DFT point) is NaN or Inf
+constexpr unsigned int kErrTimeout = 16u;    // a grid barrier of the persistent 2-D kernel gave up waiting
 
 template <typename T>
 struct Fields {
@@ -248,6 +249,29 @@ struct StepTail {
     int blocks;              // recBlocks + the sample blocks of every table (at least 1)
 };
 
+// Persistent form of a small 2-D grid: one cooperative launch runs several whole steps
+// (H pass, E pass with the soft sources, detector records and DFT samples), the blocks
+// meeting at a grid barrier between the passes. Eligible grids: the 2-D interior form,
+// no TFSF, emitters or oriented dipoles, dispersive cells only where the pass updates them
+// inline, soft sources only on E cells that the pass writes plainly (at most
+// kPersistMaxSrc entries), DFT tables sampled every step (so that a group fold falls at
+// the end of every fourth step, where the launch ends and the fold kernel runs).
+constexpr int kPersistMaxSrc = 64;
+
+template <typename T>
+struct Persist2d {
+    Pass<T> h, e;
+    SourceTable src;         // E-component entries only
+    RecordTable rec;
+    const DftTable<T>* dft;  // [nDft] (device)
+    int nDft;
+    long long dftPoints;     // points over every table
+    Fields<T> f;
+    int* step;               // the step counter, written at the end of the launch
+    unsigned int* bar;       // barrier arrivals, zero at launch
+    unsigned long long limitNs;  // longest wait at a barrier
+};
+
 // Launchers (fdtd_kernels.cu). All run on the given stream.
 template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream);
@@ -297,6 +321,18 @@ void launch_dft_sample_packed(const DftJob<T>* jobs, WorkMap m, void* stream);
 template <typename T>
 void launch_dft_fold_packed(const DftJob<T>* jobs, WorkMap m, void* stream);
 void launch_increment_packed(int* const* steps, int n, void* stream);
+
+// Blocks the persistent launch uses (resident on every SM at once), 0 when none fit.
+template <typename T>
+int persist2d_blocks(const Pass<T>& h, const Pass<T>& e, int device);
+// nsteps steps from step0 in one cooperative launch of `blocks` blocks (barrier counter
+// zeroed on the stream first). Returns the CUDA status of the launch.
+template <typename T>
+int launch_persist2d(const Persist2d<T>& a, int blocks, int step0, int nsteps, void* stream);
+// The grid barrier on its own: `blocks` cooperative blocks wait for blocks + missing
+// arrivals with the given limit; err receives kErrTimeout when the wait gives up.
+int launch_barrier_selftest(int blocks, int missing, unsigned long long limitNs, unsigned int* bar, unsigned int* err,
+                            void* stream);
 
 }  // namespace dev
 }  // namespace chiml

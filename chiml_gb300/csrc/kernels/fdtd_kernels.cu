@@ -347,9 +347,28 @@ __device__ __forceinline__ void cellTail(const Pass<T>& p, I i, uint8_t cd, T u,
     }
 }
 
-// D2: a 2-D grid (lz == 1), where the term along z is absent.
-template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false>
-__device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1) {
+// A soft source on one E cell in the persistent form: the E pass adds it to the cell's
+// field before the update, as the source launch would have (E + v, then the curl).
+template <typename T>
+struct PSrcCell {
+    int comp;
+    int cell;  // device layout index
+    T v;       // the source's value at the current step
+};
+
+// A field value written by another block of the same launch: loaded through L2 (the
+// persistent form reads its neighbours' fields after a grid barrier).
+template <bool COH, typename T>
+__device__ __forceinline__ T ldField(const T* p) {
+    if constexpr (COH) return __ldcg(p);
+    else return *p;
+}
+
+// D2: a 2-D grid (lz == 1), where the term along z is absent. COH: neighbour fields are
+// loaded through L2 and the soft sources ps[0 .. nps) are added (the persistent form).
+template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false, bool COH = false>
+__device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1, const PSrcCell<T>* ps = nullptr,
+                                          int nps = 0) {
     constexpr int A0 = (CI + 2) % 3;  // derivative axis of term J
     constexpr int A1 = (CI + 1) % 3;  // derivative axis of term K
     constexpr bool P0 = !(D2 && A0 == 2);  // term J present
@@ -389,7 +408,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
     }
     // field of the y term carried between planes: H holds G(y), E holds G(y-1)
     T carry = T(0);
-    if constexpr (TY >= 0) carry = EPASS ? c.G[TY][i - plane] : c.G[TY][i];
+    if constexpr (TY >= 0) carry = EPASS ? ldField<COH>(c.G[TY] + (i - plane)) : ldField<COH>(c.G[TY] + i);
 
 #pragma unroll kMarchUnroll
     for (int y = y0; y < y1; ++y, i += plane) {
@@ -401,35 +420,39 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
             if (P1) prefetchL2(G1 + ip);
         }
         const uint8_t cd = code[i];
-        const T u = U[i];
+        T u = U[i];
+        if constexpr (COH && EPASS) {
+            for (int k = 0; k < nps; ++k)
+                if (ps[k].comp == CI && ps[k].cell == static_cast<int>(i)) u += ps[k].v;
+        }
         T g[2] = {T(0), T(0)}, n[2] = {T(0), T(0)};
         if (TY == 0) {
             if (EPASS) {
-                g[0] = G0[i];
+                g[0] = ldField<COH>(G0 + i);
                 n[0] = carry;
                 carry = g[0];
             } else {
                 g[0] = carry;
-                n[0] = G0[i + plane];
+                n[0] = ldField<COH>(G0 + (i + plane));
                 carry = n[0];
             }
         } else if (P0) {
-            g[0] = G0[i];
-            n[0] = G0[i + off0];
+            g[0] = ldField<COH>(G0 + i);
+            n[0] = ldField<COH>(G0 + (i + off0));
         }
         if (TY == 1) {
             if (EPASS) {
-                g[1] = G1[i];
+                g[1] = ldField<COH>(G1 + i);
                 n[1] = carry;
                 carry = g[1];
             } else {
                 g[1] = carry;
-                n[1] = G1[i + plane];
+                n[1] = ldField<COH>(G1 + (i + plane));
                 carry = n[1];
             }
         } else if (P1) {
-            g[1] = G1[i];
-            n[1] = G1[i + off1];
+            g[1] = ldField<COH>(G1 + i);
+            n[1] = ldField<COH>(G1 + (i + off1));
         }
         bool in[2] = {inC[0], inC[1]};
         T kp[2] = {kpC[0], kpC[1]}, bq[2] = {bqC[0], bqC[1]}, cq[2] = {cqC[0], cqC[1]};
@@ -931,6 +954,198 @@ void launch_step_tail(const StepTail<T>& t, void* stream) {
     k_step_tail<T><<<static_cast<unsigned>(t.blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(t);
 }
 
+// ---- persistent form of small 2-D grids ----
+
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned int loadAcquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid barrier of a cooperative launch: every block adds one arrival to the counter and
+// waits until it reaches `target` (the arrivals of all barriers so far). The wait is
+// bounded: after limitNs, or once another block has given up, it sets kErrTimeout and
+// returns false, and the caller ends the launch. The fences before the arrival and after
+// the wait order every block's field writes before the other blocks' reads.
+__device__ bool gridBarrier(unsigned int* bar, unsigned int target, unsigned int* err, unsigned long long limitNs) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        __threadfence();
+        atomicAdd(bar, 1u);
+        const unsigned long long t0 = globalTimerNs();
+        while (loadAcquire(bar) < target) {
+            if (loadAcquire(err) & kErrTimeout) {
+                ok = 0;
+                break;
+            }
+            if (globalTimerNs() - t0 > limitNs) {
+                atomicOr(err, kErrTimeout);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Records and DFT samples of one component set (E and D, or H) at sample index `idx`, the
+// launch's threads striding over the record entries and then every table's points.
+template <typename T>
+__device__ void persistSamples(const Persist2d<T>& a, int idx, bool wantH) {
+    const long long nThreads = static_cast<long long>(gridDim.x) * blockDim.x;
+    const long long total = a.rec.n + a.dftPoints;
+    for (long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; j < total; j += nThreads) {
+        if (j < a.rec.n) {
+            const RecordTable& r = a.rec;
+            const int comp = r.comp[j];
+            if ((comp >= 3 && comp <= 5) != wantH) continue;
+            const int d = r.det[j];
+            const int ti = r.timeInt[d];
+            if (idx % ti != 0) continue;
+            const int ev = idx / ti;
+            if (ev >= r.nEvents[d]) continue;
+            const long long c = r.cell[j];
+            const double v = (c < 0) ? 0.0 : static_cast<double>(__ldcg(fieldOf(a.f, comp) + c));
+            r.rec[r.recBase[d] + static_cast<long long>(ev) * r.nvals[d] + r.outIndex[j]] = v;
+            if (!isfinite(v)) atomicOr(r.err, kErrNumeric);
+        } else {
+            long long pt = j - a.rec.n;
+            int q = 0;
+            while (q + 1 < a.nDft && pt >= a.dft[q].npts) pt -= a.dft[q++].npts;
+            const DftTable<T>& d = a.dft[q];
+            const int comp = d.comp[pt];
+            if ((comp >= 3 && comp <= 5) != wantH) continue;
+            if (idx % d.timeInt != 0) continue;
+            const int slot = (idx / d.timeInt) & (d.K - 1);
+            const T v = __ldcg(fieldOf(a.f, comp) + d.cell[pt]);
+            d.ring[static_cast<long long>(slot) * d.stride + pt] = v;
+            if (!isfinite(v)) atomicOr(d.err, kErrNumeric);
+        }
+    }
+}
+
+// One pass of the persistent form: the 2-D units (component, y-block, x-block) of the
+// pass, unit u on block u mod gridDim.x (the same block every step, so that each cell's
+// own field, psi and polarisations stay with one SM).
+template <typename T, bool EPASS, int CY>
+__device__ void persistPass(const Pass<T>& p, const PSrcCell<T>* ps, int nps) {
+    const int gx = pass2d_gx(p.lx), gy = pass2d_gy(p.ly, CY);
+    const int units = 3 * gx * gy;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int ci = u / (gx * gy), r = u % (gx * gy);
+        if (!p.c[ci].present) continue;
+        const int bx = r % gx, by = r / gx;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int xa = 1 + bx * 32, x = xa + lane;
+        const int y0 = 1 + (by * kP2W + w) * CY;
+        if (y0 > p.ly - 2 || x > p.lx - 2) continue;
+        const int y1 = min(y0 + CY, p.ly - 1);
+        const bool pml = blockTouchesSlab(p.c[ci], ci, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, 0, 0);
+#define CHIML_PERSIST_RUN(CIV)                                                                           \
+    if (pml) pass3dRun<T, EPASS, CIV, int, CY, 0, true, true, true>(p, x, 0, y0, y1, ps, nps);          \
+    else pass3dRun<T, EPASS, CIV, int, CY, 0, false, true, true>(p, x, 0, y0, y1, ps, nps);
+        if (ci == 0) {
+            CHIML_PERSIST_RUN(0)
+        } else if (ci == 1) {
+            CHIML_PERSIST_RUN(1)
+        } else {
+            CHIML_PERSIST_RUN(2)
+        }
+#undef CHIML_PERSIST_RUN
+    }
+}
+
+// nsteps whole steps from step0. Per step: the H pass, with the E-side samples of the
+// previous step (E is not written in the H pass); a barrier; the E pass with the sources,
+// with the H-side samples of this step (H is not written in the E pass); a barrier. The
+// E-side samples of the last step close the launch, which then sets the step counter.
+template <typename T, int CY>
+__global__ void __launch_bounds__(256) k_persist2d(const Persist2d<T> a, int step0, int nsteps) {
+    __shared__ PSrcCell<T> ps[kPersistMaxSrc];
+    const int nps = a.src.n < kPersistMaxSrc ? a.src.n : kPersistMaxSrc;
+    unsigned int target = 0;
+    for (int k = 0; k < nsteps; ++k) {
+        const int st = step0 + k;
+        persistPass<T, false, CY>(a.h, ps, 0);
+        if (k > 0) persistSamples(a, st, false);
+        target += gridDim.x;
+        if (!gridBarrier(a.bar, target, a.h.err, a.limitNs)) return;
+        // the sources of this step (their values were read before the first pass of the
+        // block; the list is rewritten only between the block's barriers)
+        for (int j = threadIdx.x; j < nps; j += blockDim.x)
+            ps[j] = PSrcCell<T>{a.src.comp[j], static_cast<int>(a.src.cell[j]),
+                                static_cast<T>(st < a.src.nSteps ? a.src.value[static_cast<long long>(a.src.src[j]) * a.src.nSteps + st] : 0.0)};
+        __syncthreads();
+        persistPass<T, true, CY>(a.e, ps, nps);
+        persistSamples(a, st + 1, true);
+        target += gridDim.x;
+        if (!gridBarrier(a.bar, target, a.h.err, a.limitNs)) return;
+    }
+    persistSamples(a, step0 + nsteps, false);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.step = step0 + nsteps;
+}
+
+constexpr int kPersistCY = 2;  // rows per warp of a persistent pass unit
+
+template <typename T>
+int persist2d_blocks(const Pass<T>& h, const Pass<T>& e, int device) {
+    int perSM = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_persist2d<T, kPersistCY>, 256, 0) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    // no more blocks than the larger pass has units
+    const int units = 3 * std::max(pass2d_gx(h.lx) * pass2d_gy(h.ly, kPersistCY), pass2d_gx(e.lx) * pass2d_gy(e.ly, kPersistCY));
+    return std::min(perSM * sms, units);
+}
+
+template <typename T>
+int launch_persist2d(const Persist2d<T>& a, int blocks, int step0, int nsteps, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return static_cast<int>(e);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(blocks));
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return static_cast<int>(cudaLaunchKernelEx(&cfg, k_persist2d<T, kPersistCY>, a, step0, nsteps));
+}
+
+__global__ void k_barrier_selftest(unsigned int* bar, unsigned int target, unsigned int* err, unsigned long long limitNs) {
+    gridBarrier(bar, target, err, limitNs);
+}
+
+int launch_barrier_selftest(int blocks, int missing, unsigned long long limitNs, unsigned int* bar, unsigned int* err,
+                            void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return static_cast<int>(e);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(blocks));
+    cfg.blockDim = dim3(32);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const unsigned int target = static_cast<unsigned int>(blocks + missing);
+    return static_cast<int>(cudaLaunchKernelEx(&cfg, k_barrier_selftest, bar, target, err, limitNs));
+}
+
 // ---- packed launches (batched sweep) ----
 
 template <typename T>
@@ -1094,6 +1309,10 @@ template void launch_sources<double>(const SourceTable&, const Fields<double>&, 
 template void launch_sources<float>(const SourceTable&, const Fields<float>&, const int*, void*);
 template void launch_step_tail<double>(const StepTail<double>&, void*);
 template void launch_step_tail<float>(const StepTail<float>&, void*);
+template int persist2d_blocks<double>(const Pass<double>&, const Pass<double>&, int);
+template int persist2d_blocks<float>(const Pass<float>&, const Pass<float>&, int);
+template int launch_persist2d<double>(const Persist2d<double>&, int, int, int, void*);
+template int launch_persist2d<float>(const Persist2d<float>&, int, int, int, void*);
 template void launch_record<double>(const RecordTable&, const Fields<double>&, const int*, void*);
 template void launch_record<float>(const RecordTable&, const Fields<float>&, const int*, void*);
 template void launch_dft_sample<double>(const DftTable<double>&, const Fields<double>&, const int*, void*);

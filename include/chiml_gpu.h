@@ -29,7 +29,7 @@ typedef enum chiml_status {
     CHIML_E_CUDA = 3,        /* a CUDA runtime error */
     CHIML_E_OOM = 4,         /* device memory exhausted */
     CHIML_E_NUMERIC = 5,     /* a detector or flux/DFT point sampled a NaN or Inf field value */
-    CHIML_E_TIMEOUT = 6,     /* reserved: no kernel of this engine spins on a flag or barrier */
+    CHIML_E_TIMEOUT = 6,     /* a grid barrier of the persistent 2-D step gave up waiting */
     CHIML_E_STATE = 7        /* call out of order (e.g. step after finalize), or a device-side
                                 bounds check of the plan failed */
 } chiml_status;
@@ -55,8 +55,9 @@ typedef struct chiml_stats {
     int32_t precision;
     double bytes_per_cell_update;  /* algorithmic HBM bytes per physical cell per step */
     double device_bytes;           /* device memory held by the handle */
-    int32_t kernels_per_step;      /* kernel launches per step */
-    int32_t reserved;
+    int32_t kernels_per_step;      /* kernel launches per step (of the launch-per-kernel form) */
+    int32_t persistent;            /* 1: chiml_step runs the persistent 2-D form (cooperative launches
+                                      of several steps; see chiml_barrier_selftest) */
     double bytes_h_pass;           /* algorithmic HBM bytes of one H-pass launch */
     double bytes_e_pass;           /* algorithmic HBM bytes of one E-pass launch */
     double bytes_dft;              /* algorithmic HBM bytes of the DFT launches of one sampled step */
@@ -169,6 +170,16 @@ void chiml_batch_destroy(chiml_batch* batch);
  * overlap on the GPU (handles of one device used from several host threads at
  * once) race on the array. */
 chiml_status chiml_get_box_noalloc(chiml_sim* sim, int comp, const int32_t box[6], double* out);
+
+/* Small 2-D grids can step in a persistent form (opt-in: CHIML_PERSIST2D=1 in the
+ * environment at chiml_create): one cooperative launch runs several steps, its blocks
+ * meeting at grid barriers whose waits are limited to one second; a wait that gives up
+ * ends the launch and the next chiml_sync / chiml_finalize returns CHIML_E_TIMEOUT. This diagnostic runs that barrier alone: `blocks` cooperative blocks
+ * of 32 threads on `device` (at most one per SM) wait for blocks + missing arrivals, each
+ * wait limited to limit_seconds (clamped to 1 ms .. 5 s). CHIML_OK when every block
+ * arrived; CHIML_E_TIMEOUT when the wait gave up (missing > 0). The device stays usable
+ * either way; chiml_last_error(NULL) holds the reason of any other failure. */
+chiml_status chiml_barrier_selftest(int device, int blocks, int missing, double limit_seconds);
 
 #ifdef __cplusplus
 }
