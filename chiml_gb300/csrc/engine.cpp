@@ -12,6 +12,7 @@
 #include <memory>
 #include <mutex>
 #include <numeric>
+#include <parallel/algorithm>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -1433,16 +1434,20 @@ private:
     std::vector<std::vector<int>> dftPos_;
 
     dev::DftTable<T> makeDft(const std::vector<int>& comp0, const std::vector<int>& cell0, const std::vector<double>& freqs, int ti) {
-        std::vector<int> order(cell0.size());
-        std::iota(order.begin(), order.end(), 0);
-        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-            return comp0[a] != comp0[b] ? comp0[a] < comp0[b] : cell0[a] < cell0[b];
-        });
+        // (component, cell, plan index) keys: unique, so that the parallel sort gives the
+        // order of a stable sort by (component, cell)
+        const long long npt = static_cast<long long>(cell0.size());
+        std::vector<std::pair<std::pair<int, int>, int>> key(cell0.size());
+#pragma omp parallel for schedule(static)
+        for (long long k = 0; k < npt; ++k) key[static_cast<std::size_t>(k)] = {{comp0[k], cell0[k]}, static_cast<int>(k)};
+        __gnu_parallel::sort(key.begin(), key.end());
         std::vector<int> comp(cell0.size()), cell(cell0.size()), pos(cell0.size());
-        for (std::size_t k = 0; k < order.size(); ++k) {
-            comp[k] = comp0[order[k]];
-            cell[k] = cell0[order[k]];
-            pos[order[k]] = static_cast<int>(k);
+#pragma omp parallel for schedule(static)
+        for (long long k = 0; k < npt; ++k) {
+            const std::size_t q = static_cast<std::size_t>(k);
+            comp[q] = key[q].first.first;
+            cell[q] = key[q].first.second;
+            pos[static_cast<std::size_t>(key[q].second)] = static_cast<int>(k);
         }
         dftPos_.push_back(std::move(pos));
         dev::DftTable<T> d{};
@@ -1451,6 +1456,7 @@ private:
             const int nSamples = P.nSteps / ti + 1;
             const int nfPad = (nf + 31) / 32 * 32;
             std::vector<T> ph(static_cast<std::size_t>(nSamples) * nfPad * 2, T(0));
+#pragma omp parallel for schedule(static)
             for (int n = 0; n < nSamples; ++n)
                 for (int f = 0; f < nf; ++f) {
                     std::complex<double> e = std::exp(std::complex<double>(0.0, -1.0 * P.tcur[static_cast<std::size_t>(n) * ti] * freqs[f]));

@@ -69,7 +69,8 @@ struct Field3 {
     Dims d;
     Buf<T> v;
     Field3() {}
-    Field3(const Dims& dd, T init) : d(dd), v(filled<T>(static_cast<std::size_t>(dd.cells()), init, omp_get_max_threads())) {}
+    Field3(const Dims& dd, T init, int threads = 0)
+        : d(dd), v(filled<T>(static_cast<std::size_t>(dd.cells()), init, threads > 0 ? threads : omp_get_max_threads())) {}
     T& at(int x, int y, int z) { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
     T at(int x, int y, int z) const { return v[static_cast<std::size_t>(d.idx(x, y, z))]; }
 };
@@ -78,6 +79,35 @@ struct Field3 {
 // (Ex,Ey,Ez,Hx,Hy,Hz) belongs to a set given as a bit mask.
 constexpr int bEX = 1, bEY = 2, bEZ = 4, bHX = 8, bHY = 16, bHZ = 32;
 inline bool inSet(int comp, int mask) { return (mask >> comp) & 1; }
+
+// Nested OpenMP teams for the duration of a scope (an outer loop over independent parts,
+// each with its own inner team). Both settings are read before either is changed: in
+// libgomp omp_set_nested(1) raises max-active-levels to its maximum and omp_set_nested(0)
+// drops it to 1, so the switch is set first and the level count after it, and on the way
+// out the switch is restored first and the level count last. Older runtimes (a host
+// application may bring its own) also gate nesting on the OpenMP 3 switch.
+class NestedTeams {
+public:
+    NestedTeams() {
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
+        prevNested_ = omp_get_nested();
+        prevLevels_ = omp_get_max_active_levels();
+        omp_set_nested(1);
+#pragma GCC diagnostic pop
+        omp_set_max_active_levels(std::max(prevLevels_, 2));
+    }
+    ~NestedTeams() {
+#pragma GCC diagnostic push
+#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
+        omp_set_nested(prevNested_);
+#pragma GCC diagnostic pop
+        omp_set_max_active_levels(prevLevels_);
+    }
+
+private:
+    int prevNested_ = 0, prevLevels_ = 1;
+};
 
 struct Builder {
     const Inputs& in;
@@ -184,9 +214,9 @@ struct Builder {
     }
 
     // setupPhysFields, parallelFDTDField.hpp:867-947
-    void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff) {
-        Field3<int> ph(D, 0);
-        Field3<double> ep(D, 1.0);
+    void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff, int threads) {
+        Field3<int> ph(D, 0, threads);
+        Field3<double> ep(D, 1.0, threads);
         const bool twoD = (D.lz == 1);
         int zmin = twoD ? 0 : 1;
         int zmax = twoD ? 1 : D.lz - 1;
@@ -203,7 +233,7 @@ struct Builder {
             // without an emitter buffer both tests are the same test
             const bool sameGeo = o.geoML == o.geo;
             const double epsHere = E ? o.epsInf : 1.0;
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
             for (int jj = j0; jj < j1; ++jj)
                 for (int ii = i0; ii < i1; ++ii)
                     for (int kk = k0; kk < k1; ++kk) {
@@ -1018,38 +1048,59 @@ struct Builder {
         od.present = true;
         od.nPoles = np;
         const Field3<int>& ph = phys[6];
-        for (int jj = 1; jj < D.ly - 1; ++jj)
-            for (int kk = 1; kk < D.lz - 1; ++kk)
-                for (int ii = 1; ii < D.lx - 1; ++ii) {
-                    const int o = ph.at(ii, jj, kk);
-                    if (o < 0) throw InputError("oriented-dipole list reaches a border cell");
-                    const Object& ob = objs[o];
-                    if (!(ob.orDip && ob.gamma.size() > 0)) continue;
-                    od.cells.push_back(D.idx(ii, jj, kk));
-                    od.obj.push_back(o);
-                    for (int pp = 0; pp < np; ++pp) {
-                        std::array<double, 3> dv = {0.0, 0.0, 0.0};
-                        if (pp < static_cast<int>(ob.dipOr.size())) {
-                            const DipOr dor = ob.dipOr[pp];
-                            if (dor == DipOr::ISOTROPIC) {
-                                dv = {1.0, 1.0, 1.0};
-                            } else if (dor == DipOr::UNIDIRECTIONAL) {
-                                dv = ob.dipE[pp];
-                            } else if (dor == DipOr::REL_TO_NORM) {
-                                const std::array<double, 3> pt = {((ii - 1) - (nvec[0] - nvec[0] % 2) / 2.0) * d[0],
-                                                                  ((jj - 1) - (nvec[1] - nvec[1] % 2) / 2.0) * d[1],
-                                                                  ((kk - 1) - (nvec[2] - nvec[2] % 2) / 2.0) * d[2]};
-                                const std::array<double, 3> n = ob.gradient(pt);
-                                const std::array<double, 3>& w = ob.dipW[static_cast<std::size_t>(pp)];
-                                const std::array<double, 3> tan = tangentDip(n, w[1], w[2]);
-                                for (int c = 0; c < 3; ++c) dv[c] = w[0] * n[c] + tan[c];
+        // rows of y in parallel, concatenated in y order (the reference's list order);
+        // the first error in that order is the one reported
+        const int rows = std::max(0, D.ly - 2);
+        std::vector<std::vector<long long>> rCells(static_cast<std::size_t>(rows));
+        std::vector<std::vector<int>> rObj(static_cast<std::size_t>(rows));
+        std::vector<std::vector<std::array<double, 3>>> rDip(static_cast<std::size_t>(rows));
+        std::vector<std::exception_ptr> rErr(static_cast<std::size_t>(rows));
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int jj = 1; jj < D.ly - 1; ++jj) {
+            const std::size_t r = static_cast<std::size_t>(jj - 1);
+            try {
+                for (int kk = 1; kk < D.lz - 1; ++kk)
+                    for (int ii = 1; ii < D.lx - 1; ++ii) {
+                        const int o = ph.at(ii, jj, kk);
+                        if (o < 0) throw InputError("oriented-dipole list reaches a border cell");
+                        const Object& ob = objs[o];
+                        if (!(ob.orDip && ob.gamma.size() > 0)) continue;
+                        rCells[r].push_back(D.idx(ii, jj, kk));
+                        rObj[r].push_back(o);
+                        for (int pp = 0; pp < np; ++pp) {
+                            std::array<double, 3> dv = {0.0, 0.0, 0.0};
+                            if (pp < static_cast<int>(ob.dipOr.size())) {
+                                const DipOr dor = ob.dipOr[pp];
+                                if (dor == DipOr::ISOTROPIC) {
+                                    dv = {1.0, 1.0, 1.0};
+                                } else if (dor == DipOr::UNIDIRECTIONAL) {
+                                    dv = ob.dipE[pp];
+                                } else if (dor == DipOr::REL_TO_NORM) {
+                                    const std::array<double, 3> pt = {((ii - 1) - (nvec[0] - nvec[0] % 2) / 2.0) * d[0],
+                                                                      ((jj - 1) - (nvec[1] - nvec[1] % 2) / 2.0) * d[1],
+                                                                      ((kk - 1) - (nvec[2] - nvec[2] % 2) / 2.0) * d[2]};
+                                    const std::array<double, 3> n = ob.gradient(pt);
+                                    const std::array<double, 3>& w = ob.dipW[static_cast<std::size_t>(pp)];
+                                    const std::array<double, 3> tan = tangentDip(n, w[1], w[2]);
+                                    for (int c = 0; c < 3; ++c) dv[c] = w[0] * n[c] + tan[c];
+                                }
+                                // the lat_tangent and long_tangent forms leave the reference's
+                                // dipole grid at zero (setupDipMoments has no branch for them)
                             }
-                            // the lat_tangent and long_tangent forms leave the reference's
-                            // dipole grid at zero (setupDipMoments has no branch for them)
+                            rDip[r].push_back(dv);
                         }
-                        od.dip.push_back(dv);
                     }
-                }
+            } catch (...) {
+                rErr[r] = std::current_exception();
+            }
+        }
+        for (int r = 0; r < rows; ++r) {
+            if (rErr[static_cast<std::size_t>(r)]) std::rethrow_exception(rErr[static_cast<std::size_t>(r)]);
+            const std::size_t q = static_cast<std::size_t>(r);
+            od.cells.insert(od.cells.end(), rCells[q].begin(), rCells[q].end());
+            od.obj.insert(od.obj.end(), rObj[q].begin(), rObj[q].end());
+            od.dip.insert(od.dip.end(), rDip[q].begin(), rDip[q].end());
+        }
         // E_c at the cell and one cell below along c enter the averaged dot product
         od.offA[0] = 1;
         od.offA[1] = static_cast<long long>(D.lx) * D.lz;
@@ -1080,13 +1131,35 @@ struct Builder {
             P.tcur[s] = t;
             t += dt;
         }
-        setupPhys(6, true, {0.0, 0.0, 0.0}, {0, 0, 0});
-        setupPhys(0, true, {0.5, 0.0, 0.0}, {1, 0, 0});
-        setupPhys(1, true, {0.0, 0.5, 0.0}, {0, 1, 0});
-        setupPhys(2, true, {0.0, 0.0, 0.5}, {0, 0, 1});
-        setupPhys(3, false, {0.0, 0.5, 0.5}, {0, 1, 1});
-        setupPhys(4, false, {0.5, 0.0, 0.5}, {1, 0, 1});
-        setupPhys(5, false, {0.5, 0.5, 0.0}, {1, 1, 0});
+        // the seven material grids are independent: built concurrently, each with its
+        // share of the threads
+        {
+            struct GridSpec {
+                int g;
+                bool E;
+                std::array<double, 3> off;
+                std::array<int, 3> end;
+            };
+            const GridSpec grids[7] = {{6, true, {0.0, 0.0, 0.0}, {0, 0, 0}}, {0, true, {0.5, 0.0, 0.0}, {1, 0, 0}},
+                                       {1, true, {0.0, 0.5, 0.0}, {0, 1, 0}}, {2, true, {0.0, 0.0, 0.5}, {0, 0, 1}},
+                                       {3, false, {0.0, 0.5, 0.5}, {0, 1, 1}}, {4, false, {0.5, 0.0, 0.5}, {1, 0, 1}},
+                                       {5, false, {0.5, 0.5, 0.0}, {1, 1, 0}}};
+            const int nThreads = omp_get_max_threads();
+            const int outer = std::min(7, nThreads);
+            const int inner = std::max(1, nThreads / outer);
+            std::exception_ptr gErr[7];
+            NestedTeams nest;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(outer)
+            for (int q = 0; q < 7; ++q) {
+                try {
+                    setupPhys(grids[q].g, grids[q].E, grids[q].off, grids[q].end, inner);
+                } catch (...) {
+                    gErr[q] = std::current_exception();
+                }
+            }
+            for (int q = 0; q < 7; ++q)
+                if (gErr[q]) std::rethrow_exception(gErr[q]);
+        }
         clk.mark("materials");
         // a barycentric test whose weights do not sum to one (Obj.cpp:485-489, 502-506)
         for (const auto& o : objs)
@@ -1123,33 +1196,18 @@ struct Builder {
         for (int c = 0; c < 6; ++c) nComp += present[c] ? 1 : 0;
         const int nThreads = omp_get_max_threads();
         innerThreads_ = std::max(1, nThreads / std::max(1, nComp));
-        // Both settings are read before either is changed: in libgomp omp_set_nested(1)
-        // raises max-active-levels to its maximum and omp_set_nested(0) drops it to 1, so
-        // the switch is set first and the level count after it, and on the way out the
-        // switch is restored first and the level count last.
-#pragma GCC diagnostic push
-#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
-        const int prevNested = omp_get_nested();
-        const int prevLevels = omp_get_max_active_levels();
-        // older runtimes (a host application may bring its own) also gate nesting on the
-        // OpenMP 3 switch
-        omp_set_nested(1);
-#pragma GCC diagnostic pop
-        omp_set_max_active_levels(std::max(prevLevels, 2));
+        {
+            NestedTeams nest;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(std::min(nThreads, std::max(1, nComp)))
-        for (int q = 0; q < 6; ++q) {
-            if (!present[order[q]]) continue;
-            try {
-                buildComp(order[q]);
-            } catch (...) {
-                err[q] = std::current_exception();
+            for (int q = 0; q < 6; ++q) {
+                if (!present[order[q]]) continue;
+                try {
+                    buildComp(order[q]);
+                } catch (...) {
+                    err[q] = std::current_exception();
+                }
             }
         }
-#pragma GCC diagnostic push
-#pragma GCC diagnostic ignored "-Wdeprecated-declarations"
-        omp_set_nested(prevNested);
-#pragma GCC diagnostic pop
-        omp_set_max_active_levels(prevLevels);
         for (int q = 0; q < 6; ++q)
             if (err[q]) std::rethrow_exception(err[q]);
         clk.mark("components");

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <parallel/algorithm>
 
 #include "plan.hpp"
 
@@ -114,7 +115,9 @@ struct TfsfBuilder {
             if (std::abs(std::tan(psi)) > 1) psiP = M_PI / 2.0 - psiP;
             if (t.circPol == Pol::R) alpha *= -1.0;
         }
+        PhaseClock clk0;
         checkVacuumSurfaces();
+        clk0.mark("tfsf-vacuum");
 
         T.m = m;
         T.mTot = mTot;
@@ -148,13 +151,23 @@ struct TfsfBuilder {
         // surfaces (parallelTFSF.hpp:332-340)
         const bool pl = (theta == 0 || ((theta == M_PI / 2.0 && std::abs(quadrant) == 4) || std::abs(quadrant) == 1)) ? false : true;
         std::vector<SurfaceTerm> hTerms, eTerms;
+        {
+            // at most two terms per component and surface cell: room for all of them
+            const std::size_t area = 2 * (static_cast<std::size_t>(sz[0]) * sz[1] + static_cast<std::size_t>(sz[1]) * sz[2] +
+                                          static_cast<std::size_t>(sz[0]) * sz[2]);
+            hTerms.reserve(6 * area);
+            eTerms.reserve(6 * area);
+        }
+        PhaseClock clk;
         segs = &T.segH;
         for (int i = 0; i < 3; ++i) addStructs(3 + i, false, pl, hTerms);
         segs = &T.segE;
         for (int i = 0; i < 3; ++i) addStructs(i, true, pl, eTerms);
         segs = nullptr;
+        clk.mark("tfsf-surfaces");
         gather(hTerms, T.addH);
         gather(eTerms, T.addE);
+        clk.mark("tfsf-gather");
         // the lines' CPMLs (parallelTFSF.hpp:342-378)
         for (int c = 0; c < 6; ++c) {
             if (!T.line[c].present) continue;
@@ -481,37 +494,34 @@ struct TfsfBuilder {
         return loc[cor] + s[cor] - (surLocC - 1) - fieldEnd;
     }
 
-    // Terms grouped by main cell, cells in order of their first term.
+    // Terms grouped by main cell (component, cell), each cell's terms in the order they
+    // were made (a cell's corrections are summed in that order); cells in key order, which
+    // no result depends on (each cell's sum is its own).
     void gather(const std::vector<SurfaceTerm>& terms, TfsfAdds& out) const {
-        std::vector<long long> k(terms.size());
-        for (std::size_t q = 0; q < terms.size(); ++q) k[q] = terms[q].comp * D.cells() + terms[q].cell;
-        std::vector<std::size_t> order(terms.size());
-        std::iota(order.begin(), order.end(), 0);
-        std::stable_sort(order.begin(), order.end(), [&](std::size_t a, std::size_t b) { return k[a] < k[b]; });
-        std::vector<std::pair<std::size_t, std::size_t>> groups;  // (first term index, position in order)
-        for (std::size_t p = 0; p < order.size(); ++p)
-            if (p == 0 || k[order[p]] != k[order[p - 1]]) groups.push_back({order[p], p});
-        std::sort(groups.begin(), groups.end());
+        const std::size_t n = terms.size();
+        std::vector<std::pair<long long, long long>> kv(n);  // (key, term index): unique pairs
+#pragma omp parallel for schedule(static)
+        for (long long q = 0; q < static_cast<long long>(n); ++q)
+            kv[static_cast<std::size_t>(q)] = {terms[static_cast<std::size_t>(q)].comp * D.cells() + terms[static_cast<std::size_t>(q)].cell, q};
+        __gnu_parallel::sort(kv.begin(), kv.end());
         out = TfsfAdds();
-        out.cell.reserve(groups.size());
-        out.comp.reserve(groups.size());
-        out.start.reserve(groups.size() + 1);
-        out.line.reserve(terms.size());
-        out.incd.reserve(terms.size());
-        out.pref.reserve(terms.size());
-        out.toD.reserve(terms.size());
-        for (auto& g : groups) {
-            out.cell.push_back(terms[g.first].cell);
-            out.comp.push_back(terms[g.first].comp);
-            for (std::size_t p = g.second; p < order.size() && k[order[p]] == k[g.first]; ++p) {
-                const SurfaceTerm& st = terms[order[p]];
-                out.line.push_back(st.line);
-                out.incd.push_back(st.incd);
-                out.pref.push_back(st.pref);
-                out.toD.push_back(st.toD ? 1 : 0);
+        out.line.reserve(n);
+        out.incd.reserve(n);
+        out.pref.reserve(n);
+        out.toD.reserve(n);
+        for (std::size_t p = 0; p < n; ++p) {
+            const SurfaceTerm& st = terms[static_cast<std::size_t>(kv[p].second)];
+            if (p == 0 || kv[p].first != kv[p - 1].first) {
+                if (p != 0) out.start.push_back(static_cast<long long>(out.line.size()));
+                out.cell.push_back(st.cell);
+                out.comp.push_back(st.comp);
             }
-            out.start.push_back(static_cast<long long>(out.line.size()));
+            out.line.push_back(st.line);
+            out.incd.push_back(st.incd);
+            out.pref.push_back(st.pref);
+            out.toD.push_back(st.toD ? 1 : 0);
         }
+        if (n) out.start.push_back(static_cast<long long>(out.line.size()));
     }
 };
 
