@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -58,21 +59,26 @@ void ck(cudaError_t e, const char* what) {
 struct DevMem {
     std::vector<void*> ptrs;
     double bytes = 0;
+    double allocSeconds = 0, copySeconds = 0;  // wall time in cudaMalloc + cudaMemset, and in copies
     template <typename T>
     T* alloc(std::size_t n, bool zero = true) {
         if (n == 0) return nullptr;
+        const auto t0 = std::chrono::steady_clock::now();
         void* p = nullptr;
         ck(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
         ptrs.push_back(p);
         bytes += static_cast<double>(n * sizeof(T));
         if (zero) ck(cudaMemset(p, 0, n * sizeof(T)), "cudaMemset");
+        allocSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return static_cast<T*>(p);
     }
     template <typename T>
     T* upload(const std::vector<T>& v) {
         if (v.empty()) return nullptr;
         T* p = alloc<T>(v.size(), false);
+        const auto t0 = std::chrono::steady_clock::now();
         ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        copySeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         h2d += static_cast<double>(v.size() * sizeof(T));
         return p;
     }
@@ -1423,6 +1429,9 @@ private:
         clk.mark("up-tfsf");
         uploadTail();
         clk.mark("up-tail");
+        if (clk.on)
+            std::fprintf(stderr, "host up: %.4f s in cudaMalloc + cudaMemset (%.0f MB), %.4f s in H2D copies (%.0f MB)\n",
+                         mem_.allocSeconds, mem_.bytes / 1e6, mem_.copySeconds, mem_.h2d / 1e6);
     }
 
     // One DFT table: point table (component, cell), phasors per sample from the accumulated
