@@ -7,6 +7,7 @@
 #include <chrono>
 #include <cmath>
 #include <complex>
+#include <exception>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -140,14 +141,24 @@ public:
         const int K = opt_.steps_per_graph;
         if (K > 0) {
             if (!graph_ && n >= K) buildGraph(K);
+            const long long period = foldPeriod();
             while (n >= K && graph_) {
+                if (graphAligned_ && stepsDone_ % period != 0) {
+                    // eager steps up to the next start of the fold period
+                    while (n > 0 && stepsDone_ % period != 0) {
+                        enqueueStep(stepsDone_, false);
+                        ++stepsDone_;
+                        --n;
+                    }
+                    continue;
+                }
                 ck(cudaGraphLaunch(graph_, stream_), "cudaGraphLaunch");
                 n -= K;
                 stepsDone_ += K;
             }
         }
         for (long long s = 0; s < n; ++s) {
-            enqueueStep();
+            enqueueStep(stepsDone_, false);
             ++stepsDone_;
         }
         ck(cudaGetLastError(), "kernel launch");
@@ -187,6 +198,23 @@ public:
         }
         ck(cudaStreamSynchronize(stream_), "DFT flush");
         clk.mark("fin-records");
+        // the face maps of every flux region, built on the host cores concurrently
+        std::vector<std::vector<FluxFaceMap>> maps(P.fluxes.size());
+        {
+            std::vector<std::exception_ptr> mErr(P.fluxes.size());
+#pragma omp parallel for schedule(dynamic, 1)
+            for (long long q = 0; q < static_cast<long long>(P.fluxes.size()); ++q) {
+                const std::size_t k = static_cast<std::size_t>(q);
+                if (P.fluxes[k].spec.save || P.fluxes[k].spec.load) continue;
+                try {
+                    maps[k] = flux_face_maps(P, k);
+                } catch (...) {
+                    mErr[k] = std::current_exception();
+                }
+            }
+            for (auto& e : mErr)
+                if (e) std::rethrow_exception(e);
+        }
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
             const int nt = stepsDone_ / P.fluxes[q].spec.timeInt + 1;
             R.fluxRe.emplace_back();
@@ -197,7 +225,7 @@ public:
                 R.fluxFaces.emplace_back();
                 downloadDft(q, P.fluxes[q].spec.freqList.size(), R.fluxRe.back(), R.fluxIm.back());
             } else {
-                R.fluxFaces.push_back(fluxFacesOnDevice(q, nt));
+                R.fluxFaces.push_back(fluxFacesOnDevice(q, nt, maps[q]));
             }
             R.fluxSamples.push_back(nt);
         }
@@ -287,10 +315,9 @@ public:
 
     // The integrated flux of every face of flux q, [freq * nFaces + face], evaluated from the
     // accumulators on the device; only these values are copied back.
-    std::vector<cplx> fluxFacesOnDevice(std::size_t q, int nt) {
+    std::vector<cplx> fluxFacesOnDevice(std::size_t q, int nt, const std::vector<FluxFaceMap>& maps) {
         const FluxPlan& fp = P.fluxes[q];
         const int nfreq = static_cast<int>(fp.spec.freqList.size());
-        const std::vector<FluxFaceMap> maps = flux_face_maps(P, q);
         const int nFaces = static_cast<int>(maps.size());
         std::vector<cplx> res(static_cast<std::size_t>(nfreq) * nFaces, cplx(0.0, 0.0));
         if (nFaces == 0 || nfreq == 0) return res;
@@ -574,6 +601,7 @@ private:
     std::string outDir_;
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
+    bool graphAligned_ = false;  // the graph holds only the fold launches of a period-aligned replay
     DevMem mem_;
     dev::Pass<T> hPass_{}, ePass_{};
     dev::Fields<T> fields_{};
@@ -597,7 +625,11 @@ private:
     double dftBytes_ = 0;
     int kernelsPerStep_ = 0;
 
-    void enqueueStep() {
+    // The step with index st (steps done before it). A table's fold kernel runs at the steps
+    // where one of its groups folds (foldsAfter); allFolds launches it every step, where
+    // the kernel itself finds whether a group folds (a graph whose replays do not all start
+    // at the same point of the fold period).
+    void enqueueStep(long long st, bool allFolds) {
         void* s = stream_;
         dev::launch_pass<T>(hPass_, false, s);
         // TFSF after the H update, before the sources (parallelFDTDField.hpp:1237-1261)
@@ -607,7 +639,21 @@ private:
         launchEmitters(s);
         // records, DFT samples and the step counter in one launch, then the folds
         dev::launch_step_tail<T>(tail_, s);
-        for (auto& d : dft_) dev::launch_dft_fold<T>(d, dStep_, s);
+        for (auto& d : dft_)
+            if (allFolds || foldsAfter(d, st + 1)) dev::launch_dft_fold<T>(d, dStep_, s);
+    }
+
+    // Whether a group of table d folds once the step counter reads `next` (the device's
+    // foldGroupNow: a sample at `next` that is the last of a stagger period).
+    static bool foldsAfter(const dev::DftTable<T>& d, long long next) {
+        return next % d.timeInt == 0 && (next / d.timeInt + 1) % dev::kFoldStagger == 0;
+    }
+
+    // Steps after which the fold pattern of every table repeats.
+    long long foldPeriod() const {
+        long long p = 1;
+        for (auto& d : dft_) p = std::lcm(p, static_cast<long long>(d.timeInt) * dev::kFoldStagger);
+        return p;
     }
 
     // ---- the device layout: rows padded from lx to pitch_ values ----
@@ -1026,10 +1072,14 @@ private:
         }
     }
 
+    // The graph of K steps. When the fold period divides K, it holds only the fold launches of
+    // a replay that starts at a multiple of the period (graphAligned_), and step() replays it
+    // only from such steps; otherwise every step carries its fold launches.
     void buildGraph(int K) {
         cudaGraph_t g;
+        graphAligned_ = K % foldPeriod() == 0;
         ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-        for (int k = 0; k < K; ++k) enqueueStep();
+        for (int k = 0; k < K; ++k) enqueueStep(k, !graphAligned_);
         ck(cudaStreamEndCapture(stream_, &g), "cudaStreamEndCapture");
         ck(cudaGraphInstantiate(&graph_, g, 0), "cudaGraphInstantiate");
         cudaGraphDestroy(g);

@@ -185,6 +185,10 @@ struct RecordTable {
 template <typename T>
 constexpr bool kFloatFloatAcc = sizeof(T) == 4;
 
+// The DFT fold is staggered: one group of point tiles folds every kFoldStagger samples
+// (fdtd_kernels.cu, foldGroupNow).
+constexpr int kFoldStagger = 4;
+
 template <typename T>
 struct DftTable {
     long long npts;

@@ -744,7 +744,8 @@ __device__ __forceinline__ void ffAdd(float& hi, float& lo, float v) {
 // written, so the ring of K slots suffices, and each step carries 1 / kFoldStagger of
 // a group fold: the fold work is spread evenly over the steps instead of arriving as
 // one launch every K samples.
-constexpr int kFoldStagger = 4;
+// (kFoldStagger: fdtd_device.hpp, shared with the host, which launches a table's fold
+// kernel only at the steps where one of its groups folds)
 
 // The sample range one group still has to fold after sample `last` (the flush at the
 // end of a run): first sample and count (count 0 when nothing is pending).

@@ -73,6 +73,33 @@ def test_graph_replay_equals_eager_launches(case, built_engine, tmp_path):
             assert open(pa, "rb").read() == open(pb, "rb").read(), f
 
 
+@pytest.mark.parametrize("graph,chunks", [(8, [5, 3, 17, 1]), (6, [7, 12])])
+def test_graph_replays_from_any_step_equal_eager_launches(graph, chunks, built_engine, tmp_path):
+    """Graphs whose length is a multiple of the DFT fold period hold only the fold launches
+    of replays that start on the period: steps that leave the count off the period run
+    eagerly until it is back on it. A graph of 6 steps (not a multiple of 4) carries every
+    step's fold launch."""
+    from chiml_gb300 import Simulation
+    case = "c1_small"
+    a = tmp_path / "eager"
+    b = tmp_path / "graph"
+    _run_gpu(case, a, graph=0)
+    stage_inputs(case, b)
+    sim = Simulation(os.path.join(GOLDEN, case, "in.json"), precision="fp64", steps_per_graph=graph, out_dir=str(b))
+    try:
+        for n in chunks:
+            sim.step(n)
+        sim.step()
+        sim.finalize()
+    finally:
+        sim.close()
+    for d, _, files in os.walk(a):
+        for f in files:
+            pa = os.path.join(d, f)
+            pb = os.path.join(b, os.path.relpath(pa, a))
+            assert open(pa, "rb").read() == open(pb, "rb").read(), f
+
+
 @pytest.mark.parametrize("case", golden_cases())
 def test_split_precision_within_tolerance(case, built_engine, tmp_path):
     _run_gpu(case, tmp_path, precision="split", graph=8)
