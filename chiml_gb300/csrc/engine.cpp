@@ -451,7 +451,7 @@ public:
                 mark(e1, k);
             }
             mark(e0, 1);
-            dev::launch_sources<T>(src_, fields_, dStep_, s);
+            if (!srcInE_) dev::launch_sources<T>(src_, fields_, dStep_, s);  // else in the E pass
             mark(e1, 1);
             mark(e0, 2);
             dev::launch_pass<T>(ePass_, true, s);
@@ -539,16 +539,7 @@ private:
         if (!dev::kInlineDispersive<T> && ePass_.nLor > 0) return;
         for (auto& d : dft_)
             if (d.timeInt != 1) return;
-        if (src_.n > dev::kPersistMaxSrc) return;
-        for (const SourcePlan& sp : P.sources) {
-            if (sp.comp > EZ) return;  // H sources: after the H update, not in the E pass
-            for (long long c : sp.cells) {
-                const uint8_t k = P.comp[sp.comp].code[static_cast<std::size_t>(c)];
-                const uint32_t fl = k < classFlags_[sp.comp].size() ? classFlags_[sp.comp][k] : 0u;
-                // the source is added to E before a plain update E = E + curl terms
-                if (k == 0 || !(fl & dev::kFcWrite) || (fl & (dev::kFcToD | dev::kFcLor | dev::kFcOrDip | dev::kFcDtoE))) return;
-            }
-        }
+        if (src_.n > 0 && !sourcesInE()) return;
         int coop = 0;
         ck(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, opt_.device), "cudaDeviceGetAttribute");
         if (!coop) return;
@@ -573,6 +564,23 @@ private:
         a.bar = mem_.alloc<unsigned int>(1);
         a.limitNs = 1000000000ull;  // one second per barrier
         persist_ = true;
+    }
+
+    // Whether the E pass can add the soft sources itself: at most kInlineMaxSrc entries, all
+    // on E components, each on a cell whose update is the plain E = E + curl terms (where
+    // adding the source to E first, as the source launch does, is the same operation).
+    bool sourcesInE() const {
+        if (src_.n > dev::kInlineMaxSrc) return false;
+        for (const SourcePlan& sp : P.sources) {
+            if (sp.comp > EZ) return false;  // H sources: after the H update, not in the E pass
+            for (long long c : sp.cells) {
+                const uint8_t k = P.comp[sp.comp].code[static_cast<std::size_t>(c)];
+                const uint32_t fl = k < classFlags_[sp.comp].size() ? classFlags_[sp.comp][k] : 0u;
+                if (k == 0 || !(fl & dev::kFcWrite) || (fl & (dev::kFcToD | dev::kFcLor | dev::kFcOrDip | dev::kFcDtoE)))
+                    return false;
+            }
+        }
+        return true;
     }
 
     // n steps in launches that end where a DFT group folds (every fourth sample) or after
@@ -601,6 +609,7 @@ private:
     std::string outDir_;
     cudaStream_t stream_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
+    bool srcInE_ = false;        // the E pass adds the soft sources (no source launch)
     bool graphAligned_ = false;  // the graph holds only the fold launches of a period-aligned replay
     DevMem mem_;
     dev::Pass<T> hPass_{}, ePass_{};
@@ -634,7 +643,7 @@ private:
         dev::launch_pass<T>(hPass_, false, s);
         // TFSF after the H update, before the sources (parallelFDTDField.hpp:1237-1261)
         for (auto& t : tfsf_) launchTfsf(t, s);
-        dev::launch_sources<T>(src_, fields_, dStep_, s);
+        if (!srcInE_) dev::launch_sources<T>(src_, fields_, dStep_, s);
         dev::launch_pass<T>(ePass_, true, s);
         launchEmitters(s);
         // records, DFT samples and the step counter in one launch, then the folds
@@ -1551,9 +1560,20 @@ private:
         ePass_.err = dErr_;
         recT_.err = dErr_;
         for (auto& d : dft_) d.err = dErr_;
+        // a few soft sources on a 2-D grid: the E pass adds them (one launch less per step)
+        srcInE_ = src_.n > 0 && ePass_.interior2d && sourcesInE();
+        if (srcInE_) {
+            ePass_.nSrcIn = src_.n;
+            ePass_.srcComp = src_.comp;
+            ePass_.srcCell = src_.cell;
+            ePass_.srcId = src_.src;
+            ePass_.srcValue = src_.value;
+            ePass_.srcSteps = src_.nSteps;
+            ePass_.step = dStep_;
+        }
         // every copy and memset above has landed before the first kernel runs
         ck(cudaDeviceSynchronize(), "upload");
-        kernelsPerStep_ = 3 + (src_.n ? 1 : 0) + static_cast<int>(dft_.size()) + (ePass_.nLor > 0 ? 1 : 0) + (ePass_.od.n > 0 ? 1 : 0) +
+        kernelsPerStep_ = 3 + (src_.n && !srcInE_ ? 1 : 0) + static_cast<int>(dft_.size()) + (ePass_.nLor > 0 ? 1 : 0) + (ePass_.od.n > 0 ? 1 : 0) +
                           3 * static_cast<int>(emit_.size()) + 2 * static_cast<int>(tfsf_.size());
         // the step tail: record blocks, then each DFT table's sample blocks
         tail_ = dev::StepTail<T>{};

@@ -136,7 +136,18 @@ struct Pass {
     long long nLor;
     const int* lorComp;
     const long long* lorCell;
+    // soft sources that the 2-D E pass adds itself (nSrcIn entries, at most kInlineMaxSrc;
+    // 0: the source kernel runs): component, device cell, source id, the source table's
+    // values [id * srcSteps + step] and the step counter
+    int nSrcIn;
+    const int* srcComp;
+    const long long* srcCell;
+    const int* srcId;
+    const double* srcValue;
+    int srcSteps;
+    const int* step;
 };
+constexpr int kInlineMaxSrc = 64;
 
 constexpr unsigned int kErrClassCode = 1u;   // a cell code outside its class table
 constexpr unsigned int kErrPoleCount = 2u;   // a class asks for more poles than its component stores
@@ -260,7 +271,7 @@ struct StepTail {
 // inline, soft sources only on E cells that the pass writes plainly (at most
 // kPersistMaxSrc entries), DFT tables sampled every step (so that a group fold falls at
 // the end of every fourth step, where the launch ends and the fold kernel runs).
-constexpr int kPersistMaxSrc = 64;
+constexpr int kPersistMaxSrc = kInlineMaxSrc;
 
 template <typename T>
 struct Persist2d {

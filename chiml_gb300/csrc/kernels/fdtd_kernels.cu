@@ -365,8 +365,10 @@ __device__ __forceinline__ T ldField(const T* p) {
 }
 
 // D2: a 2-D grid (lz == 1), where the term along z is absent. COH: neighbour fields are
-// loaded through L2 and the soft sources ps[0 .. nps) are added (the persistent form).
-template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false, bool COH = false>
+// loaded through L2 (the persistent form). SRC: the E pass adds the soft sources
+// ps[0 .. nps) to their cells' fields before the update.
+template <typename T, bool EPASS, int CI, typename I, int CY, int PD, bool PML, bool D2 = false, bool COH = false,
+          bool SRC = false>
 __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0, int y1, const PSrcCell<T>* ps = nullptr,
                                           int nps = 0) {
     constexpr int A0 = (CI + 2) % 3;  // derivative axis of term J
@@ -421,7 +423,7 @@ __device__ __forceinline__ void pass3dRun(const Pass<T>& p, int x, int z, int y0
         }
         const uint8_t cd = code[i];
         T u = U[i];
-        if constexpr (COH && EPASS) {
+        if constexpr (SRC && EPASS) {
             for (int k = 0; k < nps; ++k)
                 if (ps[k].comp == CI && ps[k].cell == static_cast<int>(i)) u += ps[k].v;
         }
@@ -538,8 +540,8 @@ constexpr int kP2W = 8;
 #define CHIML_P2CY 16
 #endif
 
-template <typename T, bool EPASS, int CI, int CY, int PD>
-__device__ __forceinline__ void pass2d(const Pass<T>& p, int bx, int by) {
+template <typename T, bool EPASS, int CI, int CY, int PD, bool SRC = false>
+__device__ __forceinline__ void pass2d(const Pass<T>& p, int bx, int by, const PSrcCell<T>* ps = nullptr, int nps = 0) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int xa = 1 + bx * 32;
     const int x = xa + lane;
@@ -548,15 +550,16 @@ __device__ __forceinline__ void pass2d(const Pass<T>& p, int bx, int by) {
     const int y1 = min(y0 + CY, p.ly - 1);
     const bool pml = blockTouchesSlab(p.c[CI], CI, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, 0, 0);
     if (x > p.lx - 2) return;
-    if (pml) pass3dRun<T, EPASS, CI, int, CY, PD, true, true>(p, x, 0, y0, y1);
-    else pass3dRun<T, EPASS, CI, int, CY, PD, false, true>(p, x, 0, y0, y1);
+    if (pml) pass3dRun<T, EPASS, CI, int, CY, PD, true, true, false, SRC>(p, x, 0, y0, y1, ps, nps);
+    else pass3dRun<T, EPASS, CI, int, CY, PD, false, true, false, SRC>(p, x, 0, y0, y1, ps, nps);
 }
 
-template <typename T, bool EPASS, int CY>
-__device__ __forceinline__ void pass2dAny(const Pass<T>& p, int ci, int bx, int by) {
-    if (ci == 0) pass2d<T, EPASS, 0, CY, 2>(p, bx, by);
-    else if (ci == 1) pass2d<T, EPASS, 1, CY, 2>(p, bx, by);
-    else pass2d<T, EPASS, 2, CY, 2>(p, bx, by);
+template <typename T, bool EPASS, int CY, bool SRC = false>
+__device__ __forceinline__ void pass2dAny(const Pass<T>& p, int ci, int bx, int by, const PSrcCell<T>* ps = nullptr,
+                                          int nps = 0) {
+    if (ci == 0) pass2d<T, EPASS, 0, CY, 2, SRC>(p, bx, by, ps, nps);
+    else if (ci == 1) pass2d<T, EPASS, 1, CY, 2, SRC>(p, bx, by, ps, nps);
+    else pass2d<T, EPASS, 2, CY, 2, SRC>(p, bx, by, ps, nps);
 }
 
 constexpr int kP2CY = CHIML_P2CY;
@@ -570,6 +573,23 @@ template <typename T, bool EPASS, int CY = kP2CY>
 __global__ void __launch_bounds__(256) k_pass2d(const Pass<T> p) {
     if (!p.c[blockIdx.z].present) return;
     pass2dAny<T, EPASS, CY>(p, blockIdx.z, blockIdx.x, blockIdx.y);
+}
+
+// The 2-D E pass with its soft sources (Pass::nSrcIn entries): each block reads the
+// sources' values at the current step, and the cell of each source adds its value to the
+// field before the update, which is the order of the source launch it replaces (E + v,
+// then the curl terms).
+template <typename T, int CY>
+__global__ void __launch_bounds__(256) k_pass2d_src(const Pass<T> p) {
+    if (!p.c[blockIdx.z].present) return;
+    __shared__ PSrcCell<T> ps[kInlineMaxSrc];
+    const int nps = p.nSrcIn < kInlineMaxSrc ? p.nSrcIn : kInlineMaxSrc;
+    const int st = *p.step;
+    for (int j = threadIdx.x; j < nps; j += blockDim.x)
+        ps[j] = PSrcCell<T>{p.srcComp[j], static_cast<int>(p.srcCell[j]),
+                            static_cast<T>(st < p.srcSteps ? p.srcValue[static_cast<long long>(p.srcId[j]) * p.srcSteps + st] : 0.0)};
+    __syncthreads();
+    pass2dAny<T, true, CY, true>(p, blockIdx.z, blockIdx.x, blockIdx.y, ps, nps);
 }
 
 __host__ __device__ inline int pass2d_gx(int lx) { return (lx - 2 + 31) / 32; }
@@ -586,13 +606,16 @@ void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
             k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
     } else if (p.interior2d) {
+        const bool src = ePass && p.nSrcIn > 0;
         if (static_cast<long long>(p.lx) * p.ly < kP2SmallCells) {
             dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly, kP2CYSmall), 3);
-            if (ePass) k_pass2d<T, true, kP2CYSmall><<<grid, 256, 0, s>>>(p);
+            if (src) k_pass2d_src<T, kP2CYSmall><<<grid, 256, 0, s>>>(p);
+            else if (ePass) k_pass2d<T, true, kP2CYSmall><<<grid, 256, 0, s>>>(p);
             else k_pass2d<T, false, kP2CYSmall><<<grid, 256, 0, s>>>(p);
         } else {
             dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
-            if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
+            if (src) k_pass2d_src<T, kP2CY><<<grid, 256, 0, s>>>(p);
+            else if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
             else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
         }
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
@@ -1053,8 +1076,8 @@ __device__ void persistPass(const Pass<T>& p, const PSrcCell<T>* ps, int nps) {
         const int y1 = min(y0 + CY, p.ly - 1);
         const bool pml = blockTouchesSlab(p.c[ci], ci, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, 0, 0);
 #define CHIML_PERSIST_RUN(CIV)                                                                           \
-    if (pml) pass3dRun<T, EPASS, CIV, int, CY, 0, true, true, true>(p, x, 0, y0, y1, ps, nps);          \
-    else pass3dRun<T, EPASS, CIV, int, CY, 0, false, true, true>(p, x, 0, y0, y1, ps, nps);
+    if (pml) pass3dRun<T, EPASS, CIV, int, CY, 0, true, true, true, true>(p, x, 0, y0, y1, ps, nps);    \
+    else pass3dRun<T, EPASS, CIV, int, CY, 0, false, true, true, true>(p, x, 0, y0, y1, ps, nps);
         if (ci == 0) {
             CHIML_PERSIST_RUN(0)
         } else if (ci == 1) {
