@@ -199,14 +199,17 @@ def config2(n=256, pml=12, steps=5000, nell=16, nfreq=150, seed=SEED0 + 2, metal
     }
 
 
-def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, coupling=C4_COUPLING, nfreq=50):
+def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, coupling=C4_COUPLING, nfreq=50,
+            cell_dipoles=True, seed=SEED0 + 3):
     """3-D Maxwell-Liouville scene: a ``slab_cells``-thick slab (normal z) of three-level
     ladder emitters across the cell inside the CPML, transitions at 2.0 and 2.2 eV with
     Gaussian inhomogeneous broadening of 20 meV sampled at ``nstates`` energies per upper
-    level (nstates^2 ensemble members per cell), z dipoles, T1 = 1 ps and T2 = 50 fs on
-    both transitions, ground-state start; an Ez plane source sheet below the slab with a
+    level (nstates^2 ensemble members per cell), T1 = 1 ps and T2 = 50 fs on both
+    transitions, ground-state start; an Ez plane source sheet below the slab with a
     Gaussian pulse at 2.1 eV, 10 fs wide, peak 5e8 V/m; a flux plane above
-    the slab, a point detector and the upper-level populations."""
+    the slab, a point detector and the upper-level populations. With ``cell_dipoles`` each
+    cell's dipole points in its own seeded random direction (the per-cell dipole extension:
+    ``dipole_orientation``), otherwise along z as in the reference."""
     dx = 0.05
     dt = 0.5 * dx / math.sqrt(3.0)
     size = (n - 1) * dx
@@ -217,6 +220,8 @@ def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, c
     qe = emitter_obj("block", [0.0, 0.0, 0.0], [(0, 0), (1, 0), (2, 0)], lv, [coupling] * 9, relax, mol_den, eps=1.0,
                      dtc_levs=[0, 4, 8], output_pol="c3_pol.dat", dtc_base="c3_qe_",
                      size=[inner, inner, slab_cells * dx])
+    if cell_dipoles:
+        qe.update(dipole_orientation="random", dipole_seed=seed)
     width = 10e-15 / T_UNIT
     src_z = -round((half - (pml + 4) * dx) / dx) * dx
     out_z = round((half - (pml + 6) * dx) / dx) * dx
@@ -236,14 +241,17 @@ def config3(n=192, pml=12, steps=8000, slab_cells=20, nstates=3, mol_den=1e26, c
 
 
 def config5(n=640, nz=320, pml=16, steps=20000, nell=16, nfreq=200, seed=SEED0 + 5, coupling=C4_COUPLING,
-            mol_den=1e26, sheet_cells=10, film_cells=10, amp=C4_AMPLITUDE):
+            mol_den=1e26, sheet_cells=10, film_cells=10, amp=C4_AMPLITUDE, cell_dipoles=True):
     """Large 3-D mixed scene (dx = 4 nm, fields in FP32 in the split form): n x n x nz cells.
 
     Inside the total-field box of a TFSF surface (``pml`` + 4 cells in from the edges): a
     ``film_cells``-thick Drude metal film (wp = 9 eV, gamma = 0.07 eV) below the middle, a
     ``sheet_cells``-thick sheet of four-level ladder emitters above it (transitions at 1.9,
-    2.0 and 2.3 eV, FP64 density matrices, z dipoles whose adjacent-level couplings are drawn
-    from 0.5-1.5 x ``coupling``, the seeded stand-in for 5-15 D dipoles; the reference has one
+    2.0 and 2.3 eV, FP64 density matrices; with ``cell_dipoles`` every cell's dipole points in
+    its own seeded random direction with a magnitude drawn from 0.5-1.5 x ``coupling`` (the
+    5-15 D dipoles of the configuration, through the per-cell dipole extension), otherwise
+    z dipoles whose adjacent-level couplings are drawn from 0.5-1.5 x ``coupling`` (a
+    stand-in the reference can run: it has one
     dipole operator per emitter object, so the draw is per transition, not per cell), and
     ``nell`` seeded uniaxial ellipsoids between the two, built as in config 2. The wave is a
     p-polarised Gaussian pulse at 550 nm along m = (1, 1, 3) (25 degrees off the film
@@ -286,12 +294,15 @@ def config5(n=640, nz=320, pml=16, steps=20000, nell=16, nfreq=200, seed=SEED0 +
     nlev = 4
     cpl = np.zeros((nlev, nlev))
     for a in range(nlev - 1):
-        cpl[a, a + 1] = cpl[a + 1, a] = coupling * float(rng.uniform(0.5, 1.5))
+        draw = float(rng.uniform(0.5, 1.5))
+        cpl[a, a + 1] = cpl[a + 1, a] = coupling * (1.0 if cell_dipoles else draw)
     lv = [emitter_level(0.0), emitter_level(1.9), emitter_level(3.9), emitter_level(6.2)]
     relax = [(1, 0, 1e12, 2e13), (2, 1, 1e12, 2e13), (3, 2, 1e12, 2e13)]
     objs.append(emitter_obj("block", [0.0, 0.0, sheet_z], [(0, 0), (1, 0), (2, 0), (3, 0)], lv,
                             [float(v) for v in cpl.ravel()], relax, mol_den, eps=1.0, dtc_levs=[5, 10, 15],
                             output_pol="c5_pol.dat", dtc_base="c5_qe_", size=[lateral, lateral, sheet_cells * dx]))
+    if cell_dipoles:
+        objs[-1].update(dipole_orientation="random", dipole_seed=seed, dipole_scale_range=[0.5, 1.5])
     width = 5e-15 / T_UNIT
     fl = 2 * (hx - (pml + 6) * dx)
     planes = []

@@ -998,6 +998,14 @@ private:
             e.invHbar = 1.0 / ep.hbar;
             e.na = ep.na;
             e.cellGrid = mem_.upload(padCells(ep.cellGrid));
+            e.cellDip = nullptr;
+            if (!ep.cellDip.empty()) {
+                if (ep.cellDip.size() != ep.cellGrid.size()) throw InputError("per-cell dipoles do not match the emitter cells");
+                std::vector<double> w(3 * ep.cellDip.size());
+                for (std::size_t q = 0; q < ep.cellDip.size(); ++q)
+                    for (int c = 0; c < 3; ++c) w[c * ep.cellDip.size() + q] = ep.cellDip[q][c];
+                e.cellDip = mem_.upload(w);
+            }
             e.cellP = mem_.upload(ep.cellP);
             e.unit[0] = 1;
             e.unit[1] = pitch_ * D.lz;

@@ -124,6 +124,32 @@ void level_combos(const std::vector<EnergyLevel>& levs, std::size_t depth, std::
 
 }  // namespace
 
+// PCG32 (O'Neill's PCG-XSH-RR generator: 64-bit LCG state, 32-bit output), the stream of the
+// per-cell dipole draws; uniform() returns a 53-bit double in [0, 1) from two outputs.
+class Pcg32 {
+public:
+    explicit Pcg32(unsigned long long seed, unsigned long long stream = 54u) {
+        inc_ = (stream << 1u) | 1u;
+        next();
+        state_ += seed;
+        next();
+    }
+    uint32_t next() {
+        const unsigned long long old = state_;
+        state_ = old * 6364136223846793005ULL + inc_;
+        const uint32_t xorshifted = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = static_cast<uint32_t>(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+    }
+    double uniform() {
+        const uint32_t a = next() >> 5, b = next() >> 6;
+        return (a * 67108864.0 + b) / 9007199254740992.0;
+    }
+
+private:
+    unsigned long long state_ = 0, inc_ = 1;
+};
+
 void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epresent[3], const double* epsOrDip,
                     Plan& P) {
     for (const EmitterSpec& em : in.emitters) {
@@ -224,6 +250,33 @@ void build_emitters(const Inputs& in, const Dims& D, double dt, const bool Epres
             const int pi = x + 1, pj = y + 1, pk = z + e.zOff;
             e.cellGrid.push_back(D.idx(e.boxBase[0] + pi, e.boxBase[1] + pj, e.boxBase[2] + pk));
             e.cellP.push_back(pi + e.pDims[0] * (pk + e.pDims[2] * pj));
+        }
+        if (em.cellDipole) {
+            // per-cell dipoles (extension): w = scale * direction for every cell, in cell order
+            const bool alongZ = !e.addMu[0] && !e.addMu[1] && e.addMu[2];
+            if (!alongZ) throw UnsupportedError("per-cell dipoles need an emitter operator along z (basis states with m = 0)");
+            if (em.randomDirection && twoD) throw UnsupportedError("random dipole directions need a 3-D grid");
+            Pcg32 rng(em.dipoleSeed);
+            const double a = em.dipoleScale[0], b = em.dipoleScale[1];
+            e.cellDip.reserve(em.locs.size());
+            for (std::size_t q = 0; q < em.locs.size(); ++q) {
+                std::array<double, 3> w = {0.0, 0.0, 1.0};
+                if (em.randomDirection) {
+                    // uniform on the sphere: z uniform on (-1, 1], azimuth uniform on [0, 2 pi)
+                    const double z = 1.0 - 2.0 * rng.uniform();
+                    const double ph = 2.0 * M_PI * rng.uniform();
+                    const double r = std::sqrt(std::max(0.0, 1.0 - z * z));
+                    w = {r * std::cos(ph), r * std::sin(ph), z};
+                }
+                if (b > a) {
+                    const double sc = a + (b - a) * rng.uniform();
+                    for (double& v : w) v *= sc;
+                } else {
+                    for (double& v : w) v *= a;
+                }
+                e.cellDip.push_back(w);
+            }
+            e.addMu = {false, false, true};
         }
         e.nPoints = static_cast<int>(em.locs.size());
         e.outputPol = em.outputPol;

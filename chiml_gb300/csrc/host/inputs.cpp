@@ -766,6 +766,21 @@ void read_emitter(const JNode& node, Object& o, Inputs& ip) {
         r.dephasing = kv.second.get<double>("dephasing_rate", 0.0) * ip.a / kSpeedOfLight;
         em.relax.push_back(r);
     }
+    // per-cell dipoles (extension; see EmitterSpec)
+    {
+        const std::string orient = node.get<std::string>("dipole_orientation", "");
+        const std::vector<double> scale = node.has("dipole_scale_range") ? as_vector(node, "dipole_scale_range") : std::vector<double>{};
+        if (!orient.empty() || !scale.empty()) {
+            if (!orient.empty() && orient != "random" && orient != "z")
+                throw InputError("dipole_orientation must be \"random\" or \"z\"");
+            if (!scale.empty() && (scale.size() != 2 || !(scale[0] > 0.0) || scale[1] < scale[0]))
+                throw InputError("dipole_scale_range must be two values 0 < a <= b");
+            em.cellDipole = true;
+            em.randomDirection = orient == "random";
+            if (!scale.empty()) em.dipoleScale = {scale[0], scale[1]};
+            em.dipoleSeed = static_cast<unsigned long long>(node.get<double>("dipole_seed", 0.0));
+        }
+    }
     em.outputPol = node.get<bool>("output_pol", false);
     if (em.outputPol) em.polFile = node.get<std::string>("output_pol_filename");
     for (auto& kv : node.child("dtc_levs").kids) em.dtcLevs.push_back(kv.second.value<int>());

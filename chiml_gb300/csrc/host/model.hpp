@@ -177,6 +177,15 @@ struct EmitterSpec {
     std::vector<int> dtcLevs;
     std::vector<std::string> dtcFiles;
     int dtcTimeInt = 1;
+    // Extension (no reference counterpart; the reference reads none of these keys): a
+    // per-cell dipole for an object whose operator lies along z. "dipole_orientation":
+    // "random" turns each cell's dipole to a direction drawn uniformly on the sphere,
+    // "z" keeps it along z; "dipole_scale_range" [a, b] scales each cell's operator by a
+    // factor drawn uniformly from [a, b); both from a PCG32 stream seeded by "dipole_seed".
+    bool cellDipole = false;
+    bool randomDirection = false;
+    std::array<double, 2> dipoleScale = {1.0, 1.0};
+    unsigned long long dipoleSeed = 0;
 };
 
 struct Inputs {

@@ -171,6 +171,9 @@ struct EmitterPlan {
     std::array<std::vector<cplx>, 3> mu;     // x/y/z_expectation_ (coupling-scaled), nlevel^2 each
     std::array<std::vector<cplx>, 3> negMu;  // neg_x/y/z_expectation_
     std::array<bool, 3> addMu = {false, false, false};  // the operator has a nonzero element
+    // per emitter cell (extension, EmitterSpec::cellDipole): the operator of the cell is
+    // w * mu[z], w = scale * direction; empty: the object's operators everywhere
+    std::vector<std::array<double, 3>> cellDip;
     // relaxation: for each flat index ii the (jj, rate) pairs, outDeriv[ii] += rho[jj] * rate
     std::vector<std::vector<std::pair<int, double>>> gam;
     double dt = 0.0, hbar = 0.0, na = 0.0;

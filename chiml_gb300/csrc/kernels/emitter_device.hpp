@@ -34,6 +34,10 @@ struct EmitterDev {
     // and 1/hbar, formed once on the host: FP64 division is slow on this GPU
     double abP[4], abC[4], invHbar;
     const long long* cellGrid;    // [nc] grid index of each cell
+    // per-cell dipoles (extension): the operator of cell q is w_q * (the z operator), w as
+    // [3][nc]; null for the object's operators everywhere. The coupling uses E . w with
+    // the z operator, and P_c = w_c * (the z polarisation)
+    const double* cellDip;
     const int* cellP;             // [nc] P-box index of each cell
     long long unit[3];            // grid index step along x, y, z
     double2* rho;                 // [nm * n2 * nc]

@@ -608,6 +608,13 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
                 else Ec[c] = 0.5 * static_cast<double>(Es[c][g]) + 0.5 * static_cast<double>(Es[c][g - e.unit[c]]);
             }
         }
+        if (e.cellDip) {
+            // a per-cell dipole w: the coupling is (E . w) times the z operator
+            const double ew = Ec[0] * e.cellDip[q] + Ec[1] * e.cellDip[e.nc + q] + Ec[2] * e.cellDip[2 * e.nc + q];
+            Ec[0] = 0.0;
+            Ec[1] = 0.0;
+            Ec[2] = ew;
+        }
         const bool zeroE = (Ec[0] == 0.0 && Ec[1] == 0.0 && Ec[2] == 0.0);
         const long long slotStride = static_cast<long long>(e.nm) * n2 * e.nc;
         const int s0 = (s - 1) & 3, s1 = (s - 2) & 3, s2 = (s - 3) & 3, s3 = s & 3;  // k_n, k_n-1, k_n-2, k_n-3
@@ -740,6 +747,12 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
                 Pc[c] += e.na * sdot;
             }
         }
+        }
+        if (e.cellDip) {
+            // P_c = w_c times the polarisation of the z operator
+            const double pz = Pc[2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Pc[c] = pz * e.cellDip[static_cast<long long>(c) * e.nc + q];
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c)

@@ -13,6 +13,10 @@
 //   TFSF surfaces        SOURCE/parallelTFSF.hpp:1058-1186, SOURCE/parallelTFSF.cpp:11-94, PML/PML.cpp:12-31
 //   emitters             ML/parallelQE.hpp:614-770 (addQE, updateDensity, denDeriv, PCABAM4),
 //                        UTIL/FDTD_up_eq.cpp:1367-1420 (addP, getE_TE/TM), ML/Hamiltonian.cpp:59-69
+//   per-cell dipoles     an extension without a reference counterpart (EmitterPlan::cellDip):
+//                        the coupling (E . w) times the z operator, P_c = w_c times the z
+//                        polarisation; pinned by its reduction to the reference (w = z gives
+//                        the reference's outputs) and by the GPU's FP64 form
 // Its outputs are pinned by the golden files of the reference's own CPU build
 // (tests/golden). Only tests, the smoke check and the CPU-baseline leg of the
 // benchmark call it; the product path never does.
@@ -161,6 +165,13 @@ struct EmitterSim {
                 if (c == 2 && e.gatherZCopy) eAt[q * 3 + c] = cplx(E[g], 0.0);
                 else eAt[q * 3 + c] = cplx(0.5 * E[g] + 0.5 * E[g - unit[c]], 0.0);
             }
+            if (!e.cellDip.empty()) {
+                // per-cell dipole w (extension): the coupling is (E . w) times the z operator
+                const std::array<double, 3>& w = e.cellDip[static_cast<std::size_t>(q)];
+                const double ew = eAt[q * 3 + 0].real() * w[0] + eAt[q * 3 + 1].real() * w[1] + eAt[q * 3 + 2].real() * w[2];
+                eAt[q * 3 + 0] = eAt[q * 3 + 1] = cplx(0.0, 0.0);
+                eAt[q * 3 + 2] = cplx(ew, 0.0);
+            }
         }
         for (auto& p : Pbox) std::fill(p.begin(), p.end(), 0.0);
         for (int m = 0; m < nm; ++m)
@@ -169,6 +180,14 @@ struct EmitterSim {
                 const cplx* r = &rho[(static_cast<std::size_t>(m) * nc + q) * n2];
                 for (std::size_t d = 0; d < e.dtcLevs.size(); ++d)
                     if (tstep % e.dtcTimeInt == 0) curPop[d] += r[e.dtcLevs[d]];
+                if (!e.cellDip.empty()) {
+                    // P_c = w_c times the polarisation of the z operator
+                    cplx s = 0.0;
+                    for (int i = 0; i < n2; ++i) s += std::conj(r[i]) * e.mu[2][i];
+                    for (int c = 0; c < 3; ++c)
+                        if (e.comp[c]) Pbox[c][e.cellP[q]] += e.na * std::real(s) * e.cellDip[static_cast<std::size_t>(q)][c];
+                    continue;
+                }
                 for (int c = 0; c < 3; ++c) {
                     if (!e.comp[c]) continue;
                     cplx s = 0.0;

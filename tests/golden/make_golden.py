@@ -167,7 +167,7 @@ def _freq_2d():
 def _c5_small():
     """Config 5 in miniature: three uniaxial ellipsoids, the Drude film, the four-level emitter
     sheet, the oblique p-polarised TFSF wave and the six flux planes, at 40 x 40 x 48 cells."""
-    return configs.config5(n=40, nz=48, pml=6, steps=480, nell=3, nfreq=5, sheet_cells=2, film_cells=2)
+    return configs.config5(n=40, nz=48, pml=6, steps=480, nell=3, nfreq=5, sheet_cells=2, film_cells=2, cell_dipoles=False)
 
 
 def _bin_planes(cfg, planes, every=20):
