@@ -701,8 +701,9 @@ private:
     }
 
     void launchTfsf(const dev::TfsfDev& t, void* s) {
-        T* const f6[6] = {fields_.f[0], fields_.f[1], fields_.f[2], fields_.f[3], fields_.f[4], fields_.f[5]};
-        dev::launch_tfsf_step<T>(t, f6, dStep_, s);
+        T* const f9[9] = {fields_.f[0], fields_.f[1], fields_.f[2], fields_.f[3], fields_.f[4],
+                          fields_.f[5], fields_.f[6], fields_.f[7], fields_.f[8]};
+        dev::launch_tfsf_step<T>(t, f9, dStep_, s);
     }
 
     // TFSF surfaces: the lines' two grids and psi lists (zeroed), the pulse table of
@@ -730,6 +731,21 @@ private:
                 d.prefact = make_double2(L.prefact.real(), L.prefact.imag());
                 d.U = mem_.alloc<double2>(static_cast<std::size_t>(tp.gridLen));
                 d.pul = mem_.alloc<double2>(static_cast<std::size_t>(tp.pulseLen));
+                const std::size_t len = static_cast<std::size_t>(tp.gridLen);
+                if (L.epMu.size() != len || L.obj.size() != len || L.nPole < 0 ||
+                    L.pa.size() != static_cast<std::size_t>(L.nPole) * len || L.px.size() != L.pa.size() ||
+                    L.pg.size() != L.pa.size() || (L.nPole > 0 && !L.dLine))
+                    throw InputError("TFSF line material set-up inconsistent");
+                d.eps = mem_.upload(L.epMu);
+                d.D = L.dLine ? mem_.alloc<double2>(len) : nullptr;
+                d.nPole = L.nPole;
+                if (L.nPole > 0) {
+                    d.P = mem_.alloc<double2>(static_cast<std::size_t>(L.nPole) * len);
+                    d.Pprev = mem_.alloc<double2>(static_cast<std::size_t>(L.nPole) * len);
+                    d.pa = mem_.upload(L.pa);
+                    d.px = mem_.upload(L.px);
+                    d.pg = mem_.upload(L.pg);
+                }
                 auto run = [](const TfsfRun& r) {
                     return dev::TfsfRunDev{r.indI, r.n, r.posJ, r.negJ, r.posK, r.negK, r.pj, r.pk};
                 };
@@ -813,6 +829,8 @@ private:
                         while (r < g.n && !multi(g.comp * P.dims.cells() + g.cell0 + r * g.cellStride)) ++r;
                         if (r == r0) continue;
                         dev::TfsfSegDev d{};
+                        d.toD = g.toD ? 1 : 0;
+                        d.div = g.div;
                         d.cell0 = pad(g.cell0 + r0 * g.cellStride);
                         d.cellStride = padOffset(g.cellStride);
                         d.incd0 = g.incd0 + r0 * g.incdStride;
@@ -824,8 +842,11 @@ private:
                         const long long lastCell = d.cell0 + static_cast<long long>(d.n - 1) * d.cellStride;
                         const long long lastIncd = d.incd0 + static_cast<long long>(d.n - 1) * d.incdStride;
                         if (d.cell0 < 0 || lastCell >= cellsPad_ || d.incd0 < 0 || lastIncd >= tp.gridLen || d.cellStride < 0 ||
-                            d.incdStride < 0 || !tp.line[d.line].present || !P.comp[d.comp].present)
+                            d.incdStride < 0 || !tp.line[d.line].present || !P.comp[d.comp].present ||
+                            (d.div >= 0 && (d.div > 5 || !tp.line[d.div].present)))
                             throw InputError("TFSF surface row outside its grids");
+                        if (d.toD && (d.comp > 2 || !fields_.f[6 + d.comp]))
+                            throw UnsupportedError("TFSF correction into a D field the grid does not have");
                         for (int c = 0; c * dev::kTfsfRowChunk < d.n; ++c) sw.push_back(make_int2(static_cast<int>(sd.size()), c));
                         sd.push_back(d);
                     }
@@ -834,7 +855,7 @@ private:
                 t.segWork[w] = mem_.upload(sw);
                 t.segBlocks[w] = static_cast<int>(sw.size());
                 std::vector<long long> cell;
-                std::vector<int> comp, start, tl, ti;
+                std::vector<int> comp, start, tl, ti, tf;
                 std::vector<double> pref;
                 if (static_cast<long long>(a.terms()) != nTerms) throw InputError("TFSF surface rows and cell lists disagree");
                 for (std::size_t q = 0; q < a.cells(); ++q) {
@@ -843,13 +864,16 @@ private:
                     comp.push_back(a.comp[q]);
                     start.push_back(static_cast<int>(tl.size()));
                     for (long long k = a.start[q]; k < a.start[q + 1]; ++k) {
-                        if (a.toD[k]) throw UnsupportedError("TFSF corrections into D");
                         if (!tp.line[a.line[k]].present || a.incd[k] < 0 || a.incd[k] >= tp.gridLen ||
-                            a.cell[q] < 0 || a.cell[q] >= P.dims.cells() || !P.comp[a.comp[q]].present)
+                            a.cell[q] < 0 || a.cell[q] >= P.dims.cells() || !P.comp[a.comp[q]].present ||
+                            (a.div[k] >= 0 && (a.div[k] > 5 || !tp.line[a.div[k]].present)))
                             throw InputError("TFSF correction outside its grids");
+                        if (a.toD[k] && (a.comp[q] > 2 || !fields_.f[6 + a.comp[q]]))
+                            throw UnsupportedError("TFSF correction into a D field the grid does not have");
                         tl.push_back(a.line[k]);
                         ti.push_back(a.incd[k]);
                         pref.push_back(a.pref[k]);
+                        tf.push_back((a.toD[k] ? 1 : 0) | ((a.div[k] + 1) << 1));
                     }
                 }
                 start.push_back(static_cast<int>(tl.size()));
@@ -860,6 +884,7 @@ private:
                 t.termLine[w] = mem_.upload(tl);
                 t.termIncd[w] = mem_.upload(ti);
                 t.termPref[w] = mem_.upload(pref);
+                t.termFlag[w] = mem_.upload(tf);
             }
             tfsf_.push_back(t);
         }

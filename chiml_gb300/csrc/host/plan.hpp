@@ -221,11 +221,21 @@ struct TfsfPsi {
     std::vector<double> b, c, cOff;
 };
 
+// A line crossing layered material (surfaces in non-vacuum material, genEpMu and
+// genFieldUpParam, parallelTFSF.hpp:591-720) has per-element eps (mu) and pole
+// coefficients: each step first moves the poles, P = alpha P + xi P_prev + gamma U
+// (updateIncdPols, parallelTFSF.cpp:44-58, U the line before this step), then the curl
+// goes to the D grid, then U = D / eps - sum_p P_p / eps (incdD2U, parallelTFSF.cpp:60-68).
 struct TfsfLine {
     bool present = false;
     bool useJ = false, useK = false;  // the j / k neighbour lines take part in the curl
     int nbrJ = -1, nbrK = -1;          // neighbour line ids (component (c+1)%3, (c+2)%3 of the other kind)
-    double epMu = 1.0;                 // uniform eps (E) or mu (H) of the line
+    std::vector<double> epMu;          // per incident-grid element: eps (E) or mu (H), gridLen values
+    std::vector<int> obj;              // per incident-grid element: the object it samples (incdPhys)
+    bool dLine = false;                // stepped through a D grid (eps other than 1 or poles on the line)
+    bool epChange = false;             // eps varies along the line: surface terms are divided by it
+    int nPole = 0;                     // poles per element (the most any element's object has)
+    std::vector<double> pa, px, pg;    // [nPole][gridLen] alpha, xi, gamma; zero past an object's poles
     std::vector<TfsfRun> runs;         // incident grid, length gridLen
     std::vector<TfsfRun> pulseRuns;    // pulse grid, length pulseLen
     std::vector<TfsfPsi> pml, pmlPulse;
@@ -234,11 +244,10 @@ struct TfsfLine {
     int recIdx = 0, recOffIdx = 0;     // pulse-grid points recorded each step
 };
 
-// Surface corrections of one main-grid cell, in the reference's order: each term adds
-// pref * Re(line[incd]) to the cell's field (toD: to its D field).
-// The surface terms of every main-grid cell that gets some, cells in the order of their
-// first term, terms of cell q in [start[q], start[q + 1]) in the reference's order:
-// F[comp[q]][cell[q]] (or D where toD) += pref * Re(line[line][incd]).
+// The surface terms of every main-grid cell that gets some; the terms of cell q are
+// [start[q], start[q + 1]) in the reference's order: F[comp[q]][cell[q]] (its D field
+// where toD) += pref * Re(line[line][incd]) (divided first by eps of line div at incd
+// where div >= 0).
 struct TfsfAdds {
     std::vector<long long> cell;
     std::vector<int> comp;              // main field component 0..5
@@ -246,16 +255,21 @@ struct TfsfAdds {
     std::vector<int> line, incd;
     std::vector<double> pref;
     std::vector<uint8_t> toD;
+    std::vector<int> div;               // -1, or the line whose eps divides the value (addIncdFieldsEPChange)
     std::size_t cells() const { return cell.size(); }
     std::size_t terms() const { return line.size(); }
 };
 
 // One row of one surface (a daxpy of addIncdFields): cell cell0 + r * cellStride of
-// component comp gets pref * Re(line[incd0 + r * incdStride]), r < n.
+// component comp (its D field where toD) gets pref * Re(line[incd0 + r * incdStride]),
+// r < n; where div >= 0 the value is first divided by eps of line div at the same index
+// (addIncdFieldsEPChange, SOURCE/parallelTFSF.cpp:98-107).
 struct TfsfSegment {
     long long cell0 = 0, cellStride = 0;
     int incd0 = 0, incdStride = 0, n = 0, line = 0, comp = 0;
     double pref = 0.0;
+    bool toD = false;
+    int div = -1;
 };
 
 struct TfsfPlan {

@@ -1761,7 +1761,7 @@ Plan build_plan(const Inputs& in) {
     if (!in.tfsf.empty()) {
         const int* ph[6];
         for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? b.phys[c].v.data() : nullptr;
-        build_tfsf(in, P.dims, P.dt, ph, in.objects, P);
+        build_tfsf(in, P.dims, P.dt, ph, P.in.objects, P);
         clk.mark("tfsf");
     }
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)

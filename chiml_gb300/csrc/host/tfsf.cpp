@@ -5,10 +5,13 @@
 //
 // Supported: any non-negative integer propagation vector m (normal and oblique
 // incidence, 2-D and 3-D), linear, circular and elliptical polarisation, surfaces in
-// vacuum. Rejected: a negative m component (the reference samples the surface material
-// only on the plus surfaces and, for negative m, divides the incident fields by a zero
-// permittivity: every output is NaN), and surfaces crossing or lying in non-vacuum
-// material (the reference's layered-medium path, parallelTFSF.hpp:591-694).
+// vacuum, in one uniform material, or crossing material layered along a normal
+// propagation direction (dielectric and Drude/Lorentz layers: the lines then carry
+// per-element eps and poles, and corrections inside dispersive layers go to D).
+// Rejected: a negative m component (the reference samples the surface material only on
+// the plus surfaces and, for negative m, divides the incident fields by a zero
+// permittivity: every output is NaN), and the material layouts the reference itself
+// refuses (genEpMu's checks, parallelTFSF.hpp:621-681).
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -28,6 +31,7 @@ struct TfsfBuilder {
     std::array<double, 3> d;
     const TfsfSpec& t;
     const int* const* phys;
+    const std::vector<Object>& objs;
     TfsfPlan& T;
 
     bool twoD = false;
@@ -38,8 +42,9 @@ struct TfsfBuilder {
     bool present[6] = {false, false, false, false, false, false};
     std::vector<TfsfSegment>* segs = nullptr;  // where genSurface records its rows
 
-    TfsfBuilder(const Inputs& i, const Dims& dd, double dtt, const TfsfSpec& tt, const int* const* ph, TfsfPlan& tp)
-        : in(i), D(dd), dt(dtt), d(i.d), t(tt), phys(ph), T(tp) {}
+    TfsfBuilder(const Inputs& i, const Dims& dd, double dtt, const TfsfSpec& tt, const int* const* ph,
+                const std::vector<Object>& ob, TfsfPlan& tp)
+        : in(i), D(dd), dt(dtt), d(i.d), t(tt), phys(ph), objs(ob), T(tp) {}
 
     // ---- parallelTFSFBase constructor, parallelTFSF.hpp:179-380 ----
     void build() {
@@ -115,10 +120,6 @@ struct TfsfBuilder {
             if (std::abs(std::tan(psi)) > 1) psiP = M_PI / 2.0 - psiP;
             if (t.circPol == Pol::R) alpha *= -1.0;
         }
-        PhaseClock clk0;
-        checkVacuumSurfaces();
-        clk0.mark("tfsf-vacuum");
-
         T.m = m;
         T.mTot = mTot;
         T.mMax = mMax;
@@ -131,19 +132,45 @@ struct TfsfBuilder {
         // lines: H then E, (i, j, k) cycled (parallelTFSF.hpp:321-327)
         const int distH[3] = {m[1] + m[2], m[0] + m[2], m[0] + m[1]};
         const int distE[3] = {m[0], m[1], m[2]};
+        PhaseClock clk0;
         for (int i = 0; i < 3; ++i) initLine(3 + i, false, distH[i], i, (i + 1) % 3, (i + 2) % 3);
         for (int i = 0; i < 3; ++i) initLine(i, true, distE[i], i, (i + 1) % 3, (i + 2) % 3);
-        // scaleDistVecSpeed multiplies by sqrt(eps mu) of the line: 1 in vacuum
+        clk0.mark("tfsf-lines");
+        // scaleDistVecSpeed (parallelTFSF.hpp:393-411, 697-702): each distance times
+        // sqrt(eps mu) of the line's first elements; in 2-D the missing lines are
+        // replaced by the ones named there
+        auto epAt = [&](int c, int x) { return T.line[c].epMu[static_cast<std::size_t>(x)]; };
+        auto scaleDist = [&](int c, int ep, int mu) {
+            if (!T.line[c].present) return;
+            for (int rr = 0; rr < mTot; ++rr) T.line[c].dist[rr] = std::sqrt(epAt(ep, rr) * epAt(mu, rr)) * T.line[c].dist[rr];
+        };
+        if (present[0] && present[3]) {
+            for (int i = 0; i < 3; ++i) {
+                scaleDist(i, i, 3 + i);
+                scaleDist(3 + i, i, 3 + i);
+            }
+        } else if (present[0]) {
+            scaleDist(0, 0, 5);
+            scaleDist(1, 1, 5);
+            scaleDist(5, 0, 5);
+        } else {
+            scaleDist(3, 2, 3);
+            scaleDist(4, 2, 4);
+            scaleDist(2, 2, 3);
+        }
+        // the pulse prefactors are divided by eps (mu) of the line at the recorded point
+        // (parallelTFSF.hpp:413-419); a missing line's own value is replaced as there
+        const int fo = pmlThick + mMax + 5 * mTot;
+        auto epFo = [&](int c, int alt) { return present[c] ? epAt(c, fo) : (present[alt] ? epAt(alt, fo) : 1.0); };
         const cplx psiJ = std::cos(psiP);
         const cplx psiK = std::sin(psiP) * std::exp(cplx(0.0, alpha));
-        const double epMu = 1.0;
         cplx pH[3], pE[3];
-        pH[0] = (psiK * std::sin(phiP) + psiJ * std::cos(theta) * std::cos(phiP)) * dt / (mTot * dr) / epMu;
-        pH[1] = (-1.0 * psiK * std::cos(phiP) + psiJ * std::cos(theta) * std::sin(phiP)) * dt / (mTot * dr) / epMu;
-        pH[2] = (-1.0 * psiJ * std::sin(theta)) * dt / (mTot * dr) / epMu;
-        pE[0] = (psiJ * std::sin(phiP) - psiK * std::cos(theta) * std::cos(phiP)) * dt / (mTot * dr) / epMu;
-        pE[1] = (-1.0 * psiJ * std::cos(phiP) - psiK * std::cos(theta) * std::sin(phiP)) * dt / (mTot * dr) / epMu;
-        pE[2] = (psiK * std::sin(theta)) * dt / (mTot * dr) / epMu;
+        pH[0] = (psiK * std::sin(phiP) + psiJ * std::cos(theta) * std::cos(phiP)) * dt / (mTot * dr) / epFo(3, 5);
+        pH[1] = (-1.0 * psiK * std::cos(phiP) + psiJ * std::cos(theta) * std::sin(phiP)) * dt / (mTot * dr) / epFo(4, 5);
+        pH[2] = (-1.0 * psiJ * std::sin(theta)) * dt / (mTot * dr) / epFo(5, 3);
+        pE[0] = (psiJ * std::sin(phiP) - psiK * std::cos(theta) * std::cos(phiP)) * dt / (mTot * dr) / epFo(0, 2);
+        pE[1] = (-1.0 * psiJ * std::cos(phiP) - psiK * std::cos(theta) * std::sin(phiP)) * dt / (mTot * dr) / epFo(1, 2);
+        pE[2] = (psiK * std::sin(theta)) * dt / (mTot * dr) / epFo(2, 0);
         for (int i = 0; i < 3; ++i) {
             T.line[3 + i].prefact = pH[i];
             T.line[i].prefact = pE[i];
@@ -168,45 +195,128 @@ struct TfsfBuilder {
         gather(hTerms, T.addH);
         gather(eTerms, T.addE);
         clk.mark("tfsf-gather");
-        // the lines' CPMLs (parallelTFSF.hpp:342-378)
+        // the lines' CPMLs (parallelTFSF.hpp:425-466): vacuum constants on the incident
+        // grid; on the pulse grid eps and mu of the lines named there, at element mMax
+        const int pulEps[6] = {0, 1, 2, 2, 2, 0}, pulMu[6] = {5, 5, 3, 3, 4, 5};
         for (int c = 0; c < 6; ++c) {
             if (!T.line[c].present) continue;
-            T.line[c].pml = incdCPML(c, gridLen);
-            T.line[c].pmlPulse = incdCPML(c, T.pulseLen);
+            T.line[c].pml = incdCPML(c, gridLen, 1.0, 1.0);
+            const double ep = present[pulEps[c]] ? epAt(pulEps[c], mMax) : 1.0;
+            const double mu = present[pulMu[c]] ? epAt(pulMu[c], mMax) : 1.0;
+            T.line[c].pmlPulse = incdCPML(c, T.pulseLen, ep, mu);
         }
     }
 
-    // The incident lines take their material from the plus surfaces of the box, sampled
-    // one cell beyond the box on each axis (genEpMu, parallelTFSF.hpp:591-694); this build
-    // requires vacuum there, where every line is uniform with eps = mu = 1.
-    void checkVacuumSurfaces() const {
+    // Object id of main-grid component c at the plane point (x, y, z) in interior
+    // coordinates (the halo cell is index 0), as the reference's getPlane* read it
+    // (GRID/parallelGrid.hpp:964-1176).
+    int planePhys(int c, int x, int y, int z) const {
+        const int gx = x + 1, gy = y + 1, gz = twoD ? 0 : z + 1;
+        if (gx < 0 || gx >= D.lx || gy < 0 || gy >= D.ly || gz < 0 || gz >= D.lz)
+            throw UnsupportedError("TFSF surface plane outside the grid");
+        return phys[c][static_cast<std::size_t>(D.idx(gx, gy, gz))];
+    }
+
+    // genEpMu (parallelTFSF.hpp:591-694): the incident line of component c takes eps (E)
+    // or mu (H, always 1 here) and the object of each element from the plus surfaces of
+    // the box, sampled one cell beyond it: a surface parallel to the propagation whose
+    // material changes gives one value per slice across the (normal) propagation
+    // direction, a uniform one fills the whole line. The reference's three consistency
+    // checks are kept with its messages.
+    void genEpMu(int c, bool E, const std::array<int, 3>& fieldEnd, std::vector<double>& ep, std::vector<int>& ob) const {
+        ep.assign(static_cast<std::size_t>(gridLen), 0.0);
+        ob.assign(static_cast<std::size_t>(gridLen), 0);
+        const int off = E ? 0 : -1;
+        const int fieldOff = pmlThick + mMax + 5 * mTot;
         const int surInds[6] = {2, 2, 1, 1, 0, 0};
+        const int locOff[6] = {off, sz[2], off, sz[1], off, sz[0]};
         const int indStart = twoD ? 2 : 0;
-        for (int c = 0; c < 6; ++c) {
-            if (!phys[c]) continue;
-            const int* ph = phys[c];
-            for (int ii = indStart; ii < 6; ++ii) {
-                if (ii % 2 == 0) continue;  // only the plus surfaces are sampled
-                const int s = surInds[ii];
-                const int a0 = (s != 2) ? (s + 2) % 3 : 0, a1 = (s != 2) ? (s + 1) % 3 : 1;
-                const int pl0 = sz[a0], pl1 = sz[a1];
-                const int f0 = nvec[a0], f1 = nvec[a1];
-                if ((pl0 <= 1 && (!twoD || (pl1 <= 1 && (f0 > 3 || f1 > 3)))) ||
-                    (pl1 <= 1 && (!twoD || (pl0 <= 1 && (f0 > 3 || f1 > 3)))))
-                    continue;
-                for (int u = 0; u < pl0; ++u)
-                    for (int v = 0; v < pl1; ++v) {
-                        std::array<int, 3> q = {0, 0, 0};
-                        q[s] = loc[s] + sz[s] + 1;
-                        q[a0] = loc[a0] + u + 1;
-                        q[a1] = loc[a1] + v + 1;
-                        if (twoD) q[2] = 0;
-                        if (q[0] < 0 || q[0] >= D.lx || q[1] < 0 || q[1] >= D.ly || q[2] < 0 || q[2] >= D.lz) continue;
-                        if (ph[static_cast<std::size_t>(D.idx(q[0], q[1], q[2]))] > 0)
-                            throw UnsupportedError("TFSF surfaces in non-vacuum material are not supported");
+        const bool threeD = !twoD;
+        for (int ii = indStart; ii < 6; ++ii) {
+            const int s = surInds[ii];
+            const std::array<int, 2> pLoc = {s != 2 ? loc[(s + 2) % 3] : loc[0], s != 2 ? loc[(s + 1) % 3] : loc[1]};
+            const std::array<int, 2> pSz = {s != 2 ? sz[(s + 2) % 3] : sz[0], s != 2 ? sz[(s + 1) % 3] : sz[1]};
+            const std::array<int, 2> fSz = {s != 2 ? nvec[(s + 2) % 3] : nvec[0], s != 2 ? nvec[(s + 1) % 3] : nvec[1]};
+            if ((pSz[0] <= 1 && (threeD || (pSz[1] <= 1 && (fSz[0] > 3 || fSz[1] > 3)))) ||
+                (pSz[1] <= 1 && (threeD || (pSz[0] <= 1 && (fSz[0] > 3 || fSz[1] > 3)))))
+                continue;
+            if (ii % 2 == 0) continue;  // only the plus surfaces (m has no negative component here)
+            // the plane as getPlaneYZ / XZ / XY return it
+            std::vector<int> pv(static_cast<std::size_t>(pSz[0]) * pSz[1], 0);
+            const int at = loc[s] + locOff[ii];
+            for (int v = 0; v < pSz[1]; ++v)
+                for (int u = 0; u < pSz[0]; ++u) {
+                    int x, y, z;
+                    if (s == 0) {  // [z + sz2 y]
+                        x = at; y = pLoc[1] + v; z = pLoc[0] + u;
+                    } else if (s == 1) {  // [x + sz0 z]
+                        x = pLoc[0] + u; y = at; z = pLoc[1] + v;
+                    } else {  // [x + sz0 y]
+                        x = pLoc[0] + u; y = pLoc[1] + v; z = at;
                     }
+                    if (s != 1 && pLoc[1] + v >= nvec[1] - 2) {
+                        pv[static_cast<std::size_t>(u + pSz[0] * v)] = 0;  // rows past the grid stay 0
+                        continue;
+                    }
+                    pv[static_cast<std::size_t>(u + pSz[0] * v)] = planePhys(c, x, y, z);
+                }
+            std::vector<double> ev(pv.size());
+            for (std::size_t q = 0; q < pv.size(); ++q) {
+                const int pp = pv[q];
+                if (pp >= static_cast<int>(objs.size())) throw InputError("TFSF surface samples an unknown object");
+                ev[q] = pp > 0 ? (E ? objs[static_cast<std::size_t>(pp)].epsInf : 1.0) : 1.0;
+            }
+            bool change = false;
+            for (int a : pv)
+                if (a != pv[0] && a > -1) change = true;
+            if (change) {
+                if (mInd == -1) throw InputError("Material changes crossing TFSF boundaries only defined for normal incidence.");
+                if (mInd == s) throw InputError("Material changes can't occur along surface that is propagating the pulse.");
+                int epSz, epStride;
+                const bool across = mInd == 0 || (mInd == 2 && s == 0);
+                if (across) {
+                    epSz = pSz[1];
+                    epStride = pSz[0];
+                } else {
+                    epSz = pSz[0];
+                    epStride = 1;
+                }
+                for (int jj = 0; jj < sz[mInd]; ++jj) {
+                    const int row = (jj < sz[mInd] - fieldEnd[mInd]) ? jj : jj - 1;
+                    const int ind = across ? row : pSz[0] * row;
+                    double asum = 0.0;  // dasum: the absolute values in order
+                    for (int q = 0; q < epSz; ++q) asum += std::abs(ev[static_cast<std::size_t>(ind + q * epStride)]);
+                    if (std::abs(asum - ev[static_cast<std::size_t>(ind)] * epSz) > 1e-10)
+                        throw InputError("1) The material is not consistent across all TFSF surfaces for each slice perpendicular to the propagating direction");
+                    const int e = fieldOff + (m[mInd] >= 0 ? jj : sz[mInd] - jj - 1);
+                    if (e < 0 || e >= gridLen) throw InputError("TFSF slice outside the incident line");
+                    if (ep[static_cast<std::size_t>(e)] == 0) {
+                        ep[static_cast<std::size_t>(e)] = ev[static_cast<std::size_t>(ind)];
+                        ob[static_cast<std::size_t>(e)] = pv[static_cast<std::size_t>(ind)] > -1 ? pv[static_cast<std::size_t>(ind)] : 0;
+                    } else if (ep[static_cast<std::size_t>(e)] != ev[static_cast<std::size_t>(ind)]) {
+                        throw InputError("2) The material is not consistent across all TFSF surfaces for each slice perpendicular to the propagating direction");
+                    }
+                }
+                const int last = fieldOff + sz[mInd];
+                if (last > gridLen) throw InputError("TFSF slice outside the incident line");
+                std::fill(ep.begin(), ep.begin() + fieldOff, ep[static_cast<std::size_t>(fieldOff)]);
+                std::fill(ep.begin() + last, ep.end(), ep[static_cast<std::size_t>(last - 1)]);
+                std::fill(ob.begin(), ob.begin() + fieldOff, ob[static_cast<std::size_t>(fieldOff)]);
+                std::fill(ob.begin() + last, ob.end(), ob[static_cast<std::size_t>(last - 1)]);
+            } else if (s != mInd || sz[0] == 1 || sz[1] == 1 || sz[2] == 1) {
+                if (ev.empty()) throw InputError("TFSF surface plane without points");
+                for (double a : ep)
+                    if (a != ev[0] && a != 0.0)
+                        throw InputError("3) The material is not consistent across all TFSF surfaces for each slice perpendicular to the propagating direction.");
+                std::fill(ep.begin(), ep.end(), ev[0]);
+                std::fill(ob.begin(), ob.end(), *std::max_element(pv.begin(), pv.end()));
             }
         }
+        for (double a : ep)
+            if (a == 0.0)
+                throw UnsupportedError("TFSF line without a material (the reference divides its incident field by zero there)");
+        for (int o : ob)
+            if (o < 0 || o >= static_cast<int>(objs.size())) throw InputError("TFSF line samples an unknown object");
     }
 
     // ---- initializeIncdFields / genFieldUpParam, parallelTFSF.hpp:500-730 ----
@@ -215,9 +325,41 @@ struct TfsfBuilder {
         TfsfLine& L = T.line[c];
         if (!present[c]) return;
         L.present = true;
-        L.epMu = 1.0;
+        std::array<int, 3> fieldEnd = {0, 0, 0};
+        if (E) {
+            if (sz[i] == nvec[i] - 2) fieldEnd[i] = 1;
+        } else {
+            if (sz[j] == nvec[j] - 2) fieldEnd[j] = 1;
+            if (sz[k] == nvec[k] - 2) fieldEnd[k] = 1;
+        }
         L.dist.resize(mTot);
         for (int rr = 0; rr < mTot; ++rr) L.dist[rr] = static_cast<double>(distBase + 2 * rr) / 2.0 * dr;
+        genEpMu(c, E, fieldEnd, L.epMu, L.obj);
+        // poles of the elements the curl runs cover (genFieldUpParam, updateIncdPols): the
+        // electric poles of each element's object; the H lines have none (no magnetic poles)
+        L.nPole = 0;
+        if (E)
+            for (int x = mTot; x < gridLen - mTot; ++x)
+                L.nPole = std::max(L.nPole, static_cast<int>(objs[static_cast<std::size_t>(L.obj[static_cast<std::size_t>(x)])].gamma.size()));
+        const std::size_t len = static_cast<std::size_t>(gridLen);
+        L.pa.assign(static_cast<std::size_t>(L.nPole) * len, 0.0);
+        L.px.assign(L.pa.size(), 0.0);
+        L.pg.assign(L.pa.size(), 0.0);
+        for (int x = mTot; x < gridLen - mTot && L.nPole > 0; ++x) {
+            const Object& o = objs[static_cast<std::size_t>(L.obj[static_cast<std::size_t>(x)])];
+            for (std::size_t p = 0; p < o.gamma.size(); ++p) {
+                L.pa[p * len + static_cast<std::size_t>(x)] = o.alpha[p];
+                L.px[p * len + static_cast<std::size_t>(x)] = o.xi[p];
+                L.pg[p * len + static_cast<std::size_t>(x)] = o.gamma[p];
+            }
+        }
+        L.epChange = false;
+        for (double a : L.epMu)
+            if (a != L.epMu[0]) L.epChange = true;
+        L.dLine = L.nPole > 0;
+        for (double a : L.epMu)
+            if (a != 1.0) L.dLine = true;
+        if (!E && L.dLine) throw UnsupportedError("TFSF line with a permeability other than 1");
         L.runs = upParams(E, gridLen, i, j, k);
         L.pulseRuns = upParams(E, T.pulseLen, i, j, k);
         // neighbours: the other kind's components j and k
@@ -230,7 +372,9 @@ struct TfsfBuilder {
         L.recOffIdx = pmlThick + mMax + 5 * mTot - distBase % 2;
     }
 
-    // One run over a uniform line (the material is vacuum everywhere on it).
+    // The curl runs of a line (genFieldUpParam): the reference starts a new run where the
+    // element's object changes, with the same offsets and prefactors, so the runs of one
+    // line are stepped here as one run over the same elements.
     std::vector<TfsfRun> upParams(bool E, int len, int i, int j, int k) const {
         (void)i;
         std::vector<TfsfRun> out;
@@ -245,7 +389,7 @@ struct TfsfBuilder {
             r.posK = ii + (E ? -1 * (m[k] + m[k] % 2) / 2 : (m[k] + m[k] % 2) / 2);
             r.negK = ii + (E ? m[k] / 2 : -1 * m[k] / 2);
             ++ii;
-            while (ii < len - mTot) ++ii;  // uniform material: one run
+            while (ii < len - mTot) ++ii;
             r.n = ii - r.indI;
             out.push_back(r);
         }
@@ -253,7 +397,8 @@ struct TfsfBuilder {
     }
 
     // ---- IncdCPML, PML/PML.hpp:117-271 ----
-    std::vector<TfsfPsi> incdCPML(int c, int gridLenI) const {
+    // epsV, muV: the material constants of both ends (epsPl = epsMn, muPl = muMn here)
+    std::vector<TfsfPsi> incdCPML(int c, int gridLenI, double epsV, double muV) const {
         const bool E = c < 3;
         const int ci = c % 3;
         const int cor_ii = ci, cor_jj = (ci + 1) % 3, cor_kk = (ci + 2) % 3;
@@ -271,25 +416,24 @@ struct TfsfBuilder {
         const int thick = pmlThick;
         if (gridK && m[cor_jj] != 0) {
             if (!psiJ) throw InputError("TFSF CPML without its auxiliary field");
-            out.push_back(upList(c, cor_jj, other + cor_kk, mOffHalf, true, gridLenI - 1 - thick - mTot, thick));
-            out.push_back(upList(c, cor_jj, other + cor_kk, mOffHalf, false, std::abs(mTot), thick));
+            out.push_back(upList(c, cor_jj, other + cor_kk, mOffHalf, true, gridLenI - 1 - thick - mTot, thick, epsV, muV));
+            out.push_back(upList(c, cor_jj, other + cor_kk, mOffHalf, false, std::abs(mTot), thick, epsV, muV));
         }
         if (gridJ && m[cor_kk] != 0) {
             if (!psiK) throw InputError("TFSF CPML without its auxiliary field");
-            out.push_back(upList(c, cor_kk, other + cor_jj, mOffHalf, true, gridLenI - 1 - thick - mTot, thick));
-            out.push_back(upList(c, cor_kk, other + cor_jj, mOffHalf, false, std::abs(mTot), thick));
+            out.push_back(upList(c, cor_kk, other + cor_jj, mOffHalf, true, gridLenI - 1 - thick - mTot, thick, epsV, muV));
+            out.push_back(upList(c, cor_kk, other + cor_jj, mOffHalf, false, std::abs(mTot), thick, epsV, muV));
         }
         return out;
     }
 
-    // getUpList, PML/PML.hpp:222-271 (eps = mu = 1 on both ends)
-    TfsfPsi upList(int c, int dir, int nbr, double distOff, bool pl, int startPt, int dirMax) const {
+    // getUpList, PML/PML.hpp:222-271
+    TfsfPsi upList(int c, int dir, int nbr, double distOff, bool pl, int startPt, int dirMax, double epsV, double muV) const {
         const bool E = c < 3;
         const int ci = c % 3;
         const int jDir = (ci + 1) % 3;
         TfsfPsi p;
         p.nbr = nbr;
-        const double epsV = 1.0, muV = 1.0;
         p.Db = dt / (d[dir] * (E ? epsV : muV));
         p.gridLoc = startPt;
         p.n = dirMax;
@@ -329,6 +473,7 @@ struct TfsfBuilder {
         int comp, line, incd;
         double pref;
         bool toD;
+        int div;
     };
 
     void addStructs(int c, bool E, bool pl, std::vector<SurfaceTerm>& out) {
@@ -445,35 +590,62 @@ struct TfsfBuilder {
         const int mOff = static_cast<int>(std::floor(mOffSet - mOffHalf));
         const int ir = std::abs(m[0] * locRelOr[0]) + std::abs(m[1] * locRelOr[1]) + std::abs(m[2] * locRelOr[2]);
         const long long cellStride = addVec1[0] + static_cast<long long>(D.lx) * (addVec1[2] + static_cast<long long>(D.lz) * addVec1[1]);
+        // the material of the corrected component's own line decides, per run of equal
+        // pole count along the row, whether the run goes to D (the object has poles) and,
+        // where eps varies along that line, the values are divided by it
+        const TfsfLine& Lc = T.line[pol];
+        const int div = Lc.epChange ? pol : -1;
+        auto lineObj = [&](long long idx) -> const Object& {
+            if (idx < 0 || idx >= gridLen) throw UnsupportedError("TFSF surface run reads its line's material outside the line");
+            return objs[static_cast<std::size_t>(Lc.obj[static_cast<std::size_t>(idx)])];
+        };
         for (int ll = 0; ll < sz1; ++ll) {
-            // one run per row: the line material is uniform (vacuum), no poles: the U list
-            const int incdStart = ir + pmlThick + mOff + 6 * mTot + ll * addIncdProp;
-            if (segs && sz0Max > 0) {
-                TfsfSegment sg;
-                sg.cell0 = D.idx(locTemp[0] + ll * addVec2[0], locTemp[1] + ll * addVec2[1], locTemp[2] + ll * addVec2[2]);
-                sg.cellStride = cellStride;
-                sg.incd0 = incdStart;
-                sg.incdStride = strideIncd;
-                sg.n = sz0Max;
-                sg.line = polIncd;
-                sg.comp = pol;
-                sg.pref = prefactor;
-                segs->push_back(sg);
-            }
-            for (int s0 = 0; s0 < sz0Max; ++s0) {
-                const int x = locTemp[0] + ll * addVec2[0] + s0 * addVec1[0];
-                const int y = locTemp[1] + ll * addVec2[1] + s0 * addVec1[1];
-                const int z = locTemp[2] + ll * addVec2[2] + s0 * addVec1[2];
-                SurfaceTerm st;
-                st.cell = D.idx(x, y, z);
-                st.comp = pol;
-                st.line = polIncd;
-                st.incd = incdStart + s0 * strideIncd;
-                st.pref = prefactor;
-                st.toD = false;
-                if (st.cell < 0 || st.cell >= D.cells() || st.incd < 0 || st.incd >= gridLen)
-                    throw InputError("TFSF surface outside the grid");
-                out.push_back(st);
+            const int base = ir + pmlThick + mOff + 6 * mTot + ll * addIncdProp;
+            int s0 = 0;
+            while (s0 < sz0Max) {
+                const int incdStart = base + s0 * strideIncd;
+                const int r0 = s0;
+                ++s0;
+                // the reference compares the run start with incdStart + s0 * stride, s0
+                // counted from the row start (parallelTFSF.hpp:955-957)
+                const std::size_t poles0 = lineObj(incdStart).gamma.size();
+                while (true) {
+                    const Object& o = lineObj(incdStart + static_cast<long long>(s0) * strideIncd);
+                    if (!((!E || o.gamma.size() == poles0) && s0 < sz0Max)) break;
+                    ++s0;
+                }
+                const int n = s0 - r0;
+                const bool toD = E && !lineObj(incdStart).alpha.empty();
+                const long long cell0 =
+                    D.idx(locTemp[0] + ll * addVec2[0] + r0 * addVec1[0], locTemp[1] + ll * addVec2[1] + r0 * addVec1[1],
+                          locTemp[2] + ll * addVec2[2] + r0 * addVec1[2]);
+                if (segs) {
+                    TfsfSegment sg;
+                    sg.cell0 = cell0;
+                    sg.cellStride = cellStride;
+                    sg.incd0 = incdStart;
+                    sg.incdStride = strideIncd;
+                    sg.n = n;
+                    sg.line = polIncd;
+                    sg.comp = pol;
+                    sg.pref = prefactor;
+                    sg.toD = toD;
+                    sg.div = toD ? -1 : div;
+                    segs->push_back(sg);
+                }
+                for (int r = 0; r < n; ++r) {
+                    SurfaceTerm st;
+                    st.cell = cell0 + r * cellStride;
+                    st.comp = pol;
+                    st.line = polIncd;
+                    st.incd = incdStart + r * strideIncd;
+                    st.pref = prefactor;
+                    st.toD = toD;
+                    st.div = toD ? -1 : div;
+                    if (st.cell < 0 || st.cell >= D.cells() || st.incd < 0 || st.incd >= gridLen)
+                        throw InputError("TFSF surface outside the grid");
+                    out.push_back(st);
+                }
             }
         }
     }
@@ -509,6 +681,7 @@ struct TfsfBuilder {
         out.incd.reserve(n);
         out.pref.reserve(n);
         out.toD.reserve(n);
+        out.div.reserve(n);
         for (std::size_t p = 0; p < n; ++p) {
             const SurfaceTerm& st = terms[static_cast<std::size_t>(kv[p].second)];
             if (p == 0 || kv[p].first != kv[p - 1].first) {
@@ -520,6 +693,7 @@ struct TfsfBuilder {
             out.incd.push_back(st.incd);
             out.pref.push_back(st.pref);
             out.toD.push_back(st.toD ? 1 : 0);
+            out.div.push_back(st.div);
         }
         if (n) out.start.push_back(static_cast<long long>(out.line.size()));
     }
@@ -529,13 +703,17 @@ struct TfsfBuilder {
 
 void build_tfsf(const Inputs& in, const Dims& D, double dt, const int* const phys[6],
                 const std::vector<Object>& objs, Plan& P) {
-    (void)objs;
     for (const TfsfSpec& t : in.tfsf) {
         // parallelFDTDField.cpp:626-628: a surface with zero x and y size is skipped
         if (t.sz[0] == 0 && t.sz[1] == 0) continue;
         TfsfPlan T;
-        TfsfBuilder b(in, D, dt, t, phys, T);
+        TfsfBuilder b(in, D, dt, t, phys, objs, T);
         b.build();
+        for (const TfsfAdds* a : {&T.addH, &T.addE})
+            for (std::size_t q = 0; q < a->cells(); ++q)
+                for (long long k = a->start[q]; k < a->start[q + 1]; ++k)
+                    if (a->toD[static_cast<std::size_t>(k)] && (a->comp[q] > 2 || !P.comp[a->comp[q]].hasD))
+                        throw UnsupportedError("TFSF correction into a D field the grid does not have");
         P.tfsf.push_back(std::move(T));
     }
 }

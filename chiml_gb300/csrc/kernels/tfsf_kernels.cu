@@ -9,10 +9,16 @@
 //                 adds the E corrections (from the new H lines). Every line element is
 //                 updated by one thread in the reference's per-element order (pulse add,
 //                 J and K curl terms, then each CPML psi list touching it): a half only
-//                 reads lines of the other kind, so its elements are independent. The
+//                 reads lines of the other kind, so its elements are independent. A line
+//                 in layered material (updateIncdPols, incdD2U, SOURCE/parallelTFSF.cpp:
+//                 44-68) moves its poles from the element's previous value first, takes
+//                 the curl into its D grid, then divides by the element's eps. The
 //                 corrections: face rows of cells with one term each, one thread per cell
 //                 along the row; cells on face edges (several terms) one thread each,
-//                 adding their terms in the reference's order: F += pref * Re(line value).
+//                 adding their terms in the reference's order: F (or D inside a dispersive
+//                 layer) += pref * Re(line value), the value first divided by eps where
+//                 eps varies along the line (addIncdFieldsEPChange,
+//                 SOURCE/parallelTFSF.cpp:98-107).
 //                 The second launch also writes the incident values recorded for flux
 //                 normalisation, from the block that finishes last.
 // The lines are complex FP64 in both precision forms (a few thousand points).
@@ -30,43 +36,72 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// The main-grid field of component c (0..5), selected without a dynamic index into an
-// array (which would live in local memory).
+// The main-grid field of component c (0..5: E, H; 6..8: D of E), selected without a
+// dynamic index into an array (which would live in local memory).
 template <typename T>
-struct Fields6 {
-    T* f0;
-    T* f1;
-    T* f2;
-    T* f3;
-    T* f4;
-    T* f5;
+struct Fields9 {
+    T* f[9];
     __device__ __forceinline__ T* operator[](int c) const {
-        T* r = f0;
-        r = c == 1 ? f1 : r;
-        r = c == 2 ? f2 : r;
-        r = c == 3 ? f3 : r;
-        r = c == 4 ? f4 : r;
-        r = c == 5 ? f5 : r;
+        T* r = f[0];
+#pragma unroll
+        for (int k = 1; k < 9; ++k) r = c == k ? f[k] : r;
         return r;
     }
 };
 
-// Surface corrections of cell q of list `which` (0 H, 1 E).
+// Re(line value) of a surface term, divided by eps of line div where div >= 0.
+__device__ __forceinline__ double termValue(const TfsfDev& t, int line, int incd, int div) {
+    double x = t.line[line].U[incd].x;
+    if (div >= 0) x = x / t.line[div].eps[incd];
+    return x;
+}
+
+// Surface corrections of cell q of list `which` (0 H, 1 E): the terms to the field and
+// those to its D field are two separate sums, each in the reference's order.
 template <typename T>
-__device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, const Fields6<T>& F) {
+__device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, const Fields9<T>& F) {
     if (q >= t.nCell[which]) return;
-    T* f = F[t.comp[which][q]];
+    const int c = t.comp[which][q];
+    T* f = F[c];
+    T* dF = F[6 + c % 3];
     const long long cell = t.cell[which][q];
-    double v = static_cast<double>(f[cell]);
-    for (int k = t.start[which][q]; k < t.start[which][q + 1]; ++k)
-        v += t.termPref[which][k] * t.line[t.termLine[which][k]].U[t.termIncd[which][k]].x;
-    f[cell] = static_cast<T>(v);
+    bool anyU = false, anyD = false;
+    double v = 0.0, w = 0.0;
+    for (int k = t.start[which][q]; k < t.start[which][q + 1]; ++k) {
+        const int flag = t.termFlag[which][k];
+        const double add = t.termPref[which][k] * termValue(t, t.termLine[which][k], t.termIncd[which][k], (flag >> 1) - 1);
+        if (flag & 1) {
+            if (!anyD) w = static_cast<double>(dF[cell]);
+            anyD = true;
+            w += add;
+        } else {
+            if (!anyU) v = static_cast<double>(f[cell]);
+            anyU = true;
+            v += add;
+        }
+    }
+    if (anyU) f[cell] = static_cast<T>(v);
+    if (anyD) dF[cell] = static_cast<T>(w);
 }
 
 // Element x of one grid of line c (incident grid when pulseGrid is false).
 __device__ __forceinline__ void lineElement(const TfsfDev& t, int c, bool pulseGrid, int x, int s) {
     const TfsfLineDev& L = t.line[c];
-    double2* G = pulseGrid ? L.pul : L.U;
+    const bool dLine = !pulseGrid && L.D != nullptr;
+    if (dLine) {
+        // poles from the element's value before this step (updateIncdPols)
+        const double2 u = L.U[x];
+        for (int p = 0; p < L.nPole; ++p) {
+            const long long i = static_cast<long long>(p) * t.gridLen + x;
+            const double2 old = L.P[i];
+            double2 n = rmul(L.pa[i], old);
+            n = cadd(n, rmul(L.px[i], L.Pprev[i]));
+            n = cadd(n, rmul(L.pg[i], u));
+            L.Pprev[i] = old;
+            L.P[i] = n;
+        }
+    }
+    double2* G = pulseGrid ? L.pul : (dLine ? L.D : L.U);
     double2 v = G[x];
     const int pr = x - t.pulAddStart;
     if (pr >= 0 && pr < t.mTot) v = cadd(v, cmul(L.prefact, t.pulseTab[(static_cast<long long>(s) * 6 + c) * t.mTot + pr]));
@@ -97,6 +132,16 @@ __device__ __forceinline__ void lineElement(const TfsfDev& t, int c, bool pulseG
         v = cadd(v, rmul(P.Db, ps));
     }
     G[x] = v;
+    if (dLine) {
+        // incdD2U: U = D / eps, then U += (-P_p) / eps for each pole
+        const double e = L.eps[x];
+        double2 u = make_double2(v.x / e, v.y / e);
+        for (int p = 0; p < L.nPole; ++p) {
+            const double2 q = L.P[static_cast<long long>(p) * t.gridLen + x];
+            u = cadd(u, make_double2((-1.0 * q.x) / e, (-1.0 * q.y) / e));
+        }
+        L.U[x] = u;
+    }
 }
 
 // Element e of the lines c0 .. c0 + 2 (incident grid, then pulse grid, per line).
@@ -131,24 +176,24 @@ __device__ __forceinline__ void recordIncident(const TfsfDev& t, int s, int c) {
 // With `record`, the block that finishes last (a ticket counter, no waiting) writes the
 // incident records once every line of the half has been stepped.
 template <typename T>
-__global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, int record, T* F0,
-                                                            T* F1, T* F2, T* F3, T* F4, T* F5, const int* __restrict__ step) {
+__global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, int record,
+                                                            const Fields9<T> F, const int* __restrict__ step) {
     const int s = *step;
     if (s >= t.nSteps) return;
     const int b = static_cast<int>(blockIdx.x);
     if (b < lineBlocks) {
         lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
     } else {
-        const Fields6<T> F{F0, F1, F2, F3, F4, F5};
         const int sb = b - lineBlocks;
         if (sb < t.segBlocks[which]) {
             const int2 w = t.segWork[which][sb];
             const TfsfSegDev& g = t.seg[which][w.x];
             const int r = w.y * kTfsfThreads + static_cast<int>(threadIdx.x);
             if (r < g.n) {
-                T* f = F[g.comp];
+                T* f = F[g.toD ? 6 + g.comp : g.comp];
                 const long long cell = g.cell0 + r * g.cellStride;
-                f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * t.line[g.line].U[g.incd0 + r * g.incdStride].x);
+                const int incd = g.incd0 + r * g.incdStride;
+                f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * termValue(t, g.line, incd, g.div));
             }
         } else {
             addCell(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
@@ -172,18 +217,19 @@ __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int
 }  // namespace
 
 template <typename T>
-void launch_tfsf_step(const TfsfDev& t, T* const fields[6], const int* step, void* stream) {
+void launch_tfsf_step(const TfsfDev& t, T* const fields[9], const int* step, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int lineBlocks = (3 * (t.gridLen + t.pulseLen) + kTfsfThreads - 1) / kTfsfThreads;
+    Fields9<T> F;
+    for (int k = 0; k < 9; ++k) F.f[k] = fields[k];
     for (int half = 0; half < 2; ++half) {
         const int addBlocks = t.segBlocks[half] + (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
-        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, fields[0],
-                                                                        fields[1], fields[2], fields[3], fields[4], fields[5], step);
+        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
     }
 }
 
-template void launch_tfsf_step<float>(const TfsfDev&, float* const[6], const int*, void*);
-template void launch_tfsf_step<double>(const TfsfDev&, double* const[6], const int*, void*);
+template void launch_tfsf_step<float>(const TfsfDev&, float* const[9], const int*, void*);
+template void launch_tfsf_step<double>(const TfsfDev&, double* const[9], const int*, void*);
 
 }  // namespace dev
 }  // namespace chiml

@@ -213,6 +213,7 @@ struct EmitterSim {
 struct TfsfSim {
     const TfsfPlan& T;
     std::vector<cplx> U[6], Dl[6], pul[6];  // incident field, its D / B, pulse grid
+    std::vector<std::vector<cplx>> P[6], Pprev[6];  // pole polarisations of a line in layered material
     std::vector<std::vector<cplx>> psi[6], psiPul[6];
     std::vector<cplx> pulseVec;
     double tStep = 0.0;
@@ -224,6 +225,8 @@ struct TfsfSim {
             U[c].assign(T.gridLen, 0.0);
             Dl[c].assign(T.gridLen, 0.0);
             pul[c].assign(T.pulseLen, 0.0);
+            P[c].assign(static_cast<std::size_t>(L.nPole), std::vector<cplx>(T.gridLen, 0.0));
+            Pprev[c] = P[c];
             for (auto& p : L.pml) psi[c].emplace_back(p.n, 0.0);
             for (auto& p : L.pmlPulse) psiPul[c].emplace_back(p.n, 0.0);
         }
@@ -232,10 +235,13 @@ struct TfsfSim {
 
     cplx rec(int c, bool off) const { return T.line[c].present ? pul[c][off ? T.line[c].recOffIdx : T.line[c].recIdx] : cplx(0.0); }
 
-    static void addSurface(const TfsfAdds& a, const std::vector<cplx>* lines, std::vector<double>* F, std::vector<double>* Dd) {
+    void addSurface(const TfsfAdds& a, std::vector<double>* F, std::vector<double>* Dd) const {
+        const std::vector<cplx>* lines = U;
         for (std::size_t c = 0; c < a.cells(); ++c)
             for (long long q = a.start[c]; q < a.start[c + 1]; ++q) {
-                const double v = a.pref[q] * std::real(lines[a.line[q]][a.incd[q]]);
+                double x = std::real(lines[a.line[q]][a.incd[q]]);
+                if (a.div[q] >= 0) x = x / T.line[a.div[q]].epMu[a.incd[q]];
+                const double v = a.pref[q] * x;
                 if (a.toD[q]) Dd[a.comp[c]][a.cell[c]] += v;
                 else F[a.comp[c]][a.cell[c]] += v;
             }
@@ -276,20 +282,45 @@ struct TfsfSim {
             for (int r = 0; r < T.mTot; ++r) pulseVec[r] = pulseVec[r] + p.value(tStep * T.dt - L.dist[r]);
     }
 
+    // updateIncdPols (SOURCE/parallelTFSF.cpp:44-58): P = alpha P + xi P_prev + gamma U
+    // from the line before this step; elements past an object's poles have zero constants
+    void updatePoles(int c) {
+        const TfsfLine& L = T.line[c];
+        const std::size_t len = static_cast<std::size_t>(T.gridLen);
+        for (int p = 0; p < L.nPole; ++p)
+            for (std::size_t x = 0; x < len; ++x) {
+                const cplx old = P[c][p][x];
+                cplx v = cplx(L.pa[p * len + x], 0.0) * old;
+                v = v + cplx(L.px[p * len + x], 0.0) * Pprev[c][p][x];
+                v = v + cplx(L.pg[p * len + x], 0.0) * U[c][x];
+                P[c][p][x] = v;
+                Pprev[c][p][x] = old;
+            }
+    }
+
+    // incdD2U (SOURCE/parallelTFSF.cpp:60-68): U = D / eps, then U += -P_p / eps per pole
+    void d2u(int c) {
+        const TfsfLine& L = T.line[c];
+        for (int x = 0; x < T.gridLen; ++x) U[c][x] = Dl[c][x] / L.epMu[x];
+        for (int p = 0; p < L.nPole; ++p)
+            for (int x = 0; x < T.gridLen; ++x) U[c][x] = U[c][x] + (-1.0 * P[c][p][x]) / L.epMu[x];
+    }
+
     void stepLines() {
         for (int h = 3; h < 6; ++h) {
             if (!T.line[h].present) continue;
             fillPulse(h);
             updateLine(h, Dl[h], T.line[h].runs, T.line[h].pml, psi[h], U);
             updateLine(h, pul[h], T.line[h].pulseRuns, T.line[h].pmlPulse, psiPul[h], pul);
-            for (int x = 0; x < T.gridLen; ++x) U[h][x] = Dl[h][x] / T.line[h].epMu;
+            d2u(h);
         }
         for (int e = 0; e < 3; ++e) {
             if (!T.line[e].present) continue;
             fillPulse(e);
+            updatePoles(e);
             updateLine(e, Dl[e], T.line[e].runs, T.line[e].pml, psi[e], U);
             updateLine(e, pul[e], T.line[e].pulseRuns, T.line[e].pmlPulse, psiPul[e], pul);
-            for (int x = 0; x < T.gridLen; ++x) U[e][x] = Dl[e][x] / T.line[e].epMu;
+            d2u(e);
         }
         tStep += 1.0;
     }
@@ -580,9 +611,9 @@ struct OracleSim {
                 rec.incH[c][2 * step + 0] = t->rec(3 + c, false);
                 rec.incH[c][2 * step + 1] = t->rec(3 + c, true);
             }
-            TfsfSim::addSurface(t->T.addH, t->U, F, Dd);
+            t->addSurface(t->T.addH, F, Dd);
             t->stepLines();
-            TfsfSim::addSurface(t->T.addE, t->U, F, Dd);
+            t->addSurface(t->T.addE, F, Dd);
             for (int c = 0; c < 3; ++c) {
                 rec.incE[c][2 * step + 0] = t->rec(c, false);
                 rec.incE[c][2 * step + 1] = t->rec(c, true);

@@ -424,6 +424,58 @@ def _qe_dists_2d():
     return cfg
 
 
+def _layer_scene(layers, m=(0, 0, 1), theta=0.0, phi=90.0, psi=0.0, n=36, steps=200, sphere=None, det="Ex"):
+    """3-D TFSF box (4 cells inside the CPML) with material layers (block objects that
+    span the cell across the propagation axis) crossing its side surfaces; the flux box
+    and a point detector of component ``det`` sit inside the box. ``layers``: (lo, hi,
+    eps, pols) along the propagation axis, in a units; ``sphere``: (centre, radius, eps),
+    a scatterer inside the flux box, so that every face of the flux box carries scattered
+    power and not only rounding noise."""
+    cfg = configs.config2(n=n, pml=6, steps=steps, nell=0, nfreq=5, metal_radius_cells=0, tfsf=True)
+    cfg["DetectorList"][0]["type"] = det
+    axis = [i for i in range(3) if m[i] != 0][0]
+    size = cfg["CompCell"]["size"][0]
+    objs = []
+    if sphere is not None:
+        objs.append(_shape("sphere", sphere[0], sphere[2], radius=sphere[1]))
+    for lo, hi, eps, pols in layers:
+        loc = [0.0, 0.0, 0.0]
+        sz = [2 * size, 2 * size, 2 * size]
+        loc[axis] = (lo + hi) / 2
+        sz[axis] = hi - lo
+        objs.append(_shape("block", loc, eps, pols, size=sz))
+    cfg["ObjectList"] = objs
+    t = cfg["TFSF"][0]
+    width = 0.2e-15 / configs.T_UNIT
+    t["PulseList"] = [configs._gauss(configs.A / 550e-9, 1.0 / width, 4.0, 2 * width)]
+    t["pmlThick"] = 8
+    t["m"] = list(m)
+    t["theta"], t["phi"], t["psi"] = theta, phi, psi
+    return cfg
+
+
+def _tfsf_layer_3d():
+    """Normal incidence along +z onto a dielectric substrate (eps 2.25) whose face lies
+    inside the TFSF box: the incident lines are layered, the surface terms inside the
+    substrate are divided by its eps."""
+    return _layer_scene([(0.1, 2.0, 2.25, [])], sphere=([0.03, 0.0, -0.11], 0.15, 3.0))
+
+
+def _tfsf_film_3d():
+    """Normal incidence along +z onto a Drude-Lorentz film (eps_inf 2) on a dielectric
+    substrate, both crossing the box sides: the lines carry the film's poles and the
+    corrections inside the film go to D."""
+    film = configs.drude_lorentz_pols(9.0, [(1.0, 0.07, 0.0), (1.0, 0.4, 2.6)])
+    return _layer_scene([(0.0, 0.2, 2.0, film), (0.2, 2.0, 1.8, [])], sphere=([0.03, 0.0, -0.15], 0.13, 3.0))
+
+
+def _tfsf_layer_x():
+    """Normal incidence along +x (Ey) onto a Lorentz layer and a dielectric substrate."""
+    lor = configs.drude_lorentz_pols(3.0, [(0.6, 0.3, 3.2)])
+    return _layer_scene([(-0.05, 0.1, 1.5, lor), (0.25, 2.0, 2.5, [])], m=(1, 0, 0), theta=90.0, phi=0.0,
+                        sphere=([-0.19, 0.03, 0.0], 0.12, 3.0), det="Ey")
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -455,6 +507,9 @@ CASES = {
     "dip_surface_b": _dip_surface_b,
     "qe_dists_3d": _qe_dists_3d,
     "qe_dists_2d": _qe_dists_2d,
+    "tfsf_layer_3d": _tfsf_layer_3d,
+    "tfsf_film_3d": _tfsf_film_3d,
+    "tfsf_layer_x": _tfsf_layer_x,
 }
 
 
@@ -513,7 +568,34 @@ INPUT_FILES = {
 
 # Inputs the reference build does not finish: <case>/ref_error.txt keeps the last line it
 # printed, and the engine must reject the input instead of running it.
+def _tfsf_layer_oblique():
+    """A substrate crossing the box under oblique incidence: the reference allows material
+    changes across the surfaces only for normal incidence (genEpMu throws)."""
+    return _layer_scene([(0.1, 2.0, 2.25, [])], m=(1, 0, 1), theta=45.0, phi=0.0)
+
+
+def _tfsf_sphere_cross():
+    """A sphere crossing the side surfaces: its slices across the propagation are not
+    uniform, which genEpMu refuses."""
+    cfg = _layer_scene([])
+    cfg["ObjectList"] = [_shape("sphere", [0.0, 0.3, 0.0], 2.0, radius=0.2)]
+    return cfg
+
+
+def _tfsf_layer_2d():
+    """2-D TE along +y onto a substrate: the normal plane fills the whole line first, so
+    the layered side plane disagrees with it and genEpMu throws."""
+    cfg = _tfsf_2d_te()
+    cfg["TFSF"][0]["m"] = [0, 1, 0]
+    cfg["TFSF"][0]["theta"], cfg["TFSF"][0]["phi"] = 90.0, 90.0
+    cfg["ObjectList"] = [_shape("block", [0.0, 1.0, 0.0], 2.0, size=[6.0, 2.0, 0.0])]
+    return cfg
+
+
 FAILING = {
+    "tfsf_layer_oblique": _tfsf_layer_oblique,
+    "tfsf_sphere_cross": _tfsf_sphere_cross,
+    "tfsf_layer_2d": _tfsf_layer_2d,
     "qe_two_objects": _qe_two_objects,
     "ordip_2d_tm": _ordip_2d("Ez"),
     "ordip_2d_te": _ordip_2d("Hz"),
