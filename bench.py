@@ -18,8 +18,9 @@ scene run to its last step (c1 and the c4 members at full size, c2 at 128^3, c3 
 c5 on the crop), the worst relative L2 of each data column group of the detector, flux and
 emitter output files.
 
-`value` is the FP32/FP64-split form (fields, CPML and polarisations in FP32,
-DFT accumulators in FP64) with all state resident in HBM; `fp64` is the same
+`value` is the split form (fields, CPML and polarisations in FP32; DFT sums and
+emitter density matrices as float-float pairs; TFSF lines in FP64) with all state
+resident in HBM; `fp64` is the same
 workload in FP64 (the parity form). `e2e` times the public C ABI end to end:
 chiml_create (JSON read, plan, upload), the K steps, chiml_finalize (flux integration
 on the device, download and file writes). Under torchrun every rank runs its own replica (the
@@ -130,11 +131,11 @@ WORKLOADS = {
     "c1": ("Gcell-updates/s (FP32/FP64-split, 2-D TMz 400^2)",
            "2-D TMz: %s cells, 20-cell CPML, dielectric disk, Ez point source, 8 point detectors, flux line x 100 freqs",
            400, "config1"),
-    "c3": ("Gcell-updates/s (FP32/FP64-split fields, FP64 density matrices, 3-D Maxwell-Liouville 192^3)",
+    "c3": ("Gcell-updates/s (FP32 fields, float-float density matrices, 3-D Maxwell-Liouville 192^3)",
            "3-D Maxwell-Liouville: %s cells, 12-cell CPML, 20-cell slab of 3-level ladder emitters (9 ensemble members "
            "per cell from 20 meV Gaussian broadening), 1e26 m^-3, Ez plane source at 2.1 eV, flux plane x 50 freqs",
            192, "config3"),
-    "c5": ("Gcell-updates/s (FP32/FP64-split fields, FP64 density matrices, 3-D mixed 640x640x320)",
+    "c5": ("Gcell-updates/s (FP32 fields, float-float density matrices, 3-D mixed 640x640x320)",
            "3-D mixed: %s cells, dx=4 nm, 16-cell CPML, 16 uniaxial ellipsoids, Drude film, 10-cell sheet of 4-level "
            "emitters (1e26 m^-3), p-polarised TFSF pulse along (1,1,3) at 550 nm, 6 DFT flux planes x 200 freqs",
            640, "config5"),
@@ -162,6 +163,11 @@ def _dims(name, n):
     if name == "c5":
         return "%dx%dx%d" % (n, n, n // 2)
     return "%d^3" % n
+
+
+def _metric(name, n):
+    """The workload's metric name, with its grid size when --n changes it."""
+    return WORKLOADS[name][0].replace(_dims(name, WORKLOADS[name][2]), _dims(name, n))
 
 
 def _workload(n, steps, name="c2"):
@@ -326,7 +332,7 @@ def run_ours(args):
     if rank == 0:
         launches = sp["stats"].kernels_per_step * args.steps
         line = {
-            "metric": WORKLOADS[args.workload][0],
+            "metric": _metric(args.workload, n),
             "value": round(value, 3),
             "unit": "Gcell-updates/s",
             "n_gpus": world,
@@ -336,7 +342,7 @@ def run_ours(args):
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f32 fields, f64 DFT accumulators",
+            "dtype": "f32 fields; DFT sums and emitter density matrices as float-float (f32 pairs)",
             "data": "synthetic (seeded PCG64 geometry, chiml_gb300.configs.%s)" % WORKLOADS[args.workload][3],
             "config": {
                 "workload": WORKLOADS[args.workload][1] % _dims(args.workload, n),
@@ -417,7 +423,7 @@ def run_reference(args):
     sim.close()
     v = cells * args.steps / total_s / 1e9
     line = {
-        "metric": WORKLOADS[args.workload][0],
+        "metric": _metric(args.workload, args.n),
         "value": round(v, 5),
         "unit": "Gcell-updates/s",
         "impl": "reference",
@@ -515,7 +521,7 @@ def run_batch(args):
         "metric": C4_METRIC, "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * t_batch / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 fields, f64 density matrices and DFT accumulators",
+        "dtype": "f32 fields; DFT sums and emitter density matrices as float-float (f32 pairs)",
         "data": "synthetic (seeded PCG64 sizes and sweep values, chiml_gb300.configs.config4)",
         "config": {"workload": C4_WORKLOAD % len(paths), "members": len(paths), "cells": cells,
                    "graph_steps": args.graph, "create_s": round(t_create, 2),
