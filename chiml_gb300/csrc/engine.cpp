@@ -738,6 +738,7 @@ private:
                     throw InputError("TFSF line material set-up inconsistent");
                 d.eps = mem_.upload(L.epMu);
                 d.D = L.dLine ? mem_.alloc<double2>(len) : nullptr;
+                if (L.dLine) t.layered = 1;
                 d.nPole = L.nPole;
                 if (L.nPole > 0) {
                     d.P = mem_.alloc<double2>(static_cast<std::size_t>(L.nPole) * len);
@@ -831,6 +832,7 @@ private:
                         dev::TfsfSegDev d{};
                         d.toD = g.toD ? 1 : 0;
                         d.div = g.div;
+                        if (d.toD || d.div >= 0) t.layered = 1;
                         d.cell0 = pad(g.cell0 + r0 * g.cellStride);
                         d.cellStride = padOffset(g.cellStride);
                         d.incd0 = g.incd0 + r0 * g.incdStride;
@@ -874,6 +876,7 @@ private:
                         ti.push_back(a.incd[k]);
                         pref.push_back(a.pref[k]);
                         tf.push_back((a.toD[k] ? 1 : 0) | ((a.div[k] + 1) << 1));
+                        if (tf.back() != 0) t.layered = 1;
                     }
                 }
                 start.push_back(static_cast<int>(tl.size()));

@@ -63,6 +63,7 @@ struct TfsfSegDev {
 
 struct TfsfDev {
     int gridLen, pulseLen, mTot, pulAddStart, nSteps;
+    int layered;               // some line has a D grid or some term goes to D / is divided by eps
     TfsfLineDev line[6];       // 0..2 Ex..Ez, 3..5 Hx..Hz
     const double2* pulseTab;   // [step][line][mTot]: sum of the pulses at the line's pulse points
     double2* rec;              // [line][2 (nSteps + 1)]: recorded incident values (flux normalisation)

@@ -49,16 +49,19 @@ struct Fields9 {
     }
 };
 
-// Re(line value) of a surface term, divided by eps of line div where div >= 0.
+// Re(line value) of a surface term, divided by eps of line div where div >= 0 (LAY: the
+// surface crosses layered material; without it no term is divided and no code for it is
+// compiled in).
+template <bool LAY>
 __device__ __forceinline__ double termValue(const TfsfDev& t, int line, int incd, int div) {
     double x = t.line[line].U[incd].x;
-    if (div >= 0) x = x / t.line[div].eps[incd];
+    if (LAY && div >= 0) x = x / t.line[div].eps[incd];
     return x;
 }
 
 // Surface corrections of cell q of list `which` (0 H, 1 E): the terms to the field and
 // those to its D field are two separate sums, each in the reference's order.
-template <typename T>
+template <typename T, bool LAY>
 __device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, const Fields9<T>& F) {
     if (q >= t.nCell[which]) return;
     const int c = t.comp[which][q];
@@ -69,8 +72,8 @@ __device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, cons
     double v = 0.0, w = 0.0;
     for (int k = t.start[which][q]; k < t.start[which][q + 1]; ++k) {
         const int flag = t.termFlag[which][k];
-        const double add = t.termPref[which][k] * termValue(t, t.termLine[which][k], t.termIncd[which][k], (flag >> 1) - 1);
-        if (flag & 1) {
+        const double add = t.termPref[which][k] * termValue<LAY>(t, t.termLine[which][k], t.termIncd[which][k], (flag >> 1) - 1);
+        if (LAY && (flag & 1)) {
             if (!anyD) w = static_cast<double>(dF[cell]);
             anyD = true;
             w += add;
@@ -85,9 +88,10 @@ __device__ __forceinline__ void addCell(const TfsfDev& t, int which, int q, cons
 }
 
 // Element x of one grid of line c (incident grid when pulseGrid is false).
+template <bool LAY>
 __device__ __forceinline__ void lineElement(const TfsfDev& t, int c, bool pulseGrid, int x, int s) {
     const TfsfLineDev& L = t.line[c];
-    const bool dLine = !pulseGrid && L.D != nullptr;
+    const bool dLine = LAY && !pulseGrid && L.D != nullptr;
     if (dLine) {
         // poles from the element's value before this step (updateIncdPols)
         const double2 u = L.U[x];
@@ -145,14 +149,15 @@ __device__ __forceinline__ void lineElement(const TfsfDev& t, int c, bool pulseG
 }
 
 // Element e of the lines c0 .. c0 + 2 (incident grid, then pulse grid, per line).
+template <bool LAY>
 __device__ __forceinline__ void lineAny(const TfsfDev& t, int c0, int e, int s) {
     const int per = t.gridLen + t.pulseLen;
     if (e >= 3 * per) return;
     const int c = c0 + e / per;
     if (!t.line[c].present) return;
     const int x = e % per;
-    if (x < t.gridLen) lineElement(t, c, false, x, s);
-    else lineElement(t, c, true, x - t.gridLen, s);
+    if (x < t.gridLen) lineElement<LAY>(t, c, false, x, s);
+    else lineElement<LAY>(t, c, true, x - t.gridLen, s);
 }
 
 constexpr int kTfsfThreads = kTfsfRowChunk;
@@ -175,14 +180,14 @@ __device__ __forceinline__ void recordIncident(const TfsfDev& t, int s, int c) {
 // the corrections read the lines of the other kind, which this half does not write.
 // With `record`, the block that finishes last (a ticket counter, no waiting) writes the
 // incident records once every line of the half has been stepped.
-template <typename T>
+template <typename T, bool LAY>
 __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, int record,
                                                             const Fields9<T> F, const int* __restrict__ step) {
     const int s = *step;
     if (s >= t.nSteps) return;
     const int b = static_cast<int>(blockIdx.x);
     if (b < lineBlocks) {
-        lineAny(t, c0, b * kTfsfThreads + threadIdx.x, s);
+        lineAny<LAY>(t, c0, b * kTfsfThreads + threadIdx.x, s);
     } else {
         const int sb = b - lineBlocks;
         if (sb < t.segBlocks[which]) {
@@ -190,13 +195,13 @@ __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int
             const TfsfSegDev& g = t.seg[which][w.x];
             const int r = w.y * kTfsfThreads + static_cast<int>(threadIdx.x);
             if (r < g.n) {
-                T* f = F[g.toD ? 6 + g.comp : g.comp];
+                T* f = F[(LAY && g.toD) ? 6 + g.comp : g.comp];
                 const long long cell = g.cell0 + r * g.cellStride;
                 const int incd = g.incd0 + r * g.incdStride;
-                f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * termValue(t, g.line, incd, g.div));
+                f[cell] = static_cast<T>(static_cast<double>(f[cell]) + g.pref * termValue<LAY>(t, g.line, incd, g.div));
             }
         } else {
-            addCell(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
+            addCell<T, LAY>(t, which, (sb - t.segBlocks[which]) * kTfsfThreads + threadIdx.x, F);
         }
     }
     if (!record) return;
@@ -224,7 +229,10 @@ void launch_tfsf_step(const TfsfDev& t, T* const fields[9], const int* step, voi
     for (int k = 0; k < 9; ++k) F.f[k] = fields[k];
     for (int half = 0; half < 2; ++half) {
         const int addBlocks = t.segBlocks[half] + (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
-        k_tfsf_half<T><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
+        if (t.layered)
+            k_tfsf_half<T, true><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
+        else
+            k_tfsf_half<T, false><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
     }
 }
 
