@@ -8,6 +8,7 @@
 #include <cmath>
 #include <complex>
 #include <exception>
+#include <functional>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -16,6 +17,7 @@
 #include <numeric>
 #include <parallel/algorithm>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -57,20 +59,27 @@ void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw CudaError(e, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// Device allocations of a handle, freed together. The upload tasks of chiml_create run
+// on several host threads at once, so the bookkeeping is guarded.
 struct DevMem {
     std::vector<void*> ptrs;
     double bytes = 0;
     double allocSeconds = 0, copySeconds = 0;  // wall time in cudaMalloc + cudaMemset, and in copies
+    double h2d = 0;
+    std::mutex mu;
     template <typename T>
     T* alloc(std::size_t n, bool zero = true) {
         if (n == 0) return nullptr;
         const auto t0 = std::chrono::steady_clock::now();
         void* p = nullptr;
         ck(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
-        ptrs.push_back(p);
-        bytes += static_cast<double>(n * sizeof(T));
+        {
+            std::lock_guard<std::mutex> g(mu);
+            ptrs.push_back(p);
+            bytes += static_cast<double>(n * sizeof(T));
+        }
         if (zero) ck(cudaMemset(p, 0, n * sizeof(T)), "cudaMemset");
-        allocSeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        addTime(allocSeconds, t0);
         return static_cast<T*>(p);
     }
     template <typename T>
@@ -79,15 +88,42 @@ struct DevMem {
         T* p = alloc<T>(v.size(), false);
         const auto t0 = std::chrono::steady_clock::now();
         ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-        copySeconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        h2d += static_cast<double>(v.size() * sizeof(T));
+        addTime(copySeconds, t0);
+        addCopied(static_cast<double>(v.size() * sizeof(T)));
         return p;
     }
-    double h2d = 0;
+    void addCopied(double b) {
+        std::lock_guard<std::mutex> g(mu);
+        h2d += b;
+    }
+    void addTime(double& acc, std::chrono::steady_clock::time_point t0) {
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::lock_guard<std::mutex> g(mu);
+        acc += dt;
+    }
     ~DevMem() {
         for (void* p : ptrs) cudaFree(p);
     }
 };
+
+// Runs the tasks on host threads of their own (each bound to the handle's device) and
+// waits for all; the first failure in task order is rethrown.
+void runConcurrently(int device, const std::vector<std::function<void()>>& tasks) {
+    std::vector<std::exception_ptr> err(tasks.size());
+    std::vector<std::thread> th;
+    for (std::size_t k = 0; k < tasks.size(); ++k)
+        th.emplace_back([&, k] {
+            try {
+                ck(cudaSetDevice(device), "cudaSetDevice");
+                tasks[k]();
+            } catch (...) {
+                err[k] = std::current_exception();
+            }
+        });
+    for (auto& t : th) t.join();
+    for (auto& e : err)
+        if (e) std::rethrow_exception(e);
+}
 
 struct SimBase {
     virtual ~SimBase() {}
@@ -198,23 +234,6 @@ public:
         }
         ck(cudaStreamSynchronize(stream_), "DFT flush");
         clk.mark("fin-records");
-        // the face maps of every flux region, built on the host cores concurrently
-        std::vector<std::vector<FluxFaceMap>> maps(P.fluxes.size());
-        {
-            std::vector<std::exception_ptr> mErr(P.fluxes.size());
-#pragma omp parallel for schedule(dynamic, 1)
-            for (long long q = 0; q < static_cast<long long>(P.fluxes.size()); ++q) {
-                const std::size_t k = static_cast<std::size_t>(q);
-                if (P.fluxes[k].spec.save || P.fluxes[k].spec.load) continue;
-                try {
-                    maps[k] = flux_face_maps(P, k);
-                } catch (...) {
-                    mErr[k] = std::current_exception();
-                }
-            }
-            for (auto& e : mErr)
-                if (e) std::rethrow_exception(e);
-        }
         for (std::size_t q = 0; q < P.fluxes.size(); ++q) {
             const int nt = stepsDone_ / P.fluxes[q].spec.timeInt + 1;
             R.fluxRe.emplace_back();
@@ -225,7 +244,7 @@ public:
                 R.fluxFaces.emplace_back();
                 downloadDft(q, P.fluxes[q].spec.freqList.size(), R.fluxRe.back(), R.fluxIm.back());
             } else {
-                R.fluxFaces.push_back(fluxFacesOnDevice(q, nt, maps[q]));
+                R.fluxFaces.push_back(fluxFacesOnDevice(q, nt));
             }
             R.fluxSamples.push_back(nt);
         }
@@ -315,52 +334,71 @@ public:
 
     // The integrated flux of every face of flux q, [freq * nFaces + face], evaluated from the
     // accumulators on the device; only these values are copied back.
-    std::vector<cplx> fluxFacesOnDevice(std::size_t q, int nt, const std::vector<FluxFaceMap>& maps) {
+    // The face maps of flux region q on the device, built at create (the integration
+    // at finalize then only launches and reads back nfreq values per face).
+    struct FluxFacesDev {
+        bool ready = false;
+        int nFaces = 0, nTiles = 0, nfreq = 0;
+        const dev::FluxFaceDev* faces = nullptr;
+        const int4* tiles = nullptr;
+        double2* partial = nullptr;
+        double2* out = nullptr;
+    };
+    std::vector<FluxFacesDev> fluxDev_;
+
+    void prepareFluxFaces(std::size_t q, const std::vector<FluxFaceMap>& maps) {
         const FluxPlan& fp = P.fluxes[q];
-        const int nfreq = static_cast<int>(fp.spec.freqList.size());
-        const int nFaces = static_cast<int>(maps.size());
-        std::vector<cplx> res(static_cast<std::size_t>(nfreq) * nFaces, cplx(0.0, 0.0));
-        if (nFaces == 0 || nfreq == 0) return res;
-        DevMem tmp;  // freed on return
-        std::vector<dev::FluxFaceDev> faces(static_cast<std::size_t>(nFaces));
+        FluxFacesDev& fd = fluxDev_[q];
+        fd.nfreq = static_cast<int>(fp.spec.freqList.size());
+        fd.nFaces = static_cast<int>(maps.size());
+        fd.ready = true;
+        if (fd.nFaces == 0 || fd.nfreq == 0) return;
+        std::vector<dev::FluxFaceDev> faces(static_cast<std::size_t>(fd.nFaces));
         std::vector<int4> tiles;
-        for (int v = 0; v < nFaces; ++v) {
+        for (int v = 0; v < fd.nFaces; ++v) {
             const FluxFaceMap& m = maps[v];
             dev::FluxFaceDev& F = faces[v];
             F.nx = m.nx;
             F.sz = m.sz;
             for (int w = 0; w < 4; ++w) {
                 F.has[w] = m.has[w] ? 1 : 0;
-                F.start[w] = m.has[w] ? tmp.upload(m.start[w]) : nullptr;
+                F.start[w] = m.has[w] ? mem_.upload(m.start[w]) : nullptr;
                 std::vector<long long> devPt(m.pt[w].size());
                 for (std::size_t k = 0; k < devPt.size(); ++k) {
                     const long long p = m.pt[w][k];
                     if (p < 0 || p >= fp.npts) throw std::logic_error("flux map point outside the accumulators");
                     devPt[k] = dftPos_[q][static_cast<std::size_t>(p)];
                 }
-                F.pt[w] = m.has[w] ? tmp.upload(devPt) : nullptr;
-                F.scale[w] = m.has[w] ? tmp.upload(m.scale[w]) : nullptr;
+                F.pt[w] = m.has[w] ? mem_.upload(devPt) : nullptr;
+                F.scale[w] = m.has[w] ? mem_.upload(m.scale[w]) : nullptr;
             }
-            F.wx = tmp.upload(m.wx);
-            F.wy = tmp.upload(m.wy);
+            F.wx = mem_.upload(m.wx);
+            F.wy = mem_.upload(m.wy);
             F.pref = m.pref;
             F.firstTile = static_cast<int>(tiles.size());
             for (int s0 = 0; s0 < m.sz; s0 += dev::kFluxTile) tiles.push_back(make_int4(v, s0, std::min(m.sz, s0 + dev::kFluxTile), 0));
             F.nTiles = static_cast<int>(tiles.size()) - F.firstTile;
         }
-        const dev::FluxFaceDev* dFaces = tmp.upload(faces);
-        const int4* dTiles = tmp.upload(tiles);
-        double2* partial = tmp.alloc<double2>(tiles.size() * static_cast<std::size_t>(nfreq), false);
-        double2* out = tmp.alloc<double2>(res.size(), false);
+        fd.faces = mem_.upload(faces);
+        fd.tiles = mem_.upload(tiles);
+        fd.nTiles = static_cast<int>(tiles.size());
+        fd.partial = mem_.alloc<double2>(tiles.size() * static_cast<std::size_t>(fd.nfreq), false);
+        fd.out = mem_.alloc<double2>(static_cast<std::size_t>(fd.nfreq) * fd.nFaces, false);
+    }
+
+    std::vector<cplx> fluxFacesOnDevice(std::size_t q, int nt) {
+        const FluxFacesDev& fd = fluxDev_[q];
+        if (!fd.ready) throw std::logic_error("flux face maps not prepared");
+        std::vector<cplx> res(static_cast<std::size_t>(fd.nfreq) * fd.nFaces, cplx(0.0, 0.0));
+        if (fd.nFaces == 0 || fd.nfreq == 0) return res;
         const double nt2 = std::pow(static_cast<double>(nt), 2.0);
-        dev::launch_flux_faces(dFaces, nFaces, dTiles, static_cast<int>(tiles.size()), nfreq, dft_[q].re, dft_[q].im,
-                               dev::kFloatFloatAcc<T>, nt2, partial, out, stream_);
+        dev::launch_flux_faces(fd.faces, fd.nFaces, fd.tiles, fd.nTiles, fd.nfreq, dft_[q].re, dft_[q].im, dev::kFloatFloatAcc<T>, nt2,
+                               fd.partial, fd.out, stream_);
         ck(cudaGetLastError(), "flux integration launch");
-        ck(cudaStreamSynchronize(stream_), "flux integration");
         std::vector<double2> h(res.size());
-        ck(cudaMemcpy(h.data(), out, h.size() * sizeof(double2), cudaMemcpyDeviceToHost), "D2H flux faces");
+        ck(cudaMemcpyAsync(h.data(), fd.out, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, stream_), "D2H flux faces");
+        ck(cudaStreamSynchronize(stream_), "flux integration");
         d2h_ += static_cast<double>(h.size() * sizeof(double2));
-        mem_.h2d += tmp.h2d;
         for (std::size_t i = 0; i < h.size(); ++i) res[i] = cplx(h[i].x, h[i].y);
         return res;
     }
@@ -696,7 +734,7 @@ private:
         ck(cudaMemcpy2D(d, static_cast<std::size_t>(pitch_), v.data(), static_cast<std::size_t>(D.lx), static_cast<std::size_t>(D.lx),
                         static_cast<std::size_t>(D.ly) * D.lz, cudaMemcpyHostToDevice),
            "cudaMemcpy2D H2D");
-        mem_.h2d += static_cast<double>(v.size());
+        mem_.addCopied(static_cast<double>(v.size()));
         return d;
     }
 
@@ -1178,6 +1216,17 @@ private:
                 }
                 if (!anyUse) continue;  // empty slab: no a satisfies a < 0 or a >= L
                 int lo = 0, hi = L;
+                if (static_cast<int>(tp.slabUse.size()) == L) {
+                    // the coordinates the plan marked: the same cells as the classes' flags
+                    for (int a = 0; a < L; ++a) {
+                        if (!tp.slabUse[a]) continue;
+                        if (2 * a < L) lo = std::max(lo, a + 1);
+                        else hi = std::min(hi, a);
+                    }
+                    dc.slabLo[t] = lo;
+                    dc.slabHi[t] = hi;
+                    continue;
+                }
                 const uint8_t* code = cp.code.data();
                 const int ax = tp.axis;
 #pragma omp parallel for schedule(static) reduction(max : lo) reduction(min : hi)
@@ -1288,6 +1337,49 @@ private:
             if (P.comp[c].present) fields_.f[c] = mem_.alloc<T>(N);
         for (int c = 0; c < 3; ++c)
             if (P.comp[c].present && P.comp[c].hasD) fields_.f[6 + c] = mem_.alloc<T>(N);
+        fluxDev_.assign(P.fluxes.size(), FluxFacesDev());
+        std::vector<std::vector<FluxFaceMap>> maps(P.fluxes.size());
+        clk.mark("up-fields");
+        // independent parts, each on a host thread of its own: the pass tables, the
+        // sources and detector records, the DFT tables, the emitters, the TFSF surfaces,
+        // and the flux face maps (host)
+        runConcurrently(opt_.device, {[&] { uploadPasses(); }, [&] { uploadSourcesRecords(); }, [&] { uploadDftTables(); },
+                                      [&] { uploadEmitters(); }, [&] { uploadTfsf(); }, [&] { buildFluxMaps(maps); }});
+        clk.mark("up-parts");
+        for (std::size_t q = 0; q < P.fluxes.size(); ++q)
+            if (!P.fluxes[q].spec.save && !P.fluxes[q].spec.load) prepareFluxFaces(q, maps[q]);
+        clk.mark("up-flux-maps");
+        uploadTail();
+        clk.mark("up-tail");
+        if (clk.on)
+            std::fprintf(stderr, "host up: %.4f s in cudaMalloc + cudaMemset (%.0f MB), %.4f s in H2D copies (%.0f MB)\n",
+                         mem_.allocSeconds, mem_.bytes / 1e6, mem_.copySeconds, mem_.h2d / 1e6);
+    }
+
+    // The face maps of every flux region (integration weights and accumulator points of
+    // each face), built on the host cores concurrently.
+    void buildFluxMaps(std::vector<std::vector<FluxFaceMap>>& maps) {
+        std::vector<std::exception_ptr> mErr(P.fluxes.size());
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long long q = 0; q < static_cast<long long>(P.fluxes.size()); ++q) {
+            const std::size_t k = static_cast<std::size_t>(q);
+            if (P.fluxes[k].spec.save || P.fluxes[k].spec.load) continue;
+            try {
+                maps[k] = flux_face_maps(P, k);
+            } catch (...) {
+                mErr[k] = std::current_exception();
+            }
+        }
+        for (auto& e : mErr)
+            if (e) std::rethrow_exception(e);
+    }
+
+    // Pole coefficients, the class codes and tables, CPML profiles and psi arrays of both
+    // passes, the oriented-dipole lists.
+    void uploadPasses() {
+        PhaseClock clk;
+        const Dims& D = P.dims;
+        const std::size_t N = static_cast<std::size_t>(cellsPad_);
         // poles: per object start / count
         std::vector<int> pStart, pCount;
         std::vector<T> al, xi, ga;
@@ -1306,7 +1398,6 @@ private:
             xi.push_back(0);
             ga.push_back(0);
         }
-        clk.mark("up-fields");
         const int* dStart = mem_.upload(pStart);
         const int* dCount = mem_.upload(pCount);
         const T* dAl = mem_.upload(al);
@@ -1335,6 +1426,7 @@ private:
                 dc.U = fields_.f[c];
                 dc.D = (c < 3) ? fields_.f[6 + c] : nullptr;
                 dc.code = uploadPadded(cp.code);
+                clk.mark("up-code");
                 std::vector<dev::Class<T>> cls(cp.classes.size());
                 for (std::size_t q = 0; q < cp.classes.size(); ++q) {
                     const ClassInfo& k = cp.classes[q];
@@ -1411,8 +1503,11 @@ private:
                 }
                 bytes += 3.0 * sizeof(T) + 1.0;  // field read + write, neighbour read, code
             }
+            clk.mark("up-classes");
             setSlabsAndForm(pass, half == 1);
+            clk.mark("up-slabs");
             if (half == 1) uploadOrDip(pass);
+            clk.mark("up-ordip");
             if (half == 1 && (pass.interior3d || pass.interior2d) && !dev::kInlineDispersive<T>) {
                 // dispersive cells leave the interior form for their own list kernel
                 std::vector<int> lc;
@@ -1433,7 +1528,9 @@ private:
             }
         }
         (void)bytes;
-        clk.mark("up-passes");
+    }
+
+    void uploadSourcesRecords() {
         // sources
         {
             std::vector<int> comp, srcId;
@@ -1493,8 +1590,10 @@ private:
             dRec_ = mem_.alloc<double>(recTotal_);
             recT_.rec = dRec_;
         }
-        clk.mark("up-src-rec");
-        // DFT tables: the flux regions, then the frequency-domain detectors
+    }
+
+    // DFT tables: the flux regions, then the frequency-domain detectors
+    void uploadDftTables() {
         for (auto& fp : P.fluxes) {
             std::vector<int> comp, cell;
             for (auto& st : fp.stores)
@@ -1517,16 +1616,6 @@ private:
                 }
             dft_.push_back(makeDft(comp, cell, dp.spec.freqList, dp.timeInt));
         }
-        clk.mark("up-dft");
-        uploadEmitters();
-        clk.mark("up-emitters");
-        uploadTfsf();
-        clk.mark("up-tfsf");
-        uploadTail();
-        clk.mark("up-tail");
-        if (clk.on)
-            std::fprintf(stderr, "host up: %.4f s in cudaMalloc + cudaMemset (%.0f MB), %.4f s in H2D copies (%.0f MB)\n",
-                         mem_.allocSeconds, mem_.bytes / 1e6, mem_.copySeconds, mem_.h2d / 1e6);
     }
 
     // One DFT table: point table (component, cell), phasors per sample from the accumulated

@@ -65,6 +65,9 @@ struct TermPlan {
     bool hasPsi = false;    // psi storage exists for this term
     std::vector<double> kprof;  // per coordinate along axis: CPML coefficient of deriv-normal slab cells
     std::vector<double> b, cpsi; // per coordinate along axis: psi recursion coefficients
+    // per coordinate along axis: 1 where some cell carries the CPML term along the axis or
+    // updates psi (the CPML slabs of the term, whose bounds the pass kernels take)
+    std::vector<uint8_t> slabUse;
 };
 
 struct ClassInfo {

@@ -7,12 +7,14 @@
 // cell, and compressed into the class-code form of plan.hpp. The compressed form
 // is then checked cell by cell against the literal accumulation.
 #include <algorithm>
-#include <cstring>
 #include <cmath>
+#include <cstring>
 #include <exception>
+#include <functional>
 #include <map>
 #include <numeric>
 #include <set>
+#include <thread>
 #include <tuple>
 #include <utility>
 
@@ -215,8 +217,10 @@ struct Builder {
 
     // setupPhysFields, parallelFDTDField.hpp:867-947
     void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff, int threads) {
+        PhaseClock clk;
         Field3<int> ph(D, 0, threads);
         Field3<double> ep(D, 1.0, threads);
+        clk.mark("mat-fill");
         const bool twoD = (D.lz == 1);
         int zmin = twoD ? 0 : 1;
         int zmax = twoD ? 1 : D.lz - 1;
@@ -246,6 +250,7 @@ struct Builder {
                         if (sameGeo ? inML : o.isObj(pt, d[0], o.geo)) ep.at(ii, jj, kk) = epsHere;
                     }
         }
+        clk.mark("mat-objects");
         zmin = 0;
         zmax = twoD ? 1 : D.lz;
         if (!twoD) {
@@ -664,6 +669,7 @@ struct Builder {
     }
     std::array<int, 3> lnMnOut[6], lnPlOut[6];
     int innerThreads_ = 1;  // threads of each component's row loops
+    std::function<void()> side;  // run concurrently with the component build
 
     // ---- update lists (parallelFDTDField.hpp:628-856) ----
     enum ListKind { L_NONE = 0, L_U = 1, L_D = 2 };
@@ -694,6 +700,7 @@ struct Builder {
         double dbBase[2], dbPsi[2];
         bool hasPsi[2] = {false, false};
         buildPml(comp, gridJ, gridK, psi, grid, dbBase, dbPsi, hasPsi);
+        clk.mark("comp-pml");
         const std::array<int, 3> lnMn = lnMnOut[comp], lnPl = lnPlOut[comp];
 
         // initializeList ranges
@@ -706,33 +713,15 @@ struct Builder {
         // one byte per cell: the curl list kind (bits 0-1), the Lorentz list (bit 2) and the
         // oriented-dipole list (bit 3)
         Buf<uint8_t> cellLists = filled<uint8_t>(static_cast<std::size_t>(D.cells()), L_NONE, nt);
+        clk.mark("comp-fill");
 
-        auto classify = [&](std::array<int, 3> a, std::array<int, 3> b, bool includeU, bool finalFill) {
-            int border = 0;  // rows write disjoint cells
-#pragma omp parallel for schedule(static) num_threads(nt) reduction(| : border)
-            for (int jj = a[1]; jj < b[1]; ++jj)
-                for (int kk = a[2]; kk < b[2]; ++kk)
-                    for (int ii = a[0]; ii < b[0]; ++ii) {
-                        int o = ph.at(ii, jj, kk);
-                        if (o < 0) {
-                            border = 1;
-                            continue;
-                        }
-                        const Object& ob = objs[o];
-                        std::size_t id = static_cast<std::size_t>(D.idx(ii, jj, kk));
-                        bool orDipCell = ob.orDip && (E && ob.gamma.size() > 0);
-                        bool uCell = includeU && ((!E) || (E && ob.gamma.size() < 1 && !ob.ML));
-                        uint8_t& cl = cellLists[id];
-                        if (finalFill) {
-                            cl = static_cast<uint8_t>((cl & ~3u) | ((!orDipCell && uCell) ? L_U : L_D));
-                        } else {
-                            if (orDipCell) cl |= 8u;
-                            else if (!uCell) cl |= 4u;
-                        }
-                    }
-            if (border) throw InputError("update list reaches a border cell");
-        };
-        // getBlasLists
+        // getBlasLists / fillBlasLists: seven regions partition the box [mn, mx) (the slabs
+        // of the CPML thickness along y, then z, then x, and the interior); a cell of a slab
+        // joins the U lists only when no material reaches into the CPML (incPML), one of the
+        // interior always can. Cells of oriented-dipole objects go to that list (bit 3), other
+        // cells that cannot join U to the Lorentz list (bit 2); the final fill over
+        // [fmn, fmx) sets the curl list kind. One pass over the box applies all eight region
+        // loops of the reference (their flags OR'ed where regions overlap).
         bool pmlMat = (E && matInPML);
         int xl = pmlMat ? lnMn[0] : 0, xr = pmlMat ? lnPl[0] : 0;
         if (xr != 0) xr -= fieldEnd[0];
@@ -741,14 +730,7 @@ struct Builder {
         bool threeBoth = D.threeD;
         int zb = (threeBoth && pmlMat) ? lnPl[2] : 0, zf = (threeBoth && pmlMat) ? lnMn[2] : 0;
         if (zf != 0) zf -= fieldEnd[2];
-        bool incPML = !matInPML;
-        classify({mn[0], mn[1], mn[2]}, {mx[0], mn[1] + yb, mx[2]}, incPML, false);
-        classify({mn[0], mx[1] - yt, mn[2]}, {mx[0], mx[1], mx[2]}, incPML, false);
-        classify({mn[0], mn[1] + yb, mn[2]}, {mx[0], mx[1] - yt, mn[2] + zb}, incPML, false);
-        classify({mn[0], mn[1] + yb, mx[2] - zf}, {mx[0], mx[1] - yt, mx[2]}, incPML, false);
-        classify({mn[0], mn[1] + yb, mn[2] + zb}, {mn[0] + xl, mx[1] - yt, mx[2] - zf}, incPML, false);
-        classify({mx[0] - xr, mn[1] + yb, mn[2] + zb}, {mx[0], mx[1] - yt, mx[2] - zf}, incPML, false);
-        classify({mn[0] + xl, mn[1] + yb, mn[2] + zb}, {mx[0] - xr, mx[1] - yt, mx[2] - zf}, true, false);
+        const bool incPML = !matInPML;
         std::array<int, 3> fmn = mn, fmx = mx;
         fmn[0] += lnMn[0];
         fmx[0] -= lnPl[0];
@@ -759,7 +741,53 @@ struct Builder {
         fmn[2] += lnPl[2];  // lnz_back() returns the plus-side thickness
         fmx[2] -= lnMn[2];  // lnz_front() returns the minus-side thickness
         if (lnMn[2] != 0) fmx[2] += fieldEnd[2];
-        classify(fmn, fmx, true, true);
+        // per object: bit 0 an oriented-dipole cell, bit 1 a cell that may join U
+        std::vector<uint8_t> objKind(objs.size());
+        for (std::size_t o = 0; o < objs.size(); ++o) {
+            const Object& ob = objs[o];
+            const bool orDipCell = ob.orDip && (E && ob.gamma.size() > 0);
+            const bool uAll = (!E) || (E && ob.gamma.size() < 1 && !ob.ML);
+            objKind[o] = static_cast<uint8_t>((orDipCell ? 1 : 0) | (uAll ? 2 : 0));
+        }
+        auto inR = [](int v, int lo, int hi) { return v >= lo && v < hi; };
+        const int y0 = std::min(mn[1], fmn[1]), y1 = std::max(mx[1], fmx[1]);
+        const int z0 = std::min(mn[2], fmn[2]), z1 = std::max(mx[2], fmx[2]);
+        const int x0 = std::min(mn[0], fmn[0]), x1 = std::max(mx[0], fmx[0]);
+        int border = 0;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(| : border)
+        for (int jj = y0; jj < y1; ++jj)
+            for (int kk = z0; kk < z1; ++kk) {
+                // the regions this row meets: y and z membership, x ranges
+                const bool inY = inR(jj, mn[1], mx[1]), inZ = inR(kk, mn[2], mx[2]);
+                const bool yMid = inR(jj, mn[1] + yb, mx[1] - yt), zMid = inR(kk, mn[2] + zb, mx[2] - zf);
+                const bool rowSlab = inY && inZ &&
+                                     (inR(jj, mn[1], mn[1] + yb) || inR(jj, mx[1] - yt, mx[1]) ||
+                                      (yMid && (inR(kk, mn[2], mn[2] + zb) || inR(kk, mx[2] - zf, mx[2]))));
+                const bool rowMid = inY && inZ && yMid && zMid;
+                const bool rowF = inR(jj, fmn[1], fmx[1]) && inR(kk, fmn[2], fmx[2]);
+                if (!rowSlab && !rowMid && !rowF) continue;
+                const long long rowBase = D.idx(0, jj, kk);
+                for (int ii = x0; ii < x1; ++ii) {
+                    const bool inX = inR(ii, mn[0], mx[0]);
+                    const bool slab = inX && (rowSlab || (rowMid && (inR(ii, mn[0], mn[0] + xl) || inR(ii, mx[0] - xr, mx[0]))));
+                    const bool mid = inX && rowMid && inR(ii, mn[0] + xl, mx[0] - xr);
+                    const bool fin = rowF && inR(ii, fmn[0], fmx[0]);
+                    if (!slab && !mid && !fin) continue;
+                    const int o = ph.v[static_cast<std::size_t>(rowBase + ii)];
+                    if (o < 0) {
+                        border = 1;
+                        continue;
+                    }
+                    const uint8_t k = objKind[static_cast<std::size_t>(o)];
+                    const bool orDipCell = k & 1, uAll = (k & 2) != 0;
+                    uint8_t cl = 0;
+                    if (slab) cl |= orDipCell ? 8u : ((incPML && uAll) ? 0u : 4u);
+                    if (mid) cl |= orDipCell ? 8u : (uAll ? 0u : 4u);
+                    if (fin) cl = static_cast<uint8_t>((cl & ~3u) | ((!orDipCell && uAll) ? L_U : L_D));
+                    cellLists[static_cast<std::size_t>(rowBase + ii)] = cl;
+                }
+            }
+        if (border) throw InputError("update list reaches a border cell");
         clk.mark("comp-lists");
 
         // term geometry: J uses grid_j (derivative along k), K uses grid_k (derivative along j)
@@ -782,6 +810,7 @@ struct Builder {
             T.kprof.assign(L, 0.0);
             T.b.assign(L, 0.0);
             T.cpsi.assign(L, 0.0);
+            T.slabUse.assign(L, 0);
         }
 
         // Per cell and term, one byte of CPML list membership: the number of grid-list
@@ -803,6 +832,10 @@ struct Builder {
             long long y = r / D.lz;
             return static_cast<int>(ax == 0 ? x : (ax == 1 ? y : z));
         };
+        // Per-entry checks and the coefficient profiles first (one value per entry, or per
+        // step of an entry that runs along the term's axis, at most the slab thickness), then
+        // the cell bytes of all entries in parallel: increments and flag bits commute, so the
+        // bytes and the errors do not depend on the order (a byte is updated atomically).
         for (int t = 0; t < 2; ++t) {
             TermPlan& T = tp[t];
             uint8_t* tb = termBits[t].data();
@@ -819,42 +852,103 @@ struct Builder {
                     if (base == 0.0) base = e.DbField;
                     if (e.DbField != base) throw UnsupportedError("CPML transverse coefficient varies");
                 }
-                const uint8_t nz = (e.DbField != 0.0) ? 0x40 : 0;
-                for (int q = 0; q < e.n; ++q) {
-                    uint8_t& b = tb[e.ind + q * e.stride];
-                    if ((b & 3u) == 3u) throw UnsupportedError("more than three CPML entries on one cell");
-                    b = static_cast<uint8_t>(b + 1u) | nz;
-                    if (along) {
-                        if (b & 0x10u) throw UnsupportedError("overlapping CPML slabs along one axis");
-                        b |= 0x10u;
-                        int ac = c0 + q * dq;
+                if (along)
+                    for (int q = 0; q < (dq == 0 ? std::min(e.n, 1) : e.n); ++q) {
+                        const int ac = c0 + q * dq;
                         if (T.kprof[ac] != 0.0 && T.kprof[ac] != e.DbField)
                             throw UnsupportedError("CPML coefficient is not a function of the normal coordinate");
                         T.kprof[ac] = e.DbField;
-                    } else {
-                        b = static_cast<uint8_t>(b + 4u);
+                        if (T.present) T.slabUse[ac] = 1;
                     }
-                }
             }
             T.db = base;
             for (auto& e : psi[t]) {
                 if (e.indOff - e.ind != T.off) throw InputError("psi offset does not match the curl offset");
-                for (int q = 0; q < e.n; ++q) {
-                    uint8_t& b = tb[e.ind + q * e.stride];
-                    if (b & 0x20u) throw UnsupportedError("a psi cell is updated twice");
-                    b |= 0x20u;
-                    int ac = e.normCoord;
-                    if ((T.b[ac] != 0.0 || T.cpsi[ac] != 0.0) && (T.b[ac] != e.b || T.cpsi[ac] != e.c))
-                        throw UnsupportedError("psi coefficients are not a function of the normal coordinate");
-                    T.b[ac] = e.b;
-                    T.cpsi[ac] = e.c;
+                if (e.n <= 0) continue;
+                const int ac = e.normCoord;
+                if ((T.b[ac] != 0.0 || T.cpsi[ac] != 0.0) && (T.b[ac] != e.b || T.cpsi[ac] != e.c))
+                    throw UnsupportedError("psi coefficients are not a function of the normal coordinate");
+                T.b[ac] = e.b;
+                T.cpsi[ac] = e.c;
+                if (T.present) {
+                    const int p0 = coordOf(e.ind, T.axis);
+                    const int dp = e.n > 1 ? coordOf(e.ind + e.stride, T.axis) - p0 : 0;
+                    for (int q = 0; q < (dp == 0 ? 1 : e.n); ++q) T.slabUse[p0 + q * dp] = 1;
                 }
             }
+            // 1: more than three entries on a cell; 2: two slabs along the axis overlap;
+            // 4: a psi cell updated twice. Each thread owns the cells of one band of y and
+            // applies every entry's steps that fall in it (a run moves along one axis: its
+            // y is constant or steps by one).
+            int fault = 0;
+            auto yStep = [&](long long ind, long long stride, int n, int& yFirst) {
+                yFirst = coordOf(ind, 1);
+                if (n < 2) return 0;
+                const int dy = coordOf(ind + stride, 1) - yFirst;
+                if (dy < -1 || dy > 1 || coordOf(ind + (n - 1) * stride, 1) != yFirst + (n - 1) * dy)
+                    throw InputError("CPML run does not follow one grid axis");
+                return dy;
+            };
+            auto qRange = [](int y0, int dy, int n, int ya, int yb, int& qa, int& qb) {
+                if (dy == 0) {
+                    qa = 0;
+                    qb = (y0 >= ya && y0 < yb) ? n : 0;
+                } else if (dy > 0) {
+                    qa = std::max(0, ya - y0);
+                    qb = std::min(n, yb - y0);
+                } else {
+                    qa = std::max(0, y0 - yb + 1);
+                    qb = std::min(n, y0 - ya + 1);
+                }
+            };
+            std::vector<std::array<int, 2>> gY(grid[t].size()), pY(psi[t].size());
+            for (std::size_t q0 = 0; q0 < grid[t].size(); ++q0)
+                gY[q0][1] = yStep(grid[t][q0].ind, grid[t][q0].stride, grid[t][q0].n, gY[q0][0]);
+            for (std::size_t q0 = 0; q0 < psi[t].size(); ++q0)
+                pY[q0][1] = yStep(psi[t][q0].ind, psi[t][q0].stride, psi[t][q0].n, pY[q0][0]);
+#pragma omp parallel num_threads(nt) reduction(| : fault)
+            {
+                const int nth = omp_get_num_threads(), me = omp_get_thread_num();
+                const int ya = static_cast<int>(static_cast<long long>(D.ly) * me / nth);
+                const int yb = static_cast<int>(static_cast<long long>(D.ly) * (me + 1) / nth);
+                for (std::size_t q0 = 0; q0 < grid[t].size(); ++q0) {
+                    const auto& e = grid[t][q0];
+                    int qa, qb;
+                    qRange(gY[q0][0], gY[q0][1], e.n, ya, yb, qa, qb);
+                    const bool along = e.slab == T.axis;
+                    const uint8_t nz = (e.DbField != 0.0) ? 0x40 : 0;
+                    for (int q = qa; q < qb; ++q) {
+                        uint8_t& bt = tb[e.ind + q * e.stride];
+                        if ((bt & 3u) == 3u) fault |= 1;
+                        bt = static_cast<uint8_t>(static_cast<uint8_t>(bt + 1u) | nz);
+                        if (along) {
+                            if (bt & 0x10u) fault |= 2;
+                            bt |= 0x10u;
+                        } else {
+                            bt = static_cast<uint8_t>(bt + 4u);
+                        }
+                    }
+                }
+                for (std::size_t q0 = 0; q0 < psi[t].size(); ++q0) {
+                    const auto& e = psi[t][q0];
+                    int qa, qb;
+                    qRange(pY[q0][0], pY[q0][1], e.n, ya, yb, qa, qb);
+                    for (int q = qa; q < qb; ++q) {
+                        uint8_t& bt = tb[e.ind + q * e.stride];
+                        if (bt & 0x20u) fault |= 4;
+                        bt |= 0x20u;
+                    }
+                }
+            }
+            if (fault & 1) throw UnsupportedError("more than three CPML entries on one cell");
+            if (fault & 2) throw UnsupportedError("overlapping CPML slabs along one axis");
+            if (fault & 4) throw UnsupportedError("a psi cell is updated twice");
             if (!T.hasPsi) {
 #pragma omp parallel for schedule(static) num_threads(nt)
                 for (long long id = 0; id < static_cast<long long>(N); ++id) tb[id] &= static_cast<uint8_t>(~3u);
             }
         }
+        clk.mark("comp-terms");
         // build classes: each cell's class (its update terms and coefficients) is looked up
         // by key; class ids are given in order of first appearance in the scan order
         // (y, z, x). Rows of y are scanned in parallel chunks with chunk-local ids, merged
@@ -1001,6 +1095,7 @@ struct Builder {
             const std::size_t b = static_cast<std::size_t>(D.idx(0, y0, 0)), e = static_cast<std::size_t>(D.idx(0, y1, 0));
             for (std::size_t id = b; id < e; ++id) cp.code[id] = rm[cp.code[id]];
         }
+        clk.mark("comp-remap");
         for (std::size_t q = 1; q < cp.classes.size(); ++q) {
             const ClassInfo& k = cp.classes[q];
             bool acts = k.toD || k.lor || k.ordip;
@@ -1146,7 +1241,7 @@ struct Builder {
                                        {5, false, {0.5, 0.5, 0.0}, {1, 1, 0}}};
             const int nThreads = omp_get_max_threads();
             const int outer = std::min(7, nThreads);
-            const int inner = std::max(1, nThreads / outer);
+            const int inner = std::max(1, (nThreads + outer - 1) / outer);
             std::exception_ptr gErr[7];
             NestedTeams nest;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(outer)
@@ -1195,7 +1290,20 @@ struct Builder {
         int nComp = 0;
         for (int c = 0; c < 6; ++c) nComp += present[c] ? 1 : 0;
         const int nThreads = omp_get_max_threads();
-        innerThreads_ = std::max(1, nThreads / std::max(1, nComp));
+        // every thread in some team (the last teams one thread larger than the fair share)
+        innerThreads_ = std::max(1, (nThreads + std::max(1, nComp) - 1) / std::max(1, nComp));
+        // the side work (emitter and TFSF set-up: it needs the material maps, not the lists)
+        // runs on a thread of its own meanwhile; its errors come after the components'
+        std::exception_ptr sideErr;
+        std::thread sideThread;
+        if (side)
+            sideThread = std::thread([&] {
+                try {
+                    side();
+                } catch (...) {
+                    sideErr = std::current_exception();
+                }
+            });
         {
             NestedTeams nest;
 #pragma omp parallel for schedule(dynamic, 1) num_threads(std::min(nThreads, std::max(1, nComp)))
@@ -1208,8 +1316,10 @@ struct Builder {
                 }
             }
         }
+        if (sideThread.joinable()) sideThread.join();
         for (int q = 0; q < 6; ++q)
             if (err[q]) std::rethrow_exception(err[q]);
+        if (sideErr) std::rethrow_exception(sideErr);
         clk.mark("components");
         for (int c = 0; c < 3; ++c) P.comp[c].hasD = P.comp[c].present && disp;
         buildOrDip();
@@ -1751,19 +1861,31 @@ struct Builder {
 Plan build_plan(const Inputs& in) {
     Plan P;
     Builder b(in, P);
+    // The emitter and TFSF set-up read the material maps, the objects and which
+    // components exist (all fixed before the component build) and write their own parts
+    // of the plan: they run beside the component build.
+    b.side = [&] {
+        PhaseClock clk;
+        if (!in.emitters.empty()) {
+            const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
+            build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v.data(), P);
+            clk.mark("emitters");
+        }
+        if (!in.tfsf.empty()) {
+            const int* ph[6];
+            for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? b.phys[c].v.data() : nullptr;
+            build_tfsf(in, P.dims, P.dt, ph, b.objs, P);
+            clk.mark("tfsf");
+        }
+    };
     b.build();
-    PhaseClock clk;
-    if (!in.emitters.empty()) {
-        const bool Ep[3] = {P.comp[EX].present, P.comp[EY].present, P.comp[EZ].present};
-        build_emitters(in, P.dims, P.dt, Ep, b.epsRel[6].v.data(), P);
-        clk.mark("emitters");
-    }
-    if (!in.tfsf.empty()) {
-        const int* ph[6];
-        for (int c = 0; c < 6; ++c) ph[c] = P.comp[c].present ? b.phys[c].v.data() : nullptr;
-        build_tfsf(in, P.dims, P.dt, ph, P.in.objects, P);
-        clk.mark("tfsf");
-    }
+    // a surface term into D needs the D field of its component
+    for (const TfsfPlan& T : P.tfsf)
+        for (const TfsfAdds* a : {&T.addH, &T.addE})
+            for (std::size_t q = 0; q < a->cells(); ++q)
+                for (long long k = a->start[q]; k < a->start[q + 1]; ++k)
+                    if (a->toD[static_cast<std::size_t>(k)] && (a->comp[q] > 2 || !P.comp[a->comp[q]].hasD))
+                        throw UnsupportedError("TFSF correction into a D field the grid does not have");
     // incident-flux normalisation areas (parallelFlux.hpp:110-135)
     for (auto& fp : P.fluxes) {
         if (!fp.spec.crossSec) {

@@ -709,11 +709,6 @@ void build_tfsf(const Inputs& in, const Dims& D, double dt, const int* const phy
         TfsfPlan T;
         TfsfBuilder b(in, D, dt, t, phys, objs, T);
         b.build();
-        for (const TfsfAdds* a : {&T.addH, &T.addE})
-            for (std::size_t q = 0; q < a->cells(); ++q)
-                for (long long k = a->start[q]; k < a->start[q + 1]; ++k)
-                    if (a->toD[static_cast<std::size_t>(k)] && (a->comp[q] > 2 || !P.comp[a->comp[q]].hasD))
-                        throw UnsupportedError("TFSF correction into a D field the grid does not have");
         P.tfsf.push_back(std::move(T));
     }
 }
