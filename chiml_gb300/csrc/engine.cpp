@@ -9,6 +9,7 @@
 #include <complex>
 #include <exception>
 #include <functional>
+#include <future>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -1324,8 +1325,6 @@ private:
 
     void upload() {
         PhaseClock clk;
-        validatePlan();
-        clk.mark("up-validate");
         const Dims& D = P.dims;
         // device rows of pitch_ >= lx values, a multiple of 4, so that every row starts on a
         // 16-byte boundary (32 bytes in FP64)
@@ -1340,15 +1339,23 @@ private:
         fluxDev_.assign(P.fluxes.size(), FluxFacesDev());
         std::vector<std::vector<FluxFaceMap>> maps(P.fluxes.size());
         clk.mark("up-fields");
-        // independent parts, each on a host thread of its own: the pass tables, the
-        // sources and detector records, the DFT tables, the emitters, the TFSF surfaces,
-        // and the flux face maps (host)
-        runConcurrently(opt_.device, {[&] { uploadPasses(); }, [&] { uploadSourcesRecords(); }, [&] { uploadDftTables(); },
-                                      [&] { uploadEmitters(); }, [&] { uploadTfsf(); }, [&] { buildFluxMaps(maps); }});
+        // independent parts, each on a host thread of its own: the plan's validation (its
+        // failure is reported before any other; no kernel runs before it has passed), the
+        // pass tables, the sources and detector records, the DFT tables and then the flux
+        // face maps on the device, the emitters, the TFSF surfaces; the flux face maps are
+        // built on the host meanwhile (the DFT task waits for them)
+        std::shared_future<void> mapsReady = std::async(std::launch::async, [&] { buildFluxMaps(maps); }).share();
+        runConcurrently(opt_.device,
+                        {[&] { validatePlan(); }, [&] { uploadPasses(); }, [&] { uploadSourcesRecords(); },
+                         [&] {
+                             uploadDftTables();
+                             mapsReady.get();
+                             for (std::size_t q = 0; q < P.fluxes.size(); ++q)
+                                 if (!P.fluxes[q].spec.save && !P.fluxes[q].spec.load) prepareFluxFaces(q, maps[q]);
+                         },
+                         [&] { uploadEmitters(); }, [&] { uploadTfsf(); }});
+        mapsReady.wait();
         clk.mark("up-parts");
-        for (std::size_t q = 0; q < P.fluxes.size(); ++q)
-            if (!P.fluxes[q].spec.save && !P.fluxes[q].spec.load) prepareFluxFaces(q, maps[q]);
-        clk.mark("up-flux-maps");
         uploadTail();
         clk.mark("up-tail");
         if (clk.on)
@@ -1515,12 +1522,14 @@ private:
                 for (int ci = 0; ci < 3; ++ci) {
                     const CompPlan& cp = P.comp[ci];
                     if (!cp.present) continue;
-                    for (long long i = 0; i < static_cast<long long>(cp.code.size()); ++i)
+                    for (long long i = 0; i < static_cast<long long>(cp.code.size()); ++i) {
+                        if (cp.code[i] >= cp.classes.size()) continue;  // rejected by validatePlan
                         if (cp.code[i] && ((cp.classes[cp.code[i]].lor && lorHasPoles(cp.classes[cp.code[i]])) ||
                                            cp.classes[cp.code[i]].ordip)) {
                             lc.push_back(ci);
                             li.push_back(i);
                         }
+                    }
                 }
                 pass.nLor = static_cast<long long>(li.size());
                 pass.lorComp = mem_.upload(lc);

@@ -403,6 +403,10 @@ struct Builder {
         int mx = pl ? gnv(dir) - 2 : p.T[dir];
         const int zoff = (D.lz != 1) ? 1 : 0;
         const Field3<int>& ph = phys[g];
+        // the planes are independent (each one's sum in its own order): computed in
+        // parallel, kept in plane order
+        std::vector<double> etaOf(static_cast<std::size_t>(std::max(0, mx - mn)), 0.0);
+#pragma omp parallel for schedule(static) num_threads(innerThreads_)
         for (int ii = mn; ii < mx; ++ii) {
             std::vector<int> plane(static_cast<std::size_t>(std::max(0, psz[0] * psz[1])), 0);
             if (dir == 0) {
@@ -424,9 +428,10 @@ struct Builder {
                     mu_sum += 1.0 / static_cast<double>(plane.size());
                 }
             double etaSum = eps_sum * mu_sum;
-            double etaVal = (etaSum != 0.00) ? etaSum : 0;
-            if (static_cast<int>(eta.size()) < p.T[dir] && etaVal != 0.0) eta.push_back(etaVal);
+            etaOf[static_cast<std::size_t>(ii - mn)] = (etaSum != 0.00) ? etaSum : 0;
         }
+        for (double etaVal : etaOf)
+            if (static_cast<int>(eta.size()) < p.T[dir] && etaVal != 0.0) eta.push_back(etaVal);
     }
 
     struct PsiEntry {  // one run of the psi list

@@ -10,7 +10,7 @@ namespace chiml {
 namespace dev {
 
 constexpr int kFluxTile = 256;     // integration points per partial sum
-constexpr int kFluxThreads = 128;  // frequencies per block
+constexpr int kFluxThreads = 256;  // frequencies per block (at most)
 
 // One face: grid w (0 Ej, 1 Ek, 2 Hj, 3 Hk) at integration point s takes the terms
 // [start[w][s], start[w][s + 1]) of scale * accumulator[pt]; the integrand at s is

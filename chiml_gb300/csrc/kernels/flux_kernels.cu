@@ -1,6 +1,6 @@
 // Flux integration on the device (parallelFlux.hpp:325-545 as a gather plus a weighted sum).
 //
-//   k_flux_partial  one block per (tile of kFluxTile integration points, 128 frequencies):
+//   k_flux_partial  one block per (tile of kFluxTile integration points, up to 256 frequencies):
 //                   each thread forms the four face-grid values of its frequency at every
 //                   point of the tile from the accumulators (the threads of a warp read
 //                   consecutive frequencies of one point), the integrand and its Simpson
@@ -34,26 +34,27 @@ __device__ __forceinline__ double2 gridValue(const FluxFaceDev& F, int w, int s,
     return g;
 }
 
-// a * conj(b) / d
-__device__ __forceinline__ double2 mulConjDiv(double2 a, double2 b, double d) {
-    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+// a * conj(b)
+__device__ __forceinline__ double2 mulConj(double2 a, double2 b) {
+    return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 
+// The tile's weighted sum of E_j conj(H_k) - E_k conj(H_j), then scaled by 1 / nt^2 once
+// (the reference divides every product by nt^2: the same value up to rounding, without
+// four FP64 divisions per point and frequency).
 __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(const FluxFaceDev* __restrict__ faces, const int4* __restrict__ tiles,
                                                                int nfreq, const double* __restrict__ re, const double* __restrict__ im,
-                                                               bool pairs, double nt2, double2* __restrict__ partial) {
-    const int ff = blockIdx.y * kFluxThreads + threadIdx.x;
+                                                               bool pairs, double invNt2, double2* __restrict__ partial) {
+    const int ff = blockIdx.y * blockDim.x + threadIdx.x;
     if (ff >= nfreq) return;
     const int4 t = tiles[blockIdx.x];
     const FluxFaceDev& F = faces[t.x];
     double2 acc = make_double2(0.0, 0.0);
     for (int s = t.y; s < t.z; ++s) {
         double2 v = make_double2(0.0, 0.0);
-        if (F.has[0])
-            v = mulConjDiv(gridValue(F, 0, s, ff, nfreq, re, im, pairs), gridValue(F, 3, s, ff, nfreq, re, im, pairs), nt2);
+        if (F.has[0]) v = mulConj(gridValue(F, 0, s, ff, nfreq, re, im, pairs), gridValue(F, 3, s, ff, nfreq, re, im, pairs));
         if (F.has[1]) {
-            const double2 u =
-                mulConjDiv(gridValue(F, 1, s, ff, nfreq, re, im, pairs), gridValue(F, 2, s, ff, nfreq, re, im, pairs), nt2);
+            const double2 u = mulConj(gridValue(F, 1, s, ff, nfreq, re, im, pairs), gridValue(F, 2, s, ff, nfreq, re, im, pairs));
             v.x -= u.x;
             v.y -= u.y;
         }
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(kFluxThreads) k_flux_partial(const FluxFaceDev
         acc.x += w * v.x;
         acc.y += w * v.y;
     }
-    partial[static_cast<long long>(blockIdx.x) * nfreq + ff] = acc;
+    partial[static_cast<long long>(blockIdx.x) * nfreq + ff] = make_double2(acc.x * invNt2, acc.y * invNt2);
 }
 
 __global__ void k_flux_sum(const FluxFaceDev* __restrict__ faces, int nFaces, int nfreq, const double2* __restrict__ partial,
@@ -86,8 +87,11 @@ void launch_flux_faces(const FluxFaceDev* faces, int nFaces, const int4* tiles, 
     if (nFaces == 0 || nfreq == 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (nTiles > 0) {
-        const dim3 grid(static_cast<unsigned>(nTiles), static_cast<unsigned>((nfreq + kFluxThreads - 1) / kFluxThreads));
-        k_flux_partial<<<grid, kFluxThreads, 0, s>>>(faces, tiles, nfreq, re, im, pairs, nt2, partial);
+        // whole warps over the frequencies: blocks of up to kFluxThreads threads
+        const int per = (nfreq + 31) / 32 * 32;
+        const int bs = per < kFluxThreads ? per : kFluxThreads;
+        const dim3 grid(static_cast<unsigned>(nTiles), static_cast<unsigned>((nfreq + bs - 1) / bs));
+        k_flux_partial<<<grid, bs, 0, s>>>(faces, tiles, nfreq, re, im, pairs, 1.0 / nt2, partial);
     }
     const int n = nFaces * nfreq;
     k_flux_sum<<<(n + 127) / 128, 128, 0, s>>>(faces, nFaces, nfreq, partial, out);
