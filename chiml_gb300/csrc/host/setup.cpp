@@ -215,6 +215,48 @@ struct Builder {
         }
     }
 
+    // Narrows [a, b) to the x indices of one row (y, z fixed) that can lie in a sphere or
+    // an ellipsoid: the row meets the shape grown by two cells on every semi-axis in an
+    // interval of x found from a quadratic; cells farther out cannot pass isObj. Other
+    // shapes keep the range (their bounding box only).
+    void rowRange(const Object& o, const std::array<double, 3>& offPt, double py, double pz, int& a, int& b) const {
+        if (o.shape != Shape::SPHERE && o.shape != Shape::ELLIPSOID) return;
+        const double grow = 2.0 * std::max(std::max(d[0], d[1]), d[2]);
+        double semi[3];
+        int dims = 3;
+        std::array<double, 9> R = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (o.shape == Shape::SPHERE) {
+            const double r = std::max(o.geo[0], o.geoML[0]);
+            semi[0] = semi[1] = semi[2] = r;
+        } else {
+            for (int i = 0; i < 3; ++i) semi[i] = 0.5 * std::max(std::abs(o.geo[i]), std::abs(o.geoML[i]));
+            if (o.geo[2] == 0.0 || o.geoML[2] == 0.0) dims = 2;  // the test sums two terms
+            R = o.coord;
+        }
+        // x of index ii: (ii + c) d0; t_i = R_i0 (x - loc0) + R_i1 (py - loc1) + R_i2 (pz - loc2)
+        const double c = -1.0 + offPt[0] - (nvec[0] - nvec[0] % 2) / 2.0;
+        double A = 0.0, B = 0.0, C = -1.0;
+        for (int i = 0; i < dims; ++i) {
+            const double s = semi[i] + grow + 1e-9 * semi[i];
+            const double u = R[i * 3 + 0] / s;
+            const double v = (R[i * 3 + 1] * (py - o.loc[1]) + R[i * 3 + 2] * (pz - o.loc[2]) - R[i * 3 + 0] * o.loc[0]) / s;
+            A += u * u;
+            B += 2.0 * u * v;
+            C += v * v;
+        }
+        if (!(A > 1e-30)) return;  // x does not enter the test: keep the range
+        const double disc = B * B - 4.0 * A * C;
+        if (disc < 0.0) {
+            b = a;  // the grown shape misses the row
+            return;
+        }
+        const double r0 = (-B - std::sqrt(disc)) / (2.0 * A), r1 = (-B + std::sqrt(disc)) / (2.0 * A);
+        // r0 <= x <= r1 (x in length units), as indices with one more cell of slack
+        const double lo = std::floor(r0 / d[0] - c) - 1.0, hi = std::ceil(r1 / d[0] - c) + 2.0;
+        if (lo > a) a = static_cast<int>(std::min(lo, static_cast<double>(b)));
+        if (hi < b) b = static_cast<int>(std::max(hi, static_cast<double>(a)));
+    }
+
     // setupPhysFields, parallelFDTDField.hpp:867-947
     void setupPhys(int g, bool E, std::array<double, 3> offPt, std::array<int, 3> endOff, int threads) {
         PhaseClock clk;
@@ -237,18 +279,23 @@ struct Builder {
             // without an emitter buffer both tests are the same test
             const bool sameGeo = o.geoML == o.geo;
             const double epsHere = E ? o.epsInf : 1.0;
+            // Cells are tested in any order: each cell's value comes from the last object
+            // that holds it, whatever the order of cells within one object.
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
             for (int jj = j0; jj < j1; ++jj)
-                for (int ii = i0; ii < i1; ++ii)
-                    for (int kk = k0; kk < k1; ++kk) {
-                        std::array<double, 3> pt;
+                for (int kk = k0; kk < k1; ++kk) {
+                    std::array<double, 3> pt;
+                    pt[1] = ((jj - 1) + offPt[1] + 0 - (nvec[1] - nvec[1] % 2) / 2.0) * d[1];
+                    pt[2] = ((kk - 1) + offPt[2] + 0 - (nvec[2] - nvec[2] % 2) / 2.0) * d[2];
+                    int a = i0, b = i1;
+                    rowRange(o, offPt, pt[1], pt[2], a, b);
+                    for (int ii = a; ii < b; ++ii) {
                         pt[0] = ((ii - 1) + offPt[0] + 0 - (nvec[0] - nvec[0] % 2) / 2.0) * d[0];
-                        pt[1] = ((jj - 1) + offPt[1] + 0 - (nvec[1] - nvec[1] % 2) / 2.0) * d[1];
-                        pt[2] = ((kk - 1) + offPt[2] + 0 - (nvec[2] - nvec[2] % 2) / 2.0) * d[2];
                         const bool inML = o.isObj(pt, d[0], o.geoML);
                         if (inML) ph.at(ii, jj, kk) = static_cast<int>(oo);
                         if (sameGeo ? inML : o.isObj(pt, d[0], o.geo)) ep.at(ii, jj, kk) = epsHere;
                     }
+                }
         }
         clk.mark("mat-objects");
         zmin = 0;

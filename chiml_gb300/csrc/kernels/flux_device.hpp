@@ -9,7 +9,7 @@
 namespace chiml {
 namespace dev {
 
-constexpr int kFluxTile = 256;     // integration points per partial sum
+constexpr int kFluxTile = 64;      // integration points per partial sum
 constexpr int kFluxThreads = 256;  // frequencies per block (at most)
 
 // One face: grid w (0 Ej, 1 Ek, 2 Hj, 3 Hk) at integration point s takes the terms
