@@ -819,24 +819,38 @@ struct Builder {
                 const bool rowF = inR(jj, fmn[1], fmx[1]) && inR(kk, fmn[2], fmx[2]);
                 if (!rowSlab && !rowMid && !rowF) continue;
                 const long long rowBase = D.idx(0, jj, kk);
-                for (int ii = x0; ii < x1; ++ii) {
-                    const bool inX = inR(ii, mn[0], mx[0]);
-                    const bool slab = inX && (rowSlab || (rowMid && (inR(ii, mn[0], mn[0] + xl) || inR(ii, mx[0] - xr, mx[0]))));
-                    const bool mid = inX && rowMid && inR(ii, mn[0] + xl, mx[0] - xr);
-                    const bool fin = rowF && inR(ii, fmn[0], fmx[0]);
+                const int* const phR = ph.v.data() + rowBase;
+                uint8_t* const clR = cellLists.data() + rowBase;
+                // the row in segments of constant region membership
+                int cut[8] = {x0, x1, mn[0], mn[0] + xl, mx[0] - xr, mx[0], fmn[0], fmx[0]};
+                for (int& v : cut) v = std::min(std::max(v, x0), x1);
+                std::sort(cut, cut + 8);
+                for (int q = 0; q < 7; ++q) {
+                    const int sa = cut[q], sb = cut[q + 1];
+                    if (sa >= sb) continue;
+                    const bool inX = inR(sa, mn[0], mx[0]);
+                    const bool slab = inX && (rowSlab || (rowMid && (inR(sa, mn[0], mn[0] + xl) || inR(sa, mx[0] - xr, mx[0]))));
+                    const bool mid = inX && rowMid && inR(sa, mn[0] + xl, mx[0] - xr);
+                    const bool fin = rowF && inR(sa, fmn[0], fmx[0]);
                     if (!slab && !mid && !fin) continue;
-                    const int o = ph.v[static_cast<std::size_t>(rowBase + ii)];
-                    if (o < 0) {
-                        border = 1;
-                        continue;
+                    // the list byte of each object kind in this segment
+                    uint8_t byKind[4];
+                    for (int k = 0; k < 4; ++k) {
+                        const bool orDipCell = k & 1, uAll = (k & 2) != 0;
+                        uint8_t cl = 0;
+                        if (slab) cl |= orDipCell ? 8u : ((incPML && uAll) ? 0u : 4u);
+                        if (mid) cl |= orDipCell ? 8u : (uAll ? 0u : 4u);
+                        if (fin) cl = static_cast<uint8_t>((cl & ~3u) | ((!orDipCell && uAll) ? L_U : L_D));
+                        byKind[k] = cl;
                     }
-                    const uint8_t k = objKind[static_cast<std::size_t>(o)];
-                    const bool orDipCell = k & 1, uAll = (k & 2) != 0;
-                    uint8_t cl = 0;
-                    if (slab) cl |= orDipCell ? 8u : ((incPML && uAll) ? 0u : 4u);
-                    if (mid) cl |= orDipCell ? 8u : (uAll ? 0u : 4u);
-                    if (fin) cl = static_cast<uint8_t>((cl & ~3u) | ((!orDipCell && uAll) ? L_U : L_D));
-                    cellLists[static_cast<std::size_t>(rowBase + ii)] = cl;
+                    for (int ii = sa; ii < sb; ++ii) {
+                        const int o = phR[ii];
+                        if (o < 0) {
+                            border = 1;
+                            continue;
+                        }
+                        clR[ii] = byKind[objKind[static_cast<std::size_t>(o)]];
+                    }
                 }
             }
         if (border) throw InputError("update list reaches a border cell");
@@ -1042,12 +1056,27 @@ struct Builder {
                 int lastId = -1;
                 const uint8_t* tb0 = termBits[0].data();
                 const uint8_t* tb1 = termBits[1].data();
+                uint8_t* const codes = cp.code.data();
                 for (int y = y0; y < y1; ++y)
-                    for (int z = 0; z < D.lz; ++z)
+                    for (int z = 0; z < D.lz; ++z) {
+                        const std::size_t row = static_cast<std::size_t>(D.idx(0, y, z));
+                        const int* const phR = ph.v.data() + row;
+                        const double* const epR = ep.v.data() + row;
                         for (int x = 0; x < D.lx; ++x) {
-                            std::size_t id = static_cast<std::size_t>(D.idx(x, y, z));
-                            const int o = ph.at(x, y, z);
-                            const double cellEps = ep.at(x, y, z);
+                            std::size_t id = row + static_cast<std::size_t>(x);
+                            // cells equal to the last one in all five take its class
+                            if (static_cast<uint32_t>(phR[x]) == static_cast<uint32_t>(lastSig) &&
+                                cellLists[id] == static_cast<uint8_t>(lastSig >> 32) && tb0[id] == static_cast<uint8_t>(lastSig >> 40) &&
+                                tb1[id] == static_cast<uint8_t>(lastSig >> 48) && lastId >= 0) {
+                                uint64_t eb;
+                                std::memcpy(&eb, epR + x, sizeof eb);
+                                if (eb == lastEpsBits) {
+                                    codes[id] = static_cast<uint8_t>(lastId);
+                                    continue;
+                                }
+                            }
+                            const int o = phR[x];
+                            const double cellEps = epR[x];
                             const uint8_t lists = cellLists[id];
                             const uint8_t tbit[2] = {tb0[id], tb1[id]};
                             const uint64_t sig = static_cast<uint64_t>(static_cast<uint32_t>(o)) |
@@ -1056,10 +1085,6 @@ struct Builder {
                                                  (static_cast<uint64_t>(tbit[1]) << 48);
                             uint64_t epsBits;
                             std::memcpy(&epsBits, &cellEps, sizeof epsBits);
-                            if (sig == lastSig && epsBits == lastEpsBits) {
-                                cp.code[id] = static_cast<uint8_t>(lastId);
-                                continue;
-                            }
                             ClassInfo c;
                             c.obj = (o < 0) ? 0 : o;
                             const uint8_t kind = lists & 3u;
@@ -1112,8 +1137,9 @@ struct Builder {
                             lastSig = sig;
                             lastEpsBits = epsBits;
                             lastId = lid;
-                            cp.code[id] = static_cast<uint8_t>(lid);
+                            codes[id] = static_cast<uint8_t>(lid);
                         }
+                    }
             } catch (...) {
                 chunkErr[ch] = std::current_exception();
             }
