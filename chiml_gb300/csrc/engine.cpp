@@ -1344,16 +1344,28 @@ private:
         // pass tables, the sources and detector records, the DFT tables and then the flux
         // face maps on the device, the emitters, the TFSF surfaces; the flux face maps are
         // built on the host meanwhile (the DFT task waits for them)
-        std::shared_future<void> mapsReady = std::async(std::launch::async, [&] { buildFluxMaps(maps); }).share();
-        runConcurrently(opt_.device,
-                        {[&] { validatePlan(); }, [&] { uploadPasses(); }, [&] { uploadSourcesRecords(); },
-                         [&] {
-                             uploadDftTables();
-                             mapsReady.get();
-                             for (std::size_t q = 0; q < P.fluxes.size(); ++q)
-                                 if (!P.fluxes[q].spec.save && !P.fluxes[q].spec.load) prepareFluxFaces(q, maps[q]);
-                         },
-                         [&] { uploadEmitters(); }, [&] { uploadTfsf(); }});
+        std::shared_future<void> mapsReady = std::async(std::launch::async, [&] {
+                                                 PhaseClock c;
+                                                 buildFluxMaps(maps);
+                                                 c.mark("task-flux-maps");
+                                             }).share();
+        auto timed = [](const char* what, const std::function<void()>& f) {
+            return [what, f] {
+                PhaseClock c;
+                f();
+                c.mark(what);
+            };
+        };
+        runConcurrently(opt_.device, {timed("task-validate", [&] { validatePlan(); }), timed("task-passes", [&] { uploadPasses(); }),
+                                      timed("task-src-rec", [&] { uploadSourcesRecords(); }),
+                                      timed("task-dft-flux",
+                                            [&] {
+                                                uploadDftTables();
+                                                mapsReady.get();
+                                                for (std::size_t q = 0; q < P.fluxes.size(); ++q)
+                                                    if (!P.fluxes[q].spec.save && !P.fluxes[q].spec.load) prepareFluxFaces(q, maps[q]);
+                                            }),
+                                      timed("task-emitters", [&] { uploadEmitters(); }), timed("task-tfsf", [&] { uploadTfsf(); })});
         mapsReady.wait();
         clk.mark("up-parts");
         uploadTail();
@@ -1364,21 +1376,10 @@ private:
     }
 
     // The face maps of every flux region (integration weights and accumulator points of
-    // each face), built on the host cores concurrently.
+    // each face; the faces of a region are built on the host cores concurrently).
     void buildFluxMaps(std::vector<std::vector<FluxFaceMap>>& maps) {
-        std::vector<std::exception_ptr> mErr(P.fluxes.size());
-#pragma omp parallel for schedule(dynamic, 1)
-        for (long long q = 0; q < static_cast<long long>(P.fluxes.size()); ++q) {
-            const std::size_t k = static_cast<std::size_t>(q);
-            if (P.fluxes[k].spec.save || P.fluxes[k].spec.load) continue;
-            try {
-                maps[k] = flux_face_maps(P, k);
-            } catch (...) {
-                mErr[k] = std::current_exception();
-            }
-        }
-        for (auto& e : mErr)
-            if (e) std::rethrow_exception(e);
+        for (std::size_t k = 0; k < P.fluxes.size(); ++k)
+            if (!P.fluxes[k].spec.save && !P.fluxes[k].spec.load) maps[k] = flux_face_maps(P, k);
     }
 
     // Pole coefficients, the class codes and tables, CPML profiles and psi arrays of both

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <exception>
 #include <fstream>
 #include <iomanip>
 #include <memory>
@@ -187,9 +188,13 @@ std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
     auto lnv = [&](int ax) { return ax == 0 ? D.lx : (ax == 1 ? D.ly : D.lz); };
     const FluxPlan& fp = P.fluxes[q];
     const auto& loc_ = fp.spec.loc;
-    std::vector<FluxFaceMap> maps;
-    for (const FluxFace& f : fp.faces) {
-        FluxFaceMap m;
+    // the faces are independent: built in parallel, kept in face order
+    std::vector<FluxFaceMap> maps(fp.faces.size());
+    std::vector<std::exception_ptr> faceErr(fp.faces.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long fi = 0; fi < static_cast<long long>(fp.faces.size()); ++fi) try {
+        const FluxFace& f = fp.faces[static_cast<std::size_t>(fi)];
+        FluxFaceMap& m = maps[static_cast<std::size_t>(fi)];
         // the face grids are (freq, y = faceSz[transCor1], z = faceSz[cor]); the product grid
         // of the integration is (x = faceSz[cor], y = faceSz[transCor1])
         m.nx = f.faceSz[f.cor];
@@ -280,8 +285,11 @@ std::vector<FluxFaceMap> flux_face_maps(const Plan& P, std::size_t q) {
         if (m.nx <= 1 && m.ny <= 1) throw UnsupportedError("a single-point flux face has no defined integral in the reference");
         m.wx = m.nx > 1 ? simps_weights(m.nx, m.dx) : std::vector<double>(1, 1.0);
         m.wy = m.ny > 1 ? simps_weights(m.ny, m.dy) : std::vector<double>(1, 1.0);
-        maps.push_back(std::move(m));
+    } catch (...) {
+        faceErr[static_cast<std::size_t>(fi)] = std::current_exception();
     }
+    for (auto& e : faceErr)
+        if (e) std::rethrow_exception(e);
     return maps;
 }
 

@@ -15,7 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
-#include <parallel/algorithm>
+#include <thread>
 
 #include "plan.hpp"
 
@@ -192,8 +192,19 @@ struct TfsfBuilder {
         for (int i = 0; i < 3; ++i) addStructs(i, true, pl, eTerms);
         segs = nullptr;
         clk.mark("tfsf-surfaces");
-        gather(hTerms, T.addH);
-        gather(eTerms, T.addE);
+        {
+            std::exception_ptr hErr;
+            std::thread hg([&] {
+                try {
+                    gather(hTerms, T.addH);
+                } catch (...) {
+                    hErr = std::current_exception();
+                }
+            });
+            gather(eTerms, T.addE);
+            hg.join();
+            if (hErr) std::rethrow_exception(hErr);
+        }
         clk.mark("tfsf-gather");
         // the lines' CPMLs (parallelTFSF.hpp:425-466): vacuum constants on the incident
         // grid; on the pulse grid eps and mu of the lines named there, at element mMax
@@ -668,14 +679,24 @@ struct TfsfBuilder {
 
     // Terms grouped by main cell (component, cell), each cell's terms in the order they
     // were made (a cell's corrections are summed in that order); cells in key order, which
-    // no result depends on (each cell's sum is its own).
+    // no result depends on (each cell's sum is its own). The (key, term) pairs are ordered
+    // by a least-significant-digit radix sort on the key's bytes: stable, so the terms of
+    // a key keep the order they were made in.
     void gather(const std::vector<SurfaceTerm>& terms, TfsfAdds& out) const {
         const std::size_t n = terms.size();
-        std::vector<std::pair<long long, long long>> kv(n);  // (key, term index): unique pairs
-#pragma omp parallel for schedule(static)
-        for (long long q = 0; q < static_cast<long long>(n); ++q)
-            kv[static_cast<std::size_t>(q)] = {terms[static_cast<std::size_t>(q)].comp * D.cells() + terms[static_cast<std::size_t>(q)].cell, q};
-        __gnu_parallel::sort(kv.begin(), kv.end());
+        std::vector<std::pair<long long, long long>> kv(n), tmp(n);  // (key, term index)
+        long long maxKey = 0;
+        for (std::size_t q = 0; q < n; ++q) {
+            kv[q] = {terms[q].comp * D.cells() + terms[q].cell, static_cast<long long>(q)};
+            maxKey = std::max(maxKey, kv[q].first);
+        }
+        for (int shift = 0; shift < 64 && (maxKey >> shift) != 0; shift += 8) {
+            std::size_t count[257] = {0};
+            for (const auto& e : kv) ++count[((e.first >> shift) & 0xff) + 1];
+            for (int b = 0; b < 256; ++b) count[b + 1] += count[b];
+            for (const auto& e : kv) tmp[count[(e.first >> shift) & 0xff]++] = e;
+            kv.swap(tmp);
+        }
         out = TfsfAdds();
         out.line.reserve(n);
         out.incd.reserve(n);
