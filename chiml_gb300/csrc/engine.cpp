@@ -10,6 +10,7 @@
 #include <exception>
 #include <functional>
 #include <future>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -549,6 +550,7 @@ public:
         for (auto& t : tfsf_) launchTfsf(t, s);
     }
     long long stepsLeft() const { return finalized_ ? 0 : static_cast<long long>(P.nSteps) - stepsDone_; }
+    bool fresh() const { return stepsDone_ == 0 && !finalized_; }  // no step has run: every field is still zero
     // Counts n steps that a packed launch sequence queued for this member.
     void stepsRunElsewhere(long long n) {
         if (finalized_) throw std::logic_error("step after finalize");
@@ -1800,7 +1802,10 @@ struct PackedBase {
 template <typename T>
 class PackedBatch : public PackedBase {
 public:
-    PackedBatch(const std::vector<Sim<T>*>& members, int device, int graphSteps) : members_(members) {
+    // march: the 2-D march depth per grid shape, chosen by the autotuner the first time
+    // (all members fresh) and reused by later packings of the same batch.
+    PackedBatch(const std::vector<Sim<T>*>& members, int device, int graphSteps, std::map<std::pair<int, int>, int>& march)
+        : members_(members) {
         ck(cudaSetDevice(device), "cudaSetDevice");
         ck(cudaStreamCreate(&stream_), "cudaStreamCreate");
         std::vector<dev::Pass<T>> hp, ep;
@@ -1889,6 +1894,7 @@ public:
         addMap_ = map(addW);
         for (int g = 0; g < 7; ++g) updMap_[g] = map(updW[g]);
         ck(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        autotune2d(hp, ep, march);
         // the packed step graph is made with the launches, not in the first run that uses it
         if (graphSteps > 0) buildGraph(graphSteps);
     }
@@ -1913,6 +1919,117 @@ public:
     }
 
 private:
+    // The autotuner of the 2-D members: the march depth (rows per warp, the tile's extent
+    // along y) is chosen per grid shape. Shapes in order of their total cells, each tries
+    // the depths in kDepths with the others fixed, and keeps the one whose packed H and E
+    // passes (all members) take least time, measured with CUDA events after one warm-up
+    // launch. It runs only while every member is fresh: the fields are zero before the
+    // first step and a pass maps zero fields to zero fields, so the trial launches leave
+    // every member's state as it was. Later packings (members that finished leave the
+    // batch) take the depths chosen then.
+    void autotune2d(std::vector<dev::Pass<T>>& hp, std::vector<dev::Pass<T>>& ep, std::map<std::pair<int, int>, int>& chosen) {
+        std::map<std::pair<int, int>, std::vector<int>> byShape;
+        for (std::size_t j = 0; j < hp.size(); ++j)
+            if (hp[j].interior2d && ep[j].interior2d) byShape[{hp[j].lx, hp[j].ly}].push_back(static_cast<int>(j));
+        if (byShape.empty()) return;
+        bool allFresh = true;
+        for (Sim<T>* m : members_) allFresh = allFresh && m->fresh();
+        bool known = true;
+        for (auto& g : byShape) known = known && chosen.count(g.first) > 0;
+        PhaseClock clk;
+        static constexpr int kDepths[5] = {2, 4, 8, 16, 32};
+        std::vector<std::pair<long long, std::vector<int>>> groups;
+        for (auto& g : byShape) groups.push_back({static_cast<long long>(g.first.first) * g.first.second * g.second.size(), g.second});
+        std::sort(groups.begin(), groups.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        // work tables of both halves for the members' current depths, in buffers sized for
+        // the shallowest depth (the most blocks)
+        auto blocks2d = [&](int h, std::vector<int2>& w) {
+            w.clear();
+            const std::vector<dev::Pass<T>>& ps = h ? ep : hp;
+            for (std::size_t j = 0; j < ps.size(); ++j) {
+                if (!(hp[j].interior2d && ep[j].interior2d)) continue;
+                const long long per = dev::pass2d_blocks_per_comp<T>(ps[j]);
+                for (int ci = 0; ci < 3; ++ci)
+                    if (ps[j].c[ci].present)
+                        for (long long b = 0; b < per; ++b) w.push_back(make_int2(static_cast<int>(j), static_cast<int>(ci * per + b)));
+            }
+        };
+        std::vector<int2> w[2];
+        std::size_t cap = 0;
+        for (auto& g : groups)
+            for (int j : g.second) hp[j].march = ep[j].march = kDepths[0];
+        for (int h = 0; h < 2; ++h) {
+            blocks2d(h, w[h]);
+            cap = std::max(cap, w[h].size());
+        }
+        int2* dW[2] = {mem_.alloc<int2>(cap, false), mem_.alloc<int2>(cap, false)};
+        auto apply = [&] {
+            ck(cudaMemcpy(dH_, hp.data(), hp.size() * sizeof(dev::Pass<T>), cudaMemcpyHostToDevice), "cudaMemcpy jobs");
+            ck(cudaMemcpy(dE_, ep.data(), ep.size() * sizeof(dev::Pass<T>), cudaMemcpyHostToDevice), "cudaMemcpy jobs");
+            for (int h = 0; h < 2; ++h) {
+                blocks2d(h, w[h]);
+                if (w[h].size() > cap) throw std::logic_error("packed work table larger than its buffer");
+                ck(cudaMemcpy(dW[h], w[h].data(), w[h].size() * sizeof(int2), cudaMemcpyHostToDevice), "cudaMemcpy work");
+                p2Map_[h] = dev::WorkMap{dW[h], static_cast<int>(w[h].size())};
+            }
+        };
+        cudaEvent_t e0, e1;
+        ck(cudaEventCreate(&e0), "cudaEventCreate");
+        ck(cudaEventCreate(&e1), "cudaEventCreate");
+        auto timePasses = [&] {
+            apply();
+            dev::launch_pass2d_packed<T>(dH_, p2Map_[0], false, stream_);
+            dev::launch_pass2d_packed<T>(dE_, p2Map_[1], true, stream_);
+            ck(cudaEventRecord(e0, stream_), "cudaEventRecord");
+            for (int r = 0; r < 3; ++r) {
+                dev::launch_pass2d_packed<T>(dH_, p2Map_[0], false, stream_);
+                dev::launch_pass2d_packed<T>(dE_, p2Map_[1], true, stream_);
+            }
+            ck(cudaEventRecord(e1, stream_), "cudaEventRecord");
+            ck(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float ms = 0.0f;
+            ck(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+            return ms;
+        };
+        if (known || !allFresh) {
+            // the depths chosen for the first packing (the default for a shape not tuned)
+            for (auto& g : byShape) {
+                const auto it = chosen.find(g.first);
+                for (int j : g.second) hp[j].march = ep[j].march = it != chosen.end() ? it->second : dev::kP2CYDefault;
+            }
+            apply();
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            ck(cudaStreamSynchronize(stream_), "packed work tables");
+            return;
+        }
+        for (auto& g : groups)
+            for (int j : g.second) hp[j].march = ep[j].march = dev::kP2CYDefault;
+        for (auto& g : groups) {
+            int best = dev::kP2CYDefault;
+            float bestMs = timePasses();
+            for (int dpt : kDepths) {
+                if (dpt == best) continue;
+                for (int j : g.second) hp[j].march = ep[j].march = dpt;
+                const float ms = timePasses();
+                if (ms < 0.98f * bestMs) {
+                    best = dpt;
+                    bestMs = ms;
+                }
+            }
+            for (int j : g.second) hp[j].march = ep[j].march = best;
+            chosen[{hp[g.second[0]].lx, hp[g.second[0]].ly}] = best;
+            if (clk.on)
+                std::fprintf(stderr, "host tune %dx%d (%zu members): march %d\n", hp[g.second[0]].lx, hp[g.second[0]].ly,
+                             g.second.size(), best);
+        }
+        apply();
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ck(cudaStreamSynchronize(stream_), "autotune");
+        clk.mark("tune-2d");
+    }
+
     void buildGraph(int graphSteps) {
         if (graph_) cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
@@ -2133,6 +2250,7 @@ struct chiml_batch {
     // packed launches of the current set of unfinished members, kept between calls
     std::unique_ptr<PackedBase> packed;
     std::vector<const void*> packedSet;
+    std::map<std::pair<int, int>, int> march;  // 2-D march depth per grid shape (autotuned)
     ~chiml_batch() {
         packed.reset();  // waits for its stream before the members' memory goes
         for (chiml_sim* m : members) chiml_destroy(m);
@@ -2167,7 +2285,7 @@ chiml_status batch_steps(chiml_batch* batch, long long maxSteps) {
             if (live.empty()) break;
             if (!batch->packed || set != batch->packedSet) {
                 batch->packed.reset();
-                batch->packed.reset(new PackedBatch<T>(live, batch->device, batch->graphSteps));
+                batch->packed.reset(new PackedBatch<T>(live, batch->device, batch->graphSteps, batch->march));
                 batch->packedSet = set;
             }
             batch->packed->run(n, batch->graphSteps);

@@ -8,6 +8,10 @@
 namespace chiml {
 namespace dev {
 
+// Rows each warp of the 2-D pass form marches along y unless the batch autotuner chose
+// another depth for the member's grid shape.
+constexpr int kP2CYDefault = 16;
+
 constexpr int kMaxPoles = 8;
 
 // One cell class of a component (the compressed update lists, see plan.hpp).
@@ -130,6 +134,7 @@ struct Pass {
     // differentiates along (c+2)%3 / (c+1)%3 with offsets -1 (E) / +1 (H) cells.
     int interior3d;
     int interior2d;         // the same conditions on a 2-D grid (lz == 1; the z terms absent)
+    int march;              // rows each warp marches in the packed 2-D form (0: kP2CYDefault)
     int index64;            // grid too large for 32-bit cell indices
     OrDipDev<T> od;         // oriented-dipole polarisations (E pass)
     // dispersive cells of the E pass, run by their own kernel in the interior form

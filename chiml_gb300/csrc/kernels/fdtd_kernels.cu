@@ -537,7 +537,7 @@ static void launch_pass3d(const Pass<T>& p, bool ePass, cudaStream_t s) {
 // CY rows along y from row 1 + (8 by + w) CY. The CPML decision is per warp.
 constexpr int kP2W = 8;
 #ifndef CHIML_P2CY
-#define CHIML_P2CY 16
+#define CHIML_P2CY kP2CYDefault
 #endif
 
 template <typename T, bool EPASS, int CI, int CY, int PD, bool SRC = false>
@@ -563,6 +563,21 @@ __device__ __forceinline__ void pass2dAny(const Pass<T>& p, int ci, int bx, int 
 }
 
 constexpr int kP2CY = CHIML_P2CY;
+
+// pass2d with the march depth cy chosen at run time (the packed form).
+template <typename T, bool EPASS, int CI>
+__device__ __forceinline__ void pass2dRt(const Pass<T>& p, int bx, int by, int cy) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int xa = 1 + bx * 32;
+    const int x = xa + lane;
+    const int y0 = 1 + (by * kP2W + w) * cy;
+    if (y0 > p.ly - 2) return;
+    const int y1 = min(y0 + cy, p.ly - 1);
+    const bool pml = blockTouchesSlab(p.c[CI], CI, xa, min(xa + 31, p.lx - 2), y0, y1 - 1, 0, 0);
+    if (x > p.lx - 2) return;
+    if (pml) pass3dRun<T, EPASS, CI, int, kP2CY, 2, true, true>(p, x, 0, y0, y1);
+    else pass3dRun<T, EPASS, CI, int, kP2CY, 2, false, true>(p, x, 0, y0, y1);
+}
 
 // A grid this small (cells) marches kP2CYSmall rows per warp instead of kP2CY: a march is
 // a chain of dependent row loads, and a small grid has too few warps to hide it.
@@ -1178,7 +1193,7 @@ long long pass_blocks(const Pass<T>& p) {
 }
 template <typename T>
 long long pass2d_blocks_per_comp(const Pass<T>& p) {
-    return static_cast<long long>(pass2d_gx(p.lx)) * pass2d_gy(p.ly);
+    return static_cast<long long>(pass2d_gx(p.lx)) * pass2d_gy(p.ly, p.march > 0 ? p.march : kP2CY);
 }
 long long lorentz_blocks(long long n) { return (n + 255) / 256; }
 long long ordip_blocks(long long n) { return (n + 255) / 256; }
@@ -1207,10 +1222,15 @@ template <typename T, bool EPASS>
 __global__ void __launch_bounds__(256) k_pass2d_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const Pass<T>& p = jobs[w.x];
-    const int gx = pass2d_gx(p.lx), gy = pass2d_gy(p.ly);
+    // each member's own march depth (the batch autotuner's choice for its grid shape)
+    const int cy = p.march > 0 ? p.march : kP2CY;
+    const int gx = pass2d_gx(p.lx), gy = pass2d_gy(p.ly, cy);
     const int bx = w.y % gx;
     const int r = w.y / gx;
-    pass2dAny<T, EPASS, kP2CY>(p, r / gy, bx, r % gy);
+    const int ci = r / gy, by = r % gy;
+    if (ci == 0) pass2dRt<T, EPASS, 0>(p, bx, by, cy);
+    else if (ci == 1) pass2dRt<T, EPASS, 1>(p, bx, by, cy);
+    else pass2dRt<T, EPASS, 2>(p, bx, by, cy);
 }
 
 template <typename T>
