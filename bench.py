@@ -454,7 +454,7 @@ def _c4_members(work, n_members, steps):
     return paths
 
 
-C4_METRIC = "aggregate Gcell-updates/s (FP32 fields, FP64 density matrices, batched sweep of 2-D emitter sheets)"
+C4_METRIC = "aggregate Gcell-updates/s (FP32 fields, float-float density matrices, batched sweep of 2-D emitter sheets)"
 C4_WORKLOAD = ("batched sweep: %d 2-D TMz simulations, sides drawn from {192..768}, 16-cell CPML, 10-cell sheet of "
                "2-level emitters, detuning -100..+100 meV x density 1e25..1e26 m^-3, T2 = 30 fs")
 
