@@ -2,8 +2,10 @@
 // drives the kernels per step (optionally as CUDA graphs of several steps),
 // and writes the outputs at finalize.
 #include <cuda_runtime.h>
+#include <omp.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -2307,8 +2309,16 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
     if (!out || !json_paths || n < 1) return CHIML_E_INPUT;
     *out = nullptr;
     std::unique_ptr<chiml_batch> b(new chiml_batch());
-    for (int i = 0; i < n; ++i) {
-        chiml_sim* m = nullptr;
+    // Members are created by a few host threads at once, each with its share of the
+    // OpenMP threads (a small member's plan does not fill the host); the first failure in
+    // member order is the one reported.
+    std::vector<chiml_sim*> made(static_cast<std::size_t>(n), nullptr);
+    std::vector<chiml_status> made_st(static_cast<std::size_t>(n), CHIML_OK);
+    std::vector<std::string> why(static_cast<std::size_t>(n));
+    std::atomic<int> next{0};
+    const int workers = std::min(n, 4);
+    const int hostThreads = omp_get_max_threads();
+    auto createOne = [&](int i) {
         // without an output directory, a member writes beside its own input file
         chiml_options o = opt ? *opt : chiml_options{CHIML_PREC_FP64, 0, 0, nullptr};
         o.steps_per_graph = 0;  // members step through the batch's packed graph, not their own
@@ -2319,14 +2329,26 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
             dir = slash == std::string::npos ? std::string(".") : dir.substr(0, slash + 1);
             o.out_dir = dir.c_str();
         }
-        const chiml_status st = chiml_create(json_paths[i], &o, &m);
-        if (st != CHIML_OK) {
-            g_createError = std::string("batch member ") + std::to_string(i) + " (" +
-                            (json_paths[i] ? json_paths[i] : "null") + "): " + g_createError;
-            return st;
-        }
-        b->members.push_back(m);
+        made_st[static_cast<std::size_t>(i)] = chiml_create(json_paths[i], &o, &made[static_cast<std::size_t>(i)]);
+        if (made_st[static_cast<std::size_t>(i)] != CHIML_OK) why[static_cast<std::size_t>(i)] = g_createError;
+    };
+    {
+        std::vector<std::thread> pool;
+        for (int w = 0; w < workers; ++w)
+            pool.emplace_back([&] {
+                omp_set_num_threads(std::max(1, hostThreads / workers));
+                for (int i = next++; i < n; i = next++) createOne(i);
+            });
+        for (auto& t : pool) t.join();
     }
+    for (int i = 0; i < n; ++i)
+        if (made_st[static_cast<std::size_t>(i)] != CHIML_OK) {
+            for (chiml_sim* m : made) chiml_destroy(m);
+            g_createError = std::string("batch member ") + std::to_string(i) + " (" + (json_paths[i] ? json_paths[i] : "null") +
+                            "): " + why[static_cast<std::size_t>(i)];
+            return made_st[static_cast<std::size_t>(i)];
+        }
+    for (chiml_sim* m : made) b->members.push_back(m);
     b->graphSteps = opt ? opt->steps_per_graph : 0;
     b->precision = opt ? opt->precision : CHIML_PREC_FP64;
     b->device = opt ? opt->device : 0;
