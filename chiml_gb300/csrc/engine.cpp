@@ -1936,6 +1936,12 @@ private:
         if (byShape.empty()) return;
         bool allFresh = true;
         for (Sim<T>* m : members_) allFresh = allFresh && m->fresh();
+        // CHIML_BATCH_MARCH=2|4|8|16|32 fixes the depth of every shape instead of tuning
+        if (const char* fixed = std::getenv("CHIML_BATCH_MARCH")) {
+            const int v = std::atoi(fixed);
+            if (v == 2 || v == 4 || v == 8 || v == 16 || v == 32)
+                for (auto& g : byShape) chosen[g.first] = v;
+        }
         bool known = true;
         for (auto& g : byShape) known = known && chosen.count(g.first) > 0;
         PhaseClock clk;

@@ -116,6 +116,28 @@ def test_batch_split_equals_members_run_alone(built_engine, tmp_path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("march", ["2", "32"])
+def test_batch_march_depth_leaves_results_unchanged(built_engine, tmp_path, monkeypatch, march):
+    """The packed 2-D passes with a fixed march depth (rows per warp; the autotuner's
+    other choices) give the same bytes as the members run alone."""
+    from chiml_gb300 import Batch, Simulation
+    monkeypatch.setenv("CHIML_BATCH_MARCH", march)
+    members = _small_sweep(n=3, steps=120)
+    paths = _write_members(tmp_path / "batch", members)
+    with Batch(paths, precision="split", steps_per_graph=16) as b:
+        b.run()
+        b.finalize()
+    for name, cfg in members:
+        alone = tmp_path / "alone" / name
+        os.makedirs(alone)
+        sim = Simulation(os.path.join(str(tmp_path / "batch"), name, "in.json"), precision="split",
+                         steps_per_graph=16, out_dir=str(alone))
+        sim.step()
+        sim.finalize()
+        _same_files(str(tmp_path / "batch" / name), str(alone))
+
+
+@pytest.mark.gpu
 def test_batch_of_golden_cases_matches_reference_outputs(built_engine, tmp_path):
     """Members of different dimensions, media, sources and step counts in one batch (3-D
     anisotropic and dispersive, 3-D and 2-D emitters, 2-D dielectric, 2-D and 3-D TFSF
