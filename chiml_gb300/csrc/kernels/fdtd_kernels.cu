@@ -930,13 +930,21 @@ __device__ __forceinline__ void foldFlush(const DftTable<T>& d, int last, long l
     }
 }
 
+// Resident blocks per SM the fold's register budget is sized for: the FP32 tile fits 63
+// registers without spilling, so four blocks (the shared-memory limit) stay resident to
+// cover the ring and accumulator loads; the FP64 form keeps its registers.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_fold(const DftTable<T> d, const int* __restrict__ step) {
+constexpr int foldMinBlocks() {
+    return sizeof(T) == 4 ? 4 : 1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_fold(const DftTable<T> d, const int* __restrict__ step) {
     foldStep(d, step, blockIdx.x, gridDim.x);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_flush(const DftTable<T> d, int last) {
+__global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_flush(const DftTable<T> d, int last) {
     foldFlush(d, last, blockIdx.x, gridDim.x);
 }
 
@@ -1274,7 +1282,7 @@ __global__ void __launch_bounds__(256) k_dft_sample_packed(const DftJob<T>* __re
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_dft_fold_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+__global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_fold_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const DftJob<T>& j = jobs[w.x];
     int g, first, count;
