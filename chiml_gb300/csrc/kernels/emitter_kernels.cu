@@ -20,6 +20,9 @@
 
 #include "emitter_device.hpp"
 
+#ifndef CHIML_EM_SPLIT_MINB_SMALL
+#define CHIML_EM_SPLIT_MINB_SMALL 6
+#endif
 #ifndef CHIML_EM_SPLIT_MINB
 #define CHIML_EM_SPLIT_MINB 4
 #endif
@@ -795,14 +798,15 @@ __device__ __forceinline__ void updateBlock(const EmitterDev& e, const T* __rest
 
 // Resident blocks per SM the register budget is sized for: the FP64 forms are bound by the
 // FP64 pipe and keep every register; the split form runs on the FP32 pipe and is closer to
-// the memory bound, where more resident cells hide more latency.
-template <bool SPLIT>
+// the memory bound, where more resident cells hide more latency: six blocks for up to three
+// levels (80 registers, C3's update 0.53 -> 0.49 ms), four for more (fewer spill).
+template <bool SPLIT, int NT = 0>
 constexpr int emitterMinBlocks() {
-    return SPLIT ? CHIML_EM_SPLIT_MINB : 1;
+    return SPLIT ? (NT > 0 && NT <= 3 ? CHIML_EM_SPLIT_MINB_SMALL : CHIML_EM_SPLIT_MINB) : 1;
 }
 
 template <typename T, int NT, bool HERM = false, bool SPLIT = false>
-__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<SPLIT>()) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
+__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<SPLIT, NT>()) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
                                                                const T* __restrict__ Ey, const T* __restrict__ Ez,
                                                                const int* __restrict__ stepPtr) {
     updateBlock<T, NT, HERM, SPLIT>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
@@ -879,7 +883,7 @@ __global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* _
 
 // The Hermitian form of a batch in FP32 fields is the split form (EmitterDev::split).
 template <typename T, int NT, bool HERM = false>
-__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<HERM && sizeof(T) == 4>()) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
+__global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<HERM && sizeof(T) == 4, NT>()) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
                                                                       const int2* __restrict__ work) {
     const int2 w = work[blockIdx.x];
     const EmitJob<T>& j = jobs[w.x];
