@@ -19,6 +19,7 @@
 #include <cstdint>
 
 #include "emitter_device.hpp"
+#include "launch_dep.hpp"
 
 #ifndef CHIML_EM_SPLIT_MINB_SMALL
 #define CHIML_EM_SPLIT_MINB_SMALL 6
@@ -147,6 +148,7 @@ __device__ __forceinline__ void addpRange(const EmitterDev& e, T* Ex, T* Ey, T* 
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_emitter_addp(const EmitterDev e, T* Ex, T* Ey, T* Ez) {
+    waitPriorGrid();
     addpRange(e, Ex, Ey, Ez, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
@@ -809,6 +811,7 @@ template <typename T, int NT, bool HERM = false, bool SPLIT = false>
 __global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<SPLIT, NT>()) k_emitter_update(const EmitterDev e, const T* __restrict__ Ex,
                                                                const T* __restrict__ Ey, const T* __restrict__ Ez,
                                                                const int* __restrict__ stepPtr) {
+    waitPriorGrid();
     updateBlock<T, NT, HERM, SPLIT>(e, Ex, Ey, Ez, stepPtr, blockIdx.x);
 }
 
@@ -867,6 +870,7 @@ __device__ __forceinline__ void reduceBody(const EmitterDev& e, const int* __res
 
 // one block per output quantity (blockIdx.y)
 __global__ void __launch_bounds__(kReduceThreads) k_emitter_reduce(const EmitterDev e, const int* __restrict__ stepPtr) {
+    waitPriorGrid();
     reduceBody(e, stepPtr, blockIdx.y);
 }
 
@@ -874,6 +878,7 @@ __global__ void __launch_bounds__(kReduceThreads) k_emitter_reduce(const Emitter
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const EmitJob<T>& j = jobs[w.x];
     const int bpc = emitter_addp_blocks_per_comp(j.e);
@@ -885,6 +890,7 @@ __global__ void __launch_bounds__(256) k_emitter_addp_packed(const EmitJob<T>* _
 template <typename T, int NT, bool HERM = false>
 __global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<HERM && sizeof(T) == 4, NT>()) k_emitter_update_packed(const EmitJob<T>* __restrict__ jobs,
                                                                       const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const EmitJob<T>& j = jobs[w.x];
     updateBlock<T, NT, HERM, HERM && sizeof(T) == 4>(j.e, j.f[0], j.f[1], j.f[2], j.step, w.y);
@@ -892,6 +898,7 @@ __global__ void __launch_bounds__(kEmThreads, emitterMinBlocks<HERM && sizeof(T)
 
 template <typename T>
 __global__ void __launch_bounds__(kReduceThreads) k_emitter_reduce_packed(const EmitJob<T>* __restrict__ jobs) {
+    waitPriorGrid();
     const EmitJob<T>& j = jobs[blockIdx.x];
     reduceBody(j.e, j.step, blockIdx.y);
 }
@@ -908,18 +915,18 @@ template <typename T>
 void launch_emitter_packed(const EmitJob<T>* jobs, int njobs, WorkMap addp, const WorkMap update[7], void* stream) {
     if (njobs <= 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (addp.blocks > 0) k_emitter_addp_packed<T><<<addp.blocks, 256, 0, s>>>(jobs, addp.work);
-    if (update[0].blocks > 0) k_emitter_update_packed<T, 2><<<update[0].blocks, kEmThreads, 0, s>>>(jobs, update[0].work);
-    if (update[1].blocks > 0) k_emitter_update_packed<T, 3><<<update[1].blocks, kEmThreads, 0, s>>>(jobs, update[1].work);
-    if (update[2].blocks > 0) k_emitter_update_packed<T, 4><<<update[2].blocks, kEmThreads, 0, s>>>(jobs, update[2].work);
-    if (update[3].blocks > 0) k_emitter_update_packed<T, 0><<<update[3].blocks, kEmThreads, 0, s>>>(jobs, update[3].work);
+    if (addp.blocks > 0) launchAfterPrior(k_emitter_addp_packed<T>, dim3(addp.blocks), dim3(256), s, jobs, addp.work);
+    if (update[0].blocks > 0) launchAfterPrior(k_emitter_update_packed<T, 2>, dim3(update[0].blocks), dim3(kEmThreads), s, jobs, update[0].work);
+    if (update[1].blocks > 0) launchAfterPrior(k_emitter_update_packed<T, 3>, dim3(update[1].blocks), dim3(kEmThreads), s, jobs, update[1].work);
+    if (update[2].blocks > 0) launchAfterPrior(k_emitter_update_packed<T, 4>, dim3(update[2].blocks), dim3(kEmThreads), s, jobs, update[2].work);
+    if (update[3].blocks > 0) launchAfterPrior(k_emitter_update_packed<T, 0>, dim3(update[3].blocks), dim3(kEmThreads), s, jobs, update[3].work);
     if (update[4].blocks > 0)
-        k_emitter_update_packed<T, 2, true><<<update[4].blocks, kEmThreads, 0, s>>>(jobs, update[4].work);
+        launchAfterPrior(k_emitter_update_packed<T, 2, true>, dim3(update[4].blocks), dim3(kEmThreads), s, jobs, update[4].work);
     if (update[5].blocks > 0)
-        k_emitter_update_packed<T, 3, true><<<update[5].blocks, kEmThreads, 0, s>>>(jobs, update[5].work);
+        launchAfterPrior(k_emitter_update_packed<T, 3, true>, dim3(update[5].blocks), dim3(kEmThreads), s, jobs, update[5].work);
     if (update[6].blocks > 0)
-        k_emitter_update_packed<T, 4, true><<<update[6].blocks, kEmThreads, 0, s>>>(jobs, update[6].work);
-    k_emitter_reduce_packed<T><<<dim3(njobs, kReduceQuantities), kReduceThreads, 0, s>>>(jobs);
+        launchAfterPrior(k_emitter_update_packed<T, 4, true>, dim3(update[6].blocks), dim3(kEmThreads), s, jobs, update[6].work);
+    launchAfterPrior(k_emitter_reduce_packed<T>, dim3(njobs, kReduceQuantities), dim3(kReduceThreads), s, jobs);
 }
 
 template void launch_emitter_packed<float>(const EmitJob<float>*, int, WorkMap, const WorkMap[7], void*);
@@ -929,21 +936,21 @@ template <typename T>
 void launch_emitter_step(const EmitterDev& e, T* const fields[3], const int* step, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     dim3 ga(emitter_addp_blocks_per_comp(e), 3);
-    k_emitter_addp<T><<<ga, 256, 0, s>>>(e, fields[0], fields[1], fields[2]);
+    launchAfterPrior(k_emitter_addp<T>, dim3(ga), dim3(256), s, e, fields[0], fields[1], fields[2]);
     const int blocks = (e.nc + kEmThreads - 1) / kEmThreads;
     // the Hermitian form in FP32 fields is the split form (EmitterDev::split)
     constexpr bool SPLIT = sizeof(T) == 4;
     if (e.herm && e.N >= 2 && e.N <= 4) {
-        if (e.N == 2) k_emitter_update<T, 2, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
-        else if (e.N == 3) k_emitter_update<T, 3, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
-        else k_emitter_update<T, 4, true, SPLIT><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step);
+        if (e.N == 2) launchAfterPrior(k_emitter_update<T, 2, true, SPLIT>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step);
+        else if (e.N == 3) launchAfterPrior(k_emitter_update<T, 3, true, SPLIT>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step);
+        else launchAfterPrior(k_emitter_update<T, 4, true, SPLIT>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step);
     } else switch (e.N) {
-        case 2: k_emitter_update<T, 2><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
-        case 3: k_emitter_update<T, 3><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
-        case 4: k_emitter_update<T, 4><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
-        default: k_emitter_update<T, 0><<<blocks, kEmThreads, 0, s>>>(e, fields[0], fields[1], fields[2], step); break;
+        case 2: launchAfterPrior(k_emitter_update<T, 2>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step); break;
+        case 3: launchAfterPrior(k_emitter_update<T, 3>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step); break;
+        case 4: launchAfterPrior(k_emitter_update<T, 4>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step); break;
+        default: launchAfterPrior(k_emitter_update<T, 0>, dim3(blocks), dim3(kEmThreads), s, e, fields[0], fields[1], fields[2], step); break;
     }
-    k_emitter_reduce<<<dim3(1, kReduceQuantities), kReduceThreads, 0, s>>>(e, step);
+    launchAfterPrior(k_emitter_reduce, dim3(1, kReduceQuantities), dim3(kReduceThreads), s, e, step);
 }
 
 template void launch_emitter_step<float>(const EmitterDev&, float* const[3], const int*, void*);

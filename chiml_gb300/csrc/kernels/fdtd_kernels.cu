@@ -13,6 +13,7 @@
 #include <type_traits>
 
 #include "fdtd_device.hpp"
+#include "launch_dep.hpp"
 
 namespace chiml {
 namespace dev {
@@ -162,6 +163,7 @@ __device__ __forceinline__ void ordipEntry(const Pass<T>& p, long long j) {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_ordip_pol(const Pass<T> p) {
+    waitPriorGrid();
     ordipEntry(p, blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x);
 }
 
@@ -181,6 +183,7 @@ constexpr int kGenBY = 8;
 
 template <typename T, bool EPASS>
 __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
+    waitPriorGrid();
     passCell<T, EPASS>(p, blockIdx.x * 32 + threadIdx.x, blockIdx.z * kGenBY + threadIdx.z, blockIdx.y);
 }
 
@@ -188,6 +191,7 @@ __global__ void __launch_bounds__(256) k_pass(const Pass<T> p) {
 // leaves them out so that its common path stays small.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pass_lorentz(const Pass<T> p) {
+    waitPriorGrid();
     const long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
     if (j >= p.nLor) return;
     const long long i = p.lorCell[j];
@@ -228,6 +232,7 @@ constexpr int kP3CY = CHIML_P3_CY;  // planes marched per block
 constexpr int kP3PD = CHIML_P3_PD;  // planes ahead of the march that are prefetched into L2
 
 __device__ __forceinline__ void prefetchL2(const void* a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
 
 // The dispersive part of one E-pass cell of the FP32 interior form, with cellGeneric's
 // arithmetic: the Lorentz ADE from E^n (u), D += curl, then D -> E with the pole sum
@@ -519,6 +524,7 @@ constexpr int passMinBlocks() {
 
 template <typename T, bool EPASS, typename I, int CY, int PD>
 __global__ void __launch_bounds__(256, passMinBlocks<T, EPASS, I>()) k_pass3d(const Pass<T> p) {
+    waitPriorGrid();
     const int ci = blockIdx.z % 3;
     if (ci == 0) pass3d<T, EPASS, 0, I, CY, PD>(p);
     else if (ci == 1) pass3d<T, EPASS, 1, I, CY, PD>(p);
@@ -529,8 +535,8 @@ template <typename T, typename I, int CY, int PD>
 static void launch_pass3d(const Pass<T>& p, bool ePass, cudaStream_t s) {
     dim3 block(32, kP3BZ, 1);
     dim3 grid((p.lx - 2 + 31) / 32, (p.lz - 2 + kP3BZ - 1) / kP3BZ, 3 * ((p.ly - 2 + CY - 1) / CY));
-    if (ePass) k_pass3d<T, true, I, CY, PD><<<grid, block, 0, s>>>(p);
-    else k_pass3d<T, false, I, CY, PD><<<grid, block, 0, s>>>(p);
+    if (ePass) launchAfterPrior(k_pass3d<T, true, I, CY, PD>, grid, block, s, p);
+    else launchAfterPrior(k_pass3d<T, false, I, CY, PD>, grid, block, s, p);
 }
 
 // 2-D form (lz == 1): a block of 32 x-columns by 8 warps; warp w of y-block by marches
@@ -586,6 +592,7 @@ constexpr long long kP2SmallCells = 1LL << 22;
 
 template <typename T, bool EPASS, int CY = kP2CY>
 __global__ void __launch_bounds__(256) k_pass2d(const Pass<T> p) {
+    waitPriorGrid();
     if (!p.c[blockIdx.z].present) return;
     pass2dAny<T, EPASS, CY>(p, blockIdx.z, blockIdx.x, blockIdx.y);
 }
@@ -596,6 +603,7 @@ __global__ void __launch_bounds__(256) k_pass2d(const Pass<T> p) {
 // then the curl terms).
 template <typename T, int CY>
 __global__ void __launch_bounds__(256) k_pass2d_src(const Pass<T> p) {
+    waitPriorGrid();
     if (!p.c[blockIdx.z].present) return;
     __shared__ PSrcCell<T> ps[kInlineMaxSrc];
     const int nps = p.nSrcIn < kInlineMaxSrc ? p.nSrcIn : kInlineMaxSrc;
@@ -614,34 +622,34 @@ template <typename T>
 void launch_pass(const Pass<T>& p, bool ePass, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (ePass && p.od.n > 0)
-        k_ordip_pol<T><<<static_cast<unsigned>((p.od.n + 255) / 256), 256, 0, s>>>(p);
+        launchAfterPrior(k_ordip_pol<T>, dim3(static_cast<unsigned>((p.od.n + 255) / 256)), dim3(256), s, p);
     if (p.interior3d) {
         if (p.index64) launch_pass3d<T, long long, kP3CY, kP3PD>(p, ePass, s);
         else launch_pass3d<T, int, kP3CY, kP3PD>(p, ePass, s);
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
-            k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
+            launchAfterPrior(k_pass_lorentz<T>, dim3(static_cast<unsigned>((p.nLor + 255) / 256)), dim3(256), s, p);
     } else if (p.interior2d) {
         const bool src = ePass && p.nSrcIn > 0;
         if (static_cast<long long>(p.lx) * p.ly < kP2SmallCells) {
             dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly, kP2CYSmall), 3);
-            if (src) k_pass2d_src<T, kP2CYSmall><<<grid, 256, 0, s>>>(p);
-            else if (ePass) k_pass2d<T, true, kP2CYSmall><<<grid, 256, 0, s>>>(p);
-            else k_pass2d<T, false, kP2CYSmall><<<grid, 256, 0, s>>>(p);
+            if (src) launchAfterPrior(k_pass2d_src<T, kP2CYSmall>, grid, dim3(256), s, p);
+            else if (ePass) launchAfterPrior(k_pass2d<T, true, kP2CYSmall>, grid, dim3(256), s, p);
+            else launchAfterPrior(k_pass2d<T, false, kP2CYSmall>, grid, dim3(256), s, p);
         } else {
             dim3 grid(pass2d_gx(p.lx), pass2d_gy(p.ly), 3);
-            if (src) k_pass2d_src<T, kP2CY><<<grid, 256, 0, s>>>(p);
-            else if (ePass) k_pass2d<T, true><<<grid, 256, 0, s>>>(p);
-            else k_pass2d<T, false><<<grid, 256, 0, s>>>(p);
+            if (src) launchAfterPrior(k_pass2d_src<T, kP2CY>, grid, dim3(256), s, p);
+            else if (ePass) launchAfterPrior(k_pass2d<T, true, kP2CY>, grid, dim3(256), s, p);
+            else launchAfterPrior(k_pass2d<T, false, kP2CY>, grid, dim3(256), s, p);
         }
         if (ePass && p.nLor > 0 && !kInlineDispersive<T>)
-            k_pass_lorentz<T><<<static_cast<unsigned>((p.nLor + 255) / 256), 256, 0, s>>>(p);
+            launchAfterPrior(k_pass_lorentz<T>, dim3(static_cast<unsigned>((p.nLor + 255) / 256)), dim3(256), s, p);
     } else {
         // 2-D grids, and 3-D grids with updated halo cells: one thread per cell,
         // all components of the pass
         dim3 block(32, 1, kGenBY);
         dim3 grid((p.lx + 31) / 32, p.lz, (p.ly + kGenBY - 1) / kGenBY);
-        if (ePass) k_pass<T, true><<<grid, block, 0, s>>>(p);
-        else k_pass<T, false><<<grid, block, 0, s>>>(p);
+        if (ePass) launchAfterPrior(k_pass<T, true>, grid, block, s, p);
+        else launchAfterPrior(k_pass<T, false>, grid, block, s, p);
     }
 }
 
@@ -668,13 +676,14 @@ __device__ __forceinline__ void sourceEntry(const SourceTable& s, const Fields<T
 
 template <typename T>
 __global__ void k_sources(const SourceTable s, const Fields<T> f, const int* __restrict__ step) {
+    waitPriorGrid();
     sourceEntry(s, f, step, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
 void launch_sources(const SourceTable& s, const Fields<T>& f, const int* step, void* stream) {
     if (s.n == 0) return;
-    k_sources<T><<<(s.n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(s, f, step);
+    launchAfterPrior(k_sources<T>, dim3((s.n + 127) / 128), dim3(128), static_cast<cudaStream_t>(stream), s, f, step);
 }
 
 template <typename T>
@@ -940,6 +949,7 @@ constexpr int foldMinBlocks() {
 
 template <typename T>
 __global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_fold(const DftTable<T> d, const int* __restrict__ step) {
+    waitPriorGrid();
     foldStep(d, step, blockIdx.x, gridDim.x);
 }
 
@@ -955,7 +965,7 @@ void launch_dft_fold(const DftTable<T>& d, const int* step, void* stream) {
     const long long G = d.K / kFoldStagger;
     const long long tiles = ((pTiles + G - 1) / G) * ((d.nfreq + kFoldTF - 1) / kFoldTF);
     const unsigned grid = static_cast<unsigned>(tiles < 152 * 4 ? tiles : 152 * 4);
-    k_dft_fold<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, step);
+    launchAfterPrior(k_dft_fold<T>, dim3(grid), dim3(256), static_cast<cudaStream_t>(stream), d, step);
 }
 
 template <typename T>
@@ -970,6 +980,7 @@ __global__ void k_increment(int* step) { *step += 1; }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_step_tail(const StepTail<T> t) {
+    waitPriorGrid();
     __shared__ int next;  // the step number after this step's increment
     if (threadIdx.x == 0) next = *t.step + 1;
     __syncthreads();
@@ -998,7 +1009,7 @@ void launch_increment(int* step, void* stream) { k_increment<<<1, 1, 0, static_c
 
 template <typename T>
 void launch_step_tail(const StepTail<T>& t, void* stream) {
-    k_step_tail<T><<<static_cast<unsigned>(t.blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(t);
+    launchAfterPrior(k_step_tail<T>, dim3(static_cast<unsigned>(t.blocks)), dim3(256), static_cast<cudaStream_t>(stream), t);
 }
 
 // ---- persistent form of small 2-D grids ----
@@ -1215,6 +1226,7 @@ long long dft_fold_blocks(long long npts, int nfreq) {
 // Block (bx, bz, by) of a member's generic pass grid from its linear block index.
 template <typename T, bool EPASS>
 __global__ void __launch_bounds__(256) k_pass_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const Pass<T>& p = jobs[w.x];
     const int gx = (p.lx + 31) / 32;
@@ -1228,6 +1240,7 @@ __global__ void __launch_bounds__(256) k_pass_packed(const Pass<T>* __restrict__
 // 2-D form: the block index of a job encodes (component, y-block, x-block).
 template <typename T, bool EPASS>
 __global__ void __launch_bounds__(256) k_pass2d_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const Pass<T>& p = jobs[w.x];
     // each member's own march depth (the batch autotuner's choice for its grid shape)
@@ -1243,6 +1256,7 @@ __global__ void __launch_bounds__(256) k_pass2d_packed(const Pass<T>* __restrict
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_lorentz_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const Pass<T>& p = jobs[w.x];
     const long long j = w.y * 256LL + threadIdx.x;
@@ -1256,12 +1270,14 @@ __global__ void __launch_bounds__(256) k_lorentz_packed(const Pass<T>* __restric
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_ordip_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     ordipEntry(jobs[w.x], w.y * 256LL + threadIdx.x);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_sources_packed(const SrcJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const SrcJob<T>& j = jobs[w.x];
     sourceEntry(j.s, j.f, j.step, w.y * 128 + static_cast<int>(threadIdx.x));
@@ -1269,6 +1285,7 @@ __global__ void __launch_bounds__(128) k_sources_packed(const SrcJob<T>* __restr
 
 template <typename T>
 __global__ void __launch_bounds__(128) k_record_packed(const RecJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const RecJob<T>& j = jobs[w.x];
     recordEntry(j.r, j.f, j.step, w.y * 128 + static_cast<int>(threadIdx.x));
@@ -1276,6 +1293,7 @@ __global__ void __launch_bounds__(128) k_record_packed(const RecJob<T>* __restri
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_dft_sample_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const DftJob<T>& j = jobs[w.x];
     dftSampleEntry(j.d, j.f, j.step, w.y * 256LL + threadIdx.x);
@@ -1283,6 +1301,7 @@ __global__ void __launch_bounds__(256) k_dft_sample_packed(const DftJob<T>* __re
 
 template <typename T>
 __global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_fold_packed(const DftJob<T>* __restrict__ jobs, const int2* __restrict__ work) {
+    waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const DftJob<T>& j = jobs[w.x];
     int g, first, count;
@@ -1294,6 +1313,7 @@ __global__ void __launch_bounds__(256, foldMinBlocks<T>()) k_dft_fold_packed(con
 }
 
 __global__ void k_increment_packed(int* const* __restrict__ steps, int n) {
+    waitPriorGrid();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < n) *steps[j] += 1;
 }
@@ -1302,42 +1322,42 @@ template <typename T>
 void launch_pass_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream) {
     if (m.blocks <= 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (ePass) k_pass_packed<T, true><<<m.blocks, 256, 0, s>>>(jobs, m.work);
-    else k_pass_packed<T, false><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+    if (ePass) launchAfterPrior(k_pass_packed<T, true>, dim3(m.blocks), dim3(256), s, jobs, m.work);
+    else launchAfterPrior(k_pass_packed<T, false>, dim3(m.blocks), dim3(256), s, jobs, m.work);
 }
 template <typename T>
 void launch_pass2d_packed(const Pass<T>* jobs, WorkMap m, bool ePass, void* stream) {
     if (m.blocks <= 0) return;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (ePass) k_pass2d_packed<T, true><<<m.blocks, 256, 0, s>>>(jobs, m.work);
-    else k_pass2d_packed<T, false><<<m.blocks, 256, 0, s>>>(jobs, m.work);
+    if (ePass) launchAfterPrior(k_pass2d_packed<T, true>, dim3(m.blocks), dim3(256), s, jobs, m.work);
+    else launchAfterPrior(k_pass2d_packed<T, false>, dim3(m.blocks), dim3(256), s, jobs, m.work);
 }
 template <typename T>
 void launch_lorentz_packed(const Pass<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_lorentz_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_lorentz_packed<T>, dim3(m.blocks), dim3(256), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 template <typename T>
 void launch_ordip_packed(const Pass<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_ordip_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_ordip_packed<T>, dim3(m.blocks), dim3(256), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 template <typename T>
 void launch_sources_packed(const SrcJob<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_sources_packed<T><<<m.blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_sources_packed<T>, dim3(m.blocks), dim3(128), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 template <typename T>
 void launch_record_packed(const RecJob<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_record_packed<T><<<m.blocks, 128, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_record_packed<T>, dim3(m.blocks), dim3(128), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 template <typename T>
 void launch_dft_sample_packed(const DftJob<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_dft_sample_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_dft_sample_packed<T>, dim3(m.blocks), dim3(256), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 template <typename T>
 void launch_dft_fold_packed(const DftJob<T>* jobs, WorkMap m, void* stream) {
-    if (m.blocks > 0) k_dft_fold_packed<T><<<m.blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(jobs, m.work);
+    if (m.blocks > 0) launchAfterPrior(k_dft_fold_packed<T>, dim3(m.blocks), dim3(256), static_cast<cudaStream_t>(stream), jobs, m.work);
 }
 void launch_increment_packed(int* const* steps, int n, void* stream) {
-    if (n > 0) k_increment_packed<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(steps, n);
+    if (n > 0) launchAfterPrior(k_increment_packed, dim3((n + 127) / 128), dim3(128), static_cast<cudaStream_t>(stream), steps, n);
 }
 
 #define CHIML_PACKED(T)                                                                   \

@@ -23,6 +23,7 @@
 //                 normalisation, from the block that finishes last.
 // The lines are complex FP64 in both precision forms (a few thousand points).
 #include "tfsf_device.hpp"
+#include "launch_dep.hpp"
 
 namespace chiml {
 namespace dev {
@@ -183,6 +184,7 @@ __device__ __forceinline__ void recordIncident(const TfsfDev& t, int s, int c) {
 template <typename T, bool LAY>
 __global__ void __launch_bounds__(kTfsfThreads) k_tfsf_half(const TfsfDev t, int c0, int which, int lineBlocks, int record,
                                                             const Fields9<T> F, const int* __restrict__ step) {
+    waitPriorGrid();
     const int s = *step;
     if (s >= t.nSteps) return;
     const int b = static_cast<int>(blockIdx.x);
@@ -229,10 +231,11 @@ void launch_tfsf_step(const TfsfDev& t, T* const fields[9], const int* step, voi
     for (int k = 0; k < 9; ++k) F.f[k] = fields[k];
     for (int half = 0; half < 2; ++half) {
         const int addBlocks = t.segBlocks[half] + (t.nCell[half] + kTfsfThreads - 1) / kTfsfThreads;
+        const dim3 grid(static_cast<unsigned>(lineBlocks + addBlocks));
         if (t.layered)
-            k_tfsf_half<T, true><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
+            launchAfterPrior(k_tfsf_half<T, true>, grid, dim3(kTfsfThreads), s, t, half == 0 ? 3 : 0, half, lineBlocks, half == 1 ? 1 : 0, F, step);
         else
-            k_tfsf_half<T, false><<<lineBlocks + addBlocks, kTfsfThreads, 0, s>>>(t, half == 0 ? 3 : 0, half, lineBlocks, half == 1, F, step);
+            launchAfterPrior(k_tfsf_half<T, false>, grid, dim3(kTfsfThreads), s, t, half == 0 ? 3 : 0, half, lineBlocks, half == 1 ? 1 : 0, F, step);
     }
 }
 
