@@ -1292,24 +1292,29 @@ private:
                 if (!P.comp[tp.field].present) throw InputError("neighbour field absent");
             }
             // every code indexes the class table and every coded cell's neighbour stays
-            // inside the grid; the cells of each class are counted on the way
+            // inside the grid (a cell farther than its offsets from either end of the
+            // array always has its neighbours inside); the cells of each class are counted
+            // on the way
             const int ncls = static_cast<int>(cp.classes.size());
             const long long off0 = cp.term[0].present ? cp.term[0].off : 0, off1 = cp.term[1].present ? cp.term[1].off : 0;
+            const long long edge = std::max(std::abs(off0), std::abs(off1));
             std::vector<long long> count(256, 0);
             int bad = 0;
+            const uint8_t* code = cp.code.data();
 #pragma omp parallel
             {
-                std::vector<long long> local(256, 0);
-#pragma omp for schedule(static) reduction(| : bad)
-                for (long long i = 0; i < N; ++i) {
-                    const uint8_t k = cp.code[i];
-                    ++local[k];
-                    if (k >= ncls) bad |= 1;
-                    else if (k != 0 && (i + off0 < 0 || i + off0 >= N || i + off1 < 0 || i + off1 >= N)) bad |= 2;
-                }
+                long long local[256] = {0};
+#pragma omp for schedule(static)
+                for (long long i = 0; i < N; ++i) ++local[code[i]];
 #pragma omp critical
                 for (int q = 0; q < 256; ++q) count[q] += local[q];
             }
+            for (int q = ncls; q < 256; ++q)
+                if (count[q]) bad |= 1;
+            for (long long i = 0; i < std::min(edge, N); ++i)
+                if (code[i] && (i + off0 < 0 || i + off0 >= N || i + off1 < 0 || i + off1 >= N)) bad |= 2;
+            for (long long i = std::max(edge, N - edge); i < N; ++i)
+                if (code[i] && (i + off0 < 0 || i + off0 >= N || i + off1 < 0 || i + off1 >= N)) bad |= 2;
             if (bad & 1) throw InputError("class code outside the class table");
             if (bad & 2) throw InputError("stencil neighbour outside the grid");
             classCount_[c].assign(count.begin(), count.begin() + ncls);
