@@ -2327,7 +2327,7 @@ chiml_status chiml_batch_create(const char* const* json_paths, int n, const chim
     std::vector<chiml_status> made_st(static_cast<std::size_t>(n), CHIML_OK);
     std::vector<std::string> why(static_cast<std::size_t>(n));
     std::atomic<int> next{0};
-    const int workers = std::min(n, 4);
+    const int workers = std::min(n, 8);
     const int hostThreads = omp_get_max_threads();
     auto createOne = [&](int i) {
         // without an output directory, a member writes beside its own input file
