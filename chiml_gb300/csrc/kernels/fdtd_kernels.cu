@@ -1239,7 +1239,7 @@ __global__ void __launch_bounds__(256) k_pass_packed(const Pass<T>* __restrict__
 
 // 2-D form: the block index of a job encodes (component, y-block, x-block).
 template <typename T, bool EPASS>
-__global__ void __launch_bounds__(256) k_pass2d_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
+__global__ void __launch_bounds__(256, 6) k_pass2d_packed(const Pass<T>* __restrict__ jobs, const int2* __restrict__ work) {
     waitPriorGrid();
     const int2 w = work[blockIdx.x];
     const Pass<T>& p = jobs[w.x];
