@@ -326,8 +326,9 @@ Object read_object(const JNode& node, const Inputs& ip) {
         o.pols = named_poles(*m, ip.a);
     } else {
         o.epsInf = node.get<double>("eps", 1.00);
-        if (node.get<double>("mu", 1.0) != 1.0)
-            throw UnsupportedError("magnetic materials (mu != 1) are not supported");
+        // a constant mu (parallelInputs.cpp:1283) enters the H-side coefficients; magnetic
+        // poles (sigma_m) stay rejected below
+        o.muInf = node.get<double>("mu", 1.0);
         if (node.get<double>("tellegen", 0.0) != 0.0)
             throw UnsupportedError("Tellegen media are not supported");
         for (auto& kv : node.child("pols").kids) {

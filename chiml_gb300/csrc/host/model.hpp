@@ -70,6 +70,7 @@ struct Object {
     Shape shape = Shape::BLOCK;
     bool ML = false;               // has an emitter basis set
     double epsInf = 1.0;
+    double muInf = 1.0;            // constant relative permeability (no magnetic poles)
     std::vector<double> geo;       // shape parameters (Obj::geoParam_)
     std::vector<double> geoML;     // geoParamML_: geo with the emitter buffer added
     std::array<double, 3> loc = {0.0, 0.0, 0.0};

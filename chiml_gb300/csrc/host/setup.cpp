@@ -197,6 +197,36 @@ struct Builder {
         return true;
     }
 
+    // Objects of constant mu. Inside the interior regions the reference puts their H cells
+    // on the U lists with the coefficient dt / (mu d) (fillBlasLists and populateUpLists,
+    // parallelFDTDField.hpp:628-644, 751-780), which the material map above gives. Three
+    // layouts take other paths there and are refused here, conservatively: mu reaching the
+    // CPML (magMatInPML_ moves the H-side CPML onto B, parallelFDTDField.cpp:60-66), TFSF
+    // surfaces (their H lines and surface terms would carry mu), and emitter objects.
+    void checkMagnetic() const {
+        for (std::size_t oo = 1; oo < objs.size(); ++oo) {
+            const Object& o = objs[oo];
+            if (o.muInf == 1.0) continue;
+            if (!(o.muInf > 0.0)) throw InputError("an object's mu must be positive");
+            if (o.ML) throw UnsupportedError("emitter objects with mu != 1 are not supported");
+            if (!in.tfsf.empty()) throw UnsupportedError("TFSF surfaces with magnetic materials (mu != 1) are not supported");
+            // per axis: the object's half extent (unbounded along an axis without a CPML, such
+            // as z in 2-D, is fine) grown by two cells must stay inside the interior
+            std::array<double, 3> h = {HUGE_VAL, HUGE_VAL, HUGE_VAL};  // unknown: unbounded
+            objectExtent(o, h);
+            for (int q = 0; q < 3; ++q) {
+                const int t = in.pmlThickness[q];
+                if (t <= 0 || nvec[q] <= 1 || d[q] <= 0) continue;
+                const double inner = (nvec[q] / 2.0 - t) * d[q];  // distance of the CPML from the centre
+                // the extent along the axis, else the bounding radius of the CPML scan
+                const double hq = (h[q] < 1e300) ? h[q] : boundingRadius(o);
+                const double reach = std::abs(o.loc[q]) + hq + 2.0 * d[q];
+                if (!(hq < 1e300) || !(reach < inner))
+                    throw UnsupportedError("magnetic materials (mu != 1) reaching the CPML are not supported");
+            }
+        }
+    }
+
     // Index range [lo, hi) per axis that contains every cell whose sample point can
     // lie inside the object (isObj is only ever true within the object's extent).
     void objectIndexBox(const Object& o, std::array<double, 3> offPt, int lo[3], int hi[3]) const {
@@ -268,7 +298,9 @@ struct Builder {
         int zmax = twoD ? 1 : D.lz - 1;
         for (std::size_t oo = 1; oo < objs.size(); ++oo) {
             const Object& o = objs[oo];
-            if (!(o.ML || o.gamma.size() > 0 || o.epsInf != 1.0)) continue;
+            // the H grids also take objects of constant mu (parallelFDTDField.hpp:880-894); on
+            // the E grids such an object is vacuum (eps 1, the same U-list coefficient)
+            if (!(o.ML || o.gamma.size() > 0 || o.epsInf != 1.0 || (!E && o.muInf != 1.0))) continue;
             // Cells outside a generous bounding box of the object cannot pass isObj;
             // the box only narrows the loops, the test itself is unchanged.
             int lo[3], hi[3];
@@ -278,7 +310,7 @@ struct Builder {
             const int k0 = twoD ? zmin : std::max(zmin, lo[2]), k1 = twoD ? zmax : std::min(zmax, hi[2]);
             // without an emitter buffer both tests are the same test
             const bool sameGeo = o.geoML == o.geo;
-            const double epsHere = E ? o.epsInf : 1.0;
+            const double epsHere = E ? o.epsInf : o.muInf;
             // Cells are tested in any order: each cell's value comes from the last object
             // that holds it, whatever the order of cells within one object.
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
@@ -1341,6 +1373,7 @@ struct Builder {
                                      ? "The sum of the boundary checks for a tetrahedron does not equal the determinant of the verticies"
                                      : "The sum of the boundary checks for a triangular base does not equal the determinant of the verticies");
         scanPML();
+        checkMagnetic();
         clk.mark("pml-scan");
         bool disp = false;
         for (auto& o : objs)

@@ -476,6 +476,31 @@ def _tfsf_layer_x():
                         sphere=([-0.19, 0.03, 0.0], 0.12, 3.0), det="Ey")
 
 
+def _mu_3d():
+    """3-D: constant-mu objects away from the CPML: a dielectric sphere with mu 1.5, a
+    mu-only block (eps 1, mu 2.5) and a Lorentz cylinder with mu 1.3; Ex plane source, flux
+    box, two BIN planes (an H plane among them)."""
+    cfg = configs.config2(n=44, pml=6, steps=200, nell=0, nfreq=5, metal_radius_cells=0, tfsf=False)
+    lor = configs.drude_lorentz_pols(5.0, [(0.6, 0.3, 2.4)])
+    cfg["ObjectList"] = [
+        _shape("sphere", [-0.3, -0.25, 0.0], 2.0, radius=0.15, mu=1.5),
+        _shape("block", [0.25, -0.2, 0.05], 1.0, size=[0.3, 0.26, 0.22], mu=2.5),
+        _shape("cylinder", [0.0, 0.3, 0.0], 1.6, pols=lor, radius=0.12, length=0.3, mu=1.3),
+    ]
+    return _bin_planes(cfg, [("Ex", (1.5, 1.5, 0.0)), ("Hy", (0.0, 1.5, 1.5))])
+
+
+def _mu_2d():
+    """2-D TMz: a disk with mu 2 and eps 1.5 and a mu-only disk; point source, text
+    detectors, flux line, one BIN plane of Hx."""
+    cfg = configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=3, nfreq=8)
+    cfg["ObjectList"] = [
+        _shape("sphere", [-0.3, 0.2, 0.0], 1.5, radius=0.25, mu=2.0),
+        _shape("sphere", [0.35, -0.3, 0.0], 1.0, radius=0.2, mu=1.8),
+    ]
+    return _bin_planes(cfg, [("Hx", (3.0, 3.0, 0.0))])
+
+
 CASES = {
     "c1_small": lambda: configs.config1(n=80, pml=10, steps=300, radius_cells=10, src_gap_cells=12, ndtc=4, nfreq=12),
     "c2_small": lambda: configs.config2(n=34, pml=6, steps=70, nell=3, nfreq=6, metal_radius_cells=20, aniso=False,
@@ -510,6 +535,8 @@ CASES = {
     "tfsf_layer_3d": _tfsf_layer_3d,
     "tfsf_film_3d": _tfsf_film_3d,
     "tfsf_layer_x": _tfsf_layer_x,
+    "mu_3d": _mu_3d,
+    "mu_2d": _mu_2d,
 }
 
 

@@ -25,7 +25,9 @@ def _base():
 @pytest.mark.parametrize("mutate,status", [
     (lambda c: c["CompCell"].__setitem__("PBC", True), 2),
     (lambda c: c["CompCell"].__setitem__("cplxFields", True), 2),
-    (lambda c: c["ObjectList"][0].__setitem__("mu", 2.0), 2),
+    # constant mu is taken inside the interior; an object of mu reaching the CPML is refused
+    (lambda c: c["ObjectList"][0].update(mu=2.0, radius=0.65), 2),
+    (lambda c: c["ObjectList"][0].__setitem__("mu", -1.0), 1),
     (lambda c: c["ObjectList"][0].__setitem__("material", "Unobtainium"), 1),
     (lambda c: c["ObjectList"][0].__setitem__("shape", "dodecahedron"), 1),
     (lambda c: c["ObjectList"][0].update(shape="cone", radSmall=0.2, radLarge=0.1, height=0.3), 1),
